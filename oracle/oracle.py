@@ -1,0 +1,195 @@
+"""ctypes wrapper of the oracle restatement (oracle/xfem_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
+by bench.py's CPU-baseline / reference arm. The product (libxfem.so and the
+xfem package) never imports this module.
+
+The float routines reproduce the reference (jak-xyz/xpbd-fem) bit for bit
+(pinned by tests/golden/, generated from the reference's own code); the
+double routines are the FP64 run of the same method.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+ENERGY_MIXED_SEL = 4      # Energy_MixedSel, XPBDFEM/Settings.h:45
+ENERGY_YEOH_SKIN_FAST = 7  # Energy_YeohSkinFast, XPBDFEM/Settings.h:48
+REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
+
+
+class Params(C.Structure):
+    """Mirror of orc_params (oracle/xfem_oracle.h)."""
+    _fields_ = [
+        ("gravity", C.c_float * 3), ("dt", C.c_float), ("time_corrected_drag", C.c_float),
+        ("compliance", C.c_float), ("poisson", C.c_float), ("energy", C.c_uint32),
+        ("simultaneous", C.c_uint32), ("yeoh", C.c_float * 3), ("lock_active", C.c_uint32),
+        ("ground", C.c_uint32), ("ground_n", C.c_float * 3), ("ground_d", C.c_float),
+        ("friction", C.c_float),
+    ]
+
+
+def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=True,
+                gravity=(0.0, 0.0, 0.0), drag=0.0, yeoh=REF_YEOH, lock=False,
+                ground=False, ground_n=(0.0, 0.0, 1.0), ground_d=0.0, friction=0.0):
+    p = Params()
+    p.gravity[:] = [float(g) for g in gravity]
+    p.dt = dt
+    p.time_corrected_drag = drag
+    p.compliance = compliance
+    p.poisson = poisson
+    p.energy = energy
+    p.simultaneous = 1 if simultaneous else 0
+    p.yeoh[:] = [float(c) for c in yeoh]
+    p.lock_active = 1 if lock else 0
+    p.ground = 1 if ground else 0
+    p.ground_n[:] = [float(c) for c in ground_n]
+    p.ground_d = ground_d
+    p.friction = friction
+    return p
+
+
+_lib = None
+
+
+def build():
+    """Compile oracle/liboracle.so with the oracle's own Makefile."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        P = C.c_void_p
+        u32 = C.c_uint32
+        L.orc_gen_tet_block.argtypes = [u32, u32, u32, C.c_float, C.c_float, C.c_float, u32, C.c_float, P, P]
+        L.orc_parse_tets.argtypes = [P, u32, P, P, P]
+        L.orc_minstd_order.argtypes = [u32, P]
+        L.orc_init_rest_f.argtypes = [P, u32, P, u32, C.c_float, P, P, P]
+        L.orc_init_rest_d.argtypes = [P, u32, P, u32, C.c_double, P, P, P]
+        L.orc_solve_tet_f.argtypes = [P, P, P, P, C.c_float, P]
+        L.orc_solve_tet_d.argtypes = [P, P, P, P, C.c_double, P]
+        L.orc_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P, P]
+        L.orc_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P, P]
+        L.orc_substeps_threaded_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, P, u32, u32, P, u32]
+        L.orc_volume_f.argtypes = [P, u32, P]
+        L.orc_volume_f.restype = C.c_float
+        L.orc_volume_d.argtypes = [P, u32, P]
+        L.orc_volume_d.restype = C.c_double
+        L.orc_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def gen_tet_block(W, H, D, scale=(1.0, 1.0, 1.0), pattern=0, wonkiness=0.0):
+    nv = (W + 1) * (H + 1) * (D + 1)
+    nodes = np.zeros(3 * nv, np.float32)
+    idx = np.zeros(30 * W * H * D, np.uint32)
+    lib().orc_gen_tet_block(W, H, D, scale[0], scale[1], scale[2], pattern, wonkiness, _p(nodes), _p(idx))
+    return nodes, idx
+
+
+def parse_tets(idx):
+    idx = np.ascontiguousarray(idx, np.uint32)
+    nt, nv = C.c_uint32(), C.c_uint32()
+    if lib().orc_parse_tets(_p(idx), idx.size, None, C.byref(nt), C.byref(nv)):
+        raise ValueError("index stream holds a non-tet element")
+    tets = np.zeros((nt.value, 4), np.uint32)
+    lib().orc_parse_tets(_p(idx), idx.size, _p(tets), C.byref(nt), C.byref(nv))
+    return tets, nv.value
+
+
+def minstd_order(nt):
+    o = np.zeros(nt, np.uint32)
+    lib().orc_minstd_order(nt, _p(o))
+    return o
+
+
+def init_rest(nodes, tets, density, dtype=np.float32):
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    nv, nt = nodes.size // 3, tets.shape[0]
+    ep = np.zeros((nt, 17), dtype)
+    w = np.zeros(nv, dtype)
+    fl = np.zeros(nv, np.uint8)
+    f = lib().orc_init_rest_f if dtype == np.float32 else lib().orc_init_rest_d
+    f(_p(nodes), nv, _p(tets), nt, density, _p(ep), _p(w), _p(fl))
+    return ep, w, fl
+
+
+def solve_tet(X, w, ep, params, mu_override=0.0, dtype=np.float32):
+    X = np.array(X, np.float64).reshape(4, 3).copy()
+    w = np.ascontiguousarray(w, dtype)
+    ep = np.ascontiguousarray(ep, dtype)
+    lam = np.zeros(2, dtype)
+    f = lib().orc_solve_tet_f if dtype == np.float32 else lib().orc_solve_tet_d
+    if f(_p(X), _p(w), _p(ep), C.byref(params), mu_override, _p(lam)):
+        raise ValueError("unsupported energy model")
+    return X, lam
+
+
+def substeps(X, V, w, tets, ep, order, nsub, params, lock_mask=None, tet_mu=None,
+             dtype=np.float32, threads=None, colour_begin=None, want_lambdas=False):
+    """Run nsub substeps in the given constraint order. Returns X, V, w,
+    contact mask of the last substep, and (optionally) per-tet lambdas."""
+    X = np.array(X, np.float64).reshape(-1).copy()
+    V = np.array(V, np.float64).reshape(-1).copy()
+    w = np.array(w, dtype).copy()
+    nv = w.size
+    tets = np.ascontiguousarray(tets, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    order = np.ascontiguousarray(order, np.uint32)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    tm = None if tet_mu is None else np.ascontiguousarray(tet_mu, dtype)
+    contact = np.zeros(nv, np.uint8)
+    lam = np.zeros(2 * tets.shape[0], dtype) if want_lambdas else None
+    if threads:
+        cb = np.ascontiguousarray(colour_begin, np.uint32)
+        rc = lib().orc_substeps_threaded_f(nv, _p(X), _p(V), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep),
+                                           _p(tm), _p(order), _p(cb), cb.size - 1, nsub, C.byref(params),
+                                           int(threads))
+        contact = None
+    else:
+        f = lib().orc_substeps_f if dtype == np.float32 else lib().orc_substeps_d
+        rc = f(nv, _p(X), _p(V), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep), _p(tm), _p(order), nsub,
+               C.byref(params), _p(contact), _p(lam))
+    if rc:
+        raise ValueError("oracle substep failed (unsupported energy model?)")
+    out = (X.reshape(-1, 3), V.reshape(-1, 3), w, contact)
+    return out + (lam.reshape(-1, 2),) if want_lambdas else out
+
+
+def volume(X, tets, dtype=np.float32):
+    X = np.ascontiguousarray(X, np.float64).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    f = lib().orc_volume_f if dtype == np.float32 else lib().orc_volume_d
+    return f(_p(X), tets.shape[0], _p(tets))
+
+
+def schedule(nodes, tets, mode=1, morton=1):
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    nv, nt = nodes.size // 3, tets.shape[0]
+    cluster_of = np.zeros(nt, np.uint32)
+    colour_of = np.zeros(max(nt, 1), np.uint32)
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nt, np.uint32)
+    cb = np.zeros(nt + 1, np.uint32)
+    ncl, ncol = C.c_uint32(), C.c_uint32()
+    rc = lib().orc_schedule(_p(nodes), nv, _p(tets), nt, mode, morton, _p(cluster_of), C.byref(ncl),
+                            _p(colour_of), C.byref(ncol), _p(rank), _p(order), _p(cb))
+    if rc:
+        raise ValueError("schedule limits exceeded")
+    return dict(cluster_of=cluster_of, clusters=ncl.value, colour_of_cluster=colour_of[:ncl.value],
+                colours=ncol.value, vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1])

@@ -1,0 +1,250 @@
+/*
+ * refgen — golden-vector generator that drives the UNMODIFIED reference solver
+ * core (jak-xyz/xpbd-fem, XPBDFEM/{Fem,Geo,Connectivity,Allocator,MeshGen,
+ * vectormath,DebugGeo}.cpp) headless.
+ *
+ * Test infrastructure only. Built by oracle/build_ref.sh into oracle/_ref/ from
+ * the reference sources where they lie; the reference is not copied or edited.
+ * tests/golden/make_golden.py runs this binary and stores its output as the
+ * committed fixtures that pin the oracle restatement (oracle/xfem_oracle.c)
+ * and, through it, the GPU path.
+ *
+ * Output: a stream of named arrays on stdout, each record
+ *   u32 name_len | name bytes | u8 dtype ('f','d','I','B') | u64 count | data
+ *
+ * Commands (argv[1]):
+ *   meshgen W H D sx sy sz pattern wonkiness
+ *       GenerateTetBlock (XPBDFEM/MeshGen.cpp:223) outputs: nodes, idx.
+ *   init W H D sx sy sz pattern wonkiness density
+ *       GeoLinear3d::Init (XPBDFEM/Geo.cpp:697): per-tet rest state
+ *       (Qi, QQ, QR, volume, surfaceArea; XPBDFEM/Fem.cpp:196-224), inverse
+ *       masses w, Left/Right flags, the MINSTD tet order tOrder
+ *       (XPBDFEM/Geo.cpp:759-771) and CalculateVolume (XPBDFEM/Geo.cpp:827).
+ *   solve seed count energy simultaneous compliance poisson dt
+ *       SolveElement (XPBDFEM/Fem.cpp:892) on `count` seeded random tets:
+ *       inputs (X, w, rest nodes) and outputs (X after the solve).
+ *   substep W H D sx sy sz wonkiness density energy simultaneous compliance
+ *           poisson gx gy dt nsub lockleft
+ *       Geo3d::Substep (XPBDFEM/Geo.cpp:305) `nsub` times in the reference's
+ *       own shuffled order; dumps X and V after 1 substep and after nsub.
+ *   ordered W H D sx sy sz wonkiness density energy simultaneous compliance
+ *           poisson gx gy dt nsub lockleft < order.u32
+ *       Same substep, but the constraint loop runs SolveElement over the tet
+ *       order read from stdin (u32 count, then the order) — the replicated
+ *       Substep used for same-order parity with the coloured GPU schedule.
+ */
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+#include <vector>
+
+#include "Allocator.h"
+#include "Geo.h"
+#include "Fem.h"
+#include "MeshGen.h"
+#include "Manipulator.h"
+#include "Settings.h"
+
+// Non-static in XPBDFEM/MeshGen.cpp:223 but not declared in MeshGen.h.
+void GenerateTetBlock(Allocator* alloc, uint32_t width, uint32_t height, uint32_t depth, vec3 scale,
+                      uint32_t elementPattern, float wonkiness, const float** outNodeData,
+                      uint32_t* outNodeDataCount, const uint32_t** outIdxData, uint32_t* outIdxDataCount);
+
+static void emit(const char* name, char dtype, const void* data, uint64_t count) {
+	uint32_t n = (uint32_t)strlen(name);
+	fwrite(&n, 4, 1, stdout);
+	fwrite(name, 1, n, stdout);
+	fwrite(&dtype, 1, 1, stdout);
+	fwrite(&count, 8, 1, stdout);
+	size_t es = dtype == 'd' ? 8 : dtype == 'B' ? 1 : 4;
+	if (count) fwrite(data, es, count, stdout);
+}
+
+// splitmix64: the project's seeded generator for harness inputs.
+static uint64_t g_rng;
+static uint64_t splitmix64() {
+	uint64_t z = (g_rng += 0x9E3779B97F4A7C15ull);
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+	return z ^ (z >> 31);
+}
+static double urand() { return (double)(splitmix64() >> 11) * (1.0 / 9007199254740992.0); }
+
+static Allocator* make_alloc(size_t bytes) {
+	Allocator* a = new Allocator();
+	a->Initialize(malloc(bytes), bytes);
+	return a;
+}
+
+static Settings make_settings(uint32_t energy, uint32_t simultaneous, float compliance, float poisson,
+                              float gx, float gy, uint32_t lockLeft) {
+	Settings s;
+	s.timeScale = 1.0f;
+	s.substepsPerSecond = 1200.0f;
+	s.volumePasses = 0;
+	s.gravity = vec2(gx, gy);
+	s.compliance = compliance;
+	s.damping = 0.0f;
+	s.pbdDamping = 0.0f;
+	s.drag = 0.0f;
+	s.poissonsRatio = poisson;
+	s.wonkiness = 0.0f;
+	s.leftRightSeparation = 1.0f;
+	s.flags = (energy << Settings_EnergyBit) | (simultaneous ? (1u << Settings_XpbdSolveBit) : 0u) |
+	          (Rayleigh_Post << Settings_RayleighTypeBit) | (lockLeft ? Settings_LockLeft : 0u) |
+	          (Element_T4 << Settings_ElementTypeBit);
+	// Derived fields (XPBDFEM/Settings.h:93-101) have no initialisers; Sim::Update
+	// (XPBDFEM/Demo.cpp:53-63) fills them. With drag = pbdDamping = 0 they are 0.
+	s.areaAndTimeCorrectedPbdDamping = 0.0f;
+	s.volumeAndTimeCorrectedPbdDamping = 0.0f;
+	s.amortizedAreaAndTimeCorrectedPbdDamping = 0.0f;
+	s.amortizedVolumeAndTimeCorrectedPbdDamping = 0.0f;
+	s.timeCorrectedDrag = 0.0f;
+	s.lockedRightTransform = mat2(1.0f);
+	s.lockedRightTransform3d = mat3(1.0f);
+	s.tickId = 0;
+	return s;
+}
+
+static void dump_geo(GeoLinear3d* g) {
+	uint32_t nt = g->con.tetCount, nv = g->vertCount;
+	std::vector<float> ep(nt * 17);
+	std::vector<uint32_t> tidx(nt * 4);
+	for (uint32_t i = 0; i < nt; i++) {
+		const ElementParamsLinearTet& e = g->t[i].ep;
+		float* o = &ep[i * 17];
+		for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[c * 3 + r] = e.Qi[c][r];
+		for (int k = 0; k < 3; k++) o[9 + k] = e.ic.QQ[k];
+		for (int k = 0; k < 3; k++) o[12 + k] = e.ic.QR[k];
+		o[15] = e.volume;
+		o[16] = e.surfaceArea;
+		for (int k = 0; k < 4; k++) tidx[i * 4 + k] = g->t[i].i[k];
+	}
+	std::vector<uint8_t> flags(g->flags, g->flags + nv);
+	emit("tet_idx", 'I', tidx.data(), tidx.size());
+	emit("ep", 'f', ep.data(), ep.size());
+	emit("w", 'f', g->w, nv);
+	emit("vflags", 'B', flags.data(), nv);
+	emit("torder", 'I', g->tOrder, nt);
+	float vol = g->CalculateVolume();
+	emit("volume", 'f', &vol, 1);
+}
+
+static void dump_state(GeoLinear3d* g, const char* xname, const char* vname) {
+	uint32_t nv = g->vertCount;
+	std::vector<double> x(nv * 3), v(nv * 3);
+	for (uint32_t i = 0; i < nv; i++)
+		for (int k = 0; k < 3; k++) { x[i * 3 + k] = g->X[i][k]; v[i * 3 + k] = g->V[i][k]; }
+	emit(xname, 'd', x.data(), x.size());
+	emit(vname, 'd', v.data(), v.size());
+}
+
+int main(int argc, char** argv) {
+	if (argc < 2) { fprintf(stderr, "usage: refgen <cmd> ...\n"); return 2; }
+	const char* cmd = argv[1];
+	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
+	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
+
+	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered")) {
+		Allocator* alloc = make_alloc((size_t)1 << 31);
+		uint32_t W = U(2), H = U(3), D = U(4);
+		vec3 scale(F(5), F(6), F(7));
+		int a = 8;
+		uint32_t pattern = 0;
+		if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init")) pattern = U(a++);
+		float wonk = F(a++);
+		const float* nodes; uint32_t nodeCount; const uint32_t* idx; uint32_t idxCount;
+		GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		if (!strcmp(cmd, "meshgen")) {
+			emit("nodes", 'f', nodes, nodeCount);
+			emit("idx", 'I', idx, idxCount);
+			return 0;
+		}
+		float density = F(a++);
+		GeoLinear3d* g = alloc->New<GeoLinear3d>();
+		g->Init(alloc, density, nodes, nodeCount, idx, idxCount, false);
+		if (!strcmp(cmd, "init")) {
+			emit("nodes", 'f', nodes, nodeCount);
+			emit("idx", 'I', idx, idxCount);
+			dump_geo(g);
+			return 0;
+		}
+		uint32_t energy = U(a++), simul = U(a++);
+		float compliance = F(a++), poisson = F(a++), gx = F(a++), gy = F(a++), dt = F(a++);
+		uint32_t nsub = U(a++), lockLeft = U(a++);
+		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
+		Manipulator manip;
+		manip.pickedGeo = nullptr;
+		emit("nodes", 'f', nodes, nodeCount);
+		emit("idx", 'I', idx, idxCount);
+		if (!strcmp(cmd, "ordered")) {
+			// Replace the shuffled tOrder by the order read from stdin; Geo3d::Substep
+			// then runs GeoLinear3d::Constrain (XPBDFEM/Geo.cpp:777) over it unchanged.
+			uint32_t n = 0;
+			if (fread(&n, 4, 1, stdin) != 1 || n != g->con.tetCount) { fprintf(stderr, "bad order\n"); return 3; }
+			if (fread(g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+		}
+		for (uint32_t k = 0; k < nsub; k++) {
+			s.tickId = k;
+			g->Substep(s, manip, dt);
+			if (k == 0) dump_state(g, "x1", "v1");
+		}
+		dump_state(g, "xn", "vn");
+		float vol = g->CalculateVolume();
+		emit("volume", 'f', &vol, 1);
+		return 0;
+	}
+
+	if (!strcmp(cmd, "solve")) {
+		g_rng = strtoull(argv[2], 0, 10);
+		uint32_t count = U(3), energy = U(4), simul = U(5);
+		float compliance = F(6), poisson = F(7), dt = F(8);
+		Settings s = make_settings(energy, simul, compliance, poisson, 0.0f, 0.0f, 0);
+		std::vector<double> xin(count * 12), xout(count * 12), rest(count * 12);
+		std::vector<float> win(count * 4), epo(count * 17);
+		for (uint32_t t = 0; t < count; t++) {
+			dvec3 X0[4], X[4], O[4];
+			float m[4] = {0, 0, 0, 0}, w[4];
+			// Rest tet: unit-scale random points, reordered to positive volume.
+			double sc = 0.02 + 0.2 * urand();
+			for (int n = 0; n < 4; n++) X0[n] = dvec3(sc * (urand() - 0.5), sc * (urand() - 0.5), sc * (urand() - 0.5));
+			X0[0] = X0[3] + dvec3(sc * (0.6 + 0.4 * urand()), 0.1 * sc * (urand() - 0.5), 0.1 * sc * (urand() - 0.5));
+			X0[1] = X0[3] + dvec3(0.1 * sc * (urand() - 0.5), sc * (0.6 + 0.4 * urand()), 0.1 * sc * (urand() - 0.5));
+			X0[2] = X0[3] + dvec3(0.1 * sc * (urand() - 0.5), 0.1 * sc * (urand() - 0.5), sc * (0.6 + 0.4 * urand()));
+			// Round rest positions to float, as node data arrives as float.
+			for (int n = 0; n < 4; n++) for (int k = 0; k < 3; k++) X0[n][k] = (double)(float)X0[n][k];
+			const uint32_t is[4] = {0, 1, 2, 3};
+			ElementParamsLinearTet ep;
+			InitFiniteElement(X0, is, 1000.0f, m, &ep);
+			// Deformed state: case mix = mild, large, inverted, w = 0 on some nodes.
+			uint32_t kind = t % 8;
+			double amp = kind < 4 ? 0.05 : kind < 6 ? 0.4 : 1.5;
+			for (int n = 0; n < 4; n++) {
+				for (int k = 0; k < 3; k++) X[n][k] = X0[n][k] + amp * sc * (urand() - 0.5);
+				O[n] = X0[n];
+				w[n] = (float)(0.5 + 2.0 * urand());
+			}
+			if (kind == 6) { dvec3 tmp = X[0]; X[0] = X[1]; X[1] = tmp; } // inverted
+			if (kind == 7) { w[0] = 0.0f; w[3] = 0.0f; }
+			for (int n = 0; n < 4; n++) {
+				win[t * 4 + n] = w[n];
+				for (int k = 0; k < 3; k++) { xin[t * 12 + n * 3 + k] = X[n][k]; rest[t * 12 + n * 3 + k] = X0[n][k]; }
+			}
+			SolveElement(dt, X, O, w, is, ep, s);
+			for (int n = 0; n < 4; n++) for (int k = 0; k < 3; k++) xout[t * 12 + n * 3 + k] = X[n][k];
+			float* o = &epo[t * 17];
+			for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[c * 3 + r] = ep.Qi[c][r];
+			for (int k = 0; k < 3; k++) { o[9 + k] = ep.ic.QQ[k]; o[12 + k] = ep.ic.QR[k]; }
+			o[15] = ep.volume; o[16] = ep.surfaceArea;
+		}
+		emit("rest", 'd', rest.data(), rest.size());
+		emit("ep", 'f', epo.data(), epo.size());
+		emit("xin", 'd', xin.data(), xin.size());
+		emit("w", 'f', win.data(), win.size());
+		emit("xout", 'd', xout.data(), xout.size());
+		return 0;
+	}
+	fprintf(stderr, "unknown command %s\n", cmd);
+	return 2;
+}

@@ -1,0 +1,393 @@
+/*
+ * xfem_oracle.c — CPU restatement of the reference's small-step XPBD tet
+ * substep and of this project's schedule (clusters, colours, Morton order).
+ * TEST INFRASTRUCTURE ONLY (see oracle/xfem_oracle.h). Build with
+ * -ffp-contract=off (oracle/Makefile) so that float results reproduce the
+ * reference bit for bit on x86-64 and on AArch64.
+ */
+#include "xfem_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---- float instantiation (reference semantics) ---------------------------- */
+#define R float
+#define SFX _f
+#define SQRT sqrtf
+#define FMAX fmaxf
+#define EPS22 1.0e-22f
+#define EPS8 0.00000001f
+#define EPS4 0.0001f
+#include "xfem_oracle_real.inc"
+#undef R
+#undef SFX
+#undef SQRT
+#undef FMAX
+#undef EPS22
+#undef EPS8
+#undef EPS4
+
+/* ---- double instantiation (FP64 run of the same method) ------------------- */
+#define R double
+#define SFX _d
+#define SQRT sqrt
+#define FMAX fmax
+#define EPS22 1.0e-22
+#define EPS8 1.0e-8
+#define EPS4 1.0e-4
+#include "xfem_oracle_real.inc"
+#undef R
+#undef SFX
+#undef SQRT
+#undef FMAX
+#undef EPS22
+#undef EPS8
+#undef EPS4
+
+/* ---- mesh ------------------------------------------------------------------ */
+/* GenerateHexBlock + GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244). */
+void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                       float wonkiness, float* nodes, uint32_t* idx) {
+	float sc[3] = {sx, sy, sz};
+	float mn[3] = {sx * (-0.5f * (float)W), sy * (-0.5f * (float)H), sz * (-0.5f * (float)D)};
+	uint32_t rs = 1;
+	for (uint32_t z = 0; z < D + 1; z++) {
+		uint32_t ze = (z == 0 || z == D);
+		for (uint32_t y = 0; y < H + 1; y++) {
+			uint32_t ye = (y == 0 || y == H);
+			for (uint32_t x = 0; x < W + 1; x++) {
+				uint32_t xe = (x == 0 || x == W);
+				uint32_t i = x + y * (W + 1) + z * (W + 1) * (H + 1);
+				/* RandF is drawn for interior coordinates only. The reference draws
+				 * inside one vec3(...) argument list, whose evaluation order C++
+				 * leaves unspecified; g++ (and MSVC) evaluate right to left, so z
+				 * is drawn first. The golden vectors come from g++. */
+				float r[3] = {0.0f, 0.0f, 0.0f};
+				uint32_t edge[3] = {xe, ye, ze};
+				for (int k = 2; k >= 0; k--) {
+					if (!edge[k]) {
+						rs = (uint32_t)(((uint64_t)rs * 48271u) % 0x7fffffffu);
+						r[k] = (float)rs * 9.3132258e-10f - 1.0f;
+					}
+				}
+				float c[3] = {(float)x, (float)y, (float)z};
+				for (int k = 0; k < 3; k++) {
+					float wig = wonkiness * r[k];
+					nodes[3 * i + k] = mn[k] + sc[k] * (c[k] + 0.5f * wig);
+				}
+			}
+		}
+	}
+	uint32_t ie = 0;
+	static const uint32_t split[6][4] = {{0, 1, 5, 7}, {0, 7, 3, 1}, {0, 2, 3, 7}, {0, 7, 6, 2}, {0, 4, 6, 7}, {0, 7, 5, 4}};
+	for (uint32_t z = 0; z < D; z++)
+		for (uint32_t y = 0; y < H; y++)
+			for (uint32_t x = 0; x < W; x++) {
+				uint32_t ih[8];
+				for (uint32_t k = 0; k < 2; k++)
+					for (uint32_t j = 0; j < 2; j++)
+						for (uint32_t i = 0; i < 2; i++) {
+							if (pattern == 0) {
+								ih[i + j * 2 + k * 4] = (x + i) + (y + j) * (W + 1) + (z + k) * (W + 1) * (H + 1);
+							} else {
+								uint32_t xx = x % 2 == 0 ? i : (1 - i);
+								uint32_t yy = y % 2 == 0 ? j : (1 - j);
+								uint32_t zz = z % 2 == 0 ? k : (1 - k);
+								uint32_t hi = i + j * 2 + k * 4;
+								if ((x + y + z) % 2 == 1) hi = 7 - hi;
+								ih[hi] = (x + xx) + (y + yy) * (W + 1) + (z + zz) * (W + 1) * (H + 1);
+							}
+						}
+				for (int t = 0; t < 6; t++) {
+					uint32_t* o = idx + 30 * (size_t)ie + 5 * t;
+					o[0] = 4;
+					for (int n = 0; n < 4; n++) o[1 + n] = ih[split[t][n]];
+				}
+				++ie;
+			}
+}
+
+int orc_parse_tets(const uint32_t* idx, uint32_t idx_count, uint32_t* tets, uint32_t* tet_count, uint32_t* vert_count) {
+	/* Connectivity3d::Init (XPBDFEM/Connectivity.cpp:251-265): tag 4 = tet,
+	 * 8 = hex (not handled by this path), anything else is an error. */
+	uint32_t nt = 0, mx = 0;
+	for (uint32_t i = 0; i < idx_count; i++) {
+		if (idx[i] != 4u || (uint64_t)i + 4u >= (uint64_t)idx_count) return -1;
+		for (int n = 0; n < 4; n++) {
+			uint32_t v = idx[i + 1 + n];
+			if (v > mx) mx = v;
+			if (tets) tets[4 * (size_t)nt + n] = v;
+		}
+		nt++;
+		i += 4;
+	}
+	*tet_count = nt;
+	*vert_count = nt ? mx + 1 : 0;
+	return 0;
+}
+
+void orc_minstd_order(uint32_t nt, uint32_t* order) {
+	for (uint32_t i = 0; i < nt; i++) order[i] = i;
+	uint32_t rs = 1;
+	for (uint32_t i = 0; i < nt; i++) {
+		rs = (uint32_t)(((uint64_t)rs * 48271u) % 0x7fffffffu);
+		uint32_t j = rs % nt;
+		uint32_t c = order[i];
+		order[i] = order[j];
+		order[j] = c;
+	}
+}
+
+float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets) {
+	float v = 0.0f;
+	for (uint32_t t = 0; t < nt; t++) v += tet_volume_f(X, tets + 4 * (size_t)t);
+	return v;
+}
+
+double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets) {
+	double v = 0.0;
+	for (uint32_t t = 0; t < nt; t++) v += tet_volume_d(X, tets + 4 * (size_t)t);
+	return v;
+}
+
+/* ---- threaded coloured run (CPU baseline) --------------------------------- */
+typedef struct {
+	orc_run_f* r;
+	const uint32_t* order;
+	const uint32_t* cb;
+	uint32_t ncol, nsub, tid, nth;
+	pthread_barrier_t* bar;
+	int rc;
+} orc_worker;
+
+static void* orc_worker_main(void* arg) {
+	orc_worker* k = (orc_worker*)arg;
+	orc_run_f* r = k->r;
+	uint32_t vb = (uint32_t)((uint64_t)r->nv * k->tid / k->nth), ve = (uint32_t)((uint64_t)r->nv * (k->tid + 1) / k->nth);
+	for (uint32_t s = 0; s < k->nsub; s++) {
+		predict_f(r, vb, ve);
+		pthread_barrier_wait(k->bar);
+		for (uint32_t c = 0; c < k->ncol; c++) {
+			uint32_t b = k->cb[c], e = k->cb[c + 1], n = e - b;
+			uint32_t tb = b + (uint32_t)((uint64_t)n * k->tid / k->nth), te = b + (uint32_t)((uint64_t)n * (k->tid + 1) / k->nth);
+			for (uint32_t i = tb; i < te; i++)
+				if (solve_one_f(r, k->order[i])) k->rc = -1;
+			pthread_barrier_wait(k->bar);
+		}
+		finalize_f(r, vb, ve);
+		pthread_barrier_wait(k->bar);
+	}
+	return NULL;
+}
+
+int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                            const uint32_t* tets, const float* ep, const float* tet_mu, const uint32_t* order,
+                            const uint32_t* colour_begin, uint32_t ncolours, uint32_t nsub, const orc_params* p,
+                            uint32_t threads) {
+	if (threads < 1) threads = 1;
+	if (threads > 256) threads = 256;
+	double* O = (double*)malloc(sizeof(double) * 3 * (size_t)(nv ? nv : 1));
+	if (!O) return -1;
+	orc_run_f r = {nv, nt, X, V, O, w, lock_mask, tets, ep, tet_mu, p, NULL, NULL};
+	pthread_barrier_t bar;
+	pthread_barrier_init(&bar, NULL, threads);
+	orc_worker wk[256];
+	pthread_t th[256];
+	for (uint32_t t = 0; t < threads; t++) {
+		wk[t] = (orc_worker){&r, order, colour_begin, ncolours, nsub, t, threads, &bar, 0};
+		if (t) pthread_create(&th[t], NULL, orc_worker_main, &wk[t]);
+	}
+	orc_worker_main(&wk[0]);
+	int rc = wk[0].rc;
+	for (uint32_t t = 1; t < threads; t++) {
+		pthread_join(th[t], NULL);
+		if (wk[t].rc) rc = wk[t].rc;
+	}
+	pthread_barrier_destroy(&bar);
+	free(O);
+	return rc;
+}
+
+/* ---- schedule restatement --------------------------------------------------- */
+#define ORC_MAXV 8u
+#define ORC_MAXT 8u
+#define ORC_MAXCOL 4096u
+
+typedef struct {
+	uint32_t* off; /* nv + 1 */
+	uint32_t* lst; /* 4 nt */
+} orc_csr;
+
+static int csr_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_csr* c) {
+	c->off = (uint32_t*)calloc((size_t)nv + 1, 4);
+	c->lst = (uint32_t*)malloc(sizeof(uint32_t) * 4 * (size_t)(nt ? nt : 1));
+	if (!c->off || !c->lst) return -1;
+	for (size_t i = 0; i < 4 * (size_t)nt; i++) c->off[tets[i] + 1]++;
+	for (uint32_t v = 0; v < nv; v++) c->off[v + 1] += c->off[v];
+	uint32_t* fill = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)nv + 1));
+	if (!fill) return -1;
+	memcpy(fill, c->off, sizeof(uint32_t) * ((size_t)nv + 1));
+	for (uint32_t t = 0; t < nt; t++)
+		for (int n = 0; n < 4; n++) c->lst[fill[tets[4 * (size_t)t + n]]++] = t;
+	free(fill);
+	return 0;
+}
+
+static int tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v || tv[2] == v || tv[3] == v; }
+
+static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+	uint32_t c = 0;
+	for (int b = 0; b < 10; b++)
+		c |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
+	return c;
+}
+
+typedef struct { uint64_t key; uint32_t id; } orc_kv;
+static int kv_cmp(const void* a, const void* b) {
+	const orc_kv* x = (const orc_kv*)a;
+	const orc_kv* y = (const orc_kv*)b;
+	if (x->key != y->key) return x->key < y->key ? -1 : 1;
+	return x->id < y->id ? -1 : (x->id > y->id);
+}
+
+int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t mode, uint32_t morton,
+                 uint32_t* cluster_of, uint32_t* cluster_count, uint32_t* colour_of_cluster, uint32_t* ncolours,
+                 uint32_t* vert_rank, uint32_t* tet_order, uint32_t* colour_tet_begin) {
+	orc_csr csr;
+	if (csr_build(tets, nt, nv, &csr)) return -1;
+	static const int E[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+	/* 1. clusters */
+	uint32_t nc = 0;
+	uint32_t* cl_begin = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)nt + 1));
+	uint32_t* cl_tets = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)nt + 1));
+	if (!cl_begin || !cl_tets) return -1;
+	for (uint32_t t = 0; t < nt; t++) cluster_of[t] = 0xffffffffu;
+	uint32_t fill = 0;
+	for (uint32_t t = 0; t < nt; t++) {
+		if (cluster_of[t] != 0xffffffffu) continue;
+		cl_begin[nc] = fill;
+		if (mode == 0) {
+			cluster_of[t] = nc;
+			cl_tets[fill++] = t;
+			nc++;
+			continue;
+		}
+		const uint32_t* tv = tets + 4 * (size_t)t;
+		int best = 0;
+		uint32_t bestc = 0;
+		for (int e = 0; e < 6; e++) {
+			uint32_t a = tv[E[e][0]], b = tv[E[e][1]], cnt = 0;
+			for (uint32_t k = csr.off[a]; k < csr.off[a + 1]; k++) {
+				uint32_t s = csr.lst[k];
+				if (cluster_of[s] == 0xffffffffu && tet_has(tets + 4 * (size_t)s, b)) cnt++;
+			}
+			if (cnt > bestc) { bestc = cnt; best = e; }
+		}
+		uint32_t a = tv[E[best][0]], b = tv[E[best][1]];
+		uint32_t verts[ORC_MAXV], nvv = 0, ntt = 0;
+		for (uint32_t k = csr.off[a]; k < csr.off[a + 1]; k++) {
+			uint32_t s = csr.lst[k];
+			const uint32_t* sv = tets + 4 * (size_t)s;
+			if (cluster_of[s] != 0xffffffffu || !tet_has(sv, b)) continue;
+			if (ntt == ORC_MAXT) break;
+			uint32_t nv2 = nvv, tmp[ORC_MAXV + 4];
+			memcpy(tmp, verts, sizeof(uint32_t) * nvv);
+			for (int n = 0; n < 4; n++) {
+				int found = 0;
+				for (uint32_t q = 0; q < nv2; q++)
+					if (tmp[q] == sv[n]) { found = 1; break; }
+				if (!found) tmp[nv2++] = sv[n];
+			}
+			if (nv2 > ORC_MAXV) continue;
+			memcpy(verts, tmp, sizeof(uint32_t) * nv2);
+			nvv = nv2;
+			cluster_of[s] = nc;
+			cl_tets[fill++] = s;
+			ntt++;
+		}
+		nc++;
+	}
+	cl_begin[nc] = fill;
+	*cluster_count = nc;
+	/* 2. greedy colouring in cluster order */
+	uint32_t ncol = 0;
+	uint32_t* mark = (uint32_t*)malloc(sizeof(uint32_t) * ORC_MAXCOL);
+	if (!mark) return -1;
+	for (uint32_t c = 0; c < ORC_MAXCOL; c++) mark[c] = 0xffffffffu;
+	for (uint32_t k = 0; k < nc; k++) {
+		for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++) {
+			const uint32_t* tv = tets + 4 * (size_t)cl_tets[q];
+			for (int n = 0; n < 4; n++)
+				for (uint32_t j = csr.off[tv[n]]; j < csr.off[tv[n] + 1]; j++) {
+					uint32_t o = cluster_of[csr.lst[j]];
+					if (o < k) mark[colour_of_cluster[o]] = k;
+				}
+		}
+		uint32_t c = 0;
+		while (c < ORC_MAXCOL && mark[c] == k) c++;
+		if (c == ORC_MAXCOL) return -1;
+		colour_of_cluster[k] = c;
+		if (c + 1 > ncol) ncol = c + 1;
+	}
+	*ncolours = ncol;
+	/* 3. vertex order */
+	if (morton) {
+		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+		for (uint32_t v = 0; v < nv; v++)
+			for (int k = 0; k < 3; k++) {
+				float x = nodes[3 * (size_t)v + k];
+				if (x < mn[k]) mn[k] = x;
+				if (x > mx[k]) mx[k] = x;
+			}
+		float sc[3];
+		for (int k = 0; k < 3; k++) sc[k] = (mx[k] - mn[k]) > 0.0f ? 1023.0f / (mx[k] - mn[k]) : 0.0f;
+		orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
+		if (!kv) return -1;
+		for (uint32_t v = 0; v < nv; v++) {
+			uint32_t q[3];
+			for (int k = 0; k < 3; k++) {
+				float f = (nodes[3 * (size_t)v + k] - mn[k]) * sc[k];
+				uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
+				q[k] = u > 1023u ? 1023u : u;
+			}
+			kv[v].key = morton3(q[0], q[1], q[2]);
+			kv[v].id = v;
+		}
+		qsort(kv, nv, sizeof(orc_kv), kv_cmp);
+		for (uint32_t i = 0; i < nv; i++) vert_rank[kv[i].id] = i;
+		free(kv);
+	} else {
+		for (uint32_t v = 0; v < nv; v++) vert_rank[v] = v;
+	}
+	/* 4. cluster order inside each colour: (colour, min vertex rank, id) */
+	orc_kv* ck = (orc_kv*)malloc(sizeof(orc_kv) * (nc ? nc : 1));
+	if (!ck) return -1;
+	for (uint32_t k = 0; k < nc; k++) {
+		uint32_t mr = 0xffffffffu;
+		for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++)
+			for (int n = 0; n < 4; n++) {
+				uint32_t r = vert_rank[tets[4 * (size_t)cl_tets[q] + n]];
+				if (r < mr) mr = r;
+			}
+		ck[k].key = ((uint64_t)colour_of_cluster[k] << 32) | mr;
+		ck[k].id = k;
+	}
+	qsort(ck, nc, sizeof(orc_kv), kv_cmp);
+	uint32_t o = 0, col = 0;
+	colour_tet_begin[0] = 0;
+	for (uint32_t i = 0; i < nc; i++) {
+		uint32_t k = ck[i].id;
+		while (col < colour_of_cluster[k]) colour_tet_begin[++col] = o;
+		for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++) tet_order[o++] = cl_tets[q];
+	}
+	while (col < ncol) colour_tet_begin[++col] = o;
+	free(ck);
+	free(mark);
+	free(cl_begin);
+	free(cl_tets);
+	free(csr.off);
+	free(csr.lst);
+	return 0;
+}

@@ -1,0 +1,134 @@
+/*
+ * xfem_oracle — CPU restatement of the reference's small-step XPBD tetrahedral
+ * substep (jak-xyz/xpbd-fem), used ONLY as test infrastructure: by tests/, by
+ * __graft_entry__.smoke() and by bench.py's CPU-baseline / reference arm, and
+ * there only as the checker or as the timed CPU baseline. The shipped solver
+ * (libxfem.so) never links, loads or calls anything in this directory.
+ *
+ * Parity status: PINNED. The float instantiation is checked bit-for-bit
+ * against golden vectors produced by the unmodified reference code
+ * (oracle/build_ref.sh + oracle/refgen.cpp -> tests/golden/), covering mesh
+ * generation, rest state, per-element solves and whole substeps.
+ *
+ * Each routine is instantiated twice from oracle/xfem_oracle_real.inc:
+ *   *_f : reference semantics — positions double, element arithmetic float,
+ *         exactly the reference's operation order (compile with
+ *         -ffp-contract=off so no multiply-add is fused);
+ *   *_d : the same method with every quantity in double (the FP64 run that
+ *         the FP32 paths are measured against).
+ *
+ * Extensions that the reference does not have (and whose parity is therefore
+ * pinned only by this restatement and hand-derived cases): 3-D gravity,
+ * parameterised Yeoh coefficients, per-tet shear modulus, an arbitrary
+ * per-vertex lock mask, and a ground plane with Coulomb friction.
+ *
+ * The schedule routines (clusters, colours, Morton order) restate the
+ * product's host algorithms independently so integer/index results can be
+ * compared bit-exactly.
+ */
+#ifndef XFEM_ORACLE_H
+#define XFEM_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Energy model ids (XPBDFEM/Settings.h:41-53). */
+#define ORC_ENERGY_MIXED_SEL 4u
+#define ORC_ENERGY_YEOH_SKIN_FAST 7u
+
+/* Element parameter record, 17 values per tet, the reference's
+ * ElementParamsLinearTet (XPBDFEM/Fem.h:52-60) flattened:
+ * Qi column-major [0..8], QQ[9..11], QR[12..14], volume[15], surfaceArea[16]. */
+#define ORC_EP 17
+
+typedef struct orc_params {
+	float gravity[3];        /* reference: vec2 (x, y) only, XPBDFEM/Settings.h:83 */
+	float dt;
+	float time_corrected_drag; /* XPBDFEM/Settings.h:97 */
+	float compliance;        /* XPBDFEM/Settings.h:84 */
+	float poisson;           /* XPBDFEM/Settings.h:88 */
+	uint32_t energy;         /* ORC_ENERGY_* */
+	uint32_t simultaneous;   /* Settings_XpbdSolveBit, XPBDFEM/Settings.h:15 */
+	float yeoh[3];           /* reference hard-codes {0.1095, 14.95, 4.595} */
+	uint32_t lock_active;    /* Settings_LockLeft: apply the lock mask */
+	uint32_t ground;         /* extension: ground plane enabled */
+	float ground_n[3];
+	float ground_d;          /* plane dot(n, x) = d, solid where dot(n, x) < d */
+	float friction;          /* Coulomb coefficient */
+} orc_params;
+
+/* ---- mesh ---------------------------------------------------------------- */
+/* GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244): nodes[3*(W+1)(H+1)(D+1)],
+ * idx[5*6*W*H*D] (tagged stream, 4 = tet). */
+void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
+                       uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
+/* Parse the tagged index stream (XPBDFEM/Connectivity.cpp:251-265). With
+ * tets == NULL only counts. Returns 0, or -1 for a non-tet tag (hexes are
+ * not supported by this path). */
+int orc_parse_tets(const uint32_t* idx, uint32_t idx_count, uint32_t* tets,
+                   uint32_t* tet_count, uint32_t* vert_count);
+/* MINSTD shuffle of tet indices (XPBDFEM/Geo.cpp:759-771). */
+void orc_minstd_order(uint32_t nt, uint32_t* order);
+
+/* ---- rest state (GeoLinear3d::Init, XPBDFEM/Geo.cpp:697-745) -------------- */
+void orc_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt,
+                     float density, float* ep, float* w, uint8_t* vflags);
+void orc_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt,
+                     double density, double* ep, double* w, uint8_t* vflags);
+
+/* ---- one element (SolveElement, XPBDFEM/Fem.cpp:892) ---------------------- */
+/* X: 4x3 doubles, updated in place. mu_override <= 0 uses 1/compliance.
+ * lambda_out (nullable) receives the two multipliers. Returns 0 or -1 for an
+ * unsupported energy model. */
+int orc_solve_tet_f(double* X, const float* w, const float* ep, const orc_params* p,
+                    float mu_override, float* lambda_out);
+int orc_solve_tet_d(double* X, const double* w, const double* ep, const orc_params* p,
+                    double mu_override, double* lambda_out);
+
+/* ---- substeps (Geo3d::Substep, XPBDFEM/Geo.cpp:305-356) ------------------- */
+/* Runs nsub substeps. order[nt] is the constraint order (the reference's own
+ * tOrder, or a coloured schedule flattened). w is updated in place (locks set
+ * it to 0, as the reference does). tet_mu (nullable) gives a per-tet shear
+ * modulus in place of 1/compliance. contact (nullable, nv) receives the
+ * ground-contact set of the last substep. lambdas (nullable, 2*nt) receives
+ * each tet's multipliers from the last substep. Returns 0 or -1. */
+int orc_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask,
+                   uint32_t nt, const uint32_t* tets, const float* ep, const float* tet_mu,
+                   const uint32_t* order, uint32_t nsub, const orc_params* p,
+                   uint8_t* contact, float* lambdas);
+int orc_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask,
+                   uint32_t nt, const uint32_t* tets, const double* ep, const double* tet_mu,
+                   const uint32_t* order, uint32_t nsub, const orc_params* p,
+                   uint8_t* contact, double* lambdas);
+/* Same schedule, colours run with `threads` POSIX threads (tets of one colour
+ * share no vertex, so the result equals the sequential run bit for bit).
+ * colour_begin[ncolours+1] delimits colours inside `order`. */
+int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask,
+                            uint32_t nt, const uint32_t* tets, const float* ep, const float* tet_mu,
+                            const uint32_t* order, const uint32_t* colour_begin, uint32_t ncolours,
+                            uint32_t nsub, const orc_params* p, uint32_t threads);
+
+/* CalculateVolume (XPBDFEM/Geo.cpp:827-832, XPBDFEM/Fem.cpp:1066). */
+float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets);
+double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets);
+
+/* ---- schedule restatement -------------------------------------------------- */
+/* Edge-star clustering (mode 1) or one tet per cluster (mode 0); greedy
+ * colouring of clusters; Morton vertex order (morton != 0) and the cluster
+ * order inside each colour. Outputs (caller-allocated, sizes nt / nv / nt+1):
+ *   cluster_of[nt], cluster_count, colour_of_cluster[nt], ncolours,
+ *   vert_rank[nv] (new index of each vertex), tet_order[nt] (the flattened
+ *   Gauss-Seidel order: colour-major, cluster, tet-in-cluster),
+ *   colour_tet_begin[ncolours+1] (offsets into tet_order).
+ * Returns 0, or -1 if a limit is exceeded. */
+int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt,
+                 uint32_t mode, uint32_t morton,
+                 uint32_t* cluster_of, uint32_t* cluster_count, uint32_t* colour_of_cluster,
+                 uint32_t* ncolours, uint32_t* vert_rank, uint32_t* tet_order,
+                 uint32_t* colour_tet_begin);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,100 @@
+"""Generates the golden fixtures in tests/golden/ from the UNMODIFIED reference.
+
+Builds oracle/_ref/refgen with oracle/build_ref.sh (it compiles the reference
+sources XPBDFEM/{Fem,Geo,Connectivity,Allocator,MeshGen,vectormath,DebugGeo}.cpp
+where they lie, plus the harness driver oracle/refgen.cpp), runs it for every
+case in CASES, and stores each case's arrays as <name>.npz next to a
+manifest.json with the parameters. Needs the reference tree, so it runs in the
+development container only; the fixtures are committed and the tests read
+them without the reference.
+
+    python tests/golden/make_golden.py
+"""
+import json
+import os
+import struct
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REFGEN = os.path.join(ROOT, "oracle", "_ref", "refgen")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+DT = 1.0 / 1200.0
+# compliance = 4 (1 + nu) / E for the Neo-Hookean cases (mu_ref = mu / 2).
+C1_COMPLIANCE = 4.0 * 1.5 / 1e5
+
+CASES = [
+    ("meshgen_8x2x2", ["meshgen", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0]),
+    ("meshgen_3x2x2_mirror_wonky", ["meshgen", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3]),
+    ("meshgen_4x3x2_aniso_wonky", ["meshgen", 4, 3, 2, 0.1, 0.05, 0.07, 0, 0.5]),
+    ("init_8x2x2", ["init", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0]),
+    ("init_3x2x2_mirror_wonky", ["init", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3, 1000.0]),
+    ("init_5x3x2_aniso_wonky", ["init", 5, 3, 2, 0.02, 0.03, 0.04, 0, 0.4, 500.0]),
+    ("solve_nh_sim_incompressible", ["solve", 11, 64, 4, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("solve_nh_sim_nu045", ["solve", 12, 64, 4, 1, 0.01, 0.45, DT]),
+    ("solve_yeoh_sim_incompressible", ["solve", 13, 64, 7, 1, 3.2, 0.5, DT]),
+    ("solve_nh_serial_nu045", ["solve", 14, 64, 4, 0, 0.01, 0.45, DT]),
+    ("solve_yeoh_serial_nu049", ["solve", 15, 64, 7, 0, 0.5, 0.49, DT]),
+    ("substep_c1_nh_native", ["substep", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
+                              0.0, -9.81, DT, 40, 1]),
+    ("substep_c1_yeoh_native", ["substep", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.5,
+                                0.0, -9.81, DT, 40, 1]),
+    ("substep_wonky_nh_serial_native", ["substep", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                        -2.0, -9.81, DT, 10, 1]),
+    ("ordered_c1_nh_star", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
+                            0.0, -9.81, DT, 40, 1]),
+    ("ordered_c1_yeoh_tet", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.5,
+                             0.0, -9.81, DT, 40, 1]),
+]
+
+
+def parse(blob):
+    out, i = {}, 0
+    dt = {"f": np.float32, "d": np.float64, "I": np.uint32, "B": np.uint8}
+    while i < len(blob):
+        (n,) = struct.unpack_from("<I", blob, i); i += 4
+        name = blob[i:i + n].decode(); i += n
+        kind = chr(blob[i]); i += 1
+        (cnt,) = struct.unpack_from("<Q", blob, i); i += 8
+        a = np.frombuffer(blob, dt[kind], cnt, i).copy()
+        i += a.nbytes
+        out[name] = a
+    return out
+
+
+def main():
+    subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    manifest = {}
+    for name, args in CASES:
+        argv = [REFGEN] + [str(a) for a in args]
+        stdin = None
+        extra = {}
+        if args[0] == "ordered":
+            import oracle  # noqa: E402
+            W, H, D, sx, sy, sz, wonk = args[1:8]
+            nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), 0, wonk)
+            tets, _ = oracle.parse_tets(idx)
+            mode = 1 if name.endswith("_star") else 0
+            sch = oracle.schedule(nodes, tets, mode=mode, morton=1)
+            order = sch["tet_order"].astype(np.uint32)
+            stdin = struct.pack("<I", order.size) + order.tobytes()
+            extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
+            manifest_mode = mode
+        r = subprocess.run(argv, input=stdin, stdout=subprocess.PIPE, check=True)
+        arrays = parse(r.stdout)
+        arrays.update(extra)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        manifest[name] = {"args": args}
+        if args[0] == "ordered":
+            manifest[name]["schedule_mode"] = manifest_mode
+        print(f"{name}: " + ", ".join(f"{k}{list(v.shape)}" for k, v in arrays.items()))
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump(manifest, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

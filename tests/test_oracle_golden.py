@@ -1,0 +1,82 @@
+"""Pins the oracle restatement (oracle/xfem_oracle.c) to the reference.
+
+Every fixture in tests/golden/ was produced by the unmodified reference code
+(tests/golden/make_golden.py). The float restatement must reproduce each one
+bit for bit: mesh generation (XPBDFEM/MeshGen.cpp:156-244), rest state and
+masses (XPBDFEM/Fem.cpp:196-224, XPBDFEM/Geo.cpp:697-745), the MINSTD order
+(XPBDFEM/Geo.cpp:759-771), single-element solves (XPBDFEM/Fem.cpp:437-564,
+XPBDFEM/Xpbd.h:87-215) and whole substeps (XPBDFEM/Geo.cpp:305-356).
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, golden_args
+
+MESH = ["meshgen_8x2x2", "meshgen_3x2x2_mirror_wonky", "meshgen_4x3x2_aniso_wonky"]
+INIT = ["init_8x2x2", "init_3x2x2_mirror_wonky", "init_5x3x2_aniso_wonky"]
+SOLVE = ["solve_nh_sim_incompressible", "solve_nh_sim_nu045", "solve_yeoh_sim_incompressible",
+         "solve_nh_serial_nu045", "solve_yeoh_serial_nu049"]
+SUBSTEP = ["substep_c1_nh_native", "substep_c1_yeoh_native", "substep_wonky_nh_serial_native",
+           "ordered_c1_nh_star", "ordered_c1_yeoh_tet"]
+
+
+@pytest.mark.parametrize("name", MESH)
+def test_meshgen_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    nodes, idx = orc.gen_tet_block(a[1], a[2], a[3], tuple(a[4:7]), a[7], a[8])
+    assert np.array_equal(idx, g["idx"])
+    assert np.array_equal(nodes.view(np.uint32), g["nodes"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", INIT)
+def test_rest_state_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    tets, nv = orc.parse_tets(g["idx"])
+    assert np.array_equal(tets.reshape(-1), g["tet_idx"])
+    ep, w, fl = orc.init_rest(g["nodes"], tets, a[9])
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["ep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+    assert np.array_equal(orc.minstd_order(tets.shape[0]), g["torder"])
+    X = g["nodes"].astype(np.float64)
+    assert np.float32(orc.volume(X, tets)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+@pytest.mark.parametrize("name", SOLVE)
+def test_element_solve_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    p = orc.make_params(dt=a[7], compliance=a[5], poisson=a[6], energy=a[3], simultaneous=bool(a[4]))
+    n = a[2]
+    xin, xout = g["xin"].reshape(n, 4, 3), g["xout"].reshape(n, 4, 3)
+    ep, w, rest = g["ep"].reshape(n, 17), g["w"].reshape(n, 4), g["rest"].reshape(n, 4, 3)
+    for t in range(n):
+        # rest state of the random tet (InitFiniteElement on float-rounded nodes)
+        e, _, _ = orc.init_rest(rest[t].astype(np.float32).reshape(-1), np.array([[0, 1, 2, 3]], np.uint32), 1000.0)
+        assert np.array_equal(e[0].view(np.uint32), ep[t].view(np.uint32)), t
+        x, _ = orc.solve_tet(xin[t], w[t], ep[t], p)
+        assert np.array_equal(x.view(np.uint64), xout[t].view(np.uint64)), t
+
+
+@pytest.mark.parametrize("name", SUBSTEP)
+def test_substeps_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    W, H, D, sx, sy, sz, wonk, dens, energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[1:]
+    tets, nv = orc.parse_tets(g["idx"])
+    ep, w, fl = orc.init_rest(g["nodes"], tets, dens)
+    order = g["order"] if "order" in g else orc.minstd_order(tets.shape[0])
+    p = orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
+                        gravity=(gx, gy, 0.0), lock=bool(lock))
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lock_mask = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.substeps(X0, V0, w, tets, ep, order, 1, p, lock_mask=lock_mask)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.substeps(X1, V1, w1, tets, ep, order, nsub - 1, p, lock_mask=lock_mask)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(orc.volume(Xn, tets)).view(np.uint32) == g["volume"].view(np.uint32)[0]
