@@ -1,0 +1,341 @@
+"""Benchmark: tet-substeps/s of the small-step XPBD substep on one GB300.
+
+Workload: the 128x64x32-cube throughput mesh (1,572,864 Neo-Hookean tets,
+276,705 nodes, 0.1 m cubes jittered by N(0, (0.005 m)^2) with a fixed seed,
+bottom face fixed, gravity -z, incompressible, dt = 1/60 s with 20 substeps).
+One bench step = one frame = 20 substeps of the whole mesh; --steps 50 is the
+configuration's 50 frames. Inputs are synthetic (seeded), the mesh has the
+shape the configuration names.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl xfem|reference]
+
+--impl xfem (default): the GPU solver through libxfem.so's C ABI.
+  value  = tet-substeps/s with the state resident in HBM (device-timed with
+           CUDA events on the solver's stream, L2 flushed between frames);
+  e2e    = the same metric through the public API with pinned host buffers:
+           every step uploads positions and velocities, steps one frame and
+           reads the positions back (host-timed, copies included);
+  roofline, cpu_baseline (the oracle port of the reference in its own
+  shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches.
+--impl reference: the reference's CPU algorithm (the oracle port, run in the
+  GPU's colour order with all host threads) on the same mesh; each step is a
+  bounded sample of substeps.
+
+Multi-GPU (torchrun): replicas only — every rank steps its own copy of the
+mesh, no collective on the data path; value sums the ranks.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "xpbd-fem_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "tet-substeps/s (1.5M tets FP32)"
+UNIT = "tet-substeps/s"
+# Survey per-unit algorithmic bytes: 80 B tet record (4 u32 indices + Qi, QQ,
+# QR, volume) + 76 B per vertex per substep (X, V, O read/write 24 B each,
+# w 4 B) x V/T.
+REC_BYTES, VERT_BYTES = 80.0, 76.0
+# DRAM bytes per tet-substep of the persistent kernel from the ncu capture
+# summarised in profiles/ (None until a capture exists).
+NCU_DRAM_BYTES_PER_TET_SUBSTEP = None
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("XFEM_BENCH_BACKEND") != "gloo" else "gloo")
+    return world, rank, local
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline_native(w, budget_s=12.0):
+    """The oracle port of the reference, in the reference's own MINSTD order
+    (XPBDFEM/Geo.cpp:759-777), single thread, on the first substeps of the
+    same mesh; sized to about budget_s seconds."""
+    import oracle
+    tets, _ = oracle.parse_tets(w["idx"])
+    ep, wi, _ = oracle.init_rest(w["nodes"], tets, w["density"])
+    order = oracle.minstd_order(tets.shape[0])
+    sdt = w["dt"] / w["substeps"]
+    p = oracle.params_from_settings(w["settings"], sdt)
+    X = w["nodes"].reshape(-1, 3).astype(np.float64)
+    V = np.zeros_like(X)
+    t0 = time.perf_counter()
+    X, V, wi, _ = oracle.substeps(X, V, wi, tets, ep, order, 1, p, lock_mask=w["lock"])
+    t1 = time.perf_counter() - t0
+    n = max(1, min(30, int(budget_s / max(t1, 1e-3)) - 1))
+    t0 = time.perf_counter()
+    oracle.substeps(X, V, wi, tets, ep, order, n, p, lock_mask=w["lock"])
+    t = time.perf_counter() - t0
+    nt = tets.shape[0]
+    return {"value": nt * n / t, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{n} substeps of the full {nt}-tet mesh after 1 untimed, reference shuffled order, 1 thread"}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the oracle port with all host threads, colour order."""
+    if rank != 0:
+        return
+    import oracle
+    from xfem import workloads as W
+    w = W.throughput()
+    tets, _ = oracle.parse_tets(w["idx"])
+    ep, wi, _ = oracle.init_rest(w["nodes"], tets, w["density"])
+    sch = oracle.schedule(w["nodes"], tets, mode=1, morton=1)
+    sdt = w["dt"] / w["substeps"]
+    p = oracle.params_from_settings(w["settings"], sdt)
+    X = w["nodes"].reshape(-1, 3).astype(np.float64)
+    V = np.zeros_like(X)
+    threads = os.cpu_count() or 1
+    per_step = 1
+    nt = tets.shape[0]
+
+    def step(X, V, wi):
+        X2, V2, w2, _ = oracle.substeps(X, V, wi, tets, ep, sch["tet_order"], per_step, p, lock_mask=w["lock"],
+                                        threads=threads, colour_begin=sch["colour_tet_begin"])
+        return X2, V2, w2
+
+    for _ in range(args.warmup):
+        X, V, wi = step(X, V, wi)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        X, V, wi = step(X, V, wi)
+    t = time.perf_counter() - t0
+    value = nt * per_step * args.steps / t
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "impl": "reference",
+            "config": {"workload": w["name"], "tets": nt, "vertices": int(X.shape[0]),
+                       "substeps_per_step": per_step, "order": "colour order (same schedule as the GPU)",
+                       "l2": "n/a (CPU)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} substep(s) of the full mesh per step, {threads} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_xfem(args, world, rank, local):
+    import torch
+
+    import xfem
+    from xfem import workloads as W
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = W.throughput()
+    nt, nv = w["idx"].size // 5, w["nodes"].size // 3
+    sdt = w["dt"] / w["substeps"]
+    S = w["substeps"]
+    stream = torch.cuda.Stream(device=dev)
+    body = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], device=local,
+                     stream=C_void_p(stream.cuda_stream), sync_mode=args.sync_mode, block_size=args.block)
+    body.set_lock_mask(w["lock"])
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+    for _ in range(args.warmup):
+        body.step_frames(1, S, sdt)
+    body.synchronize()
+    info = body.info()
+    # device-timed region: one event pair per frame on the solver's stream,
+    # the L2 flush between frames stays outside the pairs
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                ev[k][0].record(stream)
+            body.step_frames(1, S, sdt)
+            with torch.cuda.stream(stream):
+                ev[k][1].record(stream)
+        body.synchronize()
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    total_s = sum(ms) / 1e3
+    total_s = reduce_max(total_s, world)
+    tet_sub = nt * S * args.steps
+    value = world * tet_sub / total_s
+    # end to end through the public API with pinned host buffers
+    px = np.frombuffer((ctypes_buffer(xfem, 3 * nv)), np.float32)
+    pv = np.frombuffer((ctypes_buffer(xfem, 3 * nv)), np.float32)
+    px[:] = w["nodes"]
+    pv[:] = 0.0
+    e2e_steps = max(3, min(args.steps, 20))
+    body.set_positions(px)
+    body.set_velocities(pv)
+    body.step_frames(1, S, sdt)
+    e2e_t = 0.0
+    for k in range(e2e_steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        body.synchronize()
+        t0 = time.perf_counter()
+        body.set_positions(px)
+        body.set_velocities(pv)
+        body.step_frames(1, S, sdt)
+        out = body.positions()
+        e2e_t += time.perf_counter() - t0
+        px[:] = out.reshape(-1)
+    e2e_t = reduce_max(e2e_t, world)
+    e2e = world * nt * S * e2e_steps / e2e_t
+    if rank != 0:
+        return
+    hbm, peak_kind = peaks()
+    bpu = REC_BYTES + VERT_BYTES * nv / nt
+    per_launch_ms = statistics.mean(ms)
+    launches_per_frame = 1 if info["sync_mode"] == 1 else S * info["colours"] + 1
+    achieved = bpu * nt * S / (per_launch_ms / 1e3) / 1e9
+    traffic = None if NCU_DRAM_BYTES_PER_TET_SUBSTEP is None else NCU_DRAM_BYTES_PER_TET_SUBSTEP * nt * S
+    cpu = cpu_baseline_native(w) if not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": w["name"], "tets": nt, "vertices": nv, "substeps_per_step": S,
+                   "dt": w["dt"], "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MB write)",
+                   "colours": info["colours"], "clusters": info["clusters"], "sync_mode":
+                   "persistent" if info["sync_mode"] == 1 else "cuda-graph", "block": info["block_size"],
+                   "blocks": info["blocks"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": peak_kind, "bytes_per_tet_substep": bpu,
+                     "kernel": "k_persistent" if info["sync_mode"] == 1 else "k_colour (whole frame)",
+                     "launch_ms": per_launch_ms},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * nv, "d2h_bytes_per_step": 12 * nv,
+                "steps": e2e_steps},
+        "gpu_launches": launches_per_frame * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def C_void_p(v):
+    import ctypes
+    return ctypes.c_void_p(v)
+
+
+def ctypes_buffer(xfem, nfloats):
+    import ctypes
+    p = xfem.lib().xfem_alloc_host(4 * nfloats)
+    if not p:
+        raise MemoryError("pinned allocation failed")
+    return (ctypes.c_float * nfloats).from_address(p)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="xfem", choices=["xfem", "reference"])
+    ap.add_argument("--sync-mode", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_xfem(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

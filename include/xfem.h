@@ -1,0 +1,221 @@
+/*
+ * xfem.h — C ABI of the GB300 (sm_103a) small-step XPBD tetrahedral solver.
+ *
+ * A drop-in for the linear-tet path of jak-xyz/xpbd-fem: the same mesh input
+ * (tagged index stream + float node array), the same rest-state precompute,
+ * material and compliance parameters, the same Neo-Hookean / Yeoh deviatoric
+ * plus volumetric constraints and the same one-iteration-per-substep schedule,
+ * run as a graph-coloured Gauss-Seidel sweep on the GPU.
+ *
+ * Conventions
+ *   - Every call returns int: XFEM_OK (0) or a negative XFEM_E* code;
+ *     xfem_last_error() gives a message for the calling thread.
+ *   - The caller owns host arrays; they are copied in or out. The handle owns
+ *     all device memory. Arrays are in the caller's vertex and tet order (the
+ *     internal Morton / colour permutations never leak out).
+ *   - Calls on one handle are serialised on its CUDA stream. Stepping calls
+ *     are asynchronous; a device-side error (bounded-wait timeout) is reported
+ *     by the next synchronising call (a get_* call or xfem_synchronize).
+ *   - One handle per host thread at a time.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   GeoLinear3d::Init            XPBDFEM/Geo.h:147, XPBDFEM/Geo.cpp:697-772
+ *   Geo3d::Substep               XPBDFEM/Geo.h:56,  XPBDFEM/Geo.cpp:305-356
+ *   GeoLinear3d::Constrain       XPBDFEM/Geo.cpp:774-788
+ *   GeoLinear3d::CalculateVolume XPBDFEM/Geo.cpp:827-832
+ *   struct Settings              XPBDFEM/Settings.h:79-102
+ *   Sim::Update substep loop     XPBDFEM/Demo.cpp:37-103
+ *   wasm exports UpdateSettings / AddBlock / FinishAddingBlocks / ResetDemo
+ *                                wasm/main.cpp:8-17, 71-95
+ *   GenerateTetBlock             XPBDFEM/MeshGen.cpp:223-244
+ */
+#ifndef XFEM_H
+#define XFEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+#define XFEM_OK 0
+#define XFEM_EINVAL (-1)          /* bad argument (null pointer, size mismatch, index out of range) */
+#define XFEM_EUNSUPPORTED (-2)    /* hex elements, energy models or settings this path does not run */
+#define XFEM_ENOMEM (-3)          /* host or device allocation failed */
+#define XFEM_ECUDA (-4)           /* CUDA runtime error (no device, launch or copy failure) */
+#define XFEM_EDEVICE_TIMEOUT (-5) /* a device-side bounded wait (grid barrier) ran out */
+#define XFEM_ELIMIT (-6)          /* a schedule limit was exceeded (colours, cluster size) */
+
+/* ---- flags: the reference's Settings::flags layout (XPBDFEM/Settings.h:9-29) - */
+#define XFEM_ENERGY_BIT 6u
+#define XFEM_ENERGY_MASK 31u
+#define XFEM_ENERGY_MIXED_SEL 4u       /* Energy_MixedSel: Neo-Hookean, prefactored I1 */
+#define XFEM_ENERGY_YEOH_SKIN_FAST 7u  /* Energy_YeohSkinFast */
+#define XFEM_XPBD_SOLVE_BIT 11u        /* set: coupled 2x2 solve; clear: serial */
+#define XFEM_LOCK_LEFT (1u << 26)      /* Settings_LockLeft: apply the lock mask */
+
+/* Solver settings. The first block mirrors the reference's Settings field by
+ * field (XPBDFEM/Settings.h:79-91) with gravity widened to 3-D; fields this
+ * path does not use are kept so a caller can fill the struct the same way. */
+typedef struct xfem_settings {
+	float time_scale;            /* unused by the solver (the caller picks dt) */
+	float substeps_per_second;   /* unused by the solver */
+	uint32_t volume_passes;      /* must be 0 (extra volume passes not built) */
+	float gravity[3];            /* reference: vec2 (x, y) */
+	float compliance;            /* 1 / mu_ref */
+	float damping;               /* must be 0 (post-step damping not built) */
+	float pbd_damping;           /* must be 0 */
+	float drag;                  /* informational; the solver uses time_corrected_drag */
+	float poissons_ratio;        /* 0.5 = incompressible (zero volumetric compliance) */
+	float wonkiness;             /* mesh generation only */
+	float left_right_separation; /* unused */
+	uint32_t flags;              /* energy bits 6-10, solve bit 11, lock bit 26 */
+	/* The reference's derived Settings::timeCorrectedDrag
+	 * (XPBDFEM/Settings.h:97), filled by Sim::Update (XPBDFEM/Demo.cpp:63);
+	 * xfem_time_corrected_drag() computes it. */
+	float time_corrected_drag;
+	/* Extensions (no reference counterpart). */
+	float yeoh[3];               /* Yeoh multipliers; reference constants {0.1095, 14.95, 4.595} */
+	uint32_t ground;             /* 1 = ground plane with Coulomb friction */
+	float ground_normal[3];      /* unit normal; solid side is dot(n, x) < offset */
+	float ground_offset;
+	float friction;              /* Coulomb coefficient */
+} xfem_settings;
+
+/* Create-time options (all zero = defaults). */
+typedef struct xfem_options {
+	uint32_t cluster_mode; /* 0 = default (edge-star clusters), 1 = one tet per cluster, 2 = edge-star */
+	uint32_t no_morton;    /* 1 = keep the caller's vertex order on the device */
+	uint32_t sync_mode;    /* 0 = auto (autotuned), 1 = persistent kernel + grid barrier, 2 = CUDA graph */
+	uint32_t block_size;   /* 0 = auto; else 64..1024, multiple of 32 */
+	uint32_t keep_lambdas; /* 1 = record each tet's two multipliers of the last substep */
+	int32_t device;        /* CUDA device ordinal; -1 or 0 = current / 0 */
+	void* stream;          /* cudaStream_t to run on; NULL = a stream owned by the handle */
+} xfem_options;
+
+/* One mesh for xfem_batch_create, in GeoLinear3d::Init's argument form. */
+typedef struct xfem_mesh {
+	const float* node_data;   /* 3 floats per vertex */
+	uint32_t node_data_count; /* 3 * vertex count */
+	const uint32_t* idx_data; /* tagged stream: 4, i0, i1, i2, i3, 4, ... */
+	uint32_t idx_data_count;
+	float density;
+} xfem_mesh;
+
+typedef struct xfem_info {
+	uint32_t bodies, vertices, tets, clusters, colours, orphans;
+	uint32_t chunks, tet_rows, block_size, blocks, sync_mode, cluster_mode;
+	uint64_t device_bytes;
+} xfem_info;
+
+typedef struct xfem_body xfem_body;
+
+/* ---- lifecycle ------------------------------------------------------------ */
+/* Fills s with the reference's Settings defaults (XPBDFEM/Settings.h:80-91)
+ * plus gravity z = 0, time_corrected_drag 0, the reference Yeoh constants and
+ * no ground. */
+int xfem_settings_default(xfem_settings* s);
+
+/* Replaces GeoLinear3d::Init(alloc, density, nodeData, nodeDataCount, idxData,
+ * idxDataCount, autoResize = false), XPBDFEM/Geo.cpp:697-772: connectivity,
+ * double-precision rest positions, Left/Right flags, rest state per tet,
+ * lumped masses and inverse masses — then builds the colour schedule and
+ * uploads everything. Hex elements (tag 8) return XFEM_EUNSUPPORTED. */
+int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
+int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                   uint32_t idx_data_count, float density, const xfem_settings* settings,
+                   const xfem_options* options, xfem_body** out);
+/* Many independent bodies in one handle (the batched mode): one merged colour
+ * schedule, one launch per frame. settings[i] per body (NULL = defaults). Body
+ * b is addressed by index b in the per-body calls below. Replaces the
+ * sequential per-body loop of Sim::Update (XPBDFEM/Demo.cpp:86-88). */
+int xfem_batch_create(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings,
+                      const xfem_options* options, xfem_body** out);
+int xfem_destroy(xfem_body* b);
+int xfem_get_info(const xfem_body* b, xfem_info* out);
+
+/* ---- parameters ---------------------------------------------------------- */
+/* Replaces the UpdateSettings export (wasm/main.cpp:80-95) for one body. */
+int xfem_set_settings(xfem_body* b, uint32_t body, const xfem_settings* s);
+/* Per-vertex lock mask in caller order (1 = locked while XFEM_LOCK_LEFT is
+ * set). At create time the mask is the reference's Left flag (x within 2% of
+ * the minimum, XPBDFEM/Geo.cpp:724). As in the reference, a locked vertex
+ * keeps a zero inverse mass from the first substep that locks it on. */
+int xfem_set_lock_mask(xfem_body* b, uint32_t body, const uint8_t* mask);
+/* Per-tet shear modulus mu_ref (caller tet order) in place of 1/compliance;
+ * NULL returns to the uniform material. */
+int xfem_set_tet_mu(xfem_body* b, uint32_t body, const float* mu);
+
+/* ---- stepping ------------------------------------------------------------- */
+/* One call of Geo3d::Substep (XPBDFEM/Geo.cpp:305-356) for every body:
+ * predict, one coloured Gauss-Seidel sweep over all tets, locks, ground,
+ * velocity update. */
+int xfem_substep(xfem_body* b, float dt);
+/* frames * substeps substeps in one launch (persistent kernel or one CUDA
+ * graph), the loop of Sim::Update (XPBDFEM/Demo.cpp:67-90) with a fixed dt. */
+int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
+/* Waits for queued work; returns XFEM_EDEVICE_TIMEOUT if a bounded device
+ * wait ran out since the last check. */
+int xfem_synchronize(xfem_body* b);
+
+/* ---- state transfer (caller vertex order; synchronising) ------------------ */
+int xfem_get_positions(xfem_body* b, uint32_t body, float* out_xyz);
+int xfem_set_positions(xfem_body* b, uint32_t body, const float* xyz);
+int xfem_get_velocities(xfem_body* b, uint32_t body, float* out_xyz);
+int xfem_set_velocities(xfem_body* b, uint32_t body, const float* xyz);
+int xfem_get_inverse_masses(xfem_body* b, uint32_t body, float* out_w);
+/* Ground-contact set of the last substep (1 = in contact). */
+int xfem_get_contacts(xfem_body* b, uint32_t body, uint8_t* out);
+/* Multipliers (lambda0, lambda1) of each tet in the last substep; needs
+ * keep_lambdas at create time. */
+int xfem_get_lambdas(xfem_body* b, uint32_t body, float* out_2nt);
+/* GeoLinear3d::CalculateVolume (XPBDFEM/Geo.cpp:827-832), summed in double. */
+int xfem_calculate_volume(xfem_body* b, uint32_t body, double* out);
+/* Rest state per tet (caller order) as 17 floats: Qi column-major, QQ[3],
+ * QR[3], volume, surfaceArea (ElementParamsLinearTet, XPBDFEM/Fem.h:52-60),
+ * and the rest inverse masses. */
+int xfem_get_rest_state(const xfem_body* b, uint32_t body, float* out_ep17, float* out_w);
+/* The schedule: device rank of each vertex, the flattened Gauss-Seidel tet
+ * order (colour-major, cluster, tet-in-cluster; caller tet ids) and the
+ * offsets of each colour in it (ncolours + 1 entries). */
+int xfem_get_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_rank, uint32_t* tet_order,
+                      uint32_t* colour_begin, uint32_t* ncolours);
+/* Counts of one body: vertices, tets. */
+int xfem_body_counts(const xfem_body* b, uint32_t body, uint32_t* nverts, uint32_t* ntets);
+
+/* ---- host-only set-up (no GPU needed) --------------------------------------- */
+/* The rest state GeoLinear3d::Init would compute for this mesh
+ * (XPBDFEM/Geo.cpp:697-745): 17 floats per tet as in xfem_get_rest_state,
+ * inverse masses, and vertex flags (bit 0 Left, bit 1 Right, bit 4 Pickable,
+ * XPBDFEM/Geo.h:16-20). Any output may be NULL. */
+int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                            uint32_t idx_data_count, float density, float* out_ep17, float* out_w,
+                            uint8_t* out_flags);
+/* The schedule xfem_create_ex would build (cluster_mode and no_morton as in
+ * xfem_options), in the form of xfem_get_schedule; colour_begin needs room
+ * for tets + 1 entries. Any output may be NULL. */
+int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                          uint32_t idx_data_count, uint32_t cluster_mode, uint32_t no_morton, uint32_t* vert_rank,
+                          uint32_t* tet_order, uint32_t* colour_begin, uint32_t* ncolours, uint32_t* nclusters);
+
+/* ---- helpers --------------------------------------------------------------- */
+/* timeCorrectedDrag = 1 - (1 - drag)^(1000 sdt), XPBDFEM/Demo.cpp:63. */
+float xfem_time_corrected_drag(float drag, float substep_dt);
+/* GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244): a W x H x D block of cubes
+ * with edge (sx, sy, sz), 6 tets per cube. nodes needs 3 (W+1)(H+1)(D+1)
+ * floats, idx 30 W H D words. */
+int xfem_generate_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
+                            uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
+/* Pinned host memory for fast transfers (cudaMallocHost / cudaFreeHost). */
+void* xfem_alloc_host(size_t bytes);
+void xfem_free_host(void* p);
+/* Message of the last failing call on this thread ("" if none). */
+const char* xfem_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XFEM_H */

@@ -53,6 +53,18 @@ def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=T
     return p
 
 
+def params_from_settings(s, dt, lock=True):
+    """orc_params from solver settings given as an xfem Settings struct or as
+    a dict of its fields (reference semantics)."""
+    g = (lambda k: s[k]) if isinstance(s, dict) else (lambda k: getattr(s, k))
+    flags = int(g("flags"))
+    return make_params(dt=dt, compliance=g("compliance"), poisson=g("poissons_ratio"), energy=(flags >> 6) & 31,
+                       simultaneous=bool((flags >> 11) & 1), gravity=tuple(g("gravity")),
+                       drag=g("time_corrected_drag"), yeoh=tuple(g("yeoh")),
+                       lock=lock and bool(flags & (1 << 26)), ground=bool(g("ground")),
+                       ground_n=tuple(g("ground_normal")), ground_d=g("ground_offset"), friction=g("friction"))
+
+
 _lib = None
 
 

@@ -1,0 +1,41 @@
+"""Test helpers: run the oracle on the same inputs and schedule as a GPU body."""
+import numpy as np
+
+import oracle
+import xfem
+
+
+def oracle_params(s, dt, lock=True):
+    """orc_params from an xfem Settings struct or settings dict."""
+    return oracle.params_from_settings(s, dt, lock)
+
+
+def rel(a, b):
+    """max |a - b| over max |b| (the error relative to the quantity's scale)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+class OracleRun:
+    """The oracle's state for one body, stepped in the body's own schedule."""
+
+    def __init__(self, nodes, idx, density, settings, order, lock_mask=None, tet_mu=None, dtype=np.float32):
+        self.tets, nv = oracle.parse_tets(idx)
+        self.ep, self.w, fl = oracle.init_rest(nodes, self.tets, density, dtype)
+        self.lock = (fl & 1).astype(np.uint8) if lock_mask is None else np.asarray(lock_mask, np.uint8)
+        self.X = np.asarray(nodes, np.float64).reshape(-1, 3).copy()
+        self.V = np.zeros_like(self.X)
+        self.s = settings
+        self.order = order
+        self.tet_mu = tet_mu
+        self.dtype = dtype
+        self.contact = None
+        self.lam = None
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt)
+        self.X, self.V, self.w, self.contact, self.lam = oracle.substeps(
+            self.X, self.V, self.w, self.tets, self.ep, self.order, n, p, lock_mask=self.lock,
+            tet_mu=self.tet_mu, dtype=self.dtype, want_lambdas=True)
+        return self

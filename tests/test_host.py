@@ -1,0 +1,148 @@
+"""CPU tests of libxfem.so's host side (no GPU needed).
+
+- the library loads and exports every function include/xfem.h declares;
+- rest state and masses equal the reference's (golden vectors) bit for bit
+  (XPBDFEM/Fem.cpp:131-224, XPBDFEM/Geo.cpp:697-745);
+- GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244) is reproduced bit for bit;
+- the colour schedule equals the oracle's independent restatement bit for
+  bit, and is a valid Gauss-Seidel colouring (every tet once, no two tets of
+  one colour share a vertex);
+- without a CUDA device the solver refuses to run (no CPU fallback).
+"""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, golden_args
+
+import xfem
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "xfem.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|float|void\*?|const char\*)\s+\*?(xfem_\w+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = xfem.lib()
+    names = header_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(L, n), n
+    assert sorted(names) == sorted(xfem.EXPORTS)
+
+
+@pytest.mark.parametrize("name", ["meshgen_8x2x2", "meshgen_3x2x2_mirror_wonky", "meshgen_4x3x2_aniso_wonky"])
+def test_generate_tet_block_bit_exact(name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    nodes, idx = xfem.generate_tet_block(a[1], a[2], a[3], tuple(a[4:7]), a[7], a[8])
+    assert np.array_equal(idx, g["idx"])
+    assert np.array_equal(nodes.view(np.uint32), g["nodes"].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["init_8x2x2", "init_3x2x2_mirror_wonky", "init_5x3x2_aniso_wonky"])
+def test_rest_state_bit_exact_vs_reference(name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    ep, w, fl = xfem.compute_rest_state(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["ep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+
+
+def _random_mesh(seed, W, H, D):
+    rng = np.random.default_rng(seed)
+    nodes, idx = xfem.generate_tet_block(W, H, D, (0.1, 0.07, 0.05), seed % 2, 0.0)
+    nodes = nodes + rng.normal(0, 0.004, nodes.shape).astype(np.float32)
+    # shuffle vertex ids and tet order so nothing relies on generator order
+    nv = nodes.size // 3
+    perm = rng.permutation(nv).astype(np.uint32)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(nv, dtype=np.uint32)
+    tets = idx.reshape(-1, 5)[:, 1:]
+    tets = inv[tets][rng.permutation(tets.shape[0])]
+    nodes = nodes.reshape(-1, 3)[perm].reshape(-1)
+    idx = np.concatenate([np.full((tets.shape[0], 1), 4, np.uint32), tets], 1).reshape(-1)
+    return nodes.astype(np.float32), idx.astype(np.uint32)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_rest_state_matches_oracle_on_jittered_meshes(orc, seed):
+    nodes, idx = _random_mesh(seed, 5, 4, 3)
+    ep, w, fl = xfem.compute_rest_state(nodes, idx, 1000.0)
+    tets, _ = orc.parse_tets(idx)
+    e2, w2, f2 = orc.init_rest(nodes, tets, 1000.0)
+    assert np.array_equal(ep.view(np.uint32), e2.view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), w2.view(np.uint32))
+    assert np.array_equal(fl, f2)
+
+
+def check_colouring(tets, order, cb, cluster_of):
+    """Every tet once; clusters of one colour share no vertex (tets inside a
+    cluster run in sequence on one thread and may share vertices)."""
+    nt = tets.shape[0]
+    assert np.array_equal(np.sort(order), np.arange(nt))
+    for c in range(cb.size - 1):
+        ts = order[cb[c]:cb[c + 1]]
+        owner = {}
+        for t in ts:
+            for v in tets[t]:
+                k = owner.setdefault(int(v), int(cluster_of[t]))
+                assert k == cluster_of[t], f"colour {c}: clusters {k} and {cluster_of[t]} share vertex {v}"
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("morton", [True, False])
+@pytest.mark.parametrize("mesh", ["box", "jitter"])
+def test_schedule_bit_exact_vs_oracle(orc, mode, morton, mesh):
+    if mesh == "box":
+        nodes, idx = xfem.generate_tet_block(9, 5, 4, (0.1, 0.1, 0.1))
+    else:
+        nodes, idx = _random_mesh(7, 6, 5, 4)
+    s = xfem.compute_schedule(nodes, idx, cluster_mode=mode, morton=morton)
+    tets, _ = orc.parse_tets(idx)
+    # product cluster_mode: 0 default (edge stars), 1 one tet each, 2 edge stars
+    o = orc.schedule(nodes, tets, mode=0 if mode == 1 else 1, morton=int(morton))
+    assert s["colours"] == o["colours"]
+    assert s["clusters"] == o["clusters"]
+    assert np.array_equal(s["vert_rank"], o["vert_rank"])
+    assert np.array_equal(s["tet_order"], o["tet_order"])
+    assert np.array_equal(s["colour_tet_begin"], o["colour_tet_begin"])
+    check_colouring(tets, s["tet_order"], s["colour_tet_begin"], o["cluster_of"])
+
+
+def test_schedule_colour_counts_on_cube_grid():
+    # 6-tet cubes: an interior vertex touches 24 tets and 8 cubes, so one tet
+    # per cluster needs >= 24 colours and edge-star (cube) clusters >= 8.
+    nodes, idx = xfem.generate_tet_block(12, 8, 6, (0.1, 0.1, 0.1))
+    s_tet = xfem.compute_schedule(nodes, idx, cluster_mode=1)
+    s_star = xfem.compute_schedule(nodes, idx, cluster_mode=0)
+    assert s_star["clusters"] == 12 * 8 * 6
+    assert s_star["colours"] == 8
+    assert 24 <= s_tet["colours"] <= 40
+
+
+def test_errors_without_gpu_or_bad_input():
+    nodes, idx = xfem.generate_tet_block(2, 1, 1, (0.1, 0.1, 0.1))
+    hexes = np.array([8, 0, 1, 2, 3, 4, 5, 6, 7], np.uint32)
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_rest_state(np.zeros(24, np.float32), hexes, 1000.0)
+    assert e.value.code == xfem.EUNSUPPORTED
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_rest_state(nodes[:-3], idx, 1000.0)
+    assert e.value.code == xfem.EINVAL
+    import torch
+    if not torch.cuda.is_available():
+        # no silent CPU path: creating a solver needs the GPU
+        with pytest.raises(xfem.XfemError) as e:
+            xfem.Body(nodes, idx, 1000.0)
+        assert e.value.code == xfem.ECUDA
+
+
+def test_time_corrected_drag():
+    assert xfem.time_corrected_drag(0.0, 1 / 1200) == 0.0
+    v = xfem.time_corrected_drag(0.002, 1 / 3000)
+    assert abs(v - (1 - (1 - 0.002) ** (1000 / 3000))) < 1e-7

@@ -1,0 +1,75 @@
+"""Builds libxfem.so in-tree (xpbd-fem_gb300/xfem/libxfem.so) for sm_103a.
+
+    python xpbd-fem_gb300/build.py [--force]
+
+Every translation unit is compiled by nvcc in parallel, then linked with
+-shared. Host code is compiled with -ffp-contract=off: the rest-state
+precompute must reproduce the reference bit for bit and the schedule must give
+the same integers on x86-64 and AArch64.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "csrc")
+OUT_DIR = os.path.join(HERE, "xfem")
+LIB = os.path.join(OUT_DIR, "libxfem.so")
+BUILD = os.path.join(HERE, "_build")
+SOURCES = ["xfem_kernels.cu", "xfem_api.cpp", "xfem_host.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall",
+          "-I" + os.path.join(HERE, "..", "include")]
+
+
+def nvcc():
+    p = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(p):
+        raise RuntimeError("nvcc not found")
+    return p
+
+
+def _stale():
+    if not os.path.exists(LIB):
+        return True
+    t = os.path.getmtime(LIB)
+    deps = [os.path.join(SRC, f) for f in os.listdir(SRC)] + [os.path.join(HERE, "..", "include", "xfem.h"),
+                                                              os.path.abspath(__file__)]
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False):
+    if not force and not _stale():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cc = nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, src + ".o")
+        cmd = [cc] + ARCH + COMMON + ["-c", os.path.join(SRC, src), "-o", obj]
+        if src.endswith(".cu"):
+            cmd += ["-Xptxas", "-v"] if verbose else []
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        return obj, r.stderr
+
+    with cf.ThreadPoolExecutor(len(SOURCES)) as ex:
+        results = list(ex.map(compile_one, SOURCES))
+    if verbose:
+        for _, err in results:
+            if err:
+                print(err)
+    tmp = LIB + ".tmp"
+    cmd = [cc] + ARCH + ["-shared", "-o", tmp] + [o for o, _ in results] + ["-lcudart_static", "-lpthread", "-ldl", "-lrt"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,833 @@
+// C ABI of libxfem.so (include/xfem.h): handle management, packing of the
+// schedule into the device layout, stepping and transfers.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/xfem.h"
+#include "xfem_internal.h"
+
+using namespace xfem;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+	g_err = msg;
+	return code;
+}
+
+#define XCUDA(call)                                                                                    \
+	do {                                                                                               \
+		cudaError_t e_ = (call);                                                                       \
+		if (e_ != cudaSuccess) return fail(XFEM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+	} while (0)
+
+struct BodyHost {
+	uint32_t nv = 0, nt = 0, vbase = 0;
+	std::vector<float> nodes;         // rest positions, caller order
+	std::vector<uint32_t> tets;       // caller order
+	std::vector<float> ep;            // 17 per tet
+	std::vector<float> w0;            // rest inverse masses
+	std::vector<uint8_t> vflags;
+	std::vector<float> tet_mu;        // empty = uniform material
+	xfem_settings settings;
+	Schedule sched;
+	std::vector<uint32_t> tet_slot;   // caller tet -> row * 32 + lane
+};
+
+template <typename T>
+struct DevBuf {
+	T* p = nullptr;
+	size_t n = 0;
+	~DevBuf() {
+		if (p) cudaFree(p);
+	}
+	cudaError_t alloc(size_t count) {
+		n = count;
+		return cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
+	}
+};
+
+}  // namespace
+
+struct xfem_body {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	bool own_stream = false;
+	xfem_options opt{};
+	std::vector<BodyHost> bodies;
+	uint32_t nverts = 0, ntets = 0, nchunks = 0, nrows = 0, nvrows = 0, ncolours = 0;
+	// device buffers
+	DevBuf<float4> vert, trec;
+	DevBuf<uint32_t> chdr, cvid, cslot, ccb, orphans, dev_of_vert, tets_dev, bar;
+	DevBuf<ChunkMeta> chunks;
+	DevBuf<BodyParams> params;
+	DevBuf<float2> tlam;
+	DevBuf<int> err;
+	DevBuf<float> stage;
+	DevBuf<double> vol;
+	std::vector<float4> trec_host;  // kept to refresh c0 after material changes
+	uint32_t norphans = 0;
+	LaunchCfg cfg;
+	DevCtx ctx{};
+	bool tuned = false;
+	// cached CUDA graph (graph mode)
+	cudaGraphExec_t graph = nullptr;
+	uint32_t graph_nsub = 0;
+	float graph_dt = 0.0f;
+	uint64_t device_bytes = 0;
+
+	~xfem_body() {
+		if (graph) cudaGraphExecDestroy(graph);
+		if (own_stream && stream) cudaStreamDestroy(stream);
+	}
+};
+
+namespace {
+
+int validate_settings(const xfem_settings& s) {
+	const uint32_t energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+	if (energy != XFEM_ENERGY_MIXED_SEL && energy != XFEM_ENERGY_YEOH_SKIN_FAST)
+		return fail(XFEM_EUNSUPPORTED, "energy model " + std::to_string(energy) +
+		                                   " not supported (MixedSel = 4 and YeohSkinFast = 7 are)");
+	if (s.volume_passes != 0) return fail(XFEM_EUNSUPPORTED, "volume_passes must be 0");
+	if (s.damping != 0.0f || s.pbd_damping != 0.0f)
+		return fail(XFEM_EUNSUPPORTED, "post-step damping (damping, pbd_damping) is not supported");
+	if (s.flags & (1u << 27)) return fail(XFEM_EUNSUPPORTED, "Settings_LockRight is not supported");
+	if (!(s.compliance > 0.0f)) return fail(XFEM_EINVAL, "compliance must be > 0");
+	if (!(s.poissons_ratio > 0.0f && s.poissons_ratio <= 0.5f))
+		return fail(XFEM_EINVAL, "poissons_ratio must be in (0, 0.5]");
+	if (s.ground && !(s.friction >= 0.0f)) return fail(XFEM_EINVAL, "friction must be >= 0");
+	return XFEM_OK;
+}
+
+// The reference's material scalars (XPBDFEM/Fem.cpp:445-449) in float.
+BodyParams make_params(const xfem_settings& s) {
+	BodyParams p{};
+	const float mu = 1.0f / s.compliance;
+	const float nu = s.poissons_ratio;
+	const float lambda = (2.0f * mu * nu) / (1.0f - 2.0f * nu);
+	p.mu = mu;
+	p.inv_mu = 1.0f / mu;
+	p.inv_lambda = 1.0f / lambda;
+	p.a = 1.0f + mu / lambda;
+	p.ratio = mu * p.inv_lambda;
+	for (int k = 0; k < 3; k++) p.yeoh[k] = s.yeoh[k];
+	p.energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+	p.simultaneous = (s.flags >> XFEM_XPBD_SOLVE_BIT) & 1u;
+	for (int k = 0; k < 3; k++) p.gravity[k] = s.gravity[k];
+	p.drag_mul = 1.0f - s.time_corrected_drag;
+	p.lock_active = (s.flags & XFEM_LOCK_LEFT) ? 1u : 0u;
+	p.ground = s.ground ? 1u : 0u;
+	p.friction = s.friction;
+	for (int k = 0; k < 3; k++) p.ground_n[k] = s.ground_normal[k];
+	p.ground_d = s.ground_offset;
+	return p;
+}
+
+// c0 = (1/mu)/volume exactly as the reference forms comp[0] (XPBDFEM/Fem.cpp:449).
+float tet_c0(const BodyHost& b, uint32_t t) {
+	const float mu = b.tet_mu.empty() ? 1.0f / b.settings.compliance : b.tet_mu[t];
+	return 1.0f / mu / b.ep[17 * (size_t)t + 15];
+}
+
+int check_device_error(xfem_body* h) {
+	int e = 0;
+	XCUDA(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	if (e != 0) {
+		XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
+		if (e == kErrBarrierTimeout) return fail(XFEM_EDEVICE_TIMEOUT, "device grid barrier timed out");
+		return fail(XFEM_ECUDA, "device error " + std::to_string(e));
+	}
+	return XFEM_OK;
+}
+
+int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
+	if (!m.node_data || !m.idx_data) return fail(XFEM_EINVAL, "null mesh array");
+	if (m.node_data_count % 3) return fail(XFEM_EINVAL, "node_data_count must be a multiple of 3");
+	for (uint32_t i = 0; i < m.idx_data_count;) {
+		const uint32_t tag = m.idx_data[i];
+		if (tag == 8u) return fail(XFEM_EUNSUPPORTED, "hex elements (tag 8) are not supported by this path");
+		if (tag != 4u) return fail(XFEM_EINVAL, "unknown element tag " + std::to_string(tag) + " at " + std::to_string(i));
+		i += 5;
+	}
+	uint32_t nv = 0;
+	if (parse_tets(m.idx_data, m.idx_data_count, b.tets, nv)) return fail(XFEM_EINVAL, "truncated index stream");
+	// GeoLinear3d::Init asserts vertCount == nodeDataCount / 3 (XPBDFEM/Geo.cpp:700)
+	if (nv != m.node_data_count / 3)
+		return fail(XFEM_EINVAL, "vertex count " + std::to_string(nv) + " implied by the index stream != node_data_count/3 = " +
+		                             std::to_string(m.node_data_count / 3));
+	if (!(m.density > 0.0f)) return fail(XFEM_EINVAL, "density must be > 0");
+	b.nv = nv;
+	b.nt = (uint32_t)(b.tets.size() / 4);
+	b.nodes.assign(m.node_data, m.node_data + m.node_data_count);
+	b.ep.resize(17 * (size_t)b.nt);
+	b.w0.resize(nv);
+	b.vflags.resize(nv);
+	init_rest(b.nodes.data(), nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
+	return XFEM_OK;
+}
+
+int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint32_t morton, BodyHost& b) {
+	int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (s) {
+		b.settings = *s;
+	} else {
+		xfem_settings_default(&b.settings);
+	}
+	rc = validate_settings(b.settings);
+	if (rc) return rc;
+	if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, mode, morton, b.sched))
+		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
+	return XFEM_OK;
+}
+
+struct Lane {
+	uint32_t body, cluster;
+};
+
+// Packs every body's schedule into the merged device layout and uploads it.
+int build_device(xfem_body* h) {
+	const uint32_t nb = (uint32_t)h->bodies.size();
+	uint32_t nverts = 0, ntets = 0, ncol = 1;
+	for (auto& b : h->bodies) {
+		b.vbase = nverts;
+		nverts += b.nv;
+		ntets += b.nt;
+		ncol = std::max(ncol, b.sched.ncolours);
+	}
+	if (nb >= (1u << 24)) return fail(XFEM_ELIMIT, "too many bodies");
+	h->nverts = nverts;
+	h->ntets = ntets;
+	h->ncolours = ncol;
+	// chunks: colour-major, bodies in order, 32 clusters per chunk
+	std::vector<uint32_t> ccb(ncol + 1, 0);
+	std::vector<std::vector<Lane>> chunk_lanes;
+	for (uint32_t c = 0; c < ncol; c++) {
+		ccb[c] = (uint32_t)chunk_lanes.size();
+		std::vector<Lane> lanes;
+		for (uint32_t bi = 0; bi < nb; bi++) {
+			const Schedule& s = h->bodies[bi].sched;
+			if (c >= s.ncolours) continue;
+			for (uint32_t i = s.colour_cl_begin[c]; i < s.colour_cl_begin[c + 1]; i++) lanes.push_back({bi, s.colour_cl[i]});
+		}
+		for (size_t i = 0; i < lanes.size(); i += kLanes)
+			chunk_lanes.emplace_back(lanes.begin() + i, lanes.begin() + std::min(lanes.size(), i + kLanes));
+	}
+	ccb[ncol] = (uint32_t)chunk_lanes.size();
+	const uint32_t nch = (uint32_t)chunk_lanes.size();
+	std::vector<ChunkMeta> meta(nch);
+	uint32_t trows = 0, vrows = 0;
+	for (uint32_t k = 0; k < nch; k++) {
+		uint32_t ntm = 0, nvm = 0;
+		for (const Lane& L : chunk_lanes[k]) {
+			const BodyHost& b = h->bodies[L.body];
+			const uint32_t nt = b.sched.cl_begin[L.cluster + 1] - b.sched.cl_begin[L.cluster];
+			// vertex count of the cluster
+			uint32_t vs[kMaxClusterVerts + 4], nvv = 0;
+			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++)
+				for (int n = 0; n < 4; n++) {
+					const uint32_t v = b.tets[4 * (size_t)b.sched.cl_tets[q] + n];
+					if (std::find(vs, vs + nvv, v) == vs + nvv) vs[nvv++] = v;
+				}
+			ntm = std::max(ntm, nt);
+			nvm = std::max(nvm, nvv);
+		}
+		meta[k] = {trows, ntm, vrows, nvm};
+		trows += ntm;
+		vrows += nvm;
+	}
+	h->nchunks = nch;
+	h->nrows = trows;
+	h->nvrows = vrows;
+	std::vector<uint32_t> chdr((size_t)nch * kLanes, 0), cvid((size_t)vrows * kLanes, 0), cslot((size_t)trows * kLanes, 0);
+	std::vector<float4> trec((size_t)trows * 4 * kLanes, make_float4(0, 0, 0, 0));
+	std::vector<uint8_t> in_colour0(nverts, 0);
+	for (auto& b : h->bodies) b.tet_slot.assign(b.nt, 0xffffffffu);
+	for (uint32_t k = 0; k < nch; k++) {
+		const bool colour0 = k < ccb[1];
+		for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++) {
+			const Lane& L = chunk_lanes[k][lane];
+			BodyHost& b = h->bodies[L.body];
+			uint32_t vs[kMaxClusterVerts], nvv = 0, ntt = 0;
+			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++, ntt++) {
+				const uint32_t t = b.sched.cl_tets[q];
+				uint32_t slots = 0;
+				for (int n = 0; n < 4; n++) {
+					const uint32_t v = b.tets[4 * (size_t)t + n];
+					uint32_t* f = std::find(vs, vs + nvv, v);
+					if (f == vs + nvv) vs[nvv++] = v;
+					slots |= (uint32_t)(f - vs) << (4 * n);
+				}
+				const uint32_t row = meta[k].trow + ntt;
+				cslot[(size_t)row * kLanes + lane] = slots;
+				b.tet_slot[t] = row * kLanes + lane;
+				const float* e = &b.ep[17 * (size_t)t];
+				float4* r = &trec[(size_t)row * 4 * kLanes + lane];
+				r[0] = make_float4(e[0], e[1], e[2], e[3]);
+				r[kLanes] = make_float4(e[4], e[5], e[6], e[7]);
+				r[2 * kLanes] = make_float4(e[8], e[9], e[10], e[11]);
+				r[3 * kLanes] = make_float4(e[12], e[13], e[14], tet_c0(b, t));
+			}
+			for (uint32_t s = 0; s < nvv; s++) {
+				const uint32_t dv = b.vbase + b.sched.vert_rank[vs[s]];
+				cvid[(size_t)(meta[k].vrow + s) * kLanes + lane] = dv;
+				if (colour0) in_colour0[dv] = 1;
+			}
+			chdr[(size_t)k * kLanes + lane] = nvv | (ntt << 4) | (L.body << 8);
+		}
+	}
+	std::vector<uint32_t> orphans;
+	for (uint32_t v = 0; v < nverts; v++)
+		if (!in_colour0[v]) orphans.push_back(v);
+	h->norphans = (uint32_t)orphans.size();
+	// vertex state: canonical (X, V) = (rest, 0); bits = lock | body << 8
+	std::vector<float4> vert(2 * (size_t)nverts);
+	std::vector<uint32_t> dev_of(nverts), tets_dev(4 * (size_t)ntets);
+	std::vector<BodyParams> params(nb);
+	size_t tbase = 0;
+	for (uint32_t bi = 0; bi < nb; bi++) {
+		const BodyHost& b = h->bodies[bi];
+		for (uint32_t v = 0; v < b.nv; v++) {
+			const uint32_t dv = b.vbase + b.sched.vert_rank[v];
+			dev_of[b.vbase + v] = dv;
+			const uint32_t bits = (b.vflags[v] & 1u ? kFlagLocked : 0u) | (bi << 8);
+			vert[2 * (size_t)dv] = make_float4(b.nodes[3 * (size_t)v], b.nodes[3 * (size_t)v + 1], b.nodes[3 * (size_t)v + 2], b.w0[v]);
+			vert[2 * (size_t)dv + 1] = make_float4(0.0f, 0.0f, 0.0f, __builtin_bit_cast(float, bits));
+		}
+		for (size_t i = 0; i < 4 * (size_t)b.nt; i++) tets_dev[tbase + i] = b.vbase + b.sched.vert_rank[b.tets[i]];
+		tbase += 4 * (size_t)b.nt;
+		params[bi] = make_params(b.settings);
+	}
+	h->trec_host = trec;
+	// upload
+	XCUDA(h->vert.alloc(vert.size()));
+	XCUDA(h->trec.alloc(trec.size()));
+	XCUDA(h->chdr.alloc(chdr.size()));
+	XCUDA(h->cvid.alloc(cvid.size()));
+	XCUDA(h->cslot.alloc(cslot.size()));
+	XCUDA(h->ccb.alloc(ccb.size()));
+	XCUDA(h->orphans.alloc(orphans.size()));
+	XCUDA(h->dev_of_vert.alloc(dev_of.size()));
+	XCUDA(h->tets_dev.alloc(tets_dev.size()));
+	XCUDA(h->chunks.alloc(meta.size()));
+	XCUDA(h->params.alloc(params.size()));
+	XCUDA(h->bar.alloc(1));
+	XCUDA(h->err.alloc(1));
+	uint32_t maxnv = 1;
+	for (auto& b : h->bodies) maxnv = std::max(maxnv, b.nv);
+	XCUDA(h->stage.alloc(3 * (size_t)maxnv));
+	XCUDA(h->vol.alloc(1));
+	if (h->opt.keep_lambdas) XCUDA(h->tlam.alloc((size_t)trows * kLanes));
+	auto up = [&](void* dst, const void* src, size_t bytes) {
+		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+	};
+	XCUDA(up(h->vert.p, vert.data(), vert.size() * sizeof(float4)));
+	XCUDA(up(h->trec.p, trec.data(), trec.size() * sizeof(float4)));
+	XCUDA(up(h->chdr.p, chdr.data(), chdr.size() * 4));
+	XCUDA(up(h->cvid.p, cvid.data(), cvid.size() * 4));
+	XCUDA(up(h->cslot.p, cslot.data(), cslot.size() * 4));
+	XCUDA(up(h->ccb.p, ccb.data(), ccb.size() * 4));
+	XCUDA(up(h->orphans.p, orphans.data(), orphans.size() * 4));
+	XCUDA(up(h->dev_of_vert.p, dev_of.data(), dev_of.size() * 4));
+	XCUDA(up(h->tets_dev.p, tets_dev.data(), tets_dev.size() * 4));
+	XCUDA(up(h->chunks.p, meta.data(), meta.size() * sizeof(ChunkMeta)));
+	XCUDA(up(h->params.p, params.data(), params.size() * sizeof(BodyParams)));
+	XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
+	if (h->tlam.p) XCUDA(cudaMemsetAsync(h->tlam.p, 0, h->tlam.n * sizeof(float2), h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	h->device_bytes = vert.size() * 16 + trec.size() * 16 + (chdr.size() + cvid.size() + cslot.size() + ccb.size() +
+	                  orphans.size() + dev_of.size() + tets_dev.size()) * 4 + meta.size() * 16 + params.size() * 64 +
+	                  h->stage.n * 4 + h->tlam.n * 8;
+	DevCtx& c = h->ctx;
+	c.vert = h->vert.p;
+	c.chdr = h->chdr.p;
+	c.cvid = h->cvid.p;
+	c.cslot = h->cslot.p;
+	c.trec = h->trec.p;
+	c.tlam = h->tlam.p;
+	c.chunks = h->chunks.p;
+	c.colour_chunk_begin = h->ccb.p;
+	c.orphans = h->orphans.p;
+	c.bodies = h->params.p;
+	c.nverts = nverts;
+	c.norphans = h->norphans;
+	c.ncolours = ncol;
+	c.bar_count = h->bar.p;
+	c.err = h->err.p;
+	h->cfg.lambdas = h->opt.keep_lambdas != 0;
+	h->cfg.total_chunks = nch;
+	h->cfg.colour_chunk_begin_host = ccb;
+	return XFEM_OK;
+}
+
+int set_config(xfem_body* h, int sync_mode, int block) {
+	h->cfg.sync_mode = sync_mode;
+	h->cfg.block = block;
+	if (const int ek = configure_kernels(h->cfg))
+		return fail(XFEM_ECUDA, std::string("kernel configuration: ") + cudaGetErrorString((cudaError_t)ek));
+	if (sync_mode == 1) {
+		int blocks = 0;
+		const int e = persistent_grid(h->cfg, &blocks);
+		if (e) return fail(XFEM_ECUDA, std::string("occupancy query failed: ") + cudaGetErrorString((cudaError_t)e));
+		h->cfg.blocks = blocks;
+	}
+	if (h->graph) {
+		cudaGraphExecDestroy(h->graph);
+		h->graph = nullptr;
+	}
+	return XFEM_OK;
+}
+
+int run(xfem_body* h, uint32_t nsub, float dt) {
+	if (h->cfg.sync_mode == 1) {
+		const int e = launch_substeps(h->ctx, h->cfg, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("persistent launch: ") + cudaGetErrorString((cudaError_t)e));
+		return XFEM_OK;
+	}
+	if (!h->graph || h->graph_nsub != nsub || h->graph_dt != dt) {
+		if (h->graph) {
+			cudaGraphExecDestroy(h->graph);
+			h->graph = nullptr;
+		}
+		cudaGraph_t g = nullptr;
+		XCUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+		const int e = launch_substeps(h->ctx, h->cfg, nsub, dt, h->stream);
+		const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+		if (e) return fail(XFEM_ECUDA, std::string("graph capture: ") + cudaGetErrorString((cudaError_t)e));
+		if (ec != cudaSuccess) return fail(XFEM_ECUDA, std::string("graph capture: ") + cudaGetErrorString(ec));
+		const cudaError_t ei = cudaGraphInstantiate(&h->graph, g, 0);
+		cudaGraphDestroy(g);
+		if (ei != cudaSuccess) return fail(XFEM_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(ei));
+		h->graph_nsub = nsub;
+		h->graph_dt = dt;
+	}
+	XCUDA(cudaGraphLaunch(h->graph, h->stream));
+	return XFEM_OK;
+}
+
+// Times the candidate launch configurations on a saved copy of the state and
+// keeps the fastest. The state is restored afterwards.
+int autotune(xfem_body* h, uint32_t nsub, float dt) {
+	if (h->tuned) return XFEM_OK;
+	h->tuned = true;
+	const int fixed_sync = (int)h->opt.sync_mode, fixed_block = (int)h->opt.block_size;
+	std::vector<std::pair<int, int>> cand;
+	const int blocks[] = {128, 256, 512};
+	for (int sm : {1, 2}) {
+		if (fixed_sync && sm != fixed_sync) continue;
+		for (int bs : blocks) {
+			if (fixed_block && bs != fixed_block) continue;
+			cand.push_back({sm, bs});
+		}
+	}
+	if (fixed_block && cand.empty()) cand.push_back({fixed_sync ? fixed_sync : 1, fixed_block});
+	if (cand.size() == 1) return set_config(h, cand[0].first, cand[0].second);
+	DevBuf<float4> save;
+	XCUDA(save.alloc(h->vert.n));
+	XCUDA(cudaMemcpyAsync(save.p, h->vert.p, h->vert.n * sizeof(float4), cudaMemcpyDeviceToDevice, h->stream));
+	cudaEvent_t e0, e1;
+	XCUDA(cudaEventCreate(&e0));
+	XCUDA(cudaEventCreate(&e1));
+	const uint32_t ns = std::max(1u, std::min(nsub, 20u));
+	float best = 1e30f;
+	std::pair<int, int> pick = cand[0];
+	for (auto& c : cand) {
+		if (set_config(h, c.first, c.second)) continue;
+		if (run(h, ns, dt)) continue;  // warm-up (and graph build)
+		cudaEventRecord(e0, h->stream);
+		int rc = XFEM_OK;
+		for (int r = 0; r < 3 && !rc; r++) rc = run(h, ns, dt);
+		cudaEventRecord(e1, h->stream);
+		if (cudaEventSynchronize(e1) != cudaSuccess || rc) continue;
+		float ms = 0;
+		cudaEventElapsedTime(&ms, e0, e1);
+		if (ms < best) {
+			best = ms;
+			pick = c;
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	XCUDA(cudaMemcpyAsync(h->vert.p, save.p, h->vert.n * sizeof(float4), cudaMemcpyDeviceToDevice, h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	int rc = check_device_error(h);
+	if (rc) return rc;
+	return set_config(h, pick.first, pick.second);
+}
+
+int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings, const xfem_options* options,
+                  xfem_body** out) {
+	if (!out) return fail(XFEM_EINVAL, "null output handle");
+	*out = nullptr;
+	if (nbodies == 0 || !meshes) return fail(XFEM_EINVAL, "no meshes");
+	std::unique_ptr<xfem_body> h(new (std::nothrow) xfem_body());
+	if (!h) return fail(XFEM_ENOMEM, "host allocation failed");
+	if (options) h->opt = *options;
+	if (h->opt.block_size && (h->opt.block_size < 64 || h->opt.block_size > 1024 || h->opt.block_size % 32))
+		return fail(XFEM_EINVAL, "block_size must be a multiple of 32 in [64, 1024]");
+	if (h->opt.sync_mode > 2) return fail(XFEM_EINVAL, "sync_mode must be 0, 1 or 2");
+	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
+	const uint32_t mode = h->opt.cluster_mode == 1 ? 0u : 1u;
+	const uint32_t morton = h->opt.no_morton ? 0u : 1u;
+	int ndev = 0;
+	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(XFEM_ECUDA, "no CUDA device");
+	h->device = h->opt.device > 0 ? h->opt.device : 0;
+	if (h->device >= ndev) return fail(XFEM_EINVAL, "device ordinal out of range");
+	XCUDA(cudaSetDevice(h->device));
+	if (h->opt.stream) {
+		h->stream = (cudaStream_t)h->opt.stream;
+	} else {
+		XCUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+		h->own_stream = true;
+	}
+	h->bodies.resize(nbodies);
+	for (uint32_t i = 0; i < nbodies; i++) {
+		const int rc = prepare_body(meshes[i], settings ? &settings[i] : nullptr, mode, morton, h->bodies[i]);
+		if (rc) return nbodies > 1 ? fail(rc, "body " + std::to_string(i) + ": " + g_err) : rc;
+	}
+	int rc = build_device(h.get());
+	if (rc) return rc;
+	// default configuration until the first step tunes it
+	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1, h->opt.block_size ? (int)h->opt.block_size : 256);
+	if (rc) return rc;
+	if (h->opt.sync_mode && h->opt.block_size) h->tuned = true;
+	*out = h.release();
+	return XFEM_OK;
+}
+
+BodyHost* body_of(xfem_body* h, uint32_t body) {
+	if (!h || body >= h->bodies.size()) {
+		fail(XFEM_EINVAL, "bad handle or body index");
+		return nullptr;
+	}
+	return &h->bodies[body];
+}
+
+int step(xfem_body* h, uint32_t nsub, float dt) {
+	if (!h) return fail(XFEM_EINVAL, "null handle");
+	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
+	if (nsub == 0) return XFEM_OK;
+	XCUDA(cudaSetDevice(h->device));
+	int rc = autotune(h, nsub, dt);
+	if (rc) return rc;
+	return run(h, nsub, dt);
+}
+
+// which: 0 positions, 1 velocities
+int get_xyz(xfem_body* h, uint32_t body, int which, float* out) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!out) return fail(XFEM_EINVAL, "null output");
+	XCUDA(cudaSetDevice(h->device));
+	const int e = launch_gather_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, h->stage.p, h->stream);
+	if (e) return fail(XFEM_ECUDA, "gather launch failed");
+	const size_t n = which >= 2 ? b->nv : 3 * (size_t)b->nv;
+	XCUDA(cudaMemcpyAsync(out, h->stage.p, n * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+	return check_device_error(h);
+}
+
+int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!in) return fail(XFEM_EINVAL, "null input");
+	XCUDA(cudaSetDevice(h->device));
+	XCUDA(cudaMemcpyAsync(h->stage.p, in, 3 * (size_t)b->nv * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+	const int e = launch_scatter_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, h->stage.p, h->stream);
+	if (e) return fail(XFEM_ECUDA, "scatter launch failed");
+	return check_device_error(h);
+}
+
+int upload_records(xfem_body* h) {
+	for (auto& b : h->bodies)
+		for (uint32_t t = 0; t < b.nt; t++) {
+			const uint32_t s = b.tet_slot[t];
+			h->trec_host[((size_t)(s / kLanes) * 4 + 3) * kLanes + s % kLanes].w = tet_c0(b, t);
+		}
+	XCUDA(cudaMemcpyAsync(h->trec.p, h->trec_host.data(), h->trec_host.size() * sizeof(float4), cudaMemcpyHostToDevice,
+	                      h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	return XFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xfem_settings_default(xfem_settings* s) {
+	if (!s) return fail(XFEM_EINVAL, "null settings");
+	memset(s, 0, sizeof(*s));
+	// struct Settings defaults, XPBDFEM/Settings.h:80-91
+	s->time_scale = 1.0f;
+	s->substeps_per_second = 1800.0f;
+	s->volume_passes = 0;
+	s->gravity[0] = 0.0f;
+	s->gravity[1] = -9.81f;
+	s->gravity[2] = 0.0f;
+	s->compliance = 0.01f;
+	s->damping = 0.0f;
+	s->pbd_damping = 0.0f;
+	s->drag = 0.0f;
+	s->poissons_ratio = 0.45f;
+	s->wonkiness = 0.0f;
+	s->left_right_separation = 1.0f;
+	// flags = 0 in the reference selects Energy_Pixar; this path's default is
+	// the Neo-Hookean MixedSel energy with the coupled solve.
+	s->flags = (XFEM_ENERGY_MIXED_SEL << XFEM_ENERGY_BIT) | (1u << XFEM_XPBD_SOLVE_BIT);
+	s->time_corrected_drag = 0.0f;
+	s->yeoh[0] = 0.1095f;
+	s->yeoh[1] = 14.95f;
+	s->yeoh[2] = 4.595f;
+	s->ground = 0;
+	s->ground_normal[2] = 1.0f;
+	s->ground_offset = 0.0f;
+	s->friction = 0.0f;
+	return XFEM_OK;
+}
+
+int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data, uint32_t idx_data_count,
+                float density, const xfem_settings* settings, xfem_body** out) {
+	return xfem_create_ex(node_data, node_data_count, idx_data, idx_data_count, density, settings, nullptr, out);
+}
+
+int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data, uint32_t idx_data_count,
+                   float density, const xfem_settings* settings, const xfem_options* options, xfem_body** out) {
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
+	return create_common(1, &m, settings, options, out);
+}
+
+int xfem_batch_create(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings,
+                      const xfem_options* options, xfem_body** out) {
+	return create_common(nbodies, meshes, settings, options, out);
+}
+
+int xfem_destroy(xfem_body* b) {
+	if (!b) return XFEM_OK;
+	cudaSetDevice(b->device);
+	if (b->stream) cudaStreamSynchronize(b->stream);
+	delete b;
+	return XFEM_OK;
+}
+
+int xfem_get_info(const xfem_body* b, xfem_info* out) {
+	if (!b || !out) return fail(XFEM_EINVAL, "null argument");
+	uint32_t ncl = 0;
+	for (auto& x : b->bodies) ncl += x.sched.nclusters;
+	*out = {(uint32_t)b->bodies.size(), b->nverts, b->ntets, ncl, b->ncolours, b->norphans,
+	        b->nchunks, b->nrows, (uint32_t)b->cfg.block, (uint32_t)b->cfg.blocks, (uint32_t)b->cfg.sync_mode,
+	        b->opt.cluster_mode == 1 ? 1u : 2u, b->device_bytes};
+	return XFEM_OK;
+}
+
+int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!s) return fail(XFEM_EINVAL, "null settings");
+	int rc = validate_settings(*s);
+	if (rc) return rc;
+	const bool material = s->compliance != b->settings.compliance;
+	b->settings = *s;
+	XCUDA(cudaSetDevice(h->device));
+	const BodyParams p = make_params(*s);
+	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	if (material && b->tet_mu.empty()) return upload_records(h);
+	return XFEM_OK;
+}
+
+int xfem_set_lock_mask(xfem_body* h, uint32_t body, const uint8_t* mask) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!mask) return fail(XFEM_EINVAL, "null mask");
+	XCUDA(cudaSetDevice(h->device));
+	std::vector<float4> vv(2 * (size_t)b->nv);
+	XCUDA(cudaMemcpyAsync(vv.data(), h->vert.p + 2 * (size_t)b->vbase, vv.size() * sizeof(float4), cudaMemcpyDeviceToHost,
+	                      h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	for (uint32_t v = 0; v < b->nv; v++) {
+		const uint32_t dv = b->sched.vert_rank[v];
+		uint32_t bits = __builtin_bit_cast(uint32_t, vv[2 * (size_t)dv + 1].w);
+		bits = mask[v] ? (bits | kFlagLocked) : (bits & ~kFlagLocked);
+		vv[2 * (size_t)dv + 1].w = __builtin_bit_cast(float, bits);
+	}
+	XCUDA(cudaMemcpyAsync(h->vert.p + 2 * (size_t)b->vbase, vv.data(), vv.size() * sizeof(float4), cudaMemcpyHostToDevice,
+	                      h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	return XFEM_OK;
+}
+
+int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (mu) {
+		for (uint32_t t = 0; t < b->nt; t++)
+			if (!(mu[t] > 0.0f) || !isfinite(mu[t])) return fail(XFEM_EINVAL, "tet mu must be finite and > 0");
+		b->tet_mu.assign(mu, mu + b->nt);
+	} else {
+		b->tet_mu.clear();
+	}
+	XCUDA(cudaSetDevice(h->device));
+	return upload_records(h);
+}
+
+int xfem_substep(xfem_body* b, float dt) { return step(b, 1, dt); }
+
+int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt) {
+	const uint64_t n = (uint64_t)frames * substeps;
+	if (n > 0xffffffffull) return fail(XFEM_EINVAL, "too many substeps in one call");
+	return step(b, (uint32_t)n, dt);
+}
+
+int xfem_synchronize(xfem_body* b) {
+	if (!b) return fail(XFEM_EINVAL, "null handle");
+	XCUDA(cudaSetDevice(b->device));
+	return check_device_error(b);
+}
+
+int xfem_get_positions(xfem_body* b, uint32_t body, float* out) { return get_xyz(b, body, 0, out); }
+int xfem_set_positions(xfem_body* b, uint32_t body, const float* in) { return set_xyz(b, body, 0, in); }
+int xfem_get_velocities(xfem_body* b, uint32_t body, float* out) { return get_xyz(b, body, 1, out); }
+int xfem_set_velocities(xfem_body* b, uint32_t body, const float* in) { return set_xyz(b, body, 1, in); }
+int xfem_get_inverse_masses(xfem_body* b, uint32_t body, float* out) { return get_xyz(b, body, 2, out); }
+
+int xfem_get_contacts(xfem_body* h, uint32_t body, uint8_t* out) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!out) return fail(XFEM_EINVAL, "null output");
+	std::vector<float> f(b->nv);
+	const int rc = get_xyz(h, body, 3, f.data());
+	if (rc) return rc;
+	for (uint32_t v = 0; v < b->nv; v++) out[v] = f[v] != 0.0f;
+	return XFEM_OK;
+}
+
+int xfem_get_lambdas(xfem_body* h, uint32_t body, float* out) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!out) return fail(XFEM_EINVAL, "null output");
+	if (!h->tlam.p) return fail(XFEM_EINVAL, "create the handle with keep_lambdas = 1");
+	XCUDA(cudaSetDevice(h->device));
+	std::vector<float2> all(h->tlam.n);
+	XCUDA(cudaMemcpyAsync(all.data(), h->tlam.p, all.size() * sizeof(float2), cudaMemcpyDeviceToHost, h->stream));
+	const int rc = check_device_error(h);
+	if (rc) return rc;
+	for (uint32_t t = 0; t < b->nt; t++) {
+		out[2 * (size_t)t] = all[b->tet_slot[t]].x;
+		out[2 * (size_t)t + 1] = all[b->tet_slot[t]].y;
+	}
+	return XFEM_OK;
+}
+
+int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!out) return fail(XFEM_EINVAL, "null output");
+	XCUDA(cudaSetDevice(h->device));
+	size_t tb = 0;
+	for (uint32_t i = 0; i < body; i++) tb += 4 * (size_t)h->bodies[i].nt;
+	const int e = launch_volume(h->vert.p, h->tets_dev.p + tb, b->nt, h->vol.p, h->stream);
+	if (e) return fail(XFEM_ECUDA, "volume launch failed");
+	XCUDA(cudaMemcpyAsync(out, h->vol.p, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+	return check_device_error(h);
+}
+
+int xfem_get_rest_state(const xfem_body* h, uint32_t body, float* out_ep17, float* out_w) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	return XFEM_OK;
+}
+
+int xfem_get_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, uint32_t* tet_order, uint32_t* colour_begin,
+                      uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	const Schedule& s = b.sched;
+	if (vert_rank) memcpy(vert_rank, s.vert_rank.data(), s.vert_rank.size() * 4);
+	if (ncolours) *ncolours = s.ncolours;
+	uint32_t o = 0;
+	for (uint32_t c = 0; c < s.ncolours; c++) {
+		if (colour_begin) colour_begin[c] = o;
+		for (uint32_t i = s.colour_cl_begin[c]; i < s.colour_cl_begin[c + 1]; i++) {
+			const uint32_t k = s.colour_cl[i];
+			for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++) {
+				if (tet_order) tet_order[o] = s.cl_tets[q];
+				o++;
+			}
+		}
+	}
+	if (colour_begin) colour_begin[s.ncolours] = o;
+	return XFEM_OK;
+}
+
+int xfem_body_counts(const xfem_body* h, uint32_t body, uint32_t* nverts, uint32_t* ntets) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	if (nverts) *nverts = h->bodies[body].nv;
+	if (ntets) *ntets = h->bodies[body].nt;
+	return XFEM_OK;
+}
+
+int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                            uint32_t idx_data_count, float density, float* out_ep17, float* out_w, uint8_t* out_flags) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
+	return XFEM_OK;
+}
+
+int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                          uint32_t idx_data_count, uint32_t cluster_mode, uint32_t no_morton, uint32_t* vert_rank,
+                          uint32_t* tet_order, uint32_t* colour_begin, uint32_t* ncolours, uint32_t* nclusters) {
+	if (cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
+	xfem_body tmp;
+	tmp.bodies.resize(1);
+	BodyHost& b = tmp.bodies[0];
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
+	int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, cluster_mode == 1 ? 0u : 1u, no_morton ? 0u : 1u, b.sched))
+		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
+	if (nclusters) *nclusters = b.sched.nclusters;
+	return xfem_get_schedule(&tmp, 0, vert_rank, tet_order, colour_begin, ncolours);
+}
+
+float xfem_time_corrected_drag(float drag, float substep_dt) {
+	return 1.0f - powf(1.0f - drag, 1000.0f * substep_dt);
+}
+
+int xfem_generate_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                            float wonkiness, float* nodes, uint32_t* idx) {
+	if (!nodes || !idx) return fail(XFEM_EINVAL, "null output");
+	gen_tet_block(W, H, D, sx, sy, sz, pattern, wonkiness, nodes, idx);
+	return XFEM_OK;
+}
+
+void* xfem_alloc_host(size_t bytes) {
+	void* p = nullptr;
+	if (cudaMallocHost(&p, bytes) != cudaSuccess) return nullptr;
+	return p;
+}
+
+void xfem_free_host(void* p) {
+	if (p) cudaFreeHost(p);
+}
+
+const char* xfem_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,129 @@
+// Internal declarations shared by the host code (xfem_host.cpp, xfem_api.cpp)
+// and the CUDA kernels (xfem_kernels.cu) of libxfem.so.
+#pragma once
+
+#include <stdint.h>
+#include <vector_types.h>
+
+#include <vector>
+
+namespace xfem {
+
+// Limits of one cluster: the tets processed in sequence by one GPU thread.
+// An edge star of a 6-tet cube split has 6 tets on 8 vertices.
+constexpr uint32_t kMaxClusterVerts = 8;
+constexpr uint32_t kMaxClusterTets = 8;
+constexpr uint32_t kMaxColours = 4096;
+constexpr uint32_t kLanes = 32;  // clusters per chunk (one warp)
+
+// ---- host-side mesh and schedule ------------------------------------------
+// Parses the tagged index stream (4 = tet). Returns 0, -1 on a non-tet tag or a
+// truncated record.
+int parse_tets(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& tets, uint32_t& nverts);
+
+// Rest state of every tet and the inverse masses, bit for bit what
+// GeoLinear3d::Init computes (XPBDFEM/Geo.cpp:697-745, XPBDFEM/Fem.cpp:131-224).
+// ep: 17 floats per tet (Qi column-major, QQ, QR, volume, surfaceArea).
+// vflags: bit 0 Left, bit 1 Right (XPBDFEM/Geo.cpp:724-725), bit 4 Pickable.
+void init_rest(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, float density,
+               float* ep, float* w, uint8_t* vflags);
+
+// GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244).
+void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                   float wonkiness, float* nodes, uint32_t* idx);
+
+struct Schedule {
+	uint32_t nclusters = 0, ncolours = 0;
+	std::vector<uint32_t> cl_begin;      // nclusters + 1, into cl_tets
+	std::vector<uint32_t> cl_tets;       // member tets in sequence
+	std::vector<uint32_t> cl_colour;     // nclusters
+	std::vector<uint32_t> vert_rank;     // device rank of each vertex
+	std::vector<uint32_t> colour_cl;     // clusters in device order, colour-major
+	std::vector<uint32_t> colour_cl_begin;  // ncolours + 1
+};
+
+// Clusters (mode 0: one tet each; mode 1: edge stars), greedy colouring,
+// Morton vertex order (morton != 0) and cluster order inside each colour.
+// Returns 0 or -1 when a limit is exceeded.
+int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
+                   uint32_t morton, Schedule& s);
+
+// ---- device-side structures ------------------------------------------------
+// Material and step parameters of one body (uploaded on create / set_settings).
+struct BodyParams {
+	float mu, inv_mu, inv_lambda, a;  // mu = 1/compliance; inv_* = 1/mu, 1/lambda; a = 1 + mu/lambda
+	float yeoh[3];
+	uint32_t energy;        // 4 = Neo-Hookean (MixedSel), 7 = Yeoh (YeohSkinFast)
+	float gravity[3];
+	float drag_mul;         // 1 - time_corrected_drag
+	uint32_t simultaneous;  // 1 = coupled 2x2 solve
+	uint32_t lock_active;   // 1 = apply per-vertex lock bits
+	uint32_t ground;        // 1 = ground plane
+	float friction;
+	float ground_n[3];
+	float ground_d;
+	float ratio;   // mu / lambda (0 when incompressible)
+	uint32_t pad;
+};
+
+// Per-chunk metadata: 32 clusters of one colour side by side (lane = cluster).
+struct ChunkMeta {
+	uint32_t trow;  // first tet row (rows hold one tet per lane)
+	uint32_t ntmax; // rows used by this chunk
+	uint32_t vrow;  // first vertex-slot row
+	uint32_t nvmax; // vertex slots used by this chunk
+};
+
+// Everything a kernel needs, passed by value.
+struct DevCtx {
+	float4* vert;               // 2 per vertex: (O.xyz, w), (D.xyz, flag bits)
+	const uint32_t* chdr;       // per cluster lane: nv | nt << 4 | body << 8
+	const uint32_t* cvid;       // [vrow][lane] vertex ids
+	const uint32_t* cslot;      // [trow][lane] 4 x 4-bit local slots
+	const float4* trec;         // [trow][4][lane] Qi, QQ, QR, c0 = (1/mu)/volume
+	float2* tlam;               // [trow][lane] multipliers or null
+	const ChunkMeta* chunks;
+	const uint32_t* colour_chunk_begin;  // ncolours + 1
+	const uint32_t* orphans;    // vertices outside every colour-0 cluster
+	const BodyParams* bodies;
+	uint32_t nverts, norphans, ncolours;
+	uint32_t* bar_count;        // grid barrier arrival counter
+	int* err;                   // device error word (0 = ok)
+};
+
+// Vertex flag bits kept in the .w word of the second float4.
+constexpr uint32_t kFlagLocked = 1u;
+constexpr uint32_t kFlagContact = 2u;
+
+// Device error codes written to DevCtx::err.
+constexpr int kErrBarrierTimeout = 1;
+
+// ---- kernel launchers (xfem_kernels.cu) ---------------------------------------
+struct LaunchCfg {
+	int block = 256;
+	int blocks = 0;        // persistent grid size
+	int sync_mode = 1;     // 1 persistent, 2 graph-style per-colour launches
+	bool lambdas = false;
+	uint32_t total_chunks = 0;
+	std::vector<uint32_t> colour_chunk_begin_host;
+};
+
+// Runs nsub substeps (canonical (X, V) in, canonical out) on `stream`.
+// Returns a cudaError_t value (0 = success).
+int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, float dt, void* stream);
+// Sets the dynamic shared-memory limit of the solve kernels for cfg.block
+// (call before launching or capturing).
+int configure_kernels(const LaunchCfg& cfg);
+// Largest co-resident grid for the persistent kernel at this block size.
+int persistent_grid(const LaunchCfg& cfg, int* blocks_out);
+// Dynamic shared memory bytes per block of the solve kernels.
+size_t solve_smem_bytes(int block);
+
+// Transfer helpers (caller order <-> device order), run on `stream`.
+int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, float* out,
+                      void* stream);
+int launch_scatter_xyz(float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, const float* in,
+                       void* stream);
+int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, double* out, void* stream);
+
+}  // namespace xfem

@@ -1,0 +1,582 @@
+// CUDA kernels of libxfem.so (sm_103a): the coloured Gauss-Seidel XPBD substep.
+//
+// Data layout in HBM (all device-order, see xfem_internal.h):
+//   vert[2v]   = (O.x, O.y, O.z, w)   position at the start of the substep and
+//                                     inverse mass; between calls: X
+//   vert[2v+1] = (D.x, D.y, D.z, bits) displacement within the substep; between
+//                                     calls: V. bits = lock | contact | body<<8
+// One 32-byte sector per vertex, so a gather touches one sector.
+//
+// Work unit: a cluster = up to 8 tets sharing vertices, solved in sequence by
+// one thread with its (<= 8) vertices staged in shared memory. Clusters of one
+// colour share no vertex, so there is no atomic and no race. 32 clusters of a
+// colour form a chunk (one warp); chunk data is stored lane-minor so every
+// per-lane load of a warp is one contiguous 128- or 512-byte run.
+//
+// Substep schedule (Geo3d::Substep, XPBDFEM/Geo.cpp:305-356, restated):
+//   colour 0 : for each vertex of a colour-0 cluster (and every orphan vertex)
+//              finalize the previous substep (locks, ground, V = D/dt,
+//              O += D) and predict this one (V += g dt, V *= 1 - drag,
+//              D = V dt); then solve the cluster
+//   colour c : solve
+//   end      : finalize the last substep back to (X, V)
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xfem_internal.h"
+
+namespace xfem {
+
+namespace {
+
+constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;  // 2 s: far above any legal wait
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+	uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Grid-wide barrier for the co-resident persistent grid. Monotonic arrival
+// counter (zeroed before each launch); every wait is bounded: on timeout the
+// block records kErrBarrierTimeout and all blocks leave at their next barrier.
+__device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
+	__shared__ int s_ok;
+	__syncthreads();
+	target += gridDim.x;
+	if (threadIdx.x == 0) {
+		int ok = 1;
+		__threadfence();
+		atomicAdd(C.bar_count, 1u);
+		uint32_t spins = 0;
+		uint64_t t0 = 0;
+		while (ld_acquire_gpu(C.bar_count) < target) {
+			if (++spins == 256) {
+				spins = 0;
+				if (*(volatile int*)C.err) {
+					ok = 0;
+					break;
+				}
+				const uint64_t t = global_ns();
+				if (t0 == 0) {
+					t0 = t;
+				} else if (t - t0 > kBarrierTimeoutNs) {
+					atomicCAS(C.err, 0, kErrBarrierTimeout);
+					ok = 0;
+					break;
+				}
+			}
+		}
+		s_ok = ok;
+	}
+	__syncthreads();
+	return s_ok != 0;
+}
+
+struct Vec3 {
+	float x, y, z;
+};
+
+__device__ __forceinline__ Vec3 v3(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ float dot(Vec3 a, Vec3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+
+// Ground plane with Coulomb friction on the substep displacement D
+// (extension; no reference counterpart). Returns true on contact.
+__device__ __forceinline__ bool ground_contact(const BodyParams& bp, const float4& O, float4& D) {
+	const float nx = bp.ground_n[0], ny = bp.ground_n[1], nz = bp.ground_n[2];
+	const float h = (nx * O.x + ny * O.y + nz * O.z) - bp.ground_d;
+	const float depth = -(h + (nx * D.x + ny * D.y + nz * D.z));
+	if (!(depth > 0.0f)) return false;
+	D.x += depth * nx;
+	D.y += depth * ny;
+	D.z += depth * nz;
+	const float dn = nx * D.x + ny * D.y + nz * D.z;
+	const float tx = D.x - dn * nx, ty = D.y - dn * ny, tz = D.z - dn * nz;
+	const float lt = sqrtf(tx * tx + ty * ty + tz * tz);
+	const float lim = bp.friction * depth;
+	const float s = lt <= lim ? 1.0f : lim / lt;
+	D.x -= s * tx;
+	D.y -= s * ty;
+	D.z -= s * tz;
+	return true;
+}
+
+// End of a substep for one vertex: locks (XPBDFEM/Geo.cpp:318-322), ground,
+// then the velocity V = D / dt (XPBDFEM/Geo.cpp:342-344) is returned.
+__device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, float4& D, uint32_t& bits, float inv_dt) {
+	if (bp.lock_active && (bits & kFlagLocked)) {
+		D.x = D.y = D.z = 0.0f;
+		O.w = 0.0f;
+	}
+	bits &= ~kFlagContact;
+	if (bp.ground && O.w > 0.0f && ground_contact(bp, O, D)) bits |= kFlagContact;
+	return {D.x * inv_dt, D.y * inv_dt, D.z * inv_dt};
+}
+
+// Finalize the previous substep (unless `first`: (O, D) then hold the
+// canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312).
+__device__ __forceinline__ void advance_vertex(const BodyParams* bodies, float4& O, float4& D, bool first, float dt,
+                                               float inv_dt) {
+	uint32_t bits = __float_as_uint(D.w);
+	const BodyParams& bp = bodies[bits >> 8];
+	Vec3 V;
+	if (first) {
+		V = v3(D);
+	} else {
+		V = finish_vertex(bp, O, D, bits, inv_dt);
+		O.x += D.x;
+		O.y += D.y;
+		O.z += D.z;
+	}
+	V.x = (V.x + bp.gravity[0] * dt) * bp.drag_mul;
+	V.y = (V.y + bp.gravity[1] * dt) * bp.drag_mul;
+	V.z = (V.z + bp.gravity[2] * dt) * bp.drag_mul;
+	D = make_float4(V.x * dt, V.y * dt, V.z * dt, __uint_as_float(bits));
+}
+
+// Finalize the last substep of a launch: (O, D) -> canonical (X, V).
+__device__ __forceinline__ void finalize_vertex(const BodyParams* bodies, float4& O, float4& D, float inv_dt) {
+	uint32_t bits = __float_as_uint(D.w);
+	const BodyParams& bp = bodies[bits >> 8];
+	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt);
+	O.x += D.x;
+	O.y += D.y;
+	O.z += D.z;
+	D = make_float4(V.x, V.y, V.z, __uint_as_float(bits));
+}
+
+// Rest state of one tet: Qi column-major q[c][r], QQ, QR and c0 = (1/mu)/vol.
+struct TetRec {
+	float4 a, b, c, d;
+};
+
+__device__ __forceinline__ TetRec load_rec(const float4* __restrict__ trec, uint32_t row, uint32_t lane) {
+	const float4* p = trec + (size_t)row * 4 * kLanes + lane;
+	TetRec r;
+	r.a = __ldg(p);
+	r.b = __ldg(p + kLanes);
+	r.c = __ldg(p + 2 * kLanes);
+	r.d = __ldg(p + 3 * kLanes);
+	return r;
+}
+
+// Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with
+// adjugate :284-300, F :311-323, gradient :338-354). Returns U1 = (J - a)^2
+// and the gradient of the three free nodes (g[3] = -sum).
+__device__ __forceinline__ float hydrostatic(const float q[3][3], const Vec3 P[3], float a, Vec3 g[4]) {
+	// F[j][r] = sum_n Qi[n][r] * P_n[j]  (F = Qi * Ds, Ds rows = P_n)
+	float F[3][3];
+	const float Pc[3][3] = {{P[0].x, P[1].x, P[2].x}, {P[0].y, P[1].y, P[2].y}, {P[0].z, P[1].z, P[2].z}};
+#pragma unroll
+	for (int j = 0; j < 3; j++)
+#pragma unroll
+		for (int r = 0; r < 3; r++) F[j][r] = fmaf(q[0][r], Pc[j][0], fmaf(q[1][r], Pc[j][1], q[2][r] * Pc[j][2]));
+	float adj[3][3];
+	adj[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+	adj[0][1] = -(F[0][1] * F[2][2] - F[0][2] * F[2][1]);
+	adj[0][2] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+	adj[1][0] = -(F[1][0] * F[2][2] - F[1][2] * F[2][0]);
+	adj[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+	adj[1][2] = -(F[0][0] * F[1][2] - F[0][2] * F[1][0]);
+	adj[2][0] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+	adj[2][1] = -(F[0][0] * F[2][1] - F[0][1] * F[2][0]);
+	adj[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+	const float J = fmaf(F[0][0], adj[0][0], fmaf(F[0][1], adj[1][0], F[0][2] * adj[2][0]));
+	const float Ja = J - a;
+	const float s = 2.0f * Ja;
+	// g_n = column n of (s adj) * Qi: g_n[r] = s * sum_k adj[k][r] Qi[n][k]
+#pragma unroll
+	for (int n = 0; n < 3; n++) {
+		const float gx = fmaf(adj[0][0], q[n][0], fmaf(adj[1][0], q[n][1], adj[2][0] * q[n][2]));
+		const float gy = fmaf(adj[0][1], q[n][0], fmaf(adj[1][1], q[n][1], adj[2][1] * q[n][2]));
+		const float gz = fmaf(adj[0][2], q[n][0], fmaf(adj[1][2], q[n][1], adj[2][2] * q[n][2]));
+		g[n] = {s * gx, s * gy, s * gz};
+	}
+	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
+	return Ja * Ja;
+}
+
+// Deviatoric term, prefactored (XPBDFEM/Fem.cpp:163-192), with the Yeoh
+// transform of XPBDFEM/Fem.cpp:525-531 when energy == 7.
+__device__ __forceinline__ float deviatoric(const BodyParams& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
+                                            Vec3 g[4]) {
+	float U = QQ[0] * dot(P[0], P[0]);
+	U = fmaf(QQ[1], dot(P[1], P[1]), U);
+	U = fmaf(QQ[2], dot(P[2], P[2]), U);
+	U = fmaf(QR[0], dot(P[0], P[1]), U);
+	U = fmaf(QR[1], dot(P[0], P[2]), U);
+	U = fmaf(QR[2], dot(P[1], P[2]), U);
+	const float d0 = 2.0f * QQ[0], d1 = 2.0f * QQ[1], d2 = 2.0f * QQ[2];
+	g[0] = {fmaf(d0, P[0].x, fmaf(QR[0], P[1].x, QR[1] * P[2].x)), fmaf(d0, P[0].y, fmaf(QR[0], P[1].y, QR[1] * P[2].y)),
+	        fmaf(d0, P[0].z, fmaf(QR[0], P[1].z, QR[1] * P[2].z))};
+	g[1] = {fmaf(d1, P[1].x, fmaf(QR[0], P[0].x, QR[2] * P[2].x)), fmaf(d1, P[1].y, fmaf(QR[0], P[0].y, QR[2] * P[2].y)),
+	        fmaf(d1, P[1].z, fmaf(QR[0], P[0].z, QR[2] * P[2].z))};
+	g[2] = {fmaf(d2, P[2].x, fmaf(QR[1], P[0].x, QR[2] * P[1].x)), fmaf(d2, P[2].y, fmaf(QR[1], P[0].y, QR[2] * P[1].y)),
+	        fmaf(d2, P[2].z, fmaf(QR[1], P[0].z, QR[2] * P[1].z))};
+	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
+	if (bp.energy == 7u) {
+		const float IM = U - 3.0f;
+		const float C0 = bp.yeoh[0], C1 = bp.yeoh[1], C2 = bp.yeoh[2];
+		U = fmaxf(0.0001f, IM * fmaf(IM, fmaf(IM, C2, C1), C0));
+		const float gs = fmaf(IM, fmaf(IM, 3.0f * C2, 2.0f * C1), C0);
+#pragma unroll
+		for (int n = 0; n < 4; n++) g[n] = {g[n].x * gs, g[n].y * gs, g[n].z * gs};
+	}
+	return U;
+}
+
+__device__ __forceinline__ float wdot(const float w[4], const Vec3 a[4], const Vec3 b[4]) {
+	float s = 1.0e-22f;
+#pragma unroll
+	for (int n = 0; n < 4; n++) s = fmaf(w[n], dot(a[n], b[n]), s);
+	return s;
+}
+
+// One element solve: SolveElementMixed<MixedSelective | YeohSkinFast> tet path
+// (XPBDFEM/Fem.cpp:437-564) with EnergyXpbdConstrainSimultaneous<2>
+// (XPBDFEM/Xpbd.h:123-215) or the serial EnergyXpbdConstrain pair
+// (XPBDFEM/Xpbd.h:87-121). O[]: start positions + w, D[]: displacements
+// (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
+// alpha1 = alpha0 * (mu / lambda), i.e. (1/lambda)/volume/dt^2.
+__device__ __forceinline__ float2 solve_tet(const BodyParams& bp, const TetRec& r, float inv_dt2, const float4 O[4],
+                                            float4 D[4]) {
+	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
+	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
+	const float QR[3] = {r.d.x, r.d.y, r.d.z};
+	const float alpha0 = r.d.w * inv_dt2;
+	const float alpha1 = alpha0 * bp.ratio;
+	const float w[4] = {O[0].w, O[1].w, O[2].w, O[3].w};
+	Vec3 P[3];
+#pragma unroll
+	for (int i = 0; i < 3; i++)
+		P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+		        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+	Vec3 g0[4], g1[4];
+	const float U0 = deviatoric(bp, QQ, QR, P, g0);
+	float l0, l1;
+	if (bp.simultaneous) {
+		const float U1 = hydrostatic(q, P, bp.a, g1);
+		const float A0 = fmaf(2.0f * U0, alpha0, wdot(w, g0, g0));
+		const float A1 = wdot(w, g1, g0);
+		const float A2 = fmaf(2.0f * U1, alpha1, wdot(w, g1, g1));
+		const float b0 = -2.0f * U0, b1 = -2.0f * U1;
+		// Cramer's rule as in XPBDFEM/Xpbd.h:172-180
+		const float i00 = __frcp_rn(A0), i11 = __frcp_rn(A2);
+		const float r0 = A1 * i00, r1 = A1 * i11;
+		const float inv_det = __frcp_rn(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
+		const float c0 = b0 * i00, c1 = b1 * i11;
+		l0 = inv_det * fmaf(-r0, c1, c0);
+		l1 = inv_det * fmaf(-c0, r1, c1);
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			D[n].x = fmaf(w[n], fmaf(l1, g1[n].x, l0 * g0[n].x), D[n].x);
+			D[n].y = fmaf(w[n], fmaf(l1, g1[n].y, l0 * g0[n].y), D[n].y);
+			D[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), D[n].z);
+		}
+	} else {
+		l0 = (-2.0f * U0) * __frcp_rn(fmaf(2.0f * U0, alpha0, wdot(w, g0, g0)));
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l0;
+			D[n].x = fmaf(s, g0[n].x, D[n].x);
+			D[n].y = fmaf(s, g0[n].y, D[n].y);
+			D[n].z = fmaf(s, g0[n].z, D[n].z);
+		}
+#pragma unroll
+		for (int i = 0; i < 3; i++)
+			P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+			        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+		const float U1 = hydrostatic(q, P, bp.a, g1);
+		l1 = (-2.0f * U1) * __frcp_rn(fmaf(2.0f * U1, alpha1, wdot(w, g1, g1)));
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l1;
+			D[n].x = fmaf(s, g1[n].x, D[n].x);
+			D[n].y = fmaf(s, g1[n].y, D[n].y);
+			D[n].z = fmaf(s, g1[n].z, D[n].z);
+		}
+	}
+	return make_float2(l0, l1);
+}
+
+enum Phase : int { kPhaseSolve = 0, kPhasePredict = 1, kPhaseAdvance = 2 };
+
+// One lane = one cluster of one chunk.
+template <bool LAMBDAS>
+__device__ __forceinline__ void run_cluster(const DevCtx& C, uint32_t chunk, uint32_t lane, int phase, float dt,
+                                            float inv_dt, float inv_dt2, float4* sO, float4* sD, uint32_t stride) {
+	const uint4 meta = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	const ChunkMeta m = {meta.x, meta.y, meta.z, meta.w};
+	const uint32_t hdr = __ldg(C.chdr + (size_t)chunk * kLanes + lane);
+	const uint32_t nv = hdr & 15u, nt = (hdr >> 4) & 15u;
+	if (nv == 0) return;
+	const BodyParams& bp = C.bodies[hdr >> 8];
+	uint32_t vid[kMaxClusterVerts];
+#pragma unroll
+	for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
+		if (s < nv) {
+			vid[s] = __ldg(C.cvid + (size_t)(m.vrow + s) * kLanes + lane);
+			float4 O = __ldcg(C.vert + 2 * (size_t)vid[s]);
+			float4 D = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
+			if (phase != kPhaseSolve) advance_vertex(C.bodies, O, D, phase == kPhasePredict, dt, inv_dt);
+			sO[s * stride] = O;
+			sD[s * stride] = D;
+		}
+	}
+	TetRec rec = load_rec(C.trec, m.trow, lane);
+	uint32_t sl = __ldg(C.cslot + (size_t)m.trow * kLanes + lane);
+	for (uint32_t t = 0; t < nt; t++) {
+		TetRec nrec;
+		uint32_t nsl = 0;
+		if (t + 1 < nt) {
+			nrec = load_rec(C.trec, m.trow + t + 1, lane);
+			nsl = __ldg(C.cslot + (size_t)(m.trow + t + 1) * kLanes + lane);
+		}
+		const uint32_t s0 = sl & 15u, s1 = (sl >> 4) & 15u, s2 = (sl >> 8) & 15u, s3 = (sl >> 12) & 15u;
+		const float4 O[4] = {sO[s0 * stride], sO[s1 * stride], sO[s2 * stride], sO[s3 * stride]};
+		float4 D[4] = {sD[s0 * stride], sD[s1 * stride], sD[s2 * stride], sD[s3 * stride]};
+		const float2 lam = solve_tet(bp, rec, inv_dt2, O, D);
+		sD[s0 * stride] = D[0];
+		sD[s1 * stride] = D[1];
+		sD[s2 * stride] = D[2];
+		sD[s3 * stride] = D[3];
+		if (LAMBDAS) C.tlam[(size_t)(m.trow + t) * kLanes + lane] = lam;
+		rec = nrec;
+		sl = nsl;
+	}
+#pragma unroll
+	for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
+		if (s < nv) {
+			if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * stride]);
+			__stcg(C.vert + 2 * (size_t)vid[s] + 1, sD[s * stride]);
+		}
+	}
+}
+
+__device__ __forceinline__ void run_orphans(const DevCtx& C, uint32_t begin, uint32_t step, bool first, float dt,
+                                            float inv_dt) {
+	for (uint32_t i = begin; i < C.norphans; i += step) {
+		const uint32_t v = __ldg(C.orphans + i);
+		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
+		advance_vertex(C.bodies, O, D, first, dt, inv_dt);
+		__stcg(C.vert + 2 * (size_t)v, O);
+		__stcg(C.vert + 2 * (size_t)v + 1, D);
+	}
+}
+
+__device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, uint32_t step, float inv_dt) {
+	for (uint32_t v = begin; v < C.nverts; v += step) {
+		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
+		finalize_vertex(C.bodies, O, D, inv_dt);
+		__stcg(C.vert + 2 * (size_t)v, O);
+		__stcg(C.vert + 2 * (size_t)v + 1, D);
+	}
+}
+
+// Persistent kernel: nsub substeps x ncolours colour passes separated by the
+// bounded grid barrier. Must be launched cooperatively (co-resident grid).
+template <bool LAMBDAS>
+__global__ void __launch_bounds__(512) k_persistent(DevCtx C, uint32_t nsub, float dt) {
+	extern __shared__ float4 smem[];
+	const uint32_t stride = blockDim.x;
+	float4* sO = smem + threadIdx.x;
+	float4* sD = smem + kMaxClusterVerts * stride + threadIdx.x;
+	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+	// chunk i of a colour goes to block i % grid, so chunks spread over all SMs
+	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
+	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	uint32_t target = 0;
+	for (uint32_t s = 0; s < nsub; s++) {
+		for (uint32_t c = 0; c < C.ncolours; c++) {
+			const int phase = c == 0 ? (s == 0 ? kPhasePredict : kPhaseAdvance) : kPhaseSolve;
+			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
+			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps)
+				run_cluster<LAMBDAS>(C, ch, lane, phase, dt, inv_dt, inv_dt2, sO, sD, stride);
+			if (c == 0) run_orphans(C, gtid, nthreads, s == 0, dt, inv_dt);
+			if (!grid_sync(C, target)) return;
+		}
+	}
+	run_finalize(C, gtid, nthreads, inv_dt);
+}
+
+// One colour pass as its own launch (CUDA-graph mode). Blocks past the
+// colour's chunks advance orphan vertices when `phase` is not kPhaseSolve.
+template <bool LAMBDAS>
+__global__ void __launch_bounds__(512) k_colour(DevCtx C, uint32_t colour, int phase, float dt,
+                                                 uint32_t solve_blocks) {
+	extern __shared__ float4 smem[];
+	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
+	if (blockIdx.x >= solve_blocks) {
+		const uint32_t b = blockIdx.x - solve_blocks, nb = gridDim.x - solve_blocks;
+		run_orphans(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, phase == kPhasePredict, dt, inv_dt);
+		return;
+	}
+	const uint32_t stride = blockDim.x;
+	const uint32_t ch = __ldg(C.colour_chunk_begin + colour) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
+	run_cluster<LAMBDAS>(C, ch, threadIdx.x & 31u, phase, dt, inv_dt, inv_dt2, smem + threadIdx.x,
+	                     smem + kMaxClusterVerts * stride + threadIdx.x, stride);
+}
+
+__global__ void k_finalize(DevCtx C, float dt) {
+	run_finalize(C, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, 1.0f / dt);
+}
+
+// ---- transfers ----------------------------------------------------------------
+__global__ void k_gather_xyz(const float4* __restrict__ vert, int which, const uint32_t* __restrict__ dev_of,
+                             uint32_t n, float* __restrict__ out) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float4 a = vert[2 * (size_t)dev_of[i] + (which & 1)];
+	const float wv = a.w;
+	if (which == 2) {  // inverse mass
+		out[i] = wv;
+		return;
+	}
+	if (which == 3) {  // contact bit
+		out[i] = (__float_as_uint(wv) & kFlagContact) ? 1.0f : 0.0f;
+		return;
+	}
+	out[3 * (size_t)i] = a.x;
+	out[3 * (size_t)i + 1] = a.y;
+	out[3 * (size_t)i + 2] = a.z;
+}
+
+__global__ void k_scatter_xyz(float4* __restrict__ vert, int which, const uint32_t* __restrict__ dev_of, uint32_t n,
+                              const float* __restrict__ in) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	float4* p = vert + 2 * (size_t)dev_of[i] + which;
+	float4 a = *p;
+	a.x = in[3 * (size_t)i];
+	a.y = in[3 * (size_t)i + 1];
+	a.z = in[3 * (size_t)i + 2];
+	*p = a;
+}
+
+// CalculateElementVolume for T4 (XPBDFEM/Fem.cpp:1066) summed in double.
+__global__ void k_volume(const float4* __restrict__ vert, const uint32_t* __restrict__ tets, uint32_t nt,
+                         double* __restrict__ out) {
+	__shared__ double red[32];
+	double acc = 0.0;
+	for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+		const float4 x0 = vert[2 * (size_t)tets[4 * (size_t)t]], x1 = vert[2 * (size_t)tets[4 * (size_t)t + 1]];
+		const float4 x2 = vert[2 * (size_t)tets[4 * (size_t)t + 2]], x3 = vert[2 * (size_t)tets[4 * (size_t)t + 3]];
+		const double a = (double)x0.x - x3.x, b = (double)x1.x - x3.x, c = (double)x2.x - x3.x;
+		const double d = (double)x0.y - x3.y, e = (double)x1.y - x3.y, f = (double)x2.y - x3.y;
+		const double g = (double)x0.z - x3.z, h = (double)x1.z - x3.z, i = (double)x2.z - x3.z;
+		acc += (a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g)) / 6.0;
+	}
+	for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+	if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		acc = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+		for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+		if (threadIdx.x == 0) atomicAdd(out, acc);
+	}
+}
+
+}  // namespace
+
+size_t solve_smem_bytes(int block) { return (size_t)2 * kMaxClusterVerts * sizeof(float4) * (size_t)block; }
+
+static void set_smem_attr(const void* f, size_t bytes) {
+	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+int configure_kernels(const LaunchCfg& cfg) {
+	const size_t smem = solve_smem_bytes(cfg.block);
+	set_smem_attr(cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>, smem);
+	set_smem_attr(cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>, smem);
+	return (int)cudaGetLastError();
+}
+
+int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
+	const void* f = cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+	const size_t smem = solve_smem_bytes(cfg.block);
+	int dev = 0, sms = 0, per_sm = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, cfg.block, smem);
+	if (e != cudaSuccess) return (int)e;
+	*blocks_out = per_sm * sms;
+	return per_sm > 0 ? 0 : (int)cudaErrorInvalidConfiguration;
+}
+
+int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, float dt, void* stream) {
+	cudaStream_t st = (cudaStream_t)stream;
+	const size_t smem = solve_smem_bytes(cfg.block);
+	cudaError_t e = cudaSuccess;
+	if (nsub == 0) return 0;
+	if (cfg.sync_mode == 1) {
+		e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+		if (e != cudaSuccess) return (int)e;
+		DevCtx c = ctx;
+		void* args[] = {&c, &nsub, &dt};
+		const void* f = cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+		e = cudaLaunchCooperativeKernel(f, dim3(cfg.blocks), dim3(cfg.block), args, smem, st);
+		return (int)e;
+	}
+	// per-colour launches (captured into a CUDA graph by the caller when wanted)
+	const void* fc = cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>;
+	const uint32_t warps_per_block = cfg.block / 32;
+	for (uint32_t s = 0; s < nsub; s++) {
+		for (uint32_t c = 0; c < ctx.ncolours; c++) {
+			const uint32_t nch = cfg.colour_chunk_begin_host[c + 1] - cfg.colour_chunk_begin_host[c];
+			const uint32_t solve_blocks = (nch + warps_per_block - 1) / warps_per_block;
+			const int phase = c == 0 ? (s == 0 ? kPhasePredict : kPhaseAdvance) : kPhaseSolve;
+			uint32_t extra = 0;
+			if (c == 0 && ctx.norphans) extra = (ctx.norphans + cfg.block - 1) / cfg.block;
+			const uint32_t grid = solve_blocks + extra;
+			if (grid == 0) continue;
+			DevCtx cc = ctx;
+			uint32_t colour = c, sb = solve_blocks;
+			int ph = phase;
+			float dtv = dt;
+			void* args[] = {&cc, &colour, &ph, &dtv, &sb};
+			e = cudaLaunchKernel(fc, dim3(grid), dim3(cfg.block), args, smem, st);
+			if (e != cudaSuccess) return (int)e;
+		}
+	}
+	const uint32_t fb = (ctx.nverts + 255) / 256;
+	if (fb) {
+		k_finalize<<<fb, 256, 0, st>>>(ctx, dt);
+		e = cudaGetLastError();
+	}
+	return (int)e;
+}
+
+int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, float* out,
+                      void* stream) {
+	if (!n) return 0;
+	k_gather_xyz<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(vert, which, dev_of_caller, n, out);
+	return (int)cudaGetLastError();
+}
+
+int launch_scatter_xyz(float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, const float* in,
+                       void* stream) {
+	if (!n) return 0;
+	k_scatter_xyz<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(vert, which, dev_of_caller, n, in);
+	return (int)cudaGetLastError();
+}
+
+int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, double* out, void* stream) {
+	cudaStream_t st = (cudaStream_t)stream;
+	cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), st);
+	if (e != cudaSuccess || !nt) return (int)e;
+	uint32_t grid = (nt + 255) / 256;
+	grid = grid > 1024 ? 1024 : grid;
+	k_volume<<<grid, 256, 0, st>>>(vert, tets_dev, nt, out);
+	return (int)cudaGetLastError();
+}
+
+}  // namespace xfem

@@ -1,0 +1,315 @@
+"""Python mirror of the reference's body interface over libxfem.so's C ABI.
+
+`Body` plays the role of the reference's GeoLinear3d (XPBDFEM/Geo.h:137-153):
+construct it from the tagged index stream and node array exactly as
+GeoLinear3d::Init is called (XPBDFEM/Geo.cpp:697), then call `substep(dt)`
+(Geo3d::Substep, XPBDFEM/Geo.cpp:305) or `step_frames(...)` (the substep loop
+of Sim::Update, XPBDFEM/Demo.cpp:67-90). `Settings` mirrors struct Settings
+(XPBDFEM/Settings.h:79-102). All compute runs in libxfem.so on the GPU; there
+is no CPU fallback: without the library or a CUDA device every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libxfem.so")
+
+OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT = 0, -1, -2, -3, -4, -5, -6
+ENERGY_BIT = 6
+ENERGY_MIXED_SEL = 4
+ENERGY_YEOH_SKIN_FAST = 7
+XPBD_SOLVE_BIT = 11
+LOCK_LEFT = 1 << 26
+REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
+
+
+class XfemError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"xfem error {code}: {msg}")
+        self.code = code
+
+
+class Settings(C.Structure):
+    """xfem_settings (include/xfem.h); field order of Settings, XPBDFEM/Settings.h:79-91."""
+    _fields_ = [
+        ("time_scale", C.c_float), ("substeps_per_second", C.c_float), ("volume_passes", C.c_uint32),
+        ("gravity", C.c_float * 3), ("compliance", C.c_float), ("damping", C.c_float),
+        ("pbd_damping", C.c_float), ("drag", C.c_float), ("poissons_ratio", C.c_float),
+        ("wonkiness", C.c_float), ("left_right_separation", C.c_float), ("flags", C.c_uint32),
+        ("time_corrected_drag", C.c_float), ("yeoh", C.c_float * 3), ("ground", C.c_uint32),
+        ("ground_normal", C.c_float * 3), ("ground_offset", C.c_float), ("friction", C.c_float),
+    ]
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("cluster_mode", C.c_uint32), ("no_morton", C.c_uint32), ("sync_mode", C.c_uint32),
+        ("block_size", C.c_uint32), ("keep_lambdas", C.c_uint32), ("device", C.c_int32),
+        ("stream", C.c_void_p),
+    ]
+
+
+class Mesh(C.Structure):
+    _fields_ = [("node_data", C.c_void_p), ("node_data_count", C.c_uint32), ("idx_data", C.c_void_p),
+                ("idx_data_count", C.c_uint32), ("density", C.c_float)]
+
+
+class Info(C.Structure):
+    _fields_ = [(n, C.c_uint32) for n in ("bodies", "vertices", "tets", "clusters", "colours", "orphans",
+                                          "chunks", "tet_rows", "block_size", "blocks", "sync_mode",
+                                          "cluster_mode")] + [("device_bytes", C.c_uint64)]
+
+
+# every symbol include/xfem.h declares
+EXPORTS = [
+    "xfem_settings_default", "xfem_create", "xfem_create_ex", "xfem_batch_create", "xfem_destroy",
+    "xfem_get_info", "xfem_set_settings", "xfem_set_lock_mask", "xfem_set_tet_mu", "xfem_substep",
+    "xfem_step_frames", "xfem_synchronize", "xfem_get_positions", "xfem_set_positions",
+    "xfem_get_velocities", "xfem_set_velocities", "xfem_get_inverse_masses", "xfem_get_contacts",
+    "xfem_get_lambdas", "xfem_calculate_volume", "xfem_get_rest_state", "xfem_get_schedule",
+    "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
+    "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
+]
+
+_lib = None
+
+
+def lib():
+    """Loads libxfem.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing; build it with xpbd-fem_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        P, u32, f32 = C.c_void_p, C.c_uint32, C.c_float
+        for name in EXPORTS:
+            getattr(L, name).restype = C.c_int
+        L.xfem_last_error.restype = C.c_char_p
+        L.xfem_time_corrected_drag.restype = C.c_float
+        L.xfem_time_corrected_drag.argtypes = [f32, f32]
+        L.xfem_alloc_host.restype = P
+        L.xfem_alloc_host.argtypes = [C.c_size_t]
+        L.xfem_free_host.restype = None
+        L.xfem_free_host.argtypes = [P]
+        L.xfem_settings_default.argtypes = [P]
+        L.xfem_create_ex.argtypes = [P, u32, P, u32, f32, P, P, P]
+        L.xfem_create.argtypes = [P, u32, P, u32, f32, P, P]
+        L.xfem_batch_create.argtypes = [u32, P, P, P, P]
+        L.xfem_destroy.argtypes = [P]
+        L.xfem_get_info.argtypes = [P, P]
+        L.xfem_set_settings.argtypes = [P, u32, P]
+        L.xfem_set_lock_mask.argtypes = [P, u32, P]
+        L.xfem_set_tet_mu.argtypes = [P, u32, P]
+        L.xfem_substep.argtypes = [P, f32]
+        L.xfem_step_frames.argtypes = [P, u32, u32, f32]
+        L.xfem_synchronize.argtypes = [P]
+        for n in ("xfem_get_positions", "xfem_set_positions", "xfem_get_velocities", "xfem_set_velocities",
+                  "xfem_get_inverse_masses", "xfem_get_contacts", "xfem_get_lambdas", "xfem_calculate_volume"):
+            getattr(L, n).argtypes = [P, u32, P]
+        L.xfem_get_rest_state.argtypes = [P, u32, P, P]
+        L.xfem_get_schedule.argtypes = [P, u32, P, P, P, P]
+        L.xfem_body_counts.argtypes = [P, u32, P, P]
+        L.xfem_compute_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P]
+        L.xfem_compute_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P]
+        L.xfem_generate_tet_block.argtypes = [u32, u32, u32, f32, f32, f32, u32, f32, P, P]
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != OK:
+        raise XfemError(rc, lib().xfem_last_error().decode())
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_settings(**kw):
+    s = Settings()
+    _check(lib().xfem_settings_default(C.byref(s)))
+    for k, v in kw.items():
+        if k in ("gravity", "yeoh", "ground_normal"):
+            getattr(s, k)[:] = [float(x) for x in v]
+        else:
+            setattr(s, k, v)
+    return s
+
+
+def as_settings(s):
+    """A Settings struct from a Settings struct or a dict of its fields."""
+    return default_settings(**s) if isinstance(s, dict) else s
+
+
+def time_corrected_drag(drag, substep_dt):
+    """1 - (1 - drag)^(1000 dt), XPBDFEM/Demo.cpp:63."""
+    return lib().xfem_time_corrected_drag(drag, substep_dt)
+
+
+def generate_tet_block(W, H, D, scale=(1.0, 1.0, 1.0), pattern=0, wonkiness=0.0):
+    """GenerateTetBlock (XPBDFEM/MeshGen.cpp:223): returns (node_data, idx_data)."""
+    nodes = np.zeros(3 * (W + 1) * (H + 1) * (D + 1), np.float32)
+    idx = np.zeros(30 * W * H * D, np.uint32)
+    _check(lib().xfem_generate_tet_block(W, H, D, scale[0], scale[1], scale[2], pattern, wonkiness,
+                                         _p(nodes), _p(idx)))
+    return nodes, idx
+
+
+def compute_rest_state(node_data, idx_data, density):
+    """Host-only rest state (no GPU): (ep[nt, 17], w[nv], flags[nv])."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nv, nt = nd.size // 3, ix.size // 5
+    ep = np.zeros((nt, 17), np.float32)
+    w = np.zeros(nv, np.float32)
+    fl = np.zeros(nv, np.uint8)
+    _check(lib().xfem_compute_rest_state(_p(nd), nd.size, _p(ix), ix.size, density, _p(ep), _p(w), _p(fl)))
+    return ep, w, fl
+
+
+def compute_schedule(node_data, idx_data, cluster_mode=0, morton=True):
+    """Host-only schedule (no GPU), in the form of Body.schedule()."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nv, nt = nd.size // 3, ix.size // 5
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nt, np.uint32)
+    cb = np.zeros(nt + 1, np.uint32)
+    ncol, ncl = C.c_uint32(), C.c_uint32()
+    _check(lib().xfem_compute_schedule(_p(nd), nd.size, _p(ix), ix.size, cluster_mode, 0 if morton else 1,
+                                       _p(rank), _p(order), _p(cb), C.byref(ncol), C.byref(ncl)))
+    return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1], colours=ncol.value,
+                clusters=ncl.value)
+
+
+def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None):
+    o = Options()
+    o.cluster_mode, o.no_morton, o.sync_mode = cluster_mode, 0 if morton else 1, sync_mode
+    o.block_size, o.keep_lambdas, o.device, o.stream = block_size, 1 if keep_lambdas else 0, device, stream
+    return o
+
+
+class Body:
+    """One handle: a single body (GeoLinear3d) or a batch of bodies."""
+
+    def __init__(self, node_data=None, idx_data=None, density=1000.0, settings=None, meshes=None, **opts):
+        self._h = C.c_void_p()
+        self._opts = _options(**opts)
+        if meshes is None:
+            meshes = [(node_data, idx_data, density)]
+            settings = [settings] if settings is not None else None
+        self._keep = []
+        arr = (Mesh * len(meshes))()
+        for i, (nd, ix, dens) in enumerate(meshes):
+            nd = np.ascontiguousarray(nd, np.float32).reshape(-1)
+            ix = np.ascontiguousarray(ix, np.uint32).reshape(-1)
+            self._keep += [nd, ix]
+            arr[i] = Mesh(_p(nd), nd.size, _p(ix), ix.size, float(dens))
+        sarr = None
+        if settings is not None:
+            sarr = (Settings * len(meshes))(*[as_settings(s) if s is not None else default_settings()
+                                               for s in settings])
+        _check(lib().xfem_batch_create(len(meshes), arr, sarr, C.byref(self._opts), C.byref(self._h)))
+        self._keep = []
+        self.nbodies = len(meshes)
+        self.counts = []
+        for b in range(self.nbodies):
+            nv, nt = C.c_uint32(), C.c_uint32()
+            _check(lib().xfem_body_counts(self._h, b, C.byref(nv), C.byref(nt)))
+            self.counts.append((nv.value, nt.value))
+
+    # -- lifecycle
+    def close(self):
+        if self._h:
+            lib().xfem_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        i = Info()
+        _check(lib().xfem_get_info(self._h, C.byref(i)))
+        return {n: getattr(i, n) for n, _ in Info._fields_}
+
+    # -- parameters
+    def set_settings(self, s, body=0):
+        _check(lib().xfem_set_settings(self._h, body, C.byref(as_settings(s))))
+
+    def set_lock_mask(self, mask, body=0):
+        m = np.ascontiguousarray(mask, np.uint8)
+        _check(lib().xfem_set_lock_mask(self._h, body, _p(m)))
+
+    def set_tet_mu(self, mu, body=0):
+        m = None if mu is None else np.ascontiguousarray(mu, np.float32)
+        _check(lib().xfem_set_tet_mu(self._h, body, _p(m)))
+
+    # -- stepping
+    def substep(self, dt):
+        _check(lib().xfem_substep(self._h, dt))
+
+    def step_frames(self, frames, substeps, dt):
+        _check(lib().xfem_step_frames(self._h, frames, substeps, dt))
+
+    def synchronize(self):
+        _check(lib().xfem_synchronize(self._h))
+
+    # -- state
+    def _get(self, fn, body, width, dtype=np.float32):
+        nv = self.counts[body][0]
+        out = np.zeros(nv * width, dtype)
+        _check(fn(self._h, body, _p(out)))
+        return out.reshape(nv, width) if width > 1 else out
+
+    def positions(self, body=0):
+        return self._get(lib().xfem_get_positions, body, 3)
+
+    def velocities(self, body=0):
+        return self._get(lib().xfem_get_velocities, body, 3)
+
+    def inverse_masses(self, body=0):
+        return self._get(lib().xfem_get_inverse_masses, body, 1)
+
+    def contacts(self, body=0):
+        return self._get(lib().xfem_get_contacts, body, 1, np.uint8)
+
+    def set_positions(self, x, body=0):
+        a = np.ascontiguousarray(x, np.float32).reshape(-1)
+        _check(lib().xfem_set_positions(self._h, body, _p(a)))
+
+    def set_velocities(self, v, body=0):
+        a = np.ascontiguousarray(v, np.float32).reshape(-1)
+        _check(lib().xfem_set_velocities(self._h, body, _p(a)))
+
+    def lambdas(self, body=0):
+        nt = self.counts[body][1]
+        out = np.zeros(2 * nt, np.float32)
+        _check(lib().xfem_get_lambdas(self._h, body, _p(out)))
+        return out.reshape(nt, 2)
+
+    def volume(self, body=0):
+        v = C.c_double()
+        _check(lib().xfem_calculate_volume(self._h, body, C.byref(v)))
+        return v.value
+
+    def rest_state(self, body=0):
+        nv, nt = self.counts[body]
+        ep = np.zeros((nt, 17), np.float32)
+        w = np.zeros(nv, np.float32)
+        _check(lib().xfem_get_rest_state(self._h, body, _p(ep), _p(w)))
+        return ep, w
+
+    def schedule(self, body=0):
+        nv, nt = self.counts[body]
+        rank = np.zeros(nv, np.uint32)
+        order = np.zeros(nt, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_schedule(self._h, body, None, None, None, C.byref(ncol)))
+        cb = np.zeros(ncol.value + 1, np.uint32)
+        _check(lib().xfem_get_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
+        return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb, colours=ncol.value)
