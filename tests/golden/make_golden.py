@@ -49,6 +49,14 @@ CASES = [
                             0.0, -9.81, DT, 40, 1]),
     ("ordered_c1_yeoh_tet", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.5,
                              0.0, -9.81, DT, 40, 1]),
+    # compressible (nu < 0.5): the coupled solve is well conditioned here, so
+    # an FP32 implementation can be held to 1e-5 of the reference's own path
+    ("ordered_c1_nh_nu045_star", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                  0.0, -9.81, DT, 40, 1]),
+    ("ordered_c1_yeoh_nu049_tet", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.49,
+                                   0.0, -9.81, DT, 40, 1]),
+    ("ordered_wonky_nh_serial_nu045_star", ["ordered", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                            -2.0, -9.81, DT, 10, 1]),
 ]
 
 

@@ -17,7 +17,8 @@ INIT = ["init_8x2x2", "init_3x2x2_mirror_wonky", "init_5x3x2_aniso_wonky"]
 SOLVE = ["solve_nh_sim_incompressible", "solve_nh_sim_nu045", "solve_yeoh_sim_incompressible",
          "solve_nh_serial_nu045", "solve_yeoh_serial_nu049"]
 SUBSTEP = ["substep_c1_nh_native", "substep_c1_yeoh_native", "substep_wonky_nh_serial_native",
-           "ordered_c1_nh_star", "ordered_c1_yeoh_tet"]
+           "ordered_c1_nh_star", "ordered_c1_yeoh_tet", "ordered_c1_nh_nu045_star", "ordered_c1_yeoh_nu049_tet",
+           "ordered_wonky_nh_serial_nu045_star"]
 
 
 @pytest.mark.parametrize("name", MESH)
