@@ -41,7 +41,8 @@ struct BodyHost {
 	std::vector<float> tet_mu;        // empty = uniform material
 	xfem_settings settings;
 	Schedule sched;
-	std::vector<uint32_t> tet_slot;   // caller tet -> row * 32 + lane
+	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
+	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
 };
 
 template <typename T>
@@ -67,15 +68,15 @@ struct xfem_body {
 	std::vector<BodyHost> bodies;
 	uint32_t nverts = 0, ntets = 0, nchunks = 0, nrows = 0, nvrows = 0, ncolours = 0;
 	// device buffers
-	DevBuf<float4> vert, trec;
-	DevBuf<uint32_t> chdr, cvid, cslot, ccb, orphans, dev_of_vert, tets_dev, bar;
+	DevBuf<float4> vert, cblk;
+	DevBuf<uint32_t> ccb, orphans, dev_of_vert, tets_dev, bar;
 	DevBuf<ChunkMeta> chunks;
 	DevBuf<BodyParams> params;
 	DevBuf<float2> tlam;
 	DevBuf<int> err;
 	DevBuf<float> stage;
 	DevBuf<double> vol;
-	std::vector<float4> trec_host;  // kept to refresh c0 after material changes
+	std::vector<float4> cblk_host;  // kept to refresh c0 after material changes
 	uint32_t norphans = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -228,13 +229,14 @@ int build_device(xfem_body* h) {
 	ccb[ncol] = (uint32_t)chunk_lanes.size();
 	const uint32_t nch = (uint32_t)chunk_lanes.size();
 	std::vector<ChunkMeta> meta(nch);
-	uint32_t trows = 0, vrows = 0;
+	std::vector<uint32_t> shape_nt(nch), shape_nv(nch);
+	uint64_t total16 = 0;
+	uint32_t trows = 0, max_bytes = 128, max_nv = 4;
 	for (uint32_t k = 0; k < nch; k++) {
 		uint32_t ntm = 0, nvm = 0;
 		for (const Lane& L : chunk_lanes[k]) {
 			const BodyHost& b = h->bodies[L.body];
 			const uint32_t nt = b.sched.cl_begin[L.cluster + 1] - b.sched.cl_begin[L.cluster];
-			// vertex count of the cluster
 			uint32_t vs[kMaxClusterVerts + 4], nvv = 0;
 			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++)
 				for (int n = 0; n < 4; n++) {
@@ -244,19 +246,31 @@ int build_device(xfem_body* h) {
 			ntm = std::max(ntm, nt);
 			nvm = std::max(nvm, nvv);
 		}
-		meta[k] = {trows, ntm, vrows, nvm};
+		const uint32_t bytes = chunk_block_bytes(ntm, nvm);
+		if (total16 + bytes / 16 > 0xffffffffull) return fail(XFEM_ELIMIT, "chunk blocks exceed 64 GiB");
+		meta[k] = {(uint32_t)total16, bytes, ntm | (nvm << 8), trows};
+		shape_nt[k] = ntm;
+		shape_nv[k] = nvm;
+		total16 += bytes / 16;
 		trows += ntm;
-		vrows += nvm;
+		max_bytes = std::max(max_bytes, bytes);
+		max_nv = std::max(max_nv, nvm);
 	}
 	h->nchunks = nch;
 	h->nrows = trows;
-	h->nvrows = vrows;
-	std::vector<uint32_t> chdr((size_t)nch * kLanes, 0), cvid((size_t)vrows * kLanes, 0), cslot((size_t)trows * kLanes, 0);
-	std::vector<float4> trec((size_t)trows * 4 * kLanes, make_float4(0, 0, 0, 0));
+	std::vector<float4> cblk((size_t)total16, make_float4(0, 0, 0, 0));
 	std::vector<uint8_t> in_colour0(nverts, 0);
-	for (auto& b : h->bodies) b.tet_slot.assign(b.nt, 0xffffffffu);
+	for (auto& b : h->bodies) {
+		b.tet_slot.assign(b.nt, 0xffffffffu);
+		b.tet_rec.assign(b.nt, 0);
+	}
 	for (uint32_t k = 0; k < nch; k++) {
 		const bool colour0 = k < ccb[1];
+		const uint32_t ntm = shape_nt[k], nvm = shape_nv[k];
+		float4* rec = &cblk[meta[k].off16];
+		uint32_t* hdr = reinterpret_cast<uint32_t*>(rec + 128 * (size_t)ntm);
+		uint32_t* vid = hdr + kLanes;
+		uint32_t* slot = vid + kLanes * (size_t)nvm;
 		for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++) {
 			const Lane& L = chunk_lanes[k][lane];
 			BodyHost& b = h->bodies[L.body];
@@ -270,22 +284,22 @@ int build_device(xfem_body* h) {
 					if (f == vs + nvv) vs[nvv++] = v;
 					slots |= (uint32_t)(f - vs) << (4 * n);
 				}
-				const uint32_t row = meta[k].trow + ntt;
-				cslot[(size_t)row * kLanes + lane] = slots;
-				b.tet_slot[t] = row * kLanes + lane;
+				slot[(size_t)ntt * kLanes + lane] = slots;
+				b.tet_slot[t] = (meta[k].trow + ntt) * kLanes + lane;
 				const float* e = &b.ep[17 * (size_t)t];
-				float4* r = &trec[(size_t)row * 4 * kLanes + lane];
+				float4* r = rec + (size_t)ntt * 4 * kLanes + lane;
 				r[0] = make_float4(e[0], e[1], e[2], e[3]);
 				r[kLanes] = make_float4(e[4], e[5], e[6], e[7]);
 				r[2 * kLanes] = make_float4(e[8], e[9], e[10], e[11]);
 				r[3 * kLanes] = make_float4(e[12], e[13], e[14], tet_c0(b, t));
+				b.tet_rec[t] = meta[k].off16 + ((size_t)ntt * 4 + 3) * kLanes + lane;
 			}
 			for (uint32_t s = 0; s < nvv; s++) {
 				const uint32_t dv = b.vbase + b.sched.vert_rank[vs[s]];
-				cvid[(size_t)(meta[k].vrow + s) * kLanes + lane] = dv;
+				vid[(size_t)s * kLanes + lane] = dv;
 				if (colour0) in_colour0[dv] = 1;
 			}
-			chdr[(size_t)k * kLanes + lane] = nvv | (ntt << 4) | (L.body << 8);
+			hdr[lane] = nvv | (ntt << 4) | (L.body << 8);
 		}
 	}
 	std::vector<uint32_t> orphans;
@@ -310,13 +324,9 @@ int build_device(xfem_body* h) {
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
 	}
-	h->trec_host = trec;
 	// upload
 	XCUDA(h->vert.alloc(vert.size()));
-	XCUDA(h->trec.alloc(trec.size()));
-	XCUDA(h->chdr.alloc(chdr.size()));
-	XCUDA(h->cvid.alloc(cvid.size()));
-	XCUDA(h->cslot.alloc(cslot.size()));
+	XCUDA(h->cblk.alloc(cblk.size()));
 	XCUDA(h->ccb.alloc(ccb.size()));
 	XCUDA(h->orphans.alloc(orphans.size()));
 	XCUDA(h->dev_of_vert.alloc(dev_of.size()));
@@ -334,10 +344,7 @@ int build_device(xfem_body* h) {
 		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
 	};
 	XCUDA(up(h->vert.p, vert.data(), vert.size() * sizeof(float4)));
-	XCUDA(up(h->trec.p, trec.data(), trec.size() * sizeof(float4)));
-	XCUDA(up(h->chdr.p, chdr.data(), chdr.size() * 4));
-	XCUDA(up(h->cvid.p, cvid.data(), cvid.size() * 4));
-	XCUDA(up(h->cslot.p, cslot.data(), cslot.size() * 4));
+	XCUDA(up(h->cblk.p, cblk.data(), cblk.size() * sizeof(float4)));
 	XCUDA(up(h->ccb.p, ccb.data(), ccb.size() * 4));
 	XCUDA(up(h->orphans.p, orphans.data(), orphans.size() * 4));
 	XCUDA(up(h->dev_of_vert.p, dev_of.data(), dev_of.size() * 4));
@@ -347,15 +354,14 @@ int build_device(xfem_body* h) {
 	XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
 	if (h->tlam.p) XCUDA(cudaMemsetAsync(h->tlam.p, 0, h->tlam.n * sizeof(float2), h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
-	h->device_bytes = vert.size() * 16 + trec.size() * 16 + (chdr.size() + cvid.size() + cslot.size() + ccb.size() +
-	                  orphans.size() + dev_of.size() + tets_dev.size()) * 4 + meta.size() * 16 + params.size() * 64 +
-	                  h->stage.n * 4 + h->tlam.n * 8;
+	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + orphans.size() + dev_of.size() +
+	                  tets_dev.size()) * 4 + meta.size() * 16 + params.size() * 64 + h->stage.n * 4 + h->tlam.n * 8;
+	h->cblk_host.swap(cblk);
 	DevCtx& c = h->ctx;
 	c.vert = h->vert.p;
-	c.chdr = h->chdr.p;
-	c.cvid = h->cvid.p;
-	c.cslot = h->cslot.p;
-	c.trec = h->trec.p;
+	c.cblk = h->cblk.p;
+	c.chunk_smem = max_bytes;
+	c.warp_smem = max_bytes + 2u * max_nv * kLanes * 16u;
 	c.tlam = h->tlam.p;
 	c.chunks = h->chunks.p;
 	c.colour_chunk_begin = h->ccb.p;
@@ -367,12 +373,19 @@ int build_device(xfem_body* h) {
 	c.bar_count = h->bar.p;
 	c.err = h->err.p;
 	h->cfg.lambdas = h->opt.keep_lambdas != 0;
+	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
 	return XFEM_OK;
 }
 
 int set_config(xfem_body* h, int sync_mode, int block) {
+	int optin = 0;
+	XCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+	if (solve_smem_bytes(block, h->cfg.warp_smem) > (size_t)optin)
+		return fail(XFEM_EINVAL, "block size " + std::to_string(block) + " needs " +
+		                             std::to_string(solve_smem_bytes(block, h->cfg.warp_smem)) +
+		                             " bytes of shared memory; the device allows " + std::to_string(optin));
 	h->cfg.sync_mode = sync_mode;
 	h->cfg.block = block;
 	if (const int ek = configure_kernels(h->cfg))
@@ -424,7 +437,7 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	h->tuned = true;
 	const int fixed_sync = (int)h->opt.sync_mode, fixed_block = (int)h->opt.block_size;
 	std::vector<std::pair<int, int>> cand;
-	const int blocks[] = {128, 256, 512};
+	const int blocks[] = {64, 128, 256};
 	for (int sm : {1, 2}) {
 		if (fixed_sync && sm != fixed_sync) continue;
 		for (int bs : blocks) {
@@ -500,7 +513,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	int rc = build_device(h.get());
 	if (rc) return rc;
 	// default configuration until the first step tunes it
-	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1, h->opt.block_size ? (int)h->opt.block_size : 256);
+	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1, h->opt.block_size ? (int)h->opt.block_size : 128);
 	if (rc) return rc;
 	if (h->opt.sync_mode && h->opt.block_size) h->tuned = true;
 	*out = h.release();
@@ -551,11 +564,8 @@ int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
 
 int upload_records(xfem_body* h) {
 	for (auto& b : h->bodies)
-		for (uint32_t t = 0; t < b.nt; t++) {
-			const uint32_t s = b.tet_slot[t];
-			h->trec_host[((size_t)(s / kLanes) * 4 + 3) * kLanes + s % kLanes].w = tet_c0(b, t);
-		}
-	XCUDA(cudaMemcpyAsync(h->trec.p, h->trec_host.data(), h->trec_host.size() * sizeof(float4), cudaMemcpyHostToDevice,
+		for (uint32_t t = 0; t < b.nt; t++) h->cblk_host[b.tet_rec[t]].w = tet_c0(b, t);
+	XCUDA(cudaMemcpyAsync(h->cblk.p, h->cblk_host.data(), h->cblk_host.size() * sizeof(float4), cudaMemcpyHostToDevice,
 	                      h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	return XFEM_OK;

@@ -66,27 +66,33 @@ struct BodyParams {
 	uint32_t pad;
 };
 
-// Per-chunk metadata: 32 clusters of one colour side by side (lane = cluster).
+// A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
+// one contiguous block that a single bulk copy brings into shared memory:
+//   records  ntmax rows x 4 planes x 32 lanes x float4 (Qi, QQ, QR, c0)
+//   header   32 x u32: nv | nt << 4 | body << 8
+//   vids     nvmax rows x 32 x u32 (device vertex ids)
+//   slots    ntmax rows x 32 x u32 (4 x 4-bit local vertex slots per tet)
 struct ChunkMeta {
-	uint32_t trow;  // first tet row (rows hold one tet per lane)
-	uint32_t ntmax; // rows used by this chunk
-	uint32_t vrow;  // first vertex-slot row
-	uint32_t nvmax; // vertex slots used by this chunk
+	uint32_t off16;  // block offset in 16-byte units
+	uint32_t bytes;  // block size (a multiple of 128)
+	uint32_t shape;  // ntmax | nvmax << 8
+	uint32_t trow;   // first global tet row (multiplier output)
 };
+
+inline uint32_t chunk_block_bytes(uint32_t ntmax, uint32_t nvmax) { return 2048u * ntmax + 128u * (1u + nvmax + ntmax); }
 
 // Everything a kernel needs, passed by value.
 struct DevCtx {
 	float4* vert;               // 2 per vertex: (O.xyz, w), (D.xyz, flag bits)
-	const uint32_t* chdr;       // per cluster lane: nv | nt << 4 | body << 8
-	const uint32_t* cvid;       // [vrow][lane] vertex ids
-	const uint32_t* cslot;      // [trow][lane] 4 x 4-bit local slots
-	const float4* trec;         // [trow][4][lane] Qi, QQ, QR, c0 = (1/mu)/volume
+	const float4* cblk;         // chunk blocks
 	float2* tlam;               // [trow][lane] multipliers or null
 	const ChunkMeta* chunks;
 	const uint32_t* colour_chunk_begin;  // ncolours + 1
 	const uint32_t* orphans;    // vertices outside every colour-0 cluster
 	const BodyParams* bodies;
 	uint32_t nverts, norphans, ncolours;
+	uint32_t chunk_smem;        // bytes of the largest chunk block
+	uint32_t warp_smem;         // chunk_smem + vertex slots (2 x nvmax x 32 x 16 B)
 	uint32_t* bar_count;        // grid barrier arrival counter
 	int* err;                   // device error word (0 = ok)
 };
@@ -97,6 +103,7 @@ constexpr uint32_t kFlagContact = 2u;
 
 // Device error codes written to DevCtx::err.
 constexpr int kErrBarrierTimeout = 1;
+constexpr int kErrCopyTimeout = 2;
 
 // ---- kernel launchers (xfem_kernels.cu) ---------------------------------------
 struct LaunchCfg {
@@ -104,6 +111,7 @@ struct LaunchCfg {
 	int blocks = 0;        // persistent grid size
 	int sync_mode = 1;     // 1 persistent, 2 graph-style per-colour launches
 	bool lambdas = false;
+	uint32_t warp_smem = 0;
 	uint32_t total_chunks = 0;
 	std::vector<uint32_t> colour_chunk_begin_host;
 };
@@ -117,7 +125,7 @@ int configure_kernels(const LaunchCfg& cfg);
 // Largest co-resident grid for the persistent kernel at this block size.
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out);
 // Dynamic shared memory bytes per block of the solve kernels.
-size_t solve_smem_bytes(int block);
+size_t solve_smem_bytes(int block, uint32_t warp_smem);
 
 // Transfer helpers (caller order <-> device order), run on `stream`.
 int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, float* out,

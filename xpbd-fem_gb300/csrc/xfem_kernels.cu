@@ -156,14 +156,16 @@ struct TetRec {
 	float4 a, b, c, d;
 };
 
-__device__ __forceinline__ TetRec load_rec(const float4* __restrict__ trec, uint32_t row, uint32_t lane) {
-	const float4* p = trec + (size_t)row * 4 * kLanes + lane;
-	TetRec r;
-	r.a = __ldg(p);
-	r.b = __ldg(p + kLanes);
-	r.c = __ldg(p + 2 * kLanes);
-	r.d = __ldg(p + 3 * kLanes);
-	return r;
+// The material scalars a solve needs, copied to registers once per cluster.
+struct Mat {
+	float a, ratio, y0, y1, y2;
+	uint32_t energy, simultaneous;
+};
+
+__device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body) {
+	const BodyParams* b = bodies + body;
+	return {__ldg(&b->a), __ldg(&b->ratio), __ldg(&b->yeoh[0]), __ldg(&b->yeoh[1]), __ldg(&b->yeoh[2]),
+	        __ldg(&b->energy), __ldg(&b->simultaneous)};
 }
 
 // Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with
@@ -204,7 +206,7 @@ __device__ __forceinline__ float hydrostatic(const float q[3][3], const Vec3 P[3
 
 // Deviatoric term, prefactored (XPBDFEM/Fem.cpp:163-192), with the Yeoh
 // transform of XPBDFEM/Fem.cpp:525-531 when energy == 7.
-__device__ __forceinline__ float deviatoric(const BodyParams& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
+__device__ __forceinline__ float deviatoric(const Mat& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
                                             Vec3 g[4]) {
 	float U = QQ[0] * dot(P[0], P[0]);
 	U = fmaf(QQ[1], dot(P[1], P[1]), U);
@@ -222,7 +224,7 @@ __device__ __forceinline__ float deviatoric(const BodyParams& bp, const float QQ
 	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
 	if (bp.energy == 7u) {
 		const float IM = U - 3.0f;
-		const float C0 = bp.yeoh[0], C1 = bp.yeoh[1], C2 = bp.yeoh[2];
+		const float C0 = bp.y0, C1 = bp.y1, C2 = bp.y2;
 		U = fmaxf(0.0001f, IM * fmaf(IM, fmaf(IM, C2, C1), C0));
 		const float gs = fmaf(IM, fmaf(IM, 3.0f * C2, 2.0f * C1), C0);
 #pragma unroll
@@ -244,7 +246,7 @@ __device__ __forceinline__ float wdot(const float w[4], const Vec3 a[4], const V
 // (XPBDFEM/Xpbd.h:87-121). O[]: start positions + w, D[]: displacements
 // (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
 // alpha1 = alpha0 * (mu / lambda), i.e. (1/lambda)/volume/dt^2.
-__device__ __forceinline__ float2 solve_tet(const BodyParams& bp, const TetRec& r, float inv_dt2, const float4 O[4],
+__device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, float inv_dt2, const float4 O[4],
                                             float4 D[4]) {
 	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
 	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
@@ -307,54 +309,144 @@ __device__ __forceinline__ float2 solve_tet(const BodyParams& bp, const TetRec& 
 
 enum Phase : int { kPhaseSolve = 0, kPhasePredict = 1, kPhaseAdvance = 2 };
 
-// One lane = one cluster of one chunk.
+// ---- chunk staging: one TMA bulk copy per chunk into the warp's buffer ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* m) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(m)) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Issued by one lane: expect `bytes` on the barrier and start the copy.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+	asm volatile(
+	    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+	    "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+	    : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* m, uint32_t parity) {
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(m)), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+
+// Bounded wait for the copy of the current phase. On timeout the error word
+// is set and the wait continues for one more bounded period so that no copy
+// is left in flight when the block leaves.
+__device__ bool mbar_wait(const DevCtx& C, uint64_t* m, uint32_t parity) {
+	uint64_t t0 = 0;
+	for (uint32_t spins = 0;; spins++) {
+		if (mbar_test(m, parity)) return true;
+		if ((spins & 1023u) == 1023u) {
+			const uint64_t t = global_ns();
+			if (t0 == 0) {
+				t0 = t;
+			} else if (t - t0 > kBarrierTimeoutNs) {
+				atomicCAS(C.err, 0, kErrCopyTimeout);
+				for (uint32_t k = 0;; k++) {
+					if (mbar_test(m, parity)) break;
+					if ((k & 1023u) == 1023u && global_ns() - t > kBarrierTimeoutNs) break;
+				}
+				return false;
+			}
+		}
+	}
+}
+
+// Per-warp staging state: the chunk buffer, the vertex slots, the barrier.
+struct Stage {
+	uint8_t* buf;     // chunk block (records, header, vertex ids, slots)
+	float4* vs;       // vertex slots: O at [s * 32 + lane], D at [(nvmax + s) * 32 + lane]
+	uint64_t* mbar;
+	uint32_t parity;
+	int inflight;     // chunk whose copy is in flight or resident, -1 = none
+};
+
+__device__ __forceinline__ void stage_issue(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	__syncwarp();
+	if (lane == 0) bulk_copy_g2s(st.buf, C.cblk + m.x, m.y, st.mbar);
+	st.inflight = (int)chunk;
+}
+
+// Makes `chunk` resident in the warp's buffer. Returns false on timeout.
+__device__ __forceinline__ bool stage_acquire(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	if (st.inflight != (int)chunk) {
+		if (st.inflight >= 0) {  // a different copy is in flight: let it land first
+			if (!mbar_wait(C, st.mbar, st.parity)) return false;
+			st.parity ^= 1u;
+		}
+		stage_issue(C, st, chunk, lane);
+	}
+	const bool ok = mbar_wait(C, st.mbar, st.parity);
+	st.parity ^= 1u;
+	st.inflight = -1;
+	return ok;
+}
+
+// One warp processes one resident chunk; lane = cluster. `next` >= 0 is the
+// warp's next chunk: its copy is issued as soon as this chunk's records have
+// been consumed, so it overlaps the write-back and the following barrier.
 template <bool LAMBDAS>
-__device__ __forceinline__ void run_cluster(const DevCtx& C, uint32_t chunk, uint32_t lane, int phase, float dt,
-                                            float inv_dt, float inv_dt2, float4* sO, float4* sD, uint32_t stride) {
-	const uint4 meta = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
-	const ChunkMeta m = {meta.x, meta.y, meta.z, meta.w};
-	const uint32_t hdr = __ldg(C.chdr + (size_t)chunk * kLanes + lane);
+__device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, int phase,
+                                          float dt, float inv_dt, float inv_dt2) {
+	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
+	const float4* rec = reinterpret_cast<const float4*>(st.buf);
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * ntmax);
+	const uint32_t* vids = hdrs + kLanes;
+	const uint32_t* slots = vids + kLanes * nvmax;
+	const uint32_t hdr = hdrs[lane];
 	const uint32_t nv = hdr & 15u, nt = (hdr >> 4) & 15u;
-	if (nv == 0) return;
-	const BodyParams& bp = C.bodies[hdr >> 8];
+	float4* sO = st.vs + lane;
+	float4* sD = st.vs + kLanes * nvmax + lane;
 	uint32_t vid[kMaxClusterVerts];
+	if (nv) {
+		const Mat mat = load_mat(C.bodies, hdr >> 8);
 #pragma unroll
-	for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
-		if (s < nv) {
-			vid[s] = __ldg(C.cvid + (size_t)(m.vrow + s) * kLanes + lane);
-			float4 O = __ldcg(C.vert + 2 * (size_t)vid[s]);
-			float4 D = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
-			if (phase != kPhaseSolve) advance_vertex(C.bodies, O, D, phase == kPhasePredict, dt, inv_dt);
-			sO[s * stride] = O;
-			sD[s * stride] = D;
+		for (uint32_t s = 0; s < kMaxClusterVerts; s++)
+			if (s < nv) vid[s] = vids[s * kLanes + lane];
+#pragma unroll
+		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
+			if (s < nv) {
+				float4 O = __ldcg(C.vert + 2 * (size_t)vid[s]);
+				float4 D = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
+				if (phase != kPhaseSolve) advance_vertex(C.bodies, O, D, phase == kPhasePredict, dt, inv_dt);
+				sO[s * kLanes] = O;
+				sD[s * kLanes] = D;
+			}
+		}
+		for (uint32_t t = 0; t < nt; t++) {
+			const float4* r = rec + t * 4 * kLanes + lane;
+			const TetRec tr = {r[0], r[kLanes], r[2 * kLanes], r[3 * kLanes]};
+			const uint32_t sl = slots[t * kLanes + lane];
+			const uint32_t s0 = sl & 15u, s1 = (sl >> 4) & 15u, s2 = (sl >> 8) & 15u, s3 = (sl >> 12) & 15u;
+			const float4 O[4] = {sO[s0 * kLanes], sO[s1 * kLanes], sO[s2 * kLanes], sO[s3 * kLanes]};
+			float4 D[4] = {sD[s0 * kLanes], sD[s1 * kLanes], sD[s2 * kLanes], sD[s3 * kLanes]};
+			const float2 lam = solve_tet(mat, tr, inv_dt2, O, D);
+			sD[s0 * kLanes] = D[0];
+			sD[s1 * kLanes] = D[1];
+			sD[s2 * kLanes] = D[2];
+			sD[s3 * kLanes] = D[3];
+			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
 		}
 	}
-	TetRec rec = load_rec(C.trec, m.trow, lane);
-	uint32_t sl = __ldg(C.cslot + (size_t)m.trow * kLanes + lane);
-	for (uint32_t t = 0; t < nt; t++) {
-		TetRec nrec;
-		uint32_t nsl = 0;
-		if (t + 1 < nt) {
-			nrec = load_rec(C.trec, m.trow + t + 1, lane);
-			nsl = __ldg(C.cslot + (size_t)(m.trow + t + 1) * kLanes + lane);
-		}
-		const uint32_t s0 = sl & 15u, s1 = (sl >> 4) & 15u, s2 = (sl >> 8) & 15u, s3 = (sl >> 12) & 15u;
-		const float4 O[4] = {sO[s0 * stride], sO[s1 * stride], sO[s2 * stride], sO[s3 * stride]};
-		float4 D[4] = {sD[s0 * stride], sD[s1 * stride], sD[s2 * stride], sD[s3 * stride]};
-		const float2 lam = solve_tet(bp, rec, inv_dt2, O, D);
-		sD[s0 * stride] = D[0];
-		sD[s1 * stride] = D[1];
-		sD[s2 * stride] = D[2];
-		sD[s3 * stride] = D[3];
-		if (LAMBDAS) C.tlam[(size_t)(m.trow + t) * kLanes + lane] = lam;
-		rec = nrec;
-		sl = nsl;
-	}
+	(void)ntmax;
+	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
+	if (nv) {
 #pragma unroll
-	for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
-		if (s < nv) {
-			if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * stride]);
-			__stcg(C.vert + 2 * (size_t)vid[s] + 1, sD[s * stride]);
+		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
+			if (s < nv) {
+				if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * kLanes]);
+				__stcg(C.vert + 2 * (size_t)vid[s] + 1, sD[s * kLanes]);
+			}
 		}
 	}
 }
@@ -379,51 +471,91 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 	}
 }
 
+__device__ __forceinline__ Stage stage_init(const DevCtx& C, uint32_t lane) {
+	extern __shared__ __align__(128) uint8_t smem[];
+	__shared__ uint64_t mbars[32];
+	const uint32_t w = threadIdx.x >> 5;
+	uint8_t* base = smem + (size_t)w * C.warp_smem;
+	Stage st = {base, reinterpret_cast<float4*>(base + C.chunk_smem), &mbars[w], 0u, -1};
+	if (lane == 0) mbar_init(st.mbar);
+	__syncwarp();
+	return st;
+}
+
+// The warp's next chunk after `ch` (colour c of substep s): the next chunk of
+// the same colour, else its first chunk of the following colours (wrapping
+// into the next substep); -1 when the launch has no more work for it.
+__device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t nsub, uint32_t c, uint32_t ch,
+                                          uint32_t gwarp, uint32_t nwarps) {
+	if (ch + nwarps < __ldg(C.colour_chunk_begin + c + 1)) return (int)(ch + nwarps);
+	for (uint32_t k = 1; k <= C.ncolours; k++) {
+		uint32_t c2 = c + k, s2 = s;
+		if (c2 >= C.ncolours) {
+			c2 -= C.ncolours;
+			s2++;
+		}
+		if (s2 >= nsub) return -1;
+		const uint32_t first = __ldg(C.colour_chunk_begin + c2) + gwarp;
+		if (first < __ldg(C.colour_chunk_begin + c2 + 1)) return (int)first;
+	}
+	return -1;
+}
+
 // Persistent kernel: nsub substeps x ncolours colour passes separated by the
 // bounded grid barrier. Must be launched cooperatively (co-resident grid).
 template <bool LAMBDAS>
 __global__ void __launch_bounds__(512) k_persistent(DevCtx C, uint32_t nsub, float dt) {
-	extern __shared__ float4 smem[];
-	const uint32_t stride = blockDim.x;
-	float4* sO = smem + threadIdx.x;
-	float4* sD = smem + kMaxClusterVerts * stride + threadIdx.x;
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	// chunk i of a colour goes to block i % grid, so chunks spread over all SMs
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	Stage st = stage_init(C, lane);
 	uint32_t target = 0;
-	for (uint32_t s = 0; s < nsub; s++) {
-		for (uint32_t c = 0; c < C.ncolours; c++) {
+	bool ok = true;
+	for (uint32_t s = 0; s < nsub && ok; s++) {
+		for (uint32_t c = 0; c < C.ncolours && ok; c++) {
 			const int phase = c == 0 ? (s == 0 ? kPhasePredict : kPhaseAdvance) : kPhaseSolve;
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
-			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps)
-				run_cluster<LAMBDAS>(C, ch, lane, phase, dt, inv_dt, inv_dt2, sO, sD, stride);
+			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
+				if (!stage_acquire(C, st, ch, lane)) {
+					ok = false;
+					break;
+				}
+				run_chunk<LAMBDAS>(C, st, ch, next_chunk(C, s, nsub, c, ch, gwarp, nwarps), lane, phase, dt, inv_dt,
+				                   inv_dt2);
+			}
 			if (c == 0) run_orphans(C, gtid, nthreads, s == 0, dt, inv_dt);
-			if (!grid_sync(C, target)) return;
+			if (!grid_sync(C, target)) ok = false;
 		}
+	}
+	if (!ok) {
+		// leave no copy in flight
+		if (st.inflight >= 0) mbar_wait(C, st.mbar, st.parity);
+		return;
 	}
 	run_finalize(C, gtid, nthreads, inv_dt);
 }
 
-// One colour pass as its own launch (CUDA-graph mode). Blocks past the
-// colour's chunks advance orphan vertices when `phase` is not kPhaseSolve.
+// One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
+// Blocks past the colour's chunks advance orphan vertices when `phase` is not
+// kPhaseSolve.
 template <bool LAMBDAS>
 __global__ void __launch_bounds__(512) k_colour(DevCtx C, uint32_t colour, int phase, float dt,
-                                                 uint32_t solve_blocks) {
-	extern __shared__ float4 smem[];
+                                                uint32_t solve_blocks) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	if (blockIdx.x >= solve_blocks) {
 		const uint32_t b = blockIdx.x - solve_blocks, nb = gridDim.x - solve_blocks;
 		run_orphans(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, phase == kPhasePredict, dt, inv_dt);
 		return;
 	}
-	const uint32_t stride = blockDim.x;
+	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t ch = __ldg(C.colour_chunk_begin + colour) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
-	run_cluster<LAMBDAS>(C, ch, threadIdx.x & 31u, phase, dt, inv_dt, inv_dt2, smem + threadIdx.x,
-	                     smem + kMaxClusterVerts * stride + threadIdx.x, stride);
+	Stage st = stage_init(C, lane);
+	if (!stage_acquire(C, st, ch, lane)) return;
+	run_chunk<LAMBDAS>(C, st, ch, -1, lane, phase, dt, inv_dt, inv_dt2);
 }
 
 __global__ void k_finalize(DevCtx C, float dt) {
@@ -487,14 +619,14 @@ __global__ void k_volume(const float4* __restrict__ vert, const uint32_t* __rest
 
 }  // namespace
 
-size_t solve_smem_bytes(int block) { return (size_t)2 * kMaxClusterVerts * sizeof(float4) * (size_t)block; }
+size_t solve_smem_bytes(int block, uint32_t warp_smem) { return (size_t)(block / 32) * warp_smem; }
 
 static void set_smem_attr(const void* f, size_t bytes) {
 	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 int configure_kernels(const LaunchCfg& cfg) {
-	const size_t smem = solve_smem_bytes(cfg.block);
+	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	set_smem_attr(cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>, smem);
 	set_smem_attr(cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>, smem);
 	return (int)cudaGetLastError();
@@ -502,7 +634,7 @@ int configure_kernels(const LaunchCfg& cfg) {
 
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
 	const void* f = cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
-	const size_t smem = solve_smem_bytes(cfg.block);
+	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -514,7 +646,7 @@ int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
 
 int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, float dt, void* stream) {
 	cudaStream_t st = (cudaStream_t)stream;
-	const size_t smem = solve_smem_bytes(cfg.block);
+	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	cudaError_t e = cudaSuccess;
 	if (nsub == 0) return 0;
 	if (cfg.sync_mode == 1) {
