@@ -157,6 +157,22 @@ int xfem_substep(xfem_body* b, float dt);
 /* frames * substeps substeps in one launch (persistent kernel or one CUDA
  * graph), the loop of Sim::Update (XPBDFEM/Demo.cpp:67-90) with a fixed dt. */
 int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
+/* No counterpart in the reference. The same stepping as xfem_step_frames
+ * for callers that cannot allocate device memory when they step: a process
+ * whose device memory is fully reserved by another allocator, a real-time
+ * loop that must not take cudaMalloc's device-wide synchronisation, or code
+ * running while a stream is captured (cudaMalloc is not permitted there).
+ * It always runs the persistent kernel at the handle's block size, never the
+ * autotuner or the CUDA-graph builder (which may allocate), and calls no
+ * cudaMalloc, cudaFree or other allocating routine. The kernel's scratch (the
+ * grid-barrier counter and the device error word) lives in one fixed 256-byte
+ * device array that every GPU loading the library keeps until exit; all calls
+ * share it, so calls whose kernels overlap on one GPU race and must not be
+ * issued. The first call on a device looks the array's device address up; make
+ * that first call before any stream capture. Limit: frames * substeps *
+ * colours * persistent blocks must stay below 2^31 per call (else
+ * XFEM_ELIMIT). Synchronises the handle's stream and reports device errors. */
+int xfem_step_frames_noalloc(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
 /* Waits for queued work; returns XFEM_EDEVICE_TIMEOUT if a bounded device
  * wait ran out since the last check. */
 int xfem_synchronize(xfem_body* b);

@@ -699,6 +699,24 @@ int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt)
 	return step(b, (uint32_t)n, dt);
 }
 
+int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, float dt) {
+	if (!h) return fail(XFEM_EINVAL, "null handle");
+	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
+	const uint64_t n = (uint64_t)frames * substeps;
+	if (n == 0) return XFEM_OK;
+	if (n > 0xffffffffull) return fail(XFEM_EINVAL, "too many substeps in one call");
+	XCUDA(cudaSetDevice(h->device));
+	int dev_err = 0;
+	const int e = launch_substeps_noalloc(h->ctx, h->cfg.block, h->cfg.warp_smem, h->cfg.lambdas, (uint32_t)n, dt,
+	                                      h->stream, h->device, &dev_err);
+	if (e == (int)cudaErrorInvalidValue)
+		return fail(XFEM_ELIMIT, "frames * substeps * colours * persistent blocks must stay below 2^31 per call");
+	if (e) return fail(XFEM_ECUDA, std::string("allocation-free launch: ") + cudaGetErrorString((cudaError_t)e));
+	if (dev_err == kErrBarrierTimeout) return fail(XFEM_EDEVICE_TIMEOUT, "device grid barrier timed out");
+	if (dev_err) return fail(XFEM_ECUDA, "device error " + std::to_string(dev_err));
+	return XFEM_OK;
+}
+
 int xfem_synchronize(xfem_body* b) {
 	if (!b) return fail(XFEM_EINVAL, "null handle");
 	XCUDA(cudaSetDevice(b->device));

@@ -127,6 +127,13 @@ int persistent_grid(const LaunchCfg& cfg, int* blocks_out);
 // Dynamic shared memory bytes per block of the solve kernels.
 size_t solve_smem_bytes(int block, uint32_t warp_smem);
 
+// Allocation-free stepping: the persistent kernel with its scratch words in a
+// fixed device array (xfem_kernels.cu). Synchronises `stream` and returns the
+// device error word in *device_error. cudaErrorInvalidValue when the call's
+// barrier arrivals (nsub x colours x blocks) would reach 2^31.
+int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bool lambdas, uint32_t nsub, float dt,
+                            void* stream, int device, int* device_error);
+
 // Transfer helpers (caller order <-> device order), run on `stream`.
 int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, float* out,
                       void* stream);

@@ -23,6 +23,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "xfem_internal.h"
 
 namespace xfem {
@@ -709,6 +711,70 @@ int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, dou
 	grid = grid > 1024 ? 1024 : grid;
 	k_volume<<<grid, 256, 0, st>>>(vert, tets_dev, nt, out);
 	return (int)cudaGetLastError();
+}
+
+
+// ---- allocation-free stepping ---------------------------------------------------
+// Some callers cannot allocate device memory at the moment they step: a
+// process whose device memory is fully reserved by another allocator (a
+// framework's caching pool), a real-time loop that must not take cudaMalloc's
+// implicit device-wide synchronisation, or code running while a stream is
+// being captured, where cudaMalloc is not permitted. For them the persistent
+// substep kernel is launched with its scratch words (the grid-barrier arrival
+// counter and the device error word) taken from this fixed array instead of
+// buffers of the handle, and without the autotuner or CUDA-graph builder,
+// which may allocate.
+//
+// The array lives in every device that loads the library until the process
+// exits. All calls share it and it keeps the last call's contents, so each
+// call zeroes the words it uses first; calls whose kernels overlap on one GPU
+// would race on it and must not be issued.
+namespace {
+constexpr uint32_t kNoAllocScratchWords = 64;  // 256 bytes; words 0 and 1 are used
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocScratchWords];
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bool lambdas, uint32_t nsub, float dt,
+                            void* stream, int device, int* device_error) {
+	if (device < 0 || device >= kNoAllocMaxDevices) return (int)cudaErrorInvalidDevice;
+	uint32_t* p = nullptr;
+	{
+		// Set-up, once per device, with that device current: the array's name
+		// in host code is a host-side stand-in, so its device address is
+		// looked up and passed to the kernel.
+		std::lock_guard<std::mutex> lk(g_noalloc_mu);
+		if (!g_noalloc_ptr[device]) {
+			const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+			if (e != cudaSuccess) return (int)e;
+			g_noalloc_ptr[device] = p;
+		}
+		p = g_noalloc_ptr[device];
+	}
+	cudaStream_t st = (cudaStream_t)stream;
+	const void* f = lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+	const size_t smem = solve_smem_bytes(block, warp_smem);
+	int sms = 0, per_sm = 0;
+	cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, smem);
+	if (e != cudaSuccess) return (int)e;
+	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
+	const uint32_t blocks = (uint32_t)(per_sm * sms);
+	// the 32-bit arrival counter must not wrap within one call
+	if ((uint64_t)nsub * ctx.ncolours * blocks >= (1ull << 31)) return (int)cudaErrorInvalidValue;
+	e = cudaMemsetAsync(p, 0, 2 * sizeof(uint32_t), st);
+	if (e != cudaSuccess) return (int)e;
+	DevCtx c = ctx;
+	c.bar_count = p;
+	c.err = reinterpret_cast<int*>(p + 1);
+	void* args[] = {&c, &nsub, &dt};
+	e = cudaLaunchCooperativeKernel(f, dim3(blocks), dim3(block), args, smem, st);
+	if (e != cudaSuccess) return (int)e;
+	e = cudaMemcpyAsync(device_error, p + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+	return (int)e;
 }
 
 }  // namespace xfem

@@ -71,6 +71,7 @@ EXPORTS = [
     "xfem_get_lambdas", "xfem_calculate_volume", "xfem_get_rest_state", "xfem_get_schedule",
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
+    "xfem_step_frames_noalloc",
 ]
 
 _lib = None
@@ -105,6 +106,7 @@ def lib():
         L.xfem_substep.argtypes = [P, f32]
         L.xfem_step_frames.argtypes = [P, u32, u32, f32]
         L.xfem_synchronize.argtypes = [P]
+        L.xfem_step_frames_noalloc.argtypes = [P, u32, u32, f32]
         for n in ("xfem_get_positions", "xfem_set_positions", "xfem_get_velocities", "xfem_set_velocities",
                   "xfem_get_inverse_masses", "xfem_get_contacts", "xfem_get_lambdas", "xfem_calculate_volume"):
             getattr(L, n).argtypes = [P, u32, P]
@@ -255,6 +257,11 @@ class Body:
 
     def step_frames(self, frames, substeps, dt):
         _check(lib().xfem_step_frames(self._h, frames, substeps, dt))
+
+    def step_frames_noalloc(self, frames, substeps, dt):
+        """xfem_step_frames_noalloc: the same stepping without any device
+        allocation (see include/xfem.h)."""
+        _check(lib().xfem_step_frames_noalloc(self._h, frames, substeps, dt))
 
     def synchronize(self):
         _check(lib().xfem_synchronize(self._h))
