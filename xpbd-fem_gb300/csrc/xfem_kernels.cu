@@ -170,40 +170,38 @@ __device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body)
 	        __ldg(&b->energy), __ldg(&b->simultaneous)};
 }
 
-// Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with
-// adjugate :284-300, F :311-323, gradient :338-354). Returns U1 = (J - a)^2
-// and the gradient of the three free nodes (g[3] = -sum).
+// Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with the
+// adjugate :284-300, F :311-323 and the gradient :338-354). With F = Qi Ds,
+// where the rows of Ds are P0, P1, P2, J = det(Qi) P0 . (P1 x P2) and the
+// reference's gradient (2 (J - a) adj(F) Qi) e_n equals 2 (J - a) det(Qi)
+// times the cofactor row of Ds: P1 x P2, P2 x P0, P0 x P1. Same quantities,
+// about a third of the arithmetic. Returns U1 = (J - a)^2.
+__device__ __forceinline__ Vec3 cross(Vec3 a, Vec3 b) {
+	return {fmaf(a.y, b.z, -b.y * a.z), fmaf(a.z, b.x, -b.z * a.x), fmaf(a.x, b.y, -b.x * a.y)};
+}
+
 __device__ __forceinline__ float hydrostatic(const float q[3][3], const Vec3 P[3], float a, Vec3 g[4]) {
-	// F[j][r] = sum_n Qi[n][r] * P_n[j]  (F = Qi * Ds, Ds rows = P_n)
-	float F[3][3];
-	const float Pc[3][3] = {{P[0].x, P[1].x, P[2].x}, {P[0].y, P[1].y, P[2].y}, {P[0].z, P[1].z, P[2].z}};
-#pragma unroll
-	for (int j = 0; j < 3; j++)
-#pragma unroll
-		for (int r = 0; r < 3; r++) F[j][r] = fmaf(q[0][r], Pc[j][0], fmaf(q[1][r], Pc[j][1], q[2][r] * Pc[j][2]));
-	float adj[3][3];
-	adj[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
-	adj[0][1] = -(F[0][1] * F[2][2] - F[0][2] * F[2][1]);
-	adj[0][2] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
-	adj[1][0] = -(F[1][0] * F[2][2] - F[1][2] * F[2][0]);
-	adj[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
-	adj[1][2] = -(F[0][0] * F[1][2] - F[0][2] * F[1][0]);
-	adj[2][0] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
-	adj[2][1] = -(F[0][0] * F[2][1] - F[0][1] * F[2][0]);
-	adj[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
-	const float J = fmaf(F[0][0], adj[0][0], fmaf(F[0][1], adj[1][0], F[0][2] * adj[2][0]));
+	const float detQ = fmaf(q[0][0], fmaf(q[1][1], q[2][2], -q[2][1] * q[1][2]),
+	                        fmaf(-q[1][0], fmaf(q[0][1], q[2][2], -q[2][1] * q[0][2]),
+	                             q[2][0] * fmaf(q[0][1], q[1][2], -q[1][1] * q[0][2])));
+	const Vec3 c0 = cross(P[1], P[2]), c1 = cross(P[2], P[0]), c2 = cross(P[0], P[1]);
+	const float J = detQ * dot(P[0], c0);
 	const float Ja = J - a;
-	const float s = 2.0f * Ja;
-	// g_n = column n of (s adj) * Qi: g_n[r] = s * sum_k adj[k][r] Qi[n][k]
-#pragma unroll
-	for (int n = 0; n < 3; n++) {
-		const float gx = fmaf(adj[0][0], q[n][0], fmaf(adj[1][0], q[n][1], adj[2][0] * q[n][2]));
-		const float gy = fmaf(adj[0][1], q[n][0], fmaf(adj[1][1], q[n][1], adj[2][1] * q[n][2]));
-		const float gz = fmaf(adj[0][2], q[n][0], fmaf(adj[1][2], q[n][1], adj[2][2] * q[n][2]));
-		g[n] = {s * gx, s * gy, s * gz};
-	}
+	const float s = 2.0f * Ja * detQ;
+	g[0] = {s * c0.x, s * c0.y, s * c0.z};
+	g[1] = {s * c1.x, s * c1.y, s * c1.z};
+	g[2] = {s * c2.x, s * c2.y, s * c2.z};
 	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
 	return Ja * Ja;
+}
+
+// 1/x to about one ulp: hardware approximation plus one Newton step. The
+// arguments are sums of squares plus 1e-22 (or a clamp at 1e-8), never zero,
+// denormal or infinite.
+__device__ __forceinline__ float rcp(float x) {
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return fmaf(r, fmaf(-x, r, 1.0f), r);
 }
 
 // Deviatoric term, prefactored (XPBDFEM/Fem.cpp:163-192), with the Yeoh
@@ -271,9 +269,9 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 		const float A2 = fmaf(2.0f * U1, alpha1, wdot(w, g1, g1));
 		const float b0 = -2.0f * U0, b1 = -2.0f * U1;
 		// Cramer's rule as in XPBDFEM/Xpbd.h:172-180
-		const float i00 = __frcp_rn(A0), i11 = __frcp_rn(A2);
+		const float i00 = rcp(A0), i11 = rcp(A2);
 		const float r0 = A1 * i00, r1 = A1 * i11;
-		const float inv_det = __frcp_rn(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
+		const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
 		const float c0 = b0 * i00, c1 = b1 * i11;
 		l0 = inv_det * fmaf(-r0, c1, c0);
 		l1 = inv_det * fmaf(-c0, r1, c1);
@@ -284,7 +282,7 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 			D[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), D[n].z);
 		}
 	} else {
-		l0 = (-2.0f * U0) * __frcp_rn(fmaf(2.0f * U0, alpha0, wdot(w, g0, g0)));
+		l0 = (-2.0f * U0) * rcp(fmaf(2.0f * U0, alpha0, wdot(w, g0, g0)));
 #pragma unroll
 		for (int n = 0; n < 4; n++) {
 			const float s = w[n] * l0;
@@ -297,7 +295,7 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 			P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
 			        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
 		const float U1 = hydrostatic(q, P, bp.a, g1);
-		l1 = (-2.0f * U1) * __frcp_rn(fmaf(2.0f * U1, alpha1, wdot(w, g1, g1)));
+		l1 = (-2.0f * U1) * rcp(fmaf(2.0f * U1, alpha1, wdot(w, g1, g1)));
 #pragma unroll
 		for (int n = 0; n < 4; n++) {
 			const float s = w[n] * l1;
@@ -320,12 +318,18 @@ __device__ __forceinline__ void mbar_init(uint64_t* m) {
 }
 
 // Issued by one lane: expect `bytes` on the barrier and start the copy.
+// The chunk records stream through L2 once per substep (about as large as
+// L2); they are fetched with an evict-first policy so that they do not push
+// the small, hot vertex state out of L2.
 __device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+	uint64_t policy;
+	asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
 	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
 	asm volatile(
-	    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
-	    "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+	    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+	        smem_u32(dst)),
+	    "l"(src), "r"(bytes), "r"(smem_u32(mbar)), "l"(policy)
 	    : "memory");
 }
 
