@@ -301,6 +301,15 @@ int build_device(xfem_body* h) {
 			}
 			hdr[lane] = nvv | (ntt << 4) | (L.body << 8);
 		}
+		// the register-resident cube path needs every lane to be a canonical cube
+		static const uint32_t kCube[6] = {0x3210u, 0x1430u, 0x3450u, 0x5630u, 0x3670u, 0x7230u};
+		bool cube = ntm == 6 && nvm == 8;
+		for (uint32_t lane = 0; cube && lane < chunk_lanes[k].size(); lane++) {
+			if ((hdr[lane] & 0xffu) != (8u | (6u << 4))) cube = false;
+			for (uint32_t t = 0; cube && t < 6; t++)
+				if (slot[(size_t)t * kLanes + lane] != kCube[t]) cube = false;
+		}
+		if (cube) meta[k].shape |= kShapeCube;
 	}
 	std::vector<uint32_t> orphans;
 	for (uint32_t v = 0; v < nverts; v++)

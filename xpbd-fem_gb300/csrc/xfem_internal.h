@@ -75,9 +75,13 @@ struct BodyParams {
 struct ChunkMeta {
 	uint32_t off16;  // block offset in 16-byte units
 	uint32_t bytes;  // block size (a multiple of 128)
-	uint32_t shape;  // ntmax | nvmax << 8
+	uint32_t shape;  // ntmax | nvmax << 8 | kShapeCube
 	uint32_t trow;   // first global tet row (multiplier output)
 };
+
+// Chunk flag: every populated lane is a whole 6-tet cube in the generator's
+// corner order, i.e. local slots {0123, 0341, 0543, 0365, 0763, 0327}.
+constexpr uint32_t kShapeCube = 1u << 16;
 
 inline uint32_t chunk_block_bytes(uint32_t ntmax, uint32_t nvmax) { return 2048u * ntmax + 128u * (1u + nvmax + ntmax); }
 

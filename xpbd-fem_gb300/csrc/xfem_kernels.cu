@@ -397,6 +397,67 @@ __device__ __forceinline__ bool stage_acquire(const DevCtx& C, Stage& st, uint32
 	return ok;
 }
 
+// Chunks whose clusters are all whole cubes of the 6-tet split in the
+// generator's corner order (every configuration mesh) share one local
+// topology, so the 8 vertices stay in registers and the 6 solves unroll with
+// compile-time slots: no shared-memory round trip inside the sequential chain.
+// Local slot k of tet t: {0123, 0341, 0543, 0365, 0763, 0327}, packed four bits per slot.
+__host__ __device__ constexpr int cube_slot(int t, int k) {
+	return (int)(((t == 0   ? 0x3210u
+	               : t == 1 ? 0x1430u
+	               : t == 2 ? 0x3450u
+	               : t == 3 ? 0x5630u
+	               : t == 4 ? 0x3670u
+	                        : 0x7230u) >>
+	              (4 * k)) &
+	             15u);
+}
+
+template <bool LAMBDAS>
+__device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, int phase, float dt,
+                                               float inv_dt, float inv_dt2, uint32_t trow) {
+	const float4* rec = reinterpret_cast<const float4*>(st.buf);
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
+	const uint32_t* vids = hdrs + kLanes;
+	const uint32_t hdr = hdrs[lane];
+	const bool live = (hdr & 15u) != 0;
+	uint32_t vid[8];
+	float4 O[8], D[8];
+	if (live) {
+		const Mat mat = load_mat(C.bodies, hdr >> 8);
+#pragma unroll
+		for (int s = 0; s < 8; s++) vid[s] = vids[s * kLanes + lane];
+#pragma unroll
+		for (int s = 0; s < 8; s++) {
+			O[s] = __ldcg(C.vert + 2 * (size_t)vid[s]);
+			D[s] = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
+		}
+		if (phase != kPhaseSolve) {
+#pragma unroll
+			for (int s = 0; s < 8; s++) advance_vertex(C.bodies, O[s], D[s], phase == kPhasePredict, dt, inv_dt);
+		}
+#pragma unroll
+		for (int t = 0; t < 6; t++) {
+			const float4* r = rec + t * 4 * kLanes + lane;
+			const TetRec tr = {r[0], r[kLanes], r[2 * kLanes], r[3 * kLanes]};
+			const float4 Ot[4] = {O[cube_slot(t, 0)], O[cube_slot(t, 1)], O[cube_slot(t, 2)], O[cube_slot(t, 3)]};
+			float4 Dt[4] = {D[cube_slot(t, 0)], D[cube_slot(t, 1)], D[cube_slot(t, 2)], D[cube_slot(t, 3)]};
+			const float2 lam = solve_tet(mat, tr, inv_dt2, Ot, Dt);
+#pragma unroll
+			for (int k = 0; k < 4; k++) D[cube_slot(t, k)] = Dt[k];
+			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
+		}
+	}
+	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
+	if (live) {
+#pragma unroll
+		for (int s = 0; s < 8; s++) {
+			if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
+			__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
+		}
+	}
+}
+
 // One warp processes one resident chunk; lane = cluster. `next` >= 0 is the
 // warp's next chunk: its copy is issued as soon as this chunk's records have
 // been consumed, so it overlaps the write-back and the following barrier.
@@ -405,6 +466,10 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
                                           float dt, float inv_dt, float inv_dt2) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
+	if (m.z & kShapeCube) {
+		run_chunk_cube<LAMBDAS>(C, st, next, lane, phase, dt, inv_dt, inv_dt2, trow);
+		return;
+	}
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
 	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * ntmax);
 	const uint32_t* vids = hdrs + kLanes;
@@ -510,7 +575,7 @@ __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t 
 // Persistent kernel: nsub substeps x ncolours colour passes separated by the
 // bounded grid barrier. Must be launched cooperatively (co-resident grid).
 template <bool LAMBDAS>
-__global__ void __launch_bounds__(512) k_persistent(DevCtx C, uint32_t nsub, float dt) {
+__global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, float dt) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -548,7 +613,7 @@ __global__ void __launch_bounds__(512) k_persistent(DevCtx C, uint32_t nsub, flo
 // Blocks past the colour's chunks advance orphan vertices when `phase` is not
 // kPhaseSolve.
 template <bool LAMBDAS>
-__global__ void __launch_bounds__(512) k_colour(DevCtx C, uint32_t colour, int phase, float dt,
+__global__ void __launch_bounds__(256) k_colour(DevCtx C, uint32_t colour, int phase, float dt,
                                                 uint32_t solve_blocks) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	if (blockIdx.x >= solve_blocks) {
