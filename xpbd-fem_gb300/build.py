@@ -3,7 +3,7 @@
     python xpbd-fem_gb300/build.py [--force]
 
 Every translation unit is compiled by nvcc in parallel, then linked with
--shared. Host code is compiled with -ffp-contract=off: the rest-state
+-shared. Device code is compiled with -fmad=false (only explicit fmaf() fuses). Host code is compiled with -ffp-contract=off: the rest-state
 precompute must reproduce the reference bit for bit and the schedule must give
 the same integers on x86-64 and AArch64.
 """
@@ -50,6 +50,10 @@ def build(force=False, verbose=False):
         obj = os.path.join(BUILD, src + ".o")
         cmd = [cc] + ARCH + COMMON + ["-c", os.path.join(SRC, src), "-o", obj]
         if src.endswith(".cu"):
+            # Only the explicit fmaf() calls fuse: the same inlined solve then
+            # rounds identically in every kernel that runs it, whatever the
+            # surrounding code lets the compiler hoist or contract.
+            cmd += ["-fmad=false"]
             cmd += ["-Xptxas", "-v"] if verbose else []
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode:
