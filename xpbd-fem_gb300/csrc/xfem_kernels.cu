@@ -171,11 +171,13 @@ __device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body)
 }
 
 // Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with the
-// adjugate :284-300, F :311-323 and the gradient :338-354). With F = Qi Ds,
-// where the rows of Ds are P0, P1, P2, J = det(Qi) P0 . (P1 x P2) and the
-// reference's gradient (2 (J - a) adj(F) Qi) e_n equals 2 (J - a) det(Qi)
-// times the cofactor row of Ds: P1 x P2, P2 x P0, P0 x P1. Same quantities,
-// about a third of the arithmetic. Returns U1 = (J - a)^2.
+// adjugate :284-300, F :311-323 and the gradient :338-354). J is formed as
+// the reference forms it, det(F) of F = Qi Ds (rows of Ds: P0, P1, P2) through
+// the first adjugate column: with an incompressible material the multiplier
+// goes as 1 / (J - a), so J's rounding decides the result and must follow the
+// reference's path. The gradient (2 (J - a) adj(F) Qi) e_n equals
+// 2 (J - a) det(Qi) times the cofactor row of Ds (P1 x P2, P2 x P0, P0 x P1):
+// same quantity, a third of the arithmetic. Returns U1 = (J - a)^2.
 __device__ __forceinline__ Vec3 cross(Vec3 a, Vec3 b) {
 	return {fmaf(a.y, b.z, -b.y * a.z), fmaf(a.z, b.x, -b.z * a.x), fmaf(a.x, b.y, -b.x * a.y)};
 }
@@ -185,7 +187,17 @@ __device__ __forceinline__ float hydrostatic(const float q[3][3], const Vec3 P[3
 	                        fmaf(-q[1][0], fmaf(q[0][1], q[2][2], -q[2][1] * q[0][2]),
 	                             q[2][0] * fmaf(q[0][1], q[1][2], -q[1][1] * q[0][2])));
 	const Vec3 c0 = cross(P[1], P[2]), c1 = cross(P[2], P[0]), c2 = cross(P[0], P[1]);
-	const float J = detQ * dot(P[0], c0);
+	// F[j][r] = sum_n Qi[n][r] P_n[j] (column j, row r)
+	const float Pc[3][3] = {{P[0].x, P[1].x, P[2].x}, {P[0].y, P[1].y, P[2].y}, {P[0].z, P[1].z, P[2].z}};
+	float F[3][3];
+#pragma unroll
+	for (int j = 0; j < 3; j++)
+#pragma unroll
+		for (int r = 0; r < 3; r++) F[j][r] = fmaf(q[0][r], Pc[j][0], fmaf(q[1][r], Pc[j][1], q[2][r] * Pc[j][2]));
+	const float a00 = fmaf(F[1][1], F[2][2], -F[1][2] * F[2][1]);
+	const float a10 = -fmaf(F[1][0], F[2][2], -F[1][2] * F[2][0]);
+	const float a20 = fmaf(F[1][0], F[2][1], -F[1][1] * F[2][0]);
+	const float J = fmaf(F[0][0], a00, fmaf(F[0][1], a10, F[0][2] * a20));
 	const float Ja = J - a;
 	const float s = 2.0f * Ja * detQ;
 	g[0] = {s * c0.x, s * c0.y, s * c0.z};
