@@ -46,9 +46,10 @@ UNIT = "tet-substeps/s"
 # QR, volume) + 76 B per vertex per substep (X, V, O read/write 24 B each,
 # w 4 B) x V/T.
 REC_BYTES, VERT_BYTES = 80.0, 76.0
-# DRAM bytes per tet-substep of the persistent kernel from the ncu capture
-# summarised in profiles/ (None until a capture exists).
-NCU_DRAM_BYTES_PER_TET_SUBSTEP = None
+# DRAM bytes (read + write) per tet-substep of the persistent kernel, from the
+# ncu capture summarised in profiles/k_persistent_throughput_128x64x32.md
+# (2.311 GB per launch of 20 substeps x 1,572,864 tets).
+NCU_DRAM_BYTES_PER_TET_SUBSTEP = 73.47
 
 
 def peaks():
