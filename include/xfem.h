@@ -88,7 +88,8 @@ typedef struct xfem_settings {
 typedef struct xfem_options {
 	uint32_t cluster_mode; /* 0 = default (edge-star clusters), 1 = one tet per cluster, 2 = edge-star */
 	uint32_t no_morton;    /* 1 = keep the caller's vertex order on the device */
-	uint32_t sync_mode;    /* 0 = auto (autotuned), 1 = persistent kernel + grid barrier, 2 = CUDA graph */
+	uint32_t sync_mode;    /* 0 = auto (autotuned), 1 = persistent kernel + grid barrier, 2 = CUDA graph,
+	                          3 = persistent kernel, chunks wait only on neighbouring chunks (dataflow) */
 	uint32_t block_size;   /* 0 = auto; else 64..1024, multiple of 32 */
 	uint32_t keep_lambdas; /* 1 = record each tet's two multipliers of the last substep */
 	int32_t device;        /* CUDA device ordinal; -1 or 0 = current / 0 */
@@ -105,8 +106,13 @@ typedef struct xfem_mesh {
 } xfem_mesh;
 
 typedef struct xfem_info {
-	uint32_t bodies, vertices, tets, clusters, colours, orphans;
-	uint32_t chunks, tet_rows, block_size, blocks, sync_mode, cluster_mode;
+	uint32_t bodies, vertices, tets, clusters, colours;
+	uint32_t isolated;        /* vertices in no tet */
+	uint32_t chunks, tet_rows, block_size, blocks;
+	uint32_t sync_mode;       /* 1 persistent + grid barrier, 2 CUDA graph, 3 persistent dataflow */
+	uint32_t cluster_mode;    /* 1 one tet per cluster, 2 edge stars */
+	uint32_t max_chunk_deps;  /* largest neighbour-chunk list (dataflow mode) */
+	uint32_t reserved;
 	uint64_t device_bytes;
 } xfem_info;
 

@@ -69,7 +69,7 @@ struct xfem_body {
 	uint32_t nverts = 0, ntets = 0, nchunks = 0, nrows = 0, nvrows = 0, ncolours = 0;
 	// device buffers
 	DevBuf<float4> vert, cblk;
-	DevBuf<uint32_t> ccb, orphans, dev_of_vert, tets_dev, bar;
+	DevBuf<uint32_t> ccb, isolated, dev_of_vert, tets_dev, bar, dep_begin, deps, done;
 	DevBuf<ChunkMeta> chunks;
 	DevBuf<BodyParams> params;
 	DevBuf<float2> tlam;
@@ -77,7 +77,7 @@ struct xfem_body {
 	DevBuf<float> stage;
 	DevBuf<double> vol;
 	std::vector<float4> cblk_host;  // kept to refresh c0 after material changes
-	uint32_t norphans = 0;
+	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
 	bool tuned = false;
@@ -208,7 +208,7 @@ int build_device(xfem_body* h) {
 		ntets += b.nt;
 		ncol = std::max(ncol, b.sched.ncolours);
 	}
-	if (nb >= (1u << 24)) return fail(XFEM_ELIMIT, "too many bodies");
+	if (nb >= (1u << 16)) return fail(XFEM_ELIMIT, "too many bodies (at most 65535 per handle)");
 	h->nverts = nverts;
 	h->ntets = ntets;
 	h->ncolours = ncol;
@@ -259,13 +259,14 @@ int build_device(xfem_body* h) {
 	h->nchunks = nch;
 	h->nrows = trows;
 	std::vector<float4> cblk((size_t)total16, make_float4(0, 0, 0, 0));
-	std::vector<uint8_t> in_colour0(nverts, 0);
+	// owner of each vertex: the first (lowest-colour) cluster that touches it
+	std::vector<uint32_t> owner(nverts, 0xffffffffu);
+	std::vector<std::vector<uint32_t>> vert_chunks(nverts);
 	for (auto& b : h->bodies) {
 		b.tet_slot.assign(b.nt, 0xffffffffu);
 		b.tet_rec.assign(b.nt, 0);
 	}
 	for (uint32_t k = 0; k < nch; k++) {
-		const bool colour0 = k < ccb[1];
 		const uint32_t ntm = shape_nt[k], nvm = shape_nv[k];
 		float4* rec = &cblk[meta[k].off16];
 		uint32_t* hdr = reinterpret_cast<uint32_t*>(rec + 128 * (size_t)ntm);
@@ -294,12 +295,17 @@ int build_device(xfem_body* h) {
 				r[3 * kLanes] = make_float4(e[12], e[13], e[14], tet_c0(b, t));
 				b.tet_rec[t] = meta[k].off16 + ((size_t)ntt * 4 + 3) * kLanes + lane;
 			}
+			uint32_t mask = 0;
 			for (uint32_t s = 0; s < nvv; s++) {
 				const uint32_t dv = b.vbase + b.sched.vert_rank[vs[s]];
 				vid[(size_t)s * kLanes + lane] = dv;
-				if (colour0) in_colour0[dv] = 1;
+				if (owner[dv] == 0xffffffffu) {
+					owner[dv] = k * kLanes + lane;
+					mask |= 1u << s;
+				}
+				if (vert_chunks[dv].empty() || vert_chunks[dv].back() != k) vert_chunks[dv].push_back(k);
 			}
-			hdr[lane] = nvv | (ntt << 4) | (L.body << 8);
+			hdr[lane] = nvv | (ntt << 4) | (mask << 8) | (L.body << 16);
 		}
 		// the register-resident cube path needs every lane to be a canonical cube
 		static const uint32_t kCube[6] = {0x3210u, 0x1430u, 0x3450u, 0x5630u, 0x3670u, 0x7230u};
@@ -311,10 +317,31 @@ int build_device(xfem_body* h) {
 		}
 		if (cube) meta[k].shape |= kShapeCube;
 	}
-	std::vector<uint32_t> orphans;
+	std::vector<uint32_t> isolated;
 	for (uint32_t v = 0; v < nverts; v++)
-		if (!in_colour0[v]) orphans.push_back(v);
-	h->norphans = (uint32_t)orphans.size();
+		if (owner[v] == 0xffffffffu) isolated.push_back(v);
+	h->nisolated = (uint32_t)isolated.size();
+	// dataflow dependencies: chunks of other colours sharing a vertex
+	std::vector<uint32_t> chunk_colour(nch), dep_begin(nch + 1, 0), deps;
+	for (uint32_t c = 0; c < ncol; c++)
+		for (uint32_t k = ccb[c]; k < ccb[c + 1]; k++) chunk_colour[k] = c;
+	{
+		std::vector<std::vector<uint32_t>> dl(nch);
+		for (uint32_t v = 0; v < nverts; v++)
+			for (uint32_t a : vert_chunks[v])
+				for (uint32_t b2 : vert_chunks[v])
+					if (a != b2) dl[a].push_back(b2);
+		uint32_t maxd = 0;
+		for (uint32_t k = 0; k < nch; k++) {
+			std::sort(dl[k].begin(), dl[k].end());
+			dl[k].erase(std::unique(dl[k].begin(), dl[k].end()), dl[k].end());
+			dep_begin[k] = (uint32_t)deps.size();
+			for (uint32_t j : dl[k]) deps.push_back(j | (chunk_colour[j] < chunk_colour[k] ? 0x80000000u : 0u));
+			maxd = std::max(maxd, (uint32_t)dl[k].size());
+		}
+		dep_begin[nch] = (uint32_t)deps.size();
+		h->max_deps = maxd;
+	}
 	// vertex state: canonical (X, V) = (rest, 0); bits = lock | body << 8
 	std::vector<float4> vert(2 * (size_t)nverts);
 	std::vector<uint32_t> dev_of(nverts), tets_dev(4 * (size_t)ntets);
@@ -337,7 +364,10 @@ int build_device(xfem_body* h) {
 	XCUDA(h->vert.alloc(vert.size()));
 	XCUDA(h->cblk.alloc(cblk.size()));
 	XCUDA(h->ccb.alloc(ccb.size()));
-	XCUDA(h->orphans.alloc(orphans.size()));
+	XCUDA(h->isolated.alloc(isolated.size()));
+	XCUDA(h->dep_begin.alloc(dep_begin.size()));
+	XCUDA(h->deps.alloc(deps.size()));
+	XCUDA(h->done.alloc(nch));
 	XCUDA(h->dev_of_vert.alloc(dev_of.size()));
 	XCUDA(h->tets_dev.alloc(tets_dev.size()));
 	XCUDA(h->chunks.alloc(meta.size()));
@@ -355,7 +385,9 @@ int build_device(xfem_body* h) {
 	XCUDA(up(h->vert.p, vert.data(), vert.size() * sizeof(float4)));
 	XCUDA(up(h->cblk.p, cblk.data(), cblk.size() * sizeof(float4)));
 	XCUDA(up(h->ccb.p, ccb.data(), ccb.size() * 4));
-	XCUDA(up(h->orphans.p, orphans.data(), orphans.size() * 4));
+	XCUDA(up(h->isolated.p, isolated.data(), isolated.size() * 4));
+	XCUDA(up(h->dep_begin.p, dep_begin.data(), dep_begin.size() * 4));
+	XCUDA(up(h->deps.p, deps.data(), deps.size() * 4));
 	XCUDA(up(h->dev_of_vert.p, dev_of.data(), dev_of.size() * 4));
 	XCUDA(up(h->tets_dev.p, tets_dev.data(), tets_dev.size() * 4));
 	XCUDA(up(h->chunks.p, meta.data(), meta.size() * sizeof(ChunkMeta)));
@@ -363,8 +395,8 @@ int build_device(xfem_body* h) {
 	XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
 	if (h->tlam.p) XCUDA(cudaMemsetAsync(h->tlam.p, 0, h->tlam.n * sizeof(float2), h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
-	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + orphans.size() + dev_of.size() +
-	                  tets_dev.size()) * 4 + meta.size() * 16 + params.size() * 64 + h->stage.n * 4 + h->tlam.n * 8;
+	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + isolated.size() + dev_of.size() +
+	                  tets_dev.size() + dep_begin.size() + deps.size() + nch) * 4 + meta.size() * 16 + params.size() * 64 + h->stage.n * 4 + h->tlam.n * 8;
 	h->cblk_host.swap(cblk);
 	DevCtx& c = h->ctx;
 	c.vert = h->vert.p;
@@ -374,10 +406,14 @@ int build_device(xfem_body* h) {
 	c.tlam = h->tlam.p;
 	c.chunks = h->chunks.p;
 	c.colour_chunk_begin = h->ccb.p;
-	c.orphans = h->orphans.p;
+	c.isolated = h->isolated.p;
+	c.dep_begin = h->dep_begin.p;
+	c.deps = h->deps.p;
+	c.done = h->done.p;
+	c.nchunks = nch;
 	c.bodies = h->params.p;
 	c.nverts = nverts;
-	c.norphans = h->norphans;
+	c.nisolated = h->nisolated;
 	c.ncolours = ncol;
 	c.bar_count = h->bar.p;
 	c.err = h->err.p;
@@ -399,7 +435,7 @@ int set_config(xfem_body* h, int sync_mode, int block) {
 	h->cfg.block = block;
 	if (const int ek = configure_kernels(h->cfg))
 		return fail(XFEM_ECUDA, std::string("kernel configuration: ") + cudaGetErrorString((cudaError_t)ek));
-	if (sync_mode == 1) {
+	if (sync_mode == 1 || sync_mode == 3) {
 		int blocks = 0;
 		const int e = persistent_grid(h->cfg, &blocks);
 		if (e) return fail(XFEM_ECUDA, std::string("occupancy query failed: ") + cudaGetErrorString((cudaError_t)e));
@@ -413,7 +449,7 @@ int set_config(xfem_body* h, int sync_mode, int block) {
 }
 
 int run(xfem_body* h, uint32_t nsub, float dt) {
-	if (h->cfg.sync_mode == 1) {
+	if (h->cfg.sync_mode == 1 || h->cfg.sync_mode == 3) {
 		const int e = launch_substeps(h->ctx, h->cfg, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("persistent launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
@@ -447,7 +483,7 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	const int fixed_sync = (int)h->opt.sync_mode, fixed_block = (int)h->opt.block_size;
 	std::vector<std::pair<int, int>> cand;
 	const int blocks[] = {64, 128, 256};
-	for (int sm : {1, 2}) {
+	for (int sm : {1, 2, 3}) {
 		if (fixed_sync && sm != fixed_sync) continue;
 		for (int bs : blocks) {
 			if (fixed_block && bs != fixed_block) continue;
@@ -499,7 +535,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (options) h->opt = *options;
 	if (h->opt.block_size && (h->opt.block_size < 64 || h->opt.block_size > 1024 || h->opt.block_size % 32))
 		return fail(XFEM_EINVAL, "block_size must be a multiple of 32 in [64, 1024]");
-	if (h->opt.sync_mode > 2) return fail(XFEM_EINVAL, "sync_mode must be 0, 1 or 2");
+	if (h->opt.sync_mode > 3) return fail(XFEM_EINVAL, "sync_mode must be 0, 1, 2 or 3");
 	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
 	const uint32_t mode = h->opt.cluster_mode == 1 ? 0u : 1u;
 	const uint32_t morton = h->opt.no_morton ? 0u : 1u;
@@ -643,9 +679,9 @@ int xfem_get_info(const xfem_body* b, xfem_info* out) {
 	if (!b || !out) return fail(XFEM_EINVAL, "null argument");
 	uint32_t ncl = 0;
 	for (auto& x : b->bodies) ncl += x.sched.nclusters;
-	*out = {(uint32_t)b->bodies.size(), b->nverts, b->ntets, ncl, b->ncolours, b->norphans,
+	*out = {(uint32_t)b->bodies.size(), b->nverts, b->ntets, ncl, b->ncolours, b->nisolated,
 	        b->nchunks, b->nrows, (uint32_t)b->cfg.block, (uint32_t)b->cfg.blocks, (uint32_t)b->cfg.sync_mode,
-	        b->opt.cluster_mode == 1 ? 1u : 2u, b->device_bytes};
+	        b->opt.cluster_mode == 1 ? 1u : 2u, b->max_deps, 0u, b->device_bytes};
 	return XFEM_OK;
 }
 

@@ -69,7 +69,10 @@ struct BodyParams {
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
 //   records  ntmax rows x 4 planes x 32 lanes x float4 (Qi, QQ, QR, c0)
-//   header   32 x u32: nv | nt << 4 | body << 8
+//   header   32 x u32: nv | nt << 4 | advance mask << 8 | body << 16
+//            (mask bit s: this cluster owns vertex slot s, i.e. it is the
+//            lowest-colour cluster touching it, and so finalizes the previous
+//            substep and predicts the next one for that vertex)
 //   vids     nvmax rows x 32 x u32 (device vertex ids)
 //   slots    ntmax rows x 32 x u32 (4 x 4-bit local vertex slots per tet)
 struct ChunkMeta {
@@ -92,9 +95,12 @@ struct DevCtx {
 	float2* tlam;               // [trow][lane] multipliers or null
 	const ChunkMeta* chunks;
 	const uint32_t* colour_chunk_begin;  // ncolours + 1
-	const uint32_t* orphans;    // vertices outside every colour-0 cluster
+	const uint32_t* isolated;   // vertices in no tet (stepped on their own)
 	const BodyParams* bodies;
-	uint32_t nverts, norphans, ncolours;
+	const uint32_t* dep_begin;  // per chunk, into deps (dataflow mode)
+	const uint32_t* deps;       // neighbour chunk | 1 << 31 when its colour is lower
+	uint32_t* done;             // per chunk: substeps completed in this launch
+	uint32_t nverts, nisolated, ncolours, nchunks;
 	uint32_t chunk_smem;        // bytes of the largest chunk block
 	uint32_t warp_smem;         // chunk_smem + vertex slots (2 x nvmax x 32 x 16 B)
 	uint32_t* bar_count;        // grid barrier arrival counter
@@ -108,12 +114,13 @@ constexpr uint32_t kFlagContact = 2u;
 // Device error codes written to DevCtx::err.
 constexpr int kErrBarrierTimeout = 1;
 constexpr int kErrCopyTimeout = 2;
+constexpr int kErrDepTimeout = 3;
 
 // ---- kernel launchers (xfem_kernels.cu) ---------------------------------------
 struct LaunchCfg {
 	int block = 256;
 	int blocks = 0;        // persistent grid size
-	int sync_mode = 1;     // 1 persistent, 2 graph-style per-colour launches
+	int sync_mode = 1;     // 1 persistent + grid barrier, 2 per-colour launches (CUDA graph), 3 persistent dataflow
 	bool lambdas = false;
 	uint32_t warp_smem = 0;
 	uint32_t total_chunks = 0;

@@ -14,11 +14,11 @@
 // per-lane load of a warp is one contiguous 128- or 512-byte run.
 //
 // Substep schedule (Geo3d::Substep, XPBDFEM/Geo.cpp:305-356, restated):
-//   colour 0 : for each vertex of a colour-0 cluster (and every orphan vertex)
-//              finalize the previous substep (locks, ground, V = D/dt,
-//              O += D) and predict this one (V += g dt, V *= 1 - drag,
-//              D = V dt); then solve the cluster
-//   colour c : solve
+//   each colour pass: every cluster first advances the vertices it owns (it is
+//              the lowest-colour cluster touching them): finalize the
+//              previous substep (locks, ground, V = D/dt, O += D) and predict
+//              this one (V += g dt, V *= 1 - drag, D = V dt); then it solves
+//              its tets in sequence
 //   end      : finalize the last substep back to (X, V)
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -319,7 +319,6 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 	return make_float2(l0, l1);
 }
 
-enum Phase : int { kPhaseSolve = 0, kPhasePredict = 1, kPhaseAdvance = 2 };
 
 // ---- chunk staging: one TMA bulk copy per chunk into the warp's buffer ----
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -394,6 +393,12 @@ __device__ __forceinline__ void stage_issue(const DevCtx& C, Stage& st, uint32_t
 	st.inflight = (int)chunk;
 }
 
+// Starts the copy of `chunk` when the buffer is idle (dataflow mode issues it
+// before waiting on neighbours: records never depend on them).
+__device__ __forceinline__ void stage_issue_or_wait(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	if (st.inflight < 0) stage_issue(C, st, chunk, lane);
+}
+
 // Makes `chunk` resident in the warp's buffer. Returns false on timeout.
 __device__ __forceinline__ bool stage_acquire(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
 	if (st.inflight != (int)chunk) {
@@ -425,18 +430,23 @@ __host__ __device__ constexpr int cube_slot(int t, int k) {
 	             15u);
 }
 
+// Header word of a cluster lane: nv | nt << 4 | advance mask << 8 | body << 16.
+// A vertex is advanced (previous substep finalized, next one predicted) by
+// the lowest-colour cluster touching it, just before that cluster's solve.
+
 template <bool LAMBDAS>
-__device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, int phase, float dt,
+__device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first, float dt,
                                                float inv_dt, float inv_dt2, uint32_t trow) {
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
 	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
 	const uint32_t* vids = hdrs + kLanes;
 	const uint32_t hdr = hdrs[lane];
 	const bool live = (hdr & 15u) != 0;
+	const uint32_t mask = (hdr >> 8) & 0xffu;
 	uint32_t vid[8];
 	float4 O[8], D[8];
 	if (live) {
-		const Mat mat = load_mat(C.bodies, hdr >> 8);
+		const Mat mat = load_mat(C.bodies, hdr >> 16);
 #pragma unroll
 		for (int s = 0; s < 8; s++) vid[s] = vids[s * kLanes + lane];
 #pragma unroll
@@ -444,10 +454,9 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 			O[s] = __ldcg(C.vert + 2 * (size_t)vid[s]);
 			D[s] = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
 		}
-		if (phase != kPhaseSolve) {
 #pragma unroll
-			for (int s = 0; s < 8; s++) advance_vertex(C.bodies, O[s], D[s], phase == kPhasePredict, dt, inv_dt);
-		}
+		for (int s = 0; s < 8; s++)
+			if (mask & (1u << s)) advance_vertex(C.bodies, O[s], D[s], first, dt, inv_dt);
 #pragma unroll
 		for (int t = 0; t < 6; t++) {
 			const float4* r = rec + t * 4 * kLanes + lane;
@@ -464,7 +473,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 	if (live) {
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
-			if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
+			if (mask & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
 			__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
 		}
 	}
@@ -472,14 +481,14 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 
 // One warp processes one resident chunk; lane = cluster. `next` >= 0 is the
 // warp's next chunk: its copy is issued as soon as this chunk's records have
-// been consumed, so it overlaps the write-back and the following barrier.
+// been consumed, so it overlaps the write-back and what follows.
 template <bool LAMBDAS>
-__device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, int phase,
+__device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, bool first,
                                           float dt, float inv_dt, float inv_dt2) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
-		run_chunk_cube<LAMBDAS>(C, st, next, lane, phase, dt, inv_dt, inv_dt2, trow);
+		run_chunk_cube<LAMBDAS>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow);
 		return;
 	}
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
@@ -487,12 +496,12 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 	const uint32_t* vids = hdrs + kLanes;
 	const uint32_t* slots = vids + kLanes * nvmax;
 	const uint32_t hdr = hdrs[lane];
-	const uint32_t nv = hdr & 15u, nt = (hdr >> 4) & 15u;
+	const uint32_t nv = hdr & 15u, nt = (hdr >> 4) & 15u, mask = (hdr >> 8) & 0xffu;
 	float4* sO = st.vs + lane;
 	float4* sD = st.vs + kLanes * nvmax + lane;
 	uint32_t vid[kMaxClusterVerts];
 	if (nv) {
-		const Mat mat = load_mat(C.bodies, hdr >> 8);
+		const Mat mat = load_mat(C.bodies, hdr >> 16);
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++)
 			if (s < nv) vid[s] = vids[s * kLanes + lane];
@@ -501,7 +510,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			if (s < nv) {
 				float4 O = __ldcg(C.vert + 2 * (size_t)vid[s]);
 				float4 D = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
-				if (phase != kPhaseSolve) advance_vertex(C.bodies, O, D, phase == kPhasePredict, dt, inv_dt);
+				if (mask & (1u << s)) advance_vertex(C.bodies, O, D, first, dt, inv_dt);
 				sO[s * kLanes] = O;
 				sD[s * kLanes] = D;
 			}
@@ -521,25 +530,27 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
 		}
 	}
-	(void)ntmax;
 	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
 	if (nv) {
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
-				if (phase != kPhaseSolve) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * kLanes]);
+				if (mask & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * kLanes]);
 				__stcg(C.vert + 2 * (size_t)vid[s] + 1, sD[s * kLanes]);
 			}
 		}
 	}
 }
 
-__device__ __forceinline__ void run_orphans(const DevCtx& C, uint32_t begin, uint32_t step, bool first, float dt,
-                                            float inv_dt) {
-	for (uint32_t i = begin; i < C.norphans; i += step) {
-		const uint32_t v = __ldg(C.orphans + i);
+// Vertices in no tet: nothing else touches them, so one thread takes each
+// through all nsub substeps at once (predict, then finalize + predict); the
+// final finalize pass closes the last one.
+__device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, uint32_t step, uint32_t nsub, float dt,
+                                             float inv_dt) {
+	for (uint32_t i = begin; i < C.nisolated; i += step) {
+		const uint32_t v = __ldg(C.isolated + i);
 		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
-		advance_vertex(C.bodies, O, D, first, dt, inv_dt);
+		for (uint32_t s = 0; s < nsub; s++) advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
 		__stcg(C.vert + 2 * (size_t)v, O);
 		__stcg(C.vert + 2 * (size_t)v + 1, D);
 	}
@@ -595,21 +606,20 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 	Stage st = stage_init(C, lane);
+	run_isolated(C, gtid, nthreads, nsub, dt, inv_dt);
 	uint32_t target = 0;
 	bool ok = true;
 	for (uint32_t s = 0; s < nsub && ok; s++) {
 		for (uint32_t c = 0; c < C.ncolours && ok; c++) {
-			const int phase = c == 0 ? (s == 0 ? kPhasePredict : kPhaseAdvance) : kPhaseSolve;
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				if (!stage_acquire(C, st, ch, lane)) {
 					ok = false;
 					break;
 				}
-				run_chunk<LAMBDAS>(C, st, ch, next_chunk(C, s, nsub, c, ch, gwarp, nwarps), lane, phase, dt, inv_dt,
+				run_chunk<LAMBDAS>(C, st, ch, next_chunk(C, s, nsub, c, ch, gwarp, nwarps), lane, s == 0, dt, inv_dt,
 				                   inv_dt2);
 			}
-			if (c == 0) run_orphans(C, gtid, nthreads, s == 0, dt, inv_dt);
 			if (!grid_sync(C, target)) ok = false;
 		}
 	}
@@ -621,16 +631,100 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	run_finalize(C, gtid, nthreads, inv_dt);
 }
 
-// One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
-// Blocks past the colour's chunks advance orphan vertices when `phase` is not
-// kPhaseSolve.
+__device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait until every neighbour chunk of `ch` has done its share of
+// substep s: chunks of a lower colour must have completed s + 1 substeps,
+// chunks of a higher colour s substeps (the previous one). One lane per
+// neighbour; false (and the error word set) on timeout.
+__device__ bool wait_deps(const DevCtx& C, uint32_t ch, uint32_t s, uint32_t lane) {
+	const uint32_t b = __ldg(C.dep_begin + ch), e = __ldg(C.dep_begin + ch + 1);
+	bool ok = true;
+	for (uint32_t i = b + lane; i < e && ok; i += kLanes) {
+		const uint32_t d = __ldg(C.deps + i);
+		const uint32_t need = s + (d >> 31);
+		if (need == 0) continue;
+		const uint32_t* f = C.done + (d & 0x7fffffffu);
+		uint32_t spins = 0;
+		uint64_t t0 = 0;
+		while (ld_acquire_gpu(f) < need) {
+			if (++spins == 64) {
+				spins = 0;
+				if (*(volatile int*)C.err) {
+					ok = false;
+					break;
+				}
+				const uint64_t t = global_ns();
+				if (t0 == 0) {
+					t0 = t;
+				} else if (t - t0 > kBarrierTimeoutNs) {
+					atomicCAS(C.err, 0, kErrDepTimeout);
+					ok = false;
+					break;
+				}
+			}
+		}
+	}
+	return __all_sync(0xffffffffu, ok);
+}
+
+// Persistent dataflow kernel: the same chunk sequence per warp as
+// k_persistent, but a chunk waits only for the neighbouring chunks it shares
+// vertices with (per-chunk completion counters) instead of a grid barrier per
+// colour. Every dependency points to an earlier (substep, colour) item and each
+// warp walks its items in that order, so with a co-resident grid the earliest
+// unfinished item can always run: no deadlock. One grid barrier ends the
+// launch before the final finalize pass.
 template <bool LAMBDAS>
-__global__ void __launch_bounds__(256) k_colour(DevCtx C, uint32_t colour, int phase, float dt,
-                                                uint32_t solve_blocks) {
+__global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float dt) {
+	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
+	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	Stage st = stage_init(C, lane);
+	run_isolated(C, gtid, nthreads, nsub, dt, inv_dt);
+	bool ok = true;
+	for (uint32_t s = 0; s < nsub && ok; s++) {
+		for (uint32_t c = 0; c < C.ncolours && ok; c++) {
+			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
+			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
+				const int next = next_chunk(C, s, nsub, c, ch, gwarp, nwarps);
+				if (st.inflight != (int)ch) stage_issue_or_wait(C, st, ch, lane);  // records do not depend on neighbours
+				if (!wait_deps(C, ch, s, lane) || !stage_acquire(C, st, ch, lane)) {
+					ok = false;
+					break;
+				}
+				run_chunk<LAMBDAS>(C, st, ch, next, lane, s == 0, dt, inv_dt, inv_dt2);
+				__syncwarp();
+				if (lane == 0) {
+					__threadfence();
+					st_release_gpu(C.done + ch, s + 1);
+				}
+			}
+		}
+	}
+	if (!ok && st.inflight >= 0) {
+		mbar_wait(C, st.mbar, st.parity);  // leave no copy in flight
+		st.inflight = -1;
+	}
+	uint32_t target = 0;
+	if (!grid_sync(C, target) || !ok) return;
+	run_finalize(C, gtid, nthreads, inv_dt);
+}
+
+// One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
+// In the first launch of a call, blocks past the colour's chunks step the
+// isolated vertices through all nsub substeps.
+template <bool LAMBDAS>
+__global__ void __launch_bounds__(256, 1) k_colour(DevCtx C, uint32_t colour, int first, float dt, uint32_t solve_blocks,
+                                                uint32_t nsub) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	if (blockIdx.x >= solve_blocks) {
 		const uint32_t b = blockIdx.x - solve_blocks, nb = gridDim.x - solve_blocks;
-		run_orphans(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, phase == kPhasePredict, dt, inv_dt);
+		run_isolated(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, nsub, dt, inv_dt);
 		return;
 	}
 	const uint32_t lane = threadIdx.x & 31u;
@@ -638,7 +732,7 @@ __global__ void __launch_bounds__(256) k_colour(DevCtx C, uint32_t colour, int p
 	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
 	Stage st = stage_init(C, lane);
 	if (!stage_acquire(C, st, ch, lane)) return;
-	run_chunk<LAMBDAS>(C, st, ch, -1, lane, phase, dt, inv_dt, inv_dt2);
+	run_chunk<LAMBDAS>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2);
 }
 
 __global__ void k_finalize(DevCtx C, float dt) {
@@ -712,11 +806,14 @@ int configure_kernels(const LaunchCfg& cfg) {
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	set_smem_attr(cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>, smem);
 	set_smem_attr(cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>, smem);
+	set_smem_attr(cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>, smem);
 	return (int)cudaGetLastError();
 }
 
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
-	const void* f = cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+	const void* f = cfg.sync_mode == 3
+	                    ? (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>)
+	                    : (cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>);
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	cudaError_t e = cudaGetDevice(&dev);
@@ -732,12 +829,15 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	cudaError_t e = cudaSuccess;
 	if (nsub == 0) return 0;
-	if (cfg.sync_mode == 1) {
+	if (cfg.sync_mode == 1 || cfg.sync_mode == 3) {
 		e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+		if (e == cudaSuccess && cfg.sync_mode == 3) e = cudaMemsetAsync(ctx.done, 0, sizeof(uint32_t) * ctx.nchunks, st);
 		if (e != cudaSuccess) return (int)e;
 		DevCtx c = ctx;
 		void* args[] = {&c, &nsub, &dt};
-		const void* f = cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+		const void* f = cfg.sync_mode == 1
+		                    ? (cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>)
+		                    : (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>);
 		e = cudaLaunchCooperativeKernel(f, dim3(cfg.blocks), dim3(cfg.block), args, smem, st);
 		return (int)e;
 	}
@@ -747,17 +847,16 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 	for (uint32_t s = 0; s < nsub; s++) {
 		for (uint32_t c = 0; c < ctx.ncolours; c++) {
 			const uint32_t nch = cfg.colour_chunk_begin_host[c + 1] - cfg.colour_chunk_begin_host[c];
-			const uint32_t solve_blocks = (nch + warps_per_block - 1) / warps_per_block;
-			const int phase = c == 0 ? (s == 0 ? kPhasePredict : kPhaseAdvance) : kPhaseSolve;
+			uint32_t sb = (nch + warps_per_block - 1) / warps_per_block;
 			uint32_t extra = 0;
-			if (c == 0 && ctx.norphans) extra = (ctx.norphans + cfg.block - 1) / cfg.block;
-			const uint32_t grid = solve_blocks + extra;
+			if (s == 0 && c == 0 && ctx.nisolated) extra = (ctx.nisolated + cfg.block - 1) / cfg.block;
+			const uint32_t grid = sb + extra;
 			if (grid == 0) continue;
 			DevCtx cc = ctx;
-			uint32_t colour = c, sb = solve_blocks;
-			int ph = phase;
+			uint32_t colour = c, ns = nsub;
+			int first = s == 0 ? 1 : 0;
 			float dtv = dt;
-			void* args[] = {&cc, &colour, &ph, &dtv, &sb};
+			void* args[] = {&cc, &colour, &first, &dtv, &sb, &ns};
 			e = cudaLaunchKernel(fc, dim3(grid), dim3(cfg.block), args, smem, st);
 			if (e != cudaSuccess) return (int)e;
 		}

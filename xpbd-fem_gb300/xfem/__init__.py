@@ -57,9 +57,9 @@ class Mesh(C.Structure):
 
 
 class Info(C.Structure):
-    _fields_ = [(n, C.c_uint32) for n in ("bodies", "vertices", "tets", "clusters", "colours", "orphans",
+    _fields_ = [(n, C.c_uint32) for n in ("bodies", "vertices", "tets", "clusters", "colours", "isolated",
                                           "chunks", "tet_rows", "block_size", "blocks", "sync_mode",
-                                          "cluster_mode")] + [("device_bytes", C.c_uint64)]
+                                          "cluster_mode", "max_chunk_deps", "reserved")] + [("device_bytes", C.c_uint64)]
 
 
 # every symbol include/xfem.h declares
