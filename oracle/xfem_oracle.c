@@ -342,7 +342,11 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
 				if (x > mx[k]) mx[k] = x;
 			}
 		float sc[3];
-		for (int k = 0; k < 3; k++) sc[k] = (mx[k] - mn[k]) > 0.0f ? 1023.0f / (mx[k] - mn[k]) : 0.0f;
+		// one scale for all axes (the largest extent), so the curve's cells are
+		// cubes and consecutive clusters form compact blocks on any box shape
+		float ext = 0.0f;
+		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
+		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
 		orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
 		if (!kv) return -1;
 		for (uint32_t v = 0; v < nv; v++) {

@@ -235,7 +235,8 @@ bool tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v |
 //  3. greedy colouring of clusters in id order: the smallest colour not used
 //     by an earlier cluster sharing a vertex;
 //  4. vertex rank: Morton code of the rest position (10 bits per axis,
-//     quantised over the AABB) then vertex id; or the identity;
+//     quantised over the AABB with one scale, its largest extent) then
+//     vertex id; or the identity;
 //  5. inside a colour, clusters by (smallest rank of their vertices, id).
 int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
                    uint32_t morton, Schedule& s) {
@@ -332,7 +333,11 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 				mx[k] = x > mx[k] ? x : mx[k];
 			}
 		float sc[3];
-		for (int k = 0; k < 3; k++) sc[k] = (mx[k] - mn[k]) > 0.0f ? 1023.0f / (mx[k] - mn[k]) : 0.0f;
+		// one scale for all axes (the largest extent), so the curve's cells are
+		// cubes and consecutive clusters form compact blocks on any box shape
+		float ext = 0.0f;
+		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
+		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
 		std::vector<uint64_t> key(nverts);
 		for (uint32_t v = 0; v < nverts; v++) {
 			uint32_t q[3];
