@@ -244,6 +244,16 @@ static uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
 	return c;
 }
 
+static uint32_t orc_quantise(const float* p, const float* mn, const float* sc) {
+	uint32_t q[3];
+	for (int k = 0; k < 3; k++) {
+		float f = (p[k] - mn[k]) * sc[k];
+		uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
+		q[k] = u > 1023u ? 1023u : u;
+	}
+	return morton3(q[0], q[1], q[2]);
+}
+
 typedef struct { uint64_t key; uint32_t id; } orc_kv;
 static int kv_cmp(const void* a, const void* b) {
 	const orc_kv* x = (const orc_kv*)a;
@@ -333,15 +343,15 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
 	}
 	*ncolours = ncol;
 	/* 3. vertex order */
+	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+	float sc[3] = {0.0f, 0.0f, 0.0f};
 	if (morton) {
-		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
 		for (uint32_t v = 0; v < nv; v++)
 			for (int k = 0; k < 3; k++) {
 				float x = nodes[3 * (size_t)v + k];
 				if (x < mn[k]) mn[k] = x;
 				if (x > mx[k]) mx[k] = x;
 			}
-		float sc[3];
 		// one scale for all axes (the largest extent), so the curve's cells are
 		// cubes and consecutive clusters form compact blocks on any box shape
 		float ext = 0.0f;
@@ -350,13 +360,7 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
 		orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
 		if (!kv) return -1;
 		for (uint32_t v = 0; v < nv; v++) {
-			uint32_t q[3];
-			for (int k = 0; k < 3; k++) {
-				float f = (nodes[3 * (size_t)v + k] - mn[k]) * sc[k];
-				uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
-				q[k] = u > 1023u ? 1023u : u;
-			}
-			kv[v].key = morton3(q[0], q[1], q[2]);
+			kv[v].key = orc_quantise(nodes + 3 * (size_t)v, mn, sc);
 			kv[v].id = v;
 		}
 		qsort(kv, nv, sizeof(orc_kv), kv_cmp);
@@ -365,17 +369,29 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
 	} else {
 		for (uint32_t v = 0; v < nv; v++) vert_rank[v] = v;
 	}
-	/* 4. cluster order inside each colour: (colour, min vertex rank, id) */
+	/* 4. cluster order inside each colour: (colour, Morton code of the
+	 * centroid of the cluster's tet vertices, id); without Morton order,
+	 * (colour, smallest vertex id, id) */
 	orc_kv* ck = (orc_kv*)malloc(sizeof(orc_kv) * (nc ? nc : 1));
 	if (!ck) return -1;
 	for (uint32_t k = 0; k < nc; k++) {
-		uint32_t mr = 0xffffffffu;
-		for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++)
-			for (int n = 0; n < 4; n++) {
-				uint32_t r = vert_rank[tets[4 * (size_t)cl_tets[q] + n]];
-				if (r < mr) mr = r;
-			}
-		ck[k].key = ((uint64_t)colour_of_cluster[k] << 32) | mr;
+		uint32_t key = 0xffffffffu;
+		if (morton) {
+			float c[3] = {0.0f, 0.0f, 0.0f};
+			for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++)
+				for (int n = 0; n < 4; n++)
+					for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)tets[4 * (size_t)cl_tets[q] + n] + j];
+			float cnt = (float)(4u * (cl_begin[k + 1] - cl_begin[k]));
+			for (int j = 0; j < 3; j++) c[j] = c[j] / cnt;
+			key = orc_quantise(c, mn, sc);
+		} else {
+			for (uint32_t q = cl_begin[k]; q < cl_begin[k + 1]; q++)
+				for (int n = 0; n < 4; n++) {
+					uint32_t v = tets[4 * (size_t)cl_tets[q] + n];
+					if (v < key) key = v;
+				}
+		}
+		ck[k].key = ((uint64_t)colour_of_cluster[k] << 32) | key;
 		ck[k].id = k;
 	}
 	qsort(ck, nc, sizeof(orc_kv), kv_cmp);

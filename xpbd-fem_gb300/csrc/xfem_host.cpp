@@ -237,7 +237,8 @@ bool tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v |
 //  4. vertex rank: Morton code of the rest position (10 bits per axis,
 //     quantised over the AABB with one scale, its largest extent) then
 //     vertex id; or the identity;
-//  5. inside a colour, clusters by (smallest rank of their vertices, id).
+//  5. inside a colour, clusters by (Morton code of their centroid, id), or
+//     (smallest vertex id, id) without Morton order.
 int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
                    uint32_t morton, Schedule& s) {
 	std::vector<uint32_t> off(nverts + 1, 0), lst(4 * (size_t)ntets);
@@ -324,43 +325,57 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 
 	// vertex rank
 	s.vert_rank.resize(nverts);
+	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+	float sc[3] = {0.0f, 0.0f, 0.0f};
+	auto quantise = [&](const float* p3) {
+		uint32_t q[3];
+		for (int k = 0; k < 3; k++) {
+			const float f = (p3[k] - mn[k]) * sc[k];
+			const uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
+			q[k] = u > 1023u ? 1023u : u;
+		}
+		return morton_code(q[0], q[1], q[2]);
+	};
 	if (morton) {
-		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
 		for (uint32_t v = 0; v < nverts; v++)
 			for (int k = 0; k < 3; k++) {
 				const float x = nodes[3 * (size_t)v + k];
 				mn[k] = x < mn[k] ? x : mn[k];
 				mx[k] = x > mx[k] ? x : mx[k];
 			}
-		float sc[3];
 		// one scale for all axes (the largest extent), so the curve's cells are
 		// cubes and consecutive clusters form compact blocks on any box shape
 		float ext = 0.0f;
 		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
 		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
 		std::vector<uint64_t> key(nverts);
-		for (uint32_t v = 0; v < nverts; v++) {
-			uint32_t q[3];
-			for (int k = 0; k < 3; k++) {
-				const float f = (nodes[3 * (size_t)v + k] - mn[k]) * sc[k];
-				const uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
-				q[k] = u > 1023u ? 1023u : u;
-			}
-			key[v] = ((uint64_t)morton_code(q[0], q[1], q[2]) << 32) | v;
-		}
+		for (uint32_t v = 0; v < nverts; v++) key[v] = ((uint64_t)quantise(nodes + 3 * (size_t)v) << 32) | v;
 		std::sort(key.begin(), key.end());
 		for (uint32_t i = 0; i < nverts; i++) s.vert_rank[(uint32_t)key[i]] = i;
 	} else {
 		for (uint32_t v = 0; v < nverts; v++) s.vert_rank[v] = v;
 	}
 
-	// cluster order inside each colour
+	// cluster order inside each colour: Morton code of the cluster's centroid
+	// (the mean of its tets' vertex positions, summed tet by tet in float); it
+	// sits inside a curve cell, where a corner would sit on a cell boundary
+	// and flip bits with rounding. Without Morton order: smallest vertex id.
 	std::vector<std::pair<uint64_t, uint32_t>> ck(nc);
 	for (uint32_t k = 0; k < nc; k++) {
-		uint32_t mr = kNone;
-		for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++)
-			for (int n = 0; n < 4; n++) mr = std::min(mr, s.vert_rank[tets[4 * (size_t)s.cl_tets[q] + n]]);
-		ck[k] = {((uint64_t)s.cl_colour[k] << 32) | mr, k};
+		uint32_t key = kNone;
+		if (morton) {
+			float c[3] = {0.0f, 0.0f, 0.0f};
+			for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++)
+				for (int n = 0; n < 4; n++)
+					for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)tets[4 * (size_t)s.cl_tets[q] + n] + j];
+			const float cnt = (float)(4u * (s.cl_begin[k + 1] - s.cl_begin[k]));
+			for (int j = 0; j < 3; j++) c[j] = c[j] / cnt;
+			key = quantise(c);
+		} else {
+			for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++)
+				for (int n = 0; n < 4; n++) key = std::min(key, tets[4 * (size_t)s.cl_tets[q] + n]);
+		}
+		ck[k] = {((uint64_t)s.cl_colour[k] << 32) | key, k};
 	}
 	std::sort(ck.begin(), ck.end());
 	s.colour_cl.resize(nc);
