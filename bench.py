@@ -16,7 +16,8 @@ shape the configuration names.
            every step uploads positions and velocities, steps one frame and
            reads the positions back (host-timed, copies included);
   roofline, cpu_baseline (the oracle port of the reference in its own
-  shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches.
+  shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches, and
+  "batched": 512 bodies in one launch per frame against one launch per body.
 --impl reference: the reference's CPU algorithm (the oracle port, run in the
   GPU's colour order with all host threads) on the same mesh; each step is a
   bounded sample of substeps.
@@ -278,10 +279,11 @@ def run_xfem(args, world, rank, local):
     hbm, peak_kind = peaks()
     bpu = REC_BYTES + VERT_BYTES * nv / nt
     per_launch_ms = statistics.mean(ms)
-    launches_per_frame = 1 if info["sync_mode"] == 1 else S * info["colours"] + 1
+    launches_per_frame = 1 if info["sync_mode"] in (1, 3) else S * info["colours"] + 1
     achieved = bpu * nt * S / (per_launch_ms / 1e3) / 1e9
     traffic = None if NCU_DRAM_BYTES_PER_TET_SUBSTEP is None else NCU_DRAM_BYTES_PER_TET_SUBSTEP * nt * S
     cpu = cpu_baseline_native(w) if not args.no_cpu else None
+    batched = None if args.no_batched else run_batched(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -289,19 +291,70 @@ def run_xfem(args, world, rank, local):
         "config": {"workload": w["name"], "tets": nt, "vertices": nv, "substeps_per_step": S,
                    "dt": w["dt"], "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MB write)",
                    "colours": info["colours"], "clusters": info["clusters"], "sync_mode":
-                   "persistent" if info["sync_mode"] == 1 else "cuda-graph", "block": info["block_size"],
+                   {1: "persistent", 2: "cuda-graph", 3: "dataflow"}[info["sync_mode"]], "block": info["block_size"],
                    "blocks": info["blocks"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": peak_kind, "bytes_per_tet_substep": bpu,
-                     "kernel": "k_persistent" if info["sync_mode"] == 1 else "k_colour (whole frame)",
+                     "kernel": {1: "k_persistent", 3: "k_dataflow"}.get(info["sync_mode"], "k_colour (whole frame)"),
                      "launch_ms": per_launch_ms},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * nv, "d2h_bytes_per_step": 12 * nv,
                 "steps": e2e_steps},
         "gpu_launches": launches_per_frame * args.steps,
+        "batched": batched,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
+
+
+def run_batched(stream, frames=5, plain_frames=2):
+    """512 independent bodies (a, b, c ~ U{2..24} cubes, coin-flip Neo-Hookean /
+    Yeoh, log-uniform E, each on its own ground): one handle and one launch per
+    frame, against the same bodies as 512 handles stepped one launch per body
+    on the same stream. Device-timed with CUDA events; 20 substeps per frame."""
+    import torch
+
+    import xfem
+    from xfem import workloads as W
+    w = W.batched()
+    sdt = w["dt"] / w["substeps"]
+    sp = C_void_p(stream.cuda_stream)
+    batch = xfem.Body(meshes=w["meshes"], settings=w["settings"], stream=sp)
+    nt = batch.info()["tets"]
+    for _ in range(3):
+        batch.step_frames(1, 20, sdt)
+    batch.synchronize()
+
+    def timed(fn, n):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        for _ in range(n):
+            fn()
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3 / n
+
+    tb = timed(lambda: batch.step_frames(1, 20, sdt), frames)
+    info = batch.info()
+    batch.close()
+    singles = [xfem.Body(nodes, idx, d, s_, sync_mode=1, block_size=128, stream=sp)
+               for (nodes, idx, d), s_ in zip(w["meshes"], w["settings"])]
+
+    def plain():
+        for b in singles:
+            b.step_frames(1, 20, sdt)
+
+    plain()
+    tp = timed(plain, plain_frames)
+    for b in singles:
+        b.close()
+    return {"workload": w["name"], "bodies": len(w["meshes"]), "tets": nt, "substeps_per_frame": 20,
+            "value": nt * 20 / tb, "unit": UNIT, "ms_per_frame": 1e3 * tb,
+            "plain_one_body_per_launch": nt * 20 / tp, "plain_ms_per_frame": 1e3 * tp, "speedup": tp / tb,
+            "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+            "launches_per_frame": 1 if info["sync_mode"] != 2 else 20 * info["colours"] + 1}
 
 
 def C_void_p(v):
@@ -326,6 +379,7 @@ def main():
     ap.add_argument("--sync-mode", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
