@@ -96,6 +96,7 @@ def lib():
         L.orc_volume_d.argtypes = [P, u32, P]
         L.orc_volume_d.restype = C.c_double
         L.orc_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P, P, P]
+        L.orc_adjoint_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, u32, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -205,3 +206,26 @@ def schedule(nodes, tets, mode=1, morton=1):
         raise ValueError("schedule limits exceeded")
     return dict(cluster_of=cluster_of, clusters=ncl.value, colour_of_cluster=colour_of[:ncl.value],
                 colours=ncol.value, vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1])
+
+
+def adjoint(X0, V0, w, tets, ep, tet_mu, order, nsub, params, tips, targets, lock_mask=None, grad=True):
+    """FP64 loss and (optionally) dL/dmu per tet and dL/dV0 (oracle/xfem_oracle_adjoint.c)."""
+    X0 = np.ascontiguousarray(X0, np.float64).reshape(-1)
+    V0 = np.ascontiguousarray(V0, np.float64).reshape(-1)
+    w = np.ascontiguousarray(w, np.float64)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    ep = np.ascontiguousarray(ep, np.float64)
+    tet_mu = np.ascontiguousarray(tet_mu, np.float64)
+    order = np.ascontiguousarray(order, np.uint32)
+    tips = np.ascontiguousarray(tips, np.uint32)
+    targets = np.ascontiguousarray(targets, np.float64)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    loss = C.c_double()
+    dmu = np.zeros(tets.shape[0]) if grad else None
+    dv = np.zeros(X0.size) if grad else None
+    rc = lib().orc_adjoint_d(w.size, _p(X0), _p(V0), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep), _p(tet_mu),
+                             _p(order), nsub, C.byref(params), tips.size, _p(tips), _p(targets), C.byref(loss),
+                             _p(dmu), _p(dv))
+    if rc:
+        raise ValueError("adjoint: coupled Neo-Hookean only")
+    return (loss.value, dmu, dv.reshape(-1, 3)) if grad else loss.value
