@@ -183,6 +183,33 @@ int xfem_step_frames_noalloc(xfem_body* b, uint32_t frames, uint32_t substeps, f
  * wait ran out since the last check. */
 int xfem_synchronize(xfem_body* b);
 
+/* ---- reverse-mode adjoint ---------------------------------------------------- */
+/* No counterpart in the reference, which only steps forward: the derivative
+ * of Geo3d::Substep (XPBDFEM/Geo.cpp:305-356) as this library runs it, with
+ * respect to each tet's shear modulus and the initial state. Only the coupled
+ * Neo-Hookean model (energy 4 with the XPBD solve bit) is differentiated;
+ * other settings give XFEM_EUNSUPPORTED.
+ *
+ * xfem_adjoint_forward steps `substeps` substeps of dt (the same results as
+ * xfem_step_frames(b, 1, substeps, dt)) and records what the reverse pass
+ * needs. Vertices and tets are numbered in the handle's concatenated caller
+ * order (body 0's, then body 1's, ...). tip_traj (nullable):
+ * substeps x ntips x 3 floats, the position of vertex tips[q] after each
+ * substep. checkpoint_every = 0 keeps the tape of every substep on the
+ * device; K > 0 keeps the state every K substeps and the tape of K substeps,
+ * and the backward pass re-runs each segment forward once. */
+int xfem_adjoint_forward(xfem_body* b, uint32_t substeps, float dt, uint32_t checkpoint_every, uint32_t ntips,
+                         const uint32_t* tips, float* tip_traj);
+/* Reverse pass of the last xfem_adjoint_forward. grad_tip_traj (required):
+ * dL/d tip_traj. grad_x, grad_v (nullable = zero, 3 per vertex): dL/d the
+ * positions and velocities at the end. Outputs (nullable): dmu (one per tet)
+ * dL/dmu, with mu the tet's shear modulus (1/compliance or the value given
+ * to xfem_set_tet_mu); dx0, dv0 (3 per vertex): dL/d the positions and
+ * velocities at the start. The handle's state stays at the end of the
+ * forward run. Synchronising. */
+int xfem_adjoint_backward(xfem_body* b, const float* grad_tip_traj, const float* grad_x, const float* grad_v,
+                          float* dmu, float* dx0, float* dv0);
+
 /* ---- state transfer (caller vertex order; synchronising) ------------------ */
 int xfem_get_positions(xfem_body* b, uint32_t body, float* out_xyz);
 int xfem_set_positions(xfem_body* b, uint32_t body, const float* xyz);

@@ -96,7 +96,7 @@ def lib():
         L.orc_volume_d.argtypes = [P, u32, P]
         L.orc_volume_d.restype = C.c_double
         L.orc_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P, P, P]
-        L.orc_adjoint_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, u32, P, P, P, P, P]
+        L.orc_adjoint_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, u32, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -208,8 +208,10 @@ def schedule(nodes, tets, mode=1, morton=1):
                 colours=ncol.value, vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1])
 
 
-def adjoint(X0, V0, w, tets, ep, tet_mu, order, nsub, params, tips, targets, lock_mask=None, grad=True):
-    """FP64 loss and (optionally) dL/dmu per tet and dL/dV0 (oracle/xfem_oracle_adjoint.c)."""
+def adjoint(X0, V0, w, tets, ep, tet_mu, order, nsub, params, tips, targets, lock_mask=None, grad=True,
+            want_dx=False):
+    """FP64 loss and (optionally) dL/dmu per tet, dL/dV0 and (want_dx) dL/dX0
+    (oracle/xfem_oracle_adjoint.c)."""
     X0 = np.ascontiguousarray(X0, np.float64).reshape(-1)
     V0 = np.ascontiguousarray(V0, np.float64).reshape(-1)
     w = np.ascontiguousarray(w, np.float64)
@@ -223,9 +225,12 @@ def adjoint(X0, V0, w, tets, ep, tet_mu, order, nsub, params, tips, targets, loc
     loss = C.c_double()
     dmu = np.zeros(tets.shape[0]) if grad else None
     dv = np.zeros(X0.size) if grad else None
+    dx = np.zeros(X0.size) if grad else None
     rc = lib().orc_adjoint_d(w.size, _p(X0), _p(V0), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep), _p(tet_mu),
                              _p(order), nsub, C.byref(params), tips.size, _p(tips), _p(targets), C.byref(loss),
-                             _p(dmu), _p(dv))
+                             _p(dmu), _p(dv), _p(dx))
     if rc:
         raise ValueError("adjoint: coupled Neo-Hookean only")
-    return (loss.value, dmu, dv.reshape(-1, 3)) if grad else loss.value
+    if not grad:
+        return loss.value
+    return (loss.value, dmu, dv.reshape(-1, 3), dx.reshape(-1, 3)) if want_dx else (loss.value, dmu, dv.reshape(-1, 3))

@@ -116,12 +116,13 @@ double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets);
 /* ---- FP64 adjoint (oracle/xfem_oracle_adjoint.c) ---------------------------- */
 /* Forward nsub substeps in `order` with per-tet shear modulus tet_mu and the
  * loss sum_{s, q} |x_s[tips[q]] - targets[s][q]|^2 (s = state after substep
- * s + 1), then the reverse pass: dL/dmu per tet and dL/dV0 (3 nv). With
+ * s + 1), then the reverse pass: dL/dmu per tet, dL/dV0 and dL/dX0 (3 nv each,
+ * both nullable). With
  * dmu == NULL only the loss is computed. Coupled Neo-Hookean only. */
 int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double* w0, const uint8_t* lock_mask,
                   uint32_t nt, const uint32_t* tets, const double* ep, const double* tet_mu, const uint32_t* order,
                   uint32_t nsub, const orc_params* p, uint32_t ntip, const uint32_t* tips, const double* targets,
-                  double* loss, double* dmu, double* dV0);
+                  double* loss, double* dmu, double* dV0, double* dX0);
 
 /* ---- schedule restatement -------------------------------------------------- */
 /* Edge-star clustering (mode 1) or one tet per cluster (mode 0); greedy

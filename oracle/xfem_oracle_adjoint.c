@@ -8,7 +8,7 @@
  * (extension) and the velocity update (XPBDFEM/Geo.cpp:342-344).
  *
  * Loss: sum over substeps s = 1..nsub and tip vertices of |x_s - target_s|^2.
- * Outputs dL/dmu per tet (the per-tet shear modulus mu_ref) and dL/dV0;
+ * Outputs dL/dmu per tet (the per-tet shear modulus mu_ref), dL/dV0 and dL/dX0;
  * with dmu == NULL only the forward runs and the loss is returned.
  * The Cramer clamp max(1e-8, .) and the Yeoh clamp are taken as inactive;
  * only the coupled (bit 11) Neo-Hookean model is differentiated.
@@ -197,7 +197,7 @@ static void ground_reverse(const gr_fw* g, double* xb, double* ob) {
 int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double* w0, const uint8_t* lock_mask,
                   uint32_t nt, const uint32_t* tets, const double* ep, const double* tet_mu, const uint32_t* order,
                   uint32_t nsub, const orc_params* p, uint32_t ntip, const uint32_t* tips, const double* targets,
-                  double* loss, double* dmu, double* dV0) {
+                  double* loss, double* dmu, double* dV0, double* dX0) {
 	if (p->energy != ORC_ENERGY_MIXED_SEL || !p->simultaneous) return -1;
 	const size_t n3 = 3 * (size_t)nv;
 	const double dt = p->dt, inv_dt = 1.0 / dt, drag = 1.0 - (double)p->time_corrected_drag;
@@ -316,6 +316,7 @@ int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double*
 		}
 	}
 	if (dV0) memcpy(dV0, Vb, sizeof(double) * n3);
+	if (dX0) memcpy(dX0, Xb, sizeof(double) * n3);
 done:
 	free(Xp); free(Os); free(ws); free(X); free(V); free(w); free(Xb); free(Vb); free(Ob); free(Y); free(tf); free(gf);
 	return 0;

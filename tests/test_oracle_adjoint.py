@@ -2,12 +2,14 @@
 
 The oracle's reverse pass (oracle/xfem_oracle_adjoint.c) is the reference the
 GPU adjoint is checked against, so it is pinned here first: d loss / d log mu
-per tet and d loss / d V0 per vertex component, each against a central
-difference of the oracle's own FP64 forward loss. h = 1e-3 in log mu (1e-5 in
-velocity) keeps the O(h^2) truncation near 1e-6 of the derivative; the loss
-itself carries rounding noise of about 1e-13 L, so each comparison allows
-FD_TOL relative error plus NOISE * L / h absolute.
+per tet, d loss / d V0 and d loss / d X0 per vertex component, each against a
+central difference of the oracle's own FP64 forward loss. h = 1e-3 in log mu
+(1e-5 in velocity, 1e-6 in position) keeps the O(h^2) truncation near 1e-6
+of the derivative; the loss itself carries rounding noise of about 1e-13 L,
+so each comparison allows FD_TOL relative error plus NOISE * L / h absolute.
 """
+import types
+
 import numpy as np
 import pytest
 
@@ -45,50 +47,60 @@ def _case(ground, nsub=30):
     lock = (fl & 1).astype(np.uint8)
     targets = np.repeat(X0[tips][None], nsub, 0) + 1e-3 * rng.normal(size=(nsub, tips.size, 3))
 
-    def loss(m, v, grad=False):
-        return oracle.adjoint(X0, v, w, tets, ep, m, order, nsub, p, tips, targets, lock, grad=grad)
+    def loss(m=mu, v=V0, x=X0):
+        return oracle.adjoint(x, v, w, tets, ep, m, order, nsub, p, tips, targets, lock, grad=False)
 
-    def forward_loss(m, v):
-        X, V, ww = X0, v, w
+    def grads():
+        return oracle.adjoint(X0, V0, w, tets, ep, mu, order, nsub, p, tips, targets, lock, want_dx=True)
+
+    def forward_loss():
+        X, V, ww = X0, V0, w
         total = 0.0
         for k in range(nsub):
-            X, V, ww, _ = oracle.substeps(X, V, ww, tets, ep, order, 1, p, lock_mask=lock, tet_mu=m,
+            X, V, ww, _ = oracle.substeps(X, V, ww, tets, ep, order, 1, p, lock_mask=lock, tet_mu=mu,
                                           dtype=np.float64)
             total += float(((X[tips] - targets[k]) ** 2).sum())
         return total
 
-    loss.forward = forward_loss
-    return mu, V0, tips, loss
+    return types.SimpleNamespace(mu=mu, V0=V0, X0=X0, tips=tips, loss=loss, grads=grads, forward_loss=forward_loss)
+
+
+def _central(f, a, idx, h, scale=False):
+    ap, am = a.copy(), a.copy()
+    if scale:
+        ap[idx] *= np.exp(h)
+        am[idx] *= np.exp(-h)
+    else:
+        ap[idx] += h
+        am[idx] -= h
+    return (f(ap) - f(am)) / (2 * h)
 
 
 @pytest.mark.parametrize("ground", [False, True], ids=["cantilever", "ground_friction"])
 def test_adjoint_vs_central_fd(ground):
-    mu, V0, tips, loss = _case(ground)
-    L, dmu, dv = loss(mu, V0, grad=True)
-    assert L > 0 and np.isfinite(dmu).all() and np.isfinite(dv).all()
-    h = 1e-3
+    c = _case(ground)
+    L, dmu, dv, dx = c.grads()
+    assert L > 0 and np.isfinite(dmu).all() and np.isfinite(dv).all() and np.isfinite(dx).all()
     for t in [0, 7, 33, 50, 70]:
-        mp, mm = mu.copy(), mu.copy()
-        mp[t] *= np.exp(h)
-        mm[t] *= np.exp(-h)
-        fd = (loss(mp, V0) - loss(mm, V0)) / (2 * h)
-        ad = dmu[t] * mu[t]
+        h = 1e-3
+        fd = _central(lambda m: c.loss(m=m), c.mu, t, h, scale=True)
+        ad = dmu[t] * c.mu[t]
         assert abs(fd - ad) <= FD_TOL * abs(fd) + NOISE * L / h, (t, fd, ad)
-    h = 1e-5
-    for (i, k) in [(int(tips[0]), 0), (int(tips[3]), 2), (5, 1), (int(tips[-1]), 1)]:
-        vp, vm = V0.copy(), V0.copy()
-        vp[i, k] += h
-        vm[i, k] -= h
-        fd = (loss(mu, vp) - loss(mu, vm)) / (2 * h)
+    for (i, k) in [(int(c.tips[0]), 0), (int(c.tips[3]), 2), (5, 1), (int(c.tips[-1]), 1)]:
+        h = 1e-5
+        fd = _central(lambda v: c.loss(v=v), c.V0, (i, k), h)
         assert abs(fd - dv[i, k]) <= FD_TOL * abs(fd) + NOISE * L / h, (i, k, fd, dv[i, k])
+    for (i, k) in [(int(c.tips[1]), 0), (int(c.tips[2]), 2), (3, 1), (40, 2)]:
+        h = 1e-6
+        fd = _central(lambda x: c.loss(x=x), c.X0, (i, k), h)
+        assert abs(fd - dx[i, k]) <= FD_TOL * abs(fd) + NOISE * L / h, (i, k, fd, dx[i, k])
 
 
 @pytest.mark.parametrize("ground", [False, True], ids=["cantilever", "ground_friction"])
 def test_adjoint_loss_equals_forward(ground):
     """The adjoint's forward loss is the tip loss of the FP64 substep run."""
-    mu, V0, tips, loss = _case(ground, nsub=12)
-    L = loss(mu, V0)
+    c = _case(ground, nsub=12)
+    L = c.loss()
     assert np.isfinite(L) and L > 0
-    L2, _, _ = loss(mu, V0, grad=True)
-    assert L == L2
-    assert abs(L - loss.forward(mu, V0)) <= 1e-12 * L
+    assert c.grads()[0] == L
+    assert abs(L - c.forward_loss()) <= 1e-12 * L

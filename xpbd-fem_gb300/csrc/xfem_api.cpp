@@ -32,7 +32,7 @@ int fail(int code, const std::string& msg) {
 	} while (0)
 
 struct BodyHost {
-	uint32_t nv = 0, nt = 0, vbase = 0;
+	uint32_t nv = 0, nt = 0, vbase = 0, tbase = 0;
 	std::vector<float> nodes;         // rest positions, caller order
 	std::vector<uint32_t> tets;       // caller order
 	std::vector<float> ep;            // 17 per tet
@@ -53,9 +53,27 @@ struct DevBuf {
 		if (p) cudaFree(p);
 	}
 	cudaError_t alloc(size_t count) {
+		if (p) {
+			cudaFree(p);
+			p = nullptr;
+		}
 		n = count;
 		return cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
 	}
+	// keeps the buffer when it is already large enough
+	cudaError_t reserve(size_t count) { return p && n >= count ? cudaSuccess : alloc(count); }
+};
+
+// The recorded run of the last xfem_adjoint_forward.
+struct AdjointRun {
+	bool valid = false;
+	uint32_t nsub = 0, seg = 0, nseg = 0, ntips = 0;
+	float dt = 0.0f;
+	DevBuf<float4> tape_v, tape_t, tape_fin, traj, ckpt, abar, grad;
+	DevBuf<int32_t> tip_of;
+	DevBuf<float> cbar;
+	std::vector<uint32_t> tips;  // the tips tip_of holds
+	bool tips_uploaded = false;
 };
 
 }  // namespace
@@ -71,12 +89,17 @@ struct xfem_body {
 	DevBuf<float4> vert, cblk;
 	DevBuf<uint32_t> ccb, isolated, dev_of_vert, tets_dev, bar, dep_begin, deps, done;
 	DevBuf<ChunkMeta> chunks;
+	uint32_t max_colour_chunks = 0;
+	AdjointRun adj;
 	DevBuf<BodyParams> params;
 	DevBuf<float2> tlam;
 	DevBuf<int> err;
 	DevBuf<float> stage;
 	DevBuf<double> vol;
-	std::vector<float4> cblk_host;  // kept to refresh c0 after material changes
+	// per tet, caller order (all bodies): record index of c0, volume, output
+	// row (row * 32 + lane), 1/mu; staging for transfers
+	DevBuf<uint32_t> tet_rec_dev, tet_slot_dev;
+	DevBuf<float> tet_vol_dev, tet_inv_mu, io;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -204,6 +227,7 @@ int build_device(xfem_body* h) {
 	uint32_t nverts = 0, ntets = 0, ncol = 1;
 	for (auto& b : h->bodies) {
 		b.vbase = nverts;
+		b.tbase = ntets;
 		nverts += b.nv;
 		ntets += b.nt;
 		ncol = std::max(ncol, b.sched.ncolours);
@@ -258,6 +282,11 @@ int build_device(xfem_body* h) {
 	}
 	h->nchunks = nch;
 	h->nrows = trows;
+	{
+		uint32_t mc = 0;
+		for (uint32_t c = 0; c < ncol; c++) mc = std::max(mc, ccb[c + 1] - ccb[c]);
+		h->max_colour_chunks = mc;
+	}
 	std::vector<float4> cblk((size_t)total16, make_float4(0, 0, 0, 0));
 	// owner of each vertex: the first (lowest-colour) cluster that touches it
 	std::vector<uint32_t> owner(nverts, 0xffffffffu);
@@ -397,7 +426,28 @@ int build_device(xfem_body* h) {
 	XCUDA(cudaStreamSynchronize(h->stream));
 	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + isolated.size() + dev_of.size() +
 	                  tets_dev.size() + dep_begin.size() + deps.size() + nch) * 4 + meta.size() * 16 + params.size() * 64 + h->stage.n * 4 + h->tlam.n * 8;
-	h->cblk_host.swap(cblk);
+	{
+		std::vector<uint32_t> rec(ntets), slot(ntets);
+		std::vector<float> vol(ntets), inv_mu(ntets);
+		for (const BodyHost& b : h->bodies)
+			for (uint32_t t = 0; t < b.nt; t++) {
+				rec[b.tbase + t] = (uint32_t)b.tet_rec[t];
+				slot[b.tbase + t] = b.tet_slot[t];
+				vol[b.tbase + t] = b.ep[17 * (size_t)t + 15];
+				inv_mu[b.tbase + t] = 1.0f / (b.tet_mu.empty() ? 1.0f / b.settings.compliance : b.tet_mu[t]);
+			}
+		XCUDA(h->tet_rec_dev.alloc(ntets));
+		XCUDA(h->tet_slot_dev.alloc(ntets));
+		XCUDA(h->tet_vol_dev.alloc(ntets));
+		XCUDA(h->tet_inv_mu.alloc(ntets));
+		XCUDA(h->io.alloc(6 * (size_t)nverts + ntets));
+		XCUDA(up(h->tet_rec_dev.p, rec.data(), rec.size() * 4));
+		XCUDA(up(h->tet_slot_dev.p, slot.data(), slot.size() * 4));
+		XCUDA(up(h->tet_vol_dev.p, vol.data(), vol.size() * 4));
+		XCUDA(up(h->tet_inv_mu.p, inv_mu.data(), inv_mu.size() * 4));
+		XCUDA(cudaStreamSynchronize(h->stream));
+		h->device_bytes += (uint64_t)ntets * 16 + h->io.n * 4;
+	}
 	DevCtx& c = h->ctx;
 	c.vert = h->vert.p;
 	c.cblk = h->cblk.p;
@@ -405,6 +455,7 @@ int build_device(xfem_body* h) {
 	c.warp_smem = max_bytes + 2u * max_nv * kLanes * 16u;
 	c.tlam = h->tlam.p;
 	c.chunks = h->chunks.p;
+	c.ntrows = trows;
 	c.colour_chunk_begin = h->ccb.p;
 	c.isolated = h->isolated.p;
 	c.dep_begin = h->dep_begin.p;
@@ -607,11 +658,17 @@ int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
 	return check_device_error(h);
 }
 
-int upload_records(xfem_body* h) {
-	for (auto& b : h->bodies)
-		for (uint32_t t = 0; t < b.nt; t++) h->cblk_host[b.tet_rec[t]].w = tet_c0(b, t);
-	XCUDA(cudaMemcpyAsync(h->cblk.p, h->cblk_host.data(), h->cblk_host.size() * sizeof(float4), cudaMemcpyHostToDevice,
-	                      h->stream));
+// Rewrites c0 = (1/mu)/volume in one body's records on the device (and 1/mu
+// for the adjoint) after a material change.
+int update_material(xfem_body* h, const BodyHost& b) {
+	const float* mu_dev = nullptr;
+	if (!b.tet_mu.empty()) {
+		XCUDA(cudaMemcpyAsync(h->io.p, b.tet_mu.data(), b.nt * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+		mu_dev = h->io.p;
+	}
+	const int e = launch_set_c0(h->cblk.p, h->tet_rec_dev.p + b.tbase, h->tet_vol_dev.p + b.tbase, mu_dev,
+	                            1.0f / b.settings.compliance, b.nt, h->tet_inv_mu.p + b.tbase, h->stream);
+	if (e) return fail(XFEM_ECUDA, "material update launch failed");
 	XCUDA(cudaStreamSynchronize(h->stream));
 	return XFEM_OK;
 }
@@ -697,7 +754,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	const BodyParams p = make_params(*s);
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
-	if (material && b->tet_mu.empty()) return upload_records(h);
+	if (material && b->tet_mu.empty()) return update_material(h, *b);
 	return XFEM_OK;
 }
 
@@ -733,7 +790,7 @@ int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
 		b->tet_mu.clear();
 	}
 	XCUDA(cudaSetDevice(h->device));
-	return upload_records(h);
+	return update_material(h, *b);
 }
 
 int xfem_substep(xfem_body* b, float dt) { return step(b, 1, dt); }
@@ -902,5 +959,184 @@ void xfem_free_host(void* p) {
 }
 
 const char* xfem_last_error(void) { return g_err.c_str(); }
+
+}  // extern "C"
+
+// ---- reverse-mode adjoint -------------------------------------------------------
+namespace {
+
+// Device vertex of a vertex in the handle's concatenated caller order.
+uint32_t dev_vertex(const xfem_body* h, uint32_t i) {
+	for (const BodyHost& b : h->bodies)
+		if (i < b.vbase + b.nv) return b.vbase + b.sched.vert_rank[i - b.vbase];
+	return 0xffffffffu;
+}
+
+// Block size of the adjoint kernels: the largest whose staging fits.
+int adjoint_block(xfem_body* h, int* block) {
+	int optin = 0;
+	XCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+	for (int bs : {256, 128, 64, 32})
+		if (solve_smem_bytes(bs, h->cfg.warp_smem) <= (size_t)optin) {
+			*block = bs;
+			return XFEM_OK;
+		}
+	return fail(XFEM_ELIMIT, "chunk blocks too large for shared memory");
+}
+
+// The handle's DevCtx with the tape of segment j attached.
+DevCtx tape_ctx(xfem_body* h, uint32_t j) {
+	AdjointRun& a = h->adj;
+	DevCtx c = h->ctx;
+	c.tape_v = a.tape_v.p;
+	c.tape_t = a.tape_t.p;
+	c.tape_fin = a.tape_fin.p;
+	c.traj = a.traj.p;
+	c.tip_of = a.tip_of.p;
+	c.sub_base = j * a.seg;
+	c.ntips = a.ntips;
+	return c;
+}
+
+uint32_t seg_len(const AdjointRun& a, uint32_t j) { return std::min(a.seg, a.nsub - j * a.seg); }
+
+}  // namespace
+
+extern "C" {
+
+int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpoint_every, uint32_t ntips,
+                         const uint32_t* tips, float* tip_traj) {
+	if (!h) return fail(XFEM_EINVAL, "null handle");
+	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
+	if (nsub == 0) return fail(XFEM_EINVAL, "substeps must be > 0");
+	if (ntips && !tips) return fail(XFEM_EINVAL, "null tips");
+	for (const BodyHost& b : h->bodies) {
+		const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+		if (energy != XFEM_ENERGY_MIXED_SEL || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))
+			return fail(XFEM_EUNSUPPORTED, "the adjoint covers the coupled Neo-Hookean model only (energy 4, XPBD solve bit)");
+	}
+	XCUDA(cudaSetDevice(h->device));
+	AdjointRun& a = h->adj;
+	a.valid = false;
+	const bool same_tips = a.tips_uploaded && a.tips.size() == ntips && std::equal(a.tips.begin(), a.tips.end(), tips);
+	std::vector<int32_t> tip_of;
+	if (!same_tips) {
+		tip_of.assign(h->nverts, -1);
+		for (uint32_t q = 0; q < ntips; q++) {
+			const uint32_t dv = dev_vertex(h, tips[q]);
+			if (dv == 0xffffffffu) return fail(XFEM_EINVAL, "tip " + std::to_string(tips[q]) + " out of range");
+			if (tip_of[dv] >= 0) return fail(XFEM_EINVAL, "tips must be distinct");
+			tip_of[dv] = (int32_t)q;
+		}
+	}
+	const uint32_t seg = checkpoint_every == 0 || checkpoint_every > nsub ? nsub : checkpoint_every;
+	const uint32_t nseg = (nsub + seg - 1) / seg;
+	const size_t nv = h->nverts;
+	XCUDA(a.tape_v.reserve((size_t)seg * 2 * nv));
+	XCUDA(a.tape_t.reserve((size_t)seg * h->nrows * 3 * kLanes));
+	XCUDA(a.tape_fin.reserve(nv));
+	XCUDA(a.traj.reserve((size_t)nsub * std::max(ntips, 1u)));
+	XCUDA(a.grad.reserve((size_t)nsub * std::max(ntips, 1u)));
+	XCUDA(a.tip_of.reserve(nv));
+	XCUDA(a.abar.reserve(2 * nv));
+	XCUDA(a.cbar.reserve((size_t)h->nrows * kLanes));
+	if (nseg > 1) XCUDA(a.ckpt.reserve((size_t)(nseg + 1) * 2 * nv));
+	if (!same_tips) {
+		a.tips_uploaded = false;
+		XCUDA(cudaMemcpyAsync(a.tip_of.p, tip_of.data(), nv * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+		a.tips.assign(tips, tips + ntips);
+		a.tips_uploaded = true;
+	}
+	a.nsub = nsub;
+	a.seg = seg;
+	a.nseg = nseg;
+	a.ntips = ntips;
+	a.dt = dt;
+	int block = 0;
+	int rc = adjoint_block(h, &block);
+	if (rc) return rc;
+	for (uint32_t j = 0; j < nseg; j++) {
+		if (nseg > 1)
+			XCUDA(cudaMemcpyAsync(a.ckpt.p + 2 * nv * j, h->vert.p, 2 * nv * sizeof(float4), cudaMemcpyDeviceToDevice,
+			                      h->stream));
+		const int e = launch_substeps_tape(tape_ctx(h, j), block, h->cfg.warp_smem, seg_len(a, j), dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("recording launch: ") + cudaGetErrorString((cudaError_t)e));
+	}
+	if (nseg > 1)
+		XCUDA(cudaMemcpyAsync(a.ckpt.p + 2 * nv * nseg, h->vert.p, 2 * nv * sizeof(float4), cudaMemcpyDeviceToDevice,
+		                      h->stream));
+	std::vector<float4> traj;
+	if (tip_traj && ntips) {
+		traj.resize((size_t)nsub * ntips);
+		XCUDA(cudaMemcpyAsync(traj.data(), a.traj.p, traj.size() * sizeof(float4), cudaMemcpyDeviceToHost, h->stream));
+	}
+	rc = check_device_error(h);
+	if (rc) return rc;
+	for (size_t i = 0; i < traj.size(); i++) {
+		tip_traj[3 * i] = traj[i].x;
+		tip_traj[3 * i + 1] = traj[i].y;
+		tip_traj[3 * i + 2] = traj[i].z;
+	}
+	a.valid = true;
+	return XFEM_OK;
+}
+
+int xfem_adjoint_backward(xfem_body* h, const float* grad_tip_traj, const float* grad_x, const float* grad_v,
+                          float* dmu, float* dx0, float* dv0) {
+	if (!h) return fail(XFEM_EINVAL, "null handle");
+	AdjointRun& a = h->adj;
+	if (!a.valid) return fail(XFEM_EINVAL, "no recorded run: call xfem_adjoint_forward first");
+	if (a.ntips && !grad_tip_traj) return fail(XFEM_EINVAL, "null grad_tip_traj");
+	XCUDA(cudaSetDevice(h->device));
+	const size_t nv = h->nverts;
+	std::vector<float4> g((size_t)a.nsub * a.ntips);
+	for (size_t i = 0; i < g.size(); i++)
+		g[i] = make_float4(grad_tip_traj[3 * i], grad_tip_traj[3 * i + 1], grad_tip_traj[3 * i + 2], 0.0f);
+	if (!g.empty())
+		XCUDA(cudaMemcpyAsync(a.grad.p, g.data(), g.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+	// abar = the canonical dL/dX, dL/dV at the end, scattered to device order
+	XCUDA(cudaMemsetAsync(a.abar.p, 0, 2 * nv * sizeof(float4), h->stream));
+	for (int which = 0; which < 2; which++) {
+		const float* src = which == 0 ? grad_x : grad_v;
+		if (!src) continue;
+		float* stage = h->io.p + 3 * nv * which;
+		XCUDA(cudaMemcpyAsync(stage, src, 3 * nv * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+		if (launch_scatter_xyz(a.abar.p, which, h->dev_of_vert.p, (uint32_t)nv, stage, h->stream))
+			return fail(XFEM_ECUDA, "scatter launch failed");
+	}
+	XCUDA(cudaMemsetAsync(a.cbar.p, 0, (size_t)h->nrows * kLanes * sizeof(float), h->stream));
+	int block = 0;
+	int rc = adjoint_block(h, &block);
+	if (rc) return rc;
+	if (const int e = configure_adjoint_kernels(block, h->cfg.warp_smem))
+		return fail(XFEM_ECUDA, std::string("adjoint kernel configuration: ") + cudaGetErrorString((cudaError_t)e));
+	const AdjCtx actx = {a.abar.p, a.cbar.p, a.grad.p};
+	for (int j = (int)a.nseg - 1; j >= 0; j--) {
+		const DevCtx c = tape_ctx(h, (uint32_t)j);
+		if (a.nseg > 1) {  // rebuild this segment's tape from its checkpoint
+			XCUDA(cudaMemcpyAsync(h->vert.p, a.ckpt.p + 2 * nv * j, 2 * nv * sizeof(float4), cudaMemcpyDeviceToDevice,
+			                      h->stream));
+			const int e = launch_substeps_tape(c, block, h->cfg.warp_smem, seg_len(a, j), a.dt, h->stream);
+			if (e) return fail(XFEM_ECUDA, std::string("recording launch: ") + cudaGetErrorString((cudaError_t)e));
+		}
+		const int e = launch_reverse(c, actx, block, h->cfg.warp_smem, h->max_colour_chunks, seg_len(a, j), a.dt,
+		                             j == (int)a.nseg - 1, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("reverse launch: ") + cudaGetErrorString((cudaError_t)e));
+	}
+	if (a.nseg > 1)
+		XCUDA(cudaMemcpyAsync(h->vert.p, a.ckpt.p + 2 * nv * a.nseg, 2 * nv * sizeof(float4), cudaMemcpyDeviceToDevice,
+		                      h->stream));
+	// outputs in caller order, gathered on the device
+	if (dx0 && launch_gather_xyz(a.abar.p, 0, h->dev_of_vert.p, (uint32_t)nv, h->io.p, h->stream))
+		return fail(XFEM_ECUDA, "gather launch failed");
+	if (dv0 && launch_gather_xyz(a.abar.p, 1, h->dev_of_vert.p, (uint32_t)nv, h->io.p + 3 * nv, h->stream))
+		return fail(XFEM_ECUDA, "gather launch failed");
+	if (dmu && launch_gather_dmu(a.cbar.p, h->tet_slot_dev.p, h->tet_inv_mu.p, h->ntets, h->io.p + 6 * nv, h->stream))
+		return fail(XFEM_ECUDA, "gather launch failed");
+	if (dx0) XCUDA(cudaMemcpyAsync(dx0, h->io.p, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+	if (dv0) XCUDA(cudaMemcpyAsync(dv0, h->io.p + 3 * nv, 3 * nv * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+	if (dmu) XCUDA(cudaMemcpyAsync(dmu, h->io.p + 6 * nv, h->ntets * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
+	return check_device_error(h);
+}
 
 }  // extern "C"

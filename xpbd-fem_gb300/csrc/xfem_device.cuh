@@ -1,0 +1,433 @@
+// Device helpers shared by the forward substep kernels (xfem_kernels.cu) and
+// the adjoint kernels (xfem_adjoint.cu): the bounded grid barrier, the
+// per-vertex advance (finalize + predict), the element solve and the
+// bulk-copy staging of chunk blocks. Internal linkage: each translation
+// unit gets its own copy.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "xfem_internal.h"
+
+namespace xfem {
+
+namespace {
+
+constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;  // 2 s: far above any legal wait
+
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+	uint32_t v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Grid-wide barrier for the co-resident persistent grid. Monotonic arrival
+// counter (zeroed before each launch); every wait is bounded: on timeout the
+// block records kErrBarrierTimeout and all blocks leave at their next barrier.
+__device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
+	__shared__ int s_ok;
+	__syncthreads();
+	target += gridDim.x;
+	if (threadIdx.x == 0) {
+		int ok = 1;
+		__threadfence();
+		atomicAdd(C.bar_count, 1u);
+		uint32_t spins = 0;
+		uint64_t t0 = 0;
+		while (ld_acquire_gpu(C.bar_count) < target) {
+			if (++spins == 256) {
+				spins = 0;
+				if (*(volatile int*)C.err) {
+					ok = 0;
+					break;
+				}
+				const uint64_t t = global_ns();
+				if (t0 == 0) {
+					t0 = t;
+				} else if (t - t0 > kBarrierTimeoutNs) {
+					atomicCAS(C.err, 0, kErrBarrierTimeout);
+					ok = 0;
+					break;
+				}
+			}
+		}
+		s_ok = ok;
+	}
+	__syncthreads();
+	return s_ok != 0;
+}
+
+struct Vec3 {
+	float x, y, z;
+};
+
+__device__ __forceinline__ Vec3 v3(float4 a) { return {a.x, a.y, a.z}; }
+__device__ __forceinline__ float dot(Vec3 a, Vec3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+
+// Ground plane with Coulomb friction on the substep displacement D
+// (extension; no reference counterpart). Returns true on contact.
+__device__ __forceinline__ bool ground_contact(const BodyParams& bp, const float4& O, float4& D) {
+	const float nx = bp.ground_n[0], ny = bp.ground_n[1], nz = bp.ground_n[2];
+	const float h = (nx * O.x + ny * O.y + nz * O.z) - bp.ground_d;
+	const float depth = -(h + (nx * D.x + ny * D.y + nz * D.z));
+	if (!(depth > 0.0f)) return false;
+	D.x += depth * nx;
+	D.y += depth * ny;
+	D.z += depth * nz;
+	const float dn = nx * D.x + ny * D.y + nz * D.z;
+	const float tx = D.x - dn * nx, ty = D.y - dn * ny, tz = D.z - dn * nz;
+	const float lt = sqrtf(tx * tx + ty * ty + tz * tz);
+	const float lim = bp.friction * depth;
+	const float s = lt <= lim ? 1.0f : lim / lt;
+	D.x -= s * tx;
+	D.y -= s * ty;
+	D.z -= s * tz;
+	return true;
+}
+
+// End of a substep for one vertex: locks (XPBDFEM/Geo.cpp:318-322), ground,
+// then the velocity V = D / dt (XPBDFEM/Geo.cpp:342-344) is returned.
+__device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, float4& D, uint32_t& bits, float inv_dt) {
+	if (bp.lock_active && (bits & kFlagLocked)) {
+		D.x = D.y = D.z = 0.0f;
+		O.w = 0.0f;
+	}
+	bits &= ~kFlagContact;
+	if (bp.ground && O.w > 0.0f && ground_contact(bp, O, D)) bits |= kFlagContact;
+	return {D.x * inv_dt, D.y * inv_dt, D.z * inv_dt};
+}
+
+// Finalize the previous substep (unless `first`: (O, D) then hold the
+// canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312).
+__device__ __forceinline__ void advance_vertex(const BodyParams* bodies, float4& O, float4& D, bool first, float dt,
+                                               float inv_dt) {
+	uint32_t bits = __float_as_uint(D.w);
+	const BodyParams& bp = bodies[bits >> 8];
+	Vec3 V;
+	if (first) {
+		V = v3(D);
+	} else {
+		V = finish_vertex(bp, O, D, bits, inv_dt);
+		O.x += D.x;
+		O.y += D.y;
+		O.z += D.z;
+	}
+	V.x = (V.x + bp.gravity[0] * dt) * bp.drag_mul;
+	V.y = (V.y + bp.gravity[1] * dt) * bp.drag_mul;
+	V.z = (V.z + bp.gravity[2] * dt) * bp.drag_mul;
+	D = make_float4(V.x * dt, V.y * dt, V.z * dt, __uint_as_float(bits));
+}
+
+// Finalize the last substep of a launch: (O, D) -> canonical (X, V).
+__device__ __forceinline__ void finalize_vertex(const BodyParams* bodies, float4& O, float4& D, float inv_dt) {
+	uint32_t bits = __float_as_uint(D.w);
+	const BodyParams& bp = bodies[bits >> 8];
+	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt);
+	O.x += D.x;
+	O.y += D.y;
+	O.z += D.z;
+	D = make_float4(V.x, V.y, V.z, __uint_as_float(bits));
+}
+
+// Rest state of one tet: Qi column-major q[c][r], QQ, QR and c0 = (1/mu)/vol.
+struct TetRec {
+	float4 a, b, c, d;
+};
+
+// The material scalars a solve needs, copied to registers once per cluster.
+struct Mat {
+	float a, ratio, y0, y1, y2;
+	uint32_t energy, simultaneous;
+};
+
+__device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body) {
+	const BodyParams* b = bodies + body;
+	return {__ldg(&b->a), __ldg(&b->ratio), __ldg(&b->yeoh[0]), __ldg(&b->yeoh[1]), __ldg(&b->yeoh[2]),
+	        __ldg(&b->energy), __ldg(&b->simultaneous)};
+}
+
+// Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with the
+// adjugate :284-300, F :311-323 and the gradient :338-354). J is formed as
+// the reference forms it, det(F) of F = Qi Ds (rows of Ds: P0, P1, P2) through
+// the first adjugate column: with an incompressible material the multiplier
+// goes as 1 / (J - a), so J's rounding decides the result and must follow the
+// reference's path. The gradient (2 (J - a) adj(F) Qi) e_n equals
+// 2 (J - a) det(Qi) times the cofactor row of Ds (P1 x P2, P2 x P0, P0 x P1):
+// same quantity, a third of the arithmetic. Returns U1 = (J - a)^2.
+__device__ __forceinline__ Vec3 cross(Vec3 a, Vec3 b) {
+	return {fmaf(a.y, b.z, -b.y * a.z), fmaf(a.z, b.x, -b.z * a.x), fmaf(a.x, b.y, -b.x * a.y)};
+}
+
+// ja, detq (optional): J - a and det(Qi), for the adjoint.
+__device__ __forceinline__ float hydrostatic(const float q[3][3], const Vec3 P[3], float a, Vec3 g[4],
+                                             float* ja = nullptr, float* detq = nullptr) {
+	const float detQ = fmaf(q[0][0], fmaf(q[1][1], q[2][2], -q[2][1] * q[1][2]),
+	                        fmaf(-q[1][0], fmaf(q[0][1], q[2][2], -q[2][1] * q[0][2]),
+	                             q[2][0] * fmaf(q[0][1], q[1][2], -q[1][1] * q[0][2])));
+	const Vec3 c0 = cross(P[1], P[2]), c1 = cross(P[2], P[0]), c2 = cross(P[0], P[1]);
+	// F[j][r] = sum_n Qi[n][r] P_n[j] (column j, row r)
+	const float Pc[3][3] = {{P[0].x, P[1].x, P[2].x}, {P[0].y, P[1].y, P[2].y}, {P[0].z, P[1].z, P[2].z}};
+	float F[3][3];
+#pragma unroll
+	for (int j = 0; j < 3; j++)
+#pragma unroll
+		for (int r = 0; r < 3; r++) F[j][r] = fmaf(q[0][r], Pc[j][0], fmaf(q[1][r], Pc[j][1], q[2][r] * Pc[j][2]));
+	const float a00 = fmaf(F[1][1], F[2][2], -F[1][2] * F[2][1]);
+	const float a10 = -fmaf(F[1][0], F[2][2], -F[1][2] * F[2][0]);
+	const float a20 = fmaf(F[1][0], F[2][1], -F[1][1] * F[2][0]);
+	const float J = fmaf(F[0][0], a00, fmaf(F[0][1], a10, F[0][2] * a20));
+	const float Ja = J - a;
+	const float s = 2.0f * Ja * detQ;
+	g[0] = {s * c0.x, s * c0.y, s * c0.z};
+	g[1] = {s * c1.x, s * c1.y, s * c1.z};
+	g[2] = {s * c2.x, s * c2.y, s * c2.z};
+	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
+	if (ja) *ja = Ja;
+	if (detq) *detq = detQ;
+	return Ja * Ja;
+}
+
+// 1/x to about one ulp: hardware approximation plus one Newton step. The
+// arguments are sums of squares plus 1e-22 (or a clamp at 1e-8), never zero,
+// denormal or infinite.
+__device__ __forceinline__ float rcp(float x) {
+	float r;
+	asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+	return fmaf(r, fmaf(-x, r, 1.0f), r);
+}
+
+// Deviatoric term, prefactored (XPBDFEM/Fem.cpp:163-192), with the Yeoh
+// transform of XPBDFEM/Fem.cpp:525-531 when energy == 7.
+__device__ __forceinline__ float deviatoric(const Mat& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
+                                            Vec3 g[4]) {
+	float U = QQ[0] * dot(P[0], P[0]);
+	U = fmaf(QQ[1], dot(P[1], P[1]), U);
+	U = fmaf(QQ[2], dot(P[2], P[2]), U);
+	U = fmaf(QR[0], dot(P[0], P[1]), U);
+	U = fmaf(QR[1], dot(P[0], P[2]), U);
+	U = fmaf(QR[2], dot(P[1], P[2]), U);
+	const float d0 = 2.0f * QQ[0], d1 = 2.0f * QQ[1], d2 = 2.0f * QQ[2];
+	g[0] = {fmaf(d0, P[0].x, fmaf(QR[0], P[1].x, QR[1] * P[2].x)), fmaf(d0, P[0].y, fmaf(QR[0], P[1].y, QR[1] * P[2].y)),
+	        fmaf(d0, P[0].z, fmaf(QR[0], P[1].z, QR[1] * P[2].z))};
+	g[1] = {fmaf(d1, P[1].x, fmaf(QR[0], P[0].x, QR[2] * P[2].x)), fmaf(d1, P[1].y, fmaf(QR[0], P[0].y, QR[2] * P[2].y)),
+	        fmaf(d1, P[1].z, fmaf(QR[0], P[0].z, QR[2] * P[2].z))};
+	g[2] = {fmaf(d2, P[2].x, fmaf(QR[1], P[0].x, QR[2] * P[1].x)), fmaf(d2, P[2].y, fmaf(QR[1], P[0].y, QR[2] * P[1].y)),
+	        fmaf(d2, P[2].z, fmaf(QR[1], P[0].z, QR[2] * P[1].z))};
+	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
+	if (bp.energy == 7u) {
+		const float IM = U - 3.0f;
+		const float C0 = bp.y0, C1 = bp.y1, C2 = bp.y2;
+		U = fmaxf(0.0001f, IM * fmaf(IM, fmaf(IM, C2, C1), C0));
+		const float gs = fmaf(IM, fmaf(IM, 3.0f * C2, 2.0f * C1), C0);
+#pragma unroll
+		for (int n = 0; n < 4; n++) g[n] = {g[n].x * gs, g[n].y * gs, g[n].z * gs};
+	}
+	return U;
+}
+
+__device__ __forceinline__ float wdot(const float w[4], const Vec3 a[4], const Vec3 b[4]) {
+	float s = 1.0e-22f;
+#pragma unroll
+	for (int n = 0; n < 4; n++) s = fmaf(w[n], dot(a[n], b[n]), s);
+	return s;
+}
+
+// One element solve: SolveElementMixed<MixedSelective | YeohSkinFast> tet path
+// (XPBDFEM/Fem.cpp:437-564) with EnergyXpbdConstrainSimultaneous<2>
+// (XPBDFEM/Xpbd.h:123-215) or the serial EnergyXpbdConstrain pair
+// (XPBDFEM/Xpbd.h:87-121). O[]: start positions + w, D[]: displacements
+// (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
+// alpha1 = alpha0 * (mu / lambda), i.e. (1/lambda)/volume/dt^2.
+__device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, float inv_dt2, const float4 O[4],
+                                            float4 D[4]) {
+	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
+	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
+	const float QR[3] = {r.d.x, r.d.y, r.d.z};
+	const float alpha0 = r.d.w * inv_dt2;
+	const float alpha1 = alpha0 * bp.ratio;
+	const float w[4] = {O[0].w, O[1].w, O[2].w, O[3].w};
+	Vec3 P[3];
+#pragma unroll
+	for (int i = 0; i < 3; i++)
+		P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+		        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+	Vec3 g0[4], g1[4];
+	const float U0 = deviatoric(bp, QQ, QR, P, g0);
+	float l0, l1;
+	if (bp.simultaneous) {
+		const float U1 = hydrostatic(q, P, bp.a, g1);
+		const float A0 = fmaf(2.0f * U0, alpha0, wdot(w, g0, g0));
+		const float A1 = wdot(w, g1, g0);
+		const float A2 = fmaf(2.0f * U1, alpha1, wdot(w, g1, g1));
+		const float b0 = -2.0f * U0, b1 = -2.0f * U1;
+		// Cramer's rule as in XPBDFEM/Xpbd.h:172-180
+		const float i00 = rcp(A0), i11 = rcp(A2);
+		const float r0 = A1 * i00, r1 = A1 * i11;
+		const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
+		const float c0 = b0 * i00, c1 = b1 * i11;
+		l0 = inv_det * fmaf(-r0, c1, c0);
+		l1 = inv_det * fmaf(-c0, r1, c1);
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			D[n].x = fmaf(w[n], fmaf(l1, g1[n].x, l0 * g0[n].x), D[n].x);
+			D[n].y = fmaf(w[n], fmaf(l1, g1[n].y, l0 * g0[n].y), D[n].y);
+			D[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), D[n].z);
+		}
+	} else {
+		l0 = (-2.0f * U0) * rcp(fmaf(2.0f * U0, alpha0, wdot(w, g0, g0)));
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l0;
+			D[n].x = fmaf(s, g0[n].x, D[n].x);
+			D[n].y = fmaf(s, g0[n].y, D[n].y);
+			D[n].z = fmaf(s, g0[n].z, D[n].z);
+		}
+#pragma unroll
+		for (int i = 0; i < 3; i++)
+			P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+			        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+		const float U1 = hydrostatic(q, P, bp.a, g1);
+		l1 = (-2.0f * U1) * rcp(fmaf(2.0f * U1, alpha1, wdot(w, g1, g1)));
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l1;
+			D[n].x = fmaf(s, g1[n].x, D[n].x);
+			D[n].y = fmaf(s, g1[n].y, D[n].y);
+			D[n].z = fmaf(s, g1[n].z, D[n].z);
+		}
+	}
+	return make_float2(l0, l1);
+}
+
+
+// ---- chunk staging: one TMA bulk copy per chunk into the warp's buffer ----
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* m) {
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(m)) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Issued by one lane: expect `bytes` on the barrier and start the copy.
+// The chunk records stream through L2 once per substep (about as large as
+// L2); they are fetched with an evict-first policy so that they do not push
+// the small, hot vertex state out of L2.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+	uint64_t policy;
+	asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(policy));
+	asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+	asm volatile(
+	    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+	        smem_u32(dst)),
+	    "l"(src), "r"(bytes), "r"(smem_u32(mbar)), "l"(policy)
+	    : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* m, uint32_t parity) {
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(m)), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+
+// Bounded wait for the copy of the current phase. On timeout the error word
+// is set and the wait continues for one more bounded period so that no copy
+// is left in flight when the block leaves.
+__device__ bool mbar_wait(const DevCtx& C, uint64_t* m, uint32_t parity) {
+	uint64_t t0 = 0;
+	for (uint32_t spins = 0;; spins++) {
+		if (mbar_test(m, parity)) return true;
+		if ((spins & 1023u) == 1023u) {
+			const uint64_t t = global_ns();
+			if (t0 == 0) {
+				t0 = t;
+			} else if (t - t0 > kBarrierTimeoutNs) {
+				atomicCAS(C.err, 0, kErrCopyTimeout);
+				for (uint32_t k = 0;; k++) {
+					if (mbar_test(m, parity)) break;
+					if ((k & 1023u) == 1023u && global_ns() - t > kBarrierTimeoutNs) break;
+				}
+				return false;
+			}
+		}
+	}
+}
+
+// Per-warp staging state: the chunk buffer, the vertex slots, the barrier.
+struct Stage {
+	uint8_t* buf;     // chunk block (records, header, vertex ids, slots)
+	float4* vs;       // vertex slots: O at [s * 32 + lane], D at [(nvmax + s) * 32 + lane]
+	uint64_t* mbar;
+	uint32_t parity;
+	int inflight;     // chunk whose copy is in flight or resident, -1 = none
+};
+
+__device__ __forceinline__ void stage_issue(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	__syncwarp();
+	if (lane == 0) bulk_copy_g2s(st.buf, C.cblk + m.x, m.y, st.mbar);
+	st.inflight = (int)chunk;
+}
+
+// Starts the copy of `chunk` when the buffer is idle (dataflow mode issues it
+// before waiting on neighbours: records never depend on them).
+__device__ __forceinline__ void stage_issue_or_wait(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	if (st.inflight < 0) stage_issue(C, st, chunk, lane);
+}
+
+// Makes `chunk` resident in the warp's buffer. Returns false on timeout.
+__device__ __forceinline__ bool stage_acquire(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	if (st.inflight != (int)chunk) {
+		if (st.inflight >= 0) {  // a different copy is in flight: let it land first
+			if (!mbar_wait(C, st.mbar, st.parity)) return false;
+			st.parity ^= 1u;
+		}
+		stage_issue(C, st, chunk, lane);
+	}
+	const bool ok = mbar_wait(C, st.mbar, st.parity);
+	st.parity ^= 1u;
+	st.inflight = -1;
+	return ok;
+}
+
+// Chunks whose clusters are all whole cubes of the 6-tet split in the
+// generator's corner order (every configuration mesh) share one local
+// topology, so the 8 vertices stay in registers and the 6 solves unroll with
+// compile-time slots: no shared-memory round trip inside the sequential chain.
+// Local slot k of tet t: {0123, 0341, 0543, 0365, 0763, 0327}, packed four bits per slot.
+__host__ __device__ constexpr int cube_slot(int t, int k) {
+	return (int)(((t == 0   ? 0x3210u
+	               : t == 1 ? 0x1430u
+	               : t == 2 ? 0x3450u
+	               : t == 3 ? 0x5630u
+	               : t == 4 ? 0x3670u
+	                        : 0x7230u) >>
+	              (4 * k)) &
+	             15u);
+}
+
+__device__ __forceinline__ Stage stage_init(const DevCtx& C, uint32_t lane) {
+	extern __shared__ __align__(128) uint8_t smem[];
+	__shared__ uint64_t mbars[32];
+	const uint32_t w = threadIdx.x >> 5;
+	uint8_t* base = smem + (size_t)w * C.warp_smem;
+	Stage st = {base, reinterpret_cast<float4*>(base + C.chunk_smem), &mbars[w], 0u, -1};
+	if (lane == 0) mbar_init(st.mbar);
+	__syncwarp();
+	return st;
+}
+
+}  // namespace
+
+}  // namespace xfem

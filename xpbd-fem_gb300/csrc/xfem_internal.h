@@ -105,6 +105,29 @@ struct DevCtx {
 	uint32_t warp_smem;         // chunk_smem + vertex slots (2 x nvmax x 32 x 16 B)
 	uint32_t* bar_count;        // grid barrier arrival counter
 	int* err;                   // device error word (0 = ok)
+	// Adjoint tape, written only by the recording forward kernel (null otherwise).
+	// Substep indices are relative to the launch; `sub_base` is the launch's
+	// first substep in the whole run (checkpointed segments).
+	float4* tape_v;             // [substep][vertex] x 2 (one 32-byte sector): O after the
+	                            // advance (the substep's start, with the w its solves
+	                            // use) and D before it (the previous substep's swept D,
+	                            // or V on a launch's first substep), written by the owner
+	float4* tape_t;             // [substep][tet row][3][lane]: each solve's input D of its
+	                            // four vertices, 12 floats in three float4
+	float4* tape_fin;           // [vertex]: D before the closing finalize
+	float4* traj;               // [run substep][tip]: position after each substep
+	const int32_t* tip_of;      // per vertex: tip index or -1
+	uint32_t ntrows, sub_base, ntips, pad_;
+};
+
+// Reverse-pass state (xfem_adjoint.cu).
+struct AdjCtx {
+	float4* abar;        // 2 per vertex: adjoint of the current position X = O + D,
+	                     // and of O from the later substeps. At the end of the run
+	                     // (in) and at its start (out): dL/dX, dL/dV of the
+	                     // canonical state.
+	float* cbar;         // [tet row][lane]: sum over substeps of alpha0 * dL/dalpha0 + alpha1 * dL/dalpha1 (= -mu dL/dmu)
+	const float4* G;     // [run substep][tip]: dL/d(tip position after the substep)
 };
 
 // Vertex flag bits kept in the .w word of the second float4.
@@ -145,11 +168,29 @@ size_t solve_smem_bytes(int block, uint32_t warp_smem);
 int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bool lambdas, uint32_t nsub, float dt,
                             void* stream, int device, int* device_error);
 
+// Adjoint (xfem_adjoint.cu, xfem_kernels.cu). The recording forward runs nsub
+// substeps exactly as the persistent kernel does (same results bit for bit)
+// and writes the tape of ctx. The reverse kernel runs the segment's substeps
+// backwards from that tape (`last`: the run's final segment, whose closing
+// finish receives the caller's dL/dX, dL/dV). Both are cooperative
+// persistent launches.
+int launch_substeps_tape(const DevCtx& ctx, int block, uint32_t warp_smem, uint32_t nsub, float dt, void* stream);
+int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t warp_smem, uint32_t max_colour_chunks,
+                   uint32_t nsub, float dt, bool last, void* stream);
+int configure_adjoint_kernels(int block, uint32_t warp_smem);
+
 // Transfer helpers (caller order <-> device order), run on `stream`.
 int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, float* out,
                       void* stream);
 int launch_scatter_xyz(float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, const float* in,
                        void* stream);
 int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, double* out, void* stream);
+// Per-tet material (n tets from the given per-tet tables): c0 of each record
+// and 1/mu; mu null = mu_uniform for all.
+int launch_set_c0(float4* cblk, const uint32_t* rec, const float* vol, const float* mu, float mu_uniform, uint32_t n,
+                  float* inv_mu, void* stream);
+// out[t] = -cbar[slot[t]] / mu[t]
+int launch_gather_dmu(const float* cbar, const uint32_t* slot, const float* inv_mu, uint32_t n, float* out,
+                      void* stream);
 
 }  // namespace xfem

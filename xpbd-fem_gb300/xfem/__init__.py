@@ -71,7 +71,7 @@ EXPORTS = [
     "xfem_get_lambdas", "xfem_calculate_volume", "xfem_get_rest_state", "xfem_get_schedule",
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
-    "xfem_step_frames_noalloc",
+    "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward",
 ]
 
 _lib = None
@@ -116,6 +116,8 @@ def lib():
         L.xfem_compute_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P]
         L.xfem_compute_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P]
         L.xfem_generate_tet_block.argtypes = [u32, u32, u32, f32, f32, f32, u32, f32, P, P]
+        L.xfem_adjoint_forward.argtypes = [P, u32, f32, u32, u32, P, P]
+        L.xfem_adjoint_backward.argtypes = [P, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -320,3 +322,29 @@ class Body:
         cb = np.zeros(ncol.value + 1, np.uint32)
         _check(lib().xfem_get_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb, colours=ncol.value)
+
+    # -- reverse-mode adjoint (no reference counterpart; see include/xfem.h)
+    def total_counts(self):
+        """Vertices and tets of the whole handle (concatenated caller order)."""
+        return sum(c[0] for c in self.counts), sum(c[1] for c in self.counts)
+
+    def adjoint_forward(self, substeps, dt, tips, checkpoint_every=0):
+        """Steps `substeps` substeps recording the tape; returns the tip
+        trajectory, shape (substeps, len(tips), 3)."""
+        t = np.ascontiguousarray(tips, np.uint32).reshape(-1)
+        traj = np.zeros((substeps, t.size, 3), np.float32)
+        _check(lib().xfem_adjoint_forward(self._h, substeps, dt, checkpoint_every, t.size, _p(t), _p(traj)))
+        return traj
+
+    def adjoint_backward(self, grad_traj, grad_x=None, grad_v=None):
+        """Reverse pass of the last adjoint_forward. Returns (dL/dmu per tet,
+        dL/dX0, dL/dV0) in the handle's concatenated caller order."""
+        nv, nt = self.total_counts()
+        g = np.ascontiguousarray(grad_traj, np.float32).reshape(-1)
+        gx = None if grad_x is None else np.ascontiguousarray(grad_x, np.float32).reshape(-1)
+        gv = None if grad_v is None else np.ascontiguousarray(grad_v, np.float32).reshape(-1)
+        dmu = np.zeros(nt, np.float32)
+        dx = np.zeros((nv, 3), np.float32)
+        dv = np.zeros((nv, 3), np.float32)
+        _check(lib().xfem_adjoint_backward(self._h, _p(g), _p(gx), _p(gv), _p(dmu), _p(dx), _p(dv)))
+        return dmu, dx, dv

@@ -189,3 +189,28 @@ def batched(seed=4, nbodies=512, lo=2, hi=24):
         settings.append(s)
     return dict(name=f"batched {nbodies} bodies", meshes=meshes, settings=settings, dt=1.0 / 60.0, substeps=20,
                 frames=1, dims=dims)
+
+
+def adjoint_beam(seed=5, W=32, H=8, D=8, nsub=200, ntips=20, nu=0.45):
+    """Differentiation workload: a 32x8x8-cube beam (12,288 tets, 2,673
+    nodes) of 0.025 m cubes, x = min face fixed, gravity -z, Neo-Hookean with
+    nu = 0.45 (compressible, so the coupled solve is well conditioned and the
+    derivative is smooth) and a per-tet Young's modulus log E ~ N(log 1e5,
+    0.3^2). 20 tip nodes spread over the free end face; the target
+    trajectory is that of the same beam under a second field drawn from the
+    same distribution. 200 substeps of 1/1200 s. Returns the two per-tet mu
+    fields (the reference's mu = 1/compliance = E / (4 (1 + nu)))."""
+    rng = Rng(seed)
+    nodes, idx = box(W, H, D, 0.025)
+    n = nodes.reshape(-1, 3)
+    n[:, 0] -= n[:, 0].min()
+    nt = 6 * W * H * D
+    mu = np.exp(math.log(1e5) + 0.3 * rng.normal(nt)) / (4.0 * (1.0 + nu))
+    mu_target = np.exp(math.log(1e5) + 0.3 * rng.normal(nt)) / (4.0 * (1.0 + nu))
+    face = np.nonzero(n[:, 0] == n[:, 0].max())[0]
+    tips = face[np.linspace(0, face.size - 1, ntips).round().astype(np.int64)].astype(np.uint32)
+    s = default_settings(gravity=(0.0, 0.0, -9.81), compliance=nh_compliance(1e5, nu), poissons_ratio=nu,
+                         flags=NH_FLAGS)
+    return dict(name=f"adjoint beam {W}x{H}x{D} ({nt} tets)", nodes=nodes, idx=idx, density=1000.0, settings=s,
+                lock=lock_mask_axis(nodes, 0), mu=mu.astype(np.float32), mu_target=mu_target.astype(np.float32),
+                tips=tips, dt=1.0 / 1200.0, substeps=nsub)
