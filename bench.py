@@ -17,7 +17,10 @@ shape the configuration names.
            reads the positions back (host-timed, copies included);
   roofline, cpu_baseline (the oracle port of the reference in its own
   shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches, and
-  "batched": 512 bodies in one launch per frame against one launch per body.
+  "batched": 512 bodies in one launch per frame against one launch per body,
+  "adjoint": cost of the reverse-mode gradient (recording forward + backward)
+  against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
+  checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
 --impl reference: the reference's CPU algorithm (the oracle port, run in the
   GPU's colour order with all host threads) on the same mesh; each step is a
   bounded sample of substeps.
@@ -284,6 +287,7 @@ def run_xfem(args, world, rank, local):
     traffic = None if NCU_DRAM_BYTES_PER_TET_SUBSTEP is None else NCU_DRAM_BYTES_PER_TET_SUBSTEP * nt * S
     cpu = cpu_baseline_native(w) if not args.no_cpu else None
     batched = None if args.no_batched else run_batched(stream)
+    adjoint = None if args.no_adjoint else run_adjoint(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -302,6 +306,7 @@ def run_xfem(args, world, rank, local):
                 "steps": e2e_steps},
         "gpu_launches": launches_per_frame * args.steps,
         "batched": batched,
+        "adjoint": adjoint,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -357,6 +362,78 @@ def run_batched(stream, frames=5, plain_frames=2):
             "launches_per_frame": 1 if info["sync_mode"] != 2 else 20 * info["colours"] + 1}
 
 
+def run_adjoint(stream, reps=5, cases=("beam", "large"), large_substeps=None):
+    """Cost of the gradient: the recording forward (xfem_adjoint_forward) and
+    the reverse pass (xfem_adjoint_backward, host cotangent in, dL/dmu, dL/dX0,
+    dL/dV0 out) against the plain forward (xfem_step_frames) of the same
+    substeps, each device-timed with CUDA events on the solver's stream around
+    the synchronising C ABI calls (host copies included), median of `reps`."""
+    import torch
+
+    import xfem
+    from xfem import workloads as W
+    sp = C_void_p(stream.cuda_stream)
+
+    def ev_time(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            a.record(stream)
+        fn()
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    def measure(nodes, idx, s, lock, mu, tips, nsub, dt, ckpt):
+        body = xfem.Body(nodes, idx, 1000.0, s, stream=sp)
+        body.set_lock_mask(lock)
+        body.set_tet_mu(mu)
+        x0, v0 = body.positions(), body.velocities()
+        G = np.full((nsub, len(tips), 3), 1e-3, np.float32)
+
+        def reset():
+            body.set_positions(x0)
+            body.set_velocities(v0)
+            body.synchronize()
+
+        out = {"forward_ms": [], "record_ms": [], "backward_ms": [], "backward_ckpt_ms": []}
+        reset()
+        body.step_frames(1, nsub, dt)  # tunes the plain launch
+        for _ in range(reps):
+            reset()
+            out["forward_ms"].append(ev_time(lambda: (body.step_frames(1, nsub, dt), body.synchronize())))
+            reset()
+            out["record_ms"].append(ev_time(lambda: body.adjoint_forward(nsub, dt, tips, 0)))
+            out["backward_ms"].append(ev_time(lambda: body.adjoint_backward(G)))
+            if ckpt:
+                reset()
+                body.adjoint_forward(nsub, dt, tips, ckpt)
+                out["backward_ckpt_ms"].append(ev_time(lambda: body.adjoint_backward(G)))
+        body.close()
+        r = {k: statistics.median(v) for k, v in out.items() if v}
+        r["backward_over_forward"] = r["backward_ms"] / r["forward_ms"]
+        r["record_plus_backward_over_forward"] = (r["record_ms"] + r["backward_ms"]) / r["forward_ms"]
+        return r
+
+    res = {"timing": f"CUDA events around the synchronising C ABI calls, median of {reps}"}
+    if "beam" in cases:
+        d = W.adjoint_beam()
+        beam = measure(d["nodes"], d["idx"], d["settings"], d["lock"], d["mu"], d["tips"], d["substeps"], d["dt"], 20)
+        beam.update({"workload": d["name"], "substeps": d["substeps"], "tips": int(d["tips"].size),
+                     "checkpoint_every": 20})
+        res["beam"] = beam
+    if "large" in cases:
+        t = W.throughput()
+        nt = t["idx"].size // 5
+        mu = np.full(nt, 1.0 / t["settings"]["compliance"], np.float32)
+        S = large_substeps or t["substeps"]
+        big = measure(t["nodes"], t["idx"], t["settings"], t["lock"], mu, np.arange(20, dtype=np.uint32), S,
+                      t["dt"] / t["substeps"], 0)
+        big.update({"workload": t["name"], "substeps": S, "tips": 20})
+        res["large"] = big
+    return res
+
+
 def C_void_p(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -380,8 +457,19 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
+                    help="time only the adjoint (no main metric line)")
+    ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")
+    ap.add_argument("--adjoint-reps", type=int, default=5)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.adjoint_only:
+        import torch
+        stream = torch.cuda.Stream()
+        cases = ("beam", "large") if args.adjoint_only == "both" else (args.adjoint_only,)
+        print(json.dumps({"adjoint": run_adjoint(stream, args.adjoint_reps, cases, args.adjoint_substeps)}), flush=True)
+        return
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)

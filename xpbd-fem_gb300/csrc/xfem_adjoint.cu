@@ -48,7 +48,8 @@ __device__ __forceinline__ Vec3 vfma(Vec3 b, float s, Vec3 a) { return {fmaf(b.x
 // rows of Ds (P1 x P2, P2 x P0, P0 x P1), so dJ/dP_i = detQ cof_i.
 struct TetFw {
 	Vec3 P[3], g0[4], g1[4], cof[3];
-	float U0, U1, Ja, detQ, A0, A1, A2, l0, l1, alpha0, alpha1;
+	float U0, U1, Ja, detQ, A1, l0, l1, alpha0, alpha1;
+	float i00, i11, r0, r1, inv_det;  // the Cramer factors of M = [A0 A1; A1 A2]
 };
 
 __device__ __forceinline__ void tet_internals(const Mat& bp, const TetRec& r, float inv_dt2, const float4 O[4],
@@ -68,15 +69,17 @@ __device__ __forceinline__ void tet_internals(const Mat& bp, const TetRec& r, fl
 	f.cof[1] = cross(f.P[2], f.P[0]);
 	f.cof[2] = cross(f.P[0], f.P[1]);
 	const float w[4] = {O[0].w, O[1].w, O[2].w, O[3].w};
-	f.A0 = fmaf(2.0f * f.U0, f.alpha0, wdot(w, f.g0, f.g0));
+	const float A0 = fmaf(2.0f * f.U0, f.alpha0, wdot(w, f.g0, f.g0));
 	f.A1 = wdot(w, f.g1, f.g0);
-	f.A2 = fmaf(2.0f * f.U1, f.alpha1, wdot(w, f.g1, f.g1));
-	const float i00 = rcp(f.A0), i11 = rcp(f.A2);
-	const float r0 = f.A1 * i00, r1 = f.A1 * i11;
-	const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
-	const float c0 = (-2.0f * f.U0) * i00, c1 = (-2.0f * f.U1) * i11;
-	f.l0 = inv_det * fmaf(-r0, c1, c0);
-	f.l1 = inv_det * fmaf(-c0, r1, c1);
+	const float A2 = fmaf(2.0f * f.U1, f.alpha1, wdot(w, f.g1, f.g1));
+	f.i00 = rcp(A0);
+	f.i11 = rcp(A2);
+	f.r0 = f.A1 * f.i00;
+	f.r1 = f.A1 * f.i11;
+	f.inv_det = rcp(fmaxf(0.00000001f, fmaf(-f.r0, f.r1, 1.0f)));
+	const float c0 = (-2.0f * f.U0) * f.i00, c1 = (-2.0f * f.U1) * f.i11;
+	f.l0 = f.inv_det * fmaf(-f.r0, c1, c0);
+	f.l1 = f.inv_det * fmaf(-c0, f.r1, c1);
 }
 
 // Reverse of one coupled solve. xb[4]: adjoint of the tet's four positions
@@ -97,12 +100,9 @@ __device__ __forceinline__ float tet_reverse(const TetRec& r, const TetFw& f, co
 	}
 	// lambda = M^-1 b with M = [A0 A1; A1 A2] symmetric: m = M^-1 lambda_bar,
 	// b_bar = m, M_bar = -m lambda^T (same Cramer form as the forward)
-	const float i00 = rcp(f.A0), i11 = rcp(f.A2);
-	const float r0 = f.A1 * i00, r1 = f.A1 * i11;
-	const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
-	const float c0 = lb0 * i00, c1 = lb1 * i11;
-	const float m0 = inv_det * fmaf(-r0, c1, c0);
-	const float m1 = inv_det * fmaf(-c0, r1, c1);
+	const float c0 = lb0 * f.i00, c1 = lb1 * f.i11;
+	const float m0 = f.inv_det * fmaf(-f.r0, c1, c0);
+	const float m1 = f.inv_det * fmaf(-c0, f.r1, c1);
 	const float Ab0 = -m0 * f.l0, Ab2 = -m1 * f.l1, Ab1 = -fmaf(m0, f.l1, m1 * f.l0);
 	// b = (-2 U0, -2 U1); A0 = sum w |g0|^2 + 2 U0 alpha0; A1 = sum w g1.g0; A2 = sum w |g1|^2 + 2 U1 alpha1
 	const float Ub0 = fmaf(2.0f * f.alpha0, Ab0, -2.0f * m0);
@@ -394,8 +394,8 @@ __global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t ns
 
 int configure_adjoint_kernels(int, uint32_t) { return 0; }
 
-int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, uint32_t max_colour_chunks, uint32_t nsub,
-                   float dt, bool last, void* stream) {
+int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, uint32_t, uint32_t nsub, float dt, bool last,
+                   void* stream) {
 	if (nsub == 0) return 0;
 	cudaStream_t st = (cudaStream_t)stream;
 	int dev = 0, sms = 0, per_sm = 0;
@@ -404,12 +404,10 @@ int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, ui
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_reverse, block, 0);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
-	// no more blocks than the widest colour pass can use (one warp per
-	// chunk): a smaller grid makes every barrier cheaper
-	const uint32_t warps = (uint32_t)block / 32u;
-	uint32_t blocks = (max_colour_chunks + warps - 1) / warps;
-	blocks = blocks < 1u ? 1u : blocks;
-	if (blocks > (uint32_t)(per_sm * sms)) blocks = (uint32_t)(per_sm * sms);
+	// the whole co-resident grid, as the forward: chunk i of a colour goes to
+	// block i % grid, so a colour pass with fewer chunks than warps still
+	// spreads one chunk per SM (a pass lasts as long as its slowest chunk)
+	const uint32_t blocks = (uint32_t)(per_sm * sms);
 	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
