@@ -417,12 +417,13 @@ __host__ __device__ constexpr int cube_slot(int t, int k) {
 	             15u);
 }
 
+// The calling warp's chunk buffer, vertex slots and mbarrier.
 __device__ __forceinline__ Stage stage_init(const DevCtx& C, uint32_t lane) {
 	extern __shared__ __align__(128) uint8_t smem[];
 	__shared__ uint64_t mbars[32];
 	const uint32_t w = threadIdx.x >> 5;
 	uint8_t* base = smem + (size_t)w * C.warp_smem;
-	Stage st = {base, reinterpret_cast<float4*>(base + C.chunk_smem), &mbars[w], 0u, -1};
+	Stage st = {base, reinterpret_cast<float4*>(base + C.vs_off), &mbars[w], 0u, -1};
 	if (lane == 0) mbar_init(st.mbar);
 	__syncwarp();
 	return st;

@@ -102,7 +102,9 @@ struct DevCtx {
 	uint32_t* done;             // per chunk: substeps completed in this launch
 	uint32_t nverts, nisolated, ncolours, nchunks;
 	uint32_t chunk_smem;        // bytes of the largest chunk block
-	uint32_t warp_smem;         // chunk_smem + vertex slots (2 x nvmax x 32 x 16 B)
+	uint32_t warp_smem;         // chunk_smem + vertex slots (2 x nvmax x 32 x 16 B, none when
+	                            // every chunk takes the register-resident cube path)
+	uint32_t vs_off;            // byte offset of the vertex slots in a warp's area
 	uint32_t* bar_count;        // grid barrier arrival counter
 	int* err;                   // device error word (0 = ok)
 	// Adjoint tape, written only by the recording forward kernel (null otherwise).
