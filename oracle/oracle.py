@@ -29,13 +29,16 @@ class Params(C.Structure):
         ("compliance", C.c_float), ("poisson", C.c_float), ("energy", C.c_uint32),
         ("simultaneous", C.c_uint32), ("yeoh", C.c_float * 3), ("lock_active", C.c_uint32),
         ("ground", C.c_uint32), ("ground_n", C.c_float * 3), ("ground_d", C.c_float),
-        ("friction", C.c_float),
+        ("friction", C.c_float), ("damping", C.c_float), ("rayleigh_type", C.c_uint32),
+        ("pbd_damping", C.c_float), ("pbd_coeff", C.c_float), ("pbd_coeff_amortized", C.c_float),
+        ("tick", C.c_uint32),
     ]
 
 
 def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=True,
                 gravity=(0.0, 0.0, 0.0), drag=0.0, yeoh=REF_YEOH, lock=False,
-                ground=False, ground_n=(0.0, 0.0, 1.0), ground_d=0.0, friction=0.0):
+                ground=False, ground_n=(0.0, 0.0, 1.0), ground_d=0.0, friction=0.0, damping=0.0, rayleigh_type=2,
+                pbd_damping=0.0, pbd_coeff=0.0, pbd_coeff_amortized=0.0, tick=0):
     p = Params()
     p.gravity[:] = [float(g) for g in gravity]
     p.dt = dt
@@ -50,19 +53,34 @@ def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=T
     p.ground_n[:] = [float(c) for c in ground_n]
     p.ground_d = ground_d
     p.friction = friction
+    p.damping = damping
+    p.rayleigh_type = rayleigh_type
+    p.pbd_damping = pbd_damping
+    p.pbd_coeff = pbd_coeff
+    p.pbd_coeff_amortized = pbd_coeff_amortized
+    p.tick = tick
     return p
 
 
-def params_from_settings(s, dt, lock=True):
+def params_from_settings(s, dt, lock=True, tick=None):
     """orc_params from solver settings given as an xfem Settings struct or as
-    a dict of its fields (reference semantics)."""
-    g = (lambda k: s[k]) if isinstance(s, dict) else (lambda k: getattr(s, k))
+    a dict of its fields (reference semantics). tick: the tickId of the first
+    substep (default: the settings' tick_id)."""
+    def g(k, default=None):
+        if isinstance(s, dict):
+            return s.get(k, default) if default is not None else s[k]
+        return getattr(s, k, default) if default is not None else getattr(s, k)
     flags = int(g("flags"))
     return make_params(dt=dt, compliance=g("compliance"), poisson=g("poissons_ratio"), energy=(flags >> 6) & 31,
                        simultaneous=bool((flags >> 11) & 1), gravity=tuple(g("gravity")),
                        drag=g("time_corrected_drag"), yeoh=tuple(g("yeoh")),
                        lock=lock and bool(flags & (1 << 26)), ground=bool(g("ground")),
-                       ground_n=tuple(g("ground_normal")), ground_d=g("ground_offset"), friction=g("friction"))
+                       ground_n=tuple(g("ground_normal")), ground_d=g("ground_offset"), friction=g("friction"),
+                       damping=g("damping", 0.0), rayleigh_type=(flags >> 20) & 3,
+                       pbd_damping=g("pbd_damping", 0.0),
+                       pbd_coeff=g("volume_and_time_corrected_pbd_damping", 0.0),
+                       pbd_coeff_amortized=g("amortized_volume_and_time_corrected_pbd_damping", 0.0),
+                       tick=int(g("tick_id", 0)) if tick is None else int(tick))
 
 
 _lib = None
@@ -86,8 +104,8 @@ def lib():
         L.orc_minstd_order.argtypes = [u32, P]
         L.orc_init_rest_f.argtypes = [P, u32, P, u32, C.c_float, P, P, P]
         L.orc_init_rest_d.argtypes = [P, u32, P, u32, C.c_double, P, P, P]
-        L.orc_solve_tet_f.argtypes = [P, P, P, P, C.c_float, P]
-        L.orc_solve_tet_d.argtypes = [P, P, P, P, C.c_double, P]
+        L.orc_solve_tet_f.argtypes = [P, P, P, P, P, C.c_float, P]
+        L.orc_solve_tet_d.argtypes = [P, P, P, P, P, C.c_double, P]
         L.orc_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P, P]
         L.orc_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P, P]
         L.orc_substeps_threaded_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, P, u32, u32, P, u32]
@@ -141,13 +159,16 @@ def init_rest(nodes, tets, density, dtype=np.float32):
     return ep, w, fl
 
 
-def solve_tet(X, w, ep, params, mu_override=0.0, dtype=np.float32):
+def solve_tet(X, w, ep, params, mu_override=0.0, dtype=np.float32, O=None):
+    """One element solve; O (4x3, optional): start positions for the in-solve
+    Rayleigh damping."""
     X = np.array(X, np.float64).reshape(4, 3).copy()
+    Oa = None if O is None else np.ascontiguousarray(O, np.float64).reshape(4, 3)
     w = np.ascontiguousarray(w, dtype)
     ep = np.ascontiguousarray(ep, dtype)
     lam = np.zeros(2, dtype)
     f = lib().orc_solve_tet_f if dtype == np.float32 else lib().orc_solve_tet_d
-    if f(_p(X), _p(w), _p(ep), C.byref(params), mu_override, _p(lam)):
+    if f(_p(X), _p(Oa), _p(w), _p(ep), C.byref(params), mu_override, _p(lam)):
         raise ValueError("unsupported energy model")
     return X, lam
 

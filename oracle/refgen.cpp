@@ -32,6 +32,16 @@
  *       Same substep, but the constraint loop runs SolveElement over the tet
  *       order read from stdin (u32 count, then the order) — the replicated
  *       Substep used for same-order parity with the coloured GPU schedule.
+ *   damped W H D sx sy sz wonkiness density energy simultaneous compliance
+ *          poisson gx gy dt nsub lockleft damping pbdDamping drag rayleighType
+ *          spacing < order.u32
+ *       `ordered` with damping: Settings::damping, pbdDamping and drag, the
+ *       Rayleigh type in flags bits 20-21, and the derived fields filled as
+ *       Sim::Update does (XPBDFEM/Demo.cpp:53-63) with `spacing` in place of
+ *       the demo's kSpacing; Geo3d::Substep then runs GeoLinear3d::Damp
+ *       (XPBDFEM/Geo.cpp:346-355, 790-811) over the same order. Also dumps
+ *       the derived values (volume- and time-corrected PBD damping, its
+ *       amortized form, time-corrected drag).
  */
 #include <cstdio>
 #include <cstdlib>
@@ -146,7 +156,8 @@ int main(int argc, char** argv) {
 	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
 
-	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered")) {
+	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered") ||
+	    !strcmp(cmd, "damped")) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
 		uint32_t W = U(2), H = U(3), D = U(4);
 		vec3 scale(F(5), F(6), F(7));
@@ -174,11 +185,33 @@ int main(int argc, char** argv) {
 		float compliance = F(a++), poisson = F(a++), gx = F(a++), gy = F(a++), dt = F(a++);
 		uint32_t nsub = U(a++), lockLeft = U(a++);
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
+		const bool damped = !strcmp(cmd, "damped");
+		if (damped) {
+			s.damping = F(a++);
+			s.pbdDamping = F(a++);
+			s.drag = F(a++);
+			const uint32_t rtype = U(a++);
+			const float spacing = F(a++);
+			s.flags = (s.flags & ~(Settings_RayleighTypeMask << Settings_RayleighTypeBit)) |
+			          (rtype << Settings_RayleighTypeBit);
+			// XPBDFEM/Demo.cpp:53-63 with spacing for kSpacing
+			const float sdt = dt;
+			float tcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * sdt);
+			s.areaAndTimeCorrectedPbdDamping = tcpd * spacing * spacing;
+			s.volumeAndTimeCorrectedPbdDamping = tcpd * 6.0f * spacing * spacing;
+			float atcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * (float)AmortizationPeriod * sdt);
+			s.amortizedAreaAndTimeCorrectedPbdDamping = atcpd * spacing * spacing;
+			s.amortizedVolumeAndTimeCorrectedPbdDamping = atcpd * 6.0f * spacing * spacing;
+			s.timeCorrectedDrag = 1.0f - pow(1.0f - s.drag, 1000.0f * sdt);
+			const float derived[3] = {s.volumeAndTimeCorrectedPbdDamping, s.amortizedVolumeAndTimeCorrectedPbdDamping,
+			                          s.timeCorrectedDrag};
+			emit("derived", 'f', derived, 3);
+		}
 		Manipulator manip;
 		manip.pickedGeo = nullptr;
 		emit("nodes", 'f', nodes, nodeCount);
 		emit("idx", 'I', idx, idxCount);
-		if (!strcmp(cmd, "ordered")) {
+		if (!strcmp(cmd, "ordered") || damped) {
 			// Replace the shuffled tOrder by the order read from stdin; Geo3d::Substep
 			// then runs GeoLinear3d::Constrain (XPBDFEM/Geo.cpp:777) over it unchanged.
 			uint32_t n = 0;

@@ -17,6 +17,7 @@
 #define SFX _f
 #define SQRT sqrtf
 #define FMAX fmaxf
+#define FMIN fminf
 #define EPS22 1.0e-22f
 #define EPS8 0.00000001f
 #define EPS4 0.0001f
@@ -25,6 +26,7 @@
 #undef SFX
 #undef SQRT
 #undef FMAX
+#undef FMIN
 #undef EPS22
 #undef EPS8
 #undef EPS4
@@ -34,6 +36,7 @@
 #define SFX _d
 #define SQRT sqrt
 #define FMAX fmax
+#define FMIN fmin
 #define EPS22 1.0e-22
 #define EPS8 1.0e-8
 #define EPS4 1.0e-4
@@ -42,6 +45,7 @@
 #undef SFX
 #undef SQRT
 #undef FMAX
+#undef FMIN
 #undef EPS22
 #undef EPS8
 #undef EPS4
@@ -186,6 +190,8 @@ int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const u
                             const uint32_t* tets, const float* ep, const float* tet_mu, const uint32_t* order,
                             const uint32_t* colour_begin, uint32_t ncolours, uint32_t nsub, const orc_params* p,
                             uint32_t threads) {
+	/* the undamped method only: damping runs in orc_substeps_f */
+	if (p->damping > 0.0f || p->pbd_damping > 0.0f) return -1;
 	if (threads < 1) threads = 1;
 	if (threads > 256) threads = 256;
 	double* O = (double*)malloc(sizeof(double) * 3 * (size_t)(nv ? nv : 1));

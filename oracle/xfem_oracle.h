@@ -56,6 +56,13 @@ typedef struct orc_params {
 	float ground_n[3];
 	float ground_d;          /* plane dot(n, x) = d, solid where dot(n, x) < d */
 	float friction;          /* Coulomb coefficient */
+	/* Damping (XPBDFEM/Settings.h:85-86, 94-96, 102; XPBDFEM/Geo.cpp:346-355, 790-811) */
+	float damping;             /* Settings::damping, the Rayleigh ratio; 0 = off */
+	uint32_t rayleigh_type;    /* (flags >> 20) & 3: 0 Paper, 1 Limit (in the solve), 2 Post, 3 PostAmortized */
+	float pbd_damping;         /* Settings::pbdDamping (> 0 enables PBD damping) */
+	float pbd_coeff;           /* Settings::volumeAndTimeCorrectedPbdDamping */
+	float pbd_coeff_amortized; /* Settings::amortizedVolumeAndTimeCorrectedPbdDamping */
+	uint32_t tick;             /* Settings::tickId of the first substep; +1 per substep */
 } orc_params;
 
 /* ---- mesh ---------------------------------------------------------------- */
@@ -78,16 +85,19 @@ void orc_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* tets, uint
                      double density, double* ep, double* w, uint8_t* vflags);
 
 /* ---- one element (SolveElement, XPBDFEM/Fem.cpp:892) ---------------------- */
-/* X: 4x3 doubles, updated in place. mu_override <= 0 uses 1/compliance.
+/* X: 4x3 doubles, updated in place. O (nullable): the substep's start
+ * positions, which the in-solve Rayleigh damping (types 0, 1) reads; without
+ * O there is no damping term. mu_override <= 0 uses 1/compliance.
  * lambda_out (nullable) receives the two multipliers. Returns 0 or -1 for an
  * unsupported energy model. */
-int orc_solve_tet_f(double* X, const float* w, const float* ep, const orc_params* p,
+int orc_solve_tet_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p,
                     float mu_override, float* lambda_out);
-int orc_solve_tet_d(double* X, const double* w, const double* ep, const orc_params* p,
+int orc_solve_tet_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p,
                     double mu_override, double* lambda_out);
 
 /* ---- substeps (Geo3d::Substep, XPBDFEM/Geo.cpp:305-356) ------------------- */
-/* Runs nsub substeps. order[nt] is the constraint order (the reference's own
+/* Runs nsub substeps, damping included (GeoLinear3d::Damp over the same
+ * order). order[nt] is the constraint order (the reference's own
  * tOrder, or a coloured schedule flattened). w is updated in place (locks set
  * it to 0, as the reference does). tet_mu (nullable) gives a per-tet shear
  * modulus in place of 1/compliance. contact (nullable, nv) receives the
@@ -103,6 +113,7 @@ int orc_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* 
                    uint8_t* contact, double* lambdas);
 /* Same schedule, colours run with `threads` POSIX threads (tets of one colour
  * share no vertex, so the result equals the sequential run bit for bit).
+ * Undamped settings only (returns -1 when damping or pbd_damping > 0).
  * colour_begin[ncolours+1] delimits colours inside `order`. */
 int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask,
                             uint32_t nt, const uint32_t* tets, const float* ep, const float* tet_mu,

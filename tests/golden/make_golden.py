@@ -57,6 +57,23 @@ CASES = [
                                    0.0, -9.81, DT, 40, 1]),
     ("ordered_wonky_nh_serial_nu045_star", ["ordered", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
                                             -2.0, -9.81, DT, 10, 1]),
+    # damping (GeoLinear3d::Damp and the in-solve Rayleigh terms): trailing
+    # args damping, pbdDamping, drag, Rayleigh type (0 Paper, 1 Limit, 2 Post,
+    # 3 PostAmortized), spacing (the demo's kSpacing)
+    ("damped_c1_nh_nu045_amortized_pbd_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5,
+                                               0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("damped_c1_nh_nu045_post_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                      0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 2, 0.1]),
+    ("damped_c1_nh_nu045_paper_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                       0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 0, 0.1]),
+    ("damped_c1_nh_nu045_limit_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                       0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("damped_c1_yeoh_nu049_amortized_pbd_tet", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.49,
+                                                0.0, -9.81, DT, 40, 1, 0.02, 0.05, 0.0, 3, 0.1]),
+    ("damped_wonky_nh_serial_post_pbd_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                              -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05]),
+    ("damped_wonky_nh_serial_limit_pbd_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                               -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 1, 0.05]),
 ]
 
 
@@ -81,7 +98,7 @@ def main():
         argv = [REFGEN] + [str(a) for a in args]
         stdin = None
         extra = {}
-        if args[0] == "ordered":
+        if args[0] in ("ordered", "damped"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]
             nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), 0, wonk)
@@ -97,7 +114,7 @@ def main():
         arrays.update(extra)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
         manifest[name] = {"args": args}
-        if args[0] == "ordered":
+        if args[0] in ("ordered", "damped"):
             manifest[name]["schedule_mode"] = manifest_mode
         print(f"{name}: " + ", ".join(f"{k}{list(v.shape)}" for k, v in arrays.items()))
     with open(os.path.join(HERE, "manifest.json"), "w") as f:

@@ -5,7 +5,10 @@ Every fixture in tests/golden/ was produced by the unmodified reference code
 bit for bit: mesh generation (XPBDFEM/MeshGen.cpp:156-244), rest state and
 masses (XPBDFEM/Fem.cpp:196-224, XPBDFEM/Geo.cpp:697-745), the MINSTD order
 (XPBDFEM/Geo.cpp:759-771), single-element solves (XPBDFEM/Fem.cpp:437-564,
-XPBDFEM/Xpbd.h:87-215) and whole substeps (XPBDFEM/Geo.cpp:305-356).
+XPBDFEM/Xpbd.h:87-215), whole substeps (XPBDFEM/Geo.cpp:305-356), and
+substeps with damping: the in-solve Rayleigh terms (XPBDFEM/Xpbd.h:87-205),
+GeoLinear3d::Damp with DampElement and PbdDamp (XPBDFEM/Geo.cpp:346-355,
+790-811; XPBDFEM/Fem.cpp:908-931; XPBDFEM/Xpbd.h:217-346), amortized or not.
 """
 import numpy as np
 import pytest
@@ -19,6 +22,9 @@ SOLVE = ["solve_nh_sim_incompressible", "solve_nh_sim_nu045", "solve_yeoh_sim_in
 SUBSTEP = ["substep_c1_nh_native", "substep_c1_yeoh_native", "substep_wonky_nh_serial_native",
            "ordered_c1_nh_star", "ordered_c1_yeoh_tet", "ordered_c1_nh_nu045_star", "ordered_c1_yeoh_nu049_tet",
            "ordered_wonky_nh_serial_nu045_star"]
+DAMPED = ["damped_c1_nh_nu045_amortized_pbd_star", "damped_c1_nh_nu045_post_star", "damped_c1_nh_nu045_paper_star",
+          "damped_c1_nh_nu045_limit_star", "damped_c1_yeoh_nu049_amortized_pbd_tet",
+          "damped_wonky_nh_serial_post_pbd_star", "damped_wonky_nh_serial_limit_pbd_star"]
 
 
 @pytest.mark.parametrize("name", MESH)
@@ -81,3 +87,39 @@ def test_substeps_bit_exact(orc, name):
     assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
     assert np.float32(orc.volume(Xn, tets)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+def damped_params(orc, a, derived, tick):
+    """orc_params of a `damped` fixture (refgen's argument order)."""
+    W, H, D, sx, sy, sz, wonk, dens, energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[1:18]
+    damping, pbd, drag, rtype, spacing = a[18:]
+    return orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
+                           gravity=(gx, gy, 0.0), lock=bool(lock), drag=float(derived[2]), damping=damping,
+                           rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(derived[0]),
+                           pbd_coeff_amortized=float(derived[1]), tick=tick)
+
+
+@pytest.mark.parametrize("name", DAMPED)
+def test_damped_substeps_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[8], a[16]
+    tets, nv = orc.parse_tets(g["idx"])
+    ep, w, fl = orc.init_rest(g["nodes"], tets, dens)
+    order = g["order"]
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lock_mask = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.substeps(X0, V0, w, tets, ep, order, 1, damped_params(orc, a, g["derived"], 0),
+                                 lock_mask=lock_mask)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.substeps(X1, V1, w1, tets, ep, order, nsub - 1, damped_params(orc, a, g["derived"], 1),
+                                lock_mask=lock_mask)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    # the damping did something: the undamped run differs
+    p0 = damped_params(orc, a, g["derived"], 0)
+    p0.damping, p0.pbd_damping = 0.0, 0.0
+    Xu, _, _, _ = orc.substeps(X0, V0, w, tets, ep, order, nsub, p0, lock_mask=lock_mask)
+    assert not np.array_equal(Xu.reshape(-1), g["xn"])
