@@ -54,6 +54,11 @@ extern "C" {
 #define XFEM_ENERGY_MIXED_SEL 4u       /* Energy_MixedSel: Neo-Hookean, prefactored I1 */
 #define XFEM_ENERGY_YEOH_SKIN_FAST 7u  /* Energy_YeohSkinFast */
 #define XFEM_XPBD_SOLVE_BIT 11u        /* set: coupled 2x2 solve; clear: serial */
+#define XFEM_RAYLEIGH_TYPE_BIT 20u     /* Settings_RayleighTypeBit, mask 3: */
+#define XFEM_RAYLEIGH_PAPER 0u         /*   damping inside the solve (Rayleigh_Paper) */
+#define XFEM_RAYLEIGH_LIMIT 1u         /*   damping inside the solve, limited (Rayleigh_Limit) */
+#define XFEM_RAYLEIGH_POST 2u          /*   element damping after the velocity update (Rayleigh_Post) */
+#define XFEM_RAYLEIGH_POST_AMORTIZED 3u /*  the same on one eighth of the order per substep, x 8 */
 #define XFEM_LOCK_LEFT (1u << 26)      /* Settings_LockLeft: apply the lock mask */
 
 /* Solver settings. The first block mirrors the reference's Settings field by
@@ -65,13 +70,13 @@ typedef struct xfem_settings {
 	uint32_t volume_passes;      /* must be 0 (extra volume passes not built) */
 	float gravity[3];            /* reference: vec2 (x, y) */
 	float compliance;            /* 1 / mu_ref */
-	float damping;               /* must be 0 (post-step damping not built) */
-	float pbd_damping;           /* must be 0 */
+	float damping;               /* Rayleigh damping ratio (type in flags bits 20-21) */
+	float pbd_damping;           /* > 0 enables PBD damping (coefficients below) */
 	float drag;                  /* informational; the solver uses time_corrected_drag */
 	float poissons_ratio;        /* 0.5 = incompressible (zero volumetric compliance) */
 	float wonkiness;             /* mesh generation only */
 	float left_right_separation; /* unused */
-	uint32_t flags;              /* energy bits 6-10, solve bit 11, lock bit 26 */
+	uint32_t flags;              /* energy bits 6-10, solve bit 11, Rayleigh type bits 20-21, lock bit 26 */
 	/* The reference's derived Settings::timeCorrectedDrag
 	 * (XPBDFEM/Settings.h:97), filled by Sim::Update (XPBDFEM/Demo.cpp:63);
 	 * xfem_time_corrected_drag() computes it. */
@@ -82,6 +87,16 @@ typedef struct xfem_settings {
 	float ground_normal[3];      /* unit normal; solid side is dot(n, x) < offset */
 	float ground_offset;
 	float friction;              /* Coulomb coefficient */
+	/* The reference's derived Settings::volumeAndTimeCorrectedPbdDamping and
+	 * amortizedVolumeAndTimeCorrectedPbdDamping (XPBDFEM/Settings.h:95-96),
+	 * filled by Sim::Update (XPBDFEM/Demo.cpp:53-61);
+	 * xfem_pbd_damping_coefficients() computes them. */
+	float volume_and_time_corrected_pbd_damping;
+	float amortized_volume_and_time_corrected_pbd_damping;
+	/* Settings::tickId of the next substep (XPBDFEM/Settings.h:102): selects the
+	 * eighth of the order damped by Rayleigh_PostAmortized. The handle counts it
+	 * up by one per substep; xfem_set_settings sets it. */
+	uint32_t tick_id;
 } xfem_settings;
 
 /* Create-time options (all zero = defaults). */
@@ -251,6 +266,10 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
                           uint32_t* tet_order, uint32_t* colour_begin, uint32_t* ncolours, uint32_t* nclusters);
 
 /* ---- helpers --------------------------------------------------------------- */
+/* volumeAndTimeCorrectedPbdDamping and its amortized form for a substep of
+ * substep_dt and element spacing `spacing` (XPBDFEM/Demo.cpp:53-61, where
+ * spacing is the demo's kSpacing): out[0], out[1]. */
+int xfem_pbd_damping_coefficients(float pbd_damping, float substep_dt, float spacing, float* out2);
 /* timeCorrectedDrag = 1 - (1 - drag)^(1000 sdt), XPBDFEM/Demo.cpp:63. */
 float xfem_time_corrected_drag(float drag, float substep_dt);
 /* GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244): a W x H x D block of cubes

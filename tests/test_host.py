@@ -146,3 +146,17 @@ def test_time_corrected_drag():
     assert xfem.time_corrected_drag(0.0, 1 / 1200) == 0.0
     v = xfem.time_corrected_drag(0.002, 1 / 3000)
     assert abs(v - (1 - (1 - 0.002) ** (1000 / 3000))) < 1e-7
+
+
+@pytest.mark.parametrize("name", ["damped_c1_nh_nu045_amortized_pbd_star", "damped_c1_yeoh_nu049_amortized_pbd_tet",
+                                  "damped_wonky_nh_serial_post_pbd_star"])
+def test_pbd_damping_coefficients_match_reference(name):
+    """xfem_pbd_damping_coefficients and xfem_time_corrected_drag against the
+    values Sim::Update computed in the reference (XPBDFEM/Demo.cpp:53-63),
+    within 2 ulp (powf may round differently between C libraries)."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dt, pbd, drag, spacing = a[15], a[19], a[20], a[22]
+    vc, avc = xfem.pbd_damping_coefficients(pbd, dt, spacing)
+    for got, want in ((vc, g["derived"][0]), (avc, g["derived"][1]), (xfem.time_corrected_drag(drag, dt), g["derived"][2])):
+        assert abs(np.float32(got) - want) <= 2 * np.spacing(np.float32(want)), (got, want)

@@ -99,6 +99,8 @@ struct xfem_body {
 	// per tet, caller order (all bodies): record index of c0, volume, output
 	// row (row * 32 + lane), 1/mu; staging for transfers
 	DevBuf<uint32_t> tet_rec_dev, tet_slot_dev;
+	DevBuf<uint32_t> tflat, tick;   // per tet row: index in the body's order; the tick word
+	DevBuf<float> tarea;            // per tet row: surface area
 	DevBuf<float> tet_vol_dev, tet_inv_mu, io;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
@@ -124,8 +126,7 @@ int validate_settings(const xfem_settings& s) {
 		return fail(XFEM_EUNSUPPORTED, "energy model " + std::to_string(energy) +
 		                                   " not supported (MixedSel = 4 and YeohSkinFast = 7 are)");
 	if (s.volume_passes != 0) return fail(XFEM_EUNSUPPORTED, "volume_passes must be 0");
-	if (s.damping != 0.0f || s.pbd_damping != 0.0f)
-		return fail(XFEM_EUNSUPPORTED, "post-step damping (damping, pbd_damping) is not supported");
+	if (!(s.damping >= 0.0f) || !(s.pbd_damping >= 0.0f)) return fail(XFEM_EINVAL, "damping and pbd_damping must be >= 0");
 	if (s.flags & (1u << 27)) return fail(XFEM_EUNSUPPORTED, "Settings_LockRight is not supported");
 	if (!(s.compliance > 0.0f)) return fail(XFEM_EINVAL, "compliance must be > 0");
 	if (!(s.poissons_ratio > 0.0f && s.poissons_ratio <= 0.5f))
@@ -155,7 +156,32 @@ BodyParams make_params(const xfem_settings& s) {
 	p.friction = s.friction;
 	for (int k = 0; k < 3; k++) p.ground_n[k] = s.ground_normal[k];
 	p.ground_d = s.ground_offset;
+	p.damping = s.damping;
+	p.rayleigh_type = (s.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u;
+	p.pbd_on = s.pbd_damping > 0.0f ? 1u : 0u;
+	p.pbd_coeff = s.volume_and_time_corrected_pbd_damping;
+	p.pbd_coeff_amortized = s.amortized_volume_and_time_corrected_pbd_damping;
 	return p;
+}
+
+// Whether any body damps, in the solve (Paper, Limit) or after it.
+bool damp_any_of(const std::vector<BodyHost>& bodies) {
+	for (const BodyHost& b : bodies)
+		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f) return true;
+	return false;
+}
+
+// Damping sweeps the handle runs after each solve sweep: bit 0 element
+// Rayleigh damping (any body with a Post type and damping > 0), bit 1 PBD
+// damping (any body with pbd_damping > 0).
+uint32_t damp_kinds_of(const std::vector<BodyHost>& bodies) {
+	uint32_t k = 0;
+	for (const BodyHost& b : bodies) {
+		const uint32_t type = (b.settings.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u;
+		if (type >= XFEM_RAYLEIGH_POST && b.settings.damping > 0.0f) k |= 1u;
+		if (b.settings.pbd_damping > 0.0f) k |= 2u;
+	}
+	return k;
 }
 
 // c0 = (1/mu)/volume exactly as the reference forms comp[0] (XPBDFEM/Fem.cpp:449).
@@ -395,6 +421,7 @@ int build_device(xfem_body* h) {
 		for (size_t i = 0; i < 4 * (size_t)b.nt; i++) tets_dev[tbase + i] = b.vbase + b.sched.vert_rank[b.tets[i]];
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
+		params[bi].ntets = b.nt;
 	}
 	// upload
 	XCUDA(h->vert.alloc(vert.size()));
@@ -452,7 +479,30 @@ int build_device(xfem_body* h) {
 		XCUDA(up(h->tet_slot_dev.p, slot.data(), slot.size() * 4));
 		XCUDA(up(h->tet_vol_dev.p, vol.data(), vol.size() * 4));
 		XCUDA(up(h->tet_inv_mu.p, inv_mu.data(), inv_mu.size() * 4));
+		// per tet row: the index in the body's flattened order (the amortized
+		// damping slices) and the surface area (PBD damping)
+		std::vector<uint32_t> flat((size_t)trows * kLanes, 0);
+		std::vector<float> area((size_t)trows * kLanes, 1.0f);
+		for (const BodyHost& b : h->bodies) {
+			const Schedule& sc = b.sched;
+			uint32_t o = 0;
+			for (uint32_t c = 0; c < sc.ncolours; c++)
+				for (uint32_t i = sc.colour_cl_begin[c]; i < sc.colour_cl_begin[c + 1]; i++)
+					for (uint32_t q = sc.cl_begin[sc.colour_cl[i]]; q < sc.cl_begin[sc.colour_cl[i] + 1]; q++) {
+						const uint32_t t = sc.cl_tets[q];
+						flat[b.tet_slot[t]] = o++;
+						area[b.tet_slot[t]] = b.ep[17 * (size_t)t + 16];
+					}
+		}
+		XCUDA(h->tflat.alloc(flat.size()));
+		XCUDA(h->tarea.alloc(area.size()));
+		XCUDA(h->tick.alloc(1));
+		XCUDA(up(h->tflat.p, flat.data(), flat.size() * 4));
+		XCUDA(up(h->tarea.p, area.data(), area.size() * 4));
+		const uint32_t tick0 = h->bodies.empty() ? 0u : h->bodies[0].settings.tick_id;
+		XCUDA(up(h->tick.p, &tick0, 4));
 		XCUDA(cudaStreamSynchronize(h->stream));
+		h->device_bytes += (uint64_t)trows * kLanes * 8 + 4;
 		h->device_bytes += (uint64_t)ntets * 16 + h->io.n * 4;
 	}
 	DevCtx& c = h->ctx;
@@ -471,6 +521,11 @@ int build_device(xfem_body* h) {
 	c.tlam = h->tlam.p;
 	c.chunks = h->chunks.p;
 	c.ntrows = trows;
+	c.damp_kinds = damp_kinds_of(h->bodies);
+	c.damp_any = damp_any_of(h->bodies) ? 1u : 0u;
+	c.tick = h->tick.p;
+	c.tflat = h->tflat.p;
+	c.tarea = h->tarea.p;
 	c.colour_chunk_begin = h->ccb.p;
 	c.isolated = h->isolated.p;
 	c.dep_begin = h->dep_begin.p;
@@ -484,6 +539,7 @@ int build_device(xfem_body* h) {
 	c.bar_count = h->bar.p;
 	c.err = h->err.p;
 	h->cfg.lambdas = h->opt.keep_lambdas != 0;
+	h->cfg.damp = c.damp_any != 0u;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -553,16 +609,27 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	const int blocks[] = {64, 128, 192, 224, 256};
 	for (int sm : {1, 2, 3}) {
 		if (fixed_sync && sm != fixed_sync) continue;
+		if (sm == 3 && h->ctx.damp_any) continue;  // the dataflow kernel runs no damping
 		for (int bs : blocks) {
 			if (fixed_block && bs != fixed_block) continue;
 			cand.push_back({sm, bs});
 		}
 	}
+	if (fixed_sync == 3 && h->ctx.damp_any) {
+		h->tuned = false;
+		return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping");
+	}
 	if (fixed_block && cand.empty()) cand.push_back({fixed_sync ? fixed_sync : 1, fixed_block});
+	if (cand.empty()) {
+		h->tuned = false;
+		return fail(XFEM_EINVAL, "no launch configuration for these options");
+	}
 	if (cand.size() == 1) return set_config(h, cand[0].first, cand[0].second);
 	DevBuf<float4> save;
 	XCUDA(save.alloc(h->vert.n));
 	XCUDA(cudaMemcpyAsync(save.p, h->vert.p, h->vert.n * sizeof(float4), cudaMemcpyDeviceToDevice, h->stream));
+	uint32_t tick_saved = 0;  // the trial launches advance the tick too
+	XCUDA(cudaMemcpyAsync(&tick_saved, h->tick.p, 4, cudaMemcpyDeviceToHost, h->stream));
 	cudaEvent_t e0, e1;
 	XCUDA(cudaEventCreate(&e0));
 	XCUDA(cudaEventCreate(&e1));
@@ -587,6 +654,7 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	cudaEventDestroy(e0);
 	cudaEventDestroy(e1);
 	XCUDA(cudaMemcpyAsync(h->vert.p, save.p, h->vert.n * sizeof(float4), cudaMemcpyDeviceToDevice, h->stream));
+	XCUDA(cudaMemcpyAsync(h->tick.p, &tick_saved, 4, cudaMemcpyHostToDevice, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	int rc = check_device_error(h);
 	if (rc) return rc;
@@ -648,6 +716,12 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 	XCUDA(cudaSetDevice(h->device));
 	int rc = autotune(h, nsub, dt);
 	if (rc) return rc;
+	if (h->ctx.damp_any && h->cfg.sync_mode == 3) {
+		// damping switched on after the dataflow kernel was chosen
+		if (h->opt.sync_mode == 3) return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping");
+		rc = set_config(h, 1, h->cfg.block);
+		if (rc) return rc;
+	}
 	return run(h, nsub, dt);
 }
 
@@ -768,9 +842,28 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	const bool material = s->compliance != b->settings.compliance;
 	b->settings = *s;
 	XCUDA(cudaSetDevice(h->device));
-	const BodyParams p = make_params(*s);
+	BodyParams p = make_params(*s);
+	p.ntets = b->nt;
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
+	// Settings::tickId: the handle's substep counter continues from here
+	XCUDA(cudaMemcpyAsync(h->tick.p, &s->tick_id, 4, cudaMemcpyHostToDevice, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
+	const uint32_t kinds = damp_kinds_of(h->bodies);
+	const bool damp = damp_any_of(h->bodies);
+	if (kinds != h->ctx.damp_kinds || damp != h->cfg.damp) {
+		h->ctx.damp_kinds = kinds;
+		h->ctx.damp_any = damp ? 1u : 0u;
+		h->cfg.damp = damp;
+		if (h->graph) {  // the captured launches follow the old sweeps
+			cudaGraphExecDestroy(h->graph);
+			h->graph = nullptr;
+		}
+		if (h->tuned && (h->cfg.sync_mode == 1 || h->cfg.sync_mode == 3)) {
+			// the other instantiation may fit another grid
+			int blocks = 0;
+			if (persistent_grid(h->cfg, &blocks) == 0) h->cfg.blocks = blocks;
+		}
+	}
 	if (material && b->tet_mu.empty()) return update_material(h, *b);
 	return XFEM_OK;
 }
@@ -954,6 +1047,16 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
 	return xfem_get_schedule(&tmp, 0, vert_rank, tet_order, colour_begin, ncolours);
 }
 
+int xfem_pbd_damping_coefficients(float pbd_damping, float substep_dt, float spacing, float* out2) {
+	if (!out2) return fail(XFEM_EINVAL, "null output");
+	// XPBDFEM/Demo.cpp:53-61 (AmortizationPeriod = 8)
+	const float tc = 1.0f - powf(1.0f - pbd_damping, 1000.0f * substep_dt);
+	const float atc = 1.0f - powf(1.0f - pbd_damping, 1000.0f * 8.0f * substep_dt);
+	out2[0] = tc * 6.0f * spacing * spacing;
+	out2[1] = atc * 6.0f * spacing * spacing;
+	return XFEM_OK;
+}
+
 float xfem_time_corrected_drag(float drag, float substep_dt) {
 	return 1.0f - powf(1.0f - drag, 1000.0f * substep_dt);
 }
@@ -1031,6 +1134,8 @@ int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpo
 		const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 		if (energy != XFEM_ENERGY_MIXED_SEL || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))
 			return fail(XFEM_EUNSUPPORTED, "the adjoint covers the coupled Neo-Hookean model only (energy 4, XPBD solve bit)");
+		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f)
+			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate damping (damping, pbd_damping must be 0)");
 	}
 	XCUDA(cudaSetDevice(h->device));
 	AdjointRun& a = h->adj;

@@ -145,12 +145,15 @@ struct TetRec {
 struct Mat {
 	float a, ratio, y0, y1, y2;
 	uint32_t energy, simultaneous;
+	float damp;      // in-solve Rayleigh ratio: damping for types 0, 1, else 0
+	uint32_t limit;  // 1 = Rayleigh_Limit, 0 = Rayleigh_Paper
 };
 
 __device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body) {
 	const BodyParams* b = bodies + body;
+	const uint32_t type = __ldg(&b->rayleigh_type);
 	return {__ldg(&b->a), __ldg(&b->ratio), __ldg(&b->yeoh[0]), __ldg(&b->yeoh[1]), __ldg(&b->yeoh[2]),
-	        __ldg(&b->energy), __ldg(&b->simultaneous)};
+	        __ldg(&b->energy), __ldg(&b->simultaneous), type < 2u ? __ldg(&b->damping) : 0.0f, type == 1u ? 1u : 0u};
 }
 
 // Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with the
@@ -239,14 +242,45 @@ __device__ __forceinline__ float wdot(const float w[4], const Vec3 a[4], const V
 	return s;
 }
 
+// Cramer's rule for M = [A0 A1; A1 A2], b as in XPBDFEM/Xpbd.h:172-180.
+__device__ __forceinline__ void cramer(float A0, float A1, float A2, float b0, float b1, float& l0, float& l1) {
+	const float i00 = rcp(A0), i11 = rcp(A2);
+	const float r0 = A1 * i00, r1 = A1 * i11;
+	const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
+	const float c0 = b0 * i00, c1 = b1 * i11;
+	l0 = inv_det * fmaf(-r0, c1, c0);
+	l1 = inv_det * fmaf(-c0, r1, c1);
+}
+
+// One scalar constraint of the serial solve (XPBDFEM/Xpbd.h:87-121), with the
+// in-solve Rayleigh damping when DAMP and bp.damp > 0; D: displacements so far
+// (X - O).
+template <bool DAMP>
+__device__ __forceinline__ float serial_lambda(const Mat& bp, float U, const Vec3 g[4], const float w[4],
+                                               const float4 D[4], float alpha, float comp, float inv_dt) {
+	const float wgg = wdot(w, g, g);
+	if (!DAMP || !(bp.damp > 0.0f)) return (-2.0f * U) * rcp(fmaf(2.0f * U, alpha, wgg));
+	float gV = 0.0f;
+#pragma unroll
+	for (int n = 0; n < 4; n++) gV = fmaf(g[n].x, D[n].x, fmaf(g[n].y, D[n].y, fmaf(g[n].z, D[n].z, gV)));
+	const float gamma = bp.damp * inv_dt;
+	if (!bp.limit) return (-2.0f * U - gamma * gV) / fmaf(wgg, 1.0f + gamma, 2.0f * U * alpha);
+	float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
+	const float A = fmaf(2.0f * U, comp * inv_dt / bp.damp, wgg);
+	const float b = (-gV - wgg * l) * (A / fmaxf(A, 4.0f * wgg));
+	return l + b / A;
+}
+
 // One element solve: SolveElementMixed<MixedSelective | YeohSkinFast> tet path
 // (XPBDFEM/Fem.cpp:437-564) with EnergyXpbdConstrainSimultaneous<2>
 // (XPBDFEM/Xpbd.h:123-215) or the serial EnergyXpbdConstrain pair
-// (XPBDFEM/Xpbd.h:87-121). O[]: start positions + w, D[]: displacements
+// (XPBDFEM/Xpbd.h:87-121), with the in-solve Rayleigh damping (Paper, Limit)
+// compiled in when DAMP. O[]: start positions + w, D[]: displacements
 // (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
 // alpha1 = alpha0 * (mu / lambda), i.e. (1/lambda)/volume/dt^2.
-__device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, float inv_dt2, const float4 O[4],
-                                            float4 D[4]) {
+template <bool DAMP = false>
+__device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, float inv_dt, float inv_dt2,
+                                            const float4 O[4], float4 D[4]) {
 	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
 	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
 	const float QR[3] = {r.d.x, r.d.y, r.d.z};
@@ -263,17 +297,48 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 	float l0, l1;
 	if (bp.simultaneous) {
 		const float U1 = hydrostatic(q, P, bp.a, g1);
-		const float A0 = fmaf(2.0f * U0, alpha0, wdot(w, g0, g0));
-		const float A1 = wdot(w, g1, g0);
-		const float A2 = fmaf(2.0f * U1, alpha1, wdot(w, g1, g1));
-		const float b0 = -2.0f * U0, b1 = -2.0f * U1;
-		// Cramer's rule as in XPBDFEM/Xpbd.h:172-180
-		const float i00 = rcp(A0), i11 = rcp(A2);
-		const float r0 = A1 * i00, r1 = A1 * i11;
-		const float inv_det = rcp(fmaxf(0.00000001f, fmaf(-r0, r1, 1.0f)));
-		const float c0 = b0 * i00, c1 = b1 * i11;
-		l0 = inv_det * fmaf(-r0, c1, c0);
-		l1 = inv_det * fmaf(-c0, r1, c1);
+		if (!DAMP || !(bp.damp > 0.0f)) {
+			const float A0 = fmaf(2.0f * U0, alpha0, wdot(w, g0, g0));
+			const float A1 = wdot(w, g1, g0);
+			const float A2 = fmaf(2.0f * U1, alpha1, wdot(w, g1, g1));
+			// Cramer's rule as in XPBDFEM/Xpbd.h:172-180
+			cramer(A0, A1, A2, -2.0f * U0, -2.0f * U1, l0, l1);
+		} else {
+			// XPBDFEM/Xpbd.h:133-205: gV = g . (X - O), Paper scales the
+			// diagonal and right-hand side by 1 / (1 + gamma), Limit adds a
+			// second solve towards the Rayleigh target
+			const float wgg0 = wdot(w, g0, g0), wgg1 = wdot(w, g1, g0), wgg2 = wdot(w, g1, g1);
+			float gV0 = 0.0f, gV1 = 0.0f;
+#pragma unroll
+			for (int n = 0; n < 4; n++) {
+				gV0 = fmaf(g0[n].x, D[n].x, fmaf(g0[n].y, D[n].y, fmaf(g0[n].z, D[n].z, gV0)));
+				gV1 = fmaf(g1[n].x, D[n].x, fmaf(g1[n].y, D[n].y, fmaf(g1[n].z, D[n].z, gV1)));
+			}
+			const float gamma = bp.damp * inv_dt;
+			float A0, A2, b0 = -2.0f * U0, b1 = -2.0f * U1;
+			if (!bp.limit) {
+				const float s = 1.0f / (1.0f + gamma);
+				A0 = wgg0 + (2.0f * U0 * alpha0) * s;
+				A2 = wgg2 + (2.0f * U1 * alpha1) * s;
+				b0 = (b0 - gamma * gV0) * s;
+				b1 = (b1 - gamma * gV1) * s;
+			} else {
+				A0 = fmaf(2.0f * U0, alpha0, wgg0);
+				A2 = fmaf(2.0f * U1, alpha1, wgg2);
+			}
+			cramer(A0, wgg1, A2, b0, b1, l0, l1);
+			if (bp.limit) {
+				const float ib = r.d.w * inv_dt / bp.damp;  // comp0 / (dt damping)
+				const float B0 = fmaf(2.0f * U0, ib, wgg0), B2 = fmaf(2.0f * U1, ib * bp.ratio, wgg2);
+				float e0 = fmaf(b0, -1.0f - alpha0 * l0, -gV0), e1 = fmaf(b1, -1.0f - alpha1 * l1, -gV1);
+				e0 *= B0 / fmaxf(B0, 8.0f * wgg0);
+				e1 *= B2 / fmaxf(B2, 8.0f * wgg2);
+				float d0, d1;
+				cramer(B0, wgg1, B2, e0, e1, d0, d1);
+				l0 += d0;
+				l1 += d1;
+			}
+		}
 #pragma unroll
 		for (int n = 0; n < 4; n++) {
 			D[n].x = fmaf(w[n], fmaf(l1, g1[n].x, l0 * g0[n].x), D[n].x);
@@ -281,7 +346,7 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 			D[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), D[n].z);
 		}
 	} else {
-		l0 = (-2.0f * U0) * rcp(fmaf(2.0f * U0, alpha0, wdot(w, g0, g0)));
+		l0 = serial_lambda<DAMP>(bp, U0, g0, w, D, alpha0, r.d.w, inv_dt);
 #pragma unroll
 		for (int n = 0; n < 4; n++) {
 			const float s = w[n] * l0;
@@ -294,7 +359,7 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 			P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
 			        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
 		const float U1 = hydrostatic(q, P, bp.a, g1);
-		l1 = (-2.0f * U1) * rcp(fmaf(2.0f * U1, alpha1, wdot(w, g1, g1)));
+		l1 = serial_lambda<DAMP>(bp, U1, g1, w, D, alpha1, r.d.w * bp.ratio, inv_dt);
 #pragma unroll
 		for (int n = 0; n < 4; n++) {
 			const float s = w[n] * l1;
@@ -305,7 +370,6 @@ __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, floa
 	}
 	return make_float2(l0, l1);
 }
-
 
 // ---- chunk staging: one TMA bulk copy per chunk into the warp's buffer ----
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }

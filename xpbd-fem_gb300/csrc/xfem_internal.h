@@ -64,6 +64,14 @@ struct BodyParams {
 	float ground_d;
 	float ratio;   // mu / lambda (0 when incompressible)
 	uint32_t pad;
+	// damping (XPBDFEM/Geo.cpp:346-355, 790-811; XPBDFEM/Xpbd.h:87-346)
+	float damping;            // Rayleigh ratio (0 = off)
+	uint32_t rayleigh_type;   // 0 Paper, 1 Limit (in the solve), 2 Post, 3 PostAmortized
+	uint32_t pbd_on;          // pbd_damping > 0
+	float pbd_coeff;          // volume- and time-corrected PBD damping
+	float pbd_coeff_amortized;
+	uint32_t ntets;           // tets of the body (amortized slices)
+	uint32_t pad2[2];
 };
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
@@ -120,6 +128,15 @@ struct DevCtx {
 	float4* traj;               // [run substep][tip]: position after each substep
 	const int32_t* tip_of;      // per vertex: tip index or -1
 	uint32_t ntrows, sub_base, ntips, pad_;
+	// Damping sweeps after each substep's solve sweep (0 = none: the state
+	// between substeps stays (O, D) and the next advance finishes it).
+	// Bit 0: element Rayleigh damping (Post types), bit 1: PBD damping.
+	uint32_t damp_kinds;
+	uint32_t damp_any;          // some body damps (in the solve or after it): the kernels
+	                            // with damping compiled in are launched
+	uint32_t* tick;             // device word: Settings::tickId of the launch's first substep
+	const uint32_t* tflat;      // [tet row][lane]: the tet's index in its body's flattened order
+	const float* tarea;         // [tet row][lane]: the tet's surface area (rest state)
 };
 
 // Reverse-pass state (xfem_adjoint.cu).
@@ -147,6 +164,7 @@ struct LaunchCfg {
 	int blocks = 0;        // persistent grid size
 	int sync_mode = 1;     // 1 persistent + grid barrier, 2 per-colour launches (CUDA graph), 3 persistent dataflow
 	bool lambdas = false;
+	bool damp = false;     // launch the instantiations with damping (DevCtx::damp_any)
 	uint32_t warp_smem = 0;
 	uint32_t total_chunks = 0;
 	std::vector<uint32_t> colour_chunk_begin_host;

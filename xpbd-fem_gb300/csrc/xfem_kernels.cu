@@ -56,11 +56,148 @@ __device__ __forceinline__ void tape_tet(const DevCtx& C, uint32_t s, uint32_t r
 	__stcs(p + 2 * kLanes, make_float4(D[2].z, D[3].x, D[3].y, D[3].z));
 }
 
+// ---- damping after the velocity update (GeoLinear3d::Damp) ------------------
+// State during the damping sweeps: vert[2v] = (X, w), vert[2v+1] = (V, bits).
+
+// DampElement (XPBDFEM/Fem.cpp:908-931): energies and gradients of the tet at
+// its current positions, then RayleighDamp (XPBDFEM/Xpbd.h:217-263) on its
+// velocities. damp: the Rayleigh ratio (x 8 when amortized).
+__device__ __forceinline__ void rayleigh_tet(const Mat& bp, const TetRec& r, const float4 X[4], float4 V[4],
+                                             float inv_dt, float damp) {
+	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
+	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
+	const float QR[3] = {r.d.x, r.d.y, r.d.z};
+	const float w[4] = {X[0].w, X[1].w, X[2].w, X[3].w};
+	Vec3 P[3];
+#pragma unroll
+	for (int i = 0; i < 3; i++) P[i] = {X[i].x - X[3].x, X[i].y - X[3].y, X[i].z - X[3].z};
+	Vec3 g0[4], g1[4];
+	const float U0 = deviatoric(bp, QQ, QR, P, g0);
+	const float U1 = hydrostatic(q, P, bp.a, g1);
+	const float ib0 = r.d.w * inv_dt / damp, ib1 = ib0 * bp.ratio;  // comp / (dt damping)
+	if (bp.simultaneous) {
+		float b0 = 0.0f, b1 = 0.0f;
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			b0 -= fmaf(g0[n].x, V[n].x, fmaf(g0[n].y, V[n].y, g0[n].z * V[n].z));
+			b1 -= fmaf(g1[n].x, V[n].x, fmaf(g1[n].y, V[n].y, g1[n].z * V[n].z));
+		}
+		float l0, l1;
+		cramer(fmaf(2.0f * U0, ib0, wdot(w, g0, g0)), wdot(w, g0, g1), fmaf(2.0f * U1, ib1, wdot(w, g1, g1)), b0, b1, l0,
+		       l1);
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			V[n].x = fmaf(w[n], fmaf(l1, g1[n].x, l0 * g0[n].x), V[n].x);
+			V[n].y = fmaf(w[n], fmaf(l1, g1[n].y, l0 * g0[n].y), V[n].y);
+			V[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), V[n].z);
+		}
+	} else {
+		const Vec3* gs[2] = {g0, g1};
+		const float Us[2] = {U0, U1}, ibs[2] = {ib0, ib1};
+#pragma unroll
+		for (int k = 0; k < 2; k++) {
+			const Vec3* g = gs[k];
+			float gV = 0.0f;
+#pragma unroll
+			for (int n = 0; n < 4; n++) gV = fmaf(g[n].x, V[n].x, fmaf(g[n].y, V[n].y, fmaf(g[n].z, V[n].z, gV)));
+			const float l = -gV / fmaf(2.0f * Us[k], ibs[k], wdot(w, g, g));
+#pragma unroll
+			for (int n = 0; n < 4; n++) {
+				const float s = w[n] * l;
+				V[n].x = fmaf(s, g[n].x, V[n].x);
+				V[n].y = fmaf(s, g[n].y, V[n].y);
+				V[n].z = fmaf(s, g[n].z, V[n].z);
+			}
+		}
+	}
+}
+
+// PbdDamp (XPBDFEM/Xpbd.h:307-346): moves the tet's velocities towards its
+// rigid motion (mass-weighted centre velocity plus the rotation that carries
+// its angular momentum) by the fraction `damping`.
+__device__ __forceinline__ void pbd_tet(const float4 X[4], float4 V[4], float damping) {
+	float Wsum = 1.0e-8f;
+#pragma unroll
+	for (int i = 0; i < 4; i++) Wsum += X[i].w;
+	const float Wavg = Wsum * 0.25f, Wmin = 0.0001f * Wavg;
+	Vec3 x[4], xcm = {0.0f, 0.0f, 0.0f}, vcm = {0.0f, 0.0f, 0.0f};
+	float M[4], Msum = 0.0f;
+#pragma unroll
+	for (int i = 0; i < 4; i++) {
+		x[i] = {X[i].x - X[3].x, X[i].y - X[3].y, X[i].z - X[3].z};
+		M[i] = Wavg / fmaxf(Wmin, X[i].w);
+		xcm = {fmaf(x[i].x, M[i], xcm.x), fmaf(x[i].y, M[i], xcm.y), fmaf(x[i].z, M[i], xcm.z)};
+		vcm = {fmaf(V[i].x, M[i], vcm.x), fmaf(V[i].y, M[i], vcm.y), fmaf(V[i].z, M[i], vcm.z)};
+		Msum += M[i];
+	}
+	const float im = 1.0f / Msum;
+	xcm = {xcm.x * im, xcm.y * im, xcm.z * im};
+	vcm = {vcm.x * im, vcm.y * im, vcm.z * im};
+	Vec3 r[4], L = {0.0f, 0.0f, 0.0f};
+	float I00 = 0.0f, I11 = 0.0f, I22 = 0.0f, I01 = 0.0f, I12 = 0.0f, I02 = 0.0f;
+#pragma unroll
+	for (int i = 0; i < 4; i++) {
+		r[i] = {x[i].x - xcm.x, x[i].y - xcm.y, x[i].z - xcm.z};
+		const Vec3 c = cross(r[i], v3(V[i]));
+		L = {fmaf(M[i], c.x, L.x), fmaf(M[i], c.y, L.y), fmaf(M[i], c.z, L.z)};
+		const float xx = r[i].x * r[i].x, yy = r[i].y * r[i].y, zz = r[i].z * r[i].z;
+		I00 = fmaf(M[i], yy + zz, I00);
+		I11 = fmaf(M[i], xx + zz, I11);
+		I22 = fmaf(M[i], xx + yy, I22);
+		I01 = fmaf(-M[i], r[i].x * r[i].y, I01);
+		I12 = fmaf(-M[i], r[i].y * r[i].z, I12);
+		I02 = fmaf(-M[i], r[i].z * r[i].x, I02);
+	}
+	// omega = I^-1 L (I symmetric): adjugate over determinant
+	const float a00 = fmaf(I11, I22, -I12 * I12), a01 = fmaf(I02, I12, -I01 * I22), a02 = fmaf(I01, I12, -I02 * I11);
+	const float a11 = fmaf(I00, I22, -I02 * I02), a12 = fmaf(I01, I02, -I00 * I12), a22 = fmaf(I00, I11, -I01 * I01);
+	const float idet = 1.0f / fmaf(I00, a00, fmaf(I01, a01, I02 * a02));
+	const Vec3 om = {fmaf(a00, L.x, fmaf(a01, L.y, a02 * L.z)) * idet, fmaf(a01, L.x, fmaf(a11, L.y, a12 * L.z)) * idet,
+	                 fmaf(a02, L.x, fmaf(a12, L.y, a22 * L.z)) * idet};
+#pragma unroll
+	for (int i = 0; i < 4; i++) {
+		const Vec3 c = cross(om, r[i]);
+		V[i].x = fmaf(damping, (vcm.x + c.x) - V[i].x, V[i].x);
+		V[i].y = fmaf(damping, (vcm.y + c.y) - V[i].y, V[i].y);
+		V[i].z = fmaf(damping, (vcm.z + c.z) - V[i].z, V[i].z);
+	}
+}
+
+// Whether tet row `row` (lane `lane`) of body bp is damped at this tick, and
+// with which Rayleigh ratio and PBD fraction (XPBDFEM/Geo.cpp:346-352,
+// 792-798): the amortized type damps one eighth of the body's order per
+// tick, x 8.
+struct DampTet {
+	bool on;
+	float rayleigh, pbd;
+};
+
+__device__ __forceinline__ DampTet damp_of(const DevCtx& C, const BodyParams& bp, uint32_t row, uint32_t lane,
+                                           uint32_t tick, int kind) {
+	const uint32_t type = __ldg(&bp.rayleigh_type);
+	const bool amort = type == 3u;
+	DampTet d = {false, 0.0f, 0.0f};
+	if (kind == 0) {
+		d.rayleigh = __ldg(&bp.damping) * (amort ? 8.0f : 1.0f);
+		d.on = type >= 2u && d.rayleigh > 0.0f;
+	} else {
+		d.on = __ldg(&bp.pbd_on) != 0u;
+	}
+	if (!d.on) return d;
+	const size_t k = (size_t)row * kLanes + lane;
+	if (amort) {
+		const uint32_t nt = __ldg(&bp.ntets), f = __ldg(C.tflat + k), m = tick % 8u;
+		d.on = f >= nt * m / 8u && f < nt * (m + 1u) / 8u;
+	}
+	if (kind == 1) d.pbd = fminf(1.0f, (amort ? __ldg(&bp.pbd_coeff_amortized) : __ldg(&bp.pbd_coeff)) / __ldg(C.tarea + k));
+	return d;
+}
+
 // Header word of a cluster lane: nv | nt << 4 | advance mask << 8 | body << 16.
 // A vertex is advanced (previous substep finalized, next one predicted) by
 // the lowest-colour cluster touching it, just before that cluster's solve.
 
-template <bool LAMBDAS, bool TAPE>
+template <bool LAMBDAS, bool TAPE, bool DAMP>
 __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first, float dt,
                                                float inv_dt, float inv_dt2, uint32_t trow, uint32_t s_launch) {
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
@@ -94,7 +231,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 			const float4 Ot[4] = {O[cube_slot(t, 0)], O[cube_slot(t, 1)], O[cube_slot(t, 2)], O[cube_slot(t, 3)]};
 			float4 Dt[4] = {D[cube_slot(t, 0)], D[cube_slot(t, 1)], D[cube_slot(t, 2)], D[cube_slot(t, 3)]};
 			if (TAPE) tape_tet(C, s_launch, trow + t, lane, Dt);
-			const float2 lam = solve_tet(mat, tr, inv_dt2, Ot, Dt);
+			const float2 lam = solve_tet<DAMP>(mat, tr, inv_dt, inv_dt2, Ot, Dt);
 #pragma unroll
 			for (int k = 0; k < 4; k++) D[cube_slot(t, k)] = Dt[k];
 			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
@@ -113,13 +250,13 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 // One warp processes one resident chunk; lane = cluster. `next` >= 0 is the
 // warp's next chunk: its copy is issued as soon as this chunk's records have
 // been consumed, so it overlaps the write-back and what follows.
-template <bool LAMBDAS, bool TAPE = false>
+template <bool LAMBDAS, bool TAPE = false, bool DAMP = false>
 __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, bool first,
                                           float dt, float inv_dt, float inv_dt2, uint32_t s_launch = 0) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
-		run_chunk_cube<LAMBDAS, TAPE>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch);
+		run_chunk_cube<LAMBDAS, TAPE, DAMP>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch);
 		return;
 	}
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
@@ -158,7 +295,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			const float4 O[4] = {sO[s0 * kLanes], sO[s1 * kLanes], sO[s2 * kLanes], sO[s3 * kLanes]};
 			float4 D[4] = {sD[s0 * kLanes], sD[s1 * kLanes], sD[s2 * kLanes], sD[s3 * kLanes]};
 			if (TAPE) tape_tet(C, s_launch, trow + t, lane, D);
-			const float2 lam = solve_tet(mat, tr, inv_dt2, O, D);
+			const float2 lam = solve_tet<DAMP>(mat, tr, inv_dt, inv_dt2, O, D);
 			sD[s0 * kLanes] = D[0];
 			sD[s1 * kLanes] = D[1];
 			sD[s2 * kLanes] = D[2];
@@ -178,12 +315,102 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 	}
 }
 
+// One damping pass over a resident chunk (KIND 0: element Rayleigh damping,
+// 1: PBD damping); lane = cluster, tets in the cluster's order. With
+// `finish` (the sweep's first pass) the owner of each vertex first finishes
+// the substep for it (locks, ground, V = D/dt, X = O + D), as the solve
+// sweep's owner advances it. CUBE: canonical cube chunks, all in registers.
+template <bool CUBE, int KIND>
+__device__ __forceinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t ntmax, uint32_t nvmax, uint32_t trow,
+                                           int next, uint32_t lane, bool finish, float inv_dt, uint32_t tick) {
+	constexpr uint32_t NV = CUBE ? 8u : kMaxClusterVerts;
+	constexpr uint32_t NT = CUBE ? 6u : kMaxClusterTets;
+	const float4* rec = reinterpret_cast<const float4*>(st.buf);
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * ntmax);
+	const uint32_t* vids = hdrs + kLanes;
+	const uint32_t* slots = vids + kLanes * nvmax;
+	const uint32_t hdr = hdrs[lane];
+	const bool live = (hdr & 15u) != 0;
+	const uint32_t nv = CUBE ? 8u : (hdr & 15u), nt = CUBE ? 6u : ((hdr >> 4) & 15u), mask = (hdr >> 8) & 0xffu;
+	uint32_t vid[NV];
+	float4 X[NV], V[NV];
+	if (live) {
+		const BodyParams& bp = C.bodies[hdr >> 16];
+		const Mat mat = load_mat(C.bodies, hdr >> 16);
+#pragma unroll
+		for (uint32_t k = 0; k < NV; k++) {
+			if (k < nv) {
+				vid[k] = vids[k * kLanes + lane];
+				X[k] = __ldcg(C.vert + 2 * (size_t)vid[k]);
+				V[k] = __ldcg(C.vert + 2 * (size_t)vid[k] + 1);
+				if (finish && (mask & (1u << k))) finalize_vertex(C.bodies, X[k], V[k], inv_dt);
+			}
+		}
+#pragma unroll
+		for (uint32_t t = 0; t < NT; t++) {
+			if (t < nt) {
+				const DampTet d = damp_of(C, bp, trow + t, lane, tick, KIND);
+				if (d.on) {
+					const uint32_t sl = CUBE ? (uint32_t)(cube_slot(t, 0) | cube_slot(t, 1) << 4 | cube_slot(t, 2) << 8 |
+					                                      cube_slot(t, 3) << 12)
+					                         : slots[t * kLanes + lane];
+					float4 Xt[4], Vt[4];
+#pragma unroll
+					for (int k = 0; k < 4; k++) {
+						Xt[k] = X[(sl >> (4 * k)) & 15u];
+						Vt[k] = V[(sl >> (4 * k)) & 15u];
+					}
+					if (KIND == 0) {
+						const float4* r = rec + t * 4 * kLanes + lane;
+						const TetRec tr = {r[0], r[kLanes], r[2 * kLanes], r[3 * kLanes]};
+						rayleigh_tet(mat, tr, Xt, Vt, inv_dt, d.rayleigh);
+					} else {
+						pbd_tet(Xt, Vt, d.pbd);
+					}
+#pragma unroll
+					for (int k = 0; k < 4; k++) V[(sl >> (4 * k)) & 15u] = Vt[k];
+				}
+			}
+		}
+	}
+	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // records consumed: prefetch
+	if (live) {
+#pragma unroll
+		for (uint32_t k = 0; k < NV; k++) {
+			if (k < nv) {
+				if (finish && (mask & (1u << k))) __stcg(C.vert + 2 * (size_t)vid[k], X[k]);
+				__stcg(C.vert + 2 * (size_t)vid[k] + 1, V[k]);
+			}
+		}
+	}
+}
+
+// kind 0: element Rayleigh damping, 1: PBD damping.
+__device__ __forceinline__ void run_damp_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane,
+                                               int kind, bool finish, float inv_dt, uint32_t tick) {
+	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
+	if (m.z & kShapeCube) {
+		if (kind == 0)
+			damp_chunk<true, 0>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+		else
+			damp_chunk<true, 1>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+	} else {
+		if (kind == 0)
+			damp_chunk<false, 0>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+		else
+			damp_chunk<false, 1>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+	}
+}
+
 // Vertices in no tet: nothing else touches them, so one thread takes each
 // through all nsub substeps at once (predict, then finalize + predict); the
 // final finalize pass closes the last one.
+// With damping sweeps the launch ends in the canonical state without a
+// closing finalize pass, so these vertices are finalized here (finalize_end).
 template <bool TAPE = false>
 __device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, uint32_t step, uint32_t nsub, float dt,
-                                             float inv_dt) {
+                                             float inv_dt, bool finalize_end = false) {
 	for (uint32_t i = begin; i < C.nisolated; i += step) {
 		const uint32_t v = __ldg(C.isolated + i);
 		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
@@ -192,6 +419,7 @@ __device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, ui
 			advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
 			if (TAPE) tape_vertex(C, v, O, Dbefore, s, s == 0);
 		}
+		if (finalize_end) finalize_vertex(C.bodies, O, D, inv_dt);
 		__stcg(C.vert + 2 * (size_t)v, O);
 		__stcg(C.vert + 2 * (size_t)v + 1, D);
 	}
@@ -213,28 +441,43 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 	}
 }
 
-// The warp's next chunk after `ch` (colour c of substep s): the next chunk of
-// the same colour, else its first chunk of the following colours (wrapping
-// into the next substep); -1 when the launch has no more work for it.
-__device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t nsub, uint32_t c, uint32_t ch,
-                                          uint32_t gwarp, uint32_t nwarps) {
-	if (ch + nwarps < __ldg(C.colour_chunk_begin + c + 1)) return (int)(ch + nwarps);
-	for (uint32_t k = 1; k <= C.ncolours; k++) {
-		uint32_t c2 = c + k, s2 = s;
-		if (c2 >= C.ncolours) {
-			c2 -= C.ncolours;
+// A substep is P = kinds x ncolours passes: the solve sweep over the colours,
+// then each damping sweep (DevCtx::damp_kinds) over them again; pass q works
+// on colour q % ncolours.
+__device__ __forceinline__ uint32_t pass_kinds(const DevCtx& C) { return 1u + (uint32_t)__popc(C.damp_kinds); }
+
+// The warp's next chunk after `ch` (pass q of substep s, P passes per
+// substep): the next chunk of the same colour, else its first chunk of the
+// following passes (wrapping into the next substep); -1 when the launch has no
+// more work for it.
+__device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t nsub, uint32_t q, uint32_t P,
+                                          uint32_t ch, uint32_t gwarp, uint32_t nwarps) {
+	if (ch + nwarps < __ldg(C.colour_chunk_begin + q % C.ncolours + 1)) return (int)(ch + nwarps);
+	for (uint32_t k = 1; k <= P; k++) {
+		uint32_t q2 = q + k, s2 = s;
+		if (q2 >= P) {
+			q2 -= P;
 			s2++;
 		}
 		if (s2 >= nsub) return -1;
+		const uint32_t c2 = q2 % C.ncolours;
 		const uint32_t first = __ldg(C.colour_chunk_begin + c2) + gwarp;
 		if (first < __ldg(C.colour_chunk_begin + c2 + 1)) return (int)first;
 	}
 	return -1;
 }
 
-// Persistent kernel: nsub substeps x ncolours colour passes separated by the
-// bounded grid barrier. Must be launched cooperatively (co-resident grid).
-template <bool LAMBDAS, bool TAPE = false>
+// Damping kind of pass-kind index k >= 1: 0 element Rayleigh, 1 PBD.
+__device__ __forceinline__ int damp_kind(const DevCtx& C, uint32_t k) { return (k == 1u && (C.damp_kinds & 1u)) ? 0 : 1; }
+
+// Persistent kernel: nsub substeps x P passes separated by the bounded grid
+// barrier. Must be launched cooperatively (co-resident grid). Without damping
+// the substep state stays (O, D) between substeps and the closing pass
+// finalizes it; with damping sweeps they finish every substep and the state
+// between substeps is canonical (X, V).
+// DAMP: the damping sweeps and the in-solve damping compiled in (handles with
+// damping switched on); without it they cost the kernel nothing.
+template <bool LAMBDAS, bool TAPE = false, bool DAMP = false>
 __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, float dt) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t lane = threadIdx.x & 31u;
@@ -242,20 +485,27 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	// chunk i of a colour goes to block i % grid, so chunks spread over all SMs
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	const bool dmode = DAMP && C.damp_kinds != 0u;
+	const uint32_t P = (DAMP ? pass_kinds(C) : 1u) * C.ncolours;
+	const uint32_t tick0 = __ldcg(C.tick);  // read before the first barrier; block 0 advances it at the end
 	Stage st = stage_init(C, lane);
-	run_isolated<TAPE>(C, gtid, nthreads, nsub, dt, inv_dt);
+	run_isolated<TAPE>(C, gtid, nthreads, nsub, dt, inv_dt, dmode);
 	uint32_t target = 0;
 	bool ok = true;
 	for (uint32_t s = 0; s < nsub && ok; s++) {
-		for (uint32_t c = 0; c < C.ncolours && ok; c++) {
+		for (uint32_t q = 0; q < P && ok; q++) {
+			const uint32_t kind = q / C.ncolours, c = q - kind * C.ncolours;
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				if (!stage_acquire(C, st, ch, lane)) {
 					ok = false;
 					break;
 				}
-				run_chunk<LAMBDAS, TAPE>(C, st, ch, next_chunk(C, s, nsub, c, ch, gwarp, nwarps), lane, s == 0, dt,
-				                         inv_dt, inv_dt2, s);
+				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps);
+				if (!DAMP || kind == 0)
+					run_chunk<LAMBDAS, TAPE, DAMP>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s);
+				else
+					run_damp_chunk(C, st, ch, next, lane, damp_kind(C, kind), kind == 1, inv_dt, tick0 + s);
 			}
 			if (!grid_sync(C, target)) ok = false;
 		}
@@ -265,7 +515,8 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 		if (st.inflight >= 0) mbar_wait(C, st.mbar, st.parity);
 		return;
 	}
-	run_finalize<TAPE>(C, gtid, nthreads, inv_dt, nsub);
+	if (!dmode) run_finalize<TAPE>(C, gtid, nthreads, inv_dt, nsub);
+	if (gtid == 0) *C.tick = tick0 + nsub;
 }
 
 __device__ __forceinline__ void st_release_gpu(uint32_t* p, uint32_t v) {
@@ -321,6 +572,7 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	const uint32_t tick0 = __ldcg(C.tick);
 	Stage st = stage_init(C, lane);
 	run_isolated(C, gtid, nthreads, nsub, dt, inv_dt);
 	bool ok = true;
@@ -328,7 +580,7 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 		for (uint32_t c = 0; c < C.ncolours && ok; c++) {
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
-				const int next = next_chunk(C, s, nsub, c, ch, gwarp, nwarps);
+				const int next = next_chunk(C, s, nsub, c, C.ncolours, ch, gwarp, nwarps);
 				if (st.inflight != (int)ch) stage_issue_or_wait(C, st, ch, lane);  // records do not depend on neighbours
 				if (!wait_deps(C, ch, s, lane) || !stage_acquire(C, st, ch, lane)) {
 					ok = false;
@@ -350,18 +602,22 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 	uint32_t target = 0;
 	if (!grid_sync(C, target) || !ok) return;
 	run_finalize(C, gtid, nthreads, inv_dt);
+	if (gtid == 0) *C.tick = tick0 + nsub;
 }
 
 // One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
-// In the first launch of a call, blocks past the colour's chunks step the
-// isolated vertices through all nsub substeps.
-template <bool LAMBDAS>
+// kind 0 is the solve pass (first: the state is canonical), 1 and up the
+// damping passes (damp_kind; kind 1 finishes the substep); sub: the substep's
+// index in the call (its tick is *C.tick + sub). In the first launch of a
+// call, blocks past the colour's chunks step the isolated vertices through
+// all nsub substeps.
+template <bool LAMBDAS, bool DAMP = false>
 __global__ void __launch_bounds__(256, 1) k_colour(DevCtx C, uint32_t colour, int first, float dt, uint32_t solve_blocks,
-                                                uint32_t nsub) {
+                                                uint32_t nsub, uint32_t kind, uint32_t sub) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	if (blockIdx.x >= solve_blocks) {
 		const uint32_t b = blockIdx.x - solve_blocks, nb = gridDim.x - solve_blocks;
-		run_isolated(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, nsub, dt, inv_dt);
+		run_isolated(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, nsub, dt, inv_dt, DAMP && C.damp_kinds != 0u);
 		return;
 	}
 	const uint32_t lane = threadIdx.x & 31u;
@@ -369,12 +625,18 @@ __global__ void __launch_bounds__(256, 1) k_colour(DevCtx C, uint32_t colour, in
 	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
 	Stage st = stage_init(C, lane);
 	if (!stage_acquire(C, st, ch, lane)) return;
-	run_chunk<LAMBDAS>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2);
+	if (!DAMP || kind == 0)
+		run_chunk<LAMBDAS, false, DAMP>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2);
+	else
+		run_damp_chunk(C, st, ch, -1, lane, damp_kind(C, kind), kind == 1, inv_dt, __ldcg(C.tick) + sub);
 }
 
 __global__ void k_finalize(DevCtx C, float dt) {
 	run_finalize(C, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, 1.0f / dt);
 }
+
+// Advances the tick word by a call's substeps (CUDA-graph mode).
+__global__ void k_advance_tick(DevCtx C, uint32_t nsub) { *C.tick += nsub; }
 
 // ---- transfers ----------------------------------------------------------------
 __global__ void k_gather_xyz(const float4* __restrict__ vert, int which, const uint32_t* __restrict__ dev_of,
@@ -459,10 +721,22 @@ static void set_smem_attr(const void* f, size_t bytes) {
 	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+static const void* persistent_fn(bool lambdas, bool damp) {
+	if (damp) return lambdas ? (const void*)k_persistent<true, false, true> : (const void*)k_persistent<false, false, true>;
+	return lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+}
+
+static const void* colour_fn(bool lambdas, bool damp) {
+	if (damp) return lambdas ? (const void*)k_colour<true, true> : (const void*)k_colour<false, true>;
+	return lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>;
+}
+
 int configure_kernels(const LaunchCfg& cfg) {
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
-	set_smem_attr(cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>, smem);
-	set_smem_attr(cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>, smem);
+	for (bool damp : {false, true}) {
+		set_smem_attr(persistent_fn(cfg.lambdas, damp), smem);
+		set_smem_attr(colour_fn(cfg.lambdas, damp), smem);
+	}
 	set_smem_attr(cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>, smem);
 	return (int)cudaGetLastError();
 }
@@ -470,7 +744,7 @@ int configure_kernels(const LaunchCfg& cfg) {
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
 	const void* f = cfg.sync_mode == 3
 	                    ? (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>)
-	                    : (cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>);
+	                    : persistent_fn(cfg.lambdas, cfg.damp);
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	cudaError_t e = cudaGetDevice(&dev);
@@ -493,37 +767,44 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 		DevCtx c = ctx;
 		void* args[] = {&c, &nsub, &dt};
 		const void* f = cfg.sync_mode == 1
-		                    ? (cfg.lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>)
+		                    ? persistent_fn(cfg.lambdas, cfg.damp)
 		                    : (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>);
 		e = cudaLaunchCooperativeKernel(f, dim3(cfg.blocks), dim3(cfg.block), args, smem, st);
 		return (int)e;
 	}
-	// per-colour launches (captured into a CUDA graph by the caller when wanted)
-	const void* fc = cfg.lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>;
+	// per-colour launches (captured into a CUDA graph by the caller when wanted):
+	// per substep the solve sweep, then each damping sweep
+	const void* fc = colour_fn(cfg.lambdas, cfg.damp);
 	const uint32_t warps_per_block = cfg.block / 32;
+	const bool dmode = cfg.damp && ctx.damp_kinds != 0u;
+	const uint32_t kinds = dmode ? 1u + (uint32_t)__builtin_popcount(ctx.damp_kinds) : 1u;
 	for (uint32_t s = 0; s < nsub; s++) {
-		for (uint32_t c = 0; c < ctx.ncolours; c++) {
-			const uint32_t nch = cfg.colour_chunk_begin_host[c + 1] - cfg.colour_chunk_begin_host[c];
-			uint32_t sb = (nch + warps_per_block - 1) / warps_per_block;
-			uint32_t extra = 0;
-			if (s == 0 && c == 0 && ctx.nisolated) extra = (ctx.nisolated + cfg.block - 1) / cfg.block;
-			const uint32_t grid = sb + extra;
-			if (grid == 0) continue;
-			DevCtx cc = ctx;
-			uint32_t colour = c, ns = nsub;
-			int first = s == 0 ? 1 : 0;
-			float dtv = dt;
-			void* args[] = {&cc, &colour, &first, &dtv, &sb, &ns};
-			e = cudaLaunchKernel(fc, dim3(grid), dim3(cfg.block), args, smem, st);
-			if (e != cudaSuccess) return (int)e;
+		for (uint32_t kind = 0; kind < kinds; kind++) {
+			for (uint32_t c = 0; c < ctx.ncolours; c++) {
+				const uint32_t nch = cfg.colour_chunk_begin_host[c + 1] - cfg.colour_chunk_begin_host[c];
+				uint32_t sb = (nch + warps_per_block - 1) / warps_per_block;
+				uint32_t extra = 0;
+				if (s == 0 && kind == 0 && c == 0 && ctx.nisolated) extra = (ctx.nisolated + cfg.block - 1) / cfg.block;
+				const uint32_t grid = sb + extra;
+				if (grid == 0) continue;
+				DevCtx cc = ctx;
+				uint32_t colour = c, ns = nsub, kd = kind, sub = s;
+				int first = (dmode || s == 0) ? 1 : 0;
+				float dtv = dt;
+				void* args[] = {&cc, &colour, &first, &dtv, &sb, &ns, &kd, &sub};
+				e = cudaLaunchKernel(fc, dim3(grid), dim3(cfg.block), args, smem, st);
+				if (e != cudaSuccess) return (int)e;
+			}
 		}
 	}
 	const uint32_t fb = (ctx.nverts + 255) / 256;
-	if (fb) {
+	if (fb && !dmode) {
 		k_finalize<<<fb, 256, 0, st>>>(ctx, dt);
 		e = cudaGetLastError();
+		if (e != cudaSuccess) return (int)e;
 	}
-	return (int)e;
+	k_advance_tick<<<1, 1, 0, st>>>(ctx, nsub);
+	return (int)cudaGetLastError();
 }
 
 // The recording forward: k_persistent with the tape writes compiled in. The
@@ -627,7 +908,7 @@ int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bo
 		p = g_noalloc_ptr[device];
 	}
 	cudaStream_t st = (cudaStream_t)stream;
-	const void* f = lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
+	const void* f = persistent_fn(lambdas, ctx.damp_any != 0u);
 	const size_t smem = solve_smem_bytes(block, warp_smem);
 	int sms = 0, per_sm = 0;
 	cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);

@@ -40,6 +40,8 @@ class Settings(C.Structure):
         ("wonkiness", C.c_float), ("left_right_separation", C.c_float), ("flags", C.c_uint32),
         ("time_corrected_drag", C.c_float), ("yeoh", C.c_float * 3), ("ground", C.c_uint32),
         ("ground_normal", C.c_float * 3), ("ground_offset", C.c_float), ("friction", C.c_float),
+        ("volume_and_time_corrected_pbd_damping", C.c_float),
+        ("amortized_volume_and_time_corrected_pbd_damping", C.c_float), ("tick_id", C.c_uint32),
     ]
 
 
@@ -71,7 +73,7 @@ EXPORTS = [
     "xfem_get_lambdas", "xfem_calculate_volume", "xfem_get_rest_state", "xfem_get_schedule",
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
-    "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward",
+    "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward", "xfem_pbd_damping_coefficients",
 ]
 
 _lib = None
@@ -117,6 +119,7 @@ def lib():
         L.xfem_compute_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P]
         L.xfem_generate_tet_block.argtypes = [u32, u32, u32, f32, f32, f32, u32, f32, P, P]
         L.xfem_adjoint_forward.argtypes = [P, u32, f32, u32, u32, P, P]
+        L.xfem_pbd_damping_coefficients.argtypes = [f32, f32, f32, P]
         L.xfem_adjoint_backward.argtypes = [P, P, P, P, P, P, P]
         _lib = L
     return _lib
@@ -145,6 +148,14 @@ def default_settings(**kw):
 def as_settings(s):
     """A Settings struct from a Settings struct or a dict of its fields."""
     return default_settings(**s) if isinstance(s, dict) else s
+
+
+def pbd_damping_coefficients(pbd_damping, substep_dt, spacing):
+    """(volumeAndTimeCorrectedPbdDamping, its amortized form) for a substep of
+    substep_dt and element spacing `spacing` (XPBDFEM/Demo.cpp:53-61)."""
+    out = (C.c_float * 2)()
+    _check(lib().xfem_pbd_damping_coefficients(pbd_damping, substep_dt, spacing, out))
+    return float(out[0]), float(out[1])
 
 
 def time_corrected_drag(drag, substep_dt):
