@@ -18,6 +18,8 @@ shape the configuration names.
   roofline, cpu_baseline (the oracle port of the reference in its own
   shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches, and
   "batched": 512 bodies in one launch per frame against one launch per body,
+  "damped": the same mesh with the reference web UI's default damping against
+  undamped,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -288,6 +290,7 @@ def run_xfem(args, world, rank, local):
     cpu = cpu_baseline_native(w) if not args.no_cpu else None
     batched = None if args.no_batched else run_batched(stream)
     adjoint = None if args.no_adjoint else run_adjoint(stream)
+    damped = None if args.no_damped else run_damped(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -307,6 +310,7 @@ def run_xfem(args, world, rank, local):
         "gpu_launches": launches_per_frame * args.steps,
         "batched": batched,
         "adjoint": adjoint,
+        "damped": damped,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -434,6 +438,53 @@ def run_adjoint(stream, reps=5, cases=("beam", "large"), large_substeps=None):
     return res
 
 
+def run_damped(stream, frames=5):
+    """The throughput mesh with the damping the reference's web UI starts with
+    (wasm/ui.js:76-78, 88: Rayleigh PostAmortized, damping 0.005, pbdDamping
+    0.03, drag 0.002; the element spacing 0.1 m stands in for the demo's
+    kSpacing), against the same mesh undamped: device-timed frames of 20
+    substeps, L2 flushed between frames."""
+    import torch
+
+    import xfem
+    from xfem import workloads as W
+    w = W.throughput()
+    S = w["substeps"]
+    sdt = w["dt"] / S
+    sp = C_void_p(stream.cuda_stream)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    vc, avc = xfem.pbd_damping_coefficients(0.03, sdt, 0.1)
+    damp = dict(w["settings"], damping=0.005, pbd_damping=0.03, time_corrected_drag=xfem.time_corrected_drag(0.002, sdt),
+                volume_and_time_corrected_pbd_damping=vc, amortized_volume_and_time_corrected_pbd_damping=avc,
+                flags=w["settings"]["flags"] | (3 << 20))
+    out = {}
+    for key, s_ in (("undamped", w["settings"]), ("damped", damp)):
+        body = xfem.Body(w["nodes"], w["idx"], w["density"], s_, stream=sp)
+        body.set_lock_mask(w["lock"])
+        for _ in range(3):
+            body.step_frames(1, S, sdt)
+        ms = []
+        for _ in range(frames):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                a.record(stream)
+            body.step_frames(1, S, sdt)
+            with torch.cuda.stream(stream):
+                b.record(stream)
+            b.synchronize()
+            ms.append(a.elapsed_time(b))
+        info = body.info()
+        body.close()
+        nt = w["idx"].size // 5
+        out[key] = {"ms_per_frame": statistics.median(ms), "value": nt * S / (statistics.median(ms) / 1e3),
+                    "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+                    "block": info["block_size"]}
+    return {"workload": w["name"] + ", damping as the reference's web UI starts (PostAmortized 0.005, PBD 0.03, "
+                                   "drag 0.002)", "unit": UNIT, **out,
+            "cost": out["damped"]["ms_per_frame"] / out["undamped"]["ms_per_frame"]}
+
+
 def C_void_p(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -458,6 +509,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-damped", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")

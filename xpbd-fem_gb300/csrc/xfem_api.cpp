@@ -101,6 +101,8 @@ struct xfem_body {
 	DevBuf<uint32_t> tet_rec_dev, tet_slot_dev;
 	DevBuf<uint32_t> tflat, tick;   // per tet row: index in the body's order; the tick word
 	DevBuf<float> tarea;            // per tet row: surface area
+	DevBuf<uint32_t> lastmask;      // per chunk lane: slots whose last solve it makes
+	DevBuf<uint8_t> pass_on;        // [damping kind][tick % 8][colour]
 	DevBuf<float> tet_vol_dev, tet_inv_mu, io;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
@@ -182,6 +184,36 @@ uint32_t damp_kinds_of(const std::vector<BodyHost>& bodies) {
 		if (b.settings.pbd_damping > 0.0f) k |= 2u;
 	}
 	return k;
+}
+
+// [damping kind][tick % 8][colour]: whether some body damps a tet of that
+// colour at that tick (kind 0 element Rayleigh for the Post types, 1 PBD);
+// the amortized type damps the eighth [nt m / 8, nt (m + 1) / 8) of the
+// body's flattened order, which is colour-major.
+std::vector<uint8_t> pass_table(const std::vector<BodyHost>& bodies, uint32_t ncol) {
+	std::vector<uint8_t> on(16 * (size_t)ncol, 0);
+	for (const BodyHost& b : bodies) {
+		const uint32_t type = (b.settings.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u;
+		const bool kind_on[2] = {type >= XFEM_RAYLEIGH_POST && b.settings.damping > 0.0f, b.settings.pbd_damping > 0.0f};
+		const Schedule& sc = b.sched;
+		std::vector<uint32_t> ct(sc.ncolours + 1, 0);
+		for (uint32_t c = 0; c < sc.ncolours; c++) {
+			uint32_t n = 0;
+			for (uint32_t i = sc.colour_cl_begin[c]; i < sc.colour_cl_begin[c + 1]; i++)
+				n += sc.cl_begin[sc.colour_cl[i] + 1] - sc.cl_begin[sc.colour_cl[i]];
+			ct[c + 1] = ct[c] + n;
+		}
+		for (int k = 0; k < 2; k++) {
+			if (!kind_on[k]) continue;
+			for (uint32_t m = 0; m < 8; m++) {
+				const uint32_t lo = type == XFEM_RAYLEIGH_POST_AMORTIZED ? b.nt * m / 8u : 0u;
+				const uint32_t hi = type == XFEM_RAYLEIGH_POST_AMORTIZED ? b.nt * (m + 1u) / 8u : b.nt;
+				for (uint32_t c = 0; c < sc.ncolours; c++)
+					if (ct[c] < hi && lo < ct[c + 1]) on[((size_t)k * 8 + m) * ncol + c] = 1;
+			}
+		}
+	}
+	return on;
 }
 
 // c0 = (1/mu)/volume exactly as the reference forms comp[0] (XPBDFEM/Fem.cpp:449).
@@ -372,6 +404,23 @@ int build_device(xfem_body* h) {
 		}
 		if (cube) meta[k].shape |= kShapeCube;
 	}
+	// the last (highest-colour) cluster touching each vertex
+	std::vector<uint32_t> lastmask((size_t)nch * kLanes, 0);
+	{
+		std::vector<uint32_t> last(nverts, 0xffffffffu);
+		for (int pass = 0; pass < 2; pass++)
+			for (uint32_t k = 0; k < nch; k++) {
+				const float4* rec = &cblk[meta[k].off16];
+				const uint32_t* hdr = reinterpret_cast<const uint32_t*>(rec + 128 * (size_t)shape_nt[k]);
+				const uint32_t* vid = hdr + kLanes;
+				for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++)
+					for (uint32_t sl = 0; sl < (hdr[lane] & 15u); sl++) {
+						const uint32_t dv = vid[(size_t)sl * kLanes + lane];
+						if (pass == 0) last[dv] = k * kLanes + lane;  // chunks are colour-major
+						else if (last[dv] == k * kLanes + lane) lastmask[(size_t)k * kLanes + lane] |= 1u << sl;
+					}
+			}
+	}
 	// The cube path takes its slots from a table: its bulk copy stops before
 	// the slot words at the end of the block.
 	max_bytes = 128;
@@ -497,6 +546,11 @@ int build_device(xfem_body* h) {
 		XCUDA(h->tflat.alloc(flat.size()));
 		XCUDA(h->tarea.alloc(area.size()));
 		XCUDA(h->tick.alloc(1));
+		XCUDA(h->lastmask.alloc(lastmask.size()));
+		XCUDA(up(h->lastmask.p, lastmask.data(), lastmask.size() * 4));
+		XCUDA(h->pass_on.alloc(16 * (size_t)ncol));
+		const std::vector<uint8_t> pt = pass_table(h->bodies, ncol);
+		XCUDA(up(h->pass_on.p, pt.data(), pt.size()));
 		XCUDA(up(h->tflat.p, flat.data(), flat.size() * 4));
 		XCUDA(up(h->tarea.p, area.data(), area.size() * 4));
 		const uint32_t tick0 = h->bodies.empty() ? 0u : h->bodies[0].settings.tick_id;
@@ -523,6 +577,8 @@ int build_device(xfem_body* h) {
 	c.ntrows = trows;
 	c.damp_kinds = damp_kinds_of(h->bodies);
 	c.damp_any = damp_any_of(h->bodies) ? 1u : 0u;
+	c.lastmask = h->lastmask.p;
+	c.pass_on = h->pass_on.p;
 	c.tick = h->tick.p;
 	c.tflat = h->tflat.p;
 	c.tarea = h->tarea.p;
@@ -847,6 +903,8 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	// Settings::tickId: the handle's substep counter continues from here
 	XCUDA(cudaMemcpyAsync(h->tick.p, &s->tick_id, 4, cudaMemcpyHostToDevice, h->stream));
+	const std::vector<uint8_t> pt = pass_table(h->bodies, h->ncolours);
+	XCUDA(cudaMemcpyAsync(h->pass_on.p, pt.data(), pt.size(), cudaMemcpyHostToDevice, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	const uint32_t kinds = damp_kinds_of(h->bodies);
 	const bool damp = damp_any_of(h->bodies);

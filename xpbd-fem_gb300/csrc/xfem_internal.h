@@ -137,6 +137,9 @@ struct DevCtx {
 	uint32_t* tick;             // device word: Settings::tickId of the launch's first substep
 	const uint32_t* tflat;      // [tet row][lane]: the tet's index in its body's flattened order
 	const float* tarea;         // [tet row][lane]: the tet's surface area (rest state)
+	const uint32_t* lastmask;   // [chunk][lane]: slots whose last solve of a substep this
+	                            // cluster makes (it finishes them when damping sweeps run)
+	const uint8_t* pass_on;     // [damping kind][tick % 8][colour]: some tet is damped
 };
 
 // Reverse-pass state (xfem_adjoint.cu).

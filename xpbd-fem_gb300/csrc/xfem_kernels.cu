@@ -199,7 +199,8 @@ __device__ __forceinline__ DampTet damp_of(const DevCtx& C, const BodyParams& bp
 
 template <bool LAMBDAS, bool TAPE, bool DAMP>
 __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first, float dt,
-                                               float inv_dt, float inv_dt2, uint32_t trow, uint32_t s_launch) {
+                                               float inv_dt, float inv_dt2, uint32_t trow, uint32_t s_launch,
+                                               uint32_t chunk, bool finish_last) {
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
 	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
 	const uint32_t* vids = hdrs + kLanes;
@@ -239,9 +240,13 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 	}
 	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
 	if (live) {
+		// with damping sweeps, the vertex's last solve of the substep finishes
+		// it (to the canonical X, V that the sweeps work on)
+		const uint32_t last = DAMP && finish_last ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
-			if (mask & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
+			if (DAMP && (last & (1u << s))) finalize_vertex(C.bodies, O[s], D[s], inv_dt);
+			if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
 			__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
 		}
 	}
@@ -252,11 +257,13 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 // been consumed, so it overlaps the write-back and what follows.
 template <bool LAMBDAS, bool TAPE = false, bool DAMP = false>
 __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, bool first,
-                                          float dt, float inv_dt, float inv_dt2, uint32_t s_launch = 0) {
+                                          float dt, float inv_dt, float inv_dt2, uint32_t s_launch = 0,
+                                          bool finish_last = false) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
-		run_chunk_cube<LAMBDAS, TAPE, DAMP>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch);
+		run_chunk_cube<LAMBDAS, TAPE, DAMP>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch, chunk,
+		                                    finish_last);
 		return;
 	}
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
@@ -305,24 +312,27 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 	}
 	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
 	if (nv) {
+		const uint32_t last = DAMP && finish_last ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
-				if (mask & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], sO[s * kLanes]);
-				__stcg(C.vert + 2 * (size_t)vid[s] + 1, sD[s * kLanes]);
+				float4 O = sO[s * kLanes], D = sD[s * kLanes];
+				if (DAMP && (last & (1u << s))) finalize_vertex(C.bodies, O, D, inv_dt);
+				if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O);
+				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D);
 			}
 		}
 	}
 }
 
 // One damping pass over a resident chunk (KIND 0: element Rayleigh damping,
-// 1: PBD damping); lane = cluster, tets in the cluster's order. With
-// `finish` (the sweep's first pass) the owner of each vertex first finishes
-// the substep for it (locks, ground, V = D/dt, X = O + D), as the solve
-// sweep's owner advances it. CUBE: canonical cube chunks, all in registers.
+// 1: PBD damping); lane = cluster, tets in the cluster's order. The state is
+// the canonical (X, V): each vertex's last solve of the substep finished it.
+// Only velocities change. CUBE: canonical cube chunks, all in registers. Not
+// inlined: the damping passes then cost the solve path no registers.
 template <bool CUBE, int KIND>
-__device__ __forceinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t ntmax, uint32_t nvmax, uint32_t trow,
-                                           int next, uint32_t lane, bool finish, float inv_dt, uint32_t tick) {
+__device__ __noinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t ntmax, uint32_t nvmax, uint32_t trow,
+                                        int next, uint32_t lane, float inv_dt, uint32_t tick) {
 	constexpr uint32_t NV = CUBE ? 8u : kMaxClusterVerts;
 	constexpr uint32_t NT = CUBE ? 6u : kMaxClusterTets;
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
@@ -331,7 +341,7 @@ __device__ __forceinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t 
 	const uint32_t* slots = vids + kLanes * nvmax;
 	const uint32_t hdr = hdrs[lane];
 	const bool live = (hdr & 15u) != 0;
-	const uint32_t nv = CUBE ? 8u : (hdr & 15u), nt = CUBE ? 6u : ((hdr >> 4) & 15u), mask = (hdr >> 8) & 0xffu;
+	const uint32_t nv = CUBE ? 8u : (hdr & 15u), nt = CUBE ? 6u : ((hdr >> 4) & 15u);
 	uint32_t vid[NV];
 	float4 X[NV], V[NV];
 	if (live) {
@@ -343,7 +353,6 @@ __device__ __forceinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t 
 				vid[k] = vids[k * kLanes + lane];
 				X[k] = __ldcg(C.vert + 2 * (size_t)vid[k]);
 				V[k] = __ldcg(C.vert + 2 * (size_t)vid[k] + 1);
-				if (finish && (mask & (1u << k))) finalize_vertex(C.bodies, X[k], V[k], inv_dt);
 			}
 		}
 #pragma unroll
@@ -377,30 +386,32 @@ __device__ __forceinline__ void damp_chunk(const DevCtx& C, Stage& st, uint32_t 
 	if (live) {
 #pragma unroll
 		for (uint32_t k = 0; k < NV; k++) {
-			if (k < nv) {
-				if (finish && (mask & (1u << k))) __stcg(C.vert + 2 * (size_t)vid[k], X[k]);
-				__stcg(C.vert + 2 * (size_t)vid[k] + 1, V[k]);
-			}
+			if (k < nv) __stcg(C.vert + 2 * (size_t)vid[k] + 1, V[k]);
 		}
 	}
 }
 
 // kind 0: element Rayleigh damping, 1: PBD damping.
 __device__ __forceinline__ void run_damp_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane,
-                                               int kind, bool finish, float inv_dt, uint32_t tick) {
+                                               int kind, float inv_dt, uint32_t tick) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
 		if (kind == 0)
-			damp_chunk<true, 0>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+			damp_chunk<true, 0>(C, st, ntmax, nvmax, trow, next, lane, inv_dt, tick);
 		else
-			damp_chunk<true, 1>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+			damp_chunk<true, 1>(C, st, ntmax, nvmax, trow, next, lane, inv_dt, tick);
 	} else {
 		if (kind == 0)
-			damp_chunk<false, 0>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+			damp_chunk<false, 0>(C, st, ntmax, nvmax, trow, next, lane, inv_dt, tick);
 		else
-			damp_chunk<false, 1>(C, st, ntmax, nvmax, trow, next, lane, finish, inv_dt, tick);
+			damp_chunk<false, 1>(C, st, ntmax, nvmax, trow, next, lane, inv_dt, tick);
 	}
+}
+
+// Whether damping pass (kind index k >= 1, colour c) has work at this tick.
+__device__ __forceinline__ bool pass_on(const DevCtx& C, int dk, uint32_t c, uint32_t tick) {
+	return __ldg(C.pass_on + ((size_t)dk * 8u + tick % 8u) * C.ncolours + c) != 0;
 }
 
 // Vertices in no tet: nothing else touches them, so one thread takes each
@@ -446,12 +457,22 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 // on colour q % ncolours.
 __device__ __forceinline__ uint32_t pass_kinds(const DevCtx& C) { return 1u + (uint32_t)__popc(C.damp_kinds); }
 
+// Damping kind of pass-kind index k >= 1: 0 element Rayleigh, 1 PBD.
+__device__ __forceinline__ int damp_kind(const DevCtx& C, uint32_t k) { return (k == 1u && (C.damp_kinds & 1u)) ? 0 : 1; }
+
+// Whether pass q (P passes per substep) runs at `tick`: the solve passes
+// always, a damping pass only if some tet of its colour is damped then.
+__device__ __forceinline__ bool pass_runs(const DevCtx& C, uint32_t q, uint32_t tick) {
+	const uint32_t kind = q / C.ncolours;
+	return kind == 0 || pass_on(C, damp_kind(C, kind), q - kind * C.ncolours, tick);
+}
+
 // The warp's next chunk after `ch` (pass q of substep s, P passes per
-// substep): the next chunk of the same colour, else its first chunk of the
-// following passes (wrapping into the next substep); -1 when the launch has no
-// more work for it.
+// substep, tick0 the launch's first tick): the next chunk of the same colour,
+// else its first chunk of the following passes that run (wrapping into the
+// next substep); -1 when the launch has no more work for it.
 __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t nsub, uint32_t q, uint32_t P,
-                                          uint32_t ch, uint32_t gwarp, uint32_t nwarps) {
+                                          uint32_t ch, uint32_t gwarp, uint32_t nwarps, uint32_t tick0 = 0) {
 	if (ch + nwarps < __ldg(C.colour_chunk_begin + q % C.ncolours + 1)) return (int)(ch + nwarps);
 	for (uint32_t k = 1; k <= P; k++) {
 		uint32_t q2 = q + k, s2 = s;
@@ -460,15 +481,13 @@ __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t 
 			s2++;
 		}
 		if (s2 >= nsub) return -1;
+		if (P > C.ncolours && !pass_runs(C, q2, tick0 + s2)) continue;
 		const uint32_t c2 = q2 % C.ncolours;
 		const uint32_t first = __ldg(C.colour_chunk_begin + c2) + gwarp;
 		if (first < __ldg(C.colour_chunk_begin + c2 + 1)) return (int)first;
 	}
 	return -1;
 }
-
-// Damping kind of pass-kind index k >= 1: 0 element Rayleigh, 1 PBD.
-__device__ __forceinline__ int damp_kind(const DevCtx& C, uint32_t k) { return (k == 1u && (C.damp_kinds & 1u)) ? 0 : 1; }
 
 // Persistent kernel: nsub substeps x P passes separated by the bounded grid
 // barrier. Must be launched cooperatively (co-resident grid). Without damping
@@ -495,17 +514,21 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	for (uint32_t s = 0; s < nsub && ok; s++) {
 		for (uint32_t q = 0; q < P && ok; q++) {
 			const uint32_t kind = q / C.ncolours, c = q - kind * C.ncolours;
+			// a damping pass with nothing to damp at this tick is skipped by
+			// every block alike (same table, same tick): no work, no barrier
+			if (DAMP && kind > 0 && !pass_runs(C, q, tick0 + s)) continue;
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				if (!stage_acquire(C, st, ch, lane)) {
 					ok = false;
 					break;
 				}
-				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps);
+				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps, tick0);
 				if (!DAMP || kind == 0)
-					run_chunk<LAMBDAS, TAPE, DAMP>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s);
+					run_chunk<LAMBDAS, TAPE, DAMP>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s,
+					                               dmode);
 				else
-					run_damp_chunk(C, st, ch, next, lane, damp_kind(C, kind), kind == 1, inv_dt, tick0 + s);
+					run_damp_chunk(C, st, ch, next, lane, damp_kind(C, kind), inv_dt, tick0 + s);
 			}
 			if (!grid_sync(C, target)) ok = false;
 		}
@@ -623,12 +646,18 @@ __global__ void __launch_bounds__(256, 1) k_colour(DevCtx C, uint32_t colour, in
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t ch = __ldg(C.colour_chunk_begin + colour) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
+	const uint32_t tick = __ldcg(C.tick) + sub;
+	const int dk = DAMP && kind > 0 ? damp_kind(C, kind) : 0;
+	// a graph replays its launches at every tick: a damping pass with nothing
+	// to damp at this one returns at once
+	if (DAMP && kind > 0 && !pass_on(C, dk, colour, tick)) return;
 	Stage st = stage_init(C, lane);
 	if (!stage_acquire(C, st, ch, lane)) return;
 	if (!DAMP || kind == 0)
-		run_chunk<LAMBDAS, false, DAMP>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2);
+		run_chunk<LAMBDAS, false, DAMP>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2, 0,
+		                                DAMP && C.damp_kinds != 0u);
 	else
-		run_damp_chunk(C, st, ch, -1, lane, damp_kind(C, kind), kind == 1, inv_dt, __ldcg(C.tick) + sub);
+		run_damp_chunk(C, st, ch, -1, lane, dk, inv_dt, tick);
 }
 
 __global__ void k_finalize(DevCtx C, float dt) {
