@@ -17,8 +17,17 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 
-ENERGY_MIXED_SEL = 4      # Energy_MixedSel, XPBDFEM/Settings.h:45
-ENERGY_YEOH_SKIN_FAST = 7  # Energy_YeohSkinFast, XPBDFEM/Settings.h:48
+# Energy model ids, XPBDFEM/Settings.h:41-53
+ENERGY_PIXAR = 0
+ENERGY_PIXAR_REDUCED = 1
+ENERGY_PIXAR_SEL = 2
+ENERGY_MIXED = 3
+ENERGY_MIXED_SEL = 4
+ENERGY_YEOH_SKIN = 5
+ENERGY_YEOH_SKIN_SEL = 6
+ENERGY_YEOH_SKIN_FAST = 7
+ENERGY_CUBE_NEO = 11
+ENERGY_CUBE_SKIN = 12
 REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
 
 
@@ -31,14 +40,14 @@ class Params(C.Structure):
         ("ground", C.c_uint32), ("ground_n", C.c_float * 3), ("ground_d", C.c_float),
         ("friction", C.c_float), ("damping", C.c_float), ("rayleigh_type", C.c_uint32),
         ("pbd_damping", C.c_float), ("pbd_coeff", C.c_float), ("pbd_coeff_amortized", C.c_float),
-        ("tick", C.c_uint32),
+        ("tick", C.c_uint32), ("volume_passes", C.c_uint32),
     ]
 
 
 def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=True,
                 gravity=(0.0, 0.0, 0.0), drag=0.0, yeoh=REF_YEOH, lock=False,
                 ground=False, ground_n=(0.0, 0.0, 1.0), ground_d=0.0, friction=0.0, damping=0.0, rayleigh_type=2,
-                pbd_damping=0.0, pbd_coeff=0.0, pbd_coeff_amortized=0.0, tick=0):
+                pbd_damping=0.0, pbd_coeff=0.0, pbd_coeff_amortized=0.0, tick=0, volume_passes=0):
     p = Params()
     p.gravity[:] = [float(g) for g in gravity]
     p.dt = dt
@@ -59,6 +68,7 @@ def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=T
     p.pbd_coeff = pbd_coeff
     p.pbd_coeff_amortized = pbd_coeff_amortized
     p.tick = tick
+    p.volume_passes = volume_passes
     return p
 
 
@@ -80,7 +90,8 @@ def params_from_settings(s, dt, lock=True, tick=None):
                        pbd_damping=g("pbd_damping", 0.0),
                        pbd_coeff=g("volume_and_time_corrected_pbd_damping", 0.0),
                        pbd_coeff_amortized=g("amortized_volume_and_time_corrected_pbd_damping", 0.0),
-                       tick=int(g("tick_id", 0)) if tick is None else int(tick))
+                       tick=int(g("tick_id", 0)) if tick is None else int(tick),
+                       volume_passes=int(g("volume_passes", 0)))
 
 
 _lib = None

@@ -34,14 +34,17 @@
  *       Substep used for same-order parity with the coloured GPU schedule.
  *   damped W H D sx sy sz wonkiness density energy simultaneous compliance
  *          poisson gx gy dt nsub lockleft damping pbdDamping drag rayleighType
- *          spacing < order.u32
+ *          spacing [volumePasses] < order.u32
  *       `ordered` with damping: Settings::damping, pbdDamping and drag, the
  *       Rayleigh type in flags bits 20-21, and the derived fields filled as
  *       Sim::Update does (XPBDFEM/Demo.cpp:53-63) with `spacing` in place of
  *       the demo's kSpacing; Geo3d::Substep then runs GeoLinear3d::Damp
  *       (XPBDFEM/Geo.cpp:346-355, 790-811) over the same order. Also dumps
  *       the derived values (volume- and time-corrected PBD damping, its
- *       amortized form, time-corrected drag).
+ *       amortized form, time-corrected drag). volumePasses (default 0) sets
+ *       Settings::volumePasses: GeoLinear3d::Constrain then runs that many
+ *       SolveElementVolume sweeps over the order after the solve
+ *       (XPBDFEM/Geo.cpp:780-783).
  */
 #include <cstdio>
 #include <cstdlib>
@@ -206,6 +209,7 @@ int main(int argc, char** argv) {
 			const float derived[3] = {s.volumeAndTimeCorrectedPbdDamping, s.amortizedVolumeAndTimeCorrectedPbdDamping,
 			                          s.timeCorrectedDrag};
 			emit("derived", 'f', derived, 3);
+			if (a < argc) s.volumePasses = U(a++);
 		}
 		Manipulator manip;
 		manip.pickedGeo = nullptr;

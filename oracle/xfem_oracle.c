@@ -190,8 +190,8 @@ int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const u
                             const uint32_t* tets, const float* ep, const float* tet_mu, const uint32_t* order,
                             const uint32_t* colour_begin, uint32_t ncolours, uint32_t nsub, const orc_params* p,
                             uint32_t threads) {
-	/* the undamped method only: damping runs in orc_substeps_f */
-	if (p->damping > 0.0f || p->pbd_damping > 0.0f) return -1;
+	/* the undamped method without volume passes only: those run in orc_substeps_f */
+	if (p->damping > 0.0f || p->pbd_damping > 0.0f || p->volume_passes) return -1;
 	if (threads < 1) threads = 1;
 	if (threads > 256) threads = 256;
 	double* O = (double*)malloc(sizeof(double) * 3 * (size_t)(nv ? nv : 1));

@@ -33,9 +33,23 @@
 extern "C" {
 #endif
 
-/* Energy model ids (XPBDFEM/Settings.h:41-53). */
+/* Energy model ids (XPBDFEM/Settings.h:41-53). On linear tets PixarReduced
+ * equals Pixar and YeohSkinSel equals YeohSkin (one quadrature point either
+ * way); the continuous-pressure ids 8-10 are per-vertex ring solves
+ * (unsupported here); the cube ids 11-12 leave tets untouched; any id above
+ * 12 runs MixedSel (XPBDFEM/Fem.cpp:885-887). */
+#define ORC_ENERGY_PIXAR 0u
+#define ORC_ENERGY_PIXAR_REDUCED 1u
+#define ORC_ENERGY_PIXAR_SEL 2u
+#define ORC_ENERGY_MIXED 3u
 #define ORC_ENERGY_MIXED_SEL 4u
+#define ORC_ENERGY_YEOH_SKIN 5u
+#define ORC_ENERGY_YEOH_SKIN_SEL 6u
 #define ORC_ENERGY_YEOH_SKIN_FAST 7u
+#define ORC_ENERGY_CONTINUOUS_PIXAR 8u
+#define ORC_ENERGY_CONTINUOUS_SKIN 10u
+#define ORC_ENERGY_CUBE_NEO 11u
+#define ORC_ENERGY_CUBE_SKIN 12u
 
 /* Element parameter record, 17 values per tet, the reference's
  * ElementParamsLinearTet (XPBDFEM/Fem.h:52-60) flattened:
@@ -63,6 +77,7 @@ typedef struct orc_params {
 	float pbd_coeff;           /* Settings::volumeAndTimeCorrectedPbdDamping */
 	float pbd_coeff_amortized; /* Settings::amortizedVolumeAndTimeCorrectedPbdDamping */
 	uint32_t tick;             /* Settings::tickId of the first substep; +1 per substep */
+	uint32_t volume_passes;    /* Settings::volumePasses: SolveElementVolume sweeps after the solve */
 } orc_params;
 
 /* ---- mesh ---------------------------------------------------------------- */
@@ -88,8 +103,9 @@ void orc_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* tets, uint
 /* X: 4x3 doubles, updated in place. O (nullable): the substep's start
  * positions, which the in-solve Rayleigh damping (types 0, 1) reads; without
  * O there is no damping term. mu_override <= 0 uses 1/compliance.
- * lambda_out (nullable) receives the two multipliers. Returns 0 or -1 for an
- * unsupported energy model. */
+ * lambda_out (nullable) receives the two multipliers (the single-constraint
+ * Pixar models: the one multiplier and 0). Returns 0 or -1 for an
+ * unsupported energy model (the continuous-pressure ids 8-10). */
 int orc_solve_tet_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p,
                     float mu_override, float* lambda_out);
 int orc_solve_tet_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p,
@@ -113,7 +129,7 @@ int orc_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* 
                    uint8_t* contact, double* lambdas);
 /* Same schedule, colours run with `threads` POSIX threads (tets of one colour
  * share no vertex, so the result equals the sequential run bit for bit).
- * Undamped settings only (returns -1 when damping or pbd_damping > 0).
+ * Undamped settings without volume passes only (returns -1 otherwise).
  * colour_begin[ncolours+1] delimits colours inside `order`. */
 int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask,
                             uint32_t nt, const uint32_t* tets, const float* ep, const float* tet_mu,

@@ -8,7 +8,9 @@ manifest.json with the parameters. Needs the reference tree, so it runs in the
 development container only; the fixtures are committed and the tests read
 them without the reference.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every case
+    python tests/golden/make_golden.py NAME ...   # only these cases (the
+                                                  # manifest keeps the others)
 """
 import json
 import os
@@ -74,6 +76,51 @@ CASES = [
                                               -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05]),
     ("damped_wonky_nh_serial_limit_pbd_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
                                                -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 1, 0.05]),
+    # the other energy models of SolveElement on linear tets (XPBDFEM/Fem.cpp:
+    # 872-888): Pixar (0), PixarReduced (1), PixarSel (2), Mixed (3), YeohSkin
+    # (5), YeohSkinSel (6), the cube models (11: no-op on tets), an id above
+    # 12 (MixedSel)
+    ("solve_pixar_nu045", ["solve", 21, 64, 0, 1, 0.01, 0.45, DT]),
+    ("solve_pixar_reduced_nu040", ["solve", 22, 64, 1, 0, 0.02, 0.40, DT]),
+    ("solve_pixarsel_nu049", ["solve", 23, 64, 2, 1, 0.01, 0.49, DT]),
+    ("solve_mixed_sim_nu045", ["solve", 24, 64, 3, 1, 0.01, 0.45, DT]),
+    ("solve_mixed_sim_incompressible", ["solve", 25, 64, 3, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("solve_mixed_serial_nu049", ["solve", 26, 64, 3, 0, 0.01, 0.49, DT]),
+    ("solve_yeohskin_sim_nu045", ["solve", 27, 64, 5, 1, 0.5, 0.45, DT]),
+    ("solve_yeohskin_sim_incompressible", ["solve", 28, 64, 5, 1, 3.2, 0.5, DT]),
+    ("solve_yeohskinsel_serial_nu049", ["solve", 29, 64, 6, 0, 0.5, 0.49, DT]),
+    ("solve_cube_neo_noop", ["solve", 30, 16, 11, 1, 0.01, 0.45, DT]),
+    ("solve_id20_mixedsel", ["solve", 31, 64, 20, 1, 0.01, 0.45, DT]),
+    # whole substeps in the GPU's colour order with those models (the `damped`
+    # command, damping 0 where none is wanted); trailing arg: volume passes
+    ("model_c1_pixar_nu045_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("model_c1_pixarsel_nu045_tet", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 2, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                     0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("model_c1_mixed_nu045_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 3, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("model_wonky_mixed_serial_nu045_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 3, 0, 1e-3, 0.45,
+                                             -2.0, -9.81, DT, 10, 1, 0.0, 0.0, 0.0, 2, 0.05]),
+    ("model_c1_yeohskin_nu049_tet", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 5, 1, 3.2e-4, 0.49,
+                                     0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("model_wonky_yeohskinsel_serial_nu049_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 6, 0, 0.5,
+                                                   0.49, -2.0, -9.81, DT, 10, 1, 0.0, 0.0, 0.0, 2, 0.05]),
+    ("model_c1_cube_pbd_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 11, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 20, 1, 0.01, 0.03, 0.0, 2, 0.1]),
+    ("model_c1_pixar_amortized_pbd_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5,
+                                           0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("model_c1_pixar_paper_tet", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                  0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 0, 0.1]),
+    ("model_c1_mixed_limit_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 3, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("model_wonky_yeohskin_serial_post_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 5, 0, 0.5, 0.45,
+                                               -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
+    ("volume_c1_nh_nu045_2_star", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 2]),
+    ("volume_c1_yeoh_nu049_3_tet", ["damped", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.49,
+                                    0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 3]),
+    ("volume_wonky_pixar_1_post_pbd_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
+                                            -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
 ]
 
 
@@ -93,8 +140,18 @@ def parse(blob):
 
 def main():
     subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    only = set(sys.argv[1:])
+    unknown = only - {n for n, _ in CASES}
+    if unknown:
+        sys.exit(f"unknown cases: {sorted(unknown)}")
     manifest = {}
+    mpath = os.path.join(HERE, "manifest.json")
+    if only and os.path.exists(mpath):
+        with open(mpath) as f:
+            manifest = json.load(f)
     for name, args in CASES:
+        if only and name not in only:
+            continue
         argv = [REFGEN] + [str(a) for a in args]
         stdin = None
         extra = {}
@@ -117,7 +174,8 @@ def main():
         if args[0] in ("ordered", "damped"):
             manifest[name]["schedule_mode"] = manifest_mode
         print(f"{name}: " + ", ".join(f"{k}{list(v.shape)}" for k, v in arrays.items()))
-    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+    manifest = {n: manifest[n] for n, _ in CASES if n in manifest}
+    with open(mpath, "w") as f:
         json.dump(manifest, f, indent=1)
 
 

@@ -8,7 +8,9 @@ masses (XPBDFEM/Fem.cpp:196-224, XPBDFEM/Geo.cpp:697-745), the MINSTD order
 XPBDFEM/Xpbd.h:87-215), whole substeps (XPBDFEM/Geo.cpp:305-356), and
 substeps with damping: the in-solve Rayleigh terms (XPBDFEM/Xpbd.h:87-205),
 GeoLinear3d::Damp with DampElement and PbdDamp (XPBDFEM/Geo.cpp:346-355,
-790-811; XPBDFEM/Fem.cpp:908-931; XPBDFEM/Xpbd.h:217-346), amortized or not.
+790-811; XPBDFEM/Fem.cpp:908-931; XPBDFEM/Xpbd.h:217-346), amortized or not;
+every energy model SolveElement dispatches on a linear tet
+(XPBDFEM/Fem.cpp:872-888), and volume passes (XPBDFEM/Fem.cpp:840-867).
 """
 import numpy as np
 import pytest
@@ -18,13 +20,26 @@ from conftest import golden, golden_args
 MESH = ["meshgen_8x2x2", "meshgen_3x2x2_mirror_wonky", "meshgen_4x3x2_aniso_wonky"]
 INIT = ["init_8x2x2", "init_3x2x2_mirror_wonky", "init_5x3x2_aniso_wonky"]
 SOLVE = ["solve_nh_sim_incompressible", "solve_nh_sim_nu045", "solve_yeoh_sim_incompressible",
-         "solve_nh_serial_nu045", "solve_yeoh_serial_nu049"]
+         "solve_nh_serial_nu045", "solve_yeoh_serial_nu049",
+         # the other energy models (XPBDFEM/Fem.cpp:361-433, 459-522, 872-888)
+         "solve_pixar_nu045", "solve_pixar_reduced_nu040", "solve_pixarsel_nu049", "solve_mixed_sim_nu045",
+         "solve_mixed_sim_incompressible", "solve_mixed_serial_nu049", "solve_yeohskin_sim_nu045",
+         "solve_yeohskin_sim_incompressible", "solve_yeohskinsel_serial_nu049", "solve_cube_neo_noop",
+         "solve_id20_mixedsel"]
 SUBSTEP = ["substep_c1_nh_native", "substep_c1_yeoh_native", "substep_wonky_nh_serial_native",
            "ordered_c1_nh_star", "ordered_c1_yeoh_tet", "ordered_c1_nh_nu045_star", "ordered_c1_yeoh_nu049_tet",
            "ordered_wonky_nh_serial_nu045_star"]
 DAMPED = ["damped_c1_nh_nu045_amortized_pbd_star", "damped_c1_nh_nu045_post_star", "damped_c1_nh_nu045_paper_star",
           "damped_c1_nh_nu045_limit_star", "damped_c1_yeoh_nu049_amortized_pbd_tet",
           "damped_wonky_nh_serial_post_pbd_star", "damped_wonky_nh_serial_limit_pbd_star"]
+# energy models other than MixedSel / YeohSkinFast, and volume passes
+# (SolveElementVolume, XPBDFEM/Fem.cpp:840-867; XPBDFEM/Geo.cpp:780-783), in
+# the `damped` form (damping 0 where none is wanted)
+MODELS = ["model_c1_pixar_nu045_star", "model_c1_pixarsel_nu045_tet", "model_c1_mixed_nu045_star",
+          "model_wonky_mixed_serial_nu045_star", "model_c1_yeohskin_nu049_tet",
+          "model_wonky_yeohskinsel_serial_nu049_star", "model_c1_cube_pbd_star", "model_c1_pixar_amortized_pbd_star",
+          "model_c1_pixar_paper_tet", "model_c1_mixed_limit_star", "model_wonky_yeohskin_serial_post_star",
+          "volume_c1_nh_nu045_2_star", "volume_c1_yeoh_nu049_3_tet", "volume_wonky_pixar_1_post_pbd_star"]
 
 
 @pytest.mark.parametrize("name", MESH)
@@ -92,14 +107,15 @@ def test_substeps_bit_exact(orc, name):
 def damped_params(orc, a, derived, tick):
     """orc_params of a `damped` fixture (refgen's argument order)."""
     W, H, D, sx, sy, sz, wonk, dens, energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[1:18]
-    damping, pbd, drag, rtype, spacing = a[18:]
+    damping, pbd, drag, rtype, spacing = a[18:23]
+    vpasses = a[23] if len(a) > 23 else 0
     return orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
                            gravity=(gx, gy, 0.0), lock=bool(lock), drag=float(derived[2]), damping=damping,
                            rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(derived[0]),
-                           pbd_coeff_amortized=float(derived[1]), tick=tick)
+                           pbd_coeff_amortized=float(derived[1]), tick=tick, volume_passes=vpasses)
 
 
-@pytest.mark.parametrize("name", DAMPED)
+@pytest.mark.parametrize("name", DAMPED + MODELS)
 def test_damped_substeps_bit_exact(orc, name):
     g = golden(name)
     a = golden_args(name)["args"]
@@ -118,8 +134,31 @@ def test_damped_substeps_bit_exact(orc, name):
                                 lock_mask=lock_mask)
     assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
-    # the damping did something: the undamped run differs
+    # the damping, the model and the volume passes each did something: the
+    # run without them differs
     p0 = damped_params(orc, a, g["derived"], 0)
-    p0.damping, p0.pbd_damping = 0.0, 0.0
+    if p0.damping > 0 or p0.pbd_damping > 0:
+        p0.damping, p0.pbd_damping = 0.0, 0.0
+    elif p0.volume_passes:
+        p0.volume_passes = 0
+    else:
+        p0.energy = orc.ENERGY_MIXED_SEL
     Xu, _, _, _ = orc.substeps(X0, V0, w, tets, ep, order, nsub, p0, lock_mask=lock_mask)
     assert not np.array_equal(Xu.reshape(-1), g["xn"])
+
+
+def test_cube_models_leave_tets_untouched(orc):
+    """SolveElementCube acts on quads and hexes only: on a tet mesh the
+    substep is free fall (XPBDFEM/Fem.cpp:568-838)."""
+    g = golden("solve_cube_neo_noop")
+    assert np.array_equal(g["xin"], g["xout"])
+
+
+def test_continuous_models_refused(orc):
+    """The continuous-pressure models (8-10) run a per-vertex ring solve,
+    not an element solve: the element restatement refuses them."""
+    g = golden("solve_pixar_nu045")
+    for e in (8, 9, 10):
+        p = orc.make_params(dt=1 / 1200, compliance=0.01, poisson=0.45, energy=e)
+        with pytest.raises(ValueError):
+            orc.solve_tet(g["xin"][:12], g["w"][:4], g["ep"][:17], p)
