@@ -51,8 +51,20 @@ extern "C" {
 /* ---- flags: the reference's Settings::flags layout (XPBDFEM/Settings.h:9-29) - */
 #define XFEM_ENERGY_BIT 6u
 #define XFEM_ENERGY_MASK 31u
+/* Energy ids (XPBDFEM/Settings.h:41-53) as SolveElement dispatches them on a
+ * linear tet (XPBDFEM/Fem.cpp:872-888); ids above 12 run MixedSel. */
+#define XFEM_ENERGY_PIXAR 0u           /* Energy_Pixar: Stable Neo-Hookean, one constraint */
+#define XFEM_ENERGY_PIXAR_REDUCED 1u   /* Energy_PixarReduced (= Pixar on a linear tet) */
+#define XFEM_ENERGY_PIXAR_SEL 2u       /* Energy_PixarSel */
+#define XFEM_ENERGY_MIXED 3u           /* Energy_Mixed: Neo-Hookean, I1 by quadrature */
 #define XFEM_ENERGY_MIXED_SEL 4u       /* Energy_MixedSel: Neo-Hookean, prefactored I1 */
+#define XFEM_ENERGY_YEOH_SKIN 5u       /* Energy_YeohSkin */
+#define XFEM_ENERGY_YEOH_SKIN_SEL 6u   /* Energy_YeohSkinSel (= YeohSkin on a linear tet) */
 #define XFEM_ENERGY_YEOH_SKIN_FAST 7u  /* Energy_YeohSkinFast */
+                                       /* 8-10: continuous-pressure models, XFEM_EUNSUPPORTED */
+#define XFEM_ENERGY_CUBE_NEO 11u       /* Energy_CubeNeo: acts on quads and hexes, so on no tet */
+#define XFEM_ENERGY_CUBE_SKIN 12u      /* Energy_CubeSkin: likewise */
+#define XFEM_MAX_VOLUME_PASSES 64u     /* largest xfem_settings::volume_passes accepted */
 #define XFEM_XPBD_SOLVE_BIT 11u        /* set: coupled 2x2 solve; clear: serial */
 #define XFEM_RAYLEIGH_TYPE_BIT 20u     /* Settings_RayleighTypeBit, mask 3: */
 #define XFEM_RAYLEIGH_PAPER 0u         /*   damping inside the solve (Rayleigh_Paper) */
@@ -67,7 +79,7 @@ extern "C" {
 typedef struct xfem_settings {
 	float time_scale;            /* unused by the solver (the caller picks dt) */
 	float substeps_per_second;   /* unused by the solver */
-	uint32_t volume_passes;      /* must be 0 (extra volume passes not built) */
+	uint32_t volume_passes;      /* SolveElementVolume sweeps after each solve sweep (<= 64) */
 	float gravity[3];            /* reference: vec2 (x, y) */
 	float compliance;            /* 1 / mu_ref */
 	float damping;               /* Rayleigh damping ratio (type in flags bits 20-21) */

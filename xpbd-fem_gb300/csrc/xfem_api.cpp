@@ -122,12 +122,37 @@ struct xfem_body {
 
 namespace {
 
+// How the solve treats an energy id on linear tets (TSolveElement's
+// dispatch, XPBDFEM/Fem.cpp:872-888); kModelNone + 1 for the
+// continuous-pressure ids 8-10, which run a per-vertex ring solve.
+uint32_t model_of(uint32_t energy) {
+	switch (energy) {
+	case XFEM_ENERGY_PIXAR:
+	case XFEM_ENERGY_PIXAR_REDUCED:
+	case XFEM_ENERGY_PIXAR_SEL: return kModelPixar;
+	case XFEM_ENERGY_MIXED: return kModelNeoClamp;
+	case XFEM_ENERGY_YEOH_SKIN:
+	case XFEM_ENERGY_YEOH_SKIN_SEL:
+	case XFEM_ENERGY_YEOH_SKIN_FAST: return kModelYeoh;
+	case XFEM_ENERGY_CUBE_NEO:
+	case XFEM_ENERGY_CUBE_SKIN: return kModelNone;
+	case 8u:
+	case 9u:
+	case 10u: return kModelNone + 1u;
+	default: return kModelNeo;  // MixedSel, and every id above 12
+	}
+}
+
 int validate_settings(const xfem_settings& s) {
 	const uint32_t energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (energy != XFEM_ENERGY_MIXED_SEL && energy != XFEM_ENERGY_YEOH_SKIN_FAST)
+	const uint32_t model = model_of(energy);
+	if (model > kModelNone)
 		return fail(XFEM_EUNSUPPORTED, "energy model " + std::to_string(energy) +
-		                                   " not supported (MixedSel = 4 and YeohSkinFast = 7 are)");
-	if (s.volume_passes != 0) return fail(XFEM_EUNSUPPORTED, "volume_passes must be 0");
+		                                   " (continuous pressure: a per-vertex ring solve) is not supported");
+	if (s.volume_passes > XFEM_MAX_VOLUME_PASSES)
+		return fail(XFEM_EINVAL, "volume_passes must be at most " + std::to_string(XFEM_MAX_VOLUME_PASSES));
+	if (model == kModelPixar && !(s.poissons_ratio < 0.5f))
+		return fail(XFEM_EINVAL, "the Pixar models need poissons_ratio < 0.5 (lambda = 2 / (1 - 2 nu))");
 	if (!(s.damping >= 0.0f) || !(s.pbd_damping >= 0.0f)) return fail(XFEM_EINVAL, "damping and pbd_damping must be >= 0");
 	if (s.flags & (1u << 27)) return fail(XFEM_EUNSUPPORTED, "Settings_LockRight is not supported");
 	if (!(s.compliance > 0.0f)) return fail(XFEM_EINVAL, "compliance must be > 0");
@@ -150,6 +175,16 @@ BodyParams make_params(const xfem_settings& s) {
 	p.ratio = mu * p.inv_lambda;
 	for (int k = 0; k < 3; k++) p.yeoh[k] = s.yeoh[k];
 	p.energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+	p.model = model_of(p.energy);
+	if (p.model == kModelPixar) {
+		// SolveElementPixar's own material (XPBDFEM/Fem.cpp:367-368): mu = 2
+		const float lp = 2.0f / (1.0f - 2.0f * nu);
+		p.a = 1.0f + 2.0f / lp;
+		p.hw = lp / 2.0f;
+		p.ratio = 0.0f;
+	}
+	p.volume_passes = s.volume_passes;
+	p.compliance = s.compliance;
 	p.simultaneous = (s.flags >> XFEM_XPBD_SOLVE_BIT) & 1u;
 	for (int k = 0; k < 3; k++) p.gravity[k] = s.gravity[k];
 	p.drag_mul = 1.0f - s.time_corrected_drag;
@@ -166,11 +201,24 @@ BodyParams make_params(const xfem_settings& s) {
 	return p;
 }
 
-// Whether any body damps, in the solve (Paper, Limit) or after it.
-bool damp_any_of(const std::vector<BodyHost>& bodies) {
-	for (const BodyHost& b : bodies)
-		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f) return true;
+// Whether any body needs the extended kernels: it damps (in the solve or
+// after it), runs Mixed (its clamp), a Pixar or a cube model, or runs volume
+// passes.
+bool ext_any_of(const std::vector<BodyHost>& bodies) {
+	for (const BodyHost& b : bodies) {
+		const uint32_t model = model_of((b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK);
+		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f || model == kModelNeoClamp ||
+		    model >= kModelPixar || b.settings.volume_passes)
+			return true;
+	}
 	return false;
+}
+
+// Volume sweeps per substep: the most that any body runs.
+uint32_t nvol_of(const std::vector<BodyHost>& bodies) {
+	uint32_t n = 0;
+	for (const BodyHost& b : bodies) n = std::max(n, b.settings.volume_passes);
+	return n;
 }
 
 // Damping sweeps the handle runs after each solve sweep: bit 0 element
@@ -508,7 +556,7 @@ int build_device(xfem_body* h) {
 	if (h->tlam.p) XCUDA(cudaMemsetAsync(h->tlam.p, 0, h->tlam.n * sizeof(float2), h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + isolated.size() + dev_of.size() +
-	                  tets_dev.size() + dep_begin.size() + deps.size() + nch) * 4 + meta.size() * 16 + params.size() * 64 + h->stage.n * 4 + h->tlam.n * 8;
+	                  tets_dev.size() + dep_begin.size() + deps.size() + nch) * 4 + meta.size() * 16 + params.size() * sizeof(BodyParams) + h->stage.n * 4 + h->tlam.n * 8;
 	{
 		std::vector<uint32_t> rec(ntets), slot(ntets);
 		std::vector<float> vol(ntets), inv_mu(ntets);
@@ -576,7 +624,8 @@ int build_device(xfem_body* h) {
 	c.chunks = h->chunks.p;
 	c.ntrows = trows;
 	c.damp_kinds = damp_kinds_of(h->bodies);
-	c.damp_any = damp_any_of(h->bodies) ? 1u : 0u;
+	c.ext = ext_any_of(h->bodies) ? 1u : 0u;
+	c.nvol = nvol_of(h->bodies);
 	c.lastmask = h->lastmask.p;
 	c.pass_on = h->pass_on.p;
 	c.tick = h->tick.p;
@@ -595,7 +644,7 @@ int build_device(xfem_body* h) {
 	c.bar_count = h->bar.p;
 	c.err = h->err.p;
 	h->cfg.lambdas = h->opt.keep_lambdas != 0;
-	h->cfg.damp = c.damp_any != 0u;
+	h->cfg.ext = c.ext != 0u;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -665,15 +714,15 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	const int blocks[] = {64, 128, 192, 224, 256};
 	for (int sm : {1, 2, 3}) {
 		if (fixed_sync && sm != fixed_sync) continue;
-		if (sm == 3 && h->ctx.damp_any) continue;  // the dataflow kernel runs no damping
+		if (sm == 3 && h->ctx.ext) continue;  // the dataflow kernel runs only the plain solve
 		for (int bs : blocks) {
 			if (fixed_block && bs != fixed_block) continue;
 			cand.push_back({sm, bs});
 		}
 	}
-	if (fixed_sync == 3 && h->ctx.damp_any) {
+	if (fixed_sync == 3 && h->ctx.ext) {
 		h->tuned = false;
-		return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping");
+		return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping, Pixar or cube models or volume passes");
 	}
 	if (fixed_block && cand.empty()) cand.push_back({fixed_sync ? fixed_sync : 1, fixed_block});
 	if (cand.empty()) {
@@ -772,9 +821,11 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 	XCUDA(cudaSetDevice(h->device));
 	int rc = autotune(h, nsub, dt);
 	if (rc) return rc;
-	if (h->ctx.damp_any && h->cfg.sync_mode == 3) {
-		// damping switched on after the dataflow kernel was chosen
-		if (h->opt.sync_mode == 3) return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping");
+	if (h->ctx.ext && h->cfg.sync_mode == 3) {
+		// damping, a Pixar or cube model or volume passes switched on after
+		// the dataflow kernel was chosen
+		if (h->opt.sync_mode == 3)
+			return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping, Pixar or cube models or volume passes");
 		rc = set_config(h, 1, h->cfg.block);
 		if (rc) return rc;
 	}
@@ -907,11 +958,13 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	XCUDA(cudaMemcpyAsync(h->pass_on.p, pt.data(), pt.size(), cudaMemcpyHostToDevice, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	const uint32_t kinds = damp_kinds_of(h->bodies);
-	const bool damp = damp_any_of(h->bodies);
-	if (kinds != h->ctx.damp_kinds || damp != h->cfg.damp) {
+	const bool ext = ext_any_of(h->bodies);
+	const uint32_t nvol = nvol_of(h->bodies);
+	if (kinds != h->ctx.damp_kinds || ext != h->cfg.ext || nvol != h->ctx.nvol) {
 		h->ctx.damp_kinds = kinds;
-		h->ctx.damp_any = damp ? 1u : 0u;
-		h->cfg.damp = damp;
+		h->ctx.ext = ext ? 1u : 0u;
+		h->ctx.nvol = nvol;
+		h->cfg.ext = ext;
 		if (h->graph) {  // the captured launches follow the old sweeps
 			cudaGraphExecDestroy(h->graph);
 			h->graph = nullptr;
@@ -1190,8 +1243,10 @@ int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpo
 	if (ntips && !tips) return fail(XFEM_EINVAL, "null tips");
 	for (const BodyHost& b : h->bodies) {
 		const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-		if (energy != XFEM_ENERGY_MIXED_SEL || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))
+		if (model_of(energy) != kModelNeo || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))
 			return fail(XFEM_EUNSUPPORTED, "the adjoint covers the coupled Neo-Hookean model only (energy 4, XPBD solve bit)");
+		if (b.settings.volume_passes)
+			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate volume passes (volume_passes must be 0)");
 		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f)
 			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate damping (damping, pbd_damping must be 0)");
 	}

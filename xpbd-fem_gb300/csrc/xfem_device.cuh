@@ -142,18 +142,24 @@ struct TetRec {
 };
 
 // The material scalars a solve needs, copied to registers once per cluster.
+// Fields that a kernel instantiation does not read are never loaded.
 struct Mat {
 	float a, ratio, y0, y1, y2;
-	uint32_t energy, simultaneous;
-	float damp;      // in-solve Rayleigh ratio: damping for types 0, 1, else 0
-	uint32_t limit;  // 1 = Rayleigh_Limit, 0 = Rayleigh_Paper
+	uint32_t model, simultaneous;
+	float damp;        // in-solve Rayleigh ratio: damping for types 0, 1, else 0
+	uint32_t limit;    // 1 = Rayleigh_Limit, 0 = Rayleigh_Paper
+	float hw;          // Pixar models: lambda / 2
+	float compliance;  // volume passes
+	uint32_t nvol;     // volume passes of the body
 };
 
 __device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body) {
 	const BodyParams* b = bodies + body;
 	const uint32_t type = __ldg(&b->rayleigh_type);
-	return {__ldg(&b->a), __ldg(&b->ratio), __ldg(&b->yeoh[0]), __ldg(&b->yeoh[1]), __ldg(&b->yeoh[2]),
-	        __ldg(&b->energy), __ldg(&b->simultaneous), type < 2u ? __ldg(&b->damping) : 0.0f, type == 1u ? 1u : 0u};
+	return {__ldg(&b->a),          __ldg(&b->ratio),        __ldg(&b->yeoh[0]),
+	        __ldg(&b->yeoh[1]),    __ldg(&b->yeoh[2]),      __ldg(&b->model),
+	        __ldg(&b->simultaneous), type < 2u ? __ldg(&b->damping) : 0.0f, type == 1u ? 1u : 0u,
+	        __ldg(&b->hw),         __ldg(&b->compliance),   __ldg(&b->volume_passes)};
 }
 
 // Hydrostatic term at the single point (XPBDFEM/Fem.cpp:539-549 with the
@@ -206,10 +212,8 @@ __device__ __forceinline__ float rcp(float x) {
 	return fmaf(r, fmaf(-x, r, 1.0f), r);
 }
 
-// Deviatoric term, prefactored (XPBDFEM/Fem.cpp:163-192), with the Yeoh
-// transform of XPBDFEM/Fem.cpp:525-531 when energy == 7.
-__device__ __forceinline__ float deviatoric(const Mat& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
-                                            Vec3 g[4]) {
+// I1 and its gradient, prefactored (XPBDFEM/Fem.cpp:163-192).
+__device__ __forceinline__ float prefactored_i1(const float QQ[3], const float QR[3], const Vec3 P[3], Vec3 g[4]) {
 	float U = QQ[0] * dot(P[0], P[0]);
 	U = fmaf(QQ[1], dot(P[1], P[1]), U);
 	U = fmaf(QQ[2], dot(P[2], P[2]), U);
@@ -224,7 +228,19 @@ __device__ __forceinline__ float deviatoric(const Mat& bp, const float QQ[3], co
 	g[2] = {fmaf(d2, P[2].x, fmaf(QR[1], P[0].x, QR[2] * P[1].x)), fmaf(d2, P[2].y, fmaf(QR[1], P[0].y, QR[2] * P[1].y)),
 	        fmaf(d2, P[2].z, fmaf(QR[1], P[0].z, QR[2] * P[1].z))};
 	g[3] = {-(g[0].x + g[1].x + g[2].x), -(g[0].y + g[1].y + g[2].y), -(g[0].z + g[1].z + g[2].z)};
-	if (bp.energy == 7u) {
+	return U;
+}
+
+// Deviatoric term of SolveElementMixed: I1 (MixedSel; Mixed with the clamp
+// of XPBDFEM/Fem.cpp:489) or the Yeoh polynomial of I1 - 3 with its clamp
+// (YeohSkin, YeohSkinSel: XPBDFEM/Fem.cpp:467-476, 489; YeohSkinFast:
+// XPBDFEM/Fem.cpp:525-531). Mixed runs in the extended kernels only (EXT).
+template <bool EXT = false>
+__device__ __forceinline__ float deviatoric(const Mat& bp, const float QQ[3], const float QR[3], const Vec3 P[3],
+                                            Vec3 g[4]) {
+	float U = prefactored_i1(QQ, QR, P, g);
+	if (EXT && bp.model == kModelNeoClamp) U = fmaxf(0.0001f, U);
+	if (bp.model == kModelYeoh) {
 		const float IM = U - 3.0f;
 		const float C0 = bp.y0, C1 = bp.y1, C2 = bp.y2;
 		U = fmaxf(0.0001f, IM * fmaf(IM, fmaf(IM, C2, C1), C0));
@@ -271,29 +287,81 @@ __device__ __forceinline__ float serial_lambda(const Mat& bp, float U, const Vec
 	return l + b / A;
 }
 
-// One element solve: SolveElementMixed<MixedSelective | YeohSkinFast> tet path
-// (XPBDFEM/Fem.cpp:437-564) with EnergyXpbdConstrainSimultaneous<2>
-// (XPBDFEM/Xpbd.h:123-215) or the serial EnergyXpbdConstrain pair
-// (XPBDFEM/Xpbd.h:87-121), with the in-solve Rayleigh damping (Paper, Limit)
-// compiled in when DAMP. O[]: start positions + w, D[]: displacements
-// (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
+// The Pixar models' energy and gradient (XPBDFEM/Fem.cpp:361-427), mu = 2:
+// U = I1 + hw (J - a)^2, g = dI1 + hw d(J - a)^2 in g; scratch: h.
+__device__ __forceinline__ float pixar_energy(const Mat& bp, const float q[3][3], const float QQ[3], const float QR[3],
+                                              const Vec3 P[3], Vec3 g[4], Vec3 h[4]) {
+	const float U1 = hydrostatic(q, P, bp.a, h);
+	const float U = fmaf(bp.hw, U1, prefactored_i1(QQ, QR, P, g));
+#pragma unroll
+	for (int n = 0; n < 4; n++) g[n] = {fmaf(bp.hw, h[n].x, g[n].x), fmaf(bp.hw, h[n].y, g[n].y), fmaf(bp.hw, h[n].z, g[n].z)};
+	return U;
+}
+
+// One volume-pass solve, SolveVolumeOnly (XPBDFEM/Fem.cpp:840-867): U =
+// (J - 1)^2, one constraint of compliance Settings::compliance times the
+// rest volume 1 / (6 det Qi), no damping.
+__device__ __forceinline__ void volume_tet(const Mat& bp, const TetRec& r, float inv_dt2, const float4 O[4], float4 D[4]) {
+	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
+	const float w[4] = {O[0].w, O[1].w, O[2].w, O[3].w};
+	Vec3 P[3], g[4];
+#pragma unroll
+	for (int i = 0; i < 3; i++)
+		P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+		        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+	float detq;
+	const float U = hydrostatic(q, P, 1.0f, g, nullptr, &detq);
+	const float alpha = bp.compliance * inv_dt2 / (6.0f * detq);
+	const float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wdot(w, g, g));
+#pragma unroll
+	for (int n = 0; n < 4; n++) {
+		const float s = w[n] * l;
+		D[n].x = fmaf(s, g[n].x, D[n].x);
+		D[n].y = fmaf(s, g[n].y, D[n].y);
+		D[n].z = fmaf(s, g[n].z, D[n].z);
+	}
+}
+
+// One element solve: SolveElementMixed's tet path (XPBDFEM/Fem.cpp:437-564)
+// with EnergyXpbdConstrainSimultaneous<2> (XPBDFEM/Xpbd.h:123-215) or the
+// serial EnergyXpbdConstrain pair (XPBDFEM/Xpbd.h:87-121). EXT (the extended
+// kernels) adds the in-solve Rayleigh damping (Paper, Limit), Mixed's clamp,
+// the Pixar models (one constraint) and the cube models (no constraint on a
+// tet). O[]: start positions + w, D[]: displacements (updated). alpha0 = c0 / dt^2 with c0 = (1/mu)/volume stored per tet;
 // alpha1 = alpha0 * (mu / lambda), i.e. (1/lambda)/volume/dt^2.
-template <bool DAMP = false>
+template <bool EXT = false>
 __device__ __forceinline__ float2 solve_tet(const Mat& bp, const TetRec& r, float inv_dt, float inv_dt2,
                                             const float4 O[4], float4 D[4]) {
+	constexpr bool DAMP = EXT;
 	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
 	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
 	const float QR[3] = {r.d.x, r.d.y, r.d.z};
 	const float alpha0 = r.d.w * inv_dt2;
 	const float alpha1 = alpha0 * bp.ratio;
 	const float w[4] = {O[0].w, O[1].w, O[2].w, O[3].w};
+	if (EXT && bp.model == kModelNone) return make_float2(0.0f, 0.0f);
 	Vec3 P[3];
 #pragma unroll
 	for (int i = 0; i < 3; i++)
 		P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
 		        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
 	Vec3 g0[4], g1[4];
-	const float U0 = deviatoric(bp, QQ, QR, P, g0);
+	if (EXT && bp.model == kModelPixar) {
+		// SolveElementPixar (XPBDFEM/Fem.cpp:361-433): U = I1 + (lambda/2)
+		// (J - a)^2 (mu / 2 = 1) as one EnergyXpbdConstrain with the
+		// compliance per volume c0
+		const float U = pixar_energy(bp, q, QQ, QR, P, g0, g1);
+		const float l = serial_lambda<true>(bp, U, g0, w, D, alpha0, r.d.w, inv_dt);
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l;
+			D[n].x = fmaf(s, g0[n].x, D[n].x);
+			D[n].y = fmaf(s, g0[n].y, D[n].y);
+			D[n].z = fmaf(s, g0[n].z, D[n].z);
+		}
+		return make_float2(l, 0.0f);
+	}
+	const float U0 = deviatoric<EXT>(bp, QQ, QR, P, g0);
 	float l0, l1;
 	if (bp.simultaneous) {
 		const float U1 = hydrostatic(q, P, bp.a, g1);

@@ -52,8 +52,9 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 // Material and step parameters of one body (uploaded on create / set_settings).
 struct BodyParams {
 	float mu, inv_mu, inv_lambda, a;  // mu = 1/compliance; inv_* = 1/mu, 1/lambda; a = 1 + mu/lambda
+	                                  // (Pixar models: a = 1 + 2/lambda with lambda = 2/(1 - 2 nu))
 	float yeoh[3];
-	uint32_t energy;        // 4 = Neo-Hookean (MixedSel), 7 = Yeoh (YeohSkinFast)
+	uint32_t energy;        // the reference's energy id (flags bits 6-10)
 	float gravity[3];
 	float drag_mul;         // 1 - time_corrected_drag
 	uint32_t simultaneous;  // 1 = coupled 2x2 solve
@@ -63,7 +64,7 @@ struct BodyParams {
 	float ground_n[3];
 	float ground_d;
 	float ratio;   // mu / lambda (0 when incompressible)
-	uint32_t pad;
+	uint32_t model;  // kModel*: how the solve treats the energy id
 	// damping (XPBDFEM/Geo.cpp:346-355, 790-811; XPBDFEM/Xpbd.h:87-346)
 	float damping;            // Rayleigh ratio (0 = off)
 	uint32_t rayleigh_type;   // 0 Paper, 1 Limit (in the solve), 2 Post, 3 PostAmortized
@@ -71,8 +72,24 @@ struct BodyParams {
 	float pbd_coeff;          // volume- and time-corrected PBD damping
 	float pbd_coeff_amortized;
 	uint32_t ntets;           // tets of the body (amortized slices)
-	uint32_t pad2[2];
+	uint32_t volume_passes;   // Settings::volumePasses: SolveElementVolume sweeps after the solve
+	float hw;                 // Pixar models: lambda / 2, the weight of (J - a)^2
+	float compliance;         // Settings::compliance (the volume passes' compliance per volume)
+	uint32_t pad3;
 };
+
+// Energy models on linear tets, as the solve treats them (BodyParams::model).
+// With one quadrature point per tet, the quadrature forms of I1 (Mixed,
+// YeohSkin, YeohSkinSel, Pixar, PixarReduced; XPBDFEM/Fem.cpp:379-402,
+// 459-489) and the prefactored form (XPBDFEM/Fem.cpp:163-192) are the same
+// polynomial of the edge vectors: tr(F^T F) with F = Qi Ds equals
+// sum_ij (Qi^T Qi)_ij P_i . P_j, whose coefficients are QQ and QR. The
+// solve evaluates the prefactored form for all of them.
+constexpr uint32_t kModelNeo = 0;       // MixedSel (4), and ids above 12 (XPBDFEM/Fem.cpp:885-887)
+constexpr uint32_t kModelNeoClamp = 1;  // Mixed (3): U0 = I1 clamped at 1e-4 (XPBDFEM/Fem.cpp:489)
+constexpr uint32_t kModelYeoh = 2;      // YeohSkin (5), YeohSkinSel (6), YeohSkinFast (7)
+constexpr uint32_t kModelPixar = 3;     // Pixar (0), PixarReduced (1), PixarSel (2): one constraint
+constexpr uint32_t kModelNone = 4;      // CubeNeo (11), CubeSkin (12): no constraint on tets
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
@@ -127,13 +144,15 @@ struct DevCtx {
 	float4* tape_fin;           // [vertex]: D before the closing finalize
 	float4* traj;               // [run substep][tip]: position after each substep
 	const int32_t* tip_of;      // per vertex: tip index or -1
-	uint32_t ntrows, sub_base, ntips, pad_;
-	// Damping sweeps after each substep's solve sweep (0 = none: the state
-	// between substeps stays (O, D) and the next advance finishes it).
-	// Bit 0: element Rayleigh damping (Post types), bit 1: PBD damping.
+	uint32_t ntrows, sub_base, ntips;
+	uint32_t nvol;              // volume sweeps per substep (most of any body's volume_passes)
+	// Damping sweeps after each substep's solve and volume sweeps (0 = none:
+	// the state between substeps stays (O, D) and the next advance finishes
+	// it). Bit 0: element Rayleigh damping (Post types), bit 1: PBD damping.
 	uint32_t damp_kinds;
-	uint32_t damp_any;          // some body damps (in the solve or after it): the kernels
-	                            // with damping compiled in are launched
+	uint32_t ext;               // some body damps (in the solve or after it), runs a Pixar
+	                            // or cube model or volume passes: the extended kernels
+	                            // (EXT instantiations) are launched
 	uint32_t* tick;             // device word: Settings::tickId of the launch's first substep
 	const uint32_t* tflat;      // [tet row][lane]: the tet's index in its body's flattened order
 	const float* tarea;         // [tet row][lane]: the tet's surface area (rest state)
@@ -141,6 +160,8 @@ struct DevCtx {
 	                            // cluster makes (it finishes them when damping sweeps run)
 	const uint8_t* pass_on;     // [damping kind][tick % 8][colour]: some tet is damped
 };
+// A substep's passes, colour-major within each kind: the solve sweep (kind
+// 0), volume sweeps 1..nvol, then one sweep per damping kind.
 
 // Reverse-pass state (xfem_adjoint.cu).
 struct AdjCtx {
@@ -167,7 +188,7 @@ struct LaunchCfg {
 	int blocks = 0;        // persistent grid size
 	int sync_mode = 1;     // 1 persistent + grid barrier, 2 per-colour launches (CUDA graph), 3 persistent dataflow
 	bool lambdas = false;
-	bool damp = false;     // launch the instantiations with damping (DevCtx::damp_any)
+	bool ext = false;      // launch the extended instantiations (DevCtx::ext)
 	uint32_t warp_smem = 0;
 	uint32_t total_chunks = 0;
 	std::vector<uint32_t> colour_chunk_begin_host;

@@ -61,9 +61,11 @@ __device__ __forceinline__ void tape_tet(const DevCtx& C, uint32_t s, uint32_t r
 
 // DampElement (XPBDFEM/Fem.cpp:908-931): energies and gradients of the tet at
 // its current positions, then RayleighDamp (XPBDFEM/Xpbd.h:217-263) on its
-// velocities. damp: the Rayleigh ratio (x 8 when amortized).
+// velocities: one constraint for the Pixar models, the pair for the others,
+// nothing for the cube models. damp: the Rayleigh ratio (x 8 when amortized).
 __device__ __forceinline__ void rayleigh_tet(const Mat& bp, const TetRec& r, const float4 X[4], float4 V[4],
                                              float inv_dt, float damp) {
+	if (bp.model == kModelNone) return;  // SolveElementCube damps quads and hexes only
 	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
 	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
 	const float QR[3] = {r.d.x, r.d.y, r.d.z};
@@ -72,9 +74,25 @@ __device__ __forceinline__ void rayleigh_tet(const Mat& bp, const TetRec& r, con
 #pragma unroll
 	for (int i = 0; i < 3; i++) P[i] = {X[i].x - X[3].x, X[i].y - X[3].y, X[i].z - X[3].z};
 	Vec3 g0[4], g1[4];
-	const float U0 = deviatoric(bp, QQ, QR, P, g0);
-	const float U1 = hydrostatic(q, P, bp.a, g1);
 	const float ib0 = r.d.w * inv_dt / damp, ib1 = ib0 * bp.ratio;  // comp / (dt damping)
+	if (bp.model == kModelPixar) {
+		// SolveElementPixar with DampingMode::On (XPBDFEM/Fem.cpp:429-430): one constraint
+		const float U = pixar_energy(bp, q, QQ, QR, P, g0, g1);
+		float gV = 0.0f;
+#pragma unroll
+		for (int n = 0; n < 4; n++) gV = fmaf(g0[n].x, V[n].x, fmaf(g0[n].y, V[n].y, fmaf(g0[n].z, V[n].z, gV)));
+		const float l = -gV / fmaf(2.0f * U, ib0, wdot(w, g0, g0));
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			const float s = w[n] * l;
+			V[n].x = fmaf(s, g0[n].x, V[n].x);
+			V[n].y = fmaf(s, g0[n].y, V[n].y);
+			V[n].z = fmaf(s, g0[n].z, V[n].z);
+		}
+		return;
+	}
+	const float U0 = deviatoric<true>(bp, QQ, QR, P, g0);
+	const float U1 = hydrostatic(q, P, bp.a, g1);
 	if (bp.simultaneous) {
 		float b0 = 0.0f, b1 = 0.0f;
 #pragma unroll
@@ -197,7 +215,7 @@ __device__ __forceinline__ DampTet damp_of(const DevCtx& C, const BodyParams& bp
 // A vertex is advanced (previous substep finalized, next one predicted) by
 // the lowest-colour cluster touching it, just before that cluster's solve.
 
-template <bool LAMBDAS, bool TAPE, bool DAMP>
+template <bool LAMBDAS, bool TAPE, bool EXT>
 __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first, float dt,
                                                float inv_dt, float inv_dt2, uint32_t trow, uint32_t s_launch,
                                                uint32_t chunk, bool finish_last) {
@@ -209,8 +227,10 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 	const uint32_t mask = (hdr >> 8) & 0xffu;
 	uint32_t vid[8];
 	float4 O[8], D[8];
+	bool fin = false;  // this pass is the lane's last of the substep (its body runs no volume passes)
 	if (live) {
 		const Mat mat = load_mat(C.bodies, hdr >> 16);
+		fin = EXT && finish_last && mat.nvol == 0u;
 #pragma unroll
 		for (int s = 0; s < 8; s++) vid[s] = vids[s * kLanes + lane];
 #pragma unroll
@@ -232,7 +252,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 			const float4 Ot[4] = {O[cube_slot(t, 0)], O[cube_slot(t, 1)], O[cube_slot(t, 2)], O[cube_slot(t, 3)]};
 			float4 Dt[4] = {D[cube_slot(t, 0)], D[cube_slot(t, 1)], D[cube_slot(t, 2)], D[cube_slot(t, 3)]};
 			if (TAPE) tape_tet(C, s_launch, trow + t, lane, Dt);
-			const float2 lam = solve_tet<DAMP>(mat, tr, inv_dt, inv_dt2, Ot, Dt);
+			const float2 lam = solve_tet<EXT>(mat, tr, inv_dt, inv_dt2, Ot, Dt);
 #pragma unroll
 			for (int k = 0; k < 4; k++) D[cube_slot(t, k)] = Dt[k];
 			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
@@ -242,10 +262,10 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 	if (live) {
 		// with damping sweeps, the vertex's last solve of the substep finishes
 		// it (to the canonical X, V that the sweeps work on)
-		const uint32_t last = DAMP && finish_last ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
+		const uint32_t last = fin ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
-			if (DAMP && (last & (1u << s))) finalize_vertex(C.bodies, O[s], D[s], inv_dt);
+			if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O[s], D[s], inv_dt);
 			if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
 			__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
 		}
@@ -255,14 +275,14 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 // One warp processes one resident chunk; lane = cluster. `next` >= 0 is the
 // warp's next chunk: its copy is issued as soon as this chunk's records have
 // been consumed, so it overlaps the write-back and what follows.
-template <bool LAMBDAS, bool TAPE = false, bool DAMP = false>
+template <bool LAMBDAS, bool TAPE = false, bool EXT = false>
 __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, bool first,
                                           float dt, float inv_dt, float inv_dt2, uint32_t s_launch = 0,
                                           bool finish_last = false) {
 	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
-		run_chunk_cube<LAMBDAS, TAPE, DAMP>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch, chunk,
+		run_chunk_cube<LAMBDAS, TAPE, EXT>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch, chunk,
 		                                    finish_last);
 		return;
 	}
@@ -275,8 +295,10 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 	float4* sO = st.vs + lane;
 	float4* sD = st.vs + kLanes * nvmax + lane;
 	uint32_t vid[kMaxClusterVerts];
+	bool fin = false;
 	if (nv) {
 		const Mat mat = load_mat(C.bodies, hdr >> 16);
+		fin = EXT && finish_last && mat.nvol == 0u;
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++)
 			if (s < nv) vid[s] = vids[s * kLanes + lane];
@@ -302,7 +324,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			const float4 O[4] = {sO[s0 * kLanes], sO[s1 * kLanes], sO[s2 * kLanes], sO[s3 * kLanes]};
 			float4 D[4] = {sD[s0 * kLanes], sD[s1 * kLanes], sD[s2 * kLanes], sD[s3 * kLanes]};
 			if (TAPE) tape_tet(C, s_launch, trow + t, lane, D);
-			const float2 lam = solve_tet<DAMP>(mat, tr, inv_dt, inv_dt2, O, D);
+			const float2 lam = solve_tet<EXT>(mat, tr, inv_dt, inv_dt2, O, D);
 			sD[s0 * kLanes] = D[0];
 			sD[s1 * kLanes] = D[1];
 			sD[s2 * kLanes] = D[2];
@@ -312,17 +334,97 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 	}
 	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
 	if (nv) {
-		const uint32_t last = DAMP && finish_last ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
+		const uint32_t last = fin ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
 				float4 O = sO[s * kLanes], D = sD[s * kLanes];
-				if (DAMP && (last & (1u << s))) finalize_vertex(C.bodies, O, D, inv_dt);
+				if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O, D, inv_dt);
 				if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O);
 				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D);
 			}
 		}
 	}
+}
+
+// Volume sweep k (1-based) over a resident chunk: SolveElementVolume on each
+// tet of the cluster in order (GeoLinear3d::Constrain, XPBDFEM/Geo.cpp:
+// 780-783), for lanes whose body runs at least k volume passes. The state is
+// (O, D), as in the solve sweep; only D changes, except that with damping
+// sweeps (finish) the body's last volume sweep finishes the vertices whose
+// last solve this cluster makes. CUBE: canonical cube chunks, all in
+// registers. Not inlined, like the damping passes.
+template <bool CUBE>
+__device__ __noinline__ void vol_chunk(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t ntmax, uint32_t nvmax,
+                                       int next, uint32_t lane, float inv_dt, float inv_dt2, uint32_t k, bool finish) {
+	constexpr uint32_t NV = CUBE ? 8u : kMaxClusterVerts;
+	constexpr uint32_t NT = CUBE ? 6u : kMaxClusterTets;
+	const float4* rec = reinterpret_cast<const float4*>(st.buf);
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * ntmax);
+	const uint32_t* vids = hdrs + kLanes;
+	const uint32_t* slots = vids + kLanes * nvmax;
+	const uint32_t hdr = hdrs[lane];
+	const uint32_t nv = CUBE ? 8u : (hdr & 15u), nt = CUBE ? 6u : ((hdr >> 4) & 15u);
+	bool live = (hdr & 15u) != 0;
+	uint32_t vid[NV], last = 0;
+	float4 O[NV], D[NV];
+	if (live) {
+		const Mat mat = load_mat(C.bodies, hdr >> 16);
+		live = mat.nvol >= k;
+		if (finish && mat.nvol == k) last = __ldg(C.lastmask + (size_t)chunk * kLanes + lane);
+		if (live) {
+#pragma unroll
+			for (uint32_t s = 0; s < NV; s++) {
+				if (s < nv) {
+					vid[s] = vids[s * kLanes + lane];
+					O[s] = __ldcg(C.vert + 2 * (size_t)vid[s]);
+					D[s] = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
+				}
+			}
+#pragma unroll
+			for (uint32_t t = 0; t < NT; t++) {
+				if (t < nt) {
+					const uint32_t sl = CUBE ? (uint32_t)(cube_slot(t, 0) | cube_slot(t, 1) << 4 | cube_slot(t, 2) << 8 |
+					                                      cube_slot(t, 3) << 12)
+					                         : slots[t * kLanes + lane];
+					const float4* r = rec + t * 4 * kLanes + lane;
+					const TetRec tr = {r[0], r[kLanes], r[2 * kLanes], r[3 * kLanes]};
+					float4 Ot[4], Dt[4];
+#pragma unroll
+					for (int j = 0; j < 4; j++) {
+						Ot[j] = O[(sl >> (4 * j)) & 15u];
+						Dt[j] = D[(sl >> (4 * j)) & 15u];
+					}
+					volume_tet(mat, tr, inv_dt2, Ot, Dt);
+#pragma unroll
+					for (int j = 0; j < 4; j++) D[(sl >> (4 * j)) & 15u] = Dt[j];
+				}
+			}
+		}
+	}
+	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // records consumed: prefetch
+	if (live) {
+#pragma unroll
+		for (uint32_t s = 0; s < NV; s++) {
+			if (s < nv) {
+				if (last & (1u << s)) {
+					finalize_vertex(C.bodies, O[s], D[s], inv_dt);
+					__stcg(C.vert + 2 * (size_t)vid[s], O[s]);
+				}
+				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
+			}
+		}
+	}
+}
+
+__device__ __forceinline__ void run_vol_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane,
+                                              float inv_dt, float inv_dt2, uint32_t k, bool finish) {
+	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu;
+	if (m.z & kShapeCube)
+		vol_chunk<true>(C, st, chunk, ntmax, nvmax, next, lane, inv_dt, inv_dt2, k, finish);
+	else
+		vol_chunk<false>(C, st, chunk, ntmax, nvmax, next, lane, inv_dt, inv_dt2, k, finish);
 }
 
 // One damping pass over a resident chunk (KIND 0: element Rayleigh damping,
@@ -453,18 +555,22 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 }
 
 // A substep is P = kinds x ncolours passes: the solve sweep over the colours,
-// then each damping sweep (DevCtx::damp_kinds) over them again; pass q works
-// on colour q % ncolours.
-__device__ __forceinline__ uint32_t pass_kinds(const DevCtx& C) { return 1u + (uint32_t)__popc(C.damp_kinds); }
+// the volume sweeps (DevCtx::nvol), then each damping sweep
+// (DevCtx::damp_kinds) over them again; pass q works on colour q % ncolours.
+__device__ __forceinline__ uint32_t pass_kinds(const DevCtx& C) {
+	return 1u + C.nvol + (uint32_t)__popc(C.damp_kinds);
+}
 
-// Damping kind of pass-kind index k >= 1: 0 element Rayleigh, 1 PBD.
-__device__ __forceinline__ int damp_kind(const DevCtx& C, uint32_t k) { return (k == 1u && (C.damp_kinds & 1u)) ? 0 : 1; }
+// Damping kind of pass-kind index k > nvol: 0 element Rayleigh, 1 PBD.
+__device__ __forceinline__ int damp_kind(const DevCtx& C, uint32_t k) {
+	return (k == C.nvol + 1u && (C.damp_kinds & 1u)) ? 0 : 1;
+}
 
-// Whether pass q (P passes per substep) runs at `tick`: the solve passes
-// always, a damping pass only if some tet of its colour is damped then.
+// Whether pass q (P passes per substep) runs at `tick`: the solve and volume
+// passes always, a damping pass only if some tet of its colour is damped then.
 __device__ __forceinline__ bool pass_runs(const DevCtx& C, uint32_t q, uint32_t tick) {
 	const uint32_t kind = q / C.ncolours;
-	return kind == 0 || pass_on(C, damp_kind(C, kind), q - kind * C.ncolours, tick);
+	return kind <= C.nvol || pass_on(C, damp_kind(C, kind), q - kind * C.ncolours, tick);
 }
 
 // The warp's next chunk after `ch` (pass q of substep s, P passes per
@@ -494,9 +600,10 @@ __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t 
 // the substep state stays (O, D) between substeps and the closing pass
 // finalizes it; with damping sweeps they finish every substep and the state
 // between substeps is canonical (X, V).
-// DAMP: the damping sweeps and the in-solve damping compiled in (handles with
-// damping switched on); without it they cost the kernel nothing.
-template <bool LAMBDAS, bool TAPE = false, bool DAMP = false>
+// EXT: the extended kernel, with the damping sweeps, the in-solve damping,
+// the Pixar and cube models and the volume sweeps compiled in (handles that
+// use any of them); without it they cost the kernel nothing.
+template <bool LAMBDAS, bool TAPE = false, bool EXT = false>
 __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, float dt) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t lane = threadIdx.x & 31u;
@@ -504,8 +611,8 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	// chunk i of a colour goes to block i % grid, so chunks spread over all SMs
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
-	const bool dmode = DAMP && C.damp_kinds != 0u;
-	const uint32_t P = (DAMP ? pass_kinds(C) : 1u) * C.ncolours;
+	const bool dmode = EXT && C.damp_kinds != 0u;
+	const uint32_t P = (EXT ? pass_kinds(C) : 1u) * C.ncolours;
 	const uint32_t tick0 = __ldcg(C.tick);  // read before the first barrier; block 0 advances it at the end
 	Stage st = stage_init(C, lane);
 	run_isolated<TAPE>(C, gtid, nthreads, nsub, dt, inv_dt, dmode);
@@ -516,7 +623,7 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 			const uint32_t kind = q / C.ncolours, c = q - kind * C.ncolours;
 			// a damping pass with nothing to damp at this tick is skipped by
 			// every block alike (same table, same tick): no work, no barrier
-			if (DAMP && kind > 0 && !pass_runs(C, q, tick0 + s)) continue;
+			if (EXT && kind > 0 && !pass_runs(C, q, tick0 + s)) continue;
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				if (!stage_acquire(C, st, ch, lane)) {
@@ -524,9 +631,11 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 					break;
 				}
 				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps, tick0);
-				if (!DAMP || kind == 0)
-					run_chunk<LAMBDAS, TAPE, DAMP>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s,
+				if (!EXT || kind == 0)
+					run_chunk<LAMBDAS, TAPE, EXT>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s,
 					                               dmode);
+				else if (kind <= C.nvol)
+					run_vol_chunk(C, st, ch, next, lane, inv_dt, inv_dt2, kind, dmode);
 				else
 					run_damp_chunk(C, st, ch, next, lane, damp_kind(C, kind), inv_dt, tick0 + s);
 			}
@@ -629,33 +738,36 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 }
 
 // One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
-// kind 0 is the solve pass (first: the state is canonical), 1 and up the
-// damping passes (damp_kind; kind 1 finishes the substep); sub: the substep's
+// kind 0 is the solve pass (first: the state is canonical), 1..nvol the
+// volume passes, the rest the damping passes (damp_kind); sub: the substep's
 // index in the call (its tick is *C.tick + sub). In the first launch of a
 // call, blocks past the colour's chunks step the isolated vertices through
 // all nsub substeps.
-template <bool LAMBDAS, bool DAMP = false>
+template <bool LAMBDAS, bool EXT = false>
 __global__ void __launch_bounds__(256, 1) k_colour(DevCtx C, uint32_t colour, int first, float dt, uint32_t solve_blocks,
                                                 uint32_t nsub, uint32_t kind, uint32_t sub) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	if (blockIdx.x >= solve_blocks) {
 		const uint32_t b = blockIdx.x - solve_blocks, nb = gridDim.x - solve_blocks;
-		run_isolated(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, nsub, dt, inv_dt, DAMP && C.damp_kinds != 0u);
+		run_isolated(C, b * blockDim.x + threadIdx.x, nb * blockDim.x, nsub, dt, inv_dt, EXT && C.damp_kinds != 0u);
 		return;
 	}
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t ch = __ldg(C.colour_chunk_begin + colour) + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
 	if (ch >= __ldg(C.colour_chunk_begin + colour + 1)) return;
 	const uint32_t tick = __ldcg(C.tick) + sub;
-	const int dk = DAMP && kind > 0 ? damp_kind(C, kind) : 0;
+	const bool damp_pass = EXT && kind > C.nvol;
+	const int dk = damp_pass ? damp_kind(C, kind) : 0;
 	// a graph replays its launches at every tick: a damping pass with nothing
 	// to damp at this one returns at once
-	if (DAMP && kind > 0 && !pass_on(C, dk, colour, tick)) return;
+	if (damp_pass && !pass_on(C, dk, colour, tick)) return;
 	Stage st = stage_init(C, lane);
 	if (!stage_acquire(C, st, ch, lane)) return;
-	if (!DAMP || kind == 0)
-		run_chunk<LAMBDAS, false, DAMP>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2, 0,
-		                                DAMP && C.damp_kinds != 0u);
+	const bool dmode = EXT && C.damp_kinds != 0u;
+	if (!EXT || kind == 0)
+		run_chunk<LAMBDAS, false, EXT>(C, st, ch, -1, lane, first != 0, dt, inv_dt, inv_dt2, 0, dmode);
+	else if (!damp_pass)
+		run_vol_chunk(C, st, ch, -1, lane, inv_dt, inv_dt2, kind, dmode);
 	else
 		run_damp_chunk(C, st, ch, -1, lane, dk, inv_dt, tick);
 }
@@ -750,21 +862,21 @@ static void set_smem_attr(const void* f, size_t bytes) {
 	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
-static const void* persistent_fn(bool lambdas, bool damp) {
-	if (damp) return lambdas ? (const void*)k_persistent<true, false, true> : (const void*)k_persistent<false, false, true>;
+static const void* persistent_fn(bool lambdas, bool ext) {
+	if (ext) return lambdas ? (const void*)k_persistent<true, false, true> : (const void*)k_persistent<false, false, true>;
 	return lambdas ? (const void*)k_persistent<true> : (const void*)k_persistent<false>;
 }
 
-static const void* colour_fn(bool lambdas, bool damp) {
-	if (damp) return lambdas ? (const void*)k_colour<true, true> : (const void*)k_colour<false, true>;
+static const void* colour_fn(bool lambdas, bool ext) {
+	if (ext) return lambdas ? (const void*)k_colour<true, true> : (const void*)k_colour<false, true>;
 	return lambdas ? (const void*)k_colour<true> : (const void*)k_colour<false>;
 }
 
 int configure_kernels(const LaunchCfg& cfg) {
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
-	for (bool damp : {false, true}) {
-		set_smem_attr(persistent_fn(cfg.lambdas, damp), smem);
-		set_smem_attr(colour_fn(cfg.lambdas, damp), smem);
+	for (bool ext : {false, true}) {
+		set_smem_attr(persistent_fn(cfg.lambdas, ext), smem);
+		set_smem_attr(colour_fn(cfg.lambdas, ext), smem);
 	}
 	set_smem_attr(cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>, smem);
 	return (int)cudaGetLastError();
@@ -773,7 +885,7 @@ int configure_kernels(const LaunchCfg& cfg) {
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
 	const void* f = cfg.sync_mode == 3
 	                    ? (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>)
-	                    : persistent_fn(cfg.lambdas, cfg.damp);
+	                    : persistent_fn(cfg.lambdas, cfg.ext);
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	cudaError_t e = cudaGetDevice(&dev);
@@ -796,17 +908,17 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 		DevCtx c = ctx;
 		void* args[] = {&c, &nsub, &dt};
 		const void* f = cfg.sync_mode == 1
-		                    ? persistent_fn(cfg.lambdas, cfg.damp)
+		                    ? persistent_fn(cfg.lambdas, cfg.ext)
 		                    : (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>);
 		e = cudaLaunchCooperativeKernel(f, dim3(cfg.blocks), dim3(cfg.block), args, smem, st);
 		return (int)e;
 	}
 	// per-colour launches (captured into a CUDA graph by the caller when wanted):
-	// per substep the solve sweep, then each damping sweep
-	const void* fc = colour_fn(cfg.lambdas, cfg.damp);
+	// per substep the solve sweep, the volume sweeps, then each damping sweep
+	const void* fc = colour_fn(cfg.lambdas, cfg.ext);
 	const uint32_t warps_per_block = cfg.block / 32;
-	const bool dmode = cfg.damp && ctx.damp_kinds != 0u;
-	const uint32_t kinds = dmode ? 1u + (uint32_t)__builtin_popcount(ctx.damp_kinds) : 1u;
+	const bool dmode = cfg.ext && ctx.damp_kinds != 0u;
+	const uint32_t kinds = cfg.ext ? 1u + ctx.nvol + (uint32_t)__builtin_popcount(ctx.damp_kinds) : 1u;
 	for (uint32_t s = 0; s < nsub; s++) {
 		for (uint32_t kind = 0; kind < kinds; kind++) {
 			for (uint32_t c = 0; c < ctx.ncolours; c++) {
@@ -937,7 +1049,7 @@ int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bo
 		p = g_noalloc_ptr[device];
 	}
 	cudaStream_t st = (cudaStream_t)stream;
-	const void* f = persistent_fn(lambdas, ctx.damp_any != 0u);
+	const void* f = persistent_fn(lambdas, ctx.ext != 0u);
 	const size_t smem = solve_smem_bytes(block, warp_smem);
 	int sms = 0, per_sm = 0;
 	cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);

@@ -18,8 +18,18 @@ LIB_PATH = os.path.join(HERE, "libxfem.so")
 
 OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT = 0, -1, -2, -3, -4, -5, -6
 ENERGY_BIT = 6
+# energy ids, XPBDFEM/Settings.h:41-53 (8-10, the continuous-pressure models, are not run)
+ENERGY_PIXAR = 0
+ENERGY_PIXAR_REDUCED = 1
+ENERGY_PIXAR_SEL = 2
+ENERGY_MIXED = 3
 ENERGY_MIXED_SEL = 4
+ENERGY_YEOH_SKIN = 5
+ENERGY_YEOH_SKIN_SEL = 6
 ENERGY_YEOH_SKIN_FAST = 7
+ENERGY_CUBE_NEO = 11
+ENERGY_CUBE_SKIN = 12
+MAX_VOLUME_PASSES = 64
 XPBD_SOLVE_BIT = 11
 LOCK_LEFT = 1 << 26
 REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
