@@ -19,7 +19,8 @@ shape the configuration names.
   shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches, and
   "batched": 512 bodies in one launch per frame against one launch per body,
   "damped": the same mesh with the reference web UI's default damping against
-  undamped,
+  undamped, "models": the same mesh at nu = 0.45 with Mixed, YeohSkin, Pixar
+  and one volume pass against MixedSel,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -291,6 +292,7 @@ def run_xfem(args, world, rank, local):
     batched = None if args.no_batched else run_batched(stream)
     adjoint = None if args.no_adjoint else run_adjoint(stream)
     damped = None if args.no_damped else run_damped(stream)
+    models = None if args.no_models else run_models(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -311,6 +313,7 @@ def run_xfem(args, world, rank, local):
         "batched": batched,
         "adjoint": adjoint,
         "damped": damped,
+        "models": models,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -451,38 +454,68 @@ def run_damped(stream, frames=5):
     w = W.throughput()
     S = w["substeps"]
     sdt = w["dt"] / S
-    sp = C_void_p(stream.cuda_stream)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
     vc, avc = xfem.pbd_damping_coefficients(0.03, sdt, 0.1)
     damp = dict(w["settings"], damping=0.005, pbd_damping=0.03, time_corrected_drag=xfem.time_corrected_drag(0.002, sdt),
                 volume_and_time_corrected_pbd_damping=vc, amortized_volume_and_time_corrected_pbd_damping=avc,
                 flags=w["settings"]["flags"] | (3 << 20))
-    out = {}
-    for key, s_ in (("undamped", w["settings"]), ("damped", damp)):
-        body = xfem.Body(w["nodes"], w["idx"], w["density"], s_, stream=sp)
-        body.set_lock_mask(w["lock"])
-        for _ in range(3):
-            body.step_frames(1, S, sdt)
-        ms = []
-        for _ in range(frames):
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            with torch.cuda.stream(stream):
-                flush.zero_()
-                a.record(stream)
-            body.step_frames(1, S, sdt)
-            with torch.cuda.stream(stream):
-                b.record(stream)
-            b.synchronize()
-            ms.append(a.elapsed_time(b))
-        info = body.info()
-        body.close()
-        nt = w["idx"].size // 5
-        out[key] = {"ms_per_frame": statistics.median(ms), "value": nt * S / (statistics.median(ms) / 1e3),
-                    "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
-                    "block": info["block_size"]}
+    out = {key: time_frames(stream, w, s_, flush, frames)
+           for key, s_ in (("undamped", w["settings"]), ("damped", damp))}
     return {"workload": w["name"] + ", damping as the reference's web UI starts (PostAmortized 0.005, PBD 0.03, "
                                    "drag 0.002)", "unit": UNIT, **out,
             "cost": out["damped"]["ms_per_frame"] / out["undamped"]["ms_per_frame"]}
+
+
+def time_frames(stream, w, settings, flush, frames):
+    """Median device time of one frame (w's substeps) of a body of workload w
+    with the given settings, L2 flushed before each frame."""
+    import torch
+
+    import xfem
+    S = w["substeps"]
+    sdt = w["dt"] / S
+    body = xfem.Body(w["nodes"], w["idx"], w["density"], settings, stream=C_void_p(stream.cuda_stream))
+    body.set_lock_mask(w["lock"])
+    for _ in range(3):
+        body.step_frames(1, S, sdt)
+    ms = []
+    for _ in range(frames):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            a.record(stream)
+        body.step_frames(1, S, sdt)
+        with torch.cuda.stream(stream):
+            b.record(stream)
+        b.synchronize()
+        ms.append(a.elapsed_time(b))
+    info = body.info()
+    body.close()
+    nt = w["idx"].size // 5
+    return {"ms_per_frame": statistics.median(ms), "value": nt * S / (statistics.median(ms) / 1e3),
+            "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+            "block": info["block_size"]}
+
+
+def run_models(stream, frames=5):
+    """The throughput mesh at nu = 0.45 (the Pixar models need nu < 0.5) with
+    the other energy models and with volume passes, against MixedSel (the hot
+    kernel): device-timed frames of 20 substeps, L2 flushed between frames."""
+    import torch
+
+    import xfem
+    from xfem import workloads as W
+    w = W.throughput()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    base = dict(w["settings"], poissons_ratio=0.45, compliance=W.nh_compliance(5e5, 0.45))
+    solve = (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT
+    cases = (("mixed_sel", base), ("mixed", dict(base, flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)),
+             ("yeoh_skin", dict(base, flags=(xfem.ENERGY_YEOH_SKIN << xfem.ENERGY_BIT) | solve)),
+             ("pixar", dict(base, flags=(xfem.ENERGY_PIXAR << xfem.ENERGY_BIT) | solve)),
+             ("mixed_sel_volume_1", dict(base, volume_passes=1)))
+    out = {key: time_frames(stream, w, s_, flush, frames) for key, s_ in cases}
+    return {"workload": w["name"].replace("Neo-Hookean", "nu = 0.45"), "unit": UNIT, **out,
+            "cost": {k: out[k]["ms_per_frame"] / out["mixed_sel"]["ms_per_frame"] for k, _ in cases[1:]}}
 
 
 def C_void_p(v):
@@ -510,6 +543,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-damped", action="store_true")
+    ap.add_argument("--no-models", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")
