@@ -64,6 +64,24 @@ __device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
 	return s_ok != 0;
 }
 
+// One vertex's 32-byte state (vert[2v], vert[2v + 1]: one sector, 32-byte
+// aligned) in a single 256-bit access (sm_100 and later), L1 bypassed as
+// __ldcg / __stcg: half the load and store instructions, and L1 wavefronts,
+// of two 128-bit accesses. The memory clobbers keep them ordered with the
+// grid barrier and the staging copies like any other global access.
+__device__ __forceinline__ void ld_vertex(const float4* p, float4& a, float4& b) {
+	asm volatile("ld.global.cg.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+	             : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+	             : "l"(p)
+	             : "memory");
+}
+
+__device__ __forceinline__ void st_vertex(float4* p, const float4& a, const float4& b) {
+	asm volatile("st.global.cg.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(p), "f"(a.x), "f"(a.y), "f"(a.z),
+	             "f"(a.w), "f"(b.x), "f"(b.y), "f"(b.z), "f"(b.w)
+	             : "memory");
+}
+
 struct Vec3 {
 	float x, y, z;
 };

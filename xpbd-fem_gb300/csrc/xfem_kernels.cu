@@ -234,10 +234,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 #pragma unroll
 		for (int s = 0; s < 8; s++) vid[s] = vids[s * kLanes + lane];
 #pragma unroll
-		for (int s = 0; s < 8; s++) {
-			O[s] = __ldcg(C.vert + 2 * (size_t)vid[s]);
-			D[s] = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
-		}
+		for (int s = 0; s < 8; s++) ld_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
 #pragma unroll
 		for (int s = 0; s < 8; s++)
 			if (mask & (1u << s)) {
@@ -263,11 +260,12 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 		// with damping sweeps, the vertex's last solve of the substep finishes
 		// it (to the canonical X, V that the sweeps work on)
 		const uint32_t last = fin ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
+		// the whole 32-byte state: O is unchanged unless this cluster advanced
+		// or finished the vertex, and no other cluster of the pass touches it
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
 			if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O[s], D[s], inv_dt);
-			if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O[s]);
-			__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
+			st_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
 		}
 	}
 }
@@ -305,8 +303,8 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 #pragma unroll
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
-				float4 O = __ldcg(C.vert + 2 * (size_t)vid[s]);
-				float4 D = __ldcg(C.vert + 2 * (size_t)vid[s] + 1);
+				float4 O, D;
+				ld_vertex(C.vert + 2 * (size_t)vid[s], O, D);
 				if (mask & (1u << s)) {
 					const float4 Dbefore = D;
 					advance_vertex(C.bodies, O, D, first, dt, inv_dt);
@@ -340,12 +338,14 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			if (s < nv) {
 				float4 O = sO[s * kLanes], D = sD[s * kLanes];
 				if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O, D, inv_dt);
-				if ((mask | last) & (1u << s)) __stcg(C.vert + 2 * (size_t)vid[s], O);
-				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D);
+				st_vertex(C.vert + 2 * (size_t)vid[s], O, D);
 			}
 		}
 	}
 }
+
+// The damping and volume sweeps keep two 128-bit vertex accesses: with the
+// 256-bit form in both of them, ptxas (CUDA 13.0) fails on this file.
 
 // Volume sweep k (1-based) over a resident chunk: SolveElementVolume on each
 // tet of the cluster in order (GeoLinear3d::Constrain, XPBDFEM/Geo.cpp:
@@ -526,15 +526,15 @@ __device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, ui
                                              float inv_dt, bool finalize_end = false) {
 	for (uint32_t i = begin; i < C.nisolated; i += step) {
 		const uint32_t v = __ldg(C.isolated + i);
-		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
+		float4 O, D;
+		ld_vertex(C.vert + 2 * (size_t)v, O, D);
 		for (uint32_t s = 0; s < nsub; s++) {
 			const float4 Dbefore = D;
 			advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
 			if (TAPE) tape_vertex(C, v, O, Dbefore, s, s == 0);
 		}
 		if (finalize_end) finalize_vertex(C.bodies, O, D, inv_dt);
-		__stcg(C.vert + 2 * (size_t)v, O);
-		__stcg(C.vert + 2 * (size_t)v + 1, D);
+		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 }
 
@@ -542,15 +542,15 @@ template <bool TAPE = false>
 __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, uint32_t step, float inv_dt,
                                              uint32_t nsub = 0) {
 	for (uint32_t v = begin; v < C.nverts; v += step) {
-		float4 O = __ldcg(C.vert + 2 * (size_t)v), D = __ldcg(C.vert + 2 * (size_t)v + 1);
+		float4 O, D;
+		ld_vertex(C.vert + 2 * (size_t)v, O, D);
 		if (TAPE) __stcs(C.tape_fin + v, D);
 		finalize_vertex(C.bodies, O, D, inv_dt);
 		if (TAPE) {
 			const int q = __ldg(C.tip_of + v);
 			if (q >= 0) C.traj[(size_t)(C.sub_base + nsub - 1) * C.ntips + q] = O;
 		}
-		__stcg(C.vert + 2 * (size_t)v, O);
-		__stcg(C.vert + 2 * (size_t)v + 1, D);
+		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 }
 
