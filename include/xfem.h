@@ -121,6 +121,8 @@ typedef struct xfem_options {
 	uint32_t keep_lambdas; /* 1 = record each tet's two multipliers of the last substep */
 	int32_t device;        /* CUDA device ordinal; -1 or 0 = current / 0 */
 	void* stream;          /* cudaStream_t to run on; NULL = a stream owned by the handle */
+	uint32_t host_setup;   /* 1 = rest state and schedule on the host (default: their parallel
+	                          phases on the GPU; the result is the same bit for bit) */
 } xfem_options;
 
 /* One mesh for xfem_batch_create, in GeoLinear3d::Init's argument form. */

@@ -2,13 +2,17 @@
 // schedule into the device layout, stepping and transfers.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <memory>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/xfem.h"
@@ -301,14 +305,23 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	b.nv = nv;
 	b.nt = (uint32_t)(b.tets.size() / 4);
 	b.nodes.assign(m.node_data, m.node_data + m.node_data_count);
-	b.ep.resize(17 * (size_t)b.nt);
-	b.w0.resize(nv);
-	b.vflags.resize(nv);
-	init_rest(b.nodes.data(), nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
 	return XFEM_OK;
 }
 
-int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint32_t morton, BodyHost& b) {
+// The rest state on the host (GeoLinear3d::Init's precompute).
+void host_rest(const xfem_mesh& m, BodyHost& b) {
+	b.ep.resize(17 * (size_t)b.nt);
+	b.w0.resize(b.nv);
+	b.vflags.resize(b.nv);
+	init_rest(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
+}
+
+// Rest state and schedule of one body: on the host (gpu false), or with the
+// parallel phases on the GPU (rest state, incidence, vertex ranks, cluster
+// order) around the host's greedy clustering and colouring. Both give the
+// same result bit for bit.
+int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint32_t morton, bool gpu, void* stream,
+                 BodyHost& b) {
 	int rc = prepare_mesh(m, b);
 	if (rc) return rc;
 	if (s) {
@@ -318,8 +331,90 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	}
 	rc = validate_settings(b.settings);
 	if (rc) return rc;
-	if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, mode, morton, b.sched))
+	if (!gpu) {
+		host_rest(m, b);
+		if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, mode, morton, b.sched))
+			return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
+		return XFEM_OK;
+	}
+	GpuSetupMesh g;
+	int e = gpu_setup_mesh(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, morton, g, stream);
+	if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
+	b.ep = std::move(g.ep);
+	b.w0 = std::move(g.w0);
+	b.vflags = std::move(g.vflags);
+	if (cluster_and_colour(b.tets.data(), b.nt, g.off.data(), g.lst.data(), mode, b.sched))
 		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
+	b.sched.vert_rank = std::move(g.vert_rank);
+	e = gpu_cluster_order(b.nodes.data(), b.nv, b.tets.data(), b.nt, morton, g.frame, b.sched, stream);
+	if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
+	return XFEM_OK;
+}
+
+// fn(i) for i in [0, n) on the host's threads (static split; fn must only
+// write what index i owns).
+template <typename F>
+void parallel_for(uint32_t n, const F& fn) {
+	const uint32_t nt = std::min<uint32_t>(std::max(1u, std::thread::hardware_concurrency()), 64u);
+	if (n < 64 || nt == 1) {
+		for (uint32_t i = 0; i < n; i++) fn(i);
+		return;
+	}
+	std::vector<std::thread> pool;
+	for (uint32_t t = 0; t < nt; t++)
+		pool.emplace_back([&, t] {
+			const uint32_t b = (uint32_t)((uint64_t)n * t / nt), e = (uint32_t)((uint64_t)n * (t + 1) / nt);
+			for (uint32_t i = b; i < e; i++) fn(i);
+		});
+	for (std::thread& th : pool) th.join();
+}
+
+// Set-up phase timings, printed to stderr when the environment variable
+// XFEM_SETUP_TIMING is set (diagnostics for the handle set-up).
+struct SetupClock {
+	const bool on = getenv("XFEM_SETUP_TIMING") != nullptr;
+	std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+	void lap(const char* what) {
+		if (!on) return;
+		const auto n = std::chrono::steady_clock::now();
+		fprintf(stderr, "xfem set-up: %-22s %8.1f ms\n", what, std::chrono::duration<double, std::milli>(n - t).count());
+		t = n;
+	}
+};
+
+// Bodies of at least this many tets take the GPU set-up path; below it a GPU
+// round trip costs more than it saves.
+constexpr uint32_t kGpuSetupMinTets = 1u << 16;
+
+// Rest state and schedule of every body of a handle. Bodies are independent
+// and each one's result does not depend on where it is computed, so the large
+// ones run one after another with their parallel phases on the GPU (the
+// handle's stream, this thread) while host threads take the others.
+int prepare_bodies(xfem_body* h, uint32_t nb, const xfem_mesh* meshes, const xfem_settings* settings, uint32_t mode,
+                   uint32_t morton) {
+	std::vector<int> rcs(nb, XFEM_OK);
+	std::vector<std::string> errs(nb);
+	std::vector<uint32_t> on_host, on_gpu;
+	for (uint32_t i = 0; i < nb; i++)
+		(h->opt.host_setup == 0 && meshes[i].idx_data_count / 5u >= kGpuSetupMinTets ? on_gpu : on_host).push_back(i);
+	auto one = [&](uint32_t i, bool gpu) {
+		rcs[i] = prepare_body(meshes[i], settings ? &settings[i] : nullptr, mode, morton, gpu, h->stream, h->bodies[i]);
+		if (rcs[i]) errs[i] = g_err;
+	};
+	std::atomic<uint32_t> next{0};
+	const uint32_t hw = std::max(1u, std::thread::hardware_concurrency());
+	const uint32_t nthreads = (uint32_t)std::min<size_t>(on_host.size() > 1 ? on_host.size() : 0, std::min(hw, 64u));
+	std::vector<std::thread> pool;
+	for (uint32_t t = 0; t < nthreads; t++)
+		pool.emplace_back([&] {
+			for (uint32_t k; (k = next.fetch_add(1)) < on_host.size();) one(on_host[k], false);
+		});
+	if (nthreads == 0)
+		for (uint32_t i : on_host) one(i, false);
+	for (uint32_t i : on_gpu) one(i, true);
+	for (std::thread& t : pool) t.join();
+	for (uint32_t i = 0; i < nb; i++)
+		if (rcs[i]) return fail(rcs[i], nb > 1 ? "body " + std::to_string(i) + ": " + errs[i] : errs[i]);
 	return XFEM_OK;
 }
 
@@ -329,6 +424,7 @@ struct Lane {
 
 // Packs every body's schedule into the merged device layout and uploads it.
 int build_device(xfem_body* h) {
+	SetupClock clk;
 	const uint32_t nb = (uint32_t)h->bodies.size();
 	uint32_t nverts = 0, ntets = 0, ncol = 1;
 	for (auto& b : h->bodies) {
@@ -358,23 +454,36 @@ int build_device(xfem_body* h) {
 	}
 	ccb[ncol] = (uint32_t)chunk_lanes.size();
 	const uint32_t nch = (uint32_t)chunk_lanes.size();
+	// each lane's distinct vertices in first-touch order (device ids) and tet
+	// count; every later pass reads these
+	const size_t nlanes = (size_t)nch * kLanes;
+	std::vector<uint32_t> lane_dv(nlanes * kMaxClusterVerts);
+	std::vector<uint8_t> lane_nv(nlanes, 0), lane_nt(nlanes, 0);
+	parallel_for(nch, [&](uint32_t k) {
+		for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++) {
+			const Lane& L = chunk_lanes[k][lane];
+			const BodyHost& b = h->bodies[L.body];
+			uint32_t vs[kMaxClusterVerts], nvv = 0;
+			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++)
+				for (int n = 0; n < 4; n++) {
+					const uint32_t v = b.tets[4 * (size_t)b.sched.cl_tets[q] + n];
+					if (std::find(vs, vs + nvv, v) == vs + nvv) vs[nvv++] = v;
+				}
+			const size_t i = (size_t)k * kLanes + lane;
+			for (uint32_t sl = 0; sl < nvv; sl++) lane_dv[i * kMaxClusterVerts + sl] = b.vbase + b.sched.vert_rank[vs[sl]];
+			lane_nv[i] = (uint8_t)nvv;
+			lane_nt[i] = (uint8_t)(b.sched.cl_begin[L.cluster + 1] - b.sched.cl_begin[L.cluster]);
+		}
+	});
 	std::vector<ChunkMeta> meta(nch);
 	std::vector<uint32_t> shape_nt(nch), shape_nv(nch);
 	uint64_t total16 = 0;
 	uint32_t trows = 0, max_bytes = 128, max_nv = 4;
 	for (uint32_t k = 0; k < nch; k++) {
 		uint32_t ntm = 0, nvm = 0;
-		for (const Lane& L : chunk_lanes[k]) {
-			const BodyHost& b = h->bodies[L.body];
-			const uint32_t nt = b.sched.cl_begin[L.cluster + 1] - b.sched.cl_begin[L.cluster];
-			uint32_t vs[kMaxClusterVerts + 4], nvv = 0;
-			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++)
-				for (int n = 0; n < 4; n++) {
-					const uint32_t v = b.tets[4 * (size_t)b.sched.cl_tets[q] + n];
-					if (std::find(vs, vs + nvv, v) == vs + nvv) vs[nvv++] = v;
-				}
-			ntm = std::max(ntm, nt);
-			nvm = std::max(nvm, nvv);
+		for (size_t i = (size_t)k * kLanes; i < (size_t)(k + 1) * kLanes; i++) {
+			ntm = std::max<uint32_t>(ntm, lane_nt[i]);
+			nvm = std::max<uint32_t>(nvm, lane_nv[i]);
 		}
 		const uint32_t bytes = chunk_block_bytes(ntm, nvm);
 		if (total16 + bytes / 16 > 0xffffffffull) return fail(XFEM_ELIMIT, "chunk blocks exceed 64 GiB");
@@ -393,15 +502,36 @@ int build_device(xfem_body* h) {
 		for (uint32_t c = 0; c < ncol; c++) mc = std::max(mc, ccb[c + 1] - ccb[c]);
 		h->max_colour_chunks = mc;
 	}
+	// The first (lowest-colour) and the last (highest-colour) lane touching
+	// each vertex: the first advances it (its owner), the last finishes it
+	// when damping sweeps run; chunks are colour-major. Also the chunks
+	// touching each vertex (vertex -> chunk lists in increasing chunk order;
+	// one vertex appears at most once per chunk, since clusters of one colour
+	// share no vertex).
+	std::vector<uint32_t> owner(nverts, 0xffffffffu), last(nverts, 0xffffffffu), vc_off(nverts + 1, 0), vc;
+	for (size_t i = 0; i < nlanes; i++)
+		for (uint32_t sl = 0; sl < lane_nv[i]; sl++) {
+			const uint32_t dv = lane_dv[i * kMaxClusterVerts + sl];
+			if (owner[dv] == 0xffffffffu) owner[dv] = (uint32_t)i;
+			last[dv] = (uint32_t)i;
+			vc_off[dv + 1]++;
+		}
+	for (uint32_t v = 0; v < nverts; v++) vc_off[v + 1] += vc_off[v];
+	vc.resize(vc_off[nverts]);
+	{
+		std::vector<uint32_t> fill(vc_off.begin(), vc_off.end() - 1);
+		for (size_t i = 0; i < nlanes; i++)
+			for (uint32_t sl = 0; sl < lane_nv[i]; sl++) vc[fill[lane_dv[i * kMaxClusterVerts + sl]]++] = (uint32_t)(i / kLanes);
+	}
+	clk.lap("chunk shapes");
 	std::vector<float4> cblk((size_t)total16, make_float4(0, 0, 0, 0));
-	// owner of each vertex: the first (lowest-colour) cluster that touches it
-	std::vector<uint32_t> owner(nverts, 0xffffffffu);
-	std::vector<std::vector<uint32_t>> vert_chunks(nverts);
+	std::vector<uint32_t> lastmask(nlanes, 0);
 	for (auto& b : h->bodies) {
 		b.tet_slot.assign(b.nt, 0xffffffffu);
 		b.tet_rec.assign(b.nt, 0);
 	}
-	for (uint32_t k = 0; k < nch; k++) {
+	// packing: every chunk writes its own block and its own tets' entries
+	parallel_for(nch, [&](uint32_t k) {
 		const uint32_t ntm = shape_nt[k], nvm = shape_nv[k];
 		float4* rec = &cblk[meta[k].off16];
 		uint32_t* hdr = reinterpret_cast<uint32_t*>(rec + 128 * (size_t)ntm);
@@ -410,15 +540,16 @@ int build_device(xfem_body* h) {
 		for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++) {
 			const Lane& L = chunk_lanes[k][lane];
 			BodyHost& b = h->bodies[L.body];
-			uint32_t vs[kMaxClusterVerts], nvv = 0, ntt = 0;
+			const size_t i = (size_t)k * kLanes + lane;
+			const uint32_t* dvs = &lane_dv[i * kMaxClusterVerts];
+			const uint32_t nvv = lane_nv[i];
+			uint32_t ntt = 0;
 			for (uint32_t q = b.sched.cl_begin[L.cluster]; q < b.sched.cl_begin[L.cluster + 1]; q++, ntt++) {
 				const uint32_t t = b.sched.cl_tets[q];
 				uint32_t slots = 0;
 				for (int n = 0; n < 4; n++) {
-					const uint32_t v = b.tets[4 * (size_t)t + n];
-					uint32_t* f = std::find(vs, vs + nvv, v);
-					if (f == vs + nvv) vs[nvv++] = v;
-					slots |= (uint32_t)(f - vs) << (4 * n);
+					const uint32_t dv = b.vbase + b.sched.vert_rank[b.tets[4 * (size_t)t + n]];
+					slots |= (uint32_t)(std::find(dvs, dvs + nvv, dv) - dvs) << (4 * n);
 				}
 				slot[(size_t)ntt * kLanes + lane] = slots;
 				b.tet_slot[t] = (meta[k].trow + ntt) * kLanes + lane;
@@ -430,16 +561,13 @@ int build_device(xfem_body* h) {
 				r[3 * kLanes] = make_float4(e[12], e[13], e[14], tet_c0(b, t));
 				b.tet_rec[t] = meta[k].off16 + ((size_t)ntt * 4 + 3) * kLanes + lane;
 			}
-			uint32_t mask = 0;
-			for (uint32_t s = 0; s < nvv; s++) {
-				const uint32_t dv = b.vbase + b.sched.vert_rank[vs[s]];
-				vid[(size_t)s * kLanes + lane] = dv;
-				if (owner[dv] == 0xffffffffu) {
-					owner[dv] = k * kLanes + lane;
-					mask |= 1u << s;
-				}
-				if (vert_chunks[dv].empty() || vert_chunks[dv].back() != k) vert_chunks[dv].push_back(k);
+			uint32_t mask = 0, lm = 0;
+			for (uint32_t sl = 0; sl < nvv; sl++) {
+				vid[(size_t)sl * kLanes + lane] = dvs[sl];
+				if (owner[dvs[sl]] == i) mask |= 1u << sl;
+				if (last[dvs[sl]] == i) lm |= 1u << sl;
 			}
+			lastmask[i] = lm;
 			hdr[lane] = nvv | (ntt << 4) | (mask << 8) | (L.body << 16);
 		}
 		// the register-resident cube path needs every lane to be a canonical cube
@@ -451,24 +579,8 @@ int build_device(xfem_body* h) {
 				if (slot[(size_t)t * kLanes + lane] != kCube[t]) cube = false;
 		}
 		if (cube) meta[k].shape |= kShapeCube;
-	}
-	// the last (highest-colour) cluster touching each vertex
-	std::vector<uint32_t> lastmask((size_t)nch * kLanes, 0);
-	{
-		std::vector<uint32_t> last(nverts, 0xffffffffu);
-		for (int pass = 0; pass < 2; pass++)
-			for (uint32_t k = 0; k < nch; k++) {
-				const float4* rec = &cblk[meta[k].off16];
-				const uint32_t* hdr = reinterpret_cast<const uint32_t*>(rec + 128 * (size_t)shape_nt[k]);
-				const uint32_t* vid = hdr + kLanes;
-				for (uint32_t lane = 0; lane < chunk_lanes[k].size(); lane++)
-					for (uint32_t sl = 0; sl < (hdr[lane] & 15u); sl++) {
-						const uint32_t dv = vid[(size_t)sl * kLanes + lane];
-						if (pass == 0) last[dv] = k * kLanes + lane;  // chunks are colour-major
-						else if (last[dv] == k * kLanes + lane) lastmask[(size_t)k * kLanes + lane] |= 1u << sl;
-					}
-			}
-	}
+	});
+	clk.lap("chunk packing");
 	// The cube path takes its slots from a table: its bulk copy stops before
 	// the slot words at the end of the block.
 	max_bytes = 128;
@@ -480,27 +592,36 @@ int build_device(xfem_body* h) {
 	for (uint32_t v = 0; v < nverts; v++)
 		if (owner[v] == 0xffffffffu) isolated.push_back(v);
 	h->nisolated = (uint32_t)isolated.size();
-	// dataflow dependencies: chunks of other colours sharing a vertex
+	clk.lap("last masks");
+	// dataflow dependencies: the other chunks sharing a vertex, each marked
+	// when its colour is lower
 	std::vector<uint32_t> chunk_colour(nch), dep_begin(nch + 1, 0), deps;
 	for (uint32_t c = 0; c < ncol; c++)
 		for (uint32_t k = ccb[c]; k < ccb[c + 1]; k++) chunk_colour[k] = c;
 	{
 		std::vector<std::vector<uint32_t>> dl(nch);
-		for (uint32_t v = 0; v < nverts; v++)
-			for (uint32_t a : vert_chunks[v])
-				for (uint32_t b2 : vert_chunks[v])
-					if (a != b2) dl[a].push_back(b2);
+		parallel_for(nch, [&](uint32_t k) {
+			std::vector<uint32_t>& d = dl[k];
+			for (size_t i = (size_t)k * kLanes; i < (size_t)(k + 1) * kLanes; i++)
+				for (uint32_t sl = 0; sl < lane_nv[i]; sl++) {
+					const uint32_t dv = lane_dv[i * kMaxClusterVerts + sl];
+					for (uint32_t j = vc_off[dv]; j < vc_off[dv + 1]; j++)
+						if (vc[j] != k) d.push_back(vc[j]);
+				}
+			std::sort(d.begin(), d.end());
+			d.erase(std::unique(d.begin(), d.end()), d.end());
+			for (uint32_t& j : d) j |= chunk_colour[j] < chunk_colour[k] ? 0x80000000u : 0u;
+		});
 		uint32_t maxd = 0;
 		for (uint32_t k = 0; k < nch; k++) {
-			std::sort(dl[k].begin(), dl[k].end());
-			dl[k].erase(std::unique(dl[k].begin(), dl[k].end()), dl[k].end());
 			dep_begin[k] = (uint32_t)deps.size();
-			for (uint32_t j : dl[k]) deps.push_back(j | (chunk_colour[j] < chunk_colour[k] ? 0x80000000u : 0u));
+			deps.insert(deps.end(), dl[k].begin(), dl[k].end());
 			maxd = std::max(maxd, (uint32_t)dl[k].size());
 		}
 		dep_begin[nch] = (uint32_t)deps.size();
 		h->max_deps = maxd;
 	}
+	clk.lap("dataflow deps");
 	// vertex state: canonical (X, V) = (rest, 0); bits = lock | body << 8
 	std::vector<float4> vert(2 * (size_t)nverts);
 	std::vector<uint32_t> dev_of(nverts), tets_dev(4 * (size_t)ntets);
@@ -520,6 +641,7 @@ int build_device(xfem_body* h) {
 		params[bi] = make_params(b.settings);
 		params[bi].ntets = b.nt;
 	}
+	clk.lap("vertex state");
 	// upload
 	XCUDA(h->vert.alloc(vert.size()));
 	XCUDA(h->cblk.alloc(cblk.size()));
@@ -555,6 +677,7 @@ int build_device(xfem_body* h) {
 	XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
 	if (h->tlam.p) XCUDA(cudaMemsetAsync(h->tlam.p, 0, h->tlam.n * sizeof(float2), h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
+	clk.lap("upload");
 	h->device_bytes = vert.size() * 16 + cblk.size() * 16 + (ccb.size() + isolated.size() + dev_of.size() +
 	                  tets_dev.size() + dep_begin.size() + deps.size() + nch) * 4 + meta.size() * 16 + params.size() * sizeof(BodyParams) + h->stage.n * 4 + h->tlam.n * 8;
 	{
@@ -792,11 +915,12 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 		h->own_stream = true;
 	}
 	h->bodies.resize(nbodies);
-	for (uint32_t i = 0; i < nbodies; i++) {
-		const int rc = prepare_body(meshes[i], settings ? &settings[i] : nullptr, mode, morton, h->bodies[i]);
-		if (rc) return nbodies > 1 ? fail(rc, "body " + std::to_string(i) + ": " + g_err) : rc;
-	}
-	int rc = build_device(h.get());
+	SetupClock clk;
+	int rc = prepare_bodies(h.get(), nbodies, meshes, settings, mode, morton);
+	if (rc) return rc;
+	clk.lap("rest state + schedule");
+	rc = build_device(h.get());
+	clk.lap("device layout");
 	if (rc) return rc;
 	// default configuration until the first step tunes it
 	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1, h->opt.block_size ? (int)h->opt.block_size : 128);
@@ -1136,6 +1260,7 @@ int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, co
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
 	const int rc = prepare_mesh(m, b);
 	if (rc) return rc;
+	host_rest(m, b);
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());

@@ -10,80 +10,9 @@
 #include <vector>
 
 #include "xfem_internal.h"
+#include "xfem_rest.h"
 
 namespace xfem {
-
-namespace {
-
-// Small column-major 3x3 helpers in the reference's evaluation order
-// (GLSL-style mat3, XPBDFEM/vectormath.h:190-197, 501-526).
-struct M3 {
-	float c[3][3];  // c[column][row]
-};
-
-inline float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-
-// determinant(mat3), XPBDFEM/vectormath.cpp:34-39
-float det3(const M3& m) {
-	float a = m.c[0][0], b = m.c[1][0], c = m.c[2][0];
-	float d = m.c[0][1], e = m.c[1][1], f = m.c[2][1];
-	float g = m.c[0][2], h = m.c[1][2], i = m.c[2][2];
-	return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
-}
-
-// inverse(mat3), XPBDFEM/vectormath.cpp:40-58: adjugate in double rounded to
-// float, determinant and 1/det scaling in float.
-M3 inverse3(const M3& m) {
-	const double m00 = m.c[0][0], m01 = m.c[0][1], m02 = m.c[0][2];
-	const double m10 = m.c[1][0], m11 = m.c[1][1], m12 = m.c[1][2];
-	const double m20 = m.c[2][0], m21 = m.c[2][1], m22 = m.c[2][2];
-	M3 adj;
-	adj.c[0][0] = (float)(m11 * m22 - m12 * m21);
-	adj.c[0][1] = (float)-(m01 * m22 - m02 * m21);
-	adj.c[0][2] = (float)(m01 * m12 - m02 * m11);
-	adj.c[1][0] = (float)-(m10 * m22 - m12 * m20);
-	adj.c[1][1] = (float)(m00 * m22 - m02 * m20);
-	adj.c[1][2] = (float)-(m00 * m12 - m02 * m10);
-	adj.c[2][0] = (float)(m10 * m21 - m11 * m20);
-	adj.c[2][1] = (float)-(m00 * m21 - m01 * m20);
-	adj.c[2][2] = (float)(m00 * m11 - m01 * m10);
-	const float det = m.c[0][0] * adj.c[0][0] + m.c[0][1] * adj.c[1][0] + m.c[0][2] * adj.c[2][0];
-	const float s = 1.0f / det;
-	M3 out;
-	for (int c = 0; c < 3; c++)
-		for (int r = 0; r < 3; r++) out.c[c][r] = adj.c[c][r] * s;
-	return out;
-}
-
-// Map jacobian sum_n dN_n (x) P_n of the linear tet: column j, row n = P_n[j];
-// accumulating from a zero matrix normalises -0 to +0 (the "0.0f +").
-M3 map_jacobian(const float P[4][3]) {
-	M3 J;
-	for (int c = 0; c < 3; c++)
-		for (int r = 0; r < 3; r++) J.c[c][r] = 0.0f + P[r][c];
-	return J;
-}
-
-// column k of m as (m * e_k), the reference's mat3 * vec3 with a unit vector
-void column_of(const M3& m, int k, float out[3]) {
-	const float e[3] = {k == 0 ? 1.0f : 0.0f, k == 1 ? 1.0f : 0.0f, k == 2 ? 1.0f : 0.0f};
-	for (int r = 0; r < 3; r++) {
-		const float row[3] = {m.c[0][r], m.c[1][r], m.c[2][r]};
-		out[r] = dot3(row, e);
-	}
-}
-
-float face_area(const float P[4][3], int i0, int i1, int i2) {
-	float a[3], b[3];
-	for (int k = 0; k < 3; k++) {
-		a[k] = P[i0][k] - P[i2][k];
-		b[k] = P[i1][k] - P[i2][k];
-	}
-	const float c[3] = {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
-	return 0.5f * sqrtf(dot3(c, c));
-}
-
-}  // namespace
 
 int parse_tets(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& tets, uint32_t& nverts) {
 	tets.clear();
@@ -111,52 +40,11 @@ void init_rest(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32
 			mx[k] = fmaxf(mx[k], nodes[3 * (size_t)i + k]);
 		}
 	}
-	for (uint32_t i = 0; i < nverts; i++) {
-		uint8_t f = 1u << 4;
-		const float rel = (nodes[3 * (size_t)i] - mn[0]) / (mx[0] - mn[0]);
-		if (rel < 0.02f) f |= 1u;
-		if (rel > 0.98f) f |= 2u;
-		vflags[i] = f;
-	}
-	const float sixth = 1.0f / 6.0f;
+	for (uint32_t i = 0; i < nverts; i++) vflags[i] = rest::vertex_flags(nodes[3 * (size_t)i], mn[0], mx[0]);
 	for (uint32_t t = 0; t < ntets; t++) {
 		const uint32_t* is = tets + 4 * (size_t)t;
-		// P[n] = vec3(X[n] - X[root]) with X the node data widened to double
-		float P[4][3];
-		for (int n = 0; n < 4; n++)
-			for (int k = 0; k < 3; k++)
-				P[n][k] = (float)((double)nodes[3 * (size_t)is[n] + k] - (double)nodes[3 * (size_t)is[3] + k]);
-		const M3 J = map_jacobian(P);
-		const M3 Qi = inverse3(J);
-		// GeneratePrefactoredCoefficients<Tet> (XPBDFEM/Fem.cpp:131-161): four
-		// identical quadrature points of weight 0.25
-		float QQ[3] = {0, 0, 0}, QR[3] = {0, 0, 0}, vsum = 0.0f;
-		for (int p = 0; p < 4; p++) {
-			const M3 Ji = inverse3(J);
-			const float wq = det3(J) * sixth * 0.25f;
-			float q[3][3];
-			for (int i = 0; i < 3; i++) column_of(Ji, i, q[i]);
-			vsum += wq;
-			for (int i = 0; i < 3; i++) QQ[i] += wq * dot3(q[i], q[i]);
-			int head = 0;
-			for (int i = 0; i < 3; i++)
-				for (int j = i + 1; j < 3; j++) QR[head++] += wq * 2.0f * dot3(q[i], q[j]);
-		}
-		for (int i = 0; i < 3; i++) QQ[i] /= vsum;
-		for (int i = 0; i < 3; i++) QR[i] /= vsum;
-		const float vol = sixth * det3(J);
-		const float area = face_area(P, 0, 1, 2) + face_area(P, 1, 3, 2) + face_area(P, 0, 2, 3) + face_area(P, 3, 1, 0);
-		float* o = ep + 17 * (size_t)t;
-		for (int c = 0; c < 3; c++)
-			for (int r = 0; r < 3; r++) o[c * 3 + r] = Qi.c[c][r];
-		for (int i = 0; i < 3; i++) {
-			o[9 + i] = QQ[i];
-			o[12 + i] = QR[i];
-		}
-		o[15] = vol;
-		o[16] = area;
-		// lumped mass, LumpsTet4 (XPBDFEM/Fem.cpp:217-223), accumulated per node
-		const float dm = (1.0f / 4.0f) * density * vol;
+		// lumped mass accumulated per node in tet order
+		const float dm = rest::tet(nodes, is, density, ep + 17 * (size_t)t);
 		for (int n = 0; n < 4; n++) w[is[n]] += dm;
 	}
 	for (uint32_t i = 0; i < nverts; i++) w[i] = 1.0f / w[i];  // XPBDFEM/Geo.cpp:744
@@ -212,13 +100,6 @@ void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float
 
 namespace {
 
-uint32_t morton_code(uint32_t x, uint32_t y, uint32_t z) {
-	uint32_t c = 0;
-	for (int b = 0; b < 10; b++)
-		c |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
-	return c;
-}
-
 bool tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v || tv[2] == v || tv[3] == v; }
 
 }  // namespace
@@ -239,16 +120,19 @@ bool tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v |
 //     vertex id; or the identity;
 //  5. inside a colour, clusters by (Morton code of their centroid, id), or
 //     (smallest vertex id, id) without Morton order.
-int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
-                   uint32_t morton, Schedule& s) {
-	std::vector<uint32_t> off(nverts + 1, 0), lst(4 * (size_t)ntets);
+void incidence(const uint32_t* tets, uint32_t nverts, uint32_t ntets, std::vector<uint32_t>& off,
+               std::vector<uint32_t>& lst) {
+	off.assign(nverts + 1, 0);
+	lst.resize(4 * (size_t)ntets);
 	for (size_t i = 0; i < 4 * (size_t)ntets; i++) off[tets[i] + 1]++;
 	for (uint32_t v = 0; v < nverts; v++) off[v + 1] += off[v];
-	{
-		std::vector<uint32_t> fill(off.begin(), off.end() - 1);
-		for (uint32_t t = 0; t < ntets; t++)
-			for (int n = 0; n < 4; n++) lst[fill[tets[4 * (size_t)t + n]]++] = t;
-	}
+	std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+	for (uint32_t t = 0; t < ntets; t++)
+		for (int n = 0; n < 4; n++) lst[fill[tets[4 * (size_t)t + n]]++] = t;
+}
+
+int cluster_and_colour(const uint32_t* tets, uint32_t ntets, const uint32_t* off, const uint32_t* lst, uint32_t mode,
+                       Schedule& s) {
 	const uint32_t kNone = 0xffffffffu;
 	std::vector<uint32_t> cluster_of(ntets, kNone);
 	s.cl_begin.clear();
@@ -302,19 +186,22 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 	s.cl_begin.push_back((uint32_t)s.cl_tets.size());
 	s.nclusters = nc;
 
-	// greedy colouring
+	// greedy colouring, over each cluster's distinct vertices
 	s.cl_colour.assign(nc, 0);
 	std::vector<uint32_t> mark(kMaxColours, kNone);
 	uint32_t ncol = 0;
 	for (uint32_t k = 0; k < nc; k++) {
+		uint32_t vs[4 * kMaxClusterTets], nvs = 0;
 		for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++) {
 			const uint32_t* tv = tets + 4 * (size_t)s.cl_tets[q];
 			for (int n = 0; n < 4; n++)
-				for (uint32_t j = off[tv[n]]; j < off[tv[n] + 1]; j++) {
-					const uint32_t o = cluster_of[lst[j]];
-					if (o < k) mark[s.cl_colour[o]] = k;
-				}
+				if (std::find(vs, vs + nvs, tv[n]) == vs + nvs) vs[nvs++] = tv[n];
 		}
+		for (uint32_t i = 0; i < nvs; i++)
+			for (uint32_t j = off[vs[i]]; j < off[vs[i] + 1]; j++) {
+				const uint32_t o = cluster_of[lst[j]];
+				if (o < k) mark[s.cl_colour[o]] = k;
+			}
 		uint32_t c = 0;
 		while (c < kMaxColours && mark[c] == k) c++;
 		if (c == kMaxColours) return -1;
@@ -322,61 +209,48 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 		ncol = std::max(ncol, c + 1);
 	}
 	s.ncolours = ncol;
+	return 0;
+}
 
-	// vertex rank
-	s.vert_rank.resize(nverts);
-	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-	float sc[3] = {0.0f, 0.0f, 0.0f};
-	auto quantise = [&](const float* p3) {
-		uint32_t q[3];
+MortonFrame morton_frame(const float* nodes, uint32_t nverts) {
+	MortonFrame f;
+	for (int k = 0; k < 3; k++) {
+		f.mn[k] = INFINITY;
+		f.mx[k] = -INFINITY;
+	}
+	for (uint32_t v = 0; v < nverts; v++)
 		for (int k = 0; k < 3; k++) {
-			const float f = (p3[k] - mn[k]) * sc[k];
-			const uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
-			q[k] = u > 1023u ? 1023u : u;
+			const float x = nodes[3 * (size_t)v + k];
+			f.mn[k] = x < f.mn[k] ? x : f.mn[k];
+			f.mx[k] = x > f.mx[k] ? x : f.mx[k];
 		}
-		return morton_code(q[0], q[1], q[2]);
-	};
-	if (morton) {
-		for (uint32_t v = 0; v < nverts; v++)
-			for (int k = 0; k < 3; k++) {
-				const float x = nodes[3 * (size_t)v + k];
-				mn[k] = x < mn[k] ? x : mn[k];
-				mx[k] = x > mx[k] ? x : mx[k];
-			}
-		// one scale for all axes (the largest extent), so the curve's cells are
-		// cubes and consecutive clusters form compact blocks on any box shape
-		float ext = 0.0f;
-		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
-		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
-		std::vector<uint64_t> key(nverts);
-		for (uint32_t v = 0; v < nverts; v++) key[v] = ((uint64_t)quantise(nodes + 3 * (size_t)v) << 32) | v;
-		std::sort(key.begin(), key.end());
-		for (uint32_t i = 0; i < nverts; i++) s.vert_rank[(uint32_t)key[i]] = i;
-	} else {
-		for (uint32_t v = 0; v < nverts; v++) s.vert_rank[v] = v;
-	}
+	// one scale for all axes (the largest extent), so the curve's cells are
+	// cubes and consecutive clusters form compact blocks on any box shape
+	f.set_scale();
+	return f;
+}
 
-	// cluster order inside each colour: Morton code of the cluster's centroid
-	// (the mean of its tets' vertex positions, summed tet by tet in float); it
-	// sits inside a curve cell, where a corner would sit on a cell boundary
-	// and flip bits with rounding. Without Morton order: smallest vertex id.
-	std::vector<std::pair<uint64_t, uint32_t>> ck(nc);
-	for (uint32_t k = 0; k < nc; k++) {
-		uint32_t key = kNone;
-		if (morton) {
-			float c[3] = {0.0f, 0.0f, 0.0f};
-			for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++)
-				for (int n = 0; n < 4; n++)
-					for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)tets[4 * (size_t)s.cl_tets[q] + n] + j];
-			const float cnt = (float)(4u * (s.cl_begin[k + 1] - s.cl_begin[k]));
-			for (int j = 0; j < 3; j++) c[j] = c[j] / cnt;
-			key = quantise(c);
-		} else {
-			for (uint32_t q = s.cl_begin[k]; q < s.cl_begin[k + 1]; q++)
-				for (int n = 0; n < 4; n++) key = std::min(key, tets[4 * (size_t)s.cl_tets[q] + n]);
-		}
-		ck[k] = {((uint64_t)s.cl_colour[k] << 32) | key, k};
+void vertex_ranks(const float* nodes, uint32_t nverts, uint32_t morton, Schedule& s) {
+	s.vert_rank.resize(nverts);
+	if (!morton) {
+		for (uint32_t v = 0; v < nverts; v++) s.vert_rank[v] = v;
+		return;
 	}
+	const MortonFrame f = morton_frame(nodes, nverts);
+	std::vector<uint64_t> key(nverts);
+	for (uint32_t v = 0; v < nverts; v++) key[v] = ((uint64_t)f.code(nodes + 3 * (size_t)v) << 32) | v;
+	std::sort(key.begin(), key.end());
+	for (uint32_t i = 0; i < nverts; i++) s.vert_rank[(uint32_t)key[i]] = i;
+}
+
+void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t morton, Schedule& s) {
+	const uint32_t nc = s.nclusters, ncol = s.ncolours;
+	const MortonFrame f = morton ? morton_frame(nodes, nverts) : MortonFrame{};
+	std::vector<std::pair<uint64_t, uint32_t>> ck(nc);
+	for (uint32_t k = 0; k < nc; k++)
+		ck[k] = {((uint64_t)s.cl_colour[k] << 32) | cluster_key(nodes, tets, s.cl_tets.data() + s.cl_begin[k],
+		                                                         s.cl_begin[k + 1] - s.cl_begin[k], morton, f),
+		         k};
 	std::sort(ck.begin(), ck.end());
 	s.colour_cl.resize(nc);
 	s.colour_cl_begin.assign(ncol + 1, 0);
@@ -385,6 +259,15 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 		s.colour_cl_begin[s.cl_colour[ck[i].second] + 1]++;
 	}
 	for (uint32_t c = 0; c < ncol; c++) s.colour_cl_begin[c + 1] += s.colour_cl_begin[c];
+}
+
+int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
+                   uint32_t morton, Schedule& s) {
+	std::vector<uint32_t> off, lst;
+	incidence(tets, nverts, ntets, off, lst);
+	if (cluster_and_colour(tets, ntets, off.data(), lst.data(), mode, s)) return -1;
+	vertex_ranks(nodes, nverts, morton, s);
+	cluster_order(nodes, nverts, tets, morton, s);
 	return 0;
 }
 

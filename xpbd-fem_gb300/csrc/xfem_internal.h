@@ -7,6 +7,8 @@
 
 #include <vector>
 
+#include "xfem_rest.h"
+
 namespace xfem {
 
 // Limits of one cluster: the tets processed in sequence by one GPU thread.
@@ -44,9 +46,38 @@ struct Schedule {
 
 // Clusters (mode 0: one tet each; mode 1: edge stars), greedy colouring,
 // Morton vertex order (morton != 0) and cluster order inside each colour.
-// Returns 0 or -1 when a limit is exceeded.
+// Returns 0 or -1 when a limit is exceeded. The phases, which the GPU set-up
+// path (xfem_setup.cu) shares or replaces one by one:
 int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t mode,
                    uint32_t morton, Schedule& s);
+// vertex -> tets in increasing tet id (CSR: off[nverts + 1], lst[4 ntets])
+void incidence(const uint32_t* tets, uint32_t nverts, uint32_t ntets, std::vector<uint32_t>& off,
+               std::vector<uint32_t>& lst);
+// the greedy clusters and colours in tet / cluster id order (sequential by
+// definition); fills nclusters, cl_begin, cl_tets, cl_colour, ncolours
+int cluster_and_colour(const uint32_t* tets, uint32_t ntets, const uint32_t* off, const uint32_t* lst, uint32_t mode,
+                       Schedule& s);
+// vert_rank (Morton rank, or the identity)
+void vertex_ranks(const float* nodes, uint32_t nverts, uint32_t morton, Schedule& s);
+// colour_cl, colour_cl_begin
+void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t morton, Schedule& s);
+
+// ---- GPU set-up path (xfem_setup.cu) ------------------------------------------
+// The parallel phases of the set-up on the device, bit for bit the host's:
+// rest state (init_rest), incidence, Morton vertex ranks (vertex_ranks) and
+// the cluster order (cluster_order). Return a cudaError_t value (0 = ok).
+struct GpuSetupMesh {
+	std::vector<float> ep, w0;        // as init_rest
+	std::vector<uint8_t> vflags;
+	std::vector<uint32_t> off, lst;   // as incidence
+	std::vector<uint32_t> vert_rank;  // as vertex_ranks
+	MortonFrame frame;                // the curve's frame for the cluster order
+};
+int gpu_setup_mesh(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, float density,
+                   uint32_t morton, GpuSetupMesh& out, void* stream);
+// s: clusters and colours from cluster_and_colour; fills colour_cl, colour_cl_begin
+int gpu_cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, uint32_t morton,
+                      const MortonFrame& f, Schedule& s, void* stream);
 
 // ---- device-side structures ------------------------------------------------
 // Material and step parameters of one body (uploaded on create / set_settings).

@@ -1,0 +1,202 @@
+// Set-up arithmetic shared by the host (xfem_host.cpp) and the GPU set-up
+// kernels (xfem_setup.cu), so that both run the same operations in the same
+// order. The reference's rest-state precompute of one linear tet:
+// InitTriTetFiniteElement (XPBDFEM/Fem.cpp:196-224) with
+// GeneratePrefactoredCoefficients (XPBDFEM/Fem.cpp:131-161) and
+// inverse(mat3) (XPBDFEM/vectormath.cpp:40-58).
+// Bit-exact with the reference as long as nothing is fused: the host compiles
+// with -ffp-contract=off, the device with -fmad=false, and float division and
+// square root are correctly rounded on both (IEEE).
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define XFEM_HD __host__ __device__ __forceinline__
+#else
+#define XFEM_HD inline
+#endif
+
+namespace xfem {
+namespace rest {
+
+// Column-major 3x3 as the reference's GLSL-style mat3 (XPBDFEM/vectormath.h:190-197).
+struct M3 {
+	float c[3][3];  // c[column][row]
+};
+
+XFEM_HD float dot3(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// determinant(mat3), XPBDFEM/vectormath.cpp:34-39
+XFEM_HD float det3(const M3& m) {
+	float a = m.c[0][0], b = m.c[1][0], c = m.c[2][0];
+	float d = m.c[0][1], e = m.c[1][1], f = m.c[2][1];
+	float g = m.c[0][2], h = m.c[1][2], i = m.c[2][2];
+	return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+
+// inverse(mat3): adjugate in double rounded to float, determinant and 1/det
+// scaling in float.
+XFEM_HD M3 inverse3(const M3& m) {
+	const double m00 = m.c[0][0], m01 = m.c[0][1], m02 = m.c[0][2];
+	const double m10 = m.c[1][0], m11 = m.c[1][1], m12 = m.c[1][2];
+	const double m20 = m.c[2][0], m21 = m.c[2][1], m22 = m.c[2][2];
+	M3 adj;
+	adj.c[0][0] = (float)(m11 * m22 - m12 * m21);
+	adj.c[0][1] = (float)-(m01 * m22 - m02 * m21);
+	adj.c[0][2] = (float)(m01 * m12 - m02 * m11);
+	adj.c[1][0] = (float)-(m10 * m22 - m12 * m20);
+	adj.c[1][1] = (float)(m00 * m22 - m02 * m20);
+	adj.c[1][2] = (float)-(m00 * m12 - m02 * m10);
+	adj.c[2][0] = (float)(m10 * m21 - m11 * m20);
+	adj.c[2][1] = (float)-(m00 * m21 - m01 * m20);
+	adj.c[2][2] = (float)(m00 * m11 - m01 * m10);
+	const float det = m.c[0][0] * adj.c[0][0] + m.c[0][1] * adj.c[1][0] + m.c[0][2] * adj.c[2][0];
+	const float s = 1.0f / det;
+	M3 out;
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) out.c[c][r] = adj.c[c][r] * s;
+	return out;
+}
+
+// Map jacobian sum_n dN_n (x) P_n of the linear tet: column j, row n = P_n[j];
+// accumulating from a zero matrix normalises -0 to +0 (the "0.0f +").
+XFEM_HD M3 map_jacobian(const float P[4][3]) {
+	M3 J;
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) J.c[c][r] = 0.0f + P[r][c];
+	return J;
+}
+
+// column k of m as (m * e_k), the reference's mat3 * vec3 with a unit vector
+XFEM_HD void column_of(const M3& m, int k, float out[3]) {
+	const float e[3] = {k == 0 ? 1.0f : 0.0f, k == 1 ? 1.0f : 0.0f, k == 2 ? 1.0f : 0.0f};
+	for (int r = 0; r < 3; r++) {
+		const float row[3] = {m.c[0][r], m.c[1][r], m.c[2][r]};
+		out[r] = dot3(row, e);
+	}
+}
+
+// FaceArea of InitTriTetFiniteElement (XPBDFEM/Fem.cpp:211-213)
+XFEM_HD float face_area(const float P[4][3], int i0, int i1, int i2) {
+	float a[3], b[3];
+	for (int k = 0; k < 3; k++) {
+		a[k] = P[i0][k] - P[i2][k];
+		b[k] = P[i1][k] - P[i2][k];
+	}
+	const float c[3] = {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
+	return 0.5f * sqrtf(dot3(c, c));
+}
+
+// One tet: o[17] = Qi column-major, QQ, QR, volume, surfaceArea; returns the
+// mass (1/4) density volume that each of its nodes receives (LumpsTet4,
+// XPBDFEM/Fem.cpp:217-223). `nodes` is the float node array, `is` the tet's
+// four vertex ids.
+XFEM_HD float tet(const float* nodes, const uint32_t* is, float density, float* o) {
+	const float sixth = 1.0f / 6.0f;
+	// P[n] = vec3(X[n] - X[root]) with X the node data widened to double
+	float P[4][3];
+	for (int n = 0; n < 4; n++)
+		for (int k = 0; k < 3; k++)
+			P[n][k] = (float)((double)nodes[3 * (size_t)is[n] + k] - (double)nodes[3 * (size_t)is[3] + k]);
+	const M3 J = map_jacobian(P);
+	const M3 Qi = inverse3(J);
+	// GeneratePrefactoredCoefficients<Tet>: four quadrature points with the
+	// same gradients, so the same inverse and weight (det J / 6) / 4 at each;
+	// the four additions stay four additions
+	const float wq = det3(J) * sixth * 0.25f;
+	float q[3][3];
+	for (int i = 0; i < 3; i++) column_of(Qi, i, q[i]);
+	float QQ[3] = {0, 0, 0}, QR[3] = {0, 0, 0}, vsum = 0.0f;
+	for (int p = 0; p < 4; p++) {
+		vsum += wq;
+		for (int i = 0; i < 3; i++) QQ[i] += wq * dot3(q[i], q[i]);
+		int head = 0;
+		for (int i = 0; i < 3; i++)
+			for (int j = i + 1; j < 3; j++) QR[head++] += wq * 2.0f * dot3(q[i], q[j]);
+	}
+	for (int i = 0; i < 3; i++) QQ[i] /= vsum;
+	for (int i = 0; i < 3; i++) QR[i] /= vsum;
+	const float vol = sixth * det3(J);
+	const float area = face_area(P, 0, 1, 2) + face_area(P, 1, 3, 2) + face_area(P, 0, 2, 3) + face_area(P, 3, 1, 0);
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) o[c * 3 + r] = Qi.c[c][r];
+	for (int i = 0; i < 3; i++) {
+		o[9 + i] = QQ[i];
+		o[12 + i] = QR[i];
+	}
+	o[15] = vol;
+	o[16] = area;
+	return (1.0f / 4.0f) * density * vol;
+}
+
+// The Left / Right flags of a vertex (XPBDFEM/Geo.cpp:713-727) from the AABB
+// of the node data along x: bit 0 Left, bit 1 Right, bit 4 Pickable.
+XFEM_HD uint8_t vertex_flags(float x, float mn, float mx) {
+	uint8_t f = 1u << 4;
+	const float rel = (x - mn) / (mx - mn);
+	if (rel < 0.02f) f |= 1u;
+	if (rel > 0.98f) f |= 2u;
+	return f;
+}
+
+}  // namespace rest
+
+// Morton order of the schedule (vertex ranks and cluster order inside a
+// colour), shared by the host and the GPU set-up: integer and float steps
+// that give the same result on both and on x86-64 and AArch64.
+XFEM_HD uint32_t morton_code(uint32_t x, uint32_t y, uint32_t z) {
+	uint32_t c = 0;
+	for (int b = 0; b < 10; b++)
+		c |= (((x >> b) & 1u) << (3 * b)) | (((y >> b) & 1u) << (3 * b + 1)) | (((z >> b) & 1u) << (3 * b + 2));
+	return c;
+}
+
+// The curve's frame: the AABB of the node data and one scale for all axes
+// (the largest extent, 10 bits per axis).
+struct MortonFrame {
+	float mn[3] = {0.0f, 0.0f, 0.0f}, mx[3] = {0.0f, 0.0f, 0.0f}, sc[3] = {0.0f, 0.0f, 0.0f};
+
+	XFEM_HD void set_scale() {
+		float ext = 0.0f;
+		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
+		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
+	}
+
+	XFEM_HD uint32_t code(const float* p3) const {
+		uint32_t q[3];
+		for (int k = 0; k < 3; k++) {
+			const float f = (p3[k] - mn[k]) * sc[k];
+			const uint32_t u = f > 0.0f ? (uint32_t)f : 0u;
+			q[k] = u > 1023u ? 1023u : u;
+		}
+		return morton_code(q[0], q[1], q[2]);
+	}
+};
+
+// Sort key of a cluster inside its colour: the Morton code of its centroid
+// (the mean of its tets' vertex positions, summed tet by tet in float; it
+// sits inside a curve cell, where a corner would sit on a cell boundary and
+// flip bits with rounding), or without Morton order its smallest vertex id.
+XFEM_HD uint32_t cluster_key(const float* nodes, const uint32_t* tets, const uint32_t* cl_tets, uint32_t nt,
+                             uint32_t morton, const MortonFrame& f) {
+	if (morton) {
+		float c[3] = {0.0f, 0.0f, 0.0f};
+		for (uint32_t q = 0; q < nt; q++)
+			for (int n = 0; n < 4; n++)
+				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)tets[4 * (size_t)cl_tets[q] + n] + j];
+		const float cnt = (float)(4u * nt);
+		for (int j = 0; j < 3; j++) c[j] = c[j] / cnt;
+		return f.code(c);
+	}
+	uint32_t key = 0xffffffffu;
+	for (uint32_t q = 0; q < nt; q++)
+		for (int n = 0; n < 4; n++) {
+			const uint32_t v = tets[4 * (size_t)cl_tets[q] + n];
+			key = v < key ? v : key;
+		}
+	return key;
+}
+
+}  // namespace xfem

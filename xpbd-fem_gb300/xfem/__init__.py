@@ -59,7 +59,7 @@ class Options(C.Structure):
     _fields_ = [
         ("cluster_mode", C.c_uint32), ("no_morton", C.c_uint32), ("sync_mode", C.c_uint32),
         ("block_size", C.c_uint32), ("keep_lambdas", C.c_uint32), ("device", C.c_int32),
-        ("stream", C.c_void_p),
+        ("stream", C.c_void_p), ("host_setup", C.c_uint32),
     ]
 
 
@@ -209,10 +209,12 @@ def compute_schedule(node_data, idx_data, cluster_mode=0, morton=True):
                 clusters=ncl.value)
 
 
-def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None):
+def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None,
+             host_setup=False):
     o = Options()
     o.cluster_mode, o.no_morton, o.sync_mode = cluster_mode, 0 if morton else 1, sync_mode
     o.block_size, o.keep_lambdas, o.device, o.stream = block_size, 1 if keep_lambdas else 0, device, stream
+    o.host_setup = 1 if host_setup else 0
     return o
 
 
