@@ -20,7 +20,8 @@ shape the configuration names.
   "batched": 512 bodies in one launch per frame against one launch per body,
   "damped": the same mesh with the reference web UI's default damping against
   undamped, "models": the same mesh at nu = 0.45 with Mixed, YeohSkin, Pixar
-  and one volume pass against MixedSel,
+  and one volume pass against MixedSel, "setup": wall time of a handle's
+  set-up (GPU set-up path and host set-up, 1.5M-tet mesh; 512-body batch),
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -293,6 +294,7 @@ def run_xfem(args, world, rank, local):
     adjoint = None if args.no_adjoint else run_adjoint(stream)
     damped = None if args.no_damped else run_damped(stream)
     models = None if args.no_models else run_models(stream)
+    setup = None if args.no_setup else run_setup(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -314,6 +316,7 @@ def run_xfem(args, world, rank, local):
         "adjoint": adjoint,
         "damped": damped,
         "models": models,
+        "setup": setup,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -497,6 +500,30 @@ def time_frames(stream, w, settings, flush, frames):
             "block": info["block_size"]}
 
 
+def run_setup(stream):
+    """Wall time of a handle's set-up (rest state, schedule, device layout,
+    uploads; xfem_create / xfem_batch_create) for the throughput mesh with the
+    GPU set-up path and with the host set-up, and for the 512-body batch.
+    The reference's GeoLinear3d::Init of the same mesh takes about 2 s."""
+    import xfem
+    from xfem import workloads as W
+    sp = C_void_p(stream.cuda_stream)
+    w = W.throughput()
+    out = {"unit": "s"}
+    for key, host in (("throughput", False), ("throughput_host_setup", True)):
+        t = time.perf_counter()
+        b = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], stream=sp, host_setup=host)
+        out[key] = time.perf_counter() - t
+        b.close()
+    wb = W.batched()
+    t = time.perf_counter()
+    b = xfem.Body(meshes=wb["meshes"], settings=wb["settings"], stream=sp)
+    out["batched_512"] = time.perf_counter() - t
+    b.close()
+    out["workload"] = w["name"] + "; " + wb["name"] + " (%d tets)" % sum(m[1].size // 5 for m in wb["meshes"])
+    return out
+
+
 def run_models(stream, frames=5):
     """The throughput mesh at nu = 0.45 (the Pixar models need nu < 0.5) with
     the other energy models and with volume passes, against MixedSel (the hot
@@ -544,6 +571,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-damped", action="store_true")
     ap.add_argument("--no-models", action="store_true")
+    ap.add_argument("--no-setup", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")
