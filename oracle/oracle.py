@@ -26,6 +26,9 @@ ENERGY_MIXED_SEL = 4
 ENERGY_YEOH_SKIN = 5
 ENERGY_YEOH_SKIN_SEL = 6
 ENERGY_YEOH_SKIN_FAST = 7
+ENERGY_CONTINUOUS_PIXAR = 8
+ENERGY_CONTINUOUS_MIXED = 9
+ENERGY_CONTINUOUS_SKIN = 10
 ENERGY_CUBE_NEO = 11
 ENERGY_CUBE_SKIN = 12
 REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
@@ -126,6 +129,9 @@ def lib():
         L.orc_volume_d.restype = C.c_double
         L.orc_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P, P, P]
         L.orc_adjoint_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, u32, P, P, P, P, P, P]
+        L.orc_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
+        L.orc_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
+        L.orc_ring_schedule.argtypes = [P, u32, P, u32, u32, P, P, P]
         _lib = L
     return _lib
 
@@ -213,6 +219,41 @@ def substeps(X, V, w, tets, ep, order, nsub, params, lock_mask=None, tet_mu=None
         raise ValueError("oracle substep failed (unsupported energy model?)")
     out = (X.reshape(-1, 3), V.reshape(-1, 3), w, contact)
     return out + (lam.reshape(-1, 2),) if want_lambdas else out
+
+
+def substeps_rings(X, V, w, tets, ep, torder, vorder, nsub, params, lock_mask=None, dtype=np.float32):
+    """nsub substeps of a continuous-pressure model (energy 8-10): every
+    vertex's one-ring solved in `vorder`, PBD damping over the tets in
+    `torder`. Returns X, V, w, contact mask."""
+    X = np.array(X, np.float64).reshape(-1).copy()
+    V = np.array(V, np.float64).reshape(-1).copy()
+    w = np.array(w, dtype).copy()
+    nv = w.size
+    tets = np.ascontiguousarray(tets, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    torder = np.ascontiguousarray(torder, np.uint32)
+    vorder = np.ascontiguousarray(vorder, np.uint32)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    contact = np.zeros(nv, np.uint8)
+    f = lib().orc_substeps_rings_f if dtype == np.float32 else lib().orc_substeps_rings_d
+    if f(nv, _p(X), _p(V), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep), _p(torder), _p(vorder), nsub,
+         C.byref(params), _p(contact)):
+        raise ValueError("not a continuous-pressure energy model")
+    return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+
+def ring_schedule(nodes, tets, morton=1):
+    """Vertex ring order of the continuous-pressure models (colour-major) and
+    the colour offsets."""
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    nv = nodes.size // 3
+    vorder = np.zeros(nv, np.uint32)
+    cb = np.zeros(nv + 1, np.uint32)
+    ncol = C.c_uint32()
+    if lib().orc_ring_schedule(_p(nodes), nv, _p(tets), tets.shape[0], morton, _p(vorder), _p(cb), C.byref(ncol)):
+        raise ValueError("ring schedule limits exceeded")
+    return dict(vert_order=vorder, colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
 
 
 def volume(X, tets, dtype=np.float32):

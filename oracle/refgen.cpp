@@ -45,6 +45,12 @@
  *       Settings::volumePasses: GeoLinear3d::Constrain then runs that many
  *       SolveElementVolume sweeps over the order after the solve
  *       (XPBDFEM/Geo.cpp:780-783).
+ *   rings  (arguments as `damped`) < torder.u32 vorder.u32
+ *       `damped` with a continuous-pressure energy (8-10): stdin holds the
+ *       tet order and then the vertex order (each u32 count, then the ids),
+ *       which replace tOrder and vOrder; GeoLinear3d::Constrain then solves
+ *       the one-rings in that vertex order (XPBDFEM/Geo.cpp:784-787) and
+ *       GeoLinear3d::Damp damps them in it (XPBDFEM/Geo.cpp:800-806).
  */
 #include <cstdio>
 #include <cstdlib>
@@ -160,7 +166,7 @@ int main(int argc, char** argv) {
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
 
 	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered") ||
-	    !strcmp(cmd, "damped")) {
+	    !strcmp(cmd, "damped") || !strcmp(cmd, "rings")) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
 		uint32_t W = U(2), H = U(3), D = U(4);
 		vec3 scale(F(5), F(6), F(7));
@@ -188,7 +194,8 @@ int main(int argc, char** argv) {
 		float compliance = F(a++), poisson = F(a++), gx = F(a++), gy = F(a++), dt = F(a++);
 		uint32_t nsub = U(a++), lockLeft = U(a++);
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
-		const bool damped = !strcmp(cmd, "damped");
+		const bool rings = !strcmp(cmd, "rings");
+		const bool damped = !strcmp(cmd, "damped") || rings;
 		if (damped) {
 			s.damping = F(a++);
 			s.pbdDamping = F(a++);
@@ -221,6 +228,11 @@ int main(int argc, char** argv) {
 			uint32_t n = 0;
 			if (fread(&n, 4, 1, stdin) != 1 || n != g->con.tetCount) { fprintf(stderr, "bad order\n"); return 3; }
 			if (fread(g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+		}
+		if (rings) {
+			uint32_t n = 0;
+			if (fread(&n, 4, 1, stdin) != 1 || n != g->con.vertCount) { fprintf(stderr, "bad vertex order\n"); return 3; }
+			if (fread(g->vOrder, 4, n, stdin) != n) { fprintf(stderr, "short vertex order\n"); return 3; }
 		}
 		for (uint32_t k = 0; k < nsub; k++) {
 			s.tickId = k;

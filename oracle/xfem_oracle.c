@@ -12,6 +12,70 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* ---- one-rings (integer; shared by both instantiations) ------------------ */
+/* The one-ring of every vertex as OneRingConstructor builds it
+ * (XPBDFEM/Connectivity.h:114-160), filled as GeoLinear3d::Init fills it
+ * (XPBDFEM/Geo.cpp:747-757): the vertex's tets in increasing id (the order
+ * Connectivity3d::Init lists them, XPBDFEM/Connectivity.cpp:437-439); the
+ * ring's nodes, the vertex first, then each tet's vertices in order of first
+ * appearance; and for each tet corner its node index. */
+typedef struct {
+	uint32_t* tet_off;  /* nv + 1, into tet_list */
+	uint32_t* tet_list;
+	uint32_t* node_off; /* nv + 1, into nodes */
+	uint32_t* nodes;
+	uint16_t* corner;   /* 4 per tet_list entry */
+} orc_rings;
+
+static void rings_free(orc_rings* r) {
+	free(r->tet_off);
+	free(r->tet_list);
+	free(r->node_off);
+	free(r->nodes);
+	free(r->corner);
+}
+
+static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings* r) {
+	memset(r, 0, sizeof(*r));
+	r->tet_off = (uint32_t*)calloc((size_t)nv + 1, 4);
+	r->node_off = (uint32_t*)calloc((size_t)nv + 1, 4);
+	r->tet_list = (uint32_t*)malloc(4 * (size_t)(nt ? 4 * nt : 1));
+	r->corner = (uint16_t*)malloc(2 * (size_t)(nt ? 16 * nt : 1));
+	r->nodes = (uint32_t*)malloc(4 * (size_t)(nt ? 16 * nt + nv : nv + 1));
+	if (!r->tet_off || !r->node_off || !r->tet_list || !r->corner || !r->nodes) return -1;
+	for (size_t i = 0; i < 4 * (size_t)nt; i++) r->tet_off[tets[i] + 1]++;
+	for (uint32_t v = 0; v < nv; v++) r->tet_off[v + 1] += r->tet_off[v];
+	uint32_t* fill = (uint32_t*)malloc(4 * ((size_t)nv + 1));
+	if (!fill) return -1;
+	memcpy(fill, r->tet_off, 4 * (size_t)nv);
+	for (uint32_t t = 0; t < nt; t++)
+		for (int n = 0; n < 4; n++) r->tet_list[fill[tets[4 * (size_t)t + n]]++] = t;
+	free(fill);
+	uint32_t head = 0;
+	for (uint32_t v = 0; v < nv; v++) {
+		r->node_off[v] = head;
+		uint32_t* nodes = r->nodes + head;
+		uint32_t cnt = 1;
+		nodes[0] = v;
+		for (uint32_t j = r->tet_off[v]; j < r->tet_off[v + 1]; j++) {
+			const uint32_t* tv = tets + 4 * (size_t)r->tet_list[j];
+			for (int n = 0; n < 4; n++) {
+				uint32_t k = cnt;
+				for (uint32_t q = 0; q < cnt; q++)
+					if (nodes[q] == tv[n]) {
+						k = q;
+						break;
+					}
+				if (k == cnt) nodes[cnt++] = tv[n];
+				r->corner[4 * (size_t)j + n] = (uint16_t)k;
+			}
+		}
+		head += cnt;
+	}
+	r->node_off[nv] = head;
+	return 0;
+}
+
 /* ---- float instantiation (reference semantics) ---------------------------- */
 #define R float
 #define SFX _f
@@ -268,6 +332,106 @@ static int kv_cmp(const void* a, const void* b) {
 	return x->id < y->id ? -1 : (x->id > y->id);
 }
 
+/* Vertex ranks: (Morton code of the rest position over the AABB with one
+ * scale, the largest extent; vertex id), or the identity. mn, sc: the frame. */
+static int orc_vertex_ranks(const float* nodes, uint32_t nv, uint32_t morton, uint32_t* vert_rank, float mn[3],
+                            float sc[3]) {
+	float mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+	if (!morton) {
+		for (uint32_t v = 0; v < nv; v++) vert_rank[v] = v;
+		return 0;
+	}
+	for (uint32_t v = 0; v < nv; v++)
+		for (int k = 0; k < 3; k++) {
+			float x = nodes[3 * (size_t)v + k];
+			if (x < mn[k]) mn[k] = x;
+			if (x > mx[k]) mx[k] = x;
+		}
+	float ext = 0.0f;
+	for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
+	for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
+	orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
+	if (!kv) return -1;
+	for (uint32_t v = 0; v < nv; v++) {
+		kv[v].key = orc_quantise(nodes + 3 * (size_t)v, mn, sc);
+		kv[v].id = v;
+	}
+	qsort(kv, nv, sizeof(orc_kv), kv_cmp);
+	for (uint32_t i = 0; i < nv; i++) vert_rank[kv[i].id] = i;
+	free(kv);
+	return 0;
+}
+
+int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t morton,
+                      uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours) {
+	orc_rings rg;
+	if (rings_build(tets, nt, nv, &rg)) {
+		rings_free(&rg);
+		return -1;
+	}
+	/* the vertices whose ring holds each node */
+	const uint32_t ne = rg.node_off[nv];
+	uint32_t* ho = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* hl = (uint32_t*)malloc(4 * (size_t)(ne ? ne : 1));
+	uint32_t* colour = (uint32_t*)malloc(4 * (size_t)(nv ? nv : 1));
+	uint32_t* mark = (uint32_t*)malloc(4 * (size_t)ORC_MAXCOL);
+	uint32_t* rank = (uint32_t*)malloc(4 * (size_t)(nv ? nv : 1));
+	orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
+	int rc = -1;
+	if (!ho || !hl || !colour || !mark || !rank || !kv) goto done;
+	for (uint32_t i = 0; i < ne; i++) ho[rg.nodes[i] + 1]++;
+	for (uint32_t v = 0; v < nv; v++) ho[v + 1] += ho[v];
+	{
+		uint32_t* f = (uint32_t*)malloc(4 * ((size_t)nv + 1));
+		if (!f) goto done;
+		memcpy(f, ho, 4 * (size_t)nv);
+		for (uint32_t v = 0; v < nv; v++)
+			for (uint32_t i = rg.node_off[v]; i < rg.node_off[v + 1]; i++) hl[f[rg.nodes[i]]++] = v;
+		free(f);
+	}
+	/* greedy colouring in id order: rings of one colour share no node */
+	uint32_t ncol = 0;
+	for (uint32_t c = 0; c < ORC_MAXCOL; c++) mark[c] = 0xffffffffu;
+	for (uint32_t u = 0; u < nv; u++) {
+		for (uint32_t i = rg.node_off[u]; i < rg.node_off[u + 1]; i++) {
+			const uint32_t x = rg.nodes[i];
+			for (uint32_t j = ho[x]; j < ho[x + 1]; j++)
+				if (hl[j] < u) mark[colour[hl[j]]] = u;
+		}
+		uint32_t c = 0;
+		while (c < ORC_MAXCOL && mark[c] == u) c++;
+		if (c == ORC_MAXCOL) goto done;
+		colour[u] = c;
+		if (c + 1 > ncol) ncol = c + 1;
+	}
+	{
+		float mn[3] = {INFINITY, INFINITY, INFINITY}, sc[3] = {0.0f, 0.0f, 0.0f};
+		if (orc_vertex_ranks(nodes, nv, morton, rank, mn, sc)) goto done;
+	}
+	for (uint32_t v = 0; v < nv; v++) {
+		kv[v].key = ((uint64_t)colour[v] << 32) | rank[v];
+		kv[v].id = v;
+	}
+	qsort(kv, nv, sizeof(orc_kv), kv_cmp);
+	for (uint32_t c = 0; c <= ncol; c++) colour_begin[c] = 0;
+	for (uint32_t i = 0; i < nv; i++) {
+		vorder[i] = kv[i].id;
+		colour_begin[colour[kv[i].id] + 1]++;
+	}
+	for (uint32_t c = 0; c < ncol; c++) colour_begin[c + 1] += colour_begin[c];
+	*ncolours = ncol;
+	rc = 0;
+done:
+	free(ho);
+	free(hl);
+	free(colour);
+	free(mark);
+	free(rank);
+	free(kv);
+	rings_free(&rg);
+	return rc;
+}
+
 int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t mode, uint32_t morton,
                  uint32_t* cluster_of, uint32_t* cluster_count, uint32_t* colour_of_cluster, uint32_t* ncolours,
                  uint32_t* vert_rank, uint32_t* tet_order, uint32_t* colour_tet_begin) {
@@ -349,32 +513,9 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
 	}
 	*ncolours = ncol;
 	/* 3. vertex order */
-	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+	float mn[3] = {INFINITY, INFINITY, INFINITY};
 	float sc[3] = {0.0f, 0.0f, 0.0f};
-	if (morton) {
-		for (uint32_t v = 0; v < nv; v++)
-			for (int k = 0; k < 3; k++) {
-				float x = nodes[3 * (size_t)v + k];
-				if (x < mn[k]) mn[k] = x;
-				if (x > mx[k]) mx[k] = x;
-			}
-		// one scale for all axes (the largest extent), so the curve's cells are
-		// cubes and consecutive clusters form compact blocks on any box shape
-		float ext = 0.0f;
-		for (int k = 0; k < 3; k++) ext = (mx[k] - mn[k]) > ext ? (mx[k] - mn[k]) : ext;
-		for (int k = 0; k < 3; k++) sc[k] = ext > 0.0f ? 1023.0f / ext : 0.0f;
-		orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
-		if (!kv) return -1;
-		for (uint32_t v = 0; v < nv; v++) {
-			kv[v].key = orc_quantise(nodes + 3 * (size_t)v, mn, sc);
-			kv[v].id = v;
-		}
-		qsort(kv, nv, sizeof(orc_kv), kv_cmp);
-		for (uint32_t i = 0; i < nv; i++) vert_rank[kv[i].id] = i;
-		free(kv);
-	} else {
-		for (uint32_t v = 0; v < nv; v++) vert_rank[v] = v;
-	}
+	if (orc_vertex_ranks(nodes, nv, morton, vert_rank, mn, sc)) return -1;
 	/* 4. cluster order inside each colour: (colour, Morton code of the
 	 * centroid of the cluster's tet vertices, id); without Morton order,
 	 * (colour, smallest vertex id, id) */

@@ -136,6 +136,18 @@ int orc_substeps_threaded_f(uint32_t nv, double* X, double* V, float* w, const u
                             const uint32_t* order, const uint32_t* colour_begin, uint32_t ncolours,
                             uint32_t nsub, const orc_params* p, uint32_t threads);
 
+/* Substeps with a continuous-pressure model (energy 8-10; XPBDFEM/Geo.cpp:
+ * 147-193, 774-811; XPBDFEM/Fem.cpp:942-979; XPBDFEM/Geo.cpp:12-64): each
+ * substep solves every vertex's one-ring in `vorder` (nv), then the rings'
+ * post-step Rayleigh damping in `vorder` and the PBD damping over the tets in
+ * `torder` (nt). Returns 0, or -1 for another energy model. */
+int orc_substeps_rings_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                         const uint32_t* tets, const float* ep, const uint32_t* torder, const uint32_t* vorder,
+                         uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
+                         const uint32_t* tets, const double* ep, const uint32_t* torder, const uint32_t* vorder,
+                         uint32_t nsub, const orc_params* p, uint8_t* contact);
+
 /* CalculateVolume (XPBDFEM/Geo.cpp:827-832, XPBDFEM/Fem.cpp:1066). */
 float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets);
 double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets);
@@ -165,6 +177,16 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
                  uint32_t* cluster_of, uint32_t* cluster_count, uint32_t* colour_of_cluster,
                  uint32_t* ncolours, uint32_t* vert_rank, uint32_t* tet_order,
                  uint32_t* colour_tet_begin);
+
+/* Ring schedule of the continuous-pressure models: vertices coloured greedily
+ * in id order so that the rings of one colour share no node (the smallest
+ * colour not used by an earlier vertex whose ring shares a node with this
+ * one's), then ordered inside each colour by vertex rank (Morton rank of the
+ * rest position with morton != 0, else the id). Outputs vorder[nv] (the
+ * flattened ring order, colour-major), colour_begin[ncolours + 1] (caller
+ * allocates nv + 1). Returns 0, or -1 if a limit is exceeded. */
+int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t morton,
+                      uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours);
 
 #ifdef __cplusplus
 }

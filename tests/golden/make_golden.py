@@ -121,6 +121,25 @@ CASES = [
                                     0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 3]),
     ("volume_wonky_pixar_1_post_pbd_star", ["damped", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
                                             -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
+    # continuous-pressure models (one constraint pair per vertex one-ring,
+    # XPBDFEM/Geo.cpp:147-193): the `damped` arguments, with the vertex ring
+    # order of the GPU schedule (and the tet order for the PBD damping)
+    ("rings_c1_cpixar_nu045_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                    0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("rings_c1_cmixed_nu045_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                    0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("rings_c1_cmixed_incompressible_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
+                                             0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("rings_c1_cskin_nu049_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
+                                   0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("rings_wonky_cmixed_paper_star", ["rings", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
+                                       -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05]),
+    ("rings_c1_cskin_limit_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("rings_c1_cmixed_amortized_pbd_star", ["rings", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
+                                            0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("rings_wonky_cpixar_post_star", ["rings", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
+                                      -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
 ]
 
 
@@ -155,7 +174,7 @@ def main():
         argv = [REFGEN] + [str(a) for a in args]
         stdin = None
         extra = {}
-        if args[0] in ("ordered", "damped"):
+        if args[0] in ("ordered", "damped", "rings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]
             nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), 0, wonk)
@@ -166,12 +185,17 @@ def main():
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
             manifest_mode = mode
+            if args[0] == "rings":
+                rs = oracle.ring_schedule(nodes, tets, morton=1)
+                vorder = rs["vert_order"].astype(np.uint32)
+                stdin += struct.pack("<I", vorder.size) + vorder.tobytes()
+                extra.update(vorder=vorder, colour_vert_begin=rs["colour_vert_begin"])
         r = subprocess.run(argv, input=stdin, stdout=subprocess.PIPE, check=True)
         arrays = parse(r.stdout)
         arrays.update(extra)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
         manifest[name] = {"args": args}
-        if args[0] in ("ordered", "damped"):
+        if args[0] in ("ordered", "damped", "rings"):
             manifest[name]["schedule_mode"] = manifest_mode
         print(f"{name}: " + ", ".join(f"{k}{list(v.shape)}" for k, v in arrays.items()))
     manifest = {n: manifest[n] for n, _ in CASES if n in manifest}

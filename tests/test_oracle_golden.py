@@ -147,6 +147,61 @@ def test_damped_substeps_bit_exact(orc, name):
     assert not np.array_equal(Xu.reshape(-1), g["xn"])
 
 
+RINGS = ["rings_c1_cpixar_nu045_star", "rings_c1_cmixed_nu045_star", "rings_c1_cmixed_incompressible_star",
+         "rings_c1_cskin_nu049_star", "rings_wonky_cmixed_paper_star", "rings_c1_cskin_limit_star",
+         "rings_c1_cmixed_amortized_pbd_star", "rings_wonky_cpixar_post_star"]
+
+
+@pytest.mark.parametrize("name", RINGS)
+def test_ring_substeps_bit_exact(orc, name):
+    """The continuous-pressure models: every vertex's one-ring solved in the
+    fixture's vertex order (XPBDFEM/Geo.cpp:147-193, 774-811;
+    XPBDFEM/Fem.cpp:942-979; XPBDFEM/Geo.cpp:12-64), with damping where the
+    fixture has it; and the ring schedule restatement reproduces the order."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[8], a[16]
+    tets, nv = orc.parse_tets(g["idx"])
+    rs = orc.ring_schedule(g["nodes"], tets, morton=1)
+    assert np.array_equal(rs["vert_order"], g["vorder"])
+    assert np.array_equal(rs["colour_vert_begin"], g["colour_vert_begin"])
+    ep, w, fl = orc.init_rest(g["nodes"], tets, dens)
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lock_mask = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.substeps_rings(X0, V0, w, tets, ep, g["order"], g["vorder"], 1,
+                                       damped_params(orc, a, g["derived"], 0), lock_mask=lock_mask)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.substeps_rings(X1, V1, w1, tets, ep, g["order"], g["vorder"], nsub - 1,
+                                      damped_params(orc, a, g["derived"], 1), lock_mask=lock_mask)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+
+
+def test_ring_schedule_is_a_valid_colouring(orc):
+    """Rings of one colour share no node, on a jittered shuffled mesh."""
+    rng = np.random.default_rng(4)
+    nodes, idx = orc.gen_tet_block(5, 4, 3, (0.1, 0.1, 0.1), 1, 0.3)
+    tets, nv = orc.parse_tets(idx)
+    perm = rng.permutation(tets.shape[0])
+    tets = tets[perm]
+    rs = orc.ring_schedule(nodes, tets, morton=1)
+    assert np.array_equal(np.sort(rs["vert_order"]), np.arange(nv))
+    ring = [set() for _ in range(nv)]
+    for t in tets:
+        for v in t:
+            ring[v].update(int(x) for x in t)
+    for v in range(nv):
+        ring[v].add(v)
+    cb = rs["colour_vert_begin"]
+    for c in range(cb.size - 1):
+        seen = set()
+        for v in rs["vert_order"][cb[c]:cb[c + 1]]:
+            assert not (ring[v] & seen), c
+            seen |= ring[v]
+
+
 def test_cube_models_leave_tets_untouched(orc):
     """SolveElementCube acts on quads and hexes only: on a tet mesh the
     substep is free fall (XPBDFEM/Fem.cpp:568-838)."""
@@ -156,7 +211,8 @@ def test_cube_models_leave_tets_untouched(orc):
 
 def test_continuous_models_refused(orc):
     """The continuous-pressure models (8-10) run a per-vertex ring solve,
-    not an element solve: the element restatement refuses them."""
+    not an element solve: the element restatement refuses them (and the ring
+    restatement refuses element models)."""
     g = golden("solve_pixar_nu045")
     for e in (8, 9, 10):
         p = orc.make_params(dt=1 / 1200, compliance=0.01, poisson=0.45, energy=e)
