@@ -61,7 +61,9 @@ extern "C" {
 #define XFEM_ENERGY_YEOH_SKIN 5u       /* Energy_YeohSkin */
 #define XFEM_ENERGY_YEOH_SKIN_SEL 6u   /* Energy_YeohSkinSel (= YeohSkin on a linear tet) */
 #define XFEM_ENERGY_YEOH_SKIN_FAST 7u  /* Energy_YeohSkinFast */
-                                       /* 8-10: continuous-pressure models, XFEM_EUNSUPPORTED */
+#define XFEM_ENERGY_CONTINUOUS_PIXAR 8u /* continuous pressure: one constraint per vertex one-ring */
+#define XFEM_ENERGY_CONTINUOUS_MIXED 9u /* likewise, the deviatoric + hydrostatic pair */
+#define XFEM_ENERGY_CONTINUOUS_SKIN 10u /* likewise, with the Yeoh deviatoric term */
 #define XFEM_ENERGY_CUBE_NEO 11u       /* Energy_CubeNeo: acts on quads and hexes, so on no tet */
 #define XFEM_ENERGY_CUBE_SKIN 12u      /* Energy_CubeSkin: likewise */
 #define XFEM_MAX_VOLUME_PASSES 64u     /* largest xfem_settings::volume_passes accepted */
@@ -278,6 +280,20 @@ int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, co
 int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                           uint32_t idx_data_count, uint32_t cluster_mode, uint32_t no_morton, uint32_t* vert_rank,
                           uint32_t* tet_order, uint32_t* colour_begin, uint32_t* ncolours, uint32_t* nclusters);
+/* The ring schedule of the continuous-pressure models (energy 8-10), whose
+ * GeoLinear3d::Constrain solves one constraint pair per vertex over the tets
+ * around it (XPBDFEM/Geo.cpp:147-193, 784-787; the vertex order vOrder,
+ * XPBDFEM/Geo.cpp:759-771, is replaced by it): vertices coloured so that the
+ * one-rings of a colour share no vertex, in caller ids, colour-major;
+ * colour_begin needs room for vertices + 1 entries. Any output may be NULL.
+ * xfem_get_ring_schedule reads a handle's (XFEM_EUNSUPPORTED for a body that
+ * is not in one-ring mode); xfem_compute_ring_schedule computes the one
+ * xfem_create_ex would build, without a GPU. */
+int xfem_get_ring_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_order, uint32_t* colour_begin,
+                           uint32_t* ncolours);
+int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                               uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_order,
+                               uint32_t* colour_begin, uint32_t* ncolours);
 
 /* ---- helpers --------------------------------------------------------------- */
 /* volumeAndTimeCorrectedPbdDamping and its amortized form for a substep of

@@ -1,6 +1,7 @@
 """GPU energy models beyond MixedSel / YeohSkinFast, and volume passes.
 
-SolveElement's dispatch on a linear tet (XPBDFEM/Fem.cpp:872-888): the Pixar
+SolveElement's dispatch on a linear tet (XPBDFEM/Fem.cpp:872-888; the
+continuous-pressure models 8-10 are in test_gpu_rings.py): the Pixar
 models (SolveElementPixar, XPBDFEM/Fem.cpp:361-433), Mixed, YeohSkin and
 YeohSkinSel (the quadrature branch of SolveElementMixed, XPBDFEM/Fem.cpp:
 459-522), the cube models (no constraint on a tet) and ids above 12
@@ -205,11 +206,6 @@ def test_switch_models_between_calls():
 
 def test_unsupported_models_and_limits():
     nodes, idx = W.box(3, 2, 2, 0.05)
-    for e in (8, 9, 10):
-        s = xfem.default_settings(flags=(e << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT))
-        with pytest.raises(xfem.XfemError) as ex:
-            xfem.Body(nodes, idx, 1000.0, s)
-        assert ex.value.code == xfem.EUNSUPPORTED
     s = xfem.default_settings(flags=(xfem.ENERGY_PIXAR << xfem.ENERGY_BIT), poissons_ratio=0.5)
     with pytest.raises(xfem.XfemError) as ex:
         xfem.Body(nodes, idx, 1000.0, s)

@@ -160,3 +160,20 @@ def test_pbd_damping_coefficients_match_reference(name):
     vc, avc = xfem.pbd_damping_coefficients(pbd, dt, spacing)
     for got, want in ((vc, g["derived"][0]), (avc, g["derived"][1]), (xfem.time_corrected_drag(drag, dt), g["derived"][2])):
         assert abs(np.float32(got) - want) <= 2 * np.spacing(np.float32(want)), (got, want)
+
+
+@pytest.mark.parametrize("morton", [True, False])
+@pytest.mark.parametrize("mesh", ["box", "jitter"])
+def test_ring_schedule_bit_exact_vs_oracle(orc, morton, mesh):
+    """The ring schedule of the continuous-pressure models (one-rings of one
+    colour share no vertex) equals the oracle's independent restatement."""
+    if mesh == "box":
+        nodes, idx = xfem.generate_tet_block(9, 5, 4, (0.1, 0.1, 0.1))
+    else:
+        nodes, idx = _random_mesh(7, 6, 5, 4)
+    s = xfem.compute_ring_schedule(nodes, idx, morton=morton)
+    tets, _ = orc.parse_tets(idx)
+    o = orc.ring_schedule(nodes, tets, morton=int(morton))
+    assert s["colours"] == o["colours"]
+    assert np.array_equal(s["vert_order"], o["vert_order"])
+    assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])

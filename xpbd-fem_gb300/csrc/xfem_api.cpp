@@ -45,6 +45,7 @@ struct BodyHost {
 	std::vector<float> tet_mu;        // empty = uniform material
 	xfem_settings settings;
 	Schedule sched;
+	RingSchedule rings;               // continuous-pressure models only
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
 };
@@ -108,6 +109,11 @@ struct xfem_body {
 	DevBuf<uint32_t> lastmask;      // per chunk lane: slots whose last solve it makes
 	DevBuf<uint8_t> pass_on;        // [damping kind][tick % 8][colour]
 	DevBuf<float> tet_vol_dev, tet_inv_mu, io;
+	// one-ring mode (continuous-pressure models)
+	bool ring_mode = false;
+	DevBuf<uint4> ring_hdr;
+	DevBuf<uint32_t> ring_node, ring_cb;
+	DevBuf<float4> ring_ent;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -127,8 +133,8 @@ struct xfem_body {
 namespace {
 
 // How the solve treats an energy id on linear tets (TSolveElement's
-// dispatch, XPBDFEM/Fem.cpp:872-888); kModelNone + 1 for the
-// continuous-pressure ids 8-10, which run a per-vertex ring solve.
+// dispatch, XPBDFEM/Fem.cpp:872-888; the continuous-pressure ids 8-10 run a
+// per-vertex ring solve, GeoLinear3d::Constrain, XPBDFEM/Geo.cpp:784-787).
 uint32_t model_of(uint32_t energy) {
 	switch (energy) {
 	case XFEM_ENERGY_PIXAR:
@@ -142,7 +148,7 @@ uint32_t model_of(uint32_t energy) {
 	case XFEM_ENERGY_CUBE_SKIN: return kModelNone;
 	case 8u:
 	case 9u:
-	case 10u: return kModelNone + 1u;
+	case 10u: return kModelRing;
 	default: return kModelNeo;  // MixedSel, and every id above 12
 	}
 }
@@ -150,9 +156,12 @@ uint32_t model_of(uint32_t energy) {
 int validate_settings(const xfem_settings& s) {
 	const uint32_t energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	const uint32_t model = model_of(energy);
-	if (model > kModelNone)
-		return fail(XFEM_EUNSUPPORTED, "energy model " + std::to_string(energy) +
-		                                   " (continuous pressure: a per-vertex ring solve) is not supported");
+	const uint32_t rtype = (s.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u;
+	if (model == kModelRing && ((rtype >= XFEM_RAYLEIGH_POST && s.damping > 0.0f) || s.pbd_damping > 0.0f))
+		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) run no post-step damping here "
+		                               "(Rayleigh types 2, 3 with damping > 0, or pbd_damping > 0)");
+	if (energy == 8u && !(s.poissons_ratio < 0.5f))
+		return fail(XFEM_EINVAL, "ContinuousPixar needs poissons_ratio < 0.5 (lambda = 2 / (1 - 2 nu))");
 	if (s.volume_passes > XFEM_MAX_VOLUME_PASSES)
 		return fail(XFEM_EINVAL, "volume_passes must be at most " + std::to_string(XFEM_MAX_VOLUME_PASSES));
 	if (model == kModelPixar && !(s.poissons_ratio < 0.5f))
@@ -180,7 +189,8 @@ BodyParams make_params(const xfem_settings& s) {
 	for (int k = 0; k < 3; k++) p.yeoh[k] = s.yeoh[k];
 	p.energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	p.model = model_of(p.energy);
-	if (p.model == kModelPixar) {
+	p.lambda = lambda;
+	if (p.model == kModelPixar || p.energy == 8u) {
 		// SolveElementPixar's own material (XPBDFEM/Fem.cpp:367-368): mu = 2
 		const float lp = 2.0f / (1.0f - 2.0f * nu);
 		p.a = 1.0f + 2.0f / lp;
@@ -331,23 +341,35 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	}
 	rc = validate_settings(b.settings);
 	if (rc) return rc;
+	const bool ring = model_of((b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK) == kModelRing;
+	std::vector<uint32_t> off, lst;
 	if (!gpu) {
 		host_rest(m, b);
-		if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, mode, morton, b.sched))
+		incidence(b.tets.data(), b.nv, b.nt, off, lst);
+		if (cluster_and_colour(b.tets.data(), b.nt, off.data(), lst.data(), mode, b.sched))
 			return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
-		return XFEM_OK;
+		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
+		cluster_order(b.nodes.data(), b.nv, b.tets.data(), morton, b.sched);
+	} else {
+		GpuSetupMesh g;
+		int e = gpu_setup_mesh(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, morton, g, stream);
+		if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
+		b.ep = std::move(g.ep);
+		b.w0 = std::move(g.w0);
+		b.vflags = std::move(g.vflags);
+		if (cluster_and_colour(b.tets.data(), b.nt, g.off.data(), g.lst.data(), mode, b.sched))
+			return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
+		b.sched.vert_rank = std::move(g.vert_rank);
+		e = gpu_cluster_order(b.nodes.data(), b.nv, b.tets.data(), b.nt, morton, g.frame, b.sched, stream);
+		if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
+		off = std::move(g.off);
+		lst = std::move(g.lst);
 	}
-	GpuSetupMesh g;
-	int e = gpu_setup_mesh(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, morton, g, stream);
-	if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
-	b.ep = std::move(g.ep);
-	b.w0 = std::move(g.w0);
-	b.vflags = std::move(g.vflags);
-	if (cluster_and_colour(b.tets.data(), b.nt, g.off.data(), g.lst.data(), mode, b.sched))
-		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
-	b.sched.vert_rank = std::move(g.vert_rank);
-	e = gpu_cluster_order(b.nodes.data(), b.nv, b.tets.data(), b.nt, morton, g.frame, b.sched, stream);
-	if (e) return fail(XFEM_ECUDA, std::string("GPU set-up: ") + cudaGetErrorString((cudaError_t)e));
+	if (ring) {
+		const int rc2 = build_ring_schedule(b.tets.data(), b.nv, off.data(), lst.data(), b.sched.vert_rank.data(), b.rings);
+		if (rc2 == -2) return fail(XFEM_ELIMIT, "a vertex one-ring has more than 64 tets or 32 vertices");
+		if (rc2) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
+	}
 	return XFEM_OK;
 }
 
@@ -421,6 +443,65 @@ int prepare_bodies(xfem_body* h, uint32_t nb, const xfem_mesh* meshes, const xfe
 struct Lane {
 	uint32_t body, cluster;
 };
+
+// Whether a body of a one-ring handle damps in the solve (Paper, Limit): the
+// ring kernel with damping compiled in is launched.
+bool ring_damp_of(const std::vector<BodyHost>& bodies) {
+	for (const BodyHost& b : bodies)
+		if (b.settings.damping > 0.0f && ((b.settings.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u) < XFEM_RAYLEIGH_POST)
+			return true;
+	return false;
+}
+
+// The rings of every body in device order (colour-major, bodies in order):
+// per ring a header, its nodes (device vertex ids) and per ring tet its
+// prefactored I1 coefficients, volume and corner node indices.
+int build_rings(xfem_body* h) {
+	uint32_t ncol = 0;
+	for (const BodyHost& b : h->bodies) ncol = std::max(ncol, b.rings.ncolours);
+	std::vector<uint4> hdr;
+	std::vector<uint32_t> node, cb(ncol + 1, 0);
+	std::vector<float4> ent;
+	for (uint32_t c = 0; c < ncol; c++) {
+		cb[c] = (uint32_t)hdr.size();
+		for (uint32_t bi = 0; bi < (uint32_t)h->bodies.size(); bi++) {
+			const BodyHost& b = h->bodies[bi];
+			const RingSchedule& rs = b.rings;
+			if (c >= rs.ncolours) continue;
+			for (uint32_t i = rs.colour_begin[c]; i < rs.colour_begin[c + 1]; i++) {
+				const uint32_t v = rs.order[i];
+				const uint32_t nn = rs.node_off[v + 1] - rs.node_off[v], nt = rs.tet_off[v + 1] - rs.tet_off[v];
+				hdr.push_back(make_uint4((uint32_t)node.size(), (uint32_t)(ent.size() / 2), nn | (nt << 8) | (bi << 16), 0u));
+				for (uint32_t n = rs.node_off[v]; n < rs.node_off[v + 1]; n++)
+					node.push_back(b.vbase + b.sched.vert_rank[rs.nodes[n]]);
+				for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++) {
+					const float* e = &b.ep[17 * (size_t)rs.tets[j]];
+					uint32_t cn = 0;
+					for (int k = 0; k < 4; k++) cn |= (uint32_t)rs.corner[4 * (size_t)j + k] << (8 * k);
+					ent.push_back(make_float4(e[9], e[10], e[11], e[12]));
+					ent.push_back(make_float4(e[13], e[14], e[15], __builtin_bit_cast(float, cn)));
+				}
+			}
+		}
+	}
+	cb[ncol] = (uint32_t)hdr.size();
+	XCUDA(h->ring_hdr.alloc(hdr.size()));
+	XCUDA(h->ring_node.alloc(node.size()));
+	XCUDA(h->ring_ent.alloc(ent.size()));
+	XCUDA(h->ring_cb.alloc(cb.size()));
+	auto up = [&](void* dst, const void* src, size_t bytes) {
+		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+	};
+	XCUDA(up(h->ring_hdr.p, hdr.data(), hdr.size() * sizeof(uint4)));
+	XCUDA(up(h->ring_node.p, node.data(), node.size() * 4));
+	XCUDA(up(h->ring_ent.p, ent.data(), ent.size() * sizeof(float4)));
+	XCUDA(up(h->ring_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	h->ctx.ring_colours = ncol;
+	h->ctx.rings = (uint32_t)hdr.size();
+	h->device_bytes += hdr.size() * 16 + node.size() * 4 + ent.size() * 16 + cb.size() * 4;
+	return XFEM_OK;
+}
 
 // Packs every body's schedule into the merged device layout and uploads it.
 int build_device(xfem_body* h) {
@@ -730,6 +811,10 @@ int build_device(xfem_body* h) {
 		h->device_bytes += (uint64_t)trows * kLanes * 8 + 4;
 		h->device_bytes += (uint64_t)ntets * 16 + h->io.n * 4;
 	}
+	if (h->ring_mode) {
+		int rr = build_rings(h);
+		if (rr) return rr;
+	}
 	DevCtx& c = h->ctx;
 	c.vert = h->vert.p;
 	c.cblk = h->cblk.p;
@@ -768,6 +853,11 @@ int build_device(xfem_body* h) {
 	c.err = h->err.p;
 	h->cfg.lambdas = h->opt.keep_lambdas != 0;
 	h->cfg.ext = c.ext != 0u;
+	c.ring_hdr = h->ring_hdr.p;
+	c.ring_node = h->ring_node.p;
+	c.ring_ent = h->ring_ent.p;
+	c.colour_ring_begin = h->ring_cb.p;
+	if (h->ring_mode) c.ext = ring_damp_of(h->bodies) ? 1u : 0u;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -918,6 +1008,12 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	SetupClock clk;
 	int rc = prepare_bodies(h.get(), nbodies, meshes, settings, mode, morton);
 	if (rc) return rc;
+	uint32_t nring = 0;
+	for (const BodyHost& b : h->bodies)
+		nring += model_of((b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK) == kModelRing ? 1u : 0u;
+	if (nring && nring != nbodies)
+		return fail(XFEM_EUNSUPPORTED, "continuous-pressure models (energy 8-10) and element models cannot share a handle");
+	h->ring_mode = nring > 0;
 	clk.lap("rest state + schedule");
 	rc = build_device(h.get());
 	clk.lap("device layout");
@@ -943,6 +1039,11 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
 	if (nsub == 0) return XFEM_OK;
 	XCUDA(cudaSetDevice(h->device));
+	if (h->ring_mode) {
+		const int e = launch_rings(h->ctx, 256, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
+		return XFEM_OK;
+	}
 	int rc = autotune(h, nsub, dt);
 	if (rc) return rc;
 	if (h->ctx.ext && h->cfg.sync_mode == 3) {
@@ -1070,6 +1171,9 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	if (!s) return fail(XFEM_EINVAL, "null settings");
 	int rc = validate_settings(*s);
 	if (rc) return rc;
+	if ((model_of((s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK) == kModelRing) != h->ring_mode)
+		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
+		                               "element models needs a new handle (their schedules differ)");
 	const bool material = s->compliance != b->settings.compliance;
 	b->settings = *s;
 	XCUDA(cudaSetDevice(h->device));
@@ -1099,6 +1203,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 			if (persistent_grid(h->cfg, &blocks) == 0) h->cfg.blocks = blocks;
 		}
 	}
+	if (h->ring_mode) h->ctx.ext = ring_damp_of(h->bodies) ? 1u : 0u;
 	if (material && b->tet_mu.empty()) return update_material(h, *b);
 	return XFEM_OK;
 }
@@ -1127,6 +1232,8 @@ int xfem_set_lock_mask(xfem_body* h, uint32_t body, const uint8_t* mask) {
 int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
+	if (h->ring_mode && mu)
+		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) take the body's material only");
 	if (mu) {
 		for (uint32_t t = 0; t < b->nt; t++)
 			if (!(mu[t] > 0.0f) || !isfinite(mu[t])) return fail(XFEM_EINVAL, "tet mu must be finite and > 0");
@@ -1152,6 +1259,8 @@ int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, f
 	const uint64_t n = (uint64_t)frames * substeps;
 	if (n == 0) return XFEM_OK;
 	if (n > 0xffffffffull) return fail(XFEM_EINVAL, "too many substeps in one call");
+	if (h->ring_mode)
+		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) have no allocation-free launch");
 	XCUDA(cudaSetDevice(h->device));
 	int dev_err = 0;
 	const int e = launch_substeps_noalloc(h->ctx, h->cfg.block, h->cfg.warp_smem, h->cfg.lambdas, (uint32_t)n, dt,
@@ -1281,6 +1390,36 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
 		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
 	if (nclusters) *nclusters = b.sched.nclusters;
 	return xfem_get_schedule(&tmp, 0, vert_rank, tet_order, colour_begin, ncolours);
+}
+
+static int ring_schedule_out(const RingSchedule& rs, uint32_t* vert_order, uint32_t* colour_begin, uint32_t* ncolours) {
+	if (vert_order) memcpy(vert_order, rs.order.data(), rs.order.size() * 4);
+	if (colour_begin) memcpy(colour_begin, rs.colour_begin.data(), rs.colour_begin.size() * 4);
+	if (ncolours) *ncolours = rs.ncolours;
+	return XFEM_OK;
+}
+
+int xfem_get_ring_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_order, uint32_t* colour_begin,
+                           uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	if (!h->ring_mode) return fail(XFEM_EUNSUPPORTED, "the handle runs no continuous-pressure model");
+	return ring_schedule_out(h->bodies[body].rings, vert_order, colour_begin, ncolours);
+}
+
+int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                               uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_order, uint32_t* colour_begin,
+                               uint32_t* ncolours) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
+	int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	std::vector<uint32_t> off, lst;
+	incidence(b.tets.data(), b.nv, b.nt, off, lst);
+	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
+	rc = build_ring_schedule(b.tets.data(), b.nv, off.data(), lst.data(), b.sched.vert_rank.data(), b.rings);
+	if (rc == -2) return fail(XFEM_ELIMIT, "a vertex one-ring has more than 64 tets or 32 vertices");
+	if (rc) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
+	return ring_schedule_out(b.rings, vert_order, colour_begin, ncolours);
 }
 
 int xfem_pbd_damping_coefficients(float pbd_damping, float substep_dt, float spacing, float* out2) {

@@ -62,6 +62,26 @@ void vertex_ranks(const float* nodes, uint32_t nverts, uint32_t morton, Schedule
 // colour_cl, colour_cl_begin
 void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t morton, Schedule& s);
 
+// One-rings of the continuous-pressure models (OneRingConstructor,
+// XPBDFEM/Connectivity.h:114-160): per vertex its tets (the incidence list)
+// and its nodes, the vertex first, then each tet's vertices in order of first
+// appearance; and the ring schedule: vertices coloured greedily in id order
+// so that rings of one colour share no node, ordered inside each colour by
+// vertex rank.
+struct RingSchedule {
+	uint32_t ncolours = 0;
+	std::vector<uint32_t> tet_off, tets;    // the incidence: nverts + 1 offsets; tet ids
+	std::vector<uint32_t> node_off, nodes;  // nverts + 1 offsets; caller vertex ids
+	std::vector<uint8_t> corner;            // 4 per incidence entry: node index of each tet corner
+	std::vector<uint32_t> order;            // vertices in ring order, colour-major
+	std::vector<uint32_t> colour_begin;     // ncolours + 1, into order
+};
+// off / lst: the incidence (vertex -> tets in increasing id); vert_rank: the
+// vertex ranks. Returns 0, -1 when the colour limit is exceeded, -2 when a
+// ring has more than kMaxRingTets tets or kMaxRingNodes vertices.
+int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
+                        const uint32_t* vert_rank, RingSchedule& rs);
+
 // ---- GPU set-up path (xfem_setup.cu) ------------------------------------------
 // The parallel phases of the set-up on the device, bit for bit the host's:
 // rest state (init_rest), incidence, Morton vertex ranks (vertex_ranks) and
@@ -106,7 +126,7 @@ struct BodyParams {
 	uint32_t volume_passes;   // Settings::volumePasses: SolveElementVolume sweeps after the solve
 	float hw;                 // Pixar models: lambda / 2, the weight of (J - a)^2
 	float compliance;         // Settings::compliance (the volume passes' compliance per volume)
-	uint32_t pad3;
+	float lambda;             // (2 mu nu) / (1 - 2 nu) (continuous-pressure models)
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
@@ -121,6 +141,10 @@ constexpr uint32_t kModelNeoClamp = 1;  // Mixed (3): U0 = I1 clamped at 1e-4 (X
 constexpr uint32_t kModelYeoh = 2;      // YeohSkin (5), YeohSkinSel (6), YeohSkinFast (7)
 constexpr uint32_t kModelPixar = 3;     // Pixar (0), PixarReduced (1), PixarSel (2): one constraint
 constexpr uint32_t kModelNone = 4;      // CubeNeo (11), CubeSkin (12): no constraint on tets
+constexpr uint32_t kModelRing = 5;      // ContinuousPixar (8), ContinuousMixed (9), ContinuousSkin (10):
+                                        // one constraint (pair) per vertex one-ring, not per tet
+constexpr uint32_t kMaxRingNodes = 32;  // vertices of a one-ring (one warp lane each)
+constexpr uint32_t kMaxRingTets = 64;   // tets of a one-ring (two per warp lane)
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
@@ -190,6 +214,17 @@ struct DevCtx {
 	const uint32_t* lastmask;   // [chunk][lane]: slots whose last solve of a substep this
 	                            // cluster makes (it finishes them when damping sweeps run)
 	const uint8_t* pass_on;     // [damping kind][tick % 8][colour]: some tet is damped
+	// One-ring mode (continuous-pressure models; xfem_rings.cu): rings in
+	// device order, colour-major. ring_hdr[r] = (first node, first tet entry,
+	// nodes | tets << 8 | body << 16, 0); ring_node: device vertex ids;
+	// ring_ent: per ring tet two float4 (QQ, QR, volume, corner node indices
+	// packed in the last word).
+	const uint4* ring_hdr;
+	const uint32_t* ring_node;
+	const float4* ring_ent;
+	const uint32_t* colour_ring_begin;  // ring_colours + 1
+	uint32_t ring_colours;
+	uint32_t rings;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
@@ -260,6 +295,10 @@ int launch_gather_xyz(const float4* vert, int which, const uint32_t* dev_of_call
 int launch_scatter_xyz(float4* vert, int which, const uint32_t* dev_of_caller, uint32_t n, const float* in,
                        void* stream);
 int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, double* out, void* stream);
+// One-ring mode (xfem_rings.cu): nsub substeps of the continuous-pressure
+// models, a cooperative persistent launch of `block` threads per block
+// (canonical (X, V) in and out).
+int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Per-tet material (n tets from the given per-tet tables): c0 of each record
 // and 1/mu; mu null = mu_uniform for all.
 int launch_set_c0(float4* cblk, const uint32_t* rec, const float* vol, const float* mu, float mu_uniform, uint32_t n,

@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libxfem.so")
 
 OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT = 0, -1, -2, -3, -4, -5, -6
 ENERGY_BIT = 6
-# energy ids, XPBDFEM/Settings.h:41-53 (8-10, the continuous-pressure models, are not run)
+# energy ids, XPBDFEM/Settings.h:41-53
 ENERGY_PIXAR = 0
 ENERGY_PIXAR_REDUCED = 1
 ENERGY_PIXAR_SEL = 2
@@ -27,6 +27,9 @@ ENERGY_MIXED_SEL = 4
 ENERGY_YEOH_SKIN = 5
 ENERGY_YEOH_SKIN_SEL = 6
 ENERGY_YEOH_SKIN_FAST = 7
+ENERGY_CONTINUOUS_PIXAR = 8
+ENERGY_CONTINUOUS_MIXED = 9
+ENERGY_CONTINUOUS_SKIN = 10
 ENERGY_CUBE_NEO = 11
 ENERGY_CUBE_SKIN = 12
 MAX_VOLUME_PASSES = 64
@@ -84,6 +87,7 @@ EXPORTS = [
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
     "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward", "xfem_pbd_damping_coefficients",
+    "xfem_get_ring_schedule", "xfem_compute_ring_schedule",
 ]
 
 _lib = None
@@ -207,6 +211,19 @@ def compute_schedule(node_data, idx_data, cluster_mode=0, morton=True):
                                        _p(rank), _p(order), _p(cb), C.byref(ncol), C.byref(ncl)))
     return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1], colours=ncol.value,
                 clusters=ncl.value)
+
+
+def compute_ring_schedule(node_data, idx_data, morton=True):
+    """Host-only ring schedule of the continuous-pressure models (no GPU)."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nv = nd.size // 3
+    order = np.zeros(nv, np.uint32)
+    cb = np.zeros(nv + 1, np.uint32)
+    ncol = C.c_uint32()
+    _check(lib().xfem_compute_ring_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(order), _p(cb),
+                                            C.byref(ncol)))
+    return dict(vert_order=order, colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
 
 
 def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None,
@@ -345,6 +362,15 @@ class Body:
         cb = np.zeros(ncol.value + 1, np.uint32)
         _check(lib().xfem_get_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb, colours=ncol.value)
+
+    def ring_schedule(self, body=0):
+        """The ring order of a continuous-pressure body (energy 8-10)."""
+        nv, nt = self.counts[body]
+        order = np.zeros(nv, np.uint32)
+        cb = np.zeros(nv + 1, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_ring_schedule(self._h, body, _p(order), _p(cb), C.byref(ncol)))
+        return dict(vert_order=order, colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     # -- reverse-mode adjoint (no reference counterpart; see include/xfem.h)
     def total_counts(self):
