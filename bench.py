@@ -19,8 +19,8 @@ shape the configuration names.
   shuffled order, 1 thread, on a bounded sample), clocks, gpu_launches, and
   "batched": 512 bodies in one launch per frame against one launch per body,
   "damped": the same mesh with the reference web UI's default damping against
-  undamped, "models": the same mesh at nu = 0.45 with Mixed, YeohSkin, Pixar
-  and one volume pass against MixedSel, "setup": wall time of a handle's
+  undamped, "models": the same mesh at nu = 0.45 with Mixed, YeohSkin, Pixar,
+  one volume pass and ContinuousMixed (one-ring mode) against MixedSel, "setup": wall time of a handle's
   set-up (GPU set-up path and host set-up, 1.5M-tet mesh; 512-body batch),
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
@@ -526,7 +526,8 @@ def run_setup(stream):
 
 def run_models(stream, frames=5):
     """The throughput mesh at nu = 0.45 (the Pixar models need nu < 0.5) with
-    the other energy models and with volume passes, against MixedSel (the hot
+    the other energy models, with volume passes and with the continuous-
+    pressure model ContinuousMixed (one-ring mode), against MixedSel (the hot
     kernel): device-timed frames of 20 substeps, L2 flushed between frames."""
     import torch
 
@@ -539,7 +540,8 @@ def run_models(stream, frames=5):
     cases = (("mixed_sel", base), ("mixed", dict(base, flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)),
              ("yeoh_skin", dict(base, flags=(xfem.ENERGY_YEOH_SKIN << xfem.ENERGY_BIT) | solve)),
              ("pixar", dict(base, flags=(xfem.ENERGY_PIXAR << xfem.ENERGY_BIT) | solve)),
-             ("mixed_sel_volume_1", dict(base, volume_passes=1)))
+             ("mixed_sel_volume_1", dict(base, volume_passes=1)),
+             ("continuous_mixed", dict(base, flags=(xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) | solve)))
     out = {key: time_frames(stream, w, s_, flush, frames) for key, s_ in cases}
     return {"workload": w["name"].replace("Neo-Hookean", "nu = 0.45"), "unit": UNIT, **out,
             "cost": {k: out[k]["ms_per_frame"] / out["mixed_sel"]["ms_per_frame"] for k, _ in cases[1:]}}
