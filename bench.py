@@ -50,7 +50,7 @@ for _p in (os.path.join(ROOT, "xpbd-fem_gb300"), os.path.join(ROOT, "oracle")):
 
 METRIC = "tet-substeps/s (1.5M tets FP32)"
 UNIT = "tet-substeps/s"
-# Survey per-unit algorithmic bytes: 80 B tet record (4 u32 indices + Qi, QQ,
+# Per-unit algorithmic bytes of the reference layout: 80 B tet record (4 u32 indices + Qi, QQ,
 # QR, volume) + 76 B per vertex per substep (X, V, O read/write 24 B each,
 # w 4 B) x V/T.
 REC_BYTES, VERT_BYTES = 80.0, 76.0
