@@ -4,8 +4,8 @@ XPBDFEM/Geo.cpp:147-193; CalculateElementEnergyAndGradients,
 XPBDFEM/Fem.cpp:942-979; SolveSimplex, XPBDFEM/Geo.cpp:12-64).
 
 Against the reference's own substeps run in the GPU body's ring order (the
-`rings_*` fixtures of tests/golden) and against the pinned oracle on a larger
-jittered mesh. Positions within 1e-5 of max |x_ref|; velocities within 1e-3,
+`rings_*` fixtures of tests/golden, with in-solve and post-step damping) and
+against the pinned oracle on a larger jittered mesh. Positions within 1e-5 of max |x_ref|; velocities within 1e-3,
 or for the incompressible case within 3x the reference's own FP32 distance
 from the FP64 run (as for the element models at nu = 0.5).
 """
@@ -21,9 +21,9 @@ from test_gpu_models import fixture_settings
 pytestmark = pytest.mark.gpu
 
 DT = 1.0 / 1200.0
-# the fixtures without post-step damping (the one-ring mode runs the in-solve damping only)
 RINGS = ["rings_c1_cpixar_nu045_star", "rings_c1_cmixed_nu045_star", "rings_c1_cmixed_incompressible_star",
-         "rings_c1_cskin_nu049_star", "rings_wonky_cmixed_paper_star", "rings_c1_cskin_limit_star"]
+         "rings_c1_cskin_nu049_star", "rings_wonky_cmixed_paper_star", "rings_c1_cskin_limit_star",
+         "rings_c1_cmixed_amortized_pbd_star", "rings_wonky_cpixar_post_star"]
 
 
 def _fp64(name, s, nsub):
@@ -65,20 +65,24 @@ def test_ring_reference_parity(name):
             assert rel(got, f64) <= 3 * e_ref + 1e-7, (e_ref, rel(got, f64))
 
 
-@pytest.mark.parametrize("energy,nu,comp,damping,rtype", [
-    (xfem.ENERGY_CONTINUOUS_PIXAR, 0.45, 1e-3, 0.0, 2),
-    (xfem.ENERGY_CONTINUOUS_MIXED, 0.40, 1e-3, 0.01, 0),
-    (xfem.ENERGY_CONTINUOUS_SKIN, 0.45, 0.5, 0.01, 1),
+@pytest.mark.parametrize("energy,nu,comp,damping,rtype,pbd", [
+    (xfem.ENERGY_CONTINUOUS_PIXAR, 0.45, 1e-3, 0.0, 2, 0.0),
+    (xfem.ENERGY_CONTINUOUS_MIXED, 0.40, 1e-3, 0.01, 0, 0.0),
+    (xfem.ENERGY_CONTINUOUS_SKIN, 0.45, 0.5, 0.01, 1, 0.0),
+    (xfem.ENERGY_CONTINUOUS_MIXED, 0.45, 1e-3, 0.01, 3, 0.03),
+    (xfem.ENERGY_CONTINUOUS_PIXAR, 0.45, 1e-3, 0.02, 2, 0.05),
 ])
-def test_ring_oracle_parity(energy, nu, comp, damping, rtype):
+def test_ring_oracle_parity(energy, nu, comp, damping, rtype, pbd):
     """A larger jittered block over 20 substeps against the oracle run in the
     body's ring order."""
     nodes, idx = xfem.generate_tet_block(6, 3, 2, (0.05, 0.05, 0.05), 1, 0.0)
     rng = np.random.default_rng(9)
     nodes = (nodes + rng.normal(0, 0.003, nodes.shape)).astype(np.float32)
     flags = (energy << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT | (rtype << 20)
+    vc, avc = xfem.pbd_damping_coefficients(pbd, DT, 0.05)
     s = xfem.default_settings(gravity=(0.3, -9.81, -2.0), compliance=comp, poissons_ratio=nu, flags=flags,
-                              damping=damping)
+                              damping=damping, pbd_damping=pbd, volume_and_time_corrected_pbd_damping=vc,
+                              amortized_volume_and_time_corrected_pbd_damping=avc)
     b = xfem.Body(nodes, idx, 800.0, s)
     tets, _ = oracle.parse_tets(idx)
     ep, w, fl = oracle.init_rest(nodes, tets, 800.0)
@@ -86,10 +90,12 @@ def test_ring_oracle_parity(energy, nu, comp, damping, rtype):
     torder = b.schedule()["tet_order"]
     X, V, w_ = nodes.astype(np.float64).reshape(-1, 3), np.zeros((nodes.size // 3, 3)), w
     lm = (fl & 1).astype(np.uint8)
+    tick = 0
     for n in (1, 19):
         b.step_frames(1, n, DT)
-        X, V, w_, _ = oracle.substeps_rings(X, V, w_, tets, ep, torder, vorder, n, oracle.params_from_settings(s, DT),
-                                            lock_mask=lm)
+        X, V, w_, _ = oracle.substeps_rings(X, V, w_, tets, ep, torder, vorder, n,
+                                            oracle.params_from_settings(s, DT, tick=tick), lock_mask=lm)
+        tick += n
         assert rel(b.positions(), X) <= 1e-5, n
         assert rel(b.velocities(), V) <= 1e-3, n
 
@@ -114,14 +120,6 @@ def test_ring_runs_repeat_bit_for_bit():
 
 def test_ring_mode_limits():
     g, s, dens, dt, nsub, mode = fixture_settings("rings_c1_cmixed_nu045_star")
-    # post-step damping is not run in one-ring mode
-    for kw in (dict(damping=0.01, flags=s.flags | (2 << 20)), dict(pbd_damping=0.03)):
-        s2 = xfem.default_settings(**{k: getattr(s, k) for k, _ in s._fields_})
-        for k, v in kw.items():
-            setattr(s2, k, v)
-        with pytest.raises(xfem.XfemError) as e:
-            xfem.Body(g["nodes"], g["idx"], dens, s2)
-        assert e.value.code == xfem.EUNSUPPORTED
     b = xfem.Body(g["nodes"], g["idx"], dens, s)
     # switching to an element model needs a new handle
     s3 = xfem.default_settings()

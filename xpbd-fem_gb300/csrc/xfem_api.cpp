@@ -112,8 +112,10 @@ struct xfem_body {
 	// one-ring mode (continuous-pressure models)
 	bool ring_mode = false;
 	DevBuf<uint4> ring_hdr;
-	DevBuf<uint32_t> ring_node, ring_cb;
+	DevBuf<uint32_t> ring_node, ring_cb, pbd_cb;
 	DevBuf<float4> ring_ent;
+	DevBuf<uint2> pbd_cl;
+	DevBuf<uint4> pbd_ent;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -156,10 +158,6 @@ uint32_t model_of(uint32_t energy) {
 int validate_settings(const xfem_settings& s) {
 	const uint32_t energy = (s.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	const uint32_t model = model_of(energy);
-	const uint32_t rtype = (s.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u;
-	if (model == kModelRing && ((rtype >= XFEM_RAYLEIGH_POST && s.damping > 0.0f) || s.pbd_damping > 0.0f))
-		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) run no post-step damping here "
-		                               "(Rayleigh types 2, 3 with damping > 0, or pbd_damping > 0)");
 	if (energy == 8u && !(s.poissons_ratio < 0.5f))
 		return fail(XFEM_EINVAL, "ContinuousPixar needs poissons_ratio < 0.5 (lambda = 2 / (1 - 2 nu))");
 	if (s.volume_passes > XFEM_MAX_VOLUME_PASSES)
@@ -444,12 +442,11 @@ struct Lane {
 	uint32_t body, cluster;
 };
 
-// Whether a body of a one-ring handle damps in the solve (Paper, Limit): the
+// Whether a body of a one-ring handle damps (in the solve or after it): the
 // ring kernel with damping compiled in is launched.
 bool ring_damp_of(const std::vector<BodyHost>& bodies) {
 	for (const BodyHost& b : bodies)
-		if (b.settings.damping > 0.0f && ((b.settings.flags >> XFEM_RAYLEIGH_TYPE_BIT) & 3u) < XFEM_RAYLEIGH_POST)
-			return true;
+		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f) return true;
 	return false;
 }
 
@@ -471,7 +468,7 @@ int build_rings(xfem_body* h) {
 			for (uint32_t i = rs.colour_begin[c]; i < rs.colour_begin[c + 1]; i++) {
 				const uint32_t v = rs.order[i];
 				const uint32_t nn = rs.node_off[v + 1] - rs.node_off[v], nt = rs.tet_off[v + 1] - rs.tet_off[v];
-				hdr.push_back(make_uint4((uint32_t)node.size(), (uint32_t)(ent.size() / 2), nn | (nt << 8) | (bi << 16), 0u));
+				hdr.push_back(make_uint4((uint32_t)node.size(), (uint32_t)(ent.size() / 2), nn | (nt << 8) | (bi << 16), i));
 				for (uint32_t n = rs.node_off[v]; n < rs.node_off[v + 1]; n++)
 					node.push_back(b.vbase + b.sched.vert_rank[rs.nodes[n]]);
 				for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++) {
@@ -485,6 +482,35 @@ int build_rings(xfem_body* h) {
 		}
 	}
 	cb[ncol] = (uint32_t)hdr.size();
+	// PBD damping: per tet colour the clusters of every body, their tets in
+	// sequence, each with its index in its body's flattened (colour-major)
+	// tet order
+	uint32_t pcol = 0;
+	for (const BodyHost& b : h->bodies) pcol = std::max(pcol, b.sched.ncolours);
+	std::vector<uint32_t> pcb(pcol + 1, 0);
+	std::vector<uint2> pcl;
+	std::vector<uint4> pent;
+	std::vector<uint32_t> flat_pos(h->bodies.size(), 0);
+	for (uint32_t c = 0; c < pcol; c++) {
+		pcb[c] = (uint32_t)pcl.size();
+		for (uint32_t bi = 0; bi < (uint32_t)h->bodies.size(); bi++) {
+			const BodyHost& b = h->bodies[bi];
+			const Schedule& sc = b.sched;
+			if (c >= sc.ncolours) continue;
+			for (uint32_t i = sc.colour_cl_begin[c]; i < sc.colour_cl_begin[c + 1]; i++) {
+				const uint32_t k = sc.colour_cl[i];
+				pcl.push_back(make_uint2((uint32_t)pent.size(), sc.cl_begin[k + 1] - sc.cl_begin[k]));
+				for (uint32_t q = sc.cl_begin[k]; q < sc.cl_begin[k + 1]; q++) {
+					const uint32_t t = sc.cl_tets[q];
+					pent.push_back(make_uint4(b.tbase + t, flat_pos[bi]++, __builtin_bit_cast(uint32_t, b.ep[17 * (size_t)t + 16]), bi));
+				}
+			}
+		}
+	}
+	pcb[pcol] = (uint32_t)pcl.size();
+	XCUDA(h->pbd_cb.alloc(pcb.size()));
+	XCUDA(h->pbd_cl.alloc(pcl.size()));
+	XCUDA(h->pbd_ent.alloc(pent.size()));
 	XCUDA(h->ring_hdr.alloc(hdr.size()));
 	XCUDA(h->ring_node.alloc(node.size()));
 	XCUDA(h->ring_ent.alloc(ent.size()));
@@ -496,9 +522,14 @@ int build_rings(xfem_body* h) {
 	XCUDA(up(h->ring_node.p, node.data(), node.size() * 4));
 	XCUDA(up(h->ring_ent.p, ent.data(), ent.size() * sizeof(float4)));
 	XCUDA(up(h->ring_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(h->pbd_cb.p, pcb.data(), pcb.size() * 4));
+	XCUDA(up(h->pbd_cl.p, pcl.data(), pcl.size() * sizeof(uint2)));
+	XCUDA(up(h->pbd_ent.p, pent.data(), pent.size() * sizeof(uint4)));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	h->ctx.ring_colours = ncol;
 	h->ctx.rings = (uint32_t)hdr.size();
+	h->ctx.pbd_colours = pcol;
+	h->device_bytes += pcb.size() * 4 + pcl.size() * 8 + pent.size() * 16;
 	h->device_bytes += hdr.size() * 16 + node.size() * 4 + ent.size() * 16 + cb.size() * 4;
 	return XFEM_OK;
 }
@@ -721,6 +752,7 @@ int build_device(xfem_body* h) {
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
 		params[bi].ntets = b.nt;
+		params[bi].nverts = b.nv;
 	}
 	clk.lap("vertex state");
 	// upload
@@ -857,6 +889,10 @@ int build_device(xfem_body* h) {
 	c.ring_node = h->ring_node.p;
 	c.ring_ent = h->ring_ent.p;
 	c.colour_ring_begin = h->ring_cb.p;
+	c.pbd_cl_begin = h->pbd_cb.p;
+	c.pbd_cl = h->pbd_cl.p;
+	c.pbd_ent = h->pbd_ent.p;
+	c.tet_verts = h->tets_dev.p;
 	if (h->ring_mode) c.ext = ring_damp_of(h->bodies) ? 1u : 0u;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
@@ -1179,6 +1215,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	XCUDA(cudaSetDevice(h->device));
 	BodyParams p = make_params(*s);
 	p.ntets = b->nt;
+	p.nverts = b->nv;
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	// Settings::tickId: the handle's substep counter continues from here
 	XCUDA(cudaMemcpyAsync(h->tick.p, &s->tick_id, 4, cudaMemcpyHostToDevice, h->stream));

@@ -127,6 +127,8 @@ struct BodyParams {
 	float hw;                 // Pixar models: lambda / 2, the weight of (J - a)^2
 	float compliance;         // Settings::compliance (the volume passes' compliance per volume)
 	float lambda;             // (2 mu nu) / (1 - 2 nu) (continuous-pressure models)
+	uint32_t nverts;          // vertices of the body (amortized ring damping slices)
+	uint32_t pad4[3];
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
@@ -216,15 +218,25 @@ struct DevCtx {
 	const uint8_t* pass_on;     // [damping kind][tick % 8][colour]: some tet is damped
 	// One-ring mode (continuous-pressure models; xfem_rings.cu): rings in
 	// device order, colour-major. ring_hdr[r] = (first node, first tet entry,
-	// nodes | tets << 8 | body << 16, 0); ring_node: device vertex ids;
-	// ring_ent: per ring tet two float4 (QQ, QR, volume, corner node indices
-	// packed in the last word).
+	// nodes | tets << 8 | body << 16, the ring's index in its body's ring
+	// order); ring_node: device vertex ids; ring_ent: per ring tet two float4
+	// (QQ, QR, volume, corner node indices packed in the last word). The PBD
+	// damping passes: per tet colour (pbd_cl_begin) the clusters (pbd_cl:
+	// first entry, count), per entry (pbd_ent) the tet, its index in its
+	// body's tet order, its surface area bits and its body; tet_verts: the
+	// tets' device vertex ids.
 	const uint4* ring_hdr;
 	const uint32_t* ring_node;
 	const float4* ring_ent;
 	const uint32_t* colour_ring_begin;  // ring_colours + 1
 	uint32_t ring_colours;
 	uint32_t rings;
+	const uint32_t* pbd_cl_begin;  // pbd_colours + 1
+	const uint2* pbd_cl;
+	const uint4* pbd_ent;
+	const uint32_t* tet_verts;
+	uint32_t pbd_colours;
+	uint32_t pad5;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.

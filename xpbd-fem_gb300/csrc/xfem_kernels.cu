@@ -130,57 +130,6 @@ __device__ __forceinline__ void rayleigh_tet(const Mat& bp, const TetRec& r, con
 	}
 }
 
-// PbdDamp (XPBDFEM/Xpbd.h:307-346): moves the tet's velocities towards its
-// rigid motion (mass-weighted centre velocity plus the rotation that carries
-// its angular momentum) by the fraction `damping`.
-__device__ __forceinline__ void pbd_tet(const float4 X[4], float4 V[4], float damping) {
-	float Wsum = 1.0e-8f;
-#pragma unroll
-	for (int i = 0; i < 4; i++) Wsum += X[i].w;
-	const float Wavg = Wsum * 0.25f, Wmin = 0.0001f * Wavg;
-	Vec3 x[4], xcm = {0.0f, 0.0f, 0.0f}, vcm = {0.0f, 0.0f, 0.0f};
-	float M[4], Msum = 0.0f;
-#pragma unroll
-	for (int i = 0; i < 4; i++) {
-		x[i] = {X[i].x - X[3].x, X[i].y - X[3].y, X[i].z - X[3].z};
-		M[i] = Wavg / fmaxf(Wmin, X[i].w);
-		xcm = {fmaf(x[i].x, M[i], xcm.x), fmaf(x[i].y, M[i], xcm.y), fmaf(x[i].z, M[i], xcm.z)};
-		vcm = {fmaf(V[i].x, M[i], vcm.x), fmaf(V[i].y, M[i], vcm.y), fmaf(V[i].z, M[i], vcm.z)};
-		Msum += M[i];
-	}
-	const float im = 1.0f / Msum;
-	xcm = {xcm.x * im, xcm.y * im, xcm.z * im};
-	vcm = {vcm.x * im, vcm.y * im, vcm.z * im};
-	Vec3 r[4], L = {0.0f, 0.0f, 0.0f};
-	float I00 = 0.0f, I11 = 0.0f, I22 = 0.0f, I01 = 0.0f, I12 = 0.0f, I02 = 0.0f;
-#pragma unroll
-	for (int i = 0; i < 4; i++) {
-		r[i] = {x[i].x - xcm.x, x[i].y - xcm.y, x[i].z - xcm.z};
-		const Vec3 c = cross(r[i], v3(V[i]));
-		L = {fmaf(M[i], c.x, L.x), fmaf(M[i], c.y, L.y), fmaf(M[i], c.z, L.z)};
-		const float xx = r[i].x * r[i].x, yy = r[i].y * r[i].y, zz = r[i].z * r[i].z;
-		I00 = fmaf(M[i], yy + zz, I00);
-		I11 = fmaf(M[i], xx + zz, I11);
-		I22 = fmaf(M[i], xx + yy, I22);
-		I01 = fmaf(-M[i], r[i].x * r[i].y, I01);
-		I12 = fmaf(-M[i], r[i].y * r[i].z, I12);
-		I02 = fmaf(-M[i], r[i].z * r[i].x, I02);
-	}
-	// omega = I^-1 L (I symmetric): adjugate over determinant
-	const float a00 = fmaf(I11, I22, -I12 * I12), a01 = fmaf(I02, I12, -I01 * I22), a02 = fmaf(I01, I12, -I02 * I11);
-	const float a11 = fmaf(I00, I22, -I02 * I02), a12 = fmaf(I01, I02, -I00 * I12), a22 = fmaf(I00, I11, -I01 * I01);
-	const float idet = 1.0f / fmaf(I00, a00, fmaf(I01, a01, I02 * a02));
-	const Vec3 om = {fmaf(a00, L.x, fmaf(a01, L.y, a02 * L.z)) * idet, fmaf(a01, L.x, fmaf(a11, L.y, a12 * L.z)) * idet,
-	                 fmaf(a02, L.x, fmaf(a12, L.y, a22 * L.z)) * idet};
-#pragma unroll
-	for (int i = 0; i < 4; i++) {
-		const Vec3 c = cross(om, r[i]);
-		V[i].x = fmaf(damping, (vcm.x + c.x) - V[i].x, V[i].x);
-		V[i].y = fmaf(damping, (vcm.y + c.y) - V[i].y, V[i].y);
-		V[i].z = fmaf(damping, (vcm.z + c.z) - V[i].z, V[i].z);
-	}
-}
-
 // Whether tet row `row` (lane `lane`) of body bp is damped at this tick, and
 // with which Rayleigh ratio and PBD fraction (XPBDFEM/Geo.cpp:346-352,
 // 792-798): the amortized type damps one eighth of the body's order per

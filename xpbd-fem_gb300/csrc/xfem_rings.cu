@@ -39,14 +39,28 @@ __device__ __forceinline__ float warp_sum(float x) {
 	return x;
 }
 
-// SolveRing of ring r by the calling warp (every lane takes part).
-template <bool DAMP>
+// SolveRing of ring r by the calling warp (every lane takes part). VMODE:
+// the post-step Rayleigh damping form (SolveRing with V, XPBDFEM/Geo.cpp:
+// 147-193, called by GeoLinear3d::Damp, XPBDFEM/Geo.cpp:800-806) on the
+// canonical state (X, V): energies and gradients at X, RayleighDamp
+// (XPBDFEM/Xpbd.h:217-263) on V, for the rings of this tick's slice.
+template <bool DAMP, bool VMODE>
 __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_t r, uint32_t lane, float inv_dt,
-                                        float inv_dt2) {
+                                        float inv_dt2, uint32_t tick) {
 	__syncwarp();  // every lane is done with the previous ring's scratch
 	const uint4 h = __ldg(C.ring_hdr + r);
 	const uint32_t nn = h.z & 0xffu, nt = (h.z >> 8) & 0xffu;
 	const BodyParams& bp = C.bodies[h.z >> 16];
+	float rd = 0.0f;  // VMODE: the Rayleigh ratio (x 8 when amortized)
+	if (VMODE) {
+		const uint32_t type = __ldg(&bp.rayleigh_type);
+		rd = __ldg(&bp.damping) * (type == 3u ? 8.0f : 1.0f);
+		if (!(type >= 2u && rd > 0.0f)) return;
+		if (type == 3u) {
+			const uint32_t nv = __ldg(&bp.nverts), m = tick % 8u;
+			if (h.w < nv * m / 8u || h.w >= nv * (m + 1u) / 8u) return;
+		}
+	}
 	uint32_t dv = 0;
 	if (lane < nn) {
 		dv = __ldg(C.ring_node + h.x + lane);
@@ -77,8 +91,9 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 		Vec3 P[3];
 #pragma unroll
 		for (int i = 0; i < 3; i++)
-			P[i] = {(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
-			        (O[i].z - O[3].z) + (D[i].z - D[3].z)};
+			P[i] = VMODE ? Vec3{O[i].x - O[3].x, O[i].y - O[3].y, O[i].z - O[3].z}
+			             : Vec3{(O[i].x - O[3].x) + (D[i].x - D[3].x), (O[i].y - O[3].y) + (D[i].y - D[3].y),
+			                    (O[i].z - O[3].z) + (D[i].z - D[3].z)};
 		const float ew = (vol * 0.25f) / volume;  // the tet's share of the ring volume
 		Vec3 gI[4];
 		const float I1 = prefactored_i1(QQ, QR, P, gI);
@@ -131,6 +146,18 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 		const float comp = __ldg(&bp.compliance) / volume;
 		const float alpha = comp * inv_dt2;
 		const float wgg = 1.0e-22f + warp_sum(w * dot(g, g));
+		if constexpr (VMODE) {
+			const float gV = warp_sum(lane < nn ? dot(g, v3(Dn)) : 0.0f);
+			const float l = -gV / fmaf(2.0f * U, comp * inv_dt / rd, wgg);
+			if (lane < nn) {
+				const float sc = w * l;
+				Dn.x = fmaf(sc, g.x, Dn.x);
+				Dn.y = fmaf(sc, g.y, Dn.y);
+				Dn.z = fmaf(sc, g.z, Dn.z);
+				st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
+			}
+			return;
+		}
 		float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
 		if constexpr (DAMP) {
 			const float gV = warp_sum(lane < nn ? dot(g, v3(Dn)) : 0.0f);
@@ -172,6 +199,19 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 	const float wgg1 = 1.0e-22f + warp_sum(w * dot(g1, g0));
 	const float wgg2 = 1.0e-22f + warp_sum(w * dot(g1, g1));
 	float l0, l1;
+	if constexpr (VMODE) {
+		const float b0 = -warp_sum(lane < nn ? dot(g0, v3(Dn)) : 0.0f);
+		const float b1 = -warp_sum(lane < nn ? dot(g1, v3(Dn)) : 0.0f);
+		cramer(fmaf(2.0f * U0, comp0 * inv_dt / rd, wgg0), wgg1, fmaf(2.0f * U1, comp1 * inv_dt / rd, wgg2), b0, b1, l0,
+		       l1);
+		if (lane < nn) {
+			Dn.x = fmaf(w, fmaf(l1, g1.x, l0 * g0.x), Dn.x);
+			Dn.y = fmaf(w, fmaf(l1, g1.y, l0 * g0.y), Dn.y);
+			Dn.z = fmaf(w, fmaf(l1, g1.z, l0 * g0.z), Dn.z);
+			st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
+		}
+		return;
+	}
 	cramer(fmaf(2.0f * U0, alpha0, wgg0), wgg1, fmaf(2.0f * U1, alpha1, wgg2), -2.0f * U0, -2.0f * U1, l0, l1);
 	if constexpr (DAMP) {
 		// warp-uniform: one body per ring
@@ -211,7 +251,38 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 	}
 }
 
-// The persistent ring kernel (cooperative launch, co-resident grid).
+// PBD damping of one tet cluster (its tets in sequence; clusters of one
+// colour share no vertex) on the canonical state, for the tets of this
+// tick's slice (GeoLinear3d::Damp, XPBDFEM/Geo.cpp:807-810).
+__device__ void pbd_cluster(const DevCtx& C, uint32_t k, uint32_t tick) {
+	const uint2 cl = __ldg(C.pbd_cl + k);
+	for (uint32_t i = cl.x; i < cl.x + cl.y; i++) {
+		const uint4 e = __ldg(C.pbd_ent + i);  // tet, index in its body's order, area bits, body
+		const BodyParams& bp = C.bodies[e.w];
+		if (!__ldg(&bp.pbd_on)) continue;
+		const bool amort = __ldg(&bp.rayleigh_type) == 3u;
+		if (amort) {
+			const uint32_t nt = __ldg(&bp.ntets), m = tick % 8u;
+			if (e.y < nt * m / 8u || e.y >= nt * (m + 1u) / 8u) continue;
+		}
+		const float coeff = amort ? __ldg(&bp.pbd_coeff_amortized) : __ldg(&bp.pbd_coeff);
+		uint32_t v[4];
+		float4 X[4], V[4];
+#pragma unroll
+		for (int n = 0; n < 4; n++) {
+			v[n] = __ldg(C.tet_verts + 4 * (size_t)e.x + n);
+			ld_vertex(C.vert + 2 * (size_t)v[n], X[n], V[n]);
+		}
+		pbd_tet(X, V, fminf(1.0f, coeff / __uint_as_float(e.z)));
+#pragma unroll
+		for (int n = 0; n < 4; n++) st_vertex(C.vert + 2 * (size_t)v[n], X[n], V[n]);
+	}
+}
+
+// The persistent ring kernel (cooperative launch, co-resident grid). DAMP:
+// damping compiled in, in the solve and after it; with post-step damping
+// (damp_kinds) every substep ends in the canonical state and runs the ring
+// Rayleigh passes, then the PBD passes.
 template <bool DAMP>
 __global__ void __launch_bounds__(256) k_rings(DevCtx C, uint32_t nsub, float dt) {
 	extern __shared__ __align__(128) unsigned char smem[];
@@ -221,28 +292,56 @@ __global__ void __launch_bounds__(256) k_rings(DevCtx C, uint32_t nsub, float dt
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 	RingScratch& S = reinterpret_cast<RingScratch*>(smem)[wib];
 	const uint32_t tick0 = __ldcg(C.tick);
+	const bool dmode = DAMP && C.damp_kinds != 0u;
 	uint32_t target = 0;
 	for (uint32_t s = 0; s < nsub; s++) {
-		// finish the previous substep and predict this one, every vertex
+		// finish the previous substep (unless the damping passes left the
+		// canonical state) and predict this one, every vertex
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
+			advance_vertex(C.bodies, O, D, s == 0 || dmode, dt, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 		if (!grid_sync(C, target)) return;
 		for (uint32_t c = 0; c < C.ring_colours; c++) {
 			const uint32_t rb = __ldg(C.colour_ring_begin + c), re = __ldg(C.colour_ring_begin + c + 1);
-			for (uint32_t r = rb + gwarp; r < re; r += nwarps) ring_solve<DAMP>(C, S, r, lane, inv_dt, inv_dt2);
+			for (uint32_t r = rb + gwarp; r < re; r += nwarps) ring_solve<DAMP, false>(C, S, r, lane, inv_dt, inv_dt2, 0);
 			if (!grid_sync(C, target)) return;
 		}
+		if (!dmode) continue;
+		if constexpr (DAMP) {
+			for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
+				float4 O, D;
+				ld_vertex(C.vert + 2 * (size_t)v, O, D);
+				finalize_vertex(C.bodies, O, D, inv_dt);
+				st_vertex(C.vert + 2 * (size_t)v, O, D);
+			}
+			if (!grid_sync(C, target)) return;
+			const uint32_t tick = tick0 + s;
+			if (C.damp_kinds & 1u)
+				for (uint32_t c = 0; c < C.ring_colours; c++) {
+					const uint32_t rb = __ldg(C.colour_ring_begin + c), re = __ldg(C.colour_ring_begin + c + 1);
+					for (uint32_t r = rb + gwarp; r < re; r += nwarps)
+						ring_solve<true, true>(C, S, r, lane, inv_dt, inv_dt2, tick);
+					if (!grid_sync(C, target)) return;
+				}
+			if (C.damp_kinds & 2u)
+				for (uint32_t c = 0; c < C.pbd_colours; c++) {
+					const uint32_t kb = __ldg(C.pbd_cl_begin + c), ke = __ldg(C.pbd_cl_begin + c + 1);
+					for (uint32_t k = kb + gtid; k < ke; k += nthreads) pbd_cluster(C, k, tick);
+					if (!grid_sync(C, target)) return;
+				}
+		}
 	}
-	// finish the last substep: (O, D) -> canonical (X, V)
-	for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
-		float4 O, D;
-		ld_vertex(C.vert + 2 * (size_t)v, O, D);
-		finalize_vertex(C.bodies, O, D, inv_dt);
-		st_vertex(C.vert + 2 * (size_t)v, O, D);
+	if (!dmode) {
+		// finish the last substep: (O, D) -> canonical (X, V)
+		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
+			float4 O, D;
+			ld_vertex(C.vert + 2 * (size_t)v, O, D);
+			finalize_vertex(C.bodies, O, D, inv_dt);
+			st_vertex(C.vert + 2 * (size_t)v, O, D);
+		}
 	}
 	if (gtid == 0) *C.tick = tick0 + nsub;
 }
