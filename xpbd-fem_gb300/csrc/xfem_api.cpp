@@ -112,7 +112,8 @@ struct xfem_body {
 	// one-ring mode (continuous-pressure models)
 	bool ring_mode = false;
 	DevBuf<uint4> ring_hdr;
-	DevBuf<uint32_t> ring_node, ring_cb, pbd_cb;
+	DevBuf<uint32_t> ring_node, ring_cb, pbd_cb, ring_clist;
+	DevBuf<uint16_t> ring_cwords;
 	DevBuf<float4> ring_ent;
 	DevBuf<uint2> pbd_cl;
 	DevBuf<uint4> pbd_ent;
@@ -457,7 +458,8 @@ int build_rings(xfem_body* h) {
 	uint32_t ncol = 0;
 	for (const BodyHost& b : h->bodies) ncol = std::max(ncol, b.rings.ncolours);
 	std::vector<uint4> hdr;
-	std::vector<uint32_t> node, cb(ncol + 1, 0);
+	std::vector<uint32_t> node, cb(ncol + 1, 0), clist;
+	std::vector<uint16_t> cwords;
 	std::vector<float4> ent;
 	for (uint32_t c = 0; c < ncol; c++) {
 		cb[c] = (uint32_t)hdr.size();
@@ -478,6 +480,17 @@ int build_rings(xfem_body* h) {
 					ent.push_back(make_float4(e[9], e[10], e[11], e[12]));
 					ent.push_back(make_float4(e[13], e[14], e[15], __builtin_bit_cast(float, cn)));
 				}
+				// each node's corners (local tet << 2 | corner), in tet order
+				clist.push_back((uint32_t)cwords.size());
+				const size_t ob = cwords.size();
+				cwords.resize(ob + nn + 1);
+				for (uint32_t n = 0; n < nn; n++) {
+					cwords[ob + n] = (uint16_t)(cwords.size() - ob - (nn + 1));
+					for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++)
+						for (int k = 0; k < 4; k++)
+							if (rs.corner[4 * (size_t)j + k] == n) cwords.push_back((uint16_t)(((j - rs.tet_off[v]) << 2) | k));
+				}
+				cwords[ob + nn] = (uint16_t)(cwords.size() - ob - (nn + 1));
 			}
 		}
 	}
@@ -511,6 +524,8 @@ int build_rings(xfem_body* h) {
 	XCUDA(h->pbd_cb.alloc(pcb.size()));
 	XCUDA(h->pbd_cl.alloc(pcl.size()));
 	XCUDA(h->pbd_ent.alloc(pent.size()));
+	XCUDA(h->ring_clist.alloc(clist.size()));
+	XCUDA(h->ring_cwords.alloc(cwords.size()));
 	XCUDA(h->ring_hdr.alloc(hdr.size()));
 	XCUDA(h->ring_node.alloc(node.size()));
 	XCUDA(h->ring_ent.alloc(ent.size()));
@@ -522,6 +537,8 @@ int build_rings(xfem_body* h) {
 	XCUDA(up(h->ring_node.p, node.data(), node.size() * 4));
 	XCUDA(up(h->ring_ent.p, ent.data(), ent.size() * sizeof(float4)));
 	XCUDA(up(h->ring_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(h->ring_clist.p, clist.data(), clist.size() * 4));
+	XCUDA(up(h->ring_cwords.p, cwords.data(), cwords.size() * 2));
 	XCUDA(up(h->pbd_cb.p, pcb.data(), pcb.size() * 4));
 	XCUDA(up(h->pbd_cl.p, pcl.data(), pcl.size() * sizeof(uint2)));
 	XCUDA(up(h->pbd_ent.p, pent.data(), pent.size() * sizeof(uint4)));
@@ -889,6 +906,8 @@ int build_device(xfem_body* h) {
 	c.ring_node = h->ring_node.p;
 	c.ring_ent = h->ring_ent.p;
 	c.colour_ring_begin = h->ring_cb.p;
+	c.ring_clist = h->ring_clist.p;
+	c.ring_cwords = h->ring_cwords.p;
 	c.pbd_cl_begin = h->pbd_cb.p;
 	c.pbd_cl = h->pbd_cl.p;
 	c.pbd_ent = h->pbd_ent.p;

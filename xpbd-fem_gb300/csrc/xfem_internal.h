@@ -231,6 +231,9 @@ struct DevCtx {
 	const uint32_t* colour_ring_begin;  // ring_colours + 1
 	uint32_t ring_colours;
 	uint32_t rings;
+	const uint32_t* ring_clist;    // per ring: offset of its corner lists in ring_cwords
+	const uint16_t* ring_cwords;   // per ring: nodes + 1 offsets, then each node's corners
+	                               // (tet << 2 | corner) in tet order
 	const uint32_t* pbd_cl_begin;  // pbd_colours + 1
 	const uint2* pbd_cl;
 	const uint4* pbd_ent;

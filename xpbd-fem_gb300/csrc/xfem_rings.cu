@@ -13,7 +13,7 @@
 // One warp per ring: lane j takes the ring's tet j (its I1 and volume ratio J
 // with their gradients, weighted by the tet's share of the ring volume),
 // lane n the ring's node n (the sum of its gradient contributions in tet
-// order, then its update). Sums over lanes run in a fixed butterfly order,
+// order, from a per-node list of its tet corners, then its update). Sums over lanes run in a fixed butterfly order,
 // so every launch gives the same bits.
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -30,7 +30,6 @@ struct RingScratch {
 	float4 O[kMaxRingNodes], D[kMaxRingNodes];  // ring nodes: (O, w), (D, bits)
 	float g0[kMaxRingTets][4][3];               // per tet corner: I1 gradient contribution
 	float g1[kMaxRingTets][4][3];               // per tet corner: J gradient contribution
-	uint32_t corner[kMaxRingTets];              // per tet: 4 x 8-bit node indices
 };
 
 __device__ __forceinline__ float warp_sum(float x) {
@@ -69,9 +68,7 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 	// lane j takes the ring's tets j and j + 32
 	float volq = 0.0f;
 	for (uint32_t j = lane; j < nt; j += 32) {
-		const float4 e1 = __ldg(C.ring_ent + 2 * ((size_t)h.y + j) + 1);
-		volq += 0.25f * e1.z;
-		S.corner[j] = __float_as_uint(e1.w);
+		volq += 0.25f * __ldg(&C.ring_ent[2 * ((size_t)h.y + j) + 1].z);
 	}
 	const float volume = warp_sum(volq);  // the ring's volume
 	__syncwarp();
@@ -122,14 +119,12 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 	float w = 0.0f;
 	float4 Dn = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	if (lane < nn) {
-		for (uint32_t j = 0; j < nt; j++) {
-			const uint32_t c = S.corner[j];
-#pragma unroll
-			for (int k = 0; k < 4; k++)
-				if (((c >> (8 * k)) & 0xffu) == lane) {
-					g0 = {g0.x + S.g0[j][k][0], g0.y + S.g0[j][k][1], g0.z + S.g0[j][k][2]};
-					g1 = {g1.x + S.g1[j][k][0], g1.y + S.g1[j][k][1], g1.z + S.g1[j][k][2]};
-				}
+		const uint16_t* cl = C.ring_cwords + __ldg(C.ring_clist + r);
+		const uint32_t cb = __ldg(cl + lane), ce = __ldg(cl + lane + 1);
+		for (uint32_t i = cb; i < ce; i++) {
+			const uint32_t q = __ldg(cl + nn + 1 + i), j = q >> 2, k = q & 3u;
+			g0 = {g0.x + S.g0[j][k][0], g0.y + S.g0[j][k][1], g0.z + S.g0[j][k][2]};
+			g1 = {g1.x + S.g1[j][k][0], g1.y + S.g1[j][k][1], g1.z + S.g1[j][k][2]};
 		}
 		w = S.O[lane].w;
 		Dn = S.D[lane];
