@@ -51,6 +51,12 @@ CASES = [
                             0.0, -9.81, DT, 40, 1]),
     ("ordered_c1_yeoh_tet", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.5,
                              0.0, -9.81, DT, 40, 1]),
+    # the small cantilever configuration over its full 100 frames (20
+    # substeps of 1/1200 s each), in the GPU's colour order
+    ("ordered_c1_nh_100frames_star", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
+                                      0.0, -9.81, DT, 2000, 1]),
+    ("ordered_c1_yeoh_100frames_star", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.5,
+                                        0.0, -9.81, DT, 2000, 1]),
     # compressible (nu < 0.5): the coupled solve is well conditioned here, so
     # an FP32 implementation can be held to 1e-5 of the reference's own path
     ("ordered_c1_nh_nu045_star", ["ordered", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,

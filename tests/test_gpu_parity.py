@@ -66,6 +66,24 @@ def test_reference_parity_incompressible_vs_fp64(name, mode):
     assert e_gpu <= 3 * e_ref + 1e-7, (e_gpu, e_ref)
 
 
+@pytest.mark.parametrize("name", ["ordered_c1_nh_100frames_star", "ordered_c1_yeoh_100frames_star"])
+def test_hundred_frames_stated_bound(name):
+    """The small cantilever configuration over its 100 frames (2,000
+    substeps), the reference run in this body's colour order. Stated bound:
+    the GPU's distance from the FP64 run of the same method stays within 3x
+    the reference's own FP32 distance from it (the reference itself is about
+    1e-2 (Neo-Hookean) and 3e-3 (Yeoh) of max |x| from FP64 there: the
+    incompressible constraint amplifies rounding)."""
+    g, b, s, dt, nsub, dens = c1_golden_body(name, 0)
+    assert np.array_equal(b.schedule()["tet_order"], g["order"])
+    o64 = OracleRun(g["nodes"], g["idx"], dens, s, g["order"], dtype=np.float64)
+    b.step_frames(100, nsub // 100, dt)
+    o64.step(nsub, dt)
+    e_ref, e_gpu = rel(g["xn"].reshape(-1, 3), o64.X), rel(b.positions(), o64.X)
+    assert e_gpu <= 3 * e_ref, (e_gpu, e_ref)
+    assert rel(b.positions(), g["xn"].reshape(-1, 3)) <= 4 * e_ref
+
+
 def test_schedule_and_rest_state_of_handle():
     g, b, s, dt, _, _ = c1_golden_body("ordered_c1_nh_star", 0)
     sch = b.schedule()

@@ -28,7 +28,7 @@ SOLVE = ["solve_nh_sim_incompressible", "solve_nh_sim_nu045", "solve_yeoh_sim_in
          "solve_id20_mixedsel"]
 SUBSTEP = ["substep_c1_nh_native", "substep_c1_yeoh_native", "substep_wonky_nh_serial_native",
            "ordered_c1_nh_star", "ordered_c1_yeoh_tet", "ordered_c1_nh_nu045_star", "ordered_c1_yeoh_nu049_tet",
-           "ordered_wonky_nh_serial_nu045_star"]
+           "ordered_wonky_nh_serial_nu045_star", "ordered_c1_nh_100frames_star", "ordered_c1_yeoh_100frames_star"]
 DAMPED = ["damped_c1_nh_nu045_amortized_pbd_star", "damped_c1_nh_nu045_post_star", "damped_c1_nh_nu045_paper_star",
           "damped_c1_nh_nu045_limit_star", "damped_c1_yeoh_nu049_amortized_pbd_tet",
           "damped_wonky_nh_serial_post_pbd_star", "damped_wonky_nh_serial_limit_pbd_star"]
