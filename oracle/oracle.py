@@ -132,6 +132,20 @@ def lib():
         L.orc_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
         L.orc_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
         L.orc_ring_schedule.argtypes = [P, u32, P, u32, u32, P, P, P]
+        L.orc_gen_hex_block.argtypes = [u32, u32, u32, C.c_float, C.c_float, C.c_float, u32, C.c_float, P, P]
+        L.orc_parse_hexes.argtypes = [P, u32, P, P, P]
+        L.orc_hex_tables.argtypes = [P, P, P]
+        L.orc_hex_init_rest_f.argtypes = [P, u32, P, u32, C.c_float, P, P, P]
+        L.orc_hex_init_rest_d.argtypes = [P, u32, P, u32, C.c_double, P, P, P]
+        L.orc_solve_hex_f.argtypes = [P, P, P, P, P]
+        L.orc_solve_hex_d.argtypes = [P, P, P, P, P]
+        L.orc_hex_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_hex_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_hex_volume_f.argtypes = [P, u32, P, P]
+        L.orc_hex_volume_f.restype = C.c_float
+        L.orc_hex_volume_d.argtypes = [P, u32, P, P]
+        L.orc_hex_volume_d.restype = C.c_double
+        L.orc_hex_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -307,3 +321,97 @@ def adjoint(X0, V0, w, tets, ep, tet_mu, order, nsub, params, tips, targets, loc
     if not grad:
         return loss.value
     return (loss.value, dmu, dv.reshape(-1, 3), dx.reshape(-1, 3)) if want_dx else (loss.value, dmu, dv.reshape(-1, 3))
+
+
+# ---- linear hexahedra (oracle/xfem_oracle_hex.inc) ----
+HEX_EP = 120  # values per hex record (ElementParamsLinearHex flattened)
+
+
+def gen_hex_block(W, H, D, scale=(1.0, 1.0, 1.0), pattern=0, wonkiness=0.0):
+    nv = (W + 1) * (H + 1) * (D + 1)
+    nodes = np.zeros(3 * nv, np.float32)
+    idx = np.zeros(9 * W * H * D, np.uint32)
+    lib().orc_gen_hex_block(W, H, D, scale[0], scale[1], scale[2], pattern, wonkiness, _p(nodes), _p(idx))
+    return nodes, idx
+
+
+def parse_hexes(idx):
+    idx = np.ascontiguousarray(idx, np.uint32)
+    nh, nv = C.c_uint32(), C.c_uint32()
+    if lib().orc_parse_hexes(_p(idx), idx.size, None, C.byref(nh), C.byref(nv)):
+        raise ValueError("index stream holds a non-hex element")
+    hexes = np.zeros((nh.value, 8), np.uint32)
+    lib().orc_parse_hexes(_p(idx), idx.size, _p(hexes), C.byref(nh), C.byref(nv))
+    return hexes, nv.value
+
+
+def hex_tables():
+    """(n8[8][8], g8[8][8][3], g1[8][3]) as the oracle builds them."""
+    n8, g8, g1 = np.zeros((8, 8), np.float32), np.zeros((8, 8, 3), np.float32), np.zeros((8, 3), np.float32)
+    lib().orc_hex_tables(_p(n8), _p(g8), _p(g1))
+    return n8, g8, g1
+
+
+def hex_init_rest(nodes, hexes, density, dtype=np.float32):
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    nv, nh = nodes.size // 3, hexes.shape[0]
+    ep = np.zeros((nh, HEX_EP), dtype)
+    w = np.zeros(nv, dtype)
+    fl = np.zeros(nv, np.uint8)
+    f = lib().orc_hex_init_rest_f if dtype == np.float32 else lib().orc_hex_init_rest_d
+    f(_p(nodes), nv, _p(hexes), nh, density, _p(ep), _p(w), _p(fl))
+    return ep, w, fl
+
+
+def solve_hex(X, w, ep, params, O, dtype=np.float32):
+    X = np.array(X, np.float64).reshape(8, 3).copy()
+    O = np.ascontiguousarray(O, np.float64).reshape(8, 3)
+    w = np.ascontiguousarray(w, dtype)
+    ep = np.ascontiguousarray(ep, dtype)
+    f = lib().orc_solve_hex_f if dtype == np.float32 else lib().orc_solve_hex_d
+    if f(_p(X), _p(O), _p(w), _p(ep), C.byref(params)):
+        raise ValueError("energy model not covered on hexes")
+    return X
+
+
+def hex_substeps(X, V, w, hexes, ep, order, nsub, params, lock_mask=None, dtype=np.float32):
+    """nsub substeps of a hex mesh in the hex order `order`. Returns X, V, w,
+    contact mask of the last substep."""
+    X = np.array(X, np.float64).reshape(-1).copy()
+    V = np.array(V, np.float64).reshape(-1).copy()
+    w = np.array(w, dtype).copy()
+    nv = w.size
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    order = np.ascontiguousarray(order, np.uint32)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    contact = np.zeros(nv, np.uint8)
+    f = lib().orc_hex_substeps_f if dtype == np.float32 else lib().orc_hex_substeps_d
+    if f(nv, _p(X), _p(V), _p(w), _p(lm), hexes.shape[0], _p(hexes), _p(ep), _p(order), nsub, C.byref(params),
+         _p(contact)):
+        raise ValueError("energy model not covered on hexes")
+    return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+
+def hex_volume(X, hexes, ep, dtype=np.float32):
+    X = np.ascontiguousarray(X, np.float64).reshape(-1)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    f = lib().orc_hex_volume_f if dtype == np.float32 else lib().orc_hex_volume_d
+    return f(_p(X), hexes.shape[0], _p(hexes), _p(ep))
+
+
+def hex_schedule(nodes, hexes, morton=1):
+    """Hex order (colour-major), colour offsets and vertex ranks of the hex
+    schedule."""
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    nv, nh = nodes.size // 3, hexes.shape[0]
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nh, np.uint32)
+    cb = np.zeros(65, np.uint32)
+    ncol = C.c_uint32()
+    if lib().orc_hex_schedule(_p(nodes), nv, _p(hexes), nh, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
+        raise ValueError("hex schedule needs more than 64 colours")
+    return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)

@@ -51,6 +51,20 @@
  *       which replace tOrder and vOrder; GeoLinear3d::Constrain then solves
  *       the one-rings in that vertex order (XPBDFEM/Geo.cpp:784-787) and
  *       GeoLinear3d::Damp damps them in it (XPBDFEM/Geo.cpp:800-806).
+ *
+ * Linear hexahedra: the same commands prefixed with `h` run on a
+ * GenerateHexBlock mesh (XPBDFEM/MeshGen.cpp:156-221) and always take the
+ * element pattern after the scale:
+ *   hmeshgen / hinit W H D sx sy sz pattern wonkiness [density]
+ *       hinit dumps the per-hex rest state (qcLo, qcHi, ic, volume,
+ *       surfaceArea; InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265),
+ *       w, the flags, the MINSTD hex order hOrder and CalculateVolume.
+ *   hordered / hdamped W H D sx sy sz pattern wonkiness density ...
+ *       (the rest as `ordered` / `damped`) < horder.u32
+ *       the order read from stdin replaces hOrder; GeoLinear3d::Constrain
+ *       and Damp then run their hex loops (XPBDFEM/Geo.cpp:777-811).
+ *   hsolve seed count energy simultaneous compliance poisson dt
+ *       SolveElement (XPBDFEM/Fem.cpp:896) on `count` seeded random hexes.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -67,6 +81,10 @@
 
 // Non-static in XPBDFEM/MeshGen.cpp:223 but not declared in MeshGen.h.
 void GenerateTetBlock(Allocator* alloc, uint32_t width, uint32_t height, uint32_t depth, vec3 scale,
+                      uint32_t elementPattern, float wonkiness, const float** outNodeData,
+                      uint32_t* outNodeDataCount, const uint32_t** outIdxData, uint32_t* outIdxDataCount);
+// Non-static in XPBDFEM/MeshGen.cpp:156 but not declared in MeshGen.h.
+void GenerateHexBlock(Allocator* alloc, uint32_t width, uint32_t height, uint32_t depth, vec3 scale,
                       uint32_t elementPattern, float wonkiness, const float** outNodeData,
                       uint32_t* outNodeDataCount, const uint32_t** outIdxData, uint32_t* outIdxDataCount);
 
@@ -150,6 +168,39 @@ static void dump_geo(GeoLinear3d* g) {
 	emit("volume", 'f', &vol, 1);
 }
 
+// ElementParamsLinearHex (XPBDFEM/Fem.h:90-100) flattened, 120 values per hex:
+// qcLo.Ji[0] column-major, qcLo.w[0], qcHi.Ji[0..7], qcHi.w[0..7], ic.QQ[7],
+// ic.QR[21], volume, surfaceArea.
+static void hex_record(const ElementParamsLinearHex& e, float* o) {
+	for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[c * 3 + r] = e.qcLo.Ji[0][c][r];
+	o[9] = e.qcLo.w[0];
+	for (int p = 0; p < 8; p++)
+		for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[10 + 9 * p + c * 3 + r] = e.qcHi.Ji[p][c][r];
+	for (int p = 0; p < 8; p++) o[82 + p] = e.qcHi.w[p];
+	for (int k = 0; k < 7; k++) o[90 + k] = e.ic.QQ[k];
+	for (int k = 0; k < 21; k++) o[97 + k] = e.ic.QR[k];
+	o[118] = e.volume;
+	o[119] = e.surfaceArea;
+}
+
+static void dump_hex_geo(GeoLinear3d* g) {
+	uint32_t nh = g->con.hexCount, nv = g->vertCount;
+	std::vector<float> ep(nh * 120);
+	std::vector<uint32_t> hidx(nh * 8);
+	for (uint32_t i = 0; i < nh; i++) {
+		hex_record(g->h[i].ep, &ep[i * 120]);
+		for (int k = 0; k < 8; k++) hidx[i * 8 + k] = g->h[i].i[k];
+	}
+	std::vector<uint8_t> flags(g->flags, g->flags + nv);
+	emit("hex_idx", 'I', hidx.data(), hidx.size());
+	emit("hep", 'f', ep.data(), ep.size());
+	emit("w", 'f', g->w, nv);
+	emit("vflags", 'B', flags.data(), nv);
+	emit("horder", 'I', g->hOrder, nh);
+	float vol = g->CalculateVolume();
+	emit("volume", 'f', &vol, 1);
+}
+
 static void dump_state(GeoLinear3d* g, const char* xname, const char* vname) {
 	uint32_t nv = g->vertCount;
 	std::vector<double> x(nv * 3), v(nv * 3);
@@ -161,7 +212,8 @@ static void dump_state(GeoLinear3d* g, const char* xname, const char* vname) {
 
 int main(int argc, char** argv) {
 	if (argc < 2) { fprintf(stderr, "usage: refgen <cmd> ...\n"); return 2; }
-	const char* cmd = argv[1];
+	const bool hex = argv[1][0] == 'h';
+	const char* cmd = argv[1] + (hex ? 1 : 0);
 	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
 
@@ -172,10 +224,13 @@ int main(int argc, char** argv) {
 		vec3 scale(F(5), F(6), F(7));
 		int a = 8;
 		uint32_t pattern = 0;
-		if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init")) pattern = U(a++);
+		if (hex || !strcmp(cmd, "meshgen") || !strcmp(cmd, "init")) pattern = U(a++);
 		float wonk = F(a++);
 		const float* nodes; uint32_t nodeCount; const uint32_t* idx; uint32_t idxCount;
-		GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		if (hex)
+			GenerateHexBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		else
+			GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
 		if (!strcmp(cmd, "meshgen")) {
 			emit("nodes", 'f', nodes, nodeCount);
 			emit("idx", 'I', idx, idxCount);
@@ -187,7 +242,10 @@ int main(int argc, char** argv) {
 		if (!strcmp(cmd, "init")) {
 			emit("nodes", 'f', nodes, nodeCount);
 			emit("idx", 'I', idx, idxCount);
-			dump_geo(g);
+			if (hex)
+				dump_hex_geo(g);
+			else
+				dump_geo(g);
 			return 0;
 		}
 		uint32_t energy = U(a++), simul = U(a++);
@@ -226,8 +284,10 @@ int main(int argc, char** argv) {
 			// Replace the shuffled tOrder by the order read from stdin; Geo3d::Substep
 			// then runs GeoLinear3d::Constrain (XPBDFEM/Geo.cpp:777) over it unchanged.
 			uint32_t n = 0;
-			if (fread(&n, 4, 1, stdin) != 1 || n != g->con.tetCount) { fprintf(stderr, "bad order\n"); return 3; }
-			if (fread(g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+			const uint32_t want = hex ? g->con.hexCount : g->con.tetCount;
+			uint32_t* dst = hex ? g->hOrder : g->tOrder;
+			if (fread(&n, 4, 1, stdin) != 1 || n != want) { fprintf(stderr, "bad order\n"); return 3; }
+			if (fread(dst, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
 		}
 		if (rings) {
 			uint32_t n = 0;
@@ -245,7 +305,54 @@ int main(int argc, char** argv) {
 		return 0;
 	}
 
-	if (!strcmp(cmd, "solve")) {
+	if (hex && !strcmp(cmd, "solve")) {
+		g_rng = strtoull(argv[2], 0, 10);
+		uint32_t count = U(3), energy = U(4), simul = U(5);
+		float compliance = F(6), poisson = F(7), dt = F(8);
+		Settings s = make_settings(energy, simul, compliance, poisson, 0.0f, 0.0f, 0);
+		std::vector<double> xin(count * 24), xout(count * 24), rest(count * 24);
+		std::vector<float> win(count * 8), epo(count * 120);
+		for (uint32_t t = 0; t < count; t++) {
+			dvec3 X0[8], X[8], O[8];
+			float m[8] = {0, 0, 0, 0, 0, 0, 0, 0}, w[8];
+			// Rest hex: a box of random extents, corners jittered by up to
+			// 10% of the extent; node n at (i, j, k) = bits of n.
+			double ext[3];
+			for (int k = 0; k < 3; k++) ext[k] = 0.02 + 0.2 * urand();
+			for (int n = 0; n < 8; n++)
+				for (int k = 0; k < 3; k++) X0[n][k] = ext[k] * (((n >> k) & 1) + 0.1 * (urand() - 0.5));
+			for (int n = 0; n < 8; n++) for (int k = 0; k < 3; k++) X0[n][k] = (double)(float)X0[n][k];
+			const uint32_t is[8] = {0, 1, 2, 3, 4, 5, 6, 7};
+			ElementParamsLinearHex ep;
+			InitFiniteElement(X0, is, 1000.0f, m, &ep);
+			// Deformed state: mild, large, inverted, w = 0 on some nodes.
+			uint32_t kind = t % 8;
+			double amp = kind < 4 ? 0.05 : kind < 6 ? 0.4 : 1.5;
+			double sc = (ext[0] + ext[1] + ext[2]) / 3.0;
+			for (int n = 0; n < 8; n++) {
+				for (int k = 0; k < 3; k++) X[n][k] = X0[n][k] + amp * sc * (urand() - 0.5);
+				O[n] = X0[n];
+				w[n] = (float)(0.5 + 2.0 * urand());
+			}
+			if (kind == 6) { dvec3 tmp = X[0]; X[0] = X[7]; X[7] = tmp; }  // inverted
+			if (kind == 7) { w[0] = 0.0f; w[7] = 0.0f; }
+			for (int n = 0; n < 8; n++) {
+				win[t * 8 + n] = w[n];
+				for (int k = 0; k < 3; k++) { xin[t * 24 + n * 3 + k] = X[n][k]; rest[t * 24 + n * 3 + k] = X0[n][k]; }
+			}
+			SolveElement(dt, X, O, w, is, ep, s);
+			for (int n = 0; n < 8; n++) for (int k = 0; k < 3; k++) xout[t * 24 + n * 3 + k] = X[n][k];
+			hex_record(ep, &epo[t * 120]);
+		}
+		emit("rest", 'd', rest.data(), rest.size());
+		emit("hep", 'f', epo.data(), epo.size());
+		emit("xin", 'd', xin.data(), xin.size());
+		emit("w", 'f', win.data(), win.size());
+		emit("xout", 'd', xout.data(), xout.size());
+		return 0;
+	}
+
+	if (!hex && !strcmp(cmd, "solve")) {
 		g_rng = strtoull(argv[2], 0, 10);
 		uint32_t count = U(3), energy = U(4), simul = U(5);
 		float compliance = F(6), poisson = F(7), dt = F(8);

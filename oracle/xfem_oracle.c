@@ -76,6 +76,46 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 	return 0;
 }
 
+/* ---- linear-hex tables ------------------------------------------------------ */
+/* The reference tabulates the 8-node hex's shape functions and their
+ * gradients at the 2x2x2 Gauss points (XPBDFEM/Fem.cpp:40, :69) and the
+ * gradients at the centre (:68), printed to six decimals. Nodes and points
+ * are numbered i + 2j + 4k, with the sign 2 bit - 1 on each axis. Every
+ * entry is one of a few printed magnitudes, fixed by how many axes the node
+ * and the point agree on, so the tables are built here from those literals.
+ * The literals must be the reference's own, not the exact Gauss values: the
+ * rounding shows in every rest state. */
+static const float hex_n_lit[4] = {0.009437f, 0.035221f, 0.131446f, 0.490562f}; /* by axes agreeing */
+static const float hex_g_lit[3] = {0.022329f, 0.083333f, 0.311004f};           /* by other axes agreeing */
+
+/* ShapeFunctions<Hex, 8, 8>[p][n] */
+static float hex_n8(int p, int n) {
+	int agree = 0;
+	for (int a = 0; a < 3; a++) agree += !(((p ^ n) >> a) & 1);
+	return hex_n_lit[agree];
+}
+
+/* ShapeFunctionGradients<Hex, 8, 8>[p][n][k]: the sign of node n on axis k */
+static float hex_g8(int p, int n, int k) {
+	int agree = 0;
+	for (int a = 0; a < 3; a++)
+		if (a != k) agree += !(((p ^ n) >> a) & 1);
+	return ((n >> k) & 1) ? hex_g_lit[agree] : -hex_g_lit[agree];
+}
+
+/* ShapeFunctionGradients<Hex, 8, 1>[0][n][k] */
+static float hex_g1(int n, int k) { return ((n >> k) & 1) ? 0.125f : -0.125f; }
+
+void orc_hex_tables(float* n8, float* g8, float* g1) {
+	for (int p = 0; p < 8; p++)
+		for (int n = 0; n < 8; n++) {
+			n8[8 * p + n] = hex_n8(p, n);
+			for (int k = 0; k < 3; k++) g8[24 * p + 3 * n + k] = hex_g8(p, n, k);
+		}
+	for (int n = 0; n < 8; n++)
+		for (int k = 0; k < 3; k++) g1[3 * n + k] = hex_g1(n, k);
+}
+
 /* ---- float instantiation (reference semantics) ---------------------------- */
 #define R float
 #define SFX _f
@@ -86,6 +126,7 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 #define EPS8 0.00000001f
 #define EPS4 0.0001f
 #include "xfem_oracle_real.inc"
+#include "xfem_oracle_hex.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -105,6 +146,7 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 #define EPS8 1.0e-8
 #define EPS4 1.0e-4
 #include "xfem_oracle_real.inc"
+#include "xfem_oracle_hex.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -115,9 +157,9 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 #undef EPS4
 
 /* ---- mesh ------------------------------------------------------------------ */
-/* GenerateHexBlock + GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244). */
-void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
-                       float wonkiness, float* nodes, uint32_t* idx) {
+/* The vertices of GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-186). */
+static void block_nodes(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, float wonkiness,
+                        float* nodes) {
 	float sc[3] = {sx, sy, sz};
 	float mn[3] = {sx * (-0.5f * (float)W), sy * (-0.5f * (float)H), sz * (-0.5f * (float)D)};
 	uint32_t rs = 1;
@@ -148,26 +190,52 @@ void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, f
 			}
 		}
 	}
+}
+
+/* The 8 vertices of the block's cell (x, y, z), uniform (pattern 0) or
+ * mirrored in every other cell (XPBDFEM/MeshGen.cpp:189-214). */
+static void block_cell(uint32_t W, uint32_t H, uint32_t pattern, uint32_t x, uint32_t y, uint32_t z, uint32_t ih[8]) {
+	for (uint32_t k = 0; k < 2; k++)
+		for (uint32_t j = 0; j < 2; j++)
+			for (uint32_t i = 0; i < 2; i++) {
+				if (pattern == 0) {
+					ih[i + j * 2 + k * 4] = (x + i) + (y + j) * (W + 1) + (z + k) * (W + 1) * (H + 1);
+				} else {
+					uint32_t xx = x % 2 == 0 ? i : (1 - i);
+					uint32_t yy = y % 2 == 0 ? j : (1 - j);
+					uint32_t zz = z % 2 == 0 ? k : (1 - k);
+					uint32_t hi = i + j * 2 + k * 4;
+					if ((x + y + z) % 2 == 1) hi = 7 - hi;
+					ih[hi] = (x + xx) + (y + yy) * (W + 1) + (z + zz) * (W + 1) * (H + 1);
+				}
+			}
+}
+
+/* GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-221). */
+void orc_gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                       float wonkiness, float* nodes, uint32_t* idx) {
+	block_nodes(W, H, D, sx, sy, sz, wonkiness, nodes);
+	uint32_t ie = 0;
+	for (uint32_t z = 0; z < D; z++)
+		for (uint32_t y = 0; y < H; y++)
+			for (uint32_t x = 0; x < W; x++) {
+				uint32_t* o = idx + 9 * (size_t)ie++;
+				o[0] = 8;
+				block_cell(W, H, pattern, x, y, z, o + 1);
+			}
+}
+
+/* GenerateHexBlock + GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244). */
+void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                       float wonkiness, float* nodes, uint32_t* idx) {
+	block_nodes(W, H, D, sx, sy, sz, wonkiness, nodes);
 	uint32_t ie = 0;
 	static const uint32_t split[6][4] = {{0, 1, 5, 7}, {0, 7, 3, 1}, {0, 2, 3, 7}, {0, 7, 6, 2}, {0, 4, 6, 7}, {0, 7, 5, 4}};
 	for (uint32_t z = 0; z < D; z++)
 		for (uint32_t y = 0; y < H; y++)
 			for (uint32_t x = 0; x < W; x++) {
 				uint32_t ih[8];
-				for (uint32_t k = 0; k < 2; k++)
-					for (uint32_t j = 0; j < 2; j++)
-						for (uint32_t i = 0; i < 2; i++) {
-							if (pattern == 0) {
-								ih[i + j * 2 + k * 4] = (x + i) + (y + j) * (W + 1) + (z + k) * (W + 1) * (H + 1);
-							} else {
-								uint32_t xx = x % 2 == 0 ? i : (1 - i);
-								uint32_t yy = y % 2 == 0 ? j : (1 - j);
-								uint32_t zz = z % 2 == 0 ? k : (1 - k);
-								uint32_t hi = i + j * 2 + k * 4;
-								if ((x + y + z) % 2 == 1) hi = 7 - hi;
-								ih[hi] = (x + xx) + (y + yy) * (W + 1) + (z + zz) * (W + 1) * (H + 1);
-							}
-						}
+				block_cell(W, H, pattern, x, y, z, ih);
 				for (int t = 0; t < 6; t++) {
 					uint32_t* o = idx + 30 * (size_t)ie + 5 * t;
 					o[0] = 4;
@@ -175,6 +243,26 @@ void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, f
 				}
 				++ie;
 			}
+}
+
+/* Hex-only tagged stream (XPBDFEM/Connectivity.cpp:251-265): tag 8 = hex;
+ * anything else is an error here. With hexes == NULL only counts. */
+int orc_parse_hexes(const uint32_t* idx, uint32_t idx_count, uint32_t* hexes, uint32_t* hex_count,
+                    uint32_t* vert_count) {
+	uint32_t nh = 0, mx = 0;
+	for (uint32_t i = 0; i < idx_count; i++) {
+		if (idx[i] != 8u || (uint64_t)i + 8u >= (uint64_t)idx_count) return -1;
+		for (int n = 0; n < 8; n++) {
+			uint32_t v = idx[i + 1 + n];
+			if (v > mx) mx = v;
+			if (hexes) hexes[8 * (size_t)nh + n] = v;
+		}
+		nh++;
+		i += 8;
+	}
+	*hex_count = nh;
+	*vert_count = nh ? mx + 1 : 0;
+	return 0;
 }
 
 int orc_parse_tets(const uint32_t* idx, uint32_t idx_count, uint32_t* tets, uint32_t* tet_count, uint32_t* vert_count) {
@@ -429,6 +517,56 @@ done:
 	free(rank);
 	free(kv);
 	rings_free(&rg);
+	return rc;
+}
+
+int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours) {
+	uint64_t* used = (uint64_t*)calloc(nv ? nv : 1, 8);
+	uint32_t* colour = (uint32_t*)malloc(4 * (size_t)(nh ? nh : 1));
+	orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nh ? nh : 1));
+	int rc = -1;
+	uint32_t ncol = 0;
+	float mn[3] = {INFINITY, INFINITY, INFINITY}, sc[3] = {0.0f, 0.0f, 0.0f};
+	if (!used || !colour || !kv) goto done;
+	/* greedy colouring in id order: hexes of one colour share no vertex */
+	for (uint32_t h = 0; h < nh; h++) {
+		uint64_t u = 0;
+		for (int n = 0; n < 8; n++) u |= used[hexes[8 * (size_t)h + n]];
+		if (u == ~0ull) goto done; /* more than 64 colours */
+		uint32_t c = 0;
+		while ((u >> c) & 1u) c++;
+		colour[h] = c;
+		if (c + 1 > ncol) ncol = c + 1;
+		for (int n = 0; n < 8; n++) used[hexes[8 * (size_t)h + n]] |= 1ull << c;
+	}
+	if (orc_vertex_ranks(nodes, nv, morton, vert_rank, mn, sc)) goto done;
+	/* inside a colour: (Morton code of the centroid of the 8 vertices, id) */
+	for (uint32_t h = 0; h < nh; h++) {
+		uint32_t key = h;
+		if (morton) {
+			float c[3] = {0.0f, 0.0f, 0.0f};
+			for (int n = 0; n < 8; n++)
+				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)hexes[8 * (size_t)h + n] + j];
+			for (int j = 0; j < 3; j++) c[j] = c[j] / 8.0f;
+			key = orc_quantise(c, mn, sc);
+		}
+		kv[h].key = ((uint64_t)colour[h] << 32) | key;
+		kv[h].id = h;
+	}
+	qsort(kv, nh, sizeof(orc_kv), kv_cmp);
+	for (uint32_t c = 0; c <= ncol; c++) colour_begin[c] = 0;
+	for (uint32_t i = 0; i < nh; i++) {
+		hex_order[i] = kv[i].id;
+		colour_begin[colour[kv[i].id] + 1]++;
+	}
+	for (uint32_t c = 0; c < ncol; c++) colour_begin[c + 1] += colour_begin[c];
+	*ncolours = ncol;
+	rc = 0;
+done:
+	free(used);
+	free(colour);
+	free(kv);
 	return rc;
 }
 

@@ -8,7 +8,8 @@
  * Parity status: PINNED. The float instantiation is checked bit-for-bit
  * against golden vectors produced by the unmodified reference code
  * (oracle/build_ref.sh + oracle/refgen.cpp -> tests/golden/), covering mesh
- * generation, rest state, per-element solves and whole substeps.
+ * generation, rest state, per-element solves and whole substeps, on linear
+ * tets and on linear hexahedra (oracle/xfem_oracle_hex.inc).
  *
  * Each routine is instantiated twice from oracle/xfem_oracle_real.inc:
  *   *_f : reference semantics — positions double, element arithmetic float,
@@ -148,6 +149,44 @@ int orc_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uin
                          const uint32_t* tets, const double* ep, const uint32_t* torder, const uint32_t* vorder,
                          uint32_t nsub, const orc_params* p, uint8_t* contact);
 
+/* ---- linear hexahedra (oracle/xfem_oracle_hex.inc) ------------------------ */
+/* Hex record, 120 values (the reference's ElementParamsLinearHex,
+ * XPBDFEM/Fem.h:90-100, flattened): qcLo.Ji[0] column-major [0..8],
+ * qcLo.w[0] [9], qcHi.Ji[p] [10 + 9p ..], qcHi.w[p] [82 + p], ic.QQ[7]
+ * [90..96], ic.QR[21] [97..117], volume [118], surfaceArea [119]. */
+#define ORC_EPH 120
+/* GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-221): nodes[3(W+1)(H+1)(D+1)],
+ * idx[9 W H D] (tagged stream, 8 = hex). */
+void orc_gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
+                       uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
+/* Hex-only tagged stream; -1 for any other tag. hexes == NULL only counts. */
+int orc_parse_hexes(const uint32_t* idx, uint32_t idx_count, uint32_t* hexes,
+                    uint32_t* hex_count, uint32_t* vert_count);
+/* The hex tables as built: n8[8][8] (point, node), g8[8][8][3], g1[8][3]. */
+void orc_hex_tables(float* n8, float* g8, float* g1);
+/* GeoLinear3d::Init on a hex mesh (XPBDFEM/Geo.cpp:697-745, 736-740). */
+void orc_hex_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh,
+                         float density, float* ep, float* w, uint8_t* vflags);
+void orc_hex_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh,
+                         double density, double* ep, double* w, uint8_t* vflags);
+/* SolveElement on one hex (XPBDFEM/Fem.cpp:896): X 8x3 doubles in place, O
+ * (8x3) the substep's start, w[8]. Returns 0, or -1 for the ids the hex path
+ * does not cover (8-12: continuous-pressure and cube models). */
+int orc_solve_hex_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p);
+int orc_solve_hex_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p);
+/* Substeps of a hex mesh in the hex order `order` (GeoLinear3d::Constrain and
+ * Damp's hex loops, XPBDFEM/Geo.cpp:774-811): solve, volume passes, locks and
+ * velocities, post-step Rayleigh and PBD damping. Returns 0 or -1. */
+int orc_hex_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nh,
+                       const uint32_t* hexes, const float* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+int orc_hex_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nh,
+                       const uint32_t* hexes, const double* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+/* CalculateVolume of a hex mesh (XPBDFEM/Geo.cpp:830, XPBDFEM/Fem.cpp:1046-1071). */
+float orc_hex_volume_f(const double* X, uint32_t nh, const uint32_t* hexes, const float* ep);
+double orc_hex_volume_d(const double* X, uint32_t nh, const uint32_t* hexes, const double* ep);
+
 /* CalculateVolume (XPBDFEM/Geo.cpp:827-832, XPBDFEM/Fem.cpp:1066). */
 float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets);
 double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets);
@@ -187,6 +226,16 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
  * allocates nv + 1). Returns 0, or -1 if a limit is exceeded. */
 int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t morton,
                       uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours);
+
+/* Hex schedule: hexes coloured greedily in id order so that the hexes of one
+ * colour share no vertex (each takes the smallest colour not held by an
+ * earlier hex sharing a vertex; at most 64), then ordered inside each colour
+ * by (Morton code of the centroid of their 8 vertices, id), or by id with
+ * morton == 0. Outputs vert_rank[nv] (as orc_schedule's), hex_order[nh]
+ * (colour-major) and colour_begin[ncolours + 1] (caller allocates 65).
+ * Returns 0, or -1 if more than 64 colours are needed. */
+int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours);
 
 #ifdef __cplusplus
 }

@@ -146,6 +146,55 @@ CASES = [
                                             0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
     ("rings_wonky_cpixar_post_star", ["rings", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
                                       -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
+    # linear hexahedra (GeoLinear3d's hex loops on a GenerateHexBlock mesh):
+    # the `h` commands take the element pattern after the scale; the substep
+    # cases run in the GPU's hex colour order
+    ("hmeshgen_3x2x2_mirror_wonky", ["hmeshgen", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3]),
+    ("hinit_4x2x2", ["hinit", 4, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0]),
+    ("hinit_3x2x2_mirror_wonky", ["hinit", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3, 1000.0]),
+    ("hinit_4x3x2_aniso_wonky", ["hinit", 4, 3, 2, 0.02, 0.03, 0.04, 0, 0.4, 500.0]),
+    ("hsolve_nh_sim_nu045", ["hsolve", 41, 32, 4, 1, 0.01, 0.45, DT]),
+    ("hsolve_nh_sim_incompressible", ["hsolve", 42, 32, 4, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("hsolve_nh_serial_nu045", ["hsolve", 43, 32, 4, 0, 0.01, 0.45, DT]),
+    ("hsolve_yeohfast_sim_nu049", ["hsolve", 44, 32, 7, 1, 0.5, 0.49, DT]),
+    ("hsolve_yeohfast_serial_incompressible", ["hsolve", 45, 32, 7, 0, 3.2, 0.5, DT]),
+    ("hsolve_mixed_sim_nu045", ["hsolve", 46, 32, 3, 1, 0.01, 0.45, DT]),
+    ("hsolve_mixed_serial_nu049", ["hsolve", 47, 32, 3, 0, 0.01, 0.49, DT]),
+    ("hsolve_yeohskin_sim_nu045", ["hsolve", 48, 32, 5, 1, 0.5, 0.45, DT]),
+    ("hsolve_yeohskinsel_sim_nu049", ["hsolve", 49, 32, 6, 1, 0.5, 0.49, DT]),
+    ("hsolve_yeohskinsel_serial_nu045", ["hsolve", 50, 32, 6, 0, 0.5, 0.45, DT]),
+    ("hsolve_pixar_nu045", ["hsolve", 51, 32, 0, 1, 0.01, 0.45, DT]),
+    ("hsolve_pixar_reduced_nu040", ["hsolve", 52, 32, 1, 0, 0.02, 0.40, DT]),
+    ("hsolve_pixarsel_nu049", ["hsolve", 53, 32, 2, 1, 0.01, 0.49, DT]),
+    ("hsolve_id20_mixedsel", ["hsolve", 54, 32, 20, 1, 0.01, 0.45, DT]),
+    ("hordered_c1_nh_nu045", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                              0.0, -9.81, DT, 40, 1]),
+    ("hordered_c1_nh_incompressible", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
+                                       0.0, -9.81, DT, 40, 1]),
+    ("hordered_c1_yeohfast_nu049", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 7, 1, 3.2e-4, 0.49,
+                                    0.0, -9.81, DT, 40, 1]),
+    ("hordered_wonky_nh_serial_nu045", ["hordered", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                        -2.0, -9.81, DT, 10, 1]),
+    ("hordered_c1_mixed_nu045", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 3, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                 0.0, -9.81, DT, 40, 1]),
+    ("hordered_wonky_yeohskinsel_serial_nu049", ["hordered", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 6, 0, 0.5,
+                                                 0.49, -2.0, -9.81, DT, 10, 1]),
+    ("hordered_c1_pixar_nu045", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                 0.0, -9.81, DT, 40, 1]),
+    ("hdamped_c1_nh_nu045_post_pbd", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                      0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.0, 2, 0.1]),
+    ("hdamped_c1_nh_nu045_amortized_pbd", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5,
+                                           0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("hdamped_c1_nh_nu045_paper", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 0, 0.1]),
+    ("hdamped_c1_nh_nu045_limit", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("hdamped_wonky_yeohskin_serial_post", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 5, 0, 0.5, 0.45,
+                                            -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
+    ("hvolume_c1_nh_nu045_2", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                               0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 2]),
+    ("hvolume_wonky_pixar_1_post_pbd", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
+                                        -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
 ]
 
 
@@ -180,6 +229,15 @@ def main():
         argv = [REFGEN] + [str(a) for a in args]
         stdin = None
         extra = {}
+        if args[0] in ("hordered", "hdamped"):
+            import oracle  # noqa: E402
+            W, H, D, sx, sy, sz, pattern, wonk = args[1:9]
+            nodes, idx = oracle.gen_hex_block(W, H, D, (sx, sy, sz), pattern, wonk)
+            hexes, _ = oracle.parse_hexes(idx)
+            sch = oracle.hex_schedule(nodes, hexes, morton=1)
+            order = sch["hex_order"].astype(np.uint32)
+            stdin = struct.pack("<I", order.size) + order.tobytes()
+            extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
         if args[0] in ("ordered", "damped", "rings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]

@@ -11,6 +11,10 @@ GeoLinear3d::Damp with DampElement and PbdDamp (XPBDFEM/Geo.cpp:346-355,
 790-811; XPBDFEM/Fem.cpp:908-931; XPBDFEM/Xpbd.h:217-346), amortized or not;
 every energy model SolveElement dispatches on a linear tet
 (XPBDFEM/Fem.cpp:872-888), and volume passes (XPBDFEM/Fem.cpp:840-867).
+Linear hexahedra the same way: GenerateHexBlock, InitQuadHexFiniteElement
+(XPBDFEM/Fem.cpp:225-265), SolveElement on H8 for every energy model but the
+continuous-pressure and cube ones, and whole substeps with the hex loops of
+GeoLinear3d::Constrain and Damp (XPBDFEM/Geo.cpp:774-811).
 """
 import numpy as np
 import pytest
@@ -218,3 +222,136 @@ def test_continuous_models_refused(orc):
         p = orc.make_params(dt=1 / 1200, compliance=0.01, poisson=0.45, energy=e)
         with pytest.raises(ValueError):
             orc.solve_tet(g["xin"][:12], g["w"][:4], g["ep"][:17], p)
+
+
+# ---- linear hexahedra (GeoLinear3d's hex loops; oracle/xfem_oracle_hex.inc) ----
+HINIT = ["hinit_4x2x2", "hinit_3x2x2_mirror_wonky", "hinit_4x3x2_aniso_wonky"]
+HSOLVE = ["hsolve_nh_sim_nu045", "hsolve_nh_sim_incompressible", "hsolve_nh_serial_nu045",
+          "hsolve_yeohfast_sim_nu049", "hsolve_yeohfast_serial_incompressible", "hsolve_mixed_sim_nu045",
+          "hsolve_mixed_serial_nu049", "hsolve_yeohskin_sim_nu045", "hsolve_yeohskinsel_sim_nu049",
+          "hsolve_yeohskinsel_serial_nu045", "hsolve_pixar_nu045", "hsolve_pixar_reduced_nu040",
+          "hsolve_pixarsel_nu049", "hsolve_id20_mixedsel"]
+HSUBSTEP = ["hordered_c1_nh_nu045", "hordered_c1_nh_incompressible", "hordered_c1_yeohfast_nu049",
+            "hordered_wonky_nh_serial_nu045", "hordered_c1_mixed_nu045", "hordered_wonky_yeohskinsel_serial_nu049",
+            "hordered_c1_pixar_nu045", "hdamped_c1_nh_nu045_post_pbd", "hdamped_c1_nh_nu045_amortized_pbd",
+            "hdamped_c1_nh_nu045_paper", "hdamped_c1_nh_nu045_limit", "hdamped_wonky_yeohskin_serial_post",
+            "hvolume_c1_nh_nu045_2", "hvolume_wonky_pixar_1_post_pbd"]
+
+
+def test_hex_meshgen_bit_exact(orc):
+    g = golden("hmeshgen_3x2x2_mirror_wonky")
+    a = golden_args("hmeshgen_3x2x2_mirror_wonky")["args"]
+    nodes, idx = orc.gen_hex_block(a[1], a[2], a[3], tuple(a[4:7]), a[7], a[8])
+    assert np.array_equal(idx, g["idx"])
+    assert np.array_equal(nodes.view(np.uint32), g["nodes"].view(np.uint32))
+
+
+def test_hex_tables_structure(orc):
+    """The hex tables built from the reference's printed magnitudes: shape
+    functions sum to ~1 at every point, gradients to ~0, and the centre
+    gradients are the means of the Gauss-point ones up to the printing."""
+    n8, g8, g1 = orc.hex_tables()
+    assert np.allclose(n8.sum(1), 1.0, atol=1e-5)
+    assert np.allclose(g8.sum(1), 0.0, atol=1e-6)
+    assert np.allclose(g8.mean(0), g1, atol=1e-6)
+    assert np.array_equal(n8, n8.T)  # the point and node numberings agree
+
+
+@pytest.mark.parametrize("name", HINIT)
+def test_hex_rest_state_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    hexes, nv = orc.parse_hexes(g["idx"])
+    assert np.array_equal(hexes.reshape(-1), g["hex_idx"])
+    ep, w, fl = orc.hex_init_rest(g["nodes"], hexes, a[9])
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["hep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+    assert np.array_equal(orc.minstd_order(hexes.shape[0]), g["horder"])
+    X = g["nodes"].astype(np.float64)
+    assert np.float32(orc.hex_volume(X, hexes, ep)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+@pytest.mark.parametrize("name", HSOLVE)
+def test_hex_element_solve_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    p = orc.make_params(dt=a[7], compliance=a[5], poisson=a[6], energy=a[3], simultaneous=bool(a[4]))
+    n = a[2]
+    xin, xout = g["xin"].reshape(n, 8, 3), g["xout"].reshape(n, 8, 3)
+    ep, w, rest = g["hep"].reshape(n, orc.HEX_EP), g["w"].reshape(n, 8), g["rest"].reshape(n, 8, 3)
+    one = np.arange(8, dtype=np.uint32)[None]
+    for t in range(n):
+        e, _, _ = orc.hex_init_rest(rest[t].astype(np.float32).reshape(-1), one, 1000.0)
+        assert np.array_equal(e[0].view(np.uint32), ep[t].view(np.uint32)), t
+        x = orc.solve_hex(xin[t], w[t], ep[t], p, O=rest[t])
+        assert np.array_equal(x.view(np.uint64), xout[t].view(np.uint64)), t
+
+
+def hex_params(orc, a, g, tick):
+    """orc_params of an `hordered` / `hdamped` fixture (refgen's argument order)."""
+    energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[10:19]
+    kw = dict(rayleigh_type=2)
+    if a[0] == "hdamped":
+        damping, pbd, drag, rtype, spacing = a[19:24]
+        d = g["derived"]
+        kw = dict(damping=damping, rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(d[0]),
+                  pbd_coeff_amortized=float(d[1]), drag=float(d[2]), volume_passes=a[24] if len(a) > 24 else 0)
+    return orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
+                           gravity=(gx, gy, 0.0), lock=bool(lock), tick=tick, **kw)
+
+
+@pytest.mark.parametrize("name", HSUBSTEP)
+def test_hex_substeps_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[9], a[17]
+    hexes, nv = orc.parse_hexes(g["idx"])
+    ep, w, fl = orc.hex_init_rest(g["nodes"], hexes, dens)
+    # the fixture ran in the hex schedule's colour order
+    sch = orc.hex_schedule(g["nodes"], hexes)
+    assert np.array_equal(sch["hex_order"], g["order"])
+    assert np.array_equal(sch["colour_hex_begin"], g["colour_hex_begin"])
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lm = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.hex_substeps(X0, V0, w, hexes, ep, g["order"], 1, hex_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.hex_substeps(X1, V1, w1, hexes, ep, g["order"], nsub - 1, hex_params(orc, a, g, 1),
+                                    lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(orc.hex_volume(Xn, hexes, ep)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+def test_hex_schedule_is_a_valid_colouring(orc):
+    """Hexes of one colour share no vertex; greedy first fit in id order
+    (each hex takes the smallest colour free among earlier neighbours)."""
+    nodes, idx = orc.gen_hex_block(5, 4, 3, (0.1, 0.1, 0.1), 1, 0.3)
+    hexes, nv = orc.parse_hexes(idx)
+    s = orc.hex_schedule(nodes, hexes)
+    cb, order = s["colour_hex_begin"], s["hex_order"]
+    assert sorted(order.tolist()) == list(range(hexes.shape[0]))
+    colour = np.empty(hexes.shape[0], np.int64)
+    for c in range(s["colours"]):
+        hs = order[cb[c]:cb[c + 1]]
+        colour[hs] = c
+        verts = hexes[hs].reshape(-1)
+        assert np.unique(verts).size == verts.size
+    for h in range(hexes.shape[0]):
+        nb = [k for k in range(h) if np.intersect1d(hexes[k], hexes[h]).size]
+        taken = {int(colour[k]) for k in nb}
+        assert colour[h] == min(set(range(65)) - taken)
+    assert s["colours"] == 8  # a structured block needs exactly 8
+
+
+def test_hex_continuous_and_cube_models_refused(orc):
+    nodes, idx = orc.gen_hex_block(2, 1, 1, (0.1, 0.1, 0.1))
+    hexes, nv = orc.parse_hexes(idx)
+    ep, w, fl = orc.hex_init_rest(nodes, hexes, 1000.0)
+    X = nodes.astype(np.float64).reshape(-1, 3)
+    for e in (8, 9, 10, 11, 12):
+        p = orc.make_params(dt=1e-3, compliance=1e-3, poisson=0.45, energy=e)
+        with pytest.raises(ValueError):
+            orc.hex_substeps(X, np.zeros_like(X), w, hexes, ep, np.arange(2, dtype=np.uint32), 1, p)
