@@ -28,6 +28,12 @@
  *   wasm exports UpdateSettings / AddBlock / FinishAddingBlocks / ResetDemo
  *                                wasm/main.cpp:8-17, 71-95
  *   GenerateTetBlock             XPBDFEM/MeshGen.cpp:223-244
+ *   GenerateHexBlock             XPBDFEM/MeshGen.cpp:156-221
+ *
+ * Meshes of linear hexahedra (tag 8) run in hex mode: GeoLinear3d's hex loops
+ * (XPBDFEM/Geo.cpp:736-740, 777-811) with SolveElement on
+ * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), the energy models 0-7 and
+ * above 12. A mesh holds tets or hexes, not both, and so does a handle.
  */
 #ifndef XFEM_H
 #define XFEM_H
@@ -42,7 +48,7 @@ extern "C" {
 /* ---- status codes ---------------------------------------------------------- */
 #define XFEM_OK 0
 #define XFEM_EINVAL (-1)          /* bad argument (null pointer, size mismatch, index out of range) */
-#define XFEM_EUNSUPPORTED (-2)    /* hex elements, energy models or settings this path does not run */
+#define XFEM_EUNSUPPORTED (-2)    /* meshes, energy models or settings this path does not run */
 #define XFEM_ENOMEM (-3)          /* host or device allocation failed */
 #define XFEM_ECUDA (-4)           /* CUDA runtime error (no device, launch or copy failure) */
 #define XFEM_EDEVICE_TIMEOUT (-5) /* a device-side bounded wait (grid barrier) ran out */
@@ -159,7 +165,10 @@ int xfem_settings_default(xfem_settings* s);
  * idxDataCount, autoResize = false), XPBDFEM/Geo.cpp:697-772: connectivity,
  * double-precision rest positions, Left/Right flags, rest state per tet,
  * lumped masses and inverse masses — then builds the colour schedule and
- * uploads everything. Hex elements (tag 8) return XFEM_EUNSUPPORTED. */
+ * uploads everything. A mesh of hexes (tag 8) gets the hex rest state
+ * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
+ * a mesh mixing tets and hexes, or a hex mesh with the continuous-pressure or
+ * cube models (energy 8-12), returns XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -294,6 +303,32 @@ int xfem_get_ring_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_ord
 int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                                uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_order,
                                uint32_t* colour_begin, uint32_t* ncolours);
+
+/* ---- linear hexahedra (hex mode) --------------------------------------------- */
+/* Hexes of one body (0 for a tet body). */
+int xfem_body_hex_count(const xfem_body* b, uint32_t body, uint32_t* nhexes);
+/* Rest state per hex (caller order) as 120 floats, ElementParamsLinearHex
+ * (XPBDFEM/Fem.h:90-100) flattened: qcLo.Ji[0] column-major [0..8],
+ * qcLo.w[0] [9], qcHi.Ji[p] [10 + 9p ..], qcHi.w[p] [82 + p], ic.QQ[7]
+ * [90..96], ic.QR[21] [97..117], volume [118], surfaceArea [119]; and the
+ * rest inverse masses. XFEM_EUNSUPPORTED for a tet body. */
+int xfem_get_hex_rest_state(const xfem_body* b, uint32_t body, float* out_ep120, float* out_w);
+/* The hex schedule: device rank of each vertex, the hex order (colour-major;
+ * the hexes of one colour share no vertex) and the colour offsets in it
+ * (ncolours + 1 entries, at most 65). */
+int xfem_get_hex_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_rank, uint32_t* hex_order,
+                          uint32_t* colour_begin, uint32_t* ncolours);
+/* The same two, computed on the host without a handle or a GPU. */
+int xfem_compute_hex_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, float* out_ep120, float* out_w,
+                                uint8_t* out_flags);
+int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* hex_order,
+                              uint32_t* colour_begin, uint32_t* ncolours);
+/* GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-221): nodes[3 (W+1)(H+1)(D+1)],
+ * idx[9 W H D] (tag 8 and 8 vertex ids per hex). */
+int xfem_generate_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
+                            uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
 
 /* ---- helpers --------------------------------------------------------------- */
 /* volumeAndTimeCorrectedPbdDamping and its amortized form for a substep of

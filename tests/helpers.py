@@ -39,3 +39,23 @@ class OracleRun:
             self.X, self.V, self.w, self.tets, self.ep, self.order, n, p, lock_mask=self.lock,
             tet_mu=self.tet_mu, dtype=self.dtype, want_lambdas=True)
         return self
+
+
+class HexOracleRun:
+    """The oracle's state for one hex body, stepped in the body's hex order."""
+
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+        self.hexes, nv = oracle.parse_hexes(idx)
+        self.ep, self.w, fl = oracle.hex_init_rest(nodes, self.hexes, density, dtype)
+        self.lock = (fl & 1).astype(np.uint8)
+        self.X = np.asarray(nodes, np.float64).reshape(-1, 3).copy()
+        self.V = np.zeros_like(self.X)
+        self.s = settings
+        self.order = order
+        self.dtype = dtype
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt)
+        self.X, self.V, self.w, _ = oracle.hex_substeps(self.X, self.V, self.w, self.hexes, self.ep, self.order, n, p,
+                                                        lock_mask=self.lock, dtype=self.dtype)
+        return self

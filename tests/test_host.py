@@ -177,3 +177,75 @@ def test_ring_schedule_bit_exact_vs_oracle(orc, morton, mesh):
     assert s["colours"] == o["colours"]
     assert np.array_equal(s["vert_order"], o["vert_order"])
     assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])
+
+
+# ---- linear hexahedra: the host side of hex mode ----
+def test_generate_hex_block_bit_exact():
+    g = golden("hmeshgen_3x2x2_mirror_wonky")
+    a = golden_args("hmeshgen_3x2x2_mirror_wonky")["args"]
+    nodes, idx = xfem.generate_hex_block(a[1], a[2], a[3], tuple(a[4:7]), a[7], a[8])
+    assert np.array_equal(idx, g["idx"])
+    assert np.array_equal(nodes.view(np.uint32), g["nodes"].view(np.uint32))
+    # the tet block is the same grid split six ways
+    tn, _ = xfem.generate_tet_block(a[1], a[2], a[3], tuple(a[4:7]), a[7], a[8])
+    assert np.array_equal(tn.view(np.uint32), nodes.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", ["hinit_4x2x2", "hinit_3x2x2_mirror_wonky", "hinit_4x3x2_aniso_wonky"])
+def test_hex_rest_state_bit_exact_vs_reference(name):
+    """InitQuadHexFiniteElement (XPBDFEM/Fem.cpp:225-265) through
+    GeoLinear3d::Init: records, inverse masses and flags."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    ep, w, fl = xfem.compute_hex_rest_state(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["hep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_hex_rest_state_matches_oracle_on_jittered_meshes(orc, seed):
+    rng = np.random.default_rng(seed)
+    nodes, idx = xfem.generate_hex_block(5, 4, 3, (0.03, 0.05, 0.04), seed % 2, 0.4)
+    nodes = (nodes + rng.normal(0, 0.002, nodes.shape)).astype(np.float32)
+    ep, w, fl = xfem.compute_hex_rest_state(nodes, idx, 700.0)
+    hexes, _ = orc.parse_hexes(idx)
+    e2, w2, f2 = orc.hex_init_rest(nodes, hexes, 700.0)
+    assert np.array_equal(ep.view(np.uint32), e2.view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), w2.view(np.uint32))
+    assert np.array_equal(fl, f2)
+
+
+@pytest.mark.parametrize("morton", [True, False])
+@pytest.mark.parametrize("pattern", [0, 1])
+def test_hex_schedule_bit_exact_vs_oracle(orc, morton, pattern):
+    nodes, idx = xfem.generate_hex_block(6, 5, 3, (0.1, 0.1, 0.1), pattern, 0.3)
+    s = xfem.compute_hex_schedule(nodes, idx, morton=morton)
+    hexes, _ = orc.parse_hexes(idx)
+    o = orc.hex_schedule(nodes, hexes, morton=1 if morton else 0)
+    for k in ("vert_rank", "hex_order", "colour_hex_begin"):
+        assert np.array_equal(s[k], o[k]), k
+    cb, order = s["colour_hex_begin"], s["hex_order"]
+    for c in range(s["colours"]):
+        verts = hexes[order[cb[c]:cb[c + 1]]].reshape(-1)
+        assert np.unique(verts).size == verts.size
+
+
+def test_hex_mesh_errors():
+    nodes, idx = xfem.generate_hex_block(2, 2, 2, (0.1, 0.1, 0.1))
+    tn, ti = xfem.generate_tet_block(2, 2, 2, (0.1, 0.1, 0.1))
+    # a tet-only helper refuses a hex mesh and the other way round
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_rest_state(nodes, idx, 1000.0)
+    assert e.value.code == xfem.EUNSUPPORTED
+    with pytest.raises(xfem.XfemError):
+        xfem.compute_hex_rest_state(tn, ti, 1000.0)
+    # mixing tets and hexes in one stream
+    mixed = np.concatenate([idx[:9], ti[:5]])
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_hex_rest_state(nodes, mixed, 1000.0)
+    assert e.value.code == xfem.EUNSUPPORTED
+    # a truncated hex record
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_hex_rest_state(nodes, idx[:-1], 1000.0)
+    assert e.value.code == xfem.EINVAL

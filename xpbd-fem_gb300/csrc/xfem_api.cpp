@@ -48,6 +48,12 @@ struct BodyHost {
 	RingSchedule rings;               // continuous-pressure models only
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
+	// hex bodies (linear hexahedra; no tets)
+	bool hex = false;
+	uint32_t nh = 0;
+	std::vector<uint32_t> hexes;      // 8 per hex, caller order
+	std::vector<float> hep;           // rest::kHexRec per hex
+	HexSchedule hsched;
 };
 
 template <typename T>
@@ -117,6 +123,11 @@ struct xfem_body {
 	DevBuf<float4> ring_ent;
 	DevBuf<uint2> pbd_cl;
 	DevBuf<uint4> pbd_ent;
+	// hex mode (linear hexahedra)
+	bool hex_mode = false;
+	DevBuf<uint4> hex_vid;
+	DevBuf<float4> hex_rec;
+	DevBuf<uint32_t> hex_cb, hex_flat;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -298,14 +309,19 @@ int check_device_error(xfem_body* h) {
 int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	if (!m.node_data || !m.idx_data) return fail(XFEM_EINVAL, "null mesh array");
 	if (m.node_data_count % 3) return fail(XFEM_EINVAL, "node_data_count must be a multiple of 3");
+	uint32_t ntag[2] = {0, 0};
 	for (uint32_t i = 0; i < m.idx_data_count;) {
 		const uint32_t tag = m.idx_data[i];
-		if (tag == 8u) return fail(XFEM_EUNSUPPORTED, "hex elements (tag 8) are not supported by this path");
-		if (tag != 4u) return fail(XFEM_EINVAL, "unknown element tag " + std::to_string(tag) + " at " + std::to_string(i));
-		i += 5;
+		if (tag != 4u && tag != 8u)
+			return fail(XFEM_EINVAL, "unknown element tag " + std::to_string(tag) + " at " + std::to_string(i));
+		ntag[tag == 8u]++;
+		i += tag + 1;
 	}
+	if (ntag[0] && ntag[1]) return fail(XFEM_EUNSUPPORTED, "meshes mixing tets (tag 4) and hexes (tag 8) are not supported");
+	b.hex = ntag[1] > 0;
 	uint32_t nv = 0;
-	if (parse_tets(m.idx_data, m.idx_data_count, b.tets, nv)) return fail(XFEM_EINVAL, "truncated index stream");
+	if (b.hex ? parse_hexes(m.idx_data, m.idx_data_count, b.hexes, nv) : parse_tets(m.idx_data, m.idx_data_count, b.tets, nv))
+		return fail(XFEM_EINVAL, "truncated index stream");
 	// GeoLinear3d::Init asserts vertCount == nodeDataCount / 3 (XPBDFEM/Geo.cpp:700)
 	if (nv != m.node_data_count / 3)
 		return fail(XFEM_EINVAL, "vertex count " + std::to_string(nv) + " implied by the index stream != node_data_count/3 = " +
@@ -313,6 +329,7 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	if (!(m.density > 0.0f)) return fail(XFEM_EINVAL, "density must be > 0");
 	b.nv = nv;
 	b.nt = (uint32_t)(b.tets.size() / 4);
+	b.nh = (uint32_t)(b.hexes.size() / 8);
 	b.nodes.assign(m.node_data, m.node_data + m.node_data_count);
 	return XFEM_OK;
 }
@@ -322,6 +339,11 @@ void host_rest(const xfem_mesh& m, BodyHost& b) {
 	b.ep.resize(17 * (size_t)b.nt);
 	b.w0.resize(b.nv);
 	b.vflags.resize(b.nv);
+	if (b.hex) {
+		b.hep.resize((size_t)rest::kHexRec * b.nh);
+		hex_init_rest(b.nodes.data(), b.nv, b.hexes.data(), b.nh, m.density, b.hep.data(), b.w0.data(), b.vflags.data());
+		return;
+	}
 	init_rest(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
 }
 
@@ -340,7 +362,20 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	}
 	rc = validate_settings(b.settings);
 	if (rc) return rc;
-	const bool ring = model_of((b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK) == kModelRing;
+	const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+	const bool ring = model_of(energy) == kModelRing;
+	if (b.hex) {
+		// linear hexahedra: set-up on the host (rest state, Morton vertex
+		// ranks, the hex colouring)
+		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CUBE_SKIN)
+			return fail(XFEM_EUNSUPPORTED, "hex meshes run the energy models 0-7 and above 12 (not the continuous-pressure "
+			                               "or cube models)");
+		host_rest(m, b);
+		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
+		if (hex_schedule(b.nodes.data(), b.nv, b.hexes.data(), b.nh, morton, b.hsched))
+			return fail(XFEM_ELIMIT, "the hex colouring needs more than 64 colours");
+		return XFEM_OK;
+	}
 	std::vector<uint32_t> off, lst;
 	if (!gpu) {
 		host_rest(m, b);
@@ -548,6 +583,67 @@ int build_rings(xfem_body* h) {
 	h->ctx.pbd_colours = pcol;
 	h->device_bytes += pcb.size() * 4 + pcl.size() * 8 + pent.size() * 16;
 	h->device_bytes += hdr.size() * 16 + node.size() * 4 + ent.size() * 16 + cb.size() * 4;
+	return XFEM_OK;
+}
+
+// The hexes of every body in device order (colour-major, bodies in order
+// inside a colour): vertex ids, records (structure of arrays of 30 float4:
+// the centre's inverse jacobian and weight, volume, surface area, QQ, QR,
+// then the 2x2x2 points' inverse jacobians and weights) and each hex's index
+// in its body's hex order.
+int build_hexes(xfem_body* h) {
+	uint32_t ncol = 0, nhex = 0;
+	for (const BodyHost& b : h->bodies) {
+		ncol = std::max(ncol, b.hsched.ncolours);
+		nhex += b.nh;
+	}
+	std::vector<uint4> vid(2 * (size_t)nhex);
+	std::vector<uint32_t> cb(ncol + 1, 0), flat(nhex);
+	std::vector<float4> rec(30 * (size_t)nhex);
+	uint32_t o = 0;
+	for (uint32_t c = 0; c < ncol; c++) {
+		cb[c] = o;
+		for (const BodyHost& b : h->bodies) {
+			const HexSchedule& hs = b.hsched;
+			if (c >= hs.ncolours) continue;
+			for (uint32_t k = hs.colour_begin[c]; k < hs.colour_begin[c + 1]; k++, o++) {
+				const uint32_t hx = hs.order[k];
+				uint32_t d[8];
+				for (int n = 0; n < 8; n++) d[n] = b.vbase + b.sched.vert_rank[b.hexes[8 * (size_t)hx + n]];
+				vid[2 * (size_t)o] = make_uint4(d[0], d[1], d[2], d[3]);
+				vid[2 * (size_t)o + 1] = make_uint4(d[4], d[5], d[6], d[7]);
+				flat[o] = k;
+				const float* e = &b.hep[(size_t)rest::kHexRec * hx];
+				float r[120];
+				for (int j = 0; j < 9; j++) r[j] = e[rest::kHexJL + j];
+				r[9] = e[rest::kHexWL];
+				r[10] = e[rest::kHexVol];
+				r[11] = e[rest::kHexArea];
+				for (int j = 0; j < 7; j++) r[12 + j] = e[rest::kHexQQ + j];
+				for (int j = 0; j < 21; j++) r[19 + j] = e[rest::kHexQR + j];
+				for (int j = 0; j < 72; j++) r[40 + j] = e[rest::kHexJH + j];
+				for (int j = 0; j < 8; j++) r[112 + j] = e[rest::kHexWH + j];
+				for (int k4 = 0; k4 < 30; k4++)
+					rec[(size_t)k4 * nhex + o] = make_float4(r[4 * k4], r[4 * k4 + 1], r[4 * k4 + 2], r[4 * k4 + 3]);
+			}
+		}
+	}
+	cb[ncol] = o;
+	XCUDA(h->hex_vid.alloc(vid.size()));
+	XCUDA(h->hex_rec.alloc(rec.size()));
+	XCUDA(h->hex_cb.alloc(cb.size()));
+	XCUDA(h->hex_flat.alloc(flat.size()));
+	auto up = [&](void* dst, const void* src, size_t bytes) {
+		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+	};
+	XCUDA(up(h->hex_vid.p, vid.data(), vid.size() * sizeof(uint4)));
+	XCUDA(up(h->hex_rec.p, rec.data(), rec.size() * sizeof(float4)));
+	XCUDA(up(h->hex_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(h->hex_flat.p, flat.data(), flat.size() * 4));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	h->ctx.hex_colours = ncol;
+	h->ctx.nhex = nhex;
+	h->device_bytes += vid.size() * 16 + rec.size() * 16 + cb.size() * 4 + flat.size() * 4;
 	return XFEM_OK;
 }
 
@@ -768,7 +864,7 @@ int build_device(xfem_body* h) {
 		for (size_t i = 0; i < 4 * (size_t)b.nt; i++) tets_dev[tbase + i] = b.vbase + b.sched.vert_rank[b.tets[i]];
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
-		params[bi].ntets = b.nt;
+		params[bi].ntets = b.hex ? b.nh : b.nt;
 		params[bi].nverts = b.nv;
 	}
 	clk.lap("vertex state");
@@ -864,6 +960,10 @@ int build_device(xfem_body* h) {
 		int rr = build_rings(h);
 		if (rr) return rr;
 	}
+	if (h->hex_mode) {
+		int rr = build_hexes(h);
+		if (rr) return rr;
+	}
 	DevCtx& c = h->ctx;
 	c.vert = h->vert.p;
 	c.cblk = h->cblk.p;
@@ -913,6 +1013,10 @@ int build_device(xfem_body* h) {
 	c.pbd_ent = h->pbd_ent.p;
 	c.tet_verts = h->tets_dev.p;
 	if (h->ring_mode) c.ext = ring_damp_of(h->bodies) ? 1u : 0u;
+	c.hex_vid = h->hex_vid.p;
+	c.hex_rec = h->hex_rec.p;
+	c.colour_hex_begin = h->hex_cb.p;
+	c.hex_flat = h->hex_flat.p;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -1069,6 +1173,10 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (nring && nring != nbodies)
 		return fail(XFEM_EUNSUPPORTED, "continuous-pressure models (energy 8-10) and element models cannot share a handle");
 	h->ring_mode = nring > 0;
+	uint32_t nhexb = 0;
+	for (const BodyHost& b : h->bodies) nhexb += b.hex ? 1u : 0u;
+	if (nhexb && nhexb != nbodies) return fail(XFEM_EUNSUPPORTED, "hex meshes and tet meshes cannot share a handle");
+	h->hex_mode = nhexb > 0;
 	clk.lap("rest state + schedule");
 	rc = build_device(h.get());
 	clk.lap("device layout");
@@ -1097,6 +1205,11 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 	if (h->ring_mode) {
 		const int e = launch_rings(h->ctx, 256, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
+		return XFEM_OK;
+	}
+	if (h->hex_mode) {
+		const int e = launch_hexes(h->ctx, 256, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("hex launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
 	int rc = autotune(h, nsub, dt);
@@ -1226,14 +1339,17 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	if (!s) return fail(XFEM_EINVAL, "null settings");
 	int rc = validate_settings(*s);
 	if (rc) return rc;
-	if ((model_of((s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK) == kModelRing) != h->ring_mode)
+	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+	if (h->hex_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CUBE_SKIN)
+		return fail(XFEM_EUNSUPPORTED, "hex meshes run the energy models 0-7 and above 12");
+	if ((model_of(energy) == kModelRing) != h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
 		                               "element models needs a new handle (their schedules differ)");
 	const bool material = s->compliance != b->settings.compliance;
 	b->settings = *s;
 	XCUDA(cudaSetDevice(h->device));
 	BodyParams p = make_params(*s);
-	p.ntets = b->nt;
+	p.ntets = b->hex ? b->nh : b->nt;
 	p.nverts = b->nv;
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	// Settings::tickId: the handle's substep counter continues from here
@@ -1260,7 +1376,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 		}
 	}
 	if (h->ring_mode) h->ctx.ext = ring_damp_of(h->bodies) ? 1u : 0u;
-	if (material && b->tet_mu.empty()) return update_material(h, *b);
+	if (material && b->tet_mu.empty() && !h->hex_mode) return update_material(h, *b);
 	return XFEM_OK;
 }
 
@@ -1290,6 +1406,7 @@ int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
 	if (!b) return XFEM_EINVAL;
 	if (h->ring_mode && mu)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) take the body's material only");
+	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "hex meshes take the body's material only");
 	if (mu) {
 		for (uint32_t t = 0; t < b->nt; t++)
 			if (!(mu[t] > 0.0f) || !isfinite(mu[t])) return fail(XFEM_EINVAL, "tet mu must be finite and > 0");
@@ -1318,6 +1435,12 @@ int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, f
 	if (h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) have no allocation-free launch");
 	XCUDA(cudaSetDevice(h->device));
+	if (h->hex_mode) {
+		// the hex launch allocates nothing
+		const int e = launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("hex launch: ") + cudaGetErrorString((cudaError_t)e));
+		return check_device_error(h);
+	}
 	int dev_err = 0;
 	const int e = launch_substeps_noalloc(h->ctx, h->cfg.block, h->cfg.warp_smem, h->cfg.lambdas, (uint32_t)n, dt,
 	                                      h->stream, h->device, &dev_err);
@@ -1356,6 +1479,7 @@ int xfem_get_lambdas(xfem_body* h, uint32_t body, float* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
+	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "hex meshes keep no multipliers");
 	if (!h->tlam.p) return fail(XFEM_EINVAL, "create the handle with keep_lambdas = 1");
 	XCUDA(cudaSetDevice(h->device));
 	std::vector<float2> all(h->tlam.n);
@@ -1374,6 +1498,38 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
 	XCUDA(cudaSetDevice(h->device));
+	if (b->hex) {
+		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per hex: rest
+		// volume times the weighted det F over the 2x2x2 points, in double
+		std::vector<float> x(3 * (size_t)b->nv);
+		const int rc = get_xyz(h, body, 0, x.data());
+		if (rc) return rc;
+		double v = 0.0;
+		for (uint32_t hx = 0; hx < b->nh; hx++) {
+			const uint32_t* is = &b->hexes[8 * (size_t)hx];
+			const float* e = &b->hep[(size_t)rest::kHexRec * hx];
+			double P[7][3];
+			for (int i = 0; i < 7; i++)
+				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[7] + k];
+			double scale = 0.0;
+			for (int p = 0; p < 8; p++) {
+				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+				for (int n = 0; n < 7; n++)
+					for (int c = 0; c < 3; c++)
+						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::hex_g8(p, n, r) * P[n][c];
+				const float* ji = e + rest::kHexJH + 9 * p;
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
+				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+				scale += (double)e[rest::kHexWH + p] * det;
+			}
+			v += (double)e[rest::kHexVol] * scale;
+		}
+		*out = v;
+		return XFEM_OK;
+	}
 	size_t tb = 0;
 	for (uint32_t i = 0; i < body; i++) tb += 4 * (size_t)h->bodies[i].nt;
 	const int e = launch_volume(h->vert.p, h->tets_dev.p + tb, b->nt, h->vol.p, h->stream);
@@ -1385,6 +1541,7 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 int xfem_get_rest_state(const xfem_body* h, uint32_t body, float* out_ep17, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
+	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex body: use xfem_get_hex_rest_state");
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
@@ -1394,6 +1551,7 @@ int xfem_get_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, ui
                       uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
+	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex body: use xfem_get_hex_schedule");
 	const Schedule& s = b.sched;
 	if (vert_rank) memcpy(vert_rank, s.vert_rank.data(), s.vert_rank.size() * 4);
 	if (ncolours) *ncolours = s.ncolours;
@@ -1425,6 +1583,7 @@ int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, co
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
 	const int rc = prepare_mesh(m, b);
 	if (rc) return rc;
+	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_rest_state");
 	host_rest(m, b);
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
@@ -1442,6 +1601,7 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
 	int rc = prepare_mesh(m, b);
 	if (rc) return rc;
+	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_schedule");
 	if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, cluster_mode == 1 ? 0u : 1u, no_morton ? 0u : 1u, b.sched))
 		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
 	if (nclusters) *nclusters = b.sched.nclusters;
@@ -1476,6 +1636,74 @@ int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count,
 	if (rc == -2) return fail(XFEM_ELIMIT, "a vertex one-ring has more than 64 tets or 32 vertices");
 	if (rc) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
 	return ring_schedule_out(b.rings, vert_order, colour_begin, ncolours);
+}
+
+int xfem_body_hex_count(const xfem_body* h, uint32_t body, uint32_t* nhexes) {
+	if (!h || body >= h->bodies.size() || !nhexes) return fail(XFEM_EINVAL, "bad handle, body index or output");
+	*nhexes = h->bodies[body].nh;
+	return XFEM_OK;
+}
+
+int xfem_get_hex_rest_state(const xfem_body* h, uint32_t body, float* out_ep120, float* out_w) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (!b.hex) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	if (out_ep120) memcpy(out_ep120, b.hep.data(), b.hep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	return XFEM_OK;
+}
+
+static int hex_schedule_out(const BodyHost& b, uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin,
+                            uint32_t* ncolours) {
+	if (vert_rank) memcpy(vert_rank, b.sched.vert_rank.data(), b.sched.vert_rank.size() * 4);
+	if (hex_order) memcpy(hex_order, b.hsched.order.data(), b.hsched.order.size() * 4);
+	if (colour_begin) memcpy(colour_begin, b.hsched.colour_begin.data(), b.hsched.colour_begin.size() * 4);
+	if (ncolours) *ncolours = b.hsched.ncolours;
+	return XFEM_OK;
+}
+
+int xfem_get_hex_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, uint32_t* hex_order,
+                          uint32_t* colour_begin, uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (!b.hex) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	return hex_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int xfem_compute_hex_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, float* out_ep120, float* out_w,
+                                uint8_t* out_flags) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (!b.hex) return fail(XFEM_EINVAL, "not a hex mesh");
+	host_rest(m, b);
+	if (out_ep120) memcpy(out_ep120, b.hep.data(), b.hep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
+	return XFEM_OK;
+}
+
+int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* hex_order,
+                              uint32_t* colour_begin, uint32_t* ncolours) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (!b.hex) return fail(XFEM_EINVAL, "not a hex mesh");
+	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
+	if (hex_schedule(b.nodes.data(), b.nv, b.hexes.data(), b.nh, no_morton ? 0u : 1u, b.hsched))
+		return fail(XFEM_ELIMIT, "the hex colouring needs more than 64 colours");
+	return hex_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int xfem_generate_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                            float wonkiness, float* out_nodes, uint32_t* out_idx) {
+	if (!out_nodes || !out_idx) return fail(XFEM_EINVAL, "null output");
+	gen_hex_block(W, H, D, sx, sy, sz, pattern, wonkiness, out_nodes, out_idx);
+	return XFEM_OK;
 }
 
 int xfem_pbd_damping_coefficients(float pbd_damping, float substep_dt, float spacing, float* out2) {
@@ -1561,6 +1789,7 @@ int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpo
 	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
 	if (nsub == 0) return fail(XFEM_EINVAL, "substeps must be > 0");
 	if (ntips && !tips) return fail(XFEM_EINVAL, "null tips");
+	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "the adjoint covers tet meshes only");
 	for (const BodyHost& b : h->bodies) {
 		const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 		if (model_of(energy) != kModelNeo || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))

@@ -50,7 +50,7 @@ void init_rest(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32
 	for (uint32_t i = 0; i < nverts; i++) w[i] = 1.0f / w[i];  // XPBDFEM/Geo.cpp:744
 }
 
-void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+void gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
                    float wonkiness, float* nodes, uint32_t* idx) {
 	const float sc[3] = {sx, sy, sz};
 	const float mn[3] = {sx * (-0.5f * (float)W), sy * (-0.5f * (float)H), sz * (-0.5f * (float)D)};
@@ -72,12 +72,12 @@ void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float
 				const size_t i = x + (size_t)y * (W + 1) + (size_t)z * (W + 1) * (H + 1);
 				for (int k = 0; k < 3; k++) nodes[3 * i + k] = mn[k] + sc[k] * (c[k] + 0.5f * (wonkiness * r[k]));
 			}
-	static const int split[6][4] = {{0, 1, 5, 7}, {0, 7, 3, 1}, {0, 2, 3, 7}, {0, 7, 6, 2}, {0, 4, 6, 7}, {0, 7, 5, 4}};
 	size_t ie = 0;
 	for (uint32_t z = 0; z < D; z++)
 		for (uint32_t y = 0; y < H; y++)
 			for (uint32_t x = 0; x < W; x++, ie++) {
-				uint32_t ih[8];
+				uint32_t* ih = idx + 9 * ie + 1;
+				idx[9 * ie] = 8;
 				for (uint32_t k = 0; k < 2; k++)
 					for (uint32_t j = 0; j < 2; j++)
 						for (uint32_t i = 0; i < 2; i++) {
@@ -90,12 +90,57 @@ void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float
 							}
 							ih[hi] = (x + xx) + (y + yy) * (W + 1) + (z + zz) * (W + 1) * (H + 1);
 						}
-				for (int t = 0; t < 6; t++) {
-					uint32_t* o = idx + 30 * ie + 5 * t;
-					o[0] = 4;
-					for (int n = 0; n < 4; n++) o[1 + n] = ih[split[t][n]];
-				}
 			}
+}
+
+void gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                   float wonkiness, float* nodes, uint32_t* idx) {
+	const size_t ncell = (size_t)W * H * D;
+	std::vector<uint32_t> hex(9 * ncell);
+	gen_hex_block(W, H, D, sx, sy, sz, pattern, wonkiness, nodes, hex.data());
+	// six tets per cell (XPBDFEM/MeshGen.cpp:235-240)
+	static const int split[6][4] = {{0, 1, 5, 7}, {0, 7, 3, 1}, {0, 2, 3, 7}, {0, 7, 6, 2}, {0, 4, 6, 7}, {0, 7, 5, 4}};
+	for (size_t ie = 0; ie < ncell; ie++)
+		for (int t = 0; t < 6; t++) {
+			uint32_t* o = idx + 30 * ie + 5 * t;
+			o[0] = 4;
+			for (int n = 0; n < 4; n++) o[1 + n] = hex[9 * ie + 1 + split[t][n]];
+		}
+}
+
+int parse_hexes(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& hexes, uint32_t& nverts) {
+	hexes.clear();
+	uint32_t mx = 0;
+	for (uint64_t i = 0; i < idx_count; i += 9) {
+		if (idx[i] != 8u || i + 8 >= idx_count) return -1;
+		for (int n = 0; n < 8; n++) {
+			const uint32_t v = idx[i + 1 + n];
+			mx = v > mx ? v : mx;
+			hexes.push_back(v);
+		}
+	}
+	nverts = hexes.empty() ? 0 : mx + 1;
+	return 0;
+}
+
+void hex_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, float density,
+                   float* hep, float* w, uint8_t* vflags) {
+	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};
+	for (uint32_t i = 0; i < nverts; i++) {
+		w[i] = 0.0f;
+		for (int k = 0; k < 3; k++) {
+			mn[k] = fminf(mn[k], nodes[3 * (size_t)i + k]);
+			mx[k] = fmaxf(mx[k], nodes[3 * (size_t)i + k]);
+		}
+	}
+	for (uint32_t i = 0; i < nverts; i++) vflags[i] = rest::vertex_flags(nodes[3 * (size_t)i], mn[0], mx[0]);
+	for (uint32_t h = 0; h < nhexes; h++) {
+		const uint32_t* is = hexes + 8 * (size_t)h;
+		float m[8];
+		rest::hex(nodes, is, density, hep + (size_t)rest::kHexRec * h, m);
+		for (int n = 0; n < 8; n++) w[is[n]] += m[n];
+	}
+	for (uint32_t i = 0; i < nverts; i++) w[i] = 1.0f / w[i];
 }
 
 namespace {
@@ -331,6 +376,49 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 	if (cluster_and_colour(tets, ntets, off.data(), lst.data(), mode, s)) return -1;
 	vertex_ranks(nodes, nverts, morton, s);
 	cluster_order(nodes, nverts, tets, morton, s);
+	return 0;
+}
+
+// Hex schedule: hexes coloured greedily in id order so that the hexes of one
+// colour share no vertex (each takes the smallest colour no earlier hex on
+// one of its vertices holds), then ordered inside each colour by (Morton code
+// of the centroid of the 8 vertices, id), or by id without Morton order.
+int hex_schedule(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, uint32_t morton,
+                 HexSchedule& hs) {
+	std::vector<uint64_t> used(nverts, 0);
+	std::vector<uint32_t> colour(nhexes);
+	uint32_t ncol = 0;
+	for (uint32_t h = 0; h < nhexes; h++) {
+		uint64_t u = 0;
+		for (int n = 0; n < 8; n++) u |= used[hexes[8 * (size_t)h + n]];
+		if (u == ~0ull) return -1;
+		const uint32_t c = (uint32_t)__builtin_ctzll(~u);
+		colour[h] = c;
+		ncol = std::max(ncol, c + 1);
+		for (int n = 0; n < 8; n++) used[hexes[8 * (size_t)h + n]] |= 1ull << c;
+	}
+	const MortonFrame f = morton ? morton_frame(nodes, nverts) : MortonFrame{};
+	std::vector<std::pair<uint64_t, uint32_t>> key(nhexes);
+	for (uint32_t h = 0; h < nhexes; h++) {
+		uint32_t k = h;
+		if (morton) {
+			float c[3] = {0.0f, 0.0f, 0.0f};
+			for (int n = 0; n < 8; n++)
+				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)hexes[8 * (size_t)h + n] + j];
+			for (int j = 0; j < 3; j++) c[j] = c[j] / 8.0f;
+			k = f.code(c);
+		}
+		key[h] = {((uint64_t)colour[h] << 32) | k, h};
+	}
+	std::sort(key.begin(), key.end());
+	hs.ncolours = ncol;
+	hs.order.resize(nhexes);
+	hs.colour_begin.assign(ncol + 1, 0);
+	for (uint32_t i = 0; i < nhexes; i++) {
+		hs.order[i] = key[i].second;
+		hs.colour_begin[colour[key[i].second] + 1]++;
+	}
+	for (uint32_t c = 0; c < ncol; c++) hs.colour_begin[c + 1] += hs.colour_begin[c];
 	return 0;
 }
 

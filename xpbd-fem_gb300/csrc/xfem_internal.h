@@ -82,6 +82,29 @@ struct RingSchedule {
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
                         const uint32_t* vert_rank, RingSchedule& rs);
 
+// Linear hexahedra (H8). The tagged index stream with tag 8 (8 vertex ids
+// per hex); -1 on another tag or a truncated record.
+int parse_hexes(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& hexes, uint32_t& nverts);
+// GeoLinear3d::Init on a hex mesh (XPBDFEM/Geo.cpp:697-745 with
+// InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265): 120 floats per hex
+// (rest::kHex* offsets), inverse masses and vertex flags, bit for bit.
+void hex_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, float density,
+                   float* hep, float* w, uint8_t* vflags);
+// GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-221): idx holds 9 words per hex.
+void gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
+                   float wonkiness, float* nodes, uint32_t* idx);
+// The hex schedule: hexes coloured greedily in id order so that the hexes of
+// one colour share no vertex (at most 64 colours), ordered inside each colour
+// by the Morton code of their centroid (or by id without Morton order).
+struct HexSchedule {
+	uint32_t ncolours = 0;
+	std::vector<uint32_t> order;         // hexes, colour-major
+	std::vector<uint32_t> colour_begin;  // ncolours + 1, into order
+};
+// Returns 0, or -1 when more than 64 colours are needed.
+int hex_schedule(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, uint32_t morton,
+                 HexSchedule& hs);
+
 // ---- GPU set-up path (xfem_setup.cu) ------------------------------------------
 // The parallel phases of the set-up on the device, bit for bit the host's:
 // rest state (init_rest), incidence, Morton vertex ranks (vertex_ranks) and
@@ -239,7 +262,18 @@ struct DevCtx {
 	const uint4* pbd_ent;
 	const uint32_t* tet_verts;
 	uint32_t pbd_colours;
-	uint32_t pad5;
+	// Hex mode (linear hexahedra; xfem_hexes.cu): hexes in device order,
+	// colour-major (bodies in order inside a colour). hex_vid: 8 device vertex
+	// ids per hex (two uint4); hex_rec: 30 float4 records as a structure of
+	// arrays (float4 k of hex i at hex_rec[k * nhex + i]); hex_flat: each
+	// hex's index in its body's hex order (the amortized damping slices).
+	uint32_t hex_colours;
+	const uint4* hex_vid;
+	const float4* hex_rec;
+	const uint32_t* colour_hex_begin;  // hex_colours + 1
+	const uint32_t* hex_flat;
+	uint32_t nhex;
+	uint32_t pad6;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
@@ -314,6 +348,9 @@ int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, dou
 // models, a cooperative persistent launch of `block` threads per block
 // (canonical (X, V) in and out).
 int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// Hex mode (xfem_hexes.cu): nsub substeps of a hex mesh, a cooperative
+// persistent launch (canonical (X, V) in and out).
+int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Per-tet material (n tets from the given per-tet tables): c0 of each record
 // and 1/mu; mu null = mu_uniform for all.
 int launch_set_c0(float4* cblk, const uint32_t* rec, const float* vol, const float* mu, float mu_uniform, uint32_t n,

@@ -131,6 +131,123 @@ XFEM_HD float tet(const float* nodes, const uint32_t* is, float density, float* 
 	return (1.0f / 4.0f) * density * vol;
 }
 
+// ---- linear hexahedra (H8) ----
+// Nodes and quadrature points are numbered i + 2j + 4k (sign 2 bit - 1 per
+// axis). The reference tabulates the shape functions and their gradients at
+// the 2x2x2 Gauss points and the gradients at the centre to six decimals
+// (XPBDFEM/Fem.cpp:40, :68-69); each entry is one of these printed magnitudes,
+// picked by how many axes node and point agree on. The printed values, not
+// the exact Gauss values, are what every rest state is built from.
+XFEM_HD float hex_n8(int p, int n) {  // ShapeFunctions<Hex, 8, 8>[p][n]
+	const int agree = !((p ^ n) & 1) + !((p ^ n) & 2) + !((p ^ n) & 4);
+	return agree == 3 ? 0.490562f : agree == 2 ? 0.131446f : agree == 1 ? 0.035221f : 0.009437f;
+}
+
+XFEM_HD float hex_g8(int p, int n, int k) {  // ShapeFunctionGradients<Hex, 8, 8>[p][n][k]
+	int agree = 0;
+	for (int a = 0; a < 3; a++)
+		if (a != k) agree += !(((p ^ n) >> a) & 1);
+	const float m = agree == 2 ? 0.311004f : agree == 1 ? 0.083333f : 0.022329f;
+	return ((n >> k) & 1) ? m : -m;
+}
+
+XFEM_HD float hex_g1(int n, int k) { return ((n >> k) & 1) ? 0.125f : -0.125f; }  // <Hex, 8, 1>[0][n][k]
+
+// Offsets in the 120-value hex record (ElementParamsLinearHex,
+// XPBDFEM/Fem.h:90-100, flattened): qcLo.Ji[0] column-major, qcLo.w[0],
+// qcHi.Ji[p], qcHi.w[p], ic.QQ[7], ic.QR[21], volume, surfaceArea.
+constexpr int kHexJL = 0, kHexWL = 9, kHexJH = 10, kHexWH = 82, kHexQQ = 90, kHexQR = 97, kHexVol = 118,
+              kHexArea = 119, kHexRec = 120;
+
+// MatMul(dN, P) over the 8 map nodes (XPBDFEM/Fem.cpp:86-94): from zero,
+// element [c][r] accumulates dN[n][r] P[n][c] in node order.
+XFEM_HD M3 hex_map_jacobian(const float P[8][3], int hi, int p) {
+	M3 J;
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) J.c[c][r] = 0.0f;
+	for (int n = 0; n < 8; n++)
+		for (int c = 0; c < 3; c++)
+			for (int r = 0; r < 3; r++) J.c[c][r] = J.c[c][r] + (hi ? hex_g8(p, n, r) : hex_g1(n, r)) * P[n][c];
+	return J;
+}
+
+// One hex: InitQuadHexFiniteElement (XPBDFEM/Fem.cpp:225-265) with
+// GenerateMappedQuadratureCoefficients (:110-125) for the centre and the
+// 2x2x2 points and GeneratePrefactoredCoefficients (:131-161) on the 2x2x2
+// points. o: the 120-value record; m[8]: the lumped mass of each node (the
+// normalised diagonal of the mass matrix times density and volume).
+XFEM_HD void hex(const float* nodes, const uint32_t* is, float density, float* o, float m[8]) {
+	float P[8][3];
+	for (int n = 0; n < 8; n++)
+		for (int k = 0; k < 3; k++)
+			P[n][k] = (float)((double)nodes[3 * (size_t)is[n] + k] - (double)nodes[3 * (size_t)is[7] + k]);
+	for (int hi = 0; hi < 2; hi++) {
+		const int np = hi ? 8 : 1;
+		float vsum = 0.0f;
+		for (int p = 0; p < np; p++) {
+			const M3 J = hex_map_jacobian(P, hi, p);
+			const float detJ = det3(J);
+			const M3 Ji = inverse3(J);
+			float* j = o + (hi ? kHexJH + 9 * p : kHexJL);
+			for (int c = 0; c < 3; c++)
+				for (int r = 0; r < 3; r++) j[c * 3 + r] = Ji.c[c][r];
+			float& w = o[hi ? kHexWH + p : kHexWL];
+			w = detJ * (hi ? 1.0f : 8.0f);
+			vsum += w;
+		}
+		for (int p = 0; p < np; p++) o[hi ? kHexWH + p : kHexWL] /= vsum;
+	}
+	float* QQ = o + kHexQQ;
+	float* QR = o + kHexQR;
+	for (int i = 0; i < 7; i++) QQ[i] = 0.0f;
+	for (int i = 0; i < 21; i++) QR[i] = 0.0f;
+	float vsum = 0.0f, vol = 0.0f;
+	for (int p = 0; p < 8; p++) {
+		const M3 J = hex_map_jacobian(P, 1, p);
+		const M3 Ji = inverse3(J);
+		const float w = det3(J) * 1.0f * 1.0f;
+		float q[7][3];
+		for (int i = 0; i < 7; i++) {
+			const float dn[3] = {hex_g8(p, i, 0), hex_g8(p, i, 1), hex_g8(p, i, 2)};
+			for (int r = 0; r < 3; r++) {
+				const float row[3] = {Ji.c[0][r], Ji.c[1][r], Ji.c[2][r]};
+				q[i][r] = dot3(row, dn);
+			}
+		}
+		vsum += w;
+		for (int i = 0; i < 7; i++) QQ[i] += w * dot3(q[i], q[i]);
+		int head = 0;
+		for (int i = 0; i < 7; i++)
+			for (int j = i + 1; j < 7; j++) QR[head++] += w * 2.0f * dot3(q[i], q[j]);
+	}
+	for (int i = 0; i < 7; i++) QQ[i] /= vsum;
+	for (int i = 0; i < 21; i++) QR[i] /= vsum;
+	for (int p = 0; p < 8; p++) vol += det3(hex_map_jacobian(P, 1, p)) * 1.0f;
+	o[kHexVol] = vol;
+	const int faces[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}};
+	float area = 0.0f;
+	for (int f = 0; f < 6; f++) {
+		float a[3], b[3];
+		for (int k = 0; k < 3; k++) {
+			a[k] = P[faces[f][0]][k] - P[faces[f][3]][k];
+			b[k] = P[faces[f][1]][k] - P[faces[f][2]][k];
+		}
+		const float c[3] = {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
+		area += 0.5f * sqrtf(dot3(c, c));
+	}
+	o[kHexArea] = area;
+	float mmd[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, msum = 0.0f;
+	for (int p = 0; p < 8; p++) {
+		const float w = o[kHexWH + p];
+		for (int n = 0; n < 8; n++) {
+			const float Nn = hex_n8(p, n);
+			mmd[n] += w * Nn * Nn;
+			msum += w * Nn * Nn;
+		}
+	}
+	for (int n = 0; n < 8; n++) m[n] = (mmd[n] / msum) * density * vol;
+}
+
 // The Left / Right flags of a vertex (XPBDFEM/Geo.cpp:713-727) from the AABB
 // of the node data along x: bit 0 Left, bit 1 Right, bit 4 Pickable.
 XFEM_HD uint8_t vertex_flags(float x, float mn, float mx) {

@@ -87,8 +87,10 @@ EXPORTS = [
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
     "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward", "xfem_pbd_damping_coefficients",
-    "xfem_get_ring_schedule", "xfem_compute_ring_schedule",
+    "xfem_get_ring_schedule", "xfem_compute_ring_schedule", "xfem_body_hex_count", "xfem_get_hex_rest_state",
+    "xfem_get_hex_schedule", "xfem_compute_hex_rest_state", "xfem_compute_hex_schedule", "xfem_generate_hex_block",
 ]
+HEX_EP = 120  # floats per hex rest-state record (ElementParamsLinearHex flattened)
 
 _lib = None
 
@@ -135,6 +137,12 @@ def lib():
         L.xfem_adjoint_forward.argtypes = [P, u32, f32, u32, u32, P, P]
         L.xfem_pbd_damping_coefficients.argtypes = [f32, f32, f32, P]
         L.xfem_adjoint_backward.argtypes = [P, P, P, P, P, P, P]
+        L.xfem_body_hex_count.argtypes = [P, u32, P]
+        L.xfem_get_hex_rest_state.argtypes = [P, u32, P, P]
+        L.xfem_get_hex_schedule.argtypes = [P, u32, P, P, P, P]
+        L.xfem_compute_hex_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P]
+        L.xfem_compute_hex_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.xfem_generate_hex_block.argtypes = [u32, u32, u32, f32, f32, f32, u32, f32, P, P]
         _lib = L
     return _lib
 
@@ -184,6 +192,41 @@ def generate_tet_block(W, H, D, scale=(1.0, 1.0, 1.0), pattern=0, wonkiness=0.0)
     _check(lib().xfem_generate_tet_block(W, H, D, scale[0], scale[1], scale[2], pattern, wonkiness,
                                          _p(nodes), _p(idx)))
     return nodes, idx
+
+
+def generate_hex_block(W, H, D, scale=(1.0, 1.0, 1.0), pattern=0, wonkiness=0.0):
+    """GenerateHexBlock (XPBDFEM/MeshGen.cpp:156): returns (node_data, idx_data)."""
+    nodes = np.zeros(3 * (W + 1) * (H + 1) * (D + 1), np.float32)
+    idx = np.zeros(9 * W * H * D, np.uint32)
+    _check(lib().xfem_generate_hex_block(W, H, D, scale[0], scale[1], scale[2], pattern, wonkiness,
+                                         _p(nodes), _p(idx)))
+    return nodes, idx
+
+
+def compute_hex_rest_state(node_data, idx_data, density):
+    """Host-only rest state of a hex mesh (no GPU): (ep[nh, 120], w[nv], flags[nv])."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nv, nh = nd.size // 3, ix.size // 9
+    ep = np.zeros((nh, HEX_EP), np.float32)
+    w = np.zeros(nv, np.float32)
+    fl = np.zeros(nv, np.uint8)
+    _check(lib().xfem_compute_hex_rest_state(_p(nd), nd.size, _p(ix), ix.size, density, _p(ep), _p(w), _p(fl)))
+    return ep, w, fl
+
+
+def compute_hex_schedule(node_data, idx_data, morton=True):
+    """Host-only hex schedule (no GPU), in the form of Body.hex_schedule()."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nv, nh = nd.size // 3, ix.size // 9
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nh, np.uint32)
+    cb = np.zeros(65, np.uint32)
+    ncol = C.c_uint32()
+    _check(lib().xfem_compute_hex_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
+                                           _p(cb), C.byref(ncol)))
+    return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
 
 
 def compute_rest_state(node_data, idx_data, density):
@@ -362,6 +405,29 @@ class Body:
         cb = np.zeros(ncol.value + 1, np.uint32)
         _check(lib().xfem_get_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb, colours=ncol.value)
+
+    def hex_count(self, body=0):
+        n = C.c_uint32()
+        _check(lib().xfem_body_hex_count(self._h, body, C.byref(n)))
+        return n.value
+
+    def hex_rest_state(self, body=0):
+        """Rest state of a hex body: (ep[nh, 120], w[nv])."""
+        nv, nh = self.counts[body][0], self.hex_count(body)
+        ep = np.zeros((nh, HEX_EP), np.float32)
+        w = np.zeros(nv, np.float32)
+        _check(lib().xfem_get_hex_rest_state(self._h, body, _p(ep), _p(w)))
+        return ep, w
+
+    def hex_schedule(self, body=0):
+        """Vertex ranks, hex order (colour-major) and colour offsets of a hex body."""
+        nv, nh = self.counts[body][0], self.hex_count(body)
+        rank = np.zeros(nv, np.uint32)
+        order = np.zeros(nh, np.uint32)
+        cb = np.zeros(65, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_hex_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
+        return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     def ring_schedule(self, body=0):
         """The ring order of a continuous-pressure body (energy 8-10)."""
