@@ -22,6 +22,9 @@ shape the configuration names.
   undamped, "models": the same mesh at nu = 0.45 with Mixed, YeohSkin, Pixar,
   one volume pass and ContinuousMixed (one-ring mode) against MixedSel, "setup": wall time of a handle's
   set-up (GPU set-up path and host set-up, 1.5M-tet mesh; 512-body batch),
+  "hexes": hex mode on the same grid as 262,144 linear hexahedra (MixedSel,
+  YeohSkinFast, Mixed) with the oracle port's single-thread hex substep as
+  its CPU baseline,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -295,6 +298,7 @@ def run_xfem(args, world, rank, local):
     damped = None if args.no_damped else run_damped(stream)
     models = None if args.no_models else run_models(stream)
     setup = None if args.no_setup else run_setup(stream)
+    hexes = None if args.no_hexes else run_hexes(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -317,6 +321,7 @@ def run_xfem(args, world, rank, local):
         "damped": damped,
         "models": models,
         "setup": setup,
+        "hexes": hexes,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -547,6 +552,52 @@ def run_models(stream, frames=5):
             "cost": {k: out[k]["ms_per_frame"] / out["mixed_sel"]["ms_per_frame"] for k, _ in cases[1:]}}
 
 
+def run_hexes(stream, frames=5, cpu_budget_s=6.0):
+    """Hex mode: the throughput grid as 262,144 linear hexahedra (the same
+    jittered nodes; each hex is the 6 tets of the tet mesh's cube) with
+    MixedSel, YeohSkinFast and Mixed (2x2x2 quadrature), device-timed frames
+    of 20 substeps with L2 flushed between frames; and the oracle port of the
+    reference's hex substep on one host thread on the same mesh (a bounded
+    sample of substeps) as the CPU baseline."""
+    import torch
+
+    import oracle
+    import xfem
+    from xfem import workloads as W
+    w = W.throughput_hex()
+    nh = w["idx"].size // 9
+    S = w["substeps"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    solve = (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT
+    cases = (("mixed_sel", w["settings"]),
+             ("yeoh_skin_fast", dict(w["settings"], flags=(xfem.ENERGY_YEOH_SKIN_FAST << xfem.ENERGY_BIT) | solve,
+                                     compliance=3.2e-4)),
+             ("mixed", dict(w["settings"], flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)))
+    out = {}
+    for key, s_ in cases:
+        r = time_frames(stream, w, s_, flush, frames)
+        r["value"] = nh * S / (r["ms_per_frame"] / 1e3)
+        r.pop("sync_mode")
+        r.pop("block")
+        out[key] = r
+    # CPU: the oracle's float restatement, one thread, the reference's
+    # algorithm in the GPU's hex order
+    hexes, _ = oracle.parse_hexes(w["idx"])
+    ep, wi, fl = oracle.hex_init_rest(w["nodes"], hexes, w["density"])
+    order = oracle.hex_schedule(w["nodes"], hexes)["hex_order"]
+    p = oracle.params_from_settings(w["settings"], w["dt"] / S, lock=False)
+    X = w["nodes"].astype(np.float64).reshape(-1, 3)
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget_s or n == 0:
+        X, V, wi, _ = oracle.hex_substeps(X, np.zeros_like(X), wi, hexes, ep, order, 1, p)
+        n += 1
+    cpu = nh * n / (time.perf_counter() - t0)
+    return {"workload": w["name"], "unit": "hex-substeps/s", **out,
+            "cpu_baseline": {"value": cpu, "unit": "hex-substeps/s", "cores": 1, "kind": "port",
+                             "sample": "%d substeps of the same mesh (MixedSel)" % n},
+            "vs_tet_mesh_of_the_same_grid": "each hex covers the 6 tets of one cube of the throughput mesh"}
+
+
 def C_void_p(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -574,6 +625,7 @@ def main():
     ap.add_argument("--no-damped", action="store_true")
     ap.add_argument("--no-models", action="store_true")
     ap.add_argument("--no-setup", action="store_true")
+    ap.add_argument("--no-hexes", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")
