@@ -23,7 +23,7 @@ shape the configuration names.
   one volume pass and ContinuousMixed (one-ring mode) against MixedSel, "setup": wall time of a handle's
   set-up (GPU set-up path and host set-up, 1.5M-tet mesh; 512-body batch),
   "hexes": hex mode on the same grid as 262,144 linear hexahedra (MixedSel,
-  YeohSkinFast, Mixed) with the oracle port's single-thread hex substep as
+  YeohSkinFast, Mixed, CubeNeo) with the oracle port's single-thread hex substep as
   its CPU baseline,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
@@ -555,7 +555,8 @@ def run_models(stream, frames=5):
 def run_hexes(stream, frames=5, cpu_budget_s=6.0):
     """Hex mode: the throughput grid as 262,144 linear hexahedra (the same
     jittered nodes; each hex is the 6 tets of the tet mesh's cube) with
-    MixedSel, YeohSkinFast and Mixed (2x2x2 quadrature), device-timed frames
+    MixedSel, YeohSkinFast, Mixed (2x2x2 quadrature) and CubeNeo (its short
+    path at nu = 0.5), device-timed frames
     of 20 substeps with L2 flushed between frames; and the oracle port of the
     reference's hex substep on one host thread on the same mesh (a bounded
     sample of substeps) as the CPU baseline."""
@@ -572,7 +573,8 @@ def run_hexes(stream, frames=5, cpu_budget_s=6.0):
     cases = (("mixed_sel", w["settings"]),
              ("yeoh_skin_fast", dict(w["settings"], flags=(xfem.ENERGY_YEOH_SKIN_FAST << xfem.ENERGY_BIT) | solve,
                                      compliance=3.2e-4)),
-             ("mixed", dict(w["settings"], flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)))
+             ("mixed", dict(w["settings"], flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)),
+             ("cube_neo", dict(w["settings"], flags=(xfem.ENERGY_CUBE_NEO << xfem.ENERGY_BIT) | solve)))
     out = {}
     for key, s_ in cases:
         r = time_frames(stream, w, s_, flush, frames)

@@ -171,7 +171,7 @@ void orc_hex_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* hexes,
                          double density, double* ep, double* w, uint8_t* vflags);
 /* SolveElement on one hex (XPBDFEM/Fem.cpp:896): X 8x3 doubles in place, O
  * (8x3) the substep's start, w[8]. Returns 0, or -1 for the ids the hex path
- * does not cover (8-12: continuous-pressure and cube models). */
+ * does not cover (8-10: the continuous-pressure models). */
 int orc_solve_hex_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p);
 int orc_solve_hex_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p);
 /* Substeps of a hex mesh in the hex order `order` (GeoLinear3d::Constrain and

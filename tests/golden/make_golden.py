@@ -167,6 +167,10 @@ CASES = [
     ("hsolve_pixar_reduced_nu040", ["hsolve", 52, 32, 1, 0, 0.02, 0.40, DT]),
     ("hsolve_pixarsel_nu049", ["hsolve", 53, 32, 2, 1, 0.01, 0.49, DT]),
     ("hsolve_id20_mixedsel", ["hsolve", 54, 32, 20, 1, 0.01, 0.45, DT]),
+    ("hsolve_cube_neo_fast", ["hsolve", 55, 32, 11, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("hsolve_cube_neo_nu045", ["hsolve", 56, 32, 11, 1, 0.01, 0.45, DT]),
+    ("hsolve_cube_skin_nu049", ["hsolve", 57, 32, 12, 0, 0.5, 0.49, DT]),
+    ("hsolve_cube_skin_incompressible", ["hsolve", 58, 32, 12, 1, 3.2, 0.5, DT]),
     ("hordered_c1_nh_nu045", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
                               0.0, -9.81, DT, 40, 1]),
     ("hordered_c1_nh_incompressible", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
@@ -193,6 +197,19 @@ CASES = [
                                             -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
     ("hvolume_c1_nh_nu045_2", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
                                0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 2]),
+    ("hordered_c1_cube_neo_fast", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 11, 1, C1_COMPLIANCE, 0.5,
+                                   0.0, -9.81, DT, 40, 1]),
+    ("hordered_wonky_cube_neo_nu045", ["hordered", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 11, 1, 1e-3, 0.45,
+                                       -2.0, -9.81, DT, 10, 1]),
+    ("hordered_c1_cube_skin_nu049", ["hordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 12, 1, 3.2e-4, 0.49,
+                                     0.0, -9.81, DT, 40, 1]),
+    ("hdamped_c1_cube_neo_nu045_paper", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 11, 1, 4.0 * 1.45 / 1e5,
+                                         0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 0, 0.1]),
+    ("hdamped_c1_cube_skin_nu045_limit", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 12, 1, 3.2e-4, 0.45,
+                                          0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("hdamped_c1_cube_neo_incompressible_amortized_pbd", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 11, 1,
+                                                          C1_COMPLIANCE, 0.5, 0.0, -9.81, DT, 40, 1, 0.01, 0.03,
+                                                          0.002, 3, 0.1, 1]),
     ("hvolume_wonky_pixar_1_post_pbd", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
 ]

@@ -2,8 +2,8 @@
 
 GeoLinear3d's hex loops (XPBDFEM/Geo.cpp:777-811) with SolveElement on
 ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896): the Pixar models, Mixed,
-MixedSel, the Yeoh models and ids above 12, coupled or serial, in-solve and
-post-step damping, PBD damping and volume passes.
+MixedSel, the Yeoh models, the cube models and ids above 12, coupled or
+serial, in-solve and post-step damping, PBD damping and volume passes.
 
 Against the reference's own substeps run in the GPU body's hex colour order
 (the `hordered_*`, `hdamped_*` and `hvolume_*` fixtures) and against the
@@ -30,7 +30,11 @@ HFIX = ["hordered_c1_nh_nu045", "hordered_c1_nh_incompressible", "hordered_c1_ye
         "hordered_wonky_nh_serial_nu045", "hordered_c1_mixed_nu045", "hordered_wonky_yeohskinsel_serial_nu049",
         "hordered_c1_pixar_nu045", "hdamped_c1_nh_nu045_post_pbd", "hdamped_c1_nh_nu045_amortized_pbd",
         "hdamped_c1_nh_nu045_paper", "hdamped_c1_nh_nu045_limit", "hdamped_wonky_yeohskin_serial_post",
-        "hvolume_c1_nh_nu045_2", "hvolume_wonky_pixar_1_post_pbd"]
+        "hvolume_c1_nh_nu045_2", "hvolume_wonky_pixar_1_post_pbd",
+        # the cube models (SolveElementCube, XPBDFEM/Fem.cpp:566-838)
+        "hordered_c1_cube_neo_fast", "hordered_wonky_cube_neo_nu045", "hordered_c1_cube_skin_nu049",
+        "hdamped_c1_cube_neo_nu045_paper", "hdamped_c1_cube_skin_nu045_limit",
+        "hdamped_c1_cube_neo_incompressible_amortized_pbd"]
 
 
 def hex_settings(name):
@@ -120,6 +124,8 @@ def test_hex_reference_parity(name):
     (xfem.ENERGY_PIXAR_REDUCED, 1, 1e-3, 0.45, 0, 0.0, 2, 0.0),
     (xfem.ENERGY_PIXAR_SEL, 1, 1e-3, 0.40, 0, 0.01, 2, 0.0),
     (20, 1, 1e-3, 0.45, 0, 0.0, 2, 0.0),
+    (xfem.ENERGY_CUBE_NEO, 1, 1e-3, 0.45, 0, 0.01, 1, 0.0),
+    (xfem.ENERGY_CUBE_SKIN, 1, 0.5, 0.45, 1, 0.01, 3, 0.03),
 ])
 def test_hex_oracle_parity(energy, simultaneous, comp, nu, vpasses, damping, rtype, pbd):
     """A larger jittered mirrored block, 20 substeps, against the oracle in
@@ -133,13 +139,22 @@ def test_hex_oracle_parity(energy, simultaneous, comp, nu, vpasses, damping, rty
                               damping=damping, pbd_damping=pbd, volume_and_time_corrected_pbd_damping=vc,
                               amortized_volume_and_time_corrected_pbd_damping=avc, volume_passes=vpasses)
     b = xfem.Body(nodes, idx, 800.0, s)
-    o = HexOracleRun(nodes, idx, 800.0, s, b.hex_schedule()["hex_order"])
+    order = b.hex_schedule()["hex_order"]
+    o = HexOracleRun(nodes, idx, 800.0, s, order)
+    o64 = HexOracleRun(nodes, idx, 800.0, xfem.default_settings(**{k: getattr(s, k) for k, _ in s._fields_}), order,
+                       dtype=np.float64)
     for n in (1, 19):
         b.step_frames(1, n, DT)
-        o.step(n, DT)
-        o.s.tick_id += n
+        for r in (o, o64):
+            r.step(n, DT)
+            r.s.tick_id += n
         assert rel(b.positions(), o.X) <= 1e-5, n
-        assert rel(b.velocities(), o.V) <= 1e-3, n
+        if vpasses and n == 1:
+            # first-substep velocities of volume passes: within 3x the FP32
+            # oracle's own distance from FP64 (as for the tets)
+            assert rel(b.velocities(), o64.V) <= 3 * rel(o.V, o64.V), n
+        else:
+            assert rel(b.velocities(), o.V) <= 1e-3, n
 
 
 def test_hex_rest_state_and_volume():
@@ -203,7 +218,7 @@ def test_hex_batch_each_as_alone():
 def test_hex_errors():
     nodes, idx = xfem.generate_hex_block(3, 2, 2, (0.05, 0.05, 0.05))
     tn, ti = xfem.generate_tet_block(3, 2, 2, (0.05, 0.05, 0.05))
-    for e in (8, 9, 10, 11, 12):
+    for e in (8, 9, 10):
         with pytest.raises(xfem.XfemError) as ex:
             xfem.Body(nodes, idx, 1000.0, xfem.default_settings(flags=e << xfem.ENERGY_BIT))
         assert ex.value.code == xfem.EUNSUPPORTED

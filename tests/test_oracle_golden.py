@@ -13,8 +13,9 @@ every energy model SolveElement dispatches on a linear tet
 (XPBDFEM/Fem.cpp:872-888), and volume passes (XPBDFEM/Fem.cpp:840-867).
 Linear hexahedra the same way: GenerateHexBlock, InitQuadHexFiniteElement
 (XPBDFEM/Fem.cpp:225-265), SolveElement on H8 for every energy model but the
-continuous-pressure and cube ones, and whole substeps with the hex loops of
-GeoLinear3d::Constrain and Damp (XPBDFEM/Geo.cpp:774-811).
+continuous-pressure ones (the cube models' SolveElementCube included), and
+whole substeps with the hex loops of GeoLinear3d::Constrain and Damp
+(XPBDFEM/Geo.cpp:774-811).
 """
 import numpy as np
 import pytest
@@ -230,12 +231,17 @@ HSOLVE = ["hsolve_nh_sim_nu045", "hsolve_nh_sim_incompressible", "hsolve_nh_seri
           "hsolve_yeohfast_sim_nu049", "hsolve_yeohfast_serial_incompressible", "hsolve_mixed_sim_nu045",
           "hsolve_mixed_serial_nu049", "hsolve_yeohskin_sim_nu045", "hsolve_yeohskinsel_sim_nu049",
           "hsolve_yeohskinsel_serial_nu045", "hsolve_pixar_nu045", "hsolve_pixar_reduced_nu040",
-          "hsolve_pixarsel_nu049", "hsolve_id20_mixedsel"]
+          "hsolve_pixarsel_nu049", "hsolve_id20_mixedsel",
+          # SolveElementCube (XPBDFEM/Fem.cpp:566-838): the short path (CubeNeo,
+          # nu = 0.5, no damping) and the general one
+          "hsolve_cube_neo_fast", "hsolve_cube_neo_nu045", "hsolve_cube_skin_nu049", "hsolve_cube_skin_incompressible"]
 HSUBSTEP = ["hordered_c1_nh_nu045", "hordered_c1_nh_incompressible", "hordered_c1_yeohfast_nu049",
             "hordered_wonky_nh_serial_nu045", "hordered_c1_mixed_nu045", "hordered_wonky_yeohskinsel_serial_nu049",
             "hordered_c1_pixar_nu045", "hdamped_c1_nh_nu045_post_pbd", "hdamped_c1_nh_nu045_amortized_pbd",
             "hdamped_c1_nh_nu045_paper", "hdamped_c1_nh_nu045_limit", "hdamped_wonky_yeohskin_serial_post",
-            "hvolume_c1_nh_nu045_2", "hvolume_wonky_pixar_1_post_pbd"]
+            "hvolume_c1_nh_nu045_2", "hvolume_wonky_pixar_1_post_pbd", "hordered_c1_cube_neo_fast",
+            "hordered_wonky_cube_neo_nu045", "hordered_c1_cube_skin_nu049", "hdamped_c1_cube_neo_nu045_paper",
+            "hdamped_c1_cube_skin_nu045_limit", "hdamped_c1_cube_neo_incompressible_amortized_pbd"]
 
 
 def test_hex_meshgen_bit_exact(orc):
@@ -346,12 +352,12 @@ def test_hex_schedule_is_a_valid_colouring(orc):
     assert s["colours"] == 8  # a structured block needs exactly 8
 
 
-def test_hex_continuous_and_cube_models_refused(orc):
+def test_hex_continuous_models_refused(orc):
     nodes, idx = orc.gen_hex_block(2, 1, 1, (0.1, 0.1, 0.1))
     hexes, nv = orc.parse_hexes(idx)
     ep, w, fl = orc.hex_init_rest(nodes, hexes, 1000.0)
     X = nodes.astype(np.float64).reshape(-1, 3)
-    for e in (8, 9, 10, 11, 12):
+    for e in (8, 9, 10):
         p = orc.make_params(dt=1e-3, compliance=1e-3, poisson=0.45, energy=e)
         with pytest.raises(ValueError):
             orc.hex_substeps(X, np.zeros_like(X), w, hexes, ep, np.arange(2, dtype=np.uint32), 1, p)

@@ -209,6 +209,7 @@ BodyParams make_params(const xfem_settings& s) {
 	}
 	p.volume_passes = s.volume_passes;
 	p.compliance = s.compliance;
+	p.cube_fast = p.energy == XFEM_ENERGY_CUBE_NEO && nu >= 0.5f && !(s.damping > 0.0f) ? 1u : 0u;
 	p.simultaneous = (s.flags >> XFEM_XPBD_SOLVE_BIT) & 1u;
 	for (int k = 0; k < 3; k++) p.gravity[k] = s.gravity[k];
 	p.drag_mul = 1.0f - s.time_corrected_drag;
@@ -367,9 +368,8 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	if (b.hex) {
 		// linear hexahedra: set-up on the host (rest state, Morton vertex
 		// ranks, the hex colouring)
-		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CUBE_SKIN)
-			return fail(XFEM_EUNSUPPORTED, "hex meshes run the energy models 0-7 and above 12 (not the continuous-pressure "
-			                               "or cube models)");
+		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
+			return fail(XFEM_EUNSUPPORTED, "hex meshes run every energy model but the continuous-pressure ones (8-10)");
 		host_rest(m, b);
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
 		if (hex_schedule(b.nodes.data(), b.nv, b.hexes.data(), b.nh, morton, b.hsched))
@@ -1340,8 +1340,8 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	int rc = validate_settings(*s);
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (h->hex_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CUBE_SKIN)
-		return fail(XFEM_EUNSUPPORTED, "hex meshes run the energy models 0-7 and above 12");
+	if (h->hex_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
+		return fail(XFEM_EUNSUPPORTED, "hex meshes run every energy model but the continuous-pressure ones (8-10)");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
 		                               "element models needs a new handle (their schedules differ)");

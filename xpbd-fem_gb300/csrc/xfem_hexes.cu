@@ -344,6 +344,216 @@ __device__ __forceinline__ void rel(const float4 O[8], const float4 D[8], bool v
 // Pass kinds of one hex.
 enum HexPass { kSolve = 0, kVolume = 1, kRayleigh = 2 };
 
+// det(F) / 64 of F with rows (sA[i], sB[i], sC[i]) and its adjugate columns
+// scaled by 1 / 64 (XPBDFEM/Fem.cpp:613-617, 782-786).
+__device__ __forceinline__ float cube_adj(const Vec3& sA, const Vec3& sB, const Vec3& sC, Vec3 A[3]) {
+	const float F[3][3] = {{sA.x, sB.x, sC.x}, {sA.y, sB.y, sC.y}, {sA.z, sB.z, sC.z}};
+	float M[3][3];
+	const float J = adj_det(F, M) * (1.0f / 64.0f);
+#pragma unroll
+	for (int c = 0; c < 3; c++) A[c] = {M[c][0] * (1.0f / 64.0f), M[c][1] * (1.0f / 64.0f), M[c][2] * (1.0f / 64.0f)};
+	return J;
+}
+
+// sA, sB, sC: the corner sums weighted by each corner's sign on x, y, z.
+__device__ __forceinline__ void corner_sums(const Vec3 R[8], Vec3& sA, Vec3& sB, Vec3& sC) {
+	sA = sB = sC = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+	for (int n = 0; n < 8; n++) {
+		const float a = (n & 1) ? 1.0f : -1.0f, b = (n & 2) ? 1.0f : -1.0f, c = (n & 4) ? 1.0f : -1.0f;
+		sA = {fmaf(a, R[n].x, sA.x), fmaf(a, R[n].y, sA.y), fmaf(a, R[n].z, sA.z)};
+		sB = {fmaf(b, R[n].x, sB.x), fmaf(b, R[n].y, sB.y), fmaf(b, R[n].z, sB.z)};
+		sC = {fmaf(c, R[n].x, sC.x), fmaf(c, R[n].y, sC.y), fmaf(c, R[n].z, sC.z)};
+	}
+}
+
+// SolveElementCube on a hex (XPBDFEM/Fem.cpp:566-838). Positions relative
+// to node 7's substep start O7: R[n] = (O[n] - O7) + D[n] (solve mode), or
+// O[n] - O7 with V = D (VMODE, the post-step Rayleigh form on the canonical
+// state, ratio rd). CubeNeo with nu >= 0.5 and no damping takes the short
+// path of :599-640: a uniform pull towards the centroid, then one volume
+// projection. Otherwise the I1 term of the corners about the centroid
+// (Yeoh for CubeSkin) scales them, and one constraint on det(F) / 64 over the
+// four body diagonals restores the volume.
+template <bool VMODE>
+__device__ __forceinline__ void cube(const BodyParams& bp, const HexRec& R, uint32_t e, const float w[8],
+                                     const float4 O[8], float4 D[8], float dt, float inv_dt, float inv_dt2, float rd) {
+	const float vol = R(kRVol), area = R(kRArea);
+	Vec3 S[8], X[8];
+#pragma unroll
+	for (int n = 0; n < 8; n++) {
+		S[n] = {O[n].x - O[7].x, O[n].y - O[7].y, O[n].z - O[7].z};
+		X[n] = VMODE ? S[n] : Vec3{S[n].x + D[n].x, S[n].y + D[n].y, S[n].z + D[n].z};
+	}
+	Vec3 c = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+	for (int n = 0; n < 8; n++) c = {c.x + X[n].x, c.y + X[n].y, c.z + X[n].z};
+	c = {c.x * 0.125f, c.y * 0.125f, c.z * 0.125f};
+	const float damping = VMODE ? rd : __ldg(&bp.damping);
+	const uint32_t type = __ldg(&bp.rayleigh_type);
+	if (!VMODE && __ldg(&bp.cube_fast)) {
+		float wsum = 0.0f;
+#pragma unroll
+		for (int n = 0; n < 8; n++) wsum += w[n];
+		const float ctm = __ldg(&bp.compliance) / (0.125f * wsum);
+		const float side = vol / (area * (1.0f / 6.0f));
+		const float cs = -2.0f * dt * dt / ctm * (0.5f * side);
+		// the moves are added to D as increments: D is small next to the
+		// positions, and rebuilding it as X' - S would round it at the
+		// positions' ulp (the reference keeps positions in double here)
+		Vec3 dX[8];
+#pragma unroll
+		for (int n = 0; n < 8; n++) {
+			dX[n] = {cs * (X[n].x - c.x), cs * (X[n].y - c.y), cs * (X[n].z - c.z)};
+			X[n] = {X[n].x + dX[n].x, X[n].y + dX[n].y, X[n].z + dX[n].z};
+		}
+		Vec3 sA, sB, sC, A[3];
+		corner_sums(X, sA, sB, sC);
+		const float J = cube_adj(sA, sB, sC, A);
+		const float vs = (J - vol) / (8.0f * (dot(A[0], A[0]) + dot(A[1], A[1]) + dot(A[2], A[2])));
+#pragma unroll
+		for (int n = 0; n < 8; n++) {
+			const float a = (n & 1) ? 1.0f : -1.0f, b = (n & 2) ? 1.0f : -1.0f, cc = (n & 4) ? 1.0f : -1.0f;
+			const Vec3 g = {fmaf(a, A[0].x, fmaf(b, A[1].x, cc * A[2].x)), fmaf(a, A[0].y, fmaf(b, A[1].y, cc * A[2].y)),
+			                fmaf(a, A[0].z, fmaf(b, A[1].z, cc * A[2].z))};
+			D[n].x += fmaf(-vs, g.x, dX[n].x);
+			D[n].y += fmaf(-vs, g.y, dX[n].y);
+			D[n].z += fmaf(-vs, g.z, dX[n].z);
+		}
+		return;
+	}
+	Vec3 P[8], dP[8];  // corners about the centroid; their moves (added to D at the end)
+#pragma unroll
+	for (int n = 0; n < 8; n++) {
+		P[n] = {X[n].x - c.x, X[n].y - c.y, X[n].z - c.z};
+		dP[n] = {0.0f, 0.0f, 0.0f};
+	}
+	// the I1 term (Yeoh of it for CubeSkin), XPBDFEM/Fem.cpp:659-712
+	{
+		float UI = 0.0f, PPw = 0.0f;
+#pragma unroll
+		for (int n = 0; n < 8; n++) {
+			const float PP = dot(P[n], P[n]);
+			UI += PP;
+			PPw = fmaf(w[n], PP, PPw);
+		}
+		const float US = 0.5f / ((1.0f / 6.0f) * area);
+		UI *= US;
+		float gS = 2.0f * US;
+		if (e == 12u) {
+			const float C0 = __ldg(&bp.yeoh[0]), C1 = __ldg(&bp.yeoh[1]), C2 = __ldg(&bp.yeoh[2]);
+			const float IM = UI - 3.0f;
+			UI = fmaxf(0.0001f, IM * fmaf(IM, fmaf(IM, C2, C1), C0));
+			gS *= fmaf(IM, fmaf(IM, 3.0f * C2, 2.0f * C1), C0);
+		}
+		const float alpha = __ldg(&bp.compliance) / vol * inv_dt2;
+		float wgg = PPw * gS * gS;
+		float lam = (-2.0f * UI) / fmaf(2.0f * UI, alpha, wgg);
+		if (!VMODE) {
+			if (damping > 0.0f && type < 2u) {
+				float gV = 0.0f;
+#pragma unroll
+				for (int n = 0; n < 8; n++) gV = fmaf(P[n].x, D[n].x, fmaf(P[n].y, D[n].y, fmaf(P[n].z, D[n].z, gV)));
+				gV *= gS;
+				if (type == 0u) {
+					const float gamma = damping * inv_dt;
+					lam = (-2.0f * UI - gamma * gV) / fmaf(wgg, 1.0f + gamma, 2.0f * UI * alpha);
+				} else {
+					const float A = fmaf(2.0f * UI, dt * alpha / damping, wgg);
+					const float b = (-gV - wgg * lam) * (A / fmaxf(A, 4.0f * wgg));
+					lam += b / A;
+				}
+			}
+			const float PS = lam * gS;
+#pragma unroll
+			for (int n = 0; n < 8; n++) {
+				const float sc = w[n] * PS;
+				dP[n] = {P[n].x * sc, P[n].y * sc, P[n].z * sc};
+				P[n] = {P[n].x + dP[n].x, P[n].y + dP[n].y, P[n].z + dP[n].z};
+			}
+		} else if (type >= 2u) {
+			wgg += 1.0e-22f;
+			float gV = 0.0f;
+#pragma unroll
+			for (int n = 0; n < 8; n++) gV = fmaf(P[n].x, D[n].x, fmaf(P[n].y, D[n].y, fmaf(P[n].z, D[n].z, gV)));
+			const float l2 = -(gS * gV) / fmaf(2.0f * UI, dt * alpha / damping, wgg);
+#pragma unroll
+			for (int n = 0; n < 8; n++) {
+				const float sc = w[n] * l2 * gS;
+				D[n].x = fmaf(sc, P[n].x, D[n].x);
+				D[n].y = fmaf(sc, P[n].y, D[n].y);
+				D[n].z = fmaf(sc, P[n].z, D[n].z);
+			}
+		}
+	}
+	// the volume, XPBDFEM/Fem.cpp:779-830: corners q and 7 - q move along
+	// +g_q and -g_q
+	{
+		Vec3 sA, sB, sC, A[3];
+		corner_sums(P, sA, sB, sC);
+		const float J = cube_adj(sA, sB, sC, A);
+		Vec3 g[4];
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const float a = (q & 1) ? 1.0f : -1.0f, b = (q & 2) ? 1.0f : -1.0f;
+			g[q] = {fmaf(a, A[0].x, fmaf(b, A[1].x, -A[2].x)), fmaf(a, A[0].y, fmaf(b, A[1].y, -A[2].y)),
+			        fmaf(a, A[0].z, fmaf(b, A[1].z, -A[2].z))};
+		}
+		float wgg = 0.0f;
+#pragma unroll
+		for (int q = 0; q < 4; q++) wgg = fmaf(w[q] + w[7 - q], dot(g[q], g[q]), wgg);
+		const float alpha = vol * __ldg(&bp.inv_lambda) * inv_dt2;
+		const float C = J - __ldg(&bp.a) * vol;
+		if (VMODE) {
+			float gV = 0.0f;
+#pragma unroll
+			for (int q = 0; q < 4; q++)
+				gV += dot({D[q].x - D[7 - q].x, D[q].y - D[7 - q].y, D[q].z - D[7 - q].z}, g[q]);
+			const float l2 = -gV / (dt * alpha / damping + (wgg + 1.0e-22f));
+#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				const float s0 = w[q] * l2, s1 = w[7 - q] * l2;
+				D[q] = {fmaf(s0, g[q].x, D[q].x), fmaf(s0, g[q].y, D[q].y), fmaf(s0, g[q].z, D[q].z), D[q].w};
+				D[7 - q] = {fmaf(-s1, g[q].x, D[7 - q].x), fmaf(-s1, g[q].y, D[7 - q].y), fmaf(-s1, g[q].z, D[7 - q].z),
+				            D[7 - q].w};
+			}
+			return;
+		}
+		float lam = -C / (wgg + alpha);
+		if (damping > 0.0f && type < 2u) {
+			// X - O of the corners, with the I1 step's move: D + dP
+			float gV = 0.0f;
+#pragma unroll
+			for (int q = 0; q < 4; q++) {
+				const Vec3 d = {(D[q].x + dP[q].x) - (D[7 - q].x + dP[7 - q].x),
+				                (D[q].y + dP[q].y) - (D[7 - q].y + dP[7 - q].y),
+				                (D[q].z + dP[q].z) - (D[7 - q].z + dP[7 - q].z)};
+				gV += dot(d, g[q]);
+			}
+			if (type == 0u) {
+				const float gamma = damping * inv_dt;
+				lam = (-C - gamma * gV) / fmaf(wgg, 1.0f + gamma, alpha);
+			} else {
+				const float Am = wgg + dt * alpha / damping;
+				const float b = (-gV - wgg * lam) * (Am / fmaxf(Am, 4.0f * wgg));
+				lam += b / Am;
+			}
+		}
+#pragma unroll
+		for (int q = 0; q < 4; q++) {
+			const float s0 = w[q] * lam, s1 = w[7 - q] * lam;
+			dP[q] = {fmaf(s0, g[q].x, dP[q].x), fmaf(s0, g[q].y, dP[q].y), fmaf(s0, g[q].z, dP[q].z)};
+			dP[7 - q] = {fmaf(-s1, g[q].x, dP[7 - q].x), fmaf(-s1, g[q].y, dP[7 - q].y), fmaf(-s1, g[q].z, dP[7 - q].z)};
+		}
+	}
+#pragma unroll
+	for (int n = 0; n < 8; n++) {
+		D[n].x += dP[n].x;
+		D[n].y += dP[n].y;
+		D[n].z += dP[n].z;
+	}
+}
+
 // One hex of a pass. kSolve: SolveElement; kVolume: SolveVolumeOnly;
 // kRayleigh: DampElement on the canonical state (O = X, D = V) with the
 // Rayleigh ratio rd (x 8 when amortized).
@@ -363,6 +573,12 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 	const float damp = KIND == kSolve && type < 2u ? __ldg(&bp.damping) : 0.0f;
 	const bool limit = type == 1u;
 	const bool sim = __ldg(&bp.simultaneous) != 0u;
+	if (KIND != kVolume && (e == 11u || e == 12u)) {
+		cube<KIND == kRayleigh>(bp, R, e, w, O, D, 1.0f / inv_dt, inv_dt, inv_dt2, rd);
+#pragma unroll
+		for (int n = 0; n < 8; n++) st_vertex(C.vert + 2 * (size_t)dv[n], O[n], D[n]);
+		return;
+	}
 	Vec3 P[7], g0[8], g1[8];
 	rel(O, D, KIND == kRayleigh, P);
 	if (KIND == kVolume) {

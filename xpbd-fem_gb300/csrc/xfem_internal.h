@@ -151,7 +151,8 @@ struct BodyParams {
 	float compliance;         // Settings::compliance (the volume passes' compliance per volume)
 	float lambda;             // (2 mu nu) / (1 - 2 nu) (continuous-pressure models)
 	uint32_t nverts;          // vertices of the body (amortized ring damping slices)
-	uint32_t pad4[3];
+	uint32_t cube_fast;       // SolveElementCube's short path on hexes: CubeNeo, nu >= 0.5, no damping
+	uint32_t pad4[2];
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
