@@ -32,8 +32,9 @@
  *
  * Meshes of linear hexahedra (tag 8) run in hex mode: GeoLinear3d's hex loops
  * (XPBDFEM/Geo.cpp:736-740, 777-811) with SolveElement on
- * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), the energy models 0-7 and
- * above 12. A mesh holds tets or hexes, not both, and so does a handle.
+ * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), every energy model but the
+ * continuous-pressure ones (8-10). A mesh holds tets or hexes, not both, and
+ * so does a handle.
  */
 #ifndef XFEM_H
 #define XFEM_H
@@ -70,7 +71,7 @@ extern "C" {
 #define XFEM_ENERGY_CONTINUOUS_PIXAR 8u /* continuous pressure: one constraint per vertex one-ring */
 #define XFEM_ENERGY_CONTINUOUS_MIXED 9u /* likewise, the deviatoric + hydrostatic pair */
 #define XFEM_ENERGY_CONTINUOUS_SKIN 10u /* likewise, with the Yeoh deviatoric term */
-#define XFEM_ENERGY_CUBE_NEO 11u       /* Energy_CubeNeo: acts on quads and hexes, so on no tet */
+#define XFEM_ENERGY_CUBE_NEO 11u       /* Energy_CubeNeo: acts on hexes (and quads), on no tet */
 #define XFEM_ENERGY_CUBE_SKIN 12u      /* Energy_CubeSkin: likewise */
 #define XFEM_MAX_VOLUME_PASSES 64u     /* largest xfem_settings::volume_passes accepted */
 #define XFEM_XPBD_SOLVE_BIT 11u        /* set: coupled 2x2 solve; clear: serial */
@@ -167,8 +168,8 @@ int xfem_settings_default(xfem_settings* s);
  * lumped masses and inverse masses — then builds the colour schedule and
  * uploads everything. A mesh of hexes (tag 8) gets the hex rest state
  * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
- * a mesh mixing tets and hexes, or a hex mesh with the continuous-pressure or
- * cube models (energy 8-12), returns XFEM_EUNSUPPORTED. */
+ * a mesh mixing tets and hexes, or a hex mesh with the continuous-pressure
+ * models (energy 8-10), returns XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
