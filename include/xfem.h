@@ -247,7 +247,9 @@ int xfem_adjoint_forward(xfem_body* b, uint32_t substeps, float dt, uint32_t che
  * dL/dmu, with mu the tet's shear modulus (1/compliance or the value given
  * to xfem_set_tet_mu); dx0, dv0 (3 per vertex): dL/d the positions and
  * velocities at the start. The handle's state stays at the end of the
- * forward run. Synchronising. */
+ * forward run. Synchronising. The reverse kernel takes one of two forms with
+ * the same results bit for bit; XFEM_REVERSE_FORM=grouped or =lane in the
+ * environment fixes the choice (diagnostics). */
 int xfem_adjoint_backward(xfem_body* b, const float* grad_tip_traj, const float* grad_x, const float* grad_v,
                           float* dmu, float* dx0, float* dv0);
 

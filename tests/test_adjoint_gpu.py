@@ -10,9 +10,10 @@ reverse against the FP64 derivative of the same method). The end-to-end
 gradient of a tip loss (G from the GPU's own float trajectory) is checked in
 test_beam_end_to_end with the bound stated there.
 
-Bit-exact: checkpointed and full-tape runs, a batched handle against its
-bodies run alone, the recorded trajectory against the plain forward, and the
-torch.autograd binding against the C ABI. Every run starts from a freshly
+Bit-exact: checkpointed and full-tape runs, the two forms of the reverse
+kernel, a batched handle against its bodies run alone, the recorded
+trajectory against the plain forward, and the torch.autograd binding against
+the C ABI. Every run starts from a freshly
 created body: a lock zeroes the vertex's inverse mass at the end of the first
 substep, so a handle that has stepped does not repeat its first run.
 """
@@ -148,6 +149,22 @@ def test_checkpointed_equals_full_tape():
         for k in ("traj", "dmu", "dx", "dv"):
             assert np.array_equal(getattr(full, k), getattr(ck, k)), (K, k)
         assert np.array_equal(ck.body.positions(), x_end), K
+
+
+@pytest.mark.parametrize("make", [cantilever, ground_box, lambda: cantilever(cluster_mode=1)])
+def test_reverse_forms_agree(make, monkeypatch):
+    """The grouped reverse (8 lanes per cube cluster, the forward internals of
+    its six solves recomputed side by side) and the one-lane reverse give the
+    same gradients bit for bit; the small meshes here take the grouped form
+    unless told otherwise."""
+    c = make()
+    runs = {}
+    for form in ("grouped", "lane"):
+        monkeypatch.setenv("XFEM_REVERSE_FORM", form)
+        runs[form] = c.gpu(K=7)
+    for k in ("traj", "dmu", "dx", "dv"):
+        assert np.array_equal(runs["grouped"].__dict__[k], runs["lane"].__dict__[k]), k
+    c.check(runs["grouped"])
 
 
 def test_trajectory_is_the_plain_forward():

@@ -29,6 +29,7 @@
 // -mu dL/dmu since both compliances scale as 1/mu (the host divides by -mu).
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "xfem_device.cuh"
 #include "xfem_internal.h"
@@ -360,10 +361,97 @@ __device__ __forceinline__ void cluster_reverse(const DevCtx& C, const AdjCtx& A
 	}
 }
 
+// The cube reverse with a group of 8 lanes per cluster (meshes whose colour
+// passes leave most warps idle). The six solves' forward internals do not
+// depend on the reverse chain, only on the tape: lanes 0-5 of the group
+// recompute tet j's into shared memory side by side, then lane 0 runs the
+// chain of six reverses as cluster_reverse<true> does, in the same order
+// with the same arithmetic (the same results bit for bit), with one solve's
+// recompute instead of six ahead of it. sh: this group's six slots; cl: the
+// cluster's lane in its chunk; j: the lane's index in the group.
+// One solve's slot: its forward internals and the record words its reverse
+// reads (QQ in c.yzw, QR in d.xyz).
+struct TetSlot {
+	TetFw f;
+	float4 c, d;
+};
+
+__device__ __forceinline__ void cluster_reverse_grouped(const DevCtx& C, const AdjCtx& A, const float4* blk,
+                                                        uint32_t trow, uint32_t cl, uint32_t j, TetSlot* sh, uint32_t s,
+                                                        bool first, float dt, float inv_dt2) {
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(blk + 4 * kLanes * 6);
+	const uint32_t* vids = hdrs + kLanes;
+	const uint32_t hdr = __ldg(hdrs + cl);
+	const bool live = (hdr & 15u) != 0;
+	if (live && j < 6u) {
+		const Mat mat = load_mat(C.bodies, hdr >> 16);
+		const float4* r = blk + j * 4 * kLanes + cl;
+		const TetRec tr = {__ldg(r), __ldg(r + kLanes), __ldg(r + 2 * kLanes), __ldg(r + 3 * kLanes)};
+		const uint32_t sl = (uint32_t)(cube_slot((int)j, 0) | cube_slot((int)j, 1) << 4 | cube_slot((int)j, 2) << 8 |
+		                               cube_slot((int)j, 3) << 12);
+		float4 Ot[4];
+#pragma unroll
+		for (int k = 0; k < 4; k++) Ot[k] = __ldcg(tape_at(C, s, __ldg(vids + ((sl >> (4 * k)) & 15u) * kLanes + cl)));
+		Vec3 Din[4];
+		load_tet_input(C, s, trow + j, cl, Din);
+		tet_internals(mat, tr, inv_dt2, Ot, Din, sh[j].f);
+		sh[j].c = tr.c;
+		sh[j].d = tr.d;
+	}
+	__syncwarp();
+	Vec3* xs = reinterpret_cast<Vec3*>(sh);  // after the chain: the 8 vertices' adjoints
+	if (live && j == 0u) {
+		float4 O[8];
+		Vec3 xb[8];
+#pragma unroll
+		for (int k = 0; k < 8; k++) {
+			const uint32_t v = __ldg(vids + k * kLanes + cl);
+			O[k] = __ldcg(tape_at(C, s, v));
+			xb[k] = v3(__ldcg(A.abar + 2 * (size_t)v));
+		}
+#pragma unroll
+		for (int t = 5; t >= 0; t--) {
+			const TetRec tr = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f), sh[t].c, sh[t].d};
+			float w[4];
+			Vec3 xt[4];
+#pragma unroll
+			for (int k = 0; k < 4; k++) {
+				w[k] = O[cube_slot(t, k)].w;
+				xt[k] = xb[cube_slot(t, k)];
+			}
+			const TetFw f = sh[t].f;
+			const float dal = tet_reverse(tr, f, w, xt);
+#pragma unroll
+			for (int k = 0; k < 4; k++) xb[cube_slot(t, k)] = xt[k];
+			float* cb = A.cbar + (size_t)(trow + t) * kLanes + cl;
+			*cb += dal;
+		}
+		// the slots' reads above come first in this lane's program order
+#pragma unroll
+		for (int k = 0; k < 8; k++) xs[k] = xb[k];
+	}
+	__syncwarp();
+	// lane j finishes vertex j of the cluster: its advance reverse if the
+	// cluster owns it, else its adjoint
+	if (live) {
+		const uint32_t v = __ldg(vids + j * kLanes + cl);
+		const Vec3 x = xs[j];
+		if ((hdr >> (8 + j)) & 1u)
+			advance_reverse(C, A, v, s, first, dt, x);
+		else
+			__stcg(A.abar + 2 * (size_t)v, make_float4(x.x, x.y, x.z, 0.0f));
+	}
+	__syncwarp();  // the group's slots are free for the next cluster
+}
+
 // Reverse of one recorded launch of nsub substeps (one checkpoint segment).
 // Cooperative persistent grid, one warp per chunk of a colour pass; every
-// colour pass ends at the bounded grid barrier, as in the forward.
-__global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t nsub, float dt, int last) {
+// colour pass ends at the bounded grid barrier, as in the forward. grouped:
+// every colour pass's chunks, split in 8 parts of 4 clusters, fit the grid's
+// warps at once: a warp takes one part, a group of 8 lanes per cluster
+// (cluster_reverse_grouped; other chunks one lane per cluster).
+__global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t nsub, float dt, int last, int grouped) {
+	extern __shared__ __align__(16) unsigned char rsmem[];
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
@@ -373,9 +461,25 @@ __global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t ns
 	for (uint32_t v = gtid; v < C.nverts; v += nthreads) finalize_reverse(C, A, v, nsub, inv_dt, last != 0);
 	bool ok = grid_sync(C, target);
 	if (ok) isolated_reverse(C, A, gtid, nthreads, nsub, dt);
+	TetSlot* gsh = reinterpret_cast<TetSlot*>(rsmem) + (size_t)wib * 24 + (lane >> 3) * 6;
 	for (int s = (int)nsub - 1; s >= 0 && ok; s--) {
 		for (int c = (int)C.ncolours - 1; c >= 0 && ok; c--) {
 			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
+			if (grouped) {
+				for (uint32_t it = gwarp; it < 8u * (ce - cb); it += nwarps) {
+					const uint32_t ch = cb + it / 8u, cl = (it % 8u) * 4u + (lane >> 3);
+					const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + ch);
+					const float4* blk = C.cblk + m.x;
+					if (m.z & kShapeCube) {
+						cluster_reverse_grouped(C, A, blk, m.w, cl, lane & 7u, gsh, (uint32_t)s, s == 0, dt, inv_dt2);
+					} else if ((lane & 7u) == 0u) {
+						cluster_reverse<false>(C, A, blk, m.z & 0xffu, (m.z >> 8) & 0xffu, m.w, cl, (uint32_t)s, s == 0,
+						                       dt, inv_dt2);
+					}
+				}
+				if (!grid_sync(C, target)) ok = false;
+				continue;
+			}
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + ch);
 				const float4* blk = C.cblk + m.x;
@@ -394,14 +498,17 @@ __global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t ns
 
 int configure_adjoint_kernels(int, uint32_t) { return 0; }
 
-int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, uint32_t, uint32_t nsub, float dt, bool last,
-                   void* stream) {
+int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, uint32_t max_colour_chunks, uint32_t nsub,
+                   float dt, bool last, void* stream) {
 	if (nsub == 0) return 0;
 	cudaStream_t st = (cudaStream_t)stream;
 	int dev = 0, sms = 0, per_sm = 0;
-	cudaError_t e = cudaGetDevice(&dev);
+	// six forward-internal slots per 8-lane group, 4 groups per warp
+	const size_t smem = (size_t)(block / 32) * 24 * sizeof(TetSlot);
+	cudaError_t e = cudaFuncSetAttribute((const void*)k_reverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e == cudaSuccess) e = cudaGetDevice(&dev);
 	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_reverse, block, 0);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_reverse, block, smem);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
 	// the whole co-resident grid, as the forward: chunk i of a colour goes to
@@ -413,8 +520,12 @@ int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, ui
 	DevCtx c = ctx;
 	AdjCtx a = adj;
 	int lastv = last ? 1 : 0;
-	void* args[] = {&c, &a, &nsub, &dt, &lastv};
-	return (int)cudaLaunchCooperativeKernel((const void*)k_reverse, dim3(blocks), dim3(block), args, 0, st);
+	// the grouped form when one round of the grid's warps takes every part of
+	// the largest colour pass
+	int grouped = (uint64_t)max_colour_chunks * 8u <= (uint64_t)blocks * (uint32_t)(block / 32) ? 1 : 0;
+	if (const char* f = getenv("XFEM_REVERSE_FORM")) grouped = f[0] == 'g' ? 1 : f[0] == 'l' ? 0 : grouped;
+	void* args[] = {&c, &a, &nsub, &dt, &lastv, &grouped};
+	return (int)cudaLaunchCooperativeKernel((const void*)k_reverse, dim3(blocks), dim3(block), args, smem, st);
 }
 
 }  // namespace xfem
