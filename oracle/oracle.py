@@ -146,6 +146,19 @@ def lib():
         L.orc_hex_volume_d.argtypes = [P, u32, P, P]
         L.orc_hex_volume_d.restype = C.c_double
         L.orc_hex_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.orc_t10_tables.argtypes = [P, P, P]
+        L.orc_tet_edges.argtypes = [P, u32, u32, P, P, P]
+        L.orc_t10_init_rest_f.argtypes = [P, u32, P, u32, P, u32, P, C.c_float, P, P, P, P]
+        L.orc_t10_init_rest_d.argtypes = [P, u32, P, u32, P, u32, P, C.c_double, P, P, P, P]
+        L.orc_solve_t10_f.argtypes = [P, P, P, P, P]
+        L.orc_solve_t10_d.argtypes = [P, P, P, P, P]
+        L.orc_t10_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_t10_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_t10_volume_f.argtypes = [P, u32, P, P]
+        L.orc_t10_volume_f.restype = C.c_float
+        L.orc_t10_volume_d.argtypes = [P, u32, P, P]
+        L.orc_t10_volume_d.restype = C.c_double
+        L.orc_t10_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -410,8 +423,90 @@ def hex_schedule(nodes, hexes, morton=1):
     nv, nh = nodes.size // 3, hexes.shape[0]
     rank = np.zeros(nv, np.uint32)
     order = np.zeros(nh, np.uint32)
-    cb = np.zeros(65, np.uint32)
+    cb = np.zeros(nh + 1, np.uint32)
     ncol = C.c_uint32()
     if lib().orc_hex_schedule(_p(nodes), nv, _p(hexes), nh, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
-        raise ValueError("hex schedule needs more than 64 colours")
+        raise ValueError("hex schedule needs more than 4096 colours")
     return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+# ---- quadratic tetrahedra (oracle/xfem_oracle_t10.inc) ----
+T10_EP = 56  # values per T10 rest-state record (ElementParamsQuadraticTet flattened)
+
+
+def t10_tables():
+    g4, g10, w10 = np.zeros((4, 10, 3), np.float32), np.zeros((10, 10, 3), np.float32), np.zeros(10, np.float32)
+    lib().orc_t10_tables(_p(g4), _p(g10), _p(w10))
+    return g4, g10, w10
+
+
+def tet_edges(tets, nv):
+    """Connectivity3d's edge numbering and GeoQuadratic3d's T10 indices:
+    (edges[ne, 2], t10[nt, 10])."""
+    tets = np.ascontiguousarray(tets, np.uint32)
+    nt = tets.shape[0]
+    edges = np.zeros((max(6 * nt, 1), 2), np.uint32)
+    t10 = np.zeros((nt, 10), np.uint32)
+    ne = C.c_uint32()
+    if lib().orc_tet_edges(_p(tets), nt, nv, _p(edges), C.byref(ne), _p(t10)):
+        raise MemoryError("edge enumeration failed")
+    return edges[:ne.value].copy(), t10
+
+
+class Quadratic:
+    """A T10 mesh as GeoQuadratic3d builds it from a tet mesh."""
+
+    def __init__(self, nodes, idx, density, dtype=np.float32):
+        nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+        self.tets, self.nv = parse_tets(idx)
+        self.edges, self.t10 = tet_edges(self.tets, self.nv)
+        n = self.nv + self.edges.shape[0]
+        nt = self.tets.shape[0]
+        self.X0 = np.zeros((n, 3), np.float64)
+        self.ep = np.zeros((nt, T10_EP), dtype)
+        self.w = np.zeros(n, dtype)
+        self.flags = np.zeros(n, np.uint8)
+        f = lib().orc_t10_init_rest_f if dtype == np.float32 else lib().orc_t10_init_rest_d
+        f(_p(nodes), self.nv, _p(self.tets), nt, _p(self.edges), self.edges.shape[0], _p(self.t10), density,
+          _p(self.X0), _p(self.ep), _p(self.w), _p(self.flags))
+        self.dtype = dtype
+
+    def schedule(self, morton=1):
+        X = self.X0.astype(np.float32)
+        n, nt = X.shape[0], self.t10.shape[0]
+        rank = np.zeros(n, np.uint32)
+        order = np.zeros(nt, np.uint32)
+        cb = np.zeros(nt + 1, np.uint32)
+        ncol = C.c_uint32()
+        if lib().orc_t10_schedule(_p(X), n, _p(self.t10), nt, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
+            raise ValueError("T10 schedule needs more than 4096 colours")
+        return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def substeps(self, X, V, w, order, nsub, params, lock_mask=None):
+        X = np.array(X, np.float64).reshape(-1).copy()
+        V = np.array(V, np.float64).reshape(-1).copy()
+        w = np.array(w, self.dtype).copy()
+        order = np.ascontiguousarray(order, np.uint32)
+        lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+        contact = np.zeros(w.size, np.uint8)
+        f = lib().orc_t10_substeps_f if self.dtype == np.float32 else lib().orc_t10_substeps_d
+        if f(w.size, _p(X), _p(V), _p(w), _p(lm), self.t10.shape[0], _p(self.t10), _p(self.ep), _p(order), nsub,
+             C.byref(params), _p(contact)):
+            raise ValueError("energy model not covered on quadratic tets")
+        return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+    def volume(self, X):
+        X = np.ascontiguousarray(X, np.float64).reshape(-1)
+        f = lib().orc_t10_volume_f if self.dtype == np.float32 else lib().orc_t10_volume_d
+        return f(_p(X), self.t10.shape[0], _p(self.t10), _p(self.ep))
+
+
+def solve_t10(X, w, ep, params, O, dtype=np.float32):
+    X = np.array(X, np.float64).reshape(10, 3).copy()
+    O = np.ascontiguousarray(O, np.float64).reshape(10, 3)
+    w = np.ascontiguousarray(w, dtype)
+    ep = np.ascontiguousarray(ep, dtype)
+    f = lib().orc_solve_t10_f if dtype == np.float32 else lib().orc_solve_t10_d
+    if f(_p(X), _p(O), _p(w), _p(ep), C.byref(params)):
+        raise ValueError("energy model not covered on quadratic tets")
+    return X

@@ -65,6 +65,17 @@
  *       and Damp then run their hex loops (XPBDFEM/Geo.cpp:777-811).
  *   hsolve seed count energy simultaneous compliance poisson dt
  *       SolveElement (XPBDFEM/Fem.cpp:896) on `count` seeded random hexes.
+ *
+ * Quadratic tets: the same commands prefixed with `q` build GeoQuadratic3d
+ * (XPBDFEM/Geo.cpp:836-1053) on a GenerateTetBlock mesh, pattern after the
+ * scale:
+ *   qinit W H D sx sy sz pattern wonkiness density
+ *       all vertex positions (corners, then edge midpoints), the T10 indices,
+ *       the per-T10 rest state (Qi, ic.QQ[9], ic.QR[36], volume,
+ *       surfaceArea), w, flags, tOrder and CalculateVolume.
+ *   qordered / qdamped (as hordered / hdamped) < torder.u32
+ *   qsolve seed count energy simultaneous compliance poisson dt
+ *       SolveElement (XPBDFEM/Fem.cpp:893) on `count` seeded random T10s.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -201,7 +212,17 @@ static void dump_hex_geo(GeoLinear3d* g) {
 	emit("volume", 'f', &vol, 1);
 }
 
-static void dump_state(GeoLinear3d* g, const char* xname, const char* vname) {
+// ElementParamsQuadraticTet (XPBDFEM/Fem.h:61-68) flattened, 56 values.
+static void t10_record(const ElementParamsQuadraticTet& e, float* o) {
+	for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[c * 3 + r] = e.Qi[c][r];
+	for (int k = 0; k < 9; k++) o[9 + k] = e.ic.QQ[k];
+	for (int k = 0; k < 36; k++) o[18 + k] = e.ic.QR[k];
+	o[54] = e.volume;
+	o[55] = e.surfaceArea;
+}
+
+template <typename G>
+static void dump_state(G* g, const char* xname, const char* vname) {
 	uint32_t nv = g->vertCount;
 	std::vector<double> x(nv * 3), v(nv * 3);
 	for (uint32_t i = 0; i < nv; i++)
@@ -212,10 +233,132 @@ static void dump_state(GeoLinear3d* g, const char* xname, const char* vname) {
 
 int main(int argc, char** argv) {
 	if (argc < 2) { fprintf(stderr, "usage: refgen <cmd> ...\n"); return 2; }
-	const bool hex = argv[1][0] == 'h';
-	const char* cmd = argv[1] + (hex ? 1 : 0);
+	const bool hex = argv[1][0] == 'h', quad = argv[1][0] == 'q';
+	const char* cmd = argv[1] + (hex || quad ? 1 : 0);
 	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
+
+	if (quad && (!strcmp(cmd, "init") || !strcmp(cmd, "ordered") || !strcmp(cmd, "damped"))) {
+		Allocator* alloc = make_alloc((size_t)1 << 31);
+		uint32_t W = U(2), H = U(3), D = U(4);
+		vec3 scale(F(5), F(6), F(7));
+		uint32_t pattern = U(8);
+		float wonk = F(9), density = F(10);
+		int a = 11;
+		const float* nodes; uint32_t nodeCount; const uint32_t* idx; uint32_t idxCount;
+		GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		GeoQuadratic3d* g = alloc->New<GeoQuadratic3d>();
+		g->Init(alloc, density, nodes, nodeCount, idx, idxCount, false);
+		emit("nodes", 'f', nodes, nodeCount);
+		emit("idx", 'I', idx, idxCount);
+		if (!strcmp(cmd, "init")) {
+			uint32_t nt = g->con.tetCount, nv = g->vertCount;
+			std::vector<float> ep(nt * 56);
+			std::vector<uint32_t> ti(nt * 10);
+			for (uint32_t i = 0; i < nt; i++) {
+				t10_record(g->t[i].ep, &ep[i * 56]);
+				for (int k = 0; k < 10; k++) ti[i * 10 + k] = g->t[i].i[k];
+			}
+			std::vector<double> x0(nv * 3);
+			for (uint32_t i = 0; i < nv; i++) for (int k = 0; k < 3; k++) x0[i * 3 + k] = g->X[i][k];
+			std::vector<uint8_t> flags(g->flags, g->flags + nv);
+			emit("x0", 'd', x0.data(), x0.size());
+			emit("t10_idx", 'I', ti.data(), ti.size());
+			emit("qep", 'f', ep.data(), ep.size());
+			emit("w", 'f', g->w, nv);
+			emit("vflags", 'B', flags.data(), nv);
+			emit("torder", 'I', g->tOrder, nt);
+			float vol = g->CalculateVolume();
+			emit("volume", 'f', &vol, 1);
+			return 0;
+		}
+		uint32_t energy = U(a++), simul = U(a++);
+		float compliance = F(a++), poisson = F(a++), gx = F(a++), gy = F(a++), dt = F(a++);
+		uint32_t nsub = U(a++), lockLeft = U(a++);
+		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
+		s.flags = (s.flags & ~(Settings_ElementTypeMask << Settings_ElementTypeBit)) | (Element_T10 << Settings_ElementTypeBit);
+		if (!strcmp(cmd, "damped")) {
+			s.damping = F(a++);
+			s.pbdDamping = F(a++);
+			s.drag = F(a++);
+			const uint32_t rtype = U(a++);
+			const float spacing = F(a++);
+			s.flags = (s.flags & ~(Settings_RayleighTypeMask << Settings_RayleighTypeBit)) | (rtype << Settings_RayleighTypeBit);
+			const float sdt = dt;
+			float tcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * sdt);
+			s.areaAndTimeCorrectedPbdDamping = tcpd * spacing * spacing;
+			s.volumeAndTimeCorrectedPbdDamping = tcpd * 6.0f * spacing * spacing;
+			float atcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * (float)AmortizationPeriod * sdt);
+			s.amortizedAreaAndTimeCorrectedPbdDamping = atcpd * spacing * spacing;
+			s.amortizedVolumeAndTimeCorrectedPbdDamping = atcpd * 6.0f * spacing * spacing;
+			s.timeCorrectedDrag = 1.0f - pow(1.0f - s.drag, 1000.0f * sdt);
+			const float derived[3] = {s.volumeAndTimeCorrectedPbdDamping, s.amortizedVolumeAndTimeCorrectedPbdDamping,
+			                          s.timeCorrectedDrag};
+			emit("derived", 'f', derived, 3);
+			if (a < argc) s.volumePasses = U(a++);
+		}
+		uint32_t n = 0;
+		if (fread(&n, 4, 1, stdin) != 1 || n != g->con.tetCount) { fprintf(stderr, "bad order\n"); return 3; }
+		if (fread(g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+		Manipulator manip;
+		manip.pickedGeo = nullptr;
+		for (uint32_t k = 0; k < nsub; k++) {
+			s.tickId = k;
+			g->Substep(s, manip, dt);
+			if (k == 0) dump_state(g, "x1", "v1");
+		}
+		dump_state(g, "xn", "vn");
+		float vol = g->CalculateVolume();
+		emit("volume", 'f', &vol, 1);
+		return 0;
+	}
+
+	if (quad && !strcmp(cmd, "solve")) {
+		g_rng = strtoull(argv[2], 0, 10);
+		uint32_t count = U(3), energy = U(4), simul = U(5);
+		float compliance = F(6), poisson = F(7), dt = F(8);
+		Settings s = make_settings(energy, simul, compliance, poisson, 0.0f, 0.0f, 0);
+		std::vector<double> xin(count * 30), xout(count * 30), rest(count * 30);
+		std::vector<float> win(count * 10), epo(count * 56);
+		static const int te[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+		for (uint32_t t = 0; t < count; t++) {
+			dvec3 X0[10], X[10], O[10];
+			float m[10] = {0}, w[10];
+			// corners as the linear `solve` command's random tet, midpoints on the edges
+			double sc = 0.02 + 0.2 * urand();
+			for (int n = 0; n < 4; n++) X0[n] = dvec3(sc * (urand() - 0.5), sc * (urand() - 0.5), sc * (urand() - 0.5));
+			X0[0] = X0[3] + dvec3(sc * (0.6 + 0.4 * urand()), 0.1 * sc * (urand() - 0.5), 0.1 * sc * (urand() - 0.5));
+			X0[1] = X0[3] + dvec3(0.1 * sc * (urand() - 0.5), sc * (0.6 + 0.4 * urand()), 0.1 * sc * (urand() - 0.5));
+			X0[2] = X0[3] + dvec3(0.1 * sc * (urand() - 0.5), 0.1 * sc * (urand() - 0.5), sc * (0.6 + 0.4 * urand()));
+			for (int n = 0; n < 4; n++) for (int k = 0; k < 3; k++) X0[n][k] = (double)(float)X0[n][k];
+			for (int e = 0; e < 6; e++) X0[4 + e] = 0.5 * (X0[te[e][0]] + X0[te[e][1]]);
+			const uint32_t is[10] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9};
+			ElementParamsQuadraticTet ep;
+			InitFiniteElement(X0, is, 1000.0f, m, &ep);
+			uint32_t kind = t % 8;
+			double amp = kind < 4 ? 0.05 : kind < 6 ? 0.4 : 1.5;
+			for (int n = 0; n < 10; n++) {
+				for (int k = 0; k < 3; k++) X[n][k] = X0[n][k] + amp * sc * (urand() - 0.5);
+				O[n] = X0[n];
+				w[n] = (float)(0.5 + 2.0 * urand());
+			}
+			if (kind == 6) { dvec3 tmp = X[0]; X[0] = X[1]; X[1] = tmp; }
+			if (kind == 7) { w[0] = 0.0f; w[9] = 0.0f; }
+			for (int n = 0; n < 10; n++) {
+				win[t * 10 + n] = w[n];
+				for (int k = 0; k < 3; k++) { xin[t * 30 + n * 3 + k] = X[n][k]; rest[t * 30 + n * 3 + k] = X0[n][k]; }
+			}
+			SolveElement(dt, X, O, w, is, ep, s);
+			for (int n = 0; n < 10; n++) for (int k = 0; k < 3; k++) xout[t * 30 + n * 3 + k] = X[n][k];
+			t10_record(ep, &epo[t * 56]);
+		}
+		emit("rest", 'd', rest.data(), rest.size());
+		emit("qep", 'f', epo.data(), epo.size());
+		emit("xin", 'd', xin.data(), xin.size());
+		emit("w", 'f', win.data(), win.size());
+		emit("xout", 'd', xout.data(), xout.size());
+		return 0;
+	}
 
 	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered") ||
 	    !strcmp(cmd, "damped") || !strcmp(cmd, "rings")) {

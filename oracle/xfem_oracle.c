@@ -116,6 +116,66 @@ void orc_hex_tables(float* n8, float* g8, float* g1) {
 		for (int k = 0; k < 3; k++) g1[3 * n + k] = hex_g1(n, k);
 }
 
+/* ---- quadratic-tet (T10) tables -------------------------------------------- */
+/* The 10-node tet's shape-function gradients at the 4-point rule (the solve,
+ * XPBDFEM/Fem.cpp:60) and the 10-point rule (the prefactored coefficients,
+ * :61), and the weights (:11-12), printed by the reference to six decimals.
+ * Nodes: corners 0-3 with barycentric L0 = x, L1 = y, L2 = z, L3 = 1 - x - y
+ * - z, then the edges (0,1), (0,2), (0,3), (1,2), (1,3), (2,3). A corner's
+ * gradient is (4 L_c - 1) grad L_c, an edge's 4 (L_b grad L_a + L_a grad
+ * L_b). Point p of the 4-point rule has L_p = a4 and the others b4; the
+ * 10-point rule's points 0-3 have L_p = a10 (others b10) and points 4-9, one
+ * per edge in node order, L = c10 on the edge's two corners (d10 on the
+ * others). Each entry is the signed printed magnitude nearest to its value,
+ * so the tables are built from those literals. */
+static const double t10_mag4[5] = {0.447214, 0.552786, 1.341641, 1.788854, 2.341641};
+static const double t10_mag10[9] = {0.295340, 0.375023, 0.624977, 0.704660, 1.249955,
+                                    1.624977, 2.113981, 2.818642, 3.113981};
+static const int t10_edge[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+/* barycentric coordinate c of point p (rule of np points) */
+static double t10_L(int np, int p, int c) {
+	if (np == 4) return p == c ? (1.341641 + 1.0) / 4.0 : (1.0 - 0.447214) / 4.0;
+	if (p < 4) return p == c ? (2.113981 + 1.0) / 4.0 : (1.0 - 0.704660) / 4.0;
+	const int* e = t10_edge[p - 4];
+	return (c == e[0] || c == e[1]) ? (0.624977 + 1.0) / 4.0 : (1.0 - 0.624977) / 4.0;
+}
+
+static float t10_snap(double v, const double* mag, int nm) {
+	if (fabs(v) < 1e-3) return 0.0f;
+	int best = 0;
+	for (int i = 1; i < nm; i++)
+		if (fabs(fabs(v) - mag[i]) < fabs(fabs(v) - mag[best])) best = i;
+	return v < 0 ? -(float)mag[best] : (float)mag[best];
+}
+
+/* ShapeFunctionGradients<Tet, 10, np>[p][n][k], np = 4 or 10 */
+static float t10_g(int np, int p, int n, int k) {
+	static const double gl[4][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {-1, -1, -1}};
+	double v;
+	if (n < 4) {
+		v = (4.0 * t10_L(np, p, n) - 1.0) * gl[n][k];
+	} else {
+		const int a = t10_edge[n - 4][0], b = t10_edge[n - 4][1];
+		v = 4.0 * (t10_L(np, p, b) * gl[a][k] + t10_L(np, p, a) * gl[b][k]);
+	}
+	return np == 4 ? t10_snap(v, t10_mag4, 5) : t10_snap(v, t10_mag10, 9);
+}
+
+/* QuadratureWeights<Tet, np>[p] */
+static float t10_w(int np, int p) { return np == 4 ? 0.250000f : p < 4 ? 0.047633f : 0.134911f; }
+
+void orc_t10_tables(float* g4, float* g10, float* w10) {
+	for (int p = 0; p < 4; p++)
+		for (int n = 0; n < 10; n++)
+			for (int k = 0; k < 3; k++) g4[30 * p + 3 * n + k] = t10_g(4, p, n, k);
+	for (int p = 0; p < 10; p++) {
+		w10[p] = t10_w(10, p);
+		for (int n = 0; n < 10; n++)
+			for (int k = 0; k < 3; k++) g10[30 * p + 3 * n + k] = t10_g(10, p, n, k);
+	}
+}
+
 /* ---- float instantiation (reference semantics) ---------------------------- */
 #define R float
 #define SFX _f
@@ -127,6 +187,7 @@ void orc_hex_tables(float* n8, float* g8, float* g1) {
 #define EPS4 0.0001f
 #include "xfem_oracle_real.inc"
 #include "xfem_oracle_hex.inc"
+#include "xfem_oracle_t10.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -147,6 +208,7 @@ void orc_hex_tables(float* n8, float* g8, float* g1) {
 #define EPS4 1.0e-4
 #include "xfem_oracle_real.inc"
 #include "xfem_oracle_hex.inc"
+#include "xfem_oracle_t10.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -520,35 +582,53 @@ done:
 	return rc;
 }
 
-int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
-                     uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours) {
-	uint64_t* used = (uint64_t*)calloc(nv ? nv : 1, 8);
+/* Elements of `per` vertices coloured greedily in id order (each takes the
+ * smallest colour, of ORC_MAXCOL, that no earlier element sharing one of its
+ * vertices holds), then ordered inside a colour by (Morton code of the
+ * centroid of their vertices, id). */
+static int elem_schedule(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t nh, uint32_t per,
+                         uint32_t morton, uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin,
+                         uint32_t* ncolours) {
+	uint32_t* off = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* lst = (uint32_t*)malloc(4 * (size_t)(nh ? per * nh : 1));
+	uint32_t* mark = (uint32_t*)malloc(4 * (size_t)ORC_MAXCOL);
 	uint32_t* colour = (uint32_t*)malloc(4 * (size_t)(nh ? nh : 1));
 	orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nh ? nh : 1));
 	int rc = -1;
 	uint32_t ncol = 0;
 	float mn[3] = {INFINITY, INFINITY, INFINITY}, sc[3] = {0.0f, 0.0f, 0.0f};
-	if (!used || !colour || !kv) goto done;
-	/* greedy colouring in id order: hexes of one colour share no vertex */
+	if (!off || !lst || !mark || !colour || !kv) goto done;
+	for (size_t i = 0; i < (size_t)per * nh; i++) off[elems[i] + 1]++;
+	for (uint32_t v = 0; v < nv; v++) off[v + 1] += off[v];
+	{
+		uint32_t* fill = (uint32_t*)malloc(4 * ((size_t)nv + 1));
+		if (!fill) goto done;
+		memcpy(fill, off, 4 * (size_t)nv);
+		for (uint32_t h = 0; h < nh; h++)
+			for (uint32_t n = 0; n < per; n++) lst[fill[elems[per * (size_t)h + n]]++] = h;
+		free(fill);
+	}
+	for (uint32_t c = 0; c < ORC_MAXCOL; c++) mark[c] = 0xffffffffu;
 	for (uint32_t h = 0; h < nh; h++) {
-		uint64_t u = 0;
-		for (int n = 0; n < 8; n++) u |= used[hexes[8 * (size_t)h + n]];
-		if (u == ~0ull) goto done; /* more than 64 colours */
+		for (uint32_t n = 0; n < per; n++) {
+			const uint32_t v = elems[per * (size_t)h + n];
+			for (uint32_t i = off[v]; i < off[v + 1]; i++)
+				if (lst[i] < h) mark[colour[lst[i]]] = h;
+		}
 		uint32_t c = 0;
-		while ((u >> c) & 1u) c++;
+		while (c < ORC_MAXCOL && mark[c] == h) c++;
+		if (c == ORC_MAXCOL) goto done;
 		colour[h] = c;
 		if (c + 1 > ncol) ncol = c + 1;
-		for (int n = 0; n < 8; n++) used[hexes[8 * (size_t)h + n]] |= 1ull << c;
 	}
 	if (orc_vertex_ranks(nodes, nv, morton, vert_rank, mn, sc)) goto done;
-	/* inside a colour: (Morton code of the centroid of the 8 vertices, id) */
 	for (uint32_t h = 0; h < nh; h++) {
 		uint32_t key = h;
 		if (morton) {
 			float c[3] = {0.0f, 0.0f, 0.0f};
-			for (int n = 0; n < 8; n++)
-				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)hexes[8 * (size_t)h + n] + j];
-			for (int j = 0; j < 3; j++) c[j] = c[j] / 8.0f;
+			for (uint32_t n = 0; n < per; n++)
+				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)elems[per * (size_t)h + n] + j];
+			for (int j = 0; j < 3; j++) c[j] = c[j] / (float)per;
 			key = orc_quantise(c, mn, sc);
 		}
 		kv[h].key = ((uint64_t)colour[h] << 32) | key;
@@ -564,9 +644,94 @@ int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uin
 	*ncolours = ncol;
 	rc = 0;
 done:
-	free(used);
+	free(off);
+	free(lst);
+	free(mark);
 	free(colour);
 	free(kv);
+	return rc;
+}
+
+int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours) {
+	return elem_schedule(nodes, nv, hexes, nh, 8, morton, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int orc_t10_schedule(const float* nodes, uint32_t nv, const uint32_t* t10, uint32_t nt, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours) {
+	return elem_schedule(nodes, nv, t10, nt, 10, morton, vert_rank, order, colour_begin, ncolours);
+}
+
+int orc_tet_edges(const uint32_t* tets, uint32_t nt, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* t10) {
+	/* per lower vertex, its edge instances in stream order */
+	uint32_t* off = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* cnt = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* hi = (uint32_t*)malloc(4 * (size_t)(nt ? 6 * nt : 1));
+	uint32_t* lst = (uint32_t*)malloc(4 * (size_t)(nt ? 6 * nt : 1));
+	uint32_t* base = (uint32_t*)calloc((size_t)nv + 1, 4);
+	static const int te[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+	int rc = -1;
+	if (!off || !cnt || !hi || !lst || !base) goto done;
+	for (uint32_t t = 0; t < nt; t++)
+		for (int k = 0; k < 6; k++) {
+			const uint32_t a = tets[4 * (size_t)t + te[k][0]], b = tets[4 * (size_t)t + te[k][1]];
+			off[(a < b ? a : b) + 1]++;
+		}
+	for (uint32_t v = 0; v < nv; v++) off[v + 1] += off[v];
+	for (uint32_t t = 0; t < nt; t++)
+		for (int k = 0; k < 6; k++) {
+			const uint32_t a = tets[4 * (size_t)t + te[k][0]], b = tets[4 * (size_t)t + te[k][1]];
+			const uint32_t lo = a < b ? a : b, id = 6 * t + (uint32_t)k;
+			hi[id] = a < b ? b : a;
+			lst[off[lo] + cnt[lo]++] = id;
+		}
+	/* duplicates (same upper vertex) replaced by the list's last entry */
+	for (uint32_t v = 0; v < nv; v++) {
+		uint32_t* L = lst + off[v];
+		for (uint32_t j = 0; j < cnt[v]; j++)
+			for (uint32_t k = j + 1; k < cnt[v]; k++)
+				if (hi[L[j]] == hi[L[k]]) {
+					L[k] = L[cnt[v] - 1];
+					--cnt[v];
+					--k;
+				}
+	}
+	{
+		uint32_t ne = 0;
+		for (uint32_t v = 0; v < nv; v++) {
+			base[v] = ne;
+			for (uint32_t j = 0; j < cnt[v]; j++) {
+				edges[2 * (size_t)ne] = v;
+				edges[2 * (size_t)ne + 1] = hi[lst[off[v] + j]];
+				ne++;
+			}
+		}
+		*nedges = ne;
+	}
+	/* the T10 indices: corners, then nv + the edges (0,1) (0,2) (0,3) (1,2)
+	 * (1,3) (2,3) by EdgeFromVerts */
+	if (t10)
+		for (uint32_t t = 0; t < nt; t++) {
+			for (int c = 0; c < 4; c++) t10[10 * (size_t)t + c] = tets[4 * (size_t)t + c];
+			for (int k = 0; k < 6; k++) {
+				const uint32_t a = tets[4 * (size_t)t + te[k][0]], b = tets[4 * (size_t)t + te[k][1]];
+				const uint32_t lo = a < b ? a : b, h = a < b ? b : a;
+				uint32_t e = 0xffffffffu;
+				for (uint32_t j = 0; j < cnt[lo]; j++)
+					if (edges[2 * (size_t)(base[lo] + j) + 1] == h) {
+						e = base[lo] + j;
+						break;
+					}
+				t10[10 * (size_t)t + 4 + k] = nv + e;
+			}
+		}
+	rc = 0;
+done:
+	free(off);
+	free(cnt);
+	free(hi);
+	free(lst);
+	free(base);
 	return rc;
 }
 

@@ -164,6 +164,9 @@ int orc_parse_hexes(const uint32_t* idx, uint32_t idx_count, uint32_t* hexes,
                     uint32_t* hex_count, uint32_t* vert_count);
 /* The hex tables as built: n8[8][8] (point, node), g8[8][8][3], g1[8][3]. */
 void orc_hex_tables(float* n8, float* g8, float* g1);
+/* The quadratic-tet tables as built: g4[4][10][3] (point, node, axis),
+ * g10[10][10][3], w10[10]. */
+void orc_t10_tables(float* g4, float* g10, float* w10);
 /* GeoLinear3d::Init on a hex mesh (XPBDFEM/Geo.cpp:697-745, 736-740). */
 void orc_hex_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh,
                          float density, float* ep, float* w, uint8_t* vflags);
@@ -186,6 +189,45 @@ int orc_hex_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8
 /* CalculateVolume of a hex mesh (XPBDFEM/Geo.cpp:830, XPBDFEM/Fem.cpp:1046-1071). */
 float orc_hex_volume_f(const double* X, uint32_t nh, const uint32_t* hexes, const float* ep);
 double orc_hex_volume_d(const double* X, uint32_t nh, const uint32_t* hexes, const double* ep);
+
+/* ---- quadratic tetrahedra (oracle/xfem_oracle_t10.inc) -------------------- */
+/* T10 record, 56 values (ElementParamsQuadraticTet, XPBDFEM/Fem.h:61-68,
+ * flattened): Qi column-major [0..8], ic.QQ[9] [9..17], ic.QR[36] [18..53],
+ * volume [54], surfaceArea [55]. */
+#define ORC_EPQ 56
+/* The unique edges of a tet mesh as Connectivity3d::Init numbers them
+ * (XPBDFEM/Connectivity.cpp:387-548): each tet files its edges (0,1) (0,2)
+ * (0,3) (1,2) (1,3) (2,3) under their lower vertex in stream order; per
+ * vertex, a duplicate is replaced by the list's last entry; edges are
+ * numbered vertex by vertex. edges[2 e] = (lower, upper), capacity 12 nt.
+ * t10 (nullable, 10 per tet): GeoQuadratic3d's element indices
+ * (XPBDFEM/Geo.cpp:892-901): corners, then nv + EdgeFromVerts. */
+int orc_tet_edges(const uint32_t* tets, uint32_t nt, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* t10);
+/* GeoQuadratic3d::Init on a tet mesh: X (double, nv + ne vertices), rest
+ * state, inverse masses and flags of all vertices. */
+void orc_t10_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, const uint32_t* edges,
+                         uint32_t ne, const uint32_t* t10, float density, double* X, float* ep, float* w,
+                         uint8_t* vflags);
+void orc_t10_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, const uint32_t* edges,
+                         uint32_t ne, const uint32_t* t10, double density, double* X, double* ep, double* w,
+                         uint8_t* vflags);
+/* SolveElement on one T10 (X 10x3, O the substep start); -1 for 8-10. */
+int orc_solve_t10_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p);
+int orc_solve_t10_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p);
+/* Substeps of a T10 mesh in `order` (GeoQuadratic3d::Constrain and Damp's
+ * tet loops, XPBDFEM/Geo.cpp:973-1006). */
+int orc_t10_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                       const uint32_t* t10, const float* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+int orc_t10_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
+                       const uint32_t* t10, const double* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+float orc_t10_volume_f(const double* X, uint32_t nt, const uint32_t* t10, const float* ep);
+double orc_t10_volume_d(const double* X, uint32_t nt, const uint32_t* t10, const double* ep);
+/* The T10 schedule: as orc_hex_schedule over 10-vertex elements; nodes are
+ * all nv + ne vertex positions (float). */
+int orc_t10_schedule(const float* nodes, uint32_t nv, const uint32_t* t10, uint32_t nt, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours);
 
 /* CalculateVolume (XPBDFEM/Geo.cpp:827-832, XPBDFEM/Fem.cpp:1066). */
 float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets);
@@ -229,11 +271,11 @@ int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uin
 
 /* Hex schedule: hexes coloured greedily in id order so that the hexes of one
  * colour share no vertex (each takes the smallest colour not held by an
- * earlier hex sharing a vertex; at most 64), then ordered inside each colour
- * by (Morton code of the centroid of their 8 vertices, id), or by id with
- * morton == 0. Outputs vert_rank[nv] (as orc_schedule's), hex_order[nh]
- * (colour-major) and colour_begin[ncolours + 1] (caller allocates 65).
- * Returns 0, or -1 if more than 64 colours are needed. */
+ * earlier hex sharing a vertex; at most 4096), then ordered inside each
+ * colour by (Morton code of the centroid of their 8 vertices, id), or by id
+ * with morton == 0. Outputs vert_rank[nv] (as orc_schedule's), hex_order[nh]
+ * (colour-major) and colour_begin[ncolours + 1] (caller allocates nh + 1).
+ * Returns 0, or -1 if more than 4096 colours are needed. */
 int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
                      uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours);
 

@@ -210,6 +210,33 @@ CASES = [
     ("hdamped_c1_cube_neo_incompressible_amortized_pbd", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 11, 1,
                                                           C1_COMPLIANCE, 0.5, 0.0, -9.81, DT, 40, 1, 0.01, 0.03,
                                                           0.002, 3, 0.1, 1]),
+    # quadratic tets (GeoQuadratic3d on a GenerateTetBlock mesh; element
+    # type T10 in the settings' flags): the `q` commands take the pattern
+    # after the scale; the substep cases run in the GPU's T10 colour order
+    ("qinit_3x2x2", ["qinit", 3, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0]),
+    ("qinit_3x2x2_mirror_wonky", ["qinit", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3, 1000.0]),
+    ("qsolve_nh_sim_nu045", ["qsolve", 61, 32, 4, 1, 0.01, 0.45, DT]),
+    ("qsolve_nh_sim_incompressible", ["qsolve", 62, 32, 4, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("qsolve_nh_serial_nu045", ["qsolve", 63, 32, 4, 0, 0.01, 0.45, DT]),
+    ("qsolve_yeohfast_sim_nu049", ["qsolve", 64, 32, 7, 1, 0.5, 0.49, DT]),
+    ("qsolve_mixed_sim_nu045", ["qsolve", 65, 32, 3, 1, 0.01, 0.45, DT]),
+    ("qsolve_yeohskinsel_serial_nu045", ["qsolve", 66, 32, 6, 0, 0.5, 0.45, DT]),
+    ("qsolve_pixar_nu045", ["qsolve", 67, 32, 0, 1, 0.01, 0.45, DT]),
+    ("qsolve_pixarsel_nu049", ["qsolve", 68, 32, 2, 1, 0.01, 0.49, DT]),
+    ("qordered_c1_nh_nu045", ["qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                              0.0, -9.81, DT, 40, 1]),
+    ("qordered_c1_nh_incompressible", ["qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, C1_COMPLIANCE, 0.5,
+                                       0.0, -9.81, DT, 40, 1]),
+    ("qordered_wonky_yeohfast_serial_nu049", ["qordered", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 7, 0, 3.2e-4,
+                                              0.49, -2.0, -9.81, DT, 10, 1]),
+    ("qordered_c1_mixed_nu045", ["qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 3, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                 0.0, -9.81, DT, 40, 1]),
+    ("qdamped_c1_nh_nu045_amortized_pbd", ["qdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5,
+                                           0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("qdamped_c1_pixar_nu045_limit", ["qdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5,
+                                      0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("qvolume_wonky_nh_serial_1_post", ["qdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                        -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
     ("hvolume_wonky_pixar_1_post_pbd", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
 ]
@@ -255,6 +282,15 @@ def main():
             order = sch["hex_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
+        if args[0] in ("qordered", "qdamped"):
+            import oracle  # noqa: E402
+            W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]
+            nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), pattern, wonk)
+            q = oracle.Quadratic(nodes, idx, dens)
+            sch = q.schedule(morton=1)
+            order = sch["tet_order"].astype(np.uint32)
+            stdin = struct.pack("<I", order.size) + order.tobytes()
+            extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
         if args[0] in ("ordered", "damped", "rings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]

@@ -361,3 +361,95 @@ def test_hex_continuous_models_refused(orc):
         p = orc.make_params(dt=1e-3, compliance=1e-3, poisson=0.45, energy=e)
         with pytest.raises(ValueError):
             orc.hex_substeps(X, np.zeros_like(X), w, hexes, ep, np.arange(2, dtype=np.uint32), 1, p)
+
+
+# ---- quadratic tetrahedra (GeoQuadratic3d; oracle/xfem_oracle_t10.inc) ----
+QINIT = ["qinit_3x2x2", "qinit_3x2x2_mirror_wonky"]
+QSOLVE = ["qsolve_nh_sim_nu045", "qsolve_nh_sim_incompressible", "qsolve_nh_serial_nu045",
+          "qsolve_yeohfast_sim_nu049", "qsolve_mixed_sim_nu045", "qsolve_yeohskinsel_serial_nu045",
+          "qsolve_pixar_nu045", "qsolve_pixarsel_nu049"]
+QSUBSTEP = ["qordered_c1_nh_nu045", "qordered_c1_nh_incompressible", "qordered_wonky_yeohfast_serial_nu049",
+            "qordered_c1_mixed_nu045", "qdamped_c1_nh_nu045_amortized_pbd", "qdamped_c1_pixar_nu045_limit",
+            "qvolume_wonky_nh_serial_1_post"]
+
+
+def test_t10_tables_structure(orc):
+    """The quadratic-tet tables built from the reference's printed
+    magnitudes: gradients sum to ~0 at every point (the shape functions are a
+    partition of unity) and the weights to 1."""
+    g4, g10, w10 = orc.t10_tables()
+    assert np.allclose(g4.sum(1), 0.0, atol=5e-6)
+    assert np.allclose(g10.sum(1), 0.0, atol=5e-6)
+    assert abs(float(w10.sum()) - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("name", QINIT)
+def test_t10_rest_state_bit_exact(orc, name):
+    """GeoQuadratic3d::Init: Connectivity3d's edge numbering (the midpoint
+    vertex ids), midpoint positions, flags of all vertices, T10 records,
+    masses, the MINSTD order and CalculateVolume."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.Quadratic(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(q.t10.reshape(-1), g["t10_idx"])
+    assert np.array_equal(q.X0.reshape(-1).view(np.uint64), g["x0"].view(np.uint64))
+    assert np.array_equal(q.ep.reshape(-1).view(np.uint32), g["qep"].view(np.uint32))
+    assert np.array_equal(q.w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(q.flags, g["vflags"])
+    assert np.array_equal(orc.minstd_order(q.t10.shape[0]), g["torder"])
+    assert np.float32(q.volume(q.X0)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+@pytest.mark.parametrize("name", QSOLVE)
+def test_t10_element_solve_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    p = orc.make_params(dt=a[7], compliance=a[5], poisson=a[6], energy=a[3], simultaneous=bool(a[4]))
+    n = a[2]
+    xin, xout = g["xin"].reshape(n, 10, 3), g["xout"].reshape(n, 10, 3)
+    ep, w, rest = g["qep"].reshape(n, orc.T10_EP), g["w"].reshape(n, 10), g["rest"].reshape(n, 10, 3)
+    for t in range(n):
+        x = orc.solve_t10(xin[t], w[t], ep[t], p, O=rest[t])
+        assert np.array_equal(x.view(np.uint64), xout[t].view(np.uint64)), t
+
+
+def q_params(orc, a, g, tick):
+    """orc_params of a `qordered` / `qdamped` fixture."""
+    energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[10:19]
+    kw = dict(rayleigh_type=2)
+    if a[0] == "qdamped":
+        damping, pbd, drag, rtype, spacing = a[19:24]
+        d = g["derived"]
+        kw = dict(damping=damping, rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(d[0]),
+                  pbd_coeff_amortized=float(d[1]), drag=float(d[2]), volume_passes=a[24] if len(a) > 24 else 0)
+    return orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
+                           gravity=(gx, gy, 0.0), lock=bool(lock), tick=tick, **kw)
+
+
+@pytest.mark.parametrize("name", QSUBSTEP)
+def test_t10_substeps_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.Quadratic(g["nodes"], g["idx"], a[9])
+    sch = q.schedule()
+    assert np.array_equal(sch["tet_order"], g["order"])
+    assert np.array_equal(sch["colour_tet_begin"], g["colour_tet_begin"])
+    lm = (q.flags & 1).astype(np.uint8)
+    X1, V1, w1, _ = q.substeps(q.X0, np.zeros_like(q.X0), q.w, g["order"], 1, q_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = q.substeps(X1, V1, w1, g["order"], a[17] - 1, q_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+def test_t10_schedule_is_a_valid_colouring(orc):
+    nodes, idx = orc.gen_tet_block(4, 3, 2, (0.1, 0.1, 0.1), 1, 0.3)
+    q = orc.Quadratic(nodes, idx, 1000.0)
+    s = q.schedule()
+    cb, order = s["colour_tet_begin"], s["tet_order"]
+    assert sorted(order.tolist()) == list(range(q.t10.shape[0]))
+    for c in range(s["colours"]):
+        verts = q.t10[order[cb[c]:cb[c + 1]]].reshape(-1)
+        assert np.unique(verts).size == verts.size
