@@ -35,6 +35,16 @@
  * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), every energy model but the
  * continuous-pressure ones (8-10). A mesh holds tets or hexes, not both, and
  * so does a handle.
+ *
+ * A tet mesh whose settings ask for quadratic elements (element type
+ * XFEM_ELEMENT_T10 in flags bits 0-3) runs as GeoQuadratic3d
+ * (XPBDFEM/Geo.cpp:836-1053, picked by Sim::AddBlock, XPBDFEM/Demo.cpp:145-150):
+ * one node added on every edge (Connectivity3d's edge numbering), T10
+ * elements (ElementParamsQuadraticTet, SolveElement with Nodes = 10 on the
+ * 4-point rule) and the same energy models as hexes. The body's vertices are
+ * then the mesh's own followed by the edge nodes, and every per-vertex call
+ * (positions, velocities, lock mask) covers all of them. A handle holds
+ * linear tets, hexes or T10s.
  */
 #ifndef XFEM_H
 #define XFEM_H
@@ -56,6 +66,11 @@ extern "C" {
 #define XFEM_ELIMIT (-6)          /* a schedule limit was exceeded (colours, cluster size) */
 
 /* ---- flags: the reference's Settings::flags layout (XPBDFEM/Settings.h:9-29) - */
+#define XFEM_ELEMENT_TYPE_MASK 15u      /* Settings_ElementTypeMask, bits 0-3 (XPBDFEM/Settings.h:9-10, 31-39): */
+#define XFEM_ELEMENT_T4 5u              /*   Element_T4: linear tets (as 0) */
+#define XFEM_ELEMENT_T10 6u             /*   Element_T10: a tet mesh runs as quadratic tets */
+#define XFEM_ELEMENT_H8 7u              /*   Element_H8: linear hexes (as 0) */
+#define XFEM_ELEMENT_H27 8u             /*   Element_H27: quadratic; on a tet mesh as T10, on hexes not built */
 #define XFEM_ENERGY_BIT 6u
 #define XFEM_ENERGY_MASK 31u
 /* Energy ids (XPBDFEM/Settings.h:41-53) as SolveElement dispatches them on a
@@ -168,7 +183,9 @@ int xfem_settings_default(xfem_settings* s);
  * lumped masses and inverse masses — then builds the colour schedule and
  * uploads everything. A mesh of hexes (tag 8) gets the hex rest state
  * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
- * a mesh mixing tets and hexes, or a hex mesh with the continuous-pressure
+ * element type T10 (flags bits 0-3) on a tet mesh makes it a T10 body
+ * (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941); a mesh mixing tets and
+ * hexes, quadratic hexes, or hexes or T10s with the continuous-pressure
  * models (energy 8-10), returns XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
@@ -308,7 +325,7 @@ int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count,
                                uint32_t* colour_begin, uint32_t* ncolours);
 
 /* ---- linear hexahedra (hex mode) --------------------------------------------- */
-/* Hexes of one body (0 for a tet body). */
+/* Elements of one body: its hexes, or its T10s for a T10 body (0 for a tet body). */
 int xfem_body_hex_count(const xfem_body* b, uint32_t body, uint32_t* nhexes);
 /* Rest state per hex (caller order) as 120 floats, ElementParamsLinearHex
  * (XPBDFEM/Fem.h:90-100) flattened: qcLo.Ji[0] column-major [0..8],
@@ -318,7 +335,7 @@ int xfem_body_hex_count(const xfem_body* b, uint32_t body, uint32_t* nhexes);
 int xfem_get_hex_rest_state(const xfem_body* b, uint32_t body, float* out_ep120, float* out_w);
 /* The hex schedule: device rank of each vertex, the hex order (colour-major;
  * the hexes of one colour share no vertex) and the colour offsets in it
- * (ncolours + 1 entries, at most 65). */
+ * (ncolours + 1 entries, at most 4097). */
 int xfem_get_hex_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_rank, uint32_t* hex_order,
                           uint32_t* colour_begin, uint32_t* ncolours);
 /* The same two, computed on the host without a handle or a GPU. */
@@ -332,6 +349,36 @@ int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, 
  * idx[9 W H D] (tag 8 and 8 vertex ids per hex). */
 int xfem_generate_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
                             uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
+
+/* ---- quadratic tets (T10 mode) ----------------------------------------------- */
+/* T10s and edge nodes of one body; XFEM_EUNSUPPORTED for another body. */
+int xfem_body_t10_count(const xfem_body* b, uint32_t body, uint32_t* nt10, uint32_t* nedges);
+/* Rest state per T10 (caller tet order) as 56 floats, ElementParamsQuadraticTet
+ * (XPBDFEM/Fem.h:61-69) flattened: Qi column-major [0..8], ic.QQ[9] [9..17],
+ * ic.QR[36] [18..53], volume [54], surfaceArea [55]; the rest inverse masses
+ * of all vertices; the 10 indices of each T10 (corners, then the edge nodes
+ * of the local edges 01 02 03 12 13 23, XPBDFEM/Geo.cpp:893-901); the two
+ * corners of each edge node. Any output may be NULL. */
+int xfem_get_t10_rest_state(const xfem_body* b, uint32_t body, float* out_ep56, float* out_w, uint32_t* out_t10,
+                            uint32_t* out_edges);
+/* The T10 schedule: device rank of each vertex, the T10 order (colour-major;
+ * the T10s of one colour share no vertex) and the colour offsets in it. */
+int xfem_get_t10_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_rank, uint32_t* t10_order,
+                          uint32_t* colour_begin, uint32_t* ncolours);
+/* Connectivity3d's edges of a tet index stream (XPBDFEM/Connectivity.cpp:
+ * 371-393, 478-497) and the T10 indices: out_edges[2 per edge] (at most 6 per
+ * tet), out_t10[10 per tet], *out_nedges. Outputs may be NULL (count first). */
+int xfem_compute_t10_edges(const uint32_t* idx_data, uint32_t idx_data_count, uint32_t* out_edges,
+                           uint32_t* out_t10, uint32_t* out_nedges);
+/* GeoQuadratic3d::Init's rest state on the host: out_x the double rest
+ * positions of all vertices (3 each: corners, then edge midpoints), the
+ * 56-float records, inverse masses and vertex flags; and its schedule. */
+int xfem_compute_t10_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, double* out_x, float* out_ep56,
+                                float* out_w, uint8_t* out_flags);
+int xfem_compute_t10_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* t10_order,
+                              uint32_t* colour_begin, uint32_t* ncolours);
 
 /* ---- helpers --------------------------------------------------------------- */
 /* volumeAndTimeCorrectedPbdDamping and its amortized form for a substep of

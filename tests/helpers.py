@@ -59,3 +59,22 @@ class HexOracleRun:
         self.X, self.V, self.w, _ = oracle.hex_substeps(self.X, self.V, self.w, self.hexes, self.ep, self.order, n, p,
                                                         lock_mask=self.lock, dtype=self.dtype)
         return self
+
+
+class T10OracleRun:
+    """The oracle's state for one tet mesh read as T10s (GeoQuadratic3d),
+    stepped in the body's T10 order."""
+
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+        self.q = oracle.Quadratic(nodes, idx, density, dtype)
+        self.lock = (self.q.flags & 1).astype(np.uint8)
+        self.X = self.q.X0.copy()
+        self.V = np.zeros_like(self.X)
+        self.w = self.q.w.copy()
+        self.s = settings
+        self.order = order
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt)
+        self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
+        return self

@@ -249,3 +249,53 @@ def test_hex_mesh_errors():
     with pytest.raises(xfem.XfemError) as e:
         xfem.compute_hex_rest_state(nodes, idx[:-1], 1000.0)
     assert e.value.code == xfem.EINVAL
+
+
+# ---- quadratic tets (GeoQuadratic3d on a tet mesh) ----
+@pytest.mark.parametrize("name", ["qinit_3x2x2", "qinit_3x2x2_mirror_wonky"])
+def test_t10_rest_state_bit_exact_vs_reference(name):
+    """GeoQuadratic3d::Init (XPBDFEM/Geo.cpp:836-941): Connectivity3d's edge
+    numbering (the T10 indices), the double midpoint positions, the T10
+    records (InitTriTetFiniteElement on ElementParamsQuadraticTet), the
+    inverse masses (LumpsTet10) and the flags of every vertex."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    edges, t10 = xfem.compute_t10_edges(g["idx"])
+    assert np.array_equal(t10.reshape(-1), g["t10_idx"])
+    x, ep, w, fl = xfem.compute_t10_rest_state(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(x.reshape(-1).view(np.uint64), g["x0"].view(np.uint64))
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["qep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_t10_host_matches_oracle_on_jittered_meshes(orc, seed):
+    """Edges, rest state and schedule against the oracle on jittered blocks."""
+    rng = np.random.default_rng(seed)
+    nodes, idx = xfem.generate_tet_block(5, 3, 3, (0.03, 0.05, 0.04), seed % 2, 0.3)
+    nodes = (nodes + rng.normal(0, 0.002, nodes.shape)).astype(np.float32)
+    q = orc.Quadratic(nodes, idx, 700.0)
+    edges, t10 = xfem.compute_t10_edges(idx)
+    assert np.array_equal(edges, q.edges) and np.array_equal(t10, q.t10)
+    x, ep, w, fl = xfem.compute_t10_rest_state(nodes, idx, 700.0)
+    assert np.array_equal(x.view(np.uint64), q.X0.view(np.uint64))
+    assert np.array_equal(ep.view(np.uint32), q.ep.view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), q.w.view(np.uint32))
+    assert np.array_equal(fl, q.flags)
+    for morton in (True, False):
+        s = xfem.compute_t10_schedule(nodes, idx, morton=morton)
+        o = q.schedule(morton=1 if morton else 0)
+        assert np.array_equal(s["vert_rank"], o["vert_rank"])
+        assert np.array_equal(s["t10_order"], o["tet_order"])
+        assert np.array_equal(s["colour_t10_begin"], o["colour_tet_begin"])
+
+
+@pytest.mark.parametrize("name", ["qordered_c1_nh_nu045", "qvolume_wonky_nh_serial_1_post"])
+def test_t10_schedule_is_the_fixture_order(name):
+    """The product's T10 colouring is the order the reference fixtures ran in."""
+    g = golden(name)
+    s = xfem.compute_t10_schedule(g["nodes"], g["idx"])
+    assert np.array_equal(s["t10_order"], g["order"])
+    assert np.array_equal(s["colour_t10_begin"], g["colour_tet_begin"])
+

@@ -35,6 +35,11 @@ int fail(int code, const std::string& msg) {
 		if (e_ != cudaSuccess) return fail(XFEM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
 	} while (0)
 
+// Element kinds of a body: linear tets (the chunked tet path, the one-ring
+// mode), linear hexahedra (H8) and quadratic tets (T10), the last two in the
+// element kernel.
+constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2;
+
 struct BodyHost {
 	uint32_t nv = 0, nt = 0, vbase = 0, tbase = 0;
 	std::vector<float> nodes;         // rest positions, caller order
@@ -48,12 +53,14 @@ struct BodyHost {
 	RingSchedule rings;               // continuous-pressure models only
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
-	// hex bodies (linear hexahedra; no tets)
-	bool hex = false;
-	uint32_t nh = 0;
-	std::vector<uint32_t> hexes;      // 8 per hex, caller order
-	std::vector<float> hep;           // rest::kHexRec per hex
-	HexSchedule hsched;
+	// element bodies (linear hexahedra or quadratic tets; no linear tets)
+	uint32_t el = 0;                  // kElTets, kElHexes, kElT10
+	uint32_t nh = 0;                  // elements
+	uint32_t ncorner = 0;             // T10: the mesh's own vertices; the nv - ncorner edge nodes follow
+	std::vector<uint32_t> elems;      // 8 per hex or 10 per T10, caller order
+	std::vector<uint32_t> edges;      // T10: the two corners of each edge node
+	std::vector<float> eep;           // rest::kHexRec per hex or rest::kT10Rec per T10
+	ElemSchedule esched;
 };
 
 template <typename T>
@@ -123,11 +130,12 @@ struct xfem_body {
 	DevBuf<float4> ring_ent;
 	DevBuf<uint2> pbd_cl;
 	DevBuf<uint4> pbd_ent;
-	// hex mode (linear hexahedra)
-	bool hex_mode = false;
-	DevBuf<uint4> hex_vid;
-	DevBuf<float4> hex_rec;
-	DevBuf<uint32_t> hex_cb, hex_flat;
+	// element mode (kElHexes or kElT10; kElTets: the tet path)
+	uint32_t el_mode = kElTets;
+	DevBuf<uint4> el_vid;
+	DevBuf<float4> el_rec;
+	DevBuf<uint32_t> el_cb, el_flat;
+	DevBuf<float> el_g4;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -319,9 +327,10 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 		i += tag + 1;
 	}
 	if (ntag[0] && ntag[1]) return fail(XFEM_EUNSUPPORTED, "meshes mixing tets (tag 4) and hexes (tag 8) are not supported");
-	b.hex = ntag[1] > 0;
+	b.el = ntag[1] > 0 ? kElHexes : kElTets;
 	uint32_t nv = 0;
-	if (b.hex ? parse_hexes(m.idx_data, m.idx_data_count, b.hexes, nv) : parse_tets(m.idx_data, m.idx_data_count, b.tets, nv))
+	if (b.el == kElHexes ? parse_hexes(m.idx_data, m.idx_data_count, b.elems, nv)
+	                     : parse_tets(m.idx_data, m.idx_data_count, b.tets, nv))
 		return fail(XFEM_EINVAL, "truncated index stream");
 	// GeoLinear3d::Init asserts vertCount == nodeDataCount / 3 (XPBDFEM/Geo.cpp:700)
 	if (nv != m.node_data_count / 3)
@@ -330,7 +339,7 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	if (!(m.density > 0.0f)) return fail(XFEM_EINVAL, "density must be > 0");
 	b.nv = nv;
 	b.nt = (uint32_t)(b.tets.size() / 4);
-	b.nh = (uint32_t)(b.hexes.size() / 8);
+	b.nh = (uint32_t)(b.elems.size() / 8);
 	b.nodes.assign(m.node_data, m.node_data + m.node_data_count);
 	return XFEM_OK;
 }
@@ -340,12 +349,46 @@ void host_rest(const xfem_mesh& m, BodyHost& b) {
 	b.ep.resize(17 * (size_t)b.nt);
 	b.w0.resize(b.nv);
 	b.vflags.resize(b.nv);
-	if (b.hex) {
-		b.hep.resize((size_t)rest::kHexRec * b.nh);
-		hex_init_rest(b.nodes.data(), b.nv, b.hexes.data(), b.nh, m.density, b.hep.data(), b.w0.data(), b.vflags.data());
+	if (b.el == kElHexes) {
+		b.eep.resize((size_t)rest::kHexRec * b.nh);
+		hex_init_rest(b.nodes.data(), b.nv, b.elems.data(), b.nh, m.density, b.eep.data(), b.w0.data(), b.vflags.data());
 		return;
 	}
 	init_rest(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
+}
+
+// GeoQuadratic3d::Init on a tet mesh (XPBDFEM/Geo.cpp:836-941): the edge
+// nodes at the edges' midpoints and the T10 rest state. The body's vertices
+// become the corners followed by the edge nodes (their rest positions
+// rounded to float; the rest state is built from the double positions, as
+// the reference does). X: the double positions out (3 per vertex), or null.
+void prepare_t10(const xfem_mesh& m, BodyHost& b, std::vector<double>* X = nullptr) {
+	std::vector<uint32_t> t10;
+	tet_edges(b.tets.data(), b.nt, b.nv, b.edges, t10);
+	const uint32_t ne = (uint32_t)(b.edges.size() / 2), n = b.nv + ne;
+	std::vector<double> x(3 * (size_t)n);
+	b.eep.resize((size_t)rest::kT10Rec * b.nt);
+	b.w0.resize(n);
+	b.vflags.resize(n);
+	t10_init_rest(b.nodes.data(), b.nv, b.nt, b.edges.data(), ne, t10.data(), m.density, x.data(), b.eep.data(),
+	              b.w0.data(), b.vflags.data());
+	b.nodes.resize(3 * (size_t)n);
+	for (size_t i = 0; i < 3 * (size_t)n; i++) b.nodes[i] = (float)x[i];
+	b.el = kElT10;
+	b.ncorner = b.nv;
+	b.nv = n;
+	b.nh = b.nt;
+	b.elems = std::move(t10);
+	b.tets.clear();
+	b.nt = 0;
+	if (X) *X = std::move(x);
+}
+
+// Whether the settings ask for quadratic elements (GeoQuadratic3d: element
+// type T10 or H27 in flags bits 0-3, XPBDFEM/Demo.cpp:145-150).
+bool quadratic_type(uint32_t flags) {
+	const uint32_t t = flags & XFEM_ELEMENT_TYPE_MASK;
+	return t == XFEM_ELEMENT_T10 || t == XFEM_ELEMENT_H27;
 }
 
 // Rest state and schedule of one body: on the host (gpu false), or with the
@@ -365,15 +408,21 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	if (rc) return rc;
 	const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	const bool ring = model_of(energy) == kModelRing;
-	if (b.hex) {
-		// linear hexahedra: set-up on the host (rest state, Morton vertex
-		// ranks, the hex colouring)
+	const bool quad = quadratic_type(b.settings.flags);
+	if (quad && b.el == kElHexes) return fail(XFEM_EUNSUPPORTED, "quadratic hexahedra (H27) are not built");
+	if (b.el == kElHexes || quad) {
+		// hexes and T10s: set-up on the host (rest state, Morton vertex
+		// ranks, the element colouring)
 		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
-			return fail(XFEM_EUNSUPPORTED, "hex meshes run every energy model but the continuous-pressure ones (8-10)");
-		host_rest(m, b);
+			return fail(XFEM_EUNSUPPORTED,
+			            "hex and T10 meshes run every energy model but the continuous-pressure ones (8-10)");
+		if (quad)
+			prepare_t10(m, b);
+		else
+			host_rest(m, b);
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
-		if (hex_schedule(b.nodes.data(), b.nv, b.hexes.data(), b.nh, morton, b.hsched))
-			return fail(XFEM_ELIMIT, "the hex colouring needs more than 64 colours");
+		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, quad ? 10u : 8u, morton, b.esched))
+			return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
 		return XFEM_OK;
 	}
 	std::vector<uint32_t> off, lst;
@@ -586,64 +635,84 @@ int build_rings(xfem_body* h) {
 	return XFEM_OK;
 }
 
-// The hexes of every body in device order (colour-major, bodies in order
-// inside a colour): vertex ids, records (structure of arrays of 30 float4:
-// the centre's inverse jacobian and weight, volume, surface area, QQ, QR,
-// then the 2x2x2 points' inverse jacobians and weights) and each hex's index
-// in its body's hex order.
-int build_hexes(xfem_body* h) {
-	uint32_t ncol = 0, nhex = 0;
+// The elements of every body in device order (colour-major, bodies in
+// order inside a colour): vertex ids (hex: two uint4; T10: three, the last
+// two words zero), records as a structure of arrays (hex 30 float4: the
+// centre's inverse jacobian and weight, volume, surface area, QQ, QR, then
+// the 2x2x2 points' inverse jacobians and weights; T10 14 float4: Qi,
+// volume, surface area, QQ, QR), each element's index in its body's order,
+// and for T10s the shape-function gradients at the 4-point rule.
+int build_elements(xfem_body* h) {
+	const bool t10 = h->el_mode == kElT10;
+	const uint32_t per = t10 ? 10u : 8u, nvid4 = t10 ? 3u : 2u, nrec4 = t10 ? 14u : 30u;
+	const size_t rsz = t10 ? rest::kT10Rec : rest::kHexRec;
+	uint32_t ncol = 0, nel = 0;
 	for (const BodyHost& b : h->bodies) {
-		ncol = std::max(ncol, b.hsched.ncolours);
-		nhex += b.nh;
+		ncol = std::max(ncol, b.esched.ncolours);
+		nel += b.nh;
 	}
-	std::vector<uint4> vid(2 * (size_t)nhex);
-	std::vector<uint32_t> cb(ncol + 1, 0), flat(nhex);
-	std::vector<float4> rec(30 * (size_t)nhex);
+	std::vector<uint4> vid(nvid4 * (size_t)nel);
+	std::vector<uint32_t> cb(ncol + 1, 0), flat(nel);
+	std::vector<float4> rec(nrec4 * (size_t)nel);
 	uint32_t o = 0;
 	for (uint32_t c = 0; c < ncol; c++) {
 		cb[c] = o;
 		for (const BodyHost& b : h->bodies) {
-			const HexSchedule& hs = b.hsched;
-			if (c >= hs.ncolours) continue;
-			for (uint32_t k = hs.colour_begin[c]; k < hs.colour_begin[c + 1]; k++, o++) {
-				const uint32_t hx = hs.order[k];
-				uint32_t d[8];
-				for (int n = 0; n < 8; n++) d[n] = b.vbase + b.sched.vert_rank[b.hexes[8 * (size_t)hx + n]];
-				vid[2 * (size_t)o] = make_uint4(d[0], d[1], d[2], d[3]);
-				vid[2 * (size_t)o + 1] = make_uint4(d[4], d[5], d[6], d[7]);
+			const ElemSchedule& es = b.esched;
+			if (c >= es.ncolours) continue;
+			for (uint32_t k = es.colour_begin[c]; k < es.colour_begin[c + 1]; k++, o++) {
+				const uint32_t el = es.order[k];
+				uint32_t d[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+				for (uint32_t n = 0; n < per; n++) d[n] = b.vbase + b.sched.vert_rank[b.elems[per * (size_t)el + n]];
+				for (uint32_t j = 0; j < nvid4; j++)
+					vid[nvid4 * (size_t)o + j] = make_uint4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
 				flat[o] = k;
-				const float* e = &b.hep[(size_t)rest::kHexRec * hx];
+				const float* e = &b.eep[rsz * el];
 				float r[120];
-				for (int j = 0; j < 9; j++) r[j] = e[rest::kHexJL + j];
-				r[9] = e[rest::kHexWL];
-				r[10] = e[rest::kHexVol];
-				r[11] = e[rest::kHexArea];
-				for (int j = 0; j < 7; j++) r[12 + j] = e[rest::kHexQQ + j];
-				for (int j = 0; j < 21; j++) r[19 + j] = e[rest::kHexQR + j];
-				for (int j = 0; j < 72; j++) r[40 + j] = e[rest::kHexJH + j];
-				for (int j = 0; j < 8; j++) r[112 + j] = e[rest::kHexWH + j];
-				for (int k4 = 0; k4 < 30; k4++)
-					rec[(size_t)k4 * nhex + o] = make_float4(r[4 * k4], r[4 * k4 + 1], r[4 * k4 + 2], r[4 * k4 + 3]);
+				if (t10) {
+					for (int j = 0; j < 9; j++) r[j] = e[rest::kT10Qi + j];
+					r[9] = e[rest::kT10Vol];
+					r[10] = e[rest::kT10Area];
+					for (int j = 0; j < 9; j++) r[11 + j] = e[rest::kT10QQ + j];
+					for (int j = 0; j < 36; j++) r[20 + j] = e[rest::kT10QR + j];
+				} else {
+					for (int j = 0; j < 9; j++) r[j] = e[rest::kHexJL + j];
+					r[9] = e[rest::kHexWL];
+					r[10] = e[rest::kHexVol];
+					r[11] = e[rest::kHexArea];
+					for (int j = 0; j < 7; j++) r[12 + j] = e[rest::kHexQQ + j];
+					for (int j = 0; j < 21; j++) r[19 + j] = e[rest::kHexQR + j];
+					for (int j = 0; j < 72; j++) r[40 + j] = e[rest::kHexJH + j];
+					for (int j = 0; j < 8; j++) r[112 + j] = e[rest::kHexWH + j];
+				}
+				for (uint32_t k4 = 0; k4 < nrec4; k4++)
+					rec[(size_t)k4 * nel + o] = make_float4(r[4 * k4], r[4 * k4 + 1], r[4 * k4 + 2], r[4 * k4 + 3]);
 			}
 		}
 	}
 	cb[ncol] = o;
-	XCUDA(h->hex_vid.alloc(vid.size()));
-	XCUDA(h->hex_rec.alloc(rec.size()));
-	XCUDA(h->hex_cb.alloc(cb.size()));
-	XCUDA(h->hex_flat.alloc(flat.size()));
+	std::vector<float> g4(t10 ? 120 : 1, 0.0f);
+	if (t10)
+		for (int p = 0; p < 4; p++)
+			for (int n = 0; n < 10; n++)
+				for (int k = 0; k < 3; k++) g4[(p * 10 + n) * 3 + k] = rest::t10_grad(4, p, n, k);
+	XCUDA(h->el_vid.alloc(vid.size()));
+	XCUDA(h->el_rec.alloc(rec.size()));
+	XCUDA(h->el_cb.alloc(cb.size()));
+	XCUDA(h->el_flat.alloc(flat.size()));
+	XCUDA(h->el_g4.alloc(g4.size()));
 	auto up = [&](void* dst, const void* src, size_t bytes) {
 		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
 	};
-	XCUDA(up(h->hex_vid.p, vid.data(), vid.size() * sizeof(uint4)));
-	XCUDA(up(h->hex_rec.p, rec.data(), rec.size() * sizeof(float4)));
-	XCUDA(up(h->hex_cb.p, cb.data(), cb.size() * 4));
-	XCUDA(up(h->hex_flat.p, flat.data(), flat.size() * 4));
+	XCUDA(up(h->el_vid.p, vid.data(), vid.size() * sizeof(uint4)));
+	XCUDA(up(h->el_rec.p, rec.data(), rec.size() * sizeof(float4)));
+	XCUDA(up(h->el_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(h->el_flat.p, flat.data(), flat.size() * 4));
+	XCUDA(up(h->el_g4.p, g4.data(), g4.size() * 4));
 	XCUDA(cudaStreamSynchronize(h->stream));
-	h->ctx.hex_colours = ncol;
-	h->ctx.nhex = nhex;
-	h->device_bytes += vid.size() * 16 + rec.size() * 16 + cb.size() * 4 + flat.size() * 4;
+	h->ctx.el_colours = ncol;
+	h->ctx.nel = nel;
+	h->device_bytes += vid.size() * 16 + rec.size() * 16 + cb.size() * 4 + flat.size() * 4 + g4.size() * 4;
 	return XFEM_OK;
 }
 
@@ -864,7 +933,7 @@ int build_device(xfem_body* h) {
 		for (size_t i = 0; i < 4 * (size_t)b.nt; i++) tets_dev[tbase + i] = b.vbase + b.sched.vert_rank[b.tets[i]];
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
-		params[bi].ntets = b.hex ? b.nh : b.nt;
+		params[bi].ntets = b.el ? b.nh : b.nt;
 		params[bi].nverts = b.nv;
 	}
 	clk.lap("vertex state");
@@ -960,8 +1029,8 @@ int build_device(xfem_body* h) {
 		int rr = build_rings(h);
 		if (rr) return rr;
 	}
-	if (h->hex_mode) {
-		int rr = build_hexes(h);
+	if (h->el_mode) {
+		int rr = build_elements(h);
 		if (rr) return rr;
 	}
 	DevCtx& c = h->ctx;
@@ -1013,10 +1082,11 @@ int build_device(xfem_body* h) {
 	c.pbd_ent = h->pbd_ent.p;
 	c.tet_verts = h->tets_dev.p;
 	if (h->ring_mode) c.ext = ring_damp_of(h->bodies) ? 1u : 0u;
-	c.hex_vid = h->hex_vid.p;
-	c.hex_rec = h->hex_rec.p;
-	c.colour_hex_begin = h->hex_cb.p;
-	c.hex_flat = h->hex_flat.p;
+	c.el_vid = h->el_vid.p;
+	c.el_rec = h->el_rec.p;
+	c.colour_el_begin = h->el_cb.p;
+	c.el_g4 = h->el_g4.p;
+	c.el_flat = h->el_flat.p;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -1173,10 +1243,10 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (nring && nring != nbodies)
 		return fail(XFEM_EUNSUPPORTED, "continuous-pressure models (energy 8-10) and element models cannot share a handle");
 	h->ring_mode = nring > 0;
-	uint32_t nhexb = 0;
-	for (const BodyHost& b : h->bodies) nhexb += b.hex ? 1u : 0u;
-	if (nhexb && nhexb != nbodies) return fail(XFEM_EUNSUPPORTED, "hex meshes and tet meshes cannot share a handle");
-	h->hex_mode = nhexb > 0;
+	for (const BodyHost& b : h->bodies)
+		if (b.el != h->bodies[0].el)
+			return fail(XFEM_EUNSUPPORTED, "linear tets, hexes and quadratic tets cannot share a handle");
+	h->el_mode = h->bodies.empty() ? kElTets : h->bodies[0].el;
 	clk.lap("rest state + schedule");
 	rc = build_device(h.get());
 	clk.lap("device layout");
@@ -1207,9 +1277,10 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
-	if (h->hex_mode) {
-		const int e = launch_hexes(h->ctx, 256, nsub, dt, h->stream);
-		if (e) return fail(XFEM_ECUDA, std::string("hex launch: ") + cudaGetErrorString((cudaError_t)e));
+	if (h->el_mode) {
+		const int e = h->el_mode == kElT10 ? launch_t10(h->ctx, 256, nsub, dt, h->stream)
+		                                   : launch_hexes(h->ctx, 256, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
 	int rc = autotune(h, nsub, dt);
@@ -1340,8 +1411,10 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	int rc = validate_settings(*s);
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (h->hex_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
-		return fail(XFEM_EUNSUPPORTED, "hex meshes run every energy model but the continuous-pressure ones (8-10)");
+	if (h->el_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
+		return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes run every energy model but the continuous-pressure ones (8-10)");
+	if (quadratic_type(s->flags) != (b->el == kElT10))
+		return fail(XFEM_EUNSUPPORTED, "switching between linear and quadratic elements (flags bits 0-3) needs a new handle");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
 		                               "element models needs a new handle (their schedules differ)");
@@ -1349,7 +1422,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	b->settings = *s;
 	XCUDA(cudaSetDevice(h->device));
 	BodyParams p = make_params(*s);
-	p.ntets = b->hex ? b->nh : b->nt;
+	p.ntets = b->el ? b->nh : b->nt;
 	p.nverts = b->nv;
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	// Settings::tickId: the handle's substep counter continues from here
@@ -1376,7 +1449,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 		}
 	}
 	if (h->ring_mode) h->ctx.ext = ring_damp_of(h->bodies) ? 1u : 0u;
-	if (material && b->tet_mu.empty() && !h->hex_mode) return update_material(h, *b);
+	if (material && b->tet_mu.empty() && !h->el_mode) return update_material(h, *b);
 	return XFEM_OK;
 }
 
@@ -1406,7 +1479,7 @@ int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
 	if (!b) return XFEM_EINVAL;
 	if (h->ring_mode && mu)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) take the body's material only");
-	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "hex meshes take the body's material only");
+	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes take the body's material only");
 	if (mu) {
 		for (uint32_t t = 0; t < b->nt; t++)
 			if (!(mu[t] > 0.0f) || !isfinite(mu[t])) return fail(XFEM_EINVAL, "tet mu must be finite and > 0");
@@ -1435,10 +1508,11 @@ int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, f
 	if (h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) have no allocation-free launch");
 	XCUDA(cudaSetDevice(h->device));
-	if (h->hex_mode) {
-		// the hex launch allocates nothing
-		const int e = launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
-		if (e) return fail(XFEM_ECUDA, std::string("hex launch: ") + cudaGetErrorString((cudaError_t)e));
+	if (h->el_mode) {
+		// the element launches allocate nothing
+		const int e = h->el_mode == kElT10 ? launch_t10(h->ctx, 256, (uint32_t)n, dt, h->stream)
+		                                   : launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
 		return check_device_error(h);
 	}
 	int dev_err = 0;
@@ -1479,7 +1553,7 @@ int xfem_get_lambdas(xfem_body* h, uint32_t body, float* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
-	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "hex meshes keep no multipliers");
+	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes keep no multipliers");
 	if (!h->tlam.p) return fail(XFEM_EINVAL, "create the handle with keep_lambdas = 1");
 	XCUDA(cudaSetDevice(h->device));
 	std::vector<float2> all(h->tlam.n);
@@ -1498,7 +1572,39 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
 	XCUDA(cudaSetDevice(h->device));
-	if (b->hex) {
+	if (b->el == kElT10) {
+		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per T10: rest
+		// volume times the mean det F over the 4 points, in double
+		std::vector<float> x(3 * (size_t)b->nv);
+		const int rc = get_xyz(h, body, 0, x.data());
+		if (rc) return rc;
+		double v = 0.0;
+		for (uint32_t q = 0; q < b->nh; q++) {
+			const uint32_t* is = &b->elems[10 * (size_t)q];
+			const float* e = &b->eep[(size_t)rest::kT10Rec * q];
+			double P[9][3];
+			for (int i = 0; i < 9; i++)
+				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[9] + k];
+			double scale = 0.0;
+			for (int p = 0; p < 4; p++) {
+				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+				for (int n = 0; n < 9; n++)
+					for (int c = 0; c < 3; c++)
+						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::t10_grad(4, p, n, r) * P[n][c];
+				const float* qi = e + rest::kT10Qi;
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) F[c][r] = qi[r] * Dm[c][0] + qi[3 + r] * Dm[c][1] + qi[6 + r] * Dm[c][2];
+				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+				scale += 0.25 * det;
+			}
+			v += (double)e[rest::kT10Vol] * scale;
+		}
+		*out = v;
+		return XFEM_OK;
+	}
+	if (b->el == kElHexes) {
 		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per hex: rest
 		// volume times the weighted det F over the 2x2x2 points, in double
 		std::vector<float> x(3 * (size_t)b->nv);
@@ -1506,8 +1612,8 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 		if (rc) return rc;
 		double v = 0.0;
 		for (uint32_t hx = 0; hx < b->nh; hx++) {
-			const uint32_t* is = &b->hexes[8 * (size_t)hx];
-			const float* e = &b->hep[(size_t)rest::kHexRec * hx];
+			const uint32_t* is = &b->elems[8 * (size_t)hx];
+			const float* e = &b->eep[(size_t)rest::kHexRec * hx];
 			double P[7][3];
 			for (int i = 0; i < 7; i++)
 				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[7] + k];
@@ -1541,7 +1647,7 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 int xfem_get_rest_state(const xfem_body* h, uint32_t body, float* out_ep17, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex body: use xfem_get_hex_rest_state");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex or T10 body: use xfem_get_hex_rest_state or xfem_get_t10_rest_state");
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
@@ -1551,7 +1657,7 @@ int xfem_get_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, ui
                       uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex body: use xfem_get_hex_schedule");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex or T10 body: use xfem_get_hex_schedule or xfem_get_t10_schedule");
 	const Schedule& s = b.sched;
 	if (vert_rank) memcpy(vert_rank, s.vert_rank.data(), s.vert_rank.size() * 4);
 	if (ncolours) *ncolours = s.ncolours;
@@ -1583,7 +1689,7 @@ int xfem_compute_rest_state(const float* node_data, uint32_t node_data_count, co
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
 	const int rc = prepare_mesh(m, b);
 	if (rc) return rc;
-	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_rest_state");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_rest_state");
 	host_rest(m, b);
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
@@ -1601,7 +1707,7 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
 	int rc = prepare_mesh(m, b);
 	if (rc) return rc;
-	if (b.hex) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_schedule");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex mesh: use xfem_compute_hex_schedule");
 	if (build_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, cluster_mode == 1 ? 0u : 1u, no_morton ? 0u : 1u, b.sched))
 		return fail(XFEM_ELIMIT, "colour schedule limit exceeded");
 	if (nclusters) *nclusters = b.sched.nclusters;
@@ -1647,18 +1753,18 @@ int xfem_body_hex_count(const xfem_body* h, uint32_t body, uint32_t* nhexes) {
 int xfem_get_hex_rest_state(const xfem_body* h, uint32_t body, float* out_ep120, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (!b.hex) return fail(XFEM_EUNSUPPORTED, "not a hex body");
-	if (out_ep120) memcpy(out_ep120, b.hep.data(), b.hep.size() * sizeof(float));
+	if (b.el != kElHexes) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	if (out_ep120) memcpy(out_ep120, b.eep.data(), b.eep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
 }
 
-static int hex_schedule_out(const BodyHost& b, uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin,
-                            uint32_t* ncolours) {
+static int elem_schedule_out(const BodyHost& b, uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin,
+                             uint32_t* ncolours) {
 	if (vert_rank) memcpy(vert_rank, b.sched.vert_rank.data(), b.sched.vert_rank.size() * 4);
-	if (hex_order) memcpy(hex_order, b.hsched.order.data(), b.hsched.order.size() * 4);
-	if (colour_begin) memcpy(colour_begin, b.hsched.colour_begin.data(), b.hsched.colour_begin.size() * 4);
-	if (ncolours) *ncolours = b.hsched.ncolours;
+	if (order) memcpy(order, b.esched.order.data(), b.esched.order.size() * 4);
+	if (colour_begin) memcpy(colour_begin, b.esched.colour_begin.data(), b.esched.colour_begin.size() * 4);
+	if (ncolours) *ncolours = b.esched.ncolours;
 	return XFEM_OK;
 }
 
@@ -1666,8 +1772,8 @@ int xfem_get_hex_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank
                           uint32_t* colour_begin, uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (!b.hex) return fail(XFEM_EUNSUPPORTED, "not a hex body");
-	return hex_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+	if (b.el != kElHexes) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	return elem_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
 }
 
 int xfem_compute_hex_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -1677,9 +1783,9 @@ int xfem_compute_hex_rest_state(const float* node_data, uint32_t node_data_count
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
 	const int rc = prepare_mesh(m, b);
 	if (rc) return rc;
-	if (!b.hex) return fail(XFEM_EINVAL, "not a hex mesh");
+	if (b.el != kElHexes) return fail(XFEM_EINVAL, "not a hex mesh");
 	host_rest(m, b);
-	if (out_ep120) memcpy(out_ep120, b.hep.data(), b.hep.size() * sizeof(float));
+	if (out_ep120) memcpy(out_ep120, b.eep.data(), b.eep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
 	return XFEM_OK;
@@ -1692,11 +1798,89 @@ int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, 
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
 	const int rc = prepare_mesh(m, b);
 	if (rc) return rc;
-	if (!b.hex) return fail(XFEM_EINVAL, "not a hex mesh");
+	if (b.el != kElHexes) return fail(XFEM_EINVAL, "not a hex mesh");
 	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
-	if (hex_schedule(b.nodes.data(), b.nv, b.hexes.data(), b.nh, no_morton ? 0u : 1u, b.hsched))
-		return fail(XFEM_ELIMIT, "the hex colouring needs more than 64 colours");
-	return hex_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+	if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 8, no_morton ? 0u : 1u, b.esched))
+		return fail(XFEM_ELIMIT, "the hex colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+	return elem_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int xfem_body_t10_count(const xfem_body* h, uint32_t body, uint32_t* nt10, uint32_t* nedges) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	if (nt10) *nt10 = b.nh;
+	if (nedges) *nedges = (uint32_t)(b.edges.size() / 2);
+	return XFEM_OK;
+}
+
+int xfem_get_t10_rest_state(const xfem_body* h, uint32_t body, float* out_ep56, float* out_w, uint32_t* out_t10,
+                            uint32_t* out_edges) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	if (out_ep56) memcpy(out_ep56, b.eep.data(), b.eep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_t10) memcpy(out_t10, b.elems.data(), b.elems.size() * 4);
+	if (out_edges) memcpy(out_edges, b.edges.data(), b.edges.size() * 4);
+	return XFEM_OK;
+}
+
+int xfem_get_t10_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, uint32_t* t10_order,
+                          uint32_t* colour_begin, uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	return elem_schedule_out(b, vert_rank, t10_order, colour_begin, ncolours);
+}
+
+int xfem_compute_t10_edges(const uint32_t* idx_data, uint32_t idx_data_count, uint32_t* out_edges, uint32_t* out_t10,
+                           uint32_t* out_nedges) {
+	if (!idx_data) return fail(XFEM_EINVAL, "null index stream");
+	BodyHost b;
+	uint32_t nv = 0;
+	if (parse_tets(idx_data, idx_data_count, b.tets, nv)) return fail(XFEM_EINVAL, "not a tet index stream (tag 4)");
+	std::vector<uint32_t> edges, t10;
+	tet_edges(b.tets.data(), (uint32_t)(b.tets.size() / 4), nv, edges, t10);
+	if (out_edges) memcpy(out_edges, edges.data(), edges.size() * 4);
+	if (out_t10) memcpy(out_t10, t10.data(), t10.size() * 4);
+	if (out_nedges) *out_nedges = (uint32_t)(edges.size() / 2);
+	return XFEM_OK;
+}
+
+// A tet mesh read as T10s (prepare_mesh then prepare_t10).
+static int t10_mesh(const xfem_mesh& m, BodyHost& b, std::vector<double>* X) {
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (b.el != kElTets) return fail(XFEM_EINVAL, "not a tet mesh (tag 4)");
+	prepare_t10(m, b, X);
+	return XFEM_OK;
+}
+
+int xfem_compute_t10_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, double* out_x, float* out_ep56, float* out_w,
+                                uint8_t* out_flags) {
+	BodyHost b;
+	std::vector<double> X;
+	const int rc = t10_mesh({node_data, node_data_count, idx_data, idx_data_count, density}, b, &X);
+	if (rc) return rc;
+	if (out_x) memcpy(out_x, X.data(), X.size() * sizeof(double));
+	if (out_ep56) memcpy(out_ep56, b.eep.data(), b.eep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
+	return XFEM_OK;
+}
+
+int xfem_compute_t10_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* t10_order,
+                              uint32_t* colour_begin, uint32_t* ncolours) {
+	BodyHost b;
+	const int rc = t10_mesh({node_data, node_data_count, idx_data, idx_data_count, 1.0f}, b, nullptr);
+	if (rc) return rc;
+	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
+	if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 10, no_morton ? 0u : 1u, b.esched))
+		return fail(XFEM_ELIMIT, "the T10 colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+	return elem_schedule_out(b, vert_rank, t10_order, colour_begin, ncolours);
 }
 
 int xfem_generate_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
@@ -1789,7 +1973,7 @@ int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpo
 	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
 	if (nsub == 0) return fail(XFEM_EINVAL, "substeps must be > 0");
 	if (ntips && !tips) return fail(XFEM_EINVAL, "null tips");
-	if (h->hex_mode) return fail(XFEM_EUNSUPPORTED, "the adjoint covers tet meshes only");
+	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "the adjoint covers linear tet meshes only");
 	for (const BodyHost& b : h->bodies) {
 		const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 		if (model_of(energy) != kModelNeo || !((b.settings.flags >> XFEM_XPBD_SOLVE_BIT) & 1u))

@@ -12,7 +12,7 @@
 // damping passes; each pass ends at the grid barrier.
 //
 // Records: 30 float4 per hex, stored as a structure of arrays (float4 k of
-// hex i at hex_rec[k * nhex + i]) so that the threads of a pass read them
+// hex i at el_rec[k * nel + i]) so that the threads of a pass read them
 // coalesced. The first ten hold what every model reads (the centre's inverse
 // map jacobian and weight, volume, surface area, the prefactored QQ and QR);
 // the other twenty the 2x2x2 points' inverse jacobians and weights, which only
@@ -20,8 +20,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "xfem_device.cuh"
-#include "xfem_internal.h"
+#include "xfem_elements.cuh"
 
 namespace xfem {
 
@@ -64,20 +63,6 @@ __device__ __forceinline__ void def_grad(const float Ji[3][3], int hi, int p, co
 		for (int r = 0; r < 3; r++) F[c][r] = fmaf(Ji[0][r], Dm[c][0], fmaf(Ji[1][r], Dm[c][1], Ji[2][r] * Dm[c][2]));
 }
 
-// adjugate and J through the first adjugate column (XPBDFEM/Fem.cpp:284-306)
-__device__ __forceinline__ float adj_det(const float F[3][3], float A[3][3]) {
-	A[0][0] = fmaf(F[1][1], F[2][2], -F[1][2] * F[2][1]);
-	A[0][1] = -fmaf(F[0][1], F[2][2], -F[0][2] * F[2][1]);
-	A[0][2] = fmaf(F[0][1], F[1][2], -F[0][2] * F[1][1]);
-	A[1][0] = -fmaf(F[1][0], F[2][2], -F[1][2] * F[2][0]);
-	A[1][1] = fmaf(F[0][0], F[2][2], -F[0][2] * F[2][0]);
-	A[1][2] = -fmaf(F[0][0], F[1][2], -F[0][2] * F[1][0]);
-	A[2][0] = fmaf(F[1][0], F[2][1], -F[1][1] * F[2][0]);
-	A[2][1] = -fmaf(F[0][0], F[2][1], -F[0][1] * F[2][0]);
-	A[2][2] = fmaf(F[0][0], F[1][1], -F[0][1] * F[1][0]);
-	return fmaf(F[0][0], A[0][0], fmaf(F[0][1], A[1][0], F[0][2] * A[2][0]));
-}
-
 // ApplyEnergyGradient (XPBDFEM/Fem.cpp:338-354): g[n] += (G Ji) dN[n], n < 7.
 __device__ __forceinline__ void apply(const float G[3][3], const float Ji[3][3], int hi, int p, Vec3 g[8]) {
 	float M[3][3];  // M[j][r] = sum_k G[k][r] Ji[j][k]
@@ -92,18 +77,6 @@ __device__ __forceinline__ void apply(const float G[3][3], const float Ji[3][3],
 		g[n].y += fmaf(M[0][1], d0, fmaf(M[1][1], d1, M[2][1] * d2));
 		g[n].z += fmaf(M[0][2], d0, fmaf(M[1][2], d1, M[2][2] * d2));
 	}
-}
-
-__device__ __forceinline__ void root(Vec3 g[8]) {
-	Vec3 s = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-	for (int n = 0; n < 7; n++) s = {s.x + g[n].x, s.y + g[n].y, s.z + g[n].z};
-	g[7] = {g[7].x - s.x, g[7].y - s.y, g[7].z - s.z};
-}
-
-__device__ __forceinline__ void zero(Vec3 g[8]) {
-#pragma unroll
-	for (int n = 0; n < 8; n++) g[n] = {0.0f, 0.0f, 0.0f};
 }
 
 __device__ __forceinline__ void load_ji(const HexRec& R, int hi, int p, float Ji[3][3]) {
@@ -166,83 +139,8 @@ __device__ __forceinline__ float pref_i1(const HexRec& R, const Vec3 P[7], Vec3 
 			g[j] = {fmaf(qr, P[i].x, g[j].x), fmaf(qr, P[i].y, g[j].y), fmaf(qr, P[i].z, g[j].z)};
 		}
 	g[7] = {0.0f, 0.0f, 0.0f};
-	root(g);
+	rootn<8>(g);
 	return U;
-}
-
-__device__ __forceinline__ float wdot8(const float w[8], const Vec3 a[8], const Vec3 b[8]) {
-	float s = 1.0e-22f;
-#pragma unroll
-	for (int n = 0; n < 8; n++) s = fmaf(w[n], dot(a[n], b[n]), s);
-	return s;
-}
-
-__device__ __forceinline__ float gdot8(const Vec3 g[8], const float4 D[8]) {
-	float s = 0.0f;
-#pragma unroll
-	for (int n = 0; n < 8; n++) s = fmaf(g[n].x, D[n].x, fmaf(g[n].y, D[n].y, fmaf(g[n].z, D[n].z, s)));
-	return s;
-}
-
-__device__ __forceinline__ void move(const float w[8], float l, const Vec3 g[8], float4 D[8]) {
-#pragma unroll
-	for (int n = 0; n < 8; n++) {
-		const float s = w[n] * l;
-		D[n].x = fmaf(s, g[n].x, D[n].x);
-		D[n].y = fmaf(s, g[n].y, D[n].y);
-		D[n].z = fmaf(s, g[n].z, D[n].z);
-	}
-}
-
-// One constraint (XPBDFEM/Xpbd.h:87-121) with the in-solve Rayleigh damping
-// (types 0 Paper, 1 Limit) when `damp` > 0.
-__device__ __forceinline__ float lambda1(float U, const Vec3 g[8], const float w[8], const float4 D[8], float alpha,
-                                         float comp, float damp, bool limit, float inv_dt) {
-	const float wgg = wdot8(w, g, g);
-	if (!(damp > 0.0f)) return (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
-	const float gV = gdot8(g, D);
-	const float gamma = damp * inv_dt;
-	if (!limit) return (-2.0f * U - gamma * gV) / fmaf(wgg, 1.0f + gamma, 2.0f * U * alpha);
-	const float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
-	const float A = fmaf(2.0f * U, comp * inv_dt / damp, wgg);
-	const float b = (-gV - wgg * l) * (A / fmaxf(A, 4.0f * wgg));
-	return l + b / A;
-}
-
-// The coupled pair (XPBDFEM/Xpbd.h:123-215): Cramer's rule, the damping forms
-// of :133-205.
-__device__ __forceinline__ void lambda2(float U0, float U1, const Vec3 g0[8], const Vec3 g1[8], const float w[8],
-                                        const float4 D[8], float alpha0, float alpha1, float comp0, float comp1,
-                                        float damp, bool limit, float inv_dt, float& l0, float& l1) {
-	const float wgg0 = wdot8(w, g0, g0), wgg1 = wdot8(w, g1, g0), wgg2 = wdot8(w, g1, g1);
-	if (!(damp > 0.0f)) {
-		cramer(fmaf(2.0f * U0, alpha0, wgg0), wgg1, fmaf(2.0f * U1, alpha1, wgg2), -2.0f * U0, -2.0f * U1, l0, l1);
-		return;
-	}
-	const float gV0 = gdot8(g0, D), gV1 = gdot8(g1, D);
-	const float gamma = damp * inv_dt;
-	float A0, A2, b0 = -2.0f * U0, b1 = -2.0f * U1;
-	if (!limit) {
-		const float s = 1.0f / (1.0f + gamma);
-		A0 = wgg0 + (2.0f * U0 * alpha0) * s;
-		A2 = wgg2 + (2.0f * U1 * alpha1) * s;
-		b0 = (b0 - gamma * gV0) * s;
-		b1 = (b1 - gamma * gV1) * s;
-	} else {
-		A0 = fmaf(2.0f * U0, alpha0, wgg0);
-		A2 = fmaf(2.0f * U1, alpha1, wgg2);
-	}
-	cramer(A0, wgg1, A2, b0, b1, l0, l1);
-	if (limit) {
-		const float B0 = fmaf(2.0f * U0, comp0 * inv_dt / damp, wgg0), B2 = fmaf(2.0f * U1, comp1 * inv_dt / damp, wgg2);
-		float e0 = fmaf(b0, -1.0f - alpha0 * l0, -gV0), e1 = fmaf(b1, -1.0f - alpha1 * l1, -gV1);
-		e0 *= B0 / fmaxf(B0, 8.0f * wgg0);
-		e1 *= B2 / fmaxf(B2, 8.0f * wgg2);
-		float d0, d1;
-		cramer(B0, wgg1, B2, e0, e1, d0, d1);
-		l0 += d0;
-		l1 += d1;
-	}
 }
 
 // The Pixar models' U and g (SolveElementPixar, XPBDFEM/Fem.cpp:379-427), mu =
@@ -251,7 +149,7 @@ __device__ __forceinline__ void lambda2(float U0, float U1, const Vec3 g0[8], co
 __device__ __forceinline__ float pixar(const HexRec& R, const BodyParams& bp, uint32_t e, const Vec3 P[7], Vec3 g[8]) {
 	const float a = __ldg(&bp.a), hw = __ldg(&bp.hw);
 	float U = 0.0f;
-	zero(g);
+	zeron<8>(g);
 	if (e != 2u) {
 		const int hi = e == 0u;
 #pragma unroll 1
@@ -271,14 +169,14 @@ __device__ __forceinline__ float pixar(const HexRec& R, const BodyParams& bp, ui
 				for (int r = 0; r < 3; r++) G[c][r] = fmaf(q.F[r][c], s1, q.A[c][r] * s2);
 			apply(G, q.Ji, hi, p, g);
 		}
-		root(g);
+		rootn<8>(g);
 		return U;
 	}
 	hydro(R, 0, P, a, U, g);
 	U *= hw;
 #pragma unroll
 	for (int n = 0; n < 7; n++) g[n] = {g[n].x * hw, g[n].y * hw, g[n].z * hw};
-	root(g);
+	rootn<8>(g);
 	Vec3 gi[8];
 	U += pref_i1(R, P, gi);
 #pragma unroll
@@ -331,8 +229,6 @@ __device__ __forceinline__ float dev_full(const HexRec& R, const BodyParams& bp,
 	return U0;
 }
 
-__device__ __forceinline__ bool full_quadrature(uint32_t e) { return e == 3u || e == 5u || e == 6u; }
-
 __device__ __forceinline__ void rel(const float4 O[8], const float4 D[8], bool vmode, Vec3 P[7]) {
 #pragma unroll
 	for (int i = 0; i < 7; i++)
@@ -340,9 +236,6 @@ __device__ __forceinline__ void rel(const float4 O[8], const float4 D[8], bool v
 		             : Vec3{(O[i].x - O[7].x) + (D[i].x - D[7].x), (O[i].y - O[7].y) + (D[i].y - D[7].y),
 		                    (O[i].z - O[7].z) + (D[i].z - D[7].z)};
 }
-
-// Pass kinds of one hex.
-enum HexPass { kSolve = 0, kVolume = 1, kRayleigh = 2 };
 
 // det(F) / 64 of F with rows (sA[i], sB[i], sC[i]) and its adjugate columns
 // scaled by 1 / 64 (XPBDFEM/Fem.cpp:613-617, 782-786).
@@ -559,13 +452,13 @@ __device__ __forceinline__ void cube(const BodyParams& bp, const HexRec& R, uint
 // Rayleigh ratio rd (x 8 when amortized).
 template <int KIND>
 __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {
-	const uint4 va = __ldg(C.hex_vid + 2 * (size_t)i), vb = __ldg(C.hex_vid + 2 * (size_t)i + 1);
+	const uint4 va = __ldg(C.el_vid + 2 * (size_t)i), vb = __ldg(C.el_vid + 2 * (size_t)i + 1);
 	const uint32_t dv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
 	float4 O[8], D[8];
 #pragma unroll
 	for (int n = 0; n < 8; n++) ld_vertex(C.vert + 2 * (size_t)dv[n], O[n], D[n]);
 	const BodyParams& bp = C.bodies[__float_as_uint(D[0].w) >> 8];
-	const HexRec R{C.hex_rec, C.nhex, i};
+	const HexRec R{C.el_rec, C.nel, i};
 	const float w[8] = {O[0].w, O[1].w, O[2].w, O[3].w, O[4].w, O[5].w, O[6].w, O[7].w};
 	const float vol = R(kRVol);
 	const uint32_t e = __ldg(&bp.energy);
@@ -583,19 +476,19 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 	rel(O, D, KIND == kRayleigh, P);
 	if (KIND == kVolume) {
 		float U = 0.0f;
-		zero(g0);
+		zeron<8>(g0);
 		hydro(R, 0, P, 1.0f, U, g0);
-		root(g0);
+		rootn<8>(g0);
 		const float alpha = __ldg(&bp.compliance) * vol * inv_dt2;
-		move(w, (-2.0f * U) / fmaf(2.0f * U, alpha, wdot8(w, g0, g0)), g0, D);
+		moven<8>(w, (-2.0f * U) / fmaf(2.0f * U, alpha, wdotn<8>(w, g0, g0)), g0, D);
 	} else if (e <= 2u) {
 		const float U = pixar(R, bp, e, P, g0);
 		const float comp = __ldg(&bp.compliance) / vol;
 		if (KIND == kRayleigh) {
-			const float gV = gdot8(g0, D);
-			move(w, -gV / fmaf(2.0f * U, comp * inv_dt / rd, wdot8(w, g0, g0)), g0, D);
+			const float gV = gdotn<8>(g0, D);
+			moven<8>(w, -gV / fmaf(2.0f * U, comp * inv_dt / rd, wdotn<8>(w, g0, g0)), g0, D);
 		} else {
-			move(w, lambda1(U, g0, w, D, comp * inv_dt2, comp, damp, limit, inv_dt), g0, D);
+			moven<8>(w, lambda1n<8>(U, g0, w, D, comp * inv_dt2, comp, damp, limit, inv_dt), g0, D);
 		}
 	} else {
 		const float a = __ldg(&bp.a);
@@ -604,11 +497,11 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 		const bool coupled = KIND == kRayleigh || sim;
 		const bool full = full_quadrature(e);
 		float U0, U1 = 0.0f;
-		zero(g0);
-		zero(g1);
+		zeron<8>(g0);
+		zeron<8>(g1);
 		if (full) {
 			U0 = fmaxf(0.0001f, dev_full(R, bp, e, P, coupled && e != 6u, g0, U1, g1));
-			root(g0);
+			rootn<8>(g0);
 		} else {
 			U0 = pref_i1(R, P, g0);
 			if (e == 7u) {
@@ -622,14 +515,14 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 		}
 		if (coupled) {
 			if (!full || e == 6u) hydro(R, 0, P, a, U1, g1);
-			root(g1);
+			rootn<8>(g1);
 			if (KIND == kRayleigh) {
 				// RayleighDamp (XPBDFEM/Xpbd.h:217-263) on V = D
 				if (sim) {
-					const float b0 = -gdot8(g0, D), b1 = -gdot8(g1, D);
+					const float b0 = -gdotn<8>(g0, D), b1 = -gdotn<8>(g1, D);
 					float l0, l1;
-					cramer(fmaf(2.0f * U0, comp0 * inv_dt / rd, wdot8(w, g0, g0)), wdot8(w, g0, g1),
-					       fmaf(2.0f * U1, comp1 * inv_dt / rd, wdot8(w, g1, g1)), b0, b1, l0, l1);
+					cramer(fmaf(2.0f * U0, comp0 * inv_dt / rd, wdotn<8>(w, g0, g0)), wdotn<8>(w, g0, g1),
+					       fmaf(2.0f * U1, comp1 * inv_dt / rd, wdotn<8>(w, g1, g1)), b0, b1, l0, l1);
 #pragma unroll
 					for (int n = 0; n < 8; n++) {
 						const float s0 = w[n] * l0, s1 = w[n] * l1;
@@ -638,12 +531,12 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 						D[n].z = fmaf(s1, g1[n].z, fmaf(s0, g0[n].z, D[n].z));
 					}
 				} else {
-					move(w, -gdot8(g0, D) / fmaf(2.0f * U0, comp0 * inv_dt / rd, wdot8(w, g0, g0)), g0, D);
-					move(w, -gdot8(g1, D) / fmaf(2.0f * U1, comp1 * inv_dt / rd, wdot8(w, g1, g1)), g1, D);
+					moven<8>(w, -gdotn<8>(g0, D) / fmaf(2.0f * U0, comp0 * inv_dt / rd, wdotn<8>(w, g0, g0)), g0, D);
+					moven<8>(w, -gdotn<8>(g1, D) / fmaf(2.0f * U1, comp1 * inv_dt / rd, wdotn<8>(w, g1, g1)), g1, D);
 				}
 			} else {
 				float l0, l1;
-				lambda2(U0, U1, g0, g1, w, D, alpha0, alpha1, comp0, comp1, damp, limit, inv_dt, l0, l1);
+				lambda2n<8>(U0, U1, g0, g1, w, D, alpha0, alpha1, comp0, comp1, damp, limit, inv_dt, l0, l1);
 #pragma unroll
 				for (int n = 0; n < 8; n++) {
 					const float s0 = w[n] * l0, s1 = w[n] * l1;
@@ -654,172 +547,37 @@ __device__ __noinline__ void hex_pass(const DevCtx& C, uint32_t i, float inv_dt,
 			}
 		} else {
 			// serial: deviatoric, refresh P, hydrostatic (XPBDFEM/Fem.cpp:490-521, 532-551)
-			move(w, lambda1(U0, g0, w, D, alpha0, comp0, damp, limit, inv_dt), g0, D);
+			moven<8>(w, lambda1n<8>(U0, g0, w, D, alpha0, comp0, damp, limit, inv_dt), g0, D);
 			rel(O, D, false, P);
 			hydro(R, full && e != 6u, P, a, U1, g1);
-			root(g1);
-			move(w, lambda1(U1, g1, w, D, alpha1, comp1, damp, limit, inv_dt), g1, D);
+			rootn<8>(g1);
+			moven<8>(w, lambda1n<8>(U1, g1, w, D, alpha1, comp1, damp, limit, inv_dt), g1, D);
 		}
 	}
 #pragma unroll
 	for (int n = 0; n < 8; n++) st_vertex(C.vert + 2 * (size_t)dv[n], O[n], D[n]);
 }
 
-// PbdDamp over a hex's 8 nodes (XPBDFEM/Xpbd.h:306-346) on the canonical
-// state: towards the rigid motion (centre-of-mass velocity plus rotation).
+// PbdDamp over a hex's 8 nodes with coeff / surfaceArea capped at 1.
 __device__ __noinline__ void hex_pbd(const DevCtx& C, uint32_t i, float coeff) {
-	const uint4 va = __ldg(C.hex_vid + 2 * (size_t)i), vb = __ldg(C.hex_vid + 2 * (size_t)i + 1);
+	const uint4 va = __ldg(C.el_vid + 2 * (size_t)i), vb = __ldg(C.el_vid + 2 * (size_t)i + 1);
 	const uint32_t dv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
-	float4 X[8], V[8];
-#pragma unroll
-	for (int n = 0; n < 8; n++) ld_vertex(C.vert + 2 * (size_t)dv[n], X[n], V[n]);
-	const float damping = fminf(1.0f, coeff / HexRec{C.hex_rec, C.nhex, i}(kRArea));
-	float Wsum = 1.0e-8f;
-#pragma unroll
-	for (int n = 0; n < 8; n++) Wsum += X[n].w;
-	const float Wavg = Wsum * 0.125f, Wmin = 0.0001f * Wavg;
-	Vec3 x[8], xcm = {0.0f, 0.0f, 0.0f}, vcm = {0.0f, 0.0f, 0.0f};
-	float M[8], Msum = 0.0f;
-#pragma unroll
-	for (int n = 0; n < 8; n++) {
-		x[n] = {X[n].x - X[7].x, X[n].y - X[7].y, X[n].z - X[7].z};
-		M[n] = Wavg / fmaxf(Wmin, X[n].w);
-		xcm = {fmaf(x[n].x, M[n], xcm.x), fmaf(x[n].y, M[n], xcm.y), fmaf(x[n].z, M[n], xcm.z)};
-		vcm = {fmaf(V[n].x, M[n], vcm.x), fmaf(V[n].y, M[n], vcm.y), fmaf(V[n].z, M[n], vcm.z)};
-		Msum += M[n];
-	}
-	const float im = 1.0f / Msum;
-	xcm = {xcm.x * im, xcm.y * im, xcm.z * im};
-	vcm = {vcm.x * im, vcm.y * im, vcm.z * im};
-	Vec3 r[8], L = {0.0f, 0.0f, 0.0f};
-	float I00 = 0.0f, I11 = 0.0f, I22 = 0.0f, I01 = 0.0f, I12 = 0.0f, I02 = 0.0f;
-#pragma unroll
-	for (int n = 0; n < 8; n++) {
-		r[n] = {x[n].x - xcm.x, x[n].y - xcm.y, x[n].z - xcm.z};
-		const Vec3 c = cross(r[n], v3(V[n]));
-		L = {fmaf(M[n], c.x, L.x), fmaf(M[n], c.y, L.y), fmaf(M[n], c.z, L.z)};
-		const float xx = r[n].x * r[n].x, yy = r[n].y * r[n].y, zz = r[n].z * r[n].z;
-		I00 = fmaf(M[n], yy + zz, I00);
-		I11 = fmaf(M[n], xx + zz, I11);
-		I22 = fmaf(M[n], xx + yy, I22);
-		I01 = fmaf(-M[n], r[n].x * r[n].y, I01);
-		I12 = fmaf(-M[n], r[n].y * r[n].z, I12);
-		I02 = fmaf(-M[n], r[n].z * r[n].x, I02);
-	}
-	const float a00 = fmaf(I11, I22, -I12 * I12), a01 = fmaf(I02, I12, -I01 * I22), a02 = fmaf(I01, I12, -I02 * I11);
-	const float a11 = fmaf(I00, I22, -I02 * I02), a12 = fmaf(I01, I02, -I00 * I12), a22 = fmaf(I00, I11, -I01 * I01);
-	const float idet = 1.0f / fmaf(I00, a00, fmaf(I01, a01, I02 * a02));
-	const Vec3 om = {fmaf(a00, L.x, fmaf(a01, L.y, a02 * L.z)) * idet, fmaf(a01, L.x, fmaf(a11, L.y, a12 * L.z)) * idet,
-	                 fmaf(a02, L.x, fmaf(a12, L.y, a22 * L.z)) * idet};
-#pragma unroll
-	for (int n = 0; n < 8; n++) {
-		const Vec3 c = cross(om, r[n]);
-		V[n].x = fmaf(damping, (vcm.x + c.x) - V[n].x, V[n].x);
-		V[n].y = fmaf(damping, (vcm.y + c.y) - V[n].y, V[n].y);
-		V[n].z = fmaf(damping, (vcm.z + c.z) - V[n].z, V[n].z);
-		st_vertex(C.vert + 2 * (size_t)dv[n], X[n], V[n]);
-	}
+	pbd_nodes<8>(C, dv, fminf(1.0f, coeff / HexRec{C.el_rec, C.nel, i}(kRArea)));
 }
 
-// Whether hex i is in this tick's damping slice (PostAmortized: one eighth of
-// its body's hex order per substep, XPBDFEM/Geo.cpp:793-797).
-__device__ __forceinline__ bool in_slice(const DevCtx& C, const BodyParams& bp, uint32_t i, uint32_t tick) {
-	if (__ldg(&bp.rayleigh_type) != 3u) return true;
-	const uint32_t nh = __ldg(&bp.ntets), m = tick % 8u, f = __ldg(C.hex_flat + i);
-	return f >= nh * m / 8u && f < nh * (m + 1u) / 8u;
-}
-
-__device__ __forceinline__ const BodyParams& body_of_hex(const DevCtx& C, uint32_t i) {
-	const uint32_t v0 = __ldg(&C.hex_vid[2 * (size_t)i].x);
-	return C.bodies[__float_as_uint(__ldcg(&C.vert[2 * (size_t)v0 + 1].w)) >> 8];
-}
-
-// The persistent hex kernel (cooperative launch, co-resident grid).
-__global__ void __launch_bounds__(256) k_hexes(DevCtx C, uint32_t nsub, float dt) {
-	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
-	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
-	const uint32_t tick0 = __ldcg(C.tick);
-	const bool dmode = C.damp_kinds != 0u;
-	uint32_t target = 0;
-	for (uint32_t s = 0; s < nsub; s++) {
-		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
-			float4 O, D;
-			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			advance_vertex(C.bodies, O, D, s == 0 || dmode, dt, inv_dt);
-			st_vertex(C.vert + 2 * (size_t)v, O, D);
-		}
-		if (!grid_sync(C, target)) return;
-		for (uint32_t c = 0; c < C.hex_colours; c++) {
-			const uint32_t b = __ldg(C.colour_hex_begin + c), e = __ldg(C.colour_hex_begin + c + 1);
-			for (uint32_t i = b + gtid; i < e; i += nthreads) hex_pass<kSolve>(C, i, inv_dt, inv_dt2, 0.0f);
-			if (!grid_sync(C, target)) return;
-		}
-		for (uint32_t it = 0; it < C.nvol; it++)
-			for (uint32_t c = 0; c < C.hex_colours; c++) {
-				const uint32_t b = __ldg(C.colour_hex_begin + c), e = __ldg(C.colour_hex_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads)
-					if (it < __ldg(&body_of_hex(C, i).volume_passes)) hex_pass<kVolume>(C, i, inv_dt, inv_dt2, 0.0f);
-				if (!grid_sync(C, target)) return;
-			}
-		if (!dmode) continue;
-		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
-			float4 O, D;
-			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C.bodies, O, D, inv_dt);
-			st_vertex(C.vert + 2 * (size_t)v, O, D);
-		}
-		if (!grid_sync(C, target)) return;
-		const uint32_t tick = tick0 + s;
-		if (C.damp_kinds & 1u)
-			for (uint32_t c = 0; c < C.hex_colours; c++) {
-				const uint32_t b = __ldg(C.colour_hex_begin + c), e = __ldg(C.colour_hex_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads) {
-					const BodyParams& bp = body_of_hex(C, i);
-					const uint32_t type = __ldg(&bp.rayleigh_type);
-					const float rd = __ldg(&bp.damping) * (type == 3u ? 8.0f : 1.0f);
-					if (type >= 2u && rd > 0.0f && in_slice(C, bp, i, tick)) hex_pass<kRayleigh>(C, i, inv_dt, inv_dt2, rd);
-				}
-				if (!grid_sync(C, target)) return;
-			}
-		if (C.damp_kinds & 2u)
-			for (uint32_t c = 0; c < C.hex_colours; c++) {
-				const uint32_t b = __ldg(C.colour_hex_begin + c), e = __ldg(C.colour_hex_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads) {
-					const BodyParams& bp = body_of_hex(C, i);
-					if (__ldg(&bp.pbd_on) && in_slice(C, bp, i, tick))
-						hex_pbd(C, i, __ldg(&bp.rayleigh_type) == 3u ? __ldg(&bp.pbd_coeff_amortized) : __ldg(&bp.pbd_coeff));
-				}
-				if (!grid_sync(C, target)) return;
-			}
+struct HexElem {
+	static constexpr uint32_t kVid4 = 2;
+	template <int KIND>
+	__device__ static void pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {
+		hex_pass<KIND>(C, i, inv_dt, inv_dt2, rd);
 	}
-	if (!dmode) {
-		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
-			float4 O, D;
-			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C.bodies, O, D, inv_dt);
-			st_vertex(C.vert + 2 * (size_t)v, O, D);
-		}
-	}
-	if (gtid == 0) *C.tick = tick0 + nsub;
-}
+	__device__ static void pbd(const DevCtx& C, uint32_t i, float coeff) { hex_pbd(C, i, coeff); }
+};
 
 }  // namespace
 
 int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream) {
-	if (nsub == 0) return 0;
-	cudaStream_t st = (cudaStream_t)stream;
-	const void* f = (const void*)k_hexes;
-	int dev = 0, sms = 0, per_sm = 0;
-	cudaError_t e = cudaGetDevice(&dev);
-	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, 0);
-	if (e != cudaSuccess) return (int)e;
-	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
-	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
-	if (e != cudaSuccess) return (int)e;
-	DevCtx c = ctx;
-	void* args[] = {&c, &nsub, &dt};
-	return (int)cudaLaunchCooperativeKernel(f, dim3(per_sm * sms), dim3(block), args, 0, st);
+	return launch_elements<HexElem>(ctx, block, nsub, dt, stream);
 }
 
 }  // namespace xfem

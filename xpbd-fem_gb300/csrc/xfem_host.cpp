@@ -379,47 +379,137 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 	return 0;
 }
 
-// Hex schedule: hexes coloured greedily in id order so that the hexes of one
-// colour share no vertex (each takes the smallest colour no earlier hex on
-// one of its vertices holds), then ordered inside each colour by (Morton code
-// of the centroid of the 8 vertices, id), or by id without Morton order.
-int hex_schedule(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, uint32_t morton,
-                 HexSchedule& hs) {
-	std::vector<uint64_t> used(nverts, 0);
-	std::vector<uint32_t> colour(nhexes);
+// Element schedule (hexes, T10s). The colouring runs over vertex ->
+// element incidence lists: element e marks the colours of the earlier
+// elements on its vertices with e and takes the smallest unmarked one.
+int elem_schedule(const float* nodes, uint32_t nverts, const uint32_t* elems, uint32_t nel, uint32_t per,
+                  uint32_t morton, ElemSchedule& es) {
+	std::vector<uint32_t> off(nverts + 1, 0), lst((size_t)per * nel);
+	for (size_t i = 0; i < (size_t)per * nel; i++) off[elems[i] + 1]++;
+	for (uint32_t v = 0; v < nverts; v++) off[v + 1] += off[v];
+	{
+		std::vector<uint32_t> fill(off.begin(), off.end() - 1);
+		for (uint32_t e = 0; e < nel; e++)
+			for (uint32_t n = 0; n < per; n++) lst[fill[elems[per * (size_t)e + n]]++] = e;
+	}
+	std::vector<uint32_t> mark(kMaxElemColours, 0xffffffffu), colour(nel);
 	uint32_t ncol = 0;
-	for (uint32_t h = 0; h < nhexes; h++) {
-		uint64_t u = 0;
-		for (int n = 0; n < 8; n++) u |= used[hexes[8 * (size_t)h + n]];
-		if (u == ~0ull) return -1;
-		const uint32_t c = (uint32_t)__builtin_ctzll(~u);
-		colour[h] = c;
+	for (uint32_t e = 0; e < nel; e++) {
+		for (uint32_t n = 0; n < per; n++) {
+			const uint32_t v = elems[per * (size_t)e + n];
+			for (uint32_t i = off[v]; i < off[v + 1] && lst[i] < e; i++) mark[colour[lst[i]]] = e;
+		}
+		uint32_t c = 0;
+		while (c < kMaxElemColours && mark[c] == e) c++;
+		if (c == kMaxElemColours) return -1;
+		colour[e] = c;
 		ncol = std::max(ncol, c + 1);
-		for (int n = 0; n < 8; n++) used[hexes[8 * (size_t)h + n]] |= 1ull << c;
 	}
 	const MortonFrame f = morton ? morton_frame(nodes, nverts) : MortonFrame{};
-	std::vector<std::pair<uint64_t, uint32_t>> key(nhexes);
-	for (uint32_t h = 0; h < nhexes; h++) {
-		uint32_t k = h;
+	std::vector<std::pair<uint64_t, uint32_t>> key(nel);
+	for (uint32_t e = 0; e < nel; e++) {
+		uint32_t k = e;
 		if (morton) {
 			float c[3] = {0.0f, 0.0f, 0.0f};
-			for (int n = 0; n < 8; n++)
-				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)hexes[8 * (size_t)h + n] + j];
-			for (int j = 0; j < 3; j++) c[j] = c[j] / 8.0f;
+			for (uint32_t n = 0; n < per; n++)
+				for (int j = 0; j < 3; j++) c[j] += nodes[3 * (size_t)elems[per * (size_t)e + n] + j];
+			for (int j = 0; j < 3; j++) c[j] = c[j] / (float)per;
 			k = f.code(c);
 		}
-		key[h] = {((uint64_t)colour[h] << 32) | k, h};
+		key[e] = {((uint64_t)colour[e] << 32) | k, e};
 	}
 	std::sort(key.begin(), key.end());
-	hs.ncolours = ncol;
-	hs.order.resize(nhexes);
-	hs.colour_begin.assign(ncol + 1, 0);
-	for (uint32_t i = 0; i < nhexes; i++) {
-		hs.order[i] = key[i].second;
-		hs.colour_begin[colour[key[i].second] + 1]++;
+	es.ncolours = ncol;
+	es.order.resize(nel);
+	es.colour_begin.assign(ncol + 1, 0);
+	for (uint32_t i = 0; i < nel; i++) {
+		es.order[i] = key[i].second;
+		es.colour_begin[colour[key[i].second] + 1]++;
 	}
-	for (uint32_t c = 0; c < ncol; c++) hs.colour_begin[c + 1] += hs.colour_begin[c];
+	for (uint32_t c = 0; c < ncol; c++) es.colour_begin[c + 1] += es.colour_begin[c];
 	return 0;
+}
+
+void tet_edges(const uint32_t* tets, uint32_t ntets, uint32_t nverts, std::vector<uint32_t>& edges,
+               std::vector<uint32_t>& t10) {
+	// every tet edge instance, listed under its lower vertex in stream order
+	std::vector<uint32_t> off(nverts + 1, 0), upper(6 * (size_t)ntets), inst(6 * (size_t)ntets);
+	auto lo_hi = [&](uint32_t t, int k, uint32_t& lo, uint32_t& hi) {
+		const uint32_t a = tets[4 * (size_t)t + rest::kT10EdgeNodes[k][0]], b = tets[4 * (size_t)t + rest::kT10EdgeNodes[k][1]];
+		lo = std::min(a, b);
+		hi = std::max(a, b);
+	};
+	for (uint32_t t = 0; t < ntets; t++)
+		for (int k = 0; k < 6; k++) {
+			uint32_t lo, hi;
+			lo_hi(t, k, lo, hi);
+			off[lo + 1]++;
+		}
+	for (uint32_t v = 0; v < nverts; v++) off[v + 1] += off[v];
+	std::vector<uint32_t> cnt(nverts, 0);
+	for (uint32_t t = 0; t < ntets; t++)
+		for (int k = 0; k < 6; k++) {
+			uint32_t lo, hi;
+			lo_hi(t, k, lo, hi);
+			const uint32_t id = 6 * t + (uint32_t)k;
+			upper[id] = hi;
+			inst[off[lo] + cnt[lo]++] = id;
+		}
+	// a later duplicate takes the list's last entry in its place
+	for (uint32_t v = 0; v < nverts; v++) {
+		uint32_t* L = inst.data() + off[v];
+		for (uint32_t j = 0; j < cnt[v]; j++)
+			for (uint32_t k = j + 1; k < cnt[v]; k++)
+				if (upper[L[j]] == upper[L[k]]) L[k--] = L[--cnt[v]];
+	}
+	std::vector<uint32_t> first(nverts, 0);
+	edges.clear();
+	for (uint32_t v = 0; v < nverts; v++) {
+		first[v] = (uint32_t)(edges.size() / 2);
+		for (uint32_t j = 0; j < cnt[v]; j++) {
+			edges.push_back(v);
+			edges.push_back(upper[inst[off[v] + j]]);
+		}
+	}
+	t10.resize(10 * (size_t)ntets);
+	for (uint32_t t = 0; t < ntets; t++) {
+		uint32_t* o = t10.data() + 10 * (size_t)t;
+		for (int c = 0; c < 4; c++) o[c] = tets[4 * (size_t)t + c];
+		for (int k = 0; k < 6; k++) {
+			uint32_t lo, hi;
+			lo_hi(t, k, lo, hi);
+			uint32_t e = 0;
+			while (edges[2 * (size_t)(first[lo] + e) + 1] != hi) e++;
+			o[4 + k] = nverts + first[lo] + e;
+		}
+	}
+}
+
+void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const uint32_t* edges,
+                   uint32_t nedges, const uint32_t* t10, float density, double* X, float* qep, float* w,
+                   uint8_t* vflags) {
+	const uint32_t n = nverts + nedges;
+	for (size_t i = 0; i < 3 * (size_t)nverts; i++) X[i] = (double)nodes[i];
+	for (uint32_t e = 0; e < nedges; e++)
+		for (int k = 0; k < 3; k++)
+			X[3 * (size_t)(nverts + e) + k] = 0.5 * (X[3 * (size_t)edges[2 * e] + k] + X[3 * (size_t)edges[2 * e + 1] + k]);
+	// AABB and Left / Right flags over every node (XPBDFEM/Geo.cpp:870-890)
+	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};
+	for (uint32_t i = 0; i < n; i++) {
+		w[i] = 0.0f;
+		for (int k = 0; k < 3; k++) {
+			mn[k] = fminf(mn[k], (float)X[3 * (size_t)i + k]);
+			mx[k] = fmaxf(mx[k], (float)X[3 * (size_t)i + k]);
+		}
+	}
+	for (uint32_t i = 0; i < n; i++) vflags[i] = rest::vertex_flags((float)X[3 * (size_t)i], mn[0], mx[0]);
+	for (uint32_t t = 0; t < ntets; t++) {
+		const uint32_t* is = t10 + 10 * (size_t)t;
+		float m[10];
+		rest::t10(X, is, density, qep + (size_t)rest::kT10Rec * t, m);
+		for (int c = 0; c < 10; c++) w[is[c]] += m[c];
+	}
+	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
 }
 
 }  // namespace xfem

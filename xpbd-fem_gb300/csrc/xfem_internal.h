@@ -93,17 +93,38 @@ void hex_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, u
 // GenerateHexBlock (XPBDFEM/MeshGen.cpp:156-221): idx holds 9 words per hex.
 void gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
                    float wonkiness, float* nodes, uint32_t* idx);
-// The hex schedule: hexes coloured greedily in id order so that the hexes of
-// one colour share no vertex (at most 64 colours), ordered inside each colour
-// by the Morton code of their centroid (or by id without Morton order).
-struct HexSchedule {
+// The schedule of an element mode (hexes, T10s): elements coloured greedily
+// in id order so that the elements of one colour share no vertex (each takes
+// the smallest colour no earlier element on one of its vertices holds; at
+// most kMaxElemColours), ordered inside each colour by the Morton code of the
+// centroid of their `per` vertices (or by id without Morton order).
+constexpr uint32_t kMaxElemColours = 4096;
+struct ElemSchedule {
 	uint32_t ncolours = 0;
-	std::vector<uint32_t> order;         // hexes, colour-major
+	std::vector<uint32_t> order;         // elements, colour-major
 	std::vector<uint32_t> colour_begin;  // ncolours + 1, into order
 };
-// Returns 0, or -1 when more than 64 colours are needed.
-int hex_schedule(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, uint32_t morton,
-                 HexSchedule& hs);
+// Returns 0, or -1 when more than kMaxElemColours colours are needed.
+int elem_schedule(const float* nodes, uint32_t nverts, const uint32_t* elems, uint32_t nel, uint32_t per,
+                  uint32_t morton, ElemSchedule& es);
+
+// Quadratic tetrahedra (T10, GeoQuadratic3d on a tet mesh). Connectivity3d's
+// edge numbering (XPBDFEM/Connectivity.cpp:371-393, 478-520, EdgeFromVerts
+// :587): for each lower vertex in id
+// order, its distinct upper neighbours in the order their first tet edge
+// appears in the stream, a later duplicate replacing the entry by the list's
+// last one (swap-remove); edges gets 2 words per edge. t10 gets GeoQuadratic3d's
+// 10 indices per tet (XPBDFEM/Geo.cpp:893-901): the corners, then nverts +
+// the edge ids of the local edges (0,1) (0,2) (0,3) (1,2) (1,3) (2,3).
+void tet_edges(const uint32_t* tets, uint32_t ntets, uint32_t nverts, std::vector<uint32_t>& edges,
+               std::vector<uint32_t>& t10);
+// GeoQuadratic3d::Init's rest state (XPBDFEM/Geo.cpp:836-941): X (3 doubles
+// per vertex, nverts corners then one node per edge at the midpoint in
+// double), vertex flags over all of them, 56 floats per T10 (rest::kT10*
+// offsets) and the inverse lumped masses (LumpsTet10), bit for bit.
+void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const uint32_t* edges,
+                   uint32_t nedges, const uint32_t* t10, float density, double* X, float* qep, float* w,
+                   uint8_t* vflags);
 
 // ---- GPU set-up path (xfem_setup.cu) ------------------------------------------
 // The parallel phases of the set-up on the device, bit for bit the host's:
@@ -263,18 +284,22 @@ struct DevCtx {
 	const uint4* pbd_ent;
 	const uint32_t* tet_verts;
 	uint32_t pbd_colours;
-	// Hex mode (linear hexahedra; xfem_hexes.cu): hexes in device order,
-	// colour-major (bodies in order inside a colour). hex_vid: 8 device vertex
-	// ids per hex (two uint4); hex_rec: 30 float4 records as a structure of
-	// arrays (float4 k of hex i at hex_rec[k * nhex + i]); hex_flat: each
-	// hex's index in its body's hex order (the amortized damping slices).
-	uint32_t hex_colours;
-	const uint4* hex_vid;
-	const float4* hex_rec;
-	const uint32_t* colour_hex_begin;  // hex_colours + 1
-	const uint32_t* hex_flat;
-	uint32_t nhex;
+	// Element modes (xfem_hexes.cu: linear hexahedra; xfem_t10.cu: quadratic
+	// tets): elements in device order, colour-major (bodies in order inside a
+	// colour). el_vid: the element's device vertex ids (hex: 8 in two uint4;
+	// T10: 10 in three uint4); el_rec: the records as a structure of arrays
+	// (float4 k of element i at el_rec[k * nel + i]; hex 30 float4, T10 14);
+	// el_flat: each element's index in its body's element order (the
+	// amortized damping slices); el_g4 (T10): the shape-function gradients at
+	// the 4-point rule, [point][node][axis].
+	uint32_t el_colours;
+	const uint4* el_vid;
+	const float4* el_rec;
+	const uint32_t* colour_el_begin;  // el_colours + 1
+	const uint32_t* el_flat;
+	uint32_t nel;
 	uint32_t pad6;
+	const float* el_g4;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
@@ -352,6 +377,8 @@ int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* st
 // Hex mode (xfem_hexes.cu): nsub substeps of a hex mesh, a cooperative
 // persistent launch (canonical (X, V) in and out).
 int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// Quadratic-tet mode (xfem_t10.cu): nsub substeps of a T10 mesh, likewise.
+int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Per-tet material (n tets from the given per-tet tables): c0 of each record
 // and 1/mu; mu null = mu_uniform for all.
 int launch_set_c0(float4* cblk, const uint32_t* rec, const float* vol, const float* mu, float mu_uniform, uint32_t n,

@@ -248,6 +248,106 @@ XFEM_HD void hex(const float* nodes, const uint32_t* is, float density, float* o
 	for (int n = 0; n < 8; n++) m[n] = (mmd[n] / msum) * density * vol;
 }
 
+// ---- quadratic tetrahedra (T10), host only ----
+// Nodes: the corners 0-3 with barycentric coordinates L0 = x, L1 = y, L2 = z,
+// L3 = 1 - x - y - z, then one node per edge (0,1) (0,2) (0,3) (1,2) (1,3)
+// (2,3). The gradient of corner c is (4 L_c - 1) grad L_c; of edge node
+// (a, b) 4 (L_b grad L_a + L_a grad L_b). The reference prints its tables at
+// the 4-point rule (the solve, XPBDFEM/Fem.cpp:60) and the 10-point rule (the
+// prefactored coefficients, :61) to six decimals, with the weights (:11-12);
+// every entry is the printed magnitude nearest its value, so the tables are
+// built from those literals. The rule's coordinates come from the same
+// printed numbers: 4-point rule point p has L_p = a4, the others b4; the
+// 10-point rule's points 0-3 have L_p = a10 (others b10), and points 4-9,
+// one per edge in node order, c10 on the edge's two corners and d10 on the
+// other two.
+constexpr int kT10EdgeNodes[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+
+inline double t10_bary(int np, int p, int c) {
+	if (np == 4) return p == c ? (1.341641 + 1.0) / 4.0 : (1.0 - 0.447214) / 4.0;
+	if (p < 4) return p == c ? (2.113981 + 1.0) / 4.0 : (1.0 - 0.704660) / 4.0;
+	const bool on = c == kT10EdgeNodes[p - 4][0] || c == kT10EdgeNodes[p - 4][1];
+	return on ? (0.624977 + 1.0) / 4.0 : (1.0 - 0.624977) / 4.0;
+}
+
+// ShapeFunctionGradients<Tet, 10, np>[p][n][k] for np = 4 or 10
+inline float t10_grad(int np, int p, int n, int k) {
+	static const double printed4[] = {0.447214, 0.552786, 1.341641, 1.788854, 2.341641};
+	static const double printed10[] = {0.295340, 0.375023, 0.624977, 0.704660, 1.249955,
+	                                   1.624977, 2.113981, 2.818642, 3.113981};
+	// grad L_c: e_c for c < 3, (-1, -1, -1) for c = 3
+	auto gl = [](int c, int axis) { return c == 3 ? -1.0 : (c == axis ? 1.0 : 0.0); };
+	double v;
+	if (n < 4) {
+		v = (4.0 * t10_bary(np, p, n) - 1.0) * gl(n, k);
+	} else {
+		const int a = kT10EdgeNodes[n - 4][0], b = kT10EdgeNodes[n - 4][1];
+		v = 4.0 * (t10_bary(np, p, b) * gl(a, k) + t10_bary(np, p, a) * gl(b, k));
+	}
+	const double* mag = np == 4 ? printed4 : printed10;
+	const int nm = np == 4 ? 5 : 9;
+	if (fabs(v) < 1e-3) return 0.0f;
+	int best = 0;
+	for (int i = 1; i < nm; i++)
+		if (fabs(fabs(v) - mag[i]) < fabs(fabs(v) - mag[best])) best = i;
+	return v < 0.0 ? -(float)mag[best] : (float)mag[best];
+}
+
+// QuadratureWeights<Tet, np>[p]
+inline float t10_weight(int np, int p) { return np == 4 ? 0.250000f : p < 4 ? 0.047633f : 0.134911f; }
+
+// Offsets in the 56-value T10 record (ElementParamsQuadraticTet,
+// XPBDFEM/Fem.h:61-69, flattened): Qi column-major (one inverse for the whole
+// element: the map from the corners is linear), ic.QQ[9], ic.QR[36], volume,
+// surfaceArea.
+constexpr int kT10Qi = 0, kT10QQ = 9, kT10QR = 18, kT10Vol = 54, kT10Area = 55, kT10Rec = 56;
+
+// One T10: InitTriTetFiniteElement (XPBDFEM/Fem.cpp:196-224) with the corner
+// map and GeneratePrefactoredCoefficients on the 10-point rule (:131-161). X:
+// the vertex positions in double; is: the T10's 10 indices; o: the 56-value
+// record; m[10]: each node's lumped mass (LumpsTet10: 13/472 of density x
+// volume per corner, 70/472 per edge node).
+inline void t10(const double* X, const uint32_t* is, float density, float* o, float m[10]) {
+	const float sixth = 1.0f / 6.0f;
+	float P[4][3];
+	for (int n = 0; n < 4; n++)
+		for (int k = 0; k < 3; k++) P[n][k] = (float)(X[3 * (size_t)is[n] + k] - X[3 * (size_t)is[3] + k]);
+	const M3 J = map_jacobian(P);
+	const M3 Qi = inverse3(J);
+	// every point of the 10-point rule has the map's jacobian J
+	const float detJ = det3(J);
+	float* QQ = o + kT10QQ;
+	float* QR = o + kT10QR;
+	for (int i = 0; i < 9; i++) QQ[i] = 0.0f;
+	for (int i = 0; i < 36; i++) QR[i] = 0.0f;
+	float vsum = 0.0f;
+	for (int p = 0; p < 10; p++) {
+		const float w = detJ * sixth * t10_weight(10, p);
+		float q[9][3];
+		for (int i = 0; i < 9; i++) {
+			const float dn[3] = {t10_grad(10, p, i, 0), t10_grad(10, p, i, 1), t10_grad(10, p, i, 2)};
+			for (int r = 0; r < 3; r++) {
+				const float row[3] = {Qi.c[0][r], Qi.c[1][r], Qi.c[2][r]};
+				q[i][r] = dot3(row, dn);
+			}
+		}
+		vsum += w;
+		for (int i = 0; i < 9; i++) QQ[i] += w * dot3(q[i], q[i]);
+		int head = 0;
+		for (int i = 0; i < 9; i++)
+			for (int j = i + 1; j < 9; j++) QR[head++] += w * 2.0f * dot3(q[i], q[j]);
+	}
+	for (int i = 0; i < 9; i++) QQ[i] /= vsum;
+	for (int i = 0; i < 36; i++) QR[i] /= vsum;
+	const float vol = sixth * det3(J);
+	const float area = face_area(P, 0, 1, 2) + face_area(P, 1, 3, 2) + face_area(P, 0, 2, 3) + face_area(P, 3, 1, 0);
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) o[kT10Qi + c * 3 + r] = Qi.c[c][r];
+	o[kT10Vol] = vol;
+	o[kT10Area] = area;
+	for (int n = 0; n < 10; n++) m[n] = ((n < 4 ? 13.0f : 70.0f) / 472.0f) * density * vol;
+}
+
 // The Left / Right flags of a vertex (XPBDFEM/Geo.cpp:713-727) from the AABB
 // of the node data along x: bit 0 Left, bit 1 Right, bit 4 Pickable.
 XFEM_HD uint8_t vertex_flags(float x, float mn, float mx) {

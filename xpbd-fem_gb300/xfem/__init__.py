@@ -17,6 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libxfem.so")
 
 OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT = 0, -1, -2, -3, -4, -5, -6
+ELEMENT_TYPE_MASK = 15  # flags bits 0-3 (Settings_ElementTypeMask)
+ELEMENT_T4, ELEMENT_T10, ELEMENT_H8, ELEMENT_H27 = 5, 6, 7, 8
 ENERGY_BIT = 6
 # energy ids, XPBDFEM/Settings.h:41-53
 ENERGY_PIXAR = 0
@@ -89,8 +91,11 @@ EXPORTS = [
     "xfem_step_frames_noalloc", "xfem_adjoint_forward", "xfem_adjoint_backward", "xfem_pbd_damping_coefficients",
     "xfem_get_ring_schedule", "xfem_compute_ring_schedule", "xfem_body_hex_count", "xfem_get_hex_rest_state",
     "xfem_get_hex_schedule", "xfem_compute_hex_rest_state", "xfem_compute_hex_schedule", "xfem_generate_hex_block",
+    "xfem_body_t10_count", "xfem_get_t10_rest_state", "xfem_get_t10_schedule", "xfem_compute_t10_edges",
+    "xfem_compute_t10_rest_state", "xfem_compute_t10_schedule",
 ]
 HEX_EP = 120  # floats per hex rest-state record (ElementParamsLinearHex flattened)
+T10_EP = 56  # floats per T10 rest-state record (ElementParamsQuadraticTet flattened)
 
 _lib = None
 
@@ -143,6 +148,12 @@ def lib():
         L.xfem_compute_hex_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P]
         L.xfem_compute_hex_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         L.xfem_generate_hex_block.argtypes = [u32, u32, u32, f32, f32, f32, u32, f32, P, P]
+        L.xfem_body_t10_count.argtypes = [P, u32, P, P]
+        L.xfem_get_t10_rest_state.argtypes = [P, u32, P, P, P, P]
+        L.xfem_get_t10_schedule.argtypes = [P, u32, P, P, P, P]
+        L.xfem_compute_t10_edges.argtypes = [P, u32, P, P, P]
+        L.xfem_compute_t10_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P, P]
+        L.xfem_compute_t10_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -222,11 +233,55 @@ def compute_hex_schedule(node_data, idx_data, morton=True):
     nv, nh = nd.size // 3, ix.size // 9
     rank = np.zeros(nv, np.uint32)
     order = np.zeros(nh, np.uint32)
-    cb = np.zeros(65, np.uint32)
+    cb = np.zeros(nh + 1, np.uint32)
     ncol = C.c_uint32()
     _check(lib().xfem_compute_hex_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
                                            _p(cb), C.byref(ncol)))
     return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+def compute_t10_edges(idx_data):
+    """Connectivity3d's edges of a tet mesh and GeoQuadratic3d's T10 indices
+    (no GPU): (edges[ne, 2], t10[nt, 10])."""
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nt = ix.size // 5
+    edges = np.zeros((max(6 * nt, 1), 2), np.uint32)
+    t10 = np.zeros((nt, 10), np.uint32)
+    ne = C.c_uint32()
+    _check(lib().xfem_compute_t10_edges(_p(ix), ix.size, _p(edges), _p(t10), C.byref(ne)))
+    return edges[:ne.value].copy(), t10
+
+
+def compute_t10_rest_state(node_data, idx_data, density):
+    """Host-only rest state of a tet mesh read as T10s (no GPU):
+    (x[nv, 3] double, ep[nt, 56], w[nv], flags[nv]) over all vertices (the
+    mesh's own, then one per edge)."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    edges, t10 = compute_t10_edges(ix)
+    nv, nt = nd.size // 3 + edges.shape[0], t10.shape[0]
+    x = np.zeros((nv, 3), np.float64)
+    ep = np.zeros((nt, T10_EP), np.float32)
+    w = np.zeros(nv, np.float32)
+    fl = np.zeros(nv, np.uint8)
+    _check(lib().xfem_compute_t10_rest_state(_p(nd), nd.size, _p(ix), ix.size, density, _p(x), _p(ep), _p(w),
+                                             _p(fl)))
+    return x, ep, w, fl
+
+
+def compute_t10_schedule(node_data, idx_data, morton=True):
+    """Host-only T10 schedule (no GPU), in the form of Body.t10_schedule()."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    edges, t10 = compute_t10_edges(ix)
+    nv, nt = nd.size // 3 + edges.shape[0], t10.shape[0]
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nt, np.uint32)
+    cb = np.zeros(nt + 1, np.uint32)
+    ncol = C.c_uint32()
+    _check(lib().xfem_compute_t10_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
+                                           _p(cb), C.byref(ncol)))
+    return dict(vert_rank=rank, t10_order=order, colour_t10_begin=cb[:ncol.value + 1], colours=ncol.value)
 
 
 def compute_rest_state(node_data, idx_data, density):
@@ -424,10 +479,38 @@ class Body:
         nv, nh = self.counts[body][0], self.hex_count(body)
         rank = np.zeros(nv, np.uint32)
         order = np.zeros(nh, np.uint32)
-        cb = np.zeros(65, np.uint32)
+        cb = np.zeros(nh + 1, np.uint32)
         ncol = C.c_uint32()
         _check(lib().xfem_get_hex_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def t10_count(self, body=0):
+        """(T10s, edge nodes) of a T10 body."""
+        n, ne = C.c_uint32(), C.c_uint32()
+        _check(lib().xfem_body_t10_count(self._h, body, C.byref(n), C.byref(ne)))
+        return n.value, ne.value
+
+    def t10_rest_state(self, body=0):
+        """Rest state of a T10 body: (ep[nt, 56], w[nv], t10[nt, 10], edges[ne, 2])."""
+        nv = self.counts[body][0]
+        nt, ne = self.t10_count(body)
+        ep = np.zeros((nt, T10_EP), np.float32)
+        w = np.zeros(nv, np.float32)
+        t10 = np.zeros((nt, 10), np.uint32)
+        edges = np.zeros((ne, 2), np.uint32)
+        _check(lib().xfem_get_t10_rest_state(self._h, body, _p(ep), _p(w), _p(t10), _p(edges)))
+        return ep, w, t10, edges
+
+    def t10_schedule(self, body=0):
+        """Vertex ranks, T10 order (colour-major) and colour offsets of a T10 body."""
+        nv = self.counts[body][0]
+        nt, _ = self.t10_count(body)
+        rank = np.zeros(nv, np.uint32)
+        order = np.zeros(nt, np.uint32)
+        cb = np.zeros(nt + 1, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_t10_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
+        return dict(vert_rank=rank, t10_order=order, colour_t10_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     def ring_schedule(self, body=0):
         """The ring order of a continuous-pressure body (energy 8-10)."""
