@@ -24,7 +24,9 @@ shape the configuration names.
   set-up (GPU set-up path and host set-up, 1.5M-tet mesh; 512-body batch),
   "hexes": hex mode on the same grid as 262,144 linear hexahedra (MixedSel,
   YeohSkinFast, Mixed, CubeNeo) with the oracle port's single-thread hex substep as
-  its CPU baseline,
+  its CPU baseline, "t10": quadratic-tet mode on the same mesh's 1,572,864 tets
+  read as T10s (MixedSel, YeohSkinFast) with the oracle port's single-thread
+  T10 substep as its CPU baseline,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -299,6 +301,7 @@ def run_xfem(args, world, rank, local):
     models = None if args.no_models else run_models(stream)
     setup = None if args.no_setup else run_setup(stream)
     hexes = None if args.no_hexes else run_hexes(stream)
+    t10 = None if args.no_t10 else run_t10(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -322,6 +325,7 @@ def run_xfem(args, world, rank, local):
         "models": models,
         "setup": setup,
         "hexes": hexes,
+        "t10": t10,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -483,7 +487,10 @@ def time_frames(stream, w, settings, flush, frames):
     S = w["substeps"]
     sdt = w["dt"] / S
     body = xfem.Body(w["nodes"], w["idx"], w["density"], settings, stream=C_void_p(stream.cuda_stream))
-    body.set_lock_mask(w["lock"])
+    # a T10 body has more vertices than the mesh (its edge nodes): its lock
+    # mask comes from its own rest positions by the same rule
+    from xfem import workloads as W
+    body.set_lock_mask(w["lock"] if w["lock"] is not None else W.lock_mask_axis(body.positions(), 2))
     for _ in range(3):
         body.step_frames(1, S, sdt)
     ms = []
@@ -600,6 +607,49 @@ def run_hexes(stream, frames=5, cpu_budget_s=6.0):
             "vs_tet_mesh_of_the_same_grid": "each hex covers the 6 tets of one cube of the throughput mesh"}
 
 
+def run_t10(stream, frames=5, cpu_budget_s=6.0):
+    """Quadratic-tet mode: the throughput mesh's 1,572,864 tets read as T10s
+    (GeoQuadratic3d: a node on each of the 1.9 M edges, 10-node elements on
+    the 4-point rule) with MixedSel and YeohSkinFast, device-timed frames of
+    20 substeps with L2 flushed between frames; and the oracle port of the
+    reference's T10 substep on one host thread on the same mesh (a bounded
+    sample of substeps) as the CPU baseline."""
+    import torch
+
+    import oracle
+    import xfem
+    from xfem import workloads as W
+    w = dict(W.throughput(), lock=None)
+    nt = w["idx"].size // 5
+    S = w["substeps"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    solve = (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT | xfem.ELEMENT_T10
+    cases = (("mixed_sel", dict(w["settings"], flags=w["settings"]["flags"] | xfem.ELEMENT_T10)),
+             ("yeoh_skin_fast", dict(w["settings"], flags=(xfem.ENERGY_YEOH_SKIN_FAST << xfem.ENERGY_BIT) | solve,
+                                     compliance=3.2e-4)))
+    out = {}
+    for key, s_ in cases:
+        r = time_frames(stream, w, s_, flush, frames)
+        r["value"] = nt * S / (r["ms_per_frame"] / 1e3)
+        r.pop("sync_mode")
+        r.pop("block")
+        out[key] = r
+    # CPU: the oracle's float restatement, one thread, the reference's
+    # algorithm in the GPU's T10 order
+    q = oracle.Quadratic(w["nodes"], w["idx"], w["density"])
+    order = q.schedule()["tet_order"]
+    p = oracle.params_from_settings(w["settings"], w["dt"] / S, lock=False)
+    X, wi = q.X0.copy(), q.w.copy()
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget_s or n == 0:
+        X, V, wi, _ = q.substeps(X, np.zeros_like(X), wi, order, 1, p)
+        n += 1
+    cpu = nt * n / (time.perf_counter() - t0)
+    return {"workload": w["name"] + " as T10s", "unit": "T10-substeps/s", "vertices": int(q.X0.shape[0]), **out,
+            "cpu_baseline": {"value": cpu, "unit": "T10-substeps/s", "cores": 1, "kind": "port",
+                             "sample": "%d substeps of the same mesh (MixedSel)" % n}}
+
+
 def C_void_p(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -628,6 +678,7 @@ def main():
     ap.add_argument("--no-models", action="store_true")
     ap.add_argument("--no-setup", action="store_true")
     ap.add_argument("--no-hexes", action="store_true")
+    ap.add_argument("--no-t10", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")

@@ -695,7 +695,7 @@ int build_elements(xfem_body* h) {
 	if (t10)
 		for (int p = 0; p < 4; p++)
 			for (int n = 0; n < 10; n++)
-				for (int k = 0; k < 3; k++) g4[(p * 10 + n) * 3 + k] = rest::t10_grad(4, p, n, k);
+				for (int k = 0; k < 3; k++) g4[(p * 10 + n) * 3 + k] = rest::t10_tables().g4[p][n][k];
 	XCUDA(h->el_vid.alloc(vid.size()));
 	XCUDA(h->el_rec.alloc(rec.size()));
 	XCUDA(h->el_cb.alloc(cb.size()));
@@ -1590,7 +1590,7 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
 				for (int n = 0; n < 9; n++)
 					for (int c = 0; c < 3; c++)
-						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::t10_grad(4, p, n, r) * P[n][c];
+						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::t10_tables().g4[p][n][r] * P[n][c];
 				const float* qi = e + rest::kT10Qi;
 				for (int c = 0; c < 3; c++)
 					for (int r = 0; r < 3; r++) F[c][r] = qi[r] * Dm[c][0] + qi[3 + r] * Dm[c][1] + qi[6 + r] * Dm[c][2];

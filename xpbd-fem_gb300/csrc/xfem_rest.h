@@ -296,6 +296,27 @@ inline float t10_grad(int np, int p, int n, int k) {
 // QuadratureWeights<Tet, np>[p]
 inline float t10_weight(int np, int p) { return np == 4 ? 0.250000f : p < 4 ? 0.047633f : 0.134911f; }
 
+// The tables built once: g4[p][n][k] at the 4-point rule, g10 at the 10-point
+// rule, w10 its weights.
+struct T10Tables {
+	float g4[4][10][3], g10[10][10][3], w10[10];
+};
+inline const T10Tables& t10_tables() {
+	static const T10Tables t = [] {
+		T10Tables r;
+		for (int p = 0; p < 10; p++) {
+			r.w10[p] = t10_weight(10, p);
+			for (int n = 0; n < 10; n++)
+				for (int k = 0; k < 3; k++) {
+					if (p < 4) r.g4[p][n][k] = t10_grad(4, p, n, k);
+					r.g10[p][n][k] = t10_grad(10, p, n, k);
+				}
+		}
+		return r;
+	}();
+	return t;
+}
+
 // Offsets in the 56-value T10 record (ElementParamsQuadraticTet,
 // XPBDFEM/Fem.h:61-69, flattened): Qi column-major (one inverse for the whole
 // element: the map from the corners is linear), ic.QQ[9], ic.QR[36], volume,
@@ -316,16 +337,17 @@ inline void t10(const double* X, const uint32_t* is, float density, float* o, fl
 	const M3 Qi = inverse3(J);
 	// every point of the 10-point rule has the map's jacobian J
 	const float detJ = det3(J);
+	const T10Tables& tb = t10_tables();
 	float* QQ = o + kT10QQ;
 	float* QR = o + kT10QR;
 	for (int i = 0; i < 9; i++) QQ[i] = 0.0f;
 	for (int i = 0; i < 36; i++) QR[i] = 0.0f;
 	float vsum = 0.0f;
 	for (int p = 0; p < 10; p++) {
-		const float w = detJ * sixth * t10_weight(10, p);
+		const float w = detJ * sixth * tb.w10[p];
 		float q[9][3];
 		for (int i = 0; i < 9; i++) {
-			const float dn[3] = {t10_grad(10, p, i, 0), t10_grad(10, p, i, 1), t10_grad(10, p, i, 2)};
+			const float* dn = tb.g10[p][i];
 			for (int r = 0; r < 3; r++) {
 				const float row[3] = {Qi.c[0][r], Qi.c[1][r], Qi.c[2][r]};
 				q[i][r] = dot3(row, dn);
