@@ -159,6 +159,19 @@ def lib():
         L.orc_t10_volume_d.argtypes = [P, u32, P, P]
         L.orc_t10_volume_d.restype = C.c_double
         L.orc_t10_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.orc_h27_tables.argtypes = [P, P, P, P, P]
+        L.orc_h27_mesh.argtypes = [P, u32, u32, P, P, P, P, P]
+        L.orc_h27_init_rest_f.argtypes = [P, u32, P, u32, P, u32, P, u32, P, C.c_float, P, P, P, P]
+        L.orc_h27_init_rest_d.argtypes = [P, u32, P, u32, P, u32, P, u32, P, C.c_double, P, P, P, P]
+        L.orc_solve_h27_f.argtypes = [P, P, P, P, P]
+        L.orc_solve_h27_d.argtypes = [P, P, P, P, P]
+        L.orc_h27_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_h27_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_h27_volume_f.argtypes = [P, u32, P, P]
+        L.orc_h27_volume_f.restype = C.c_float
+        L.orc_h27_volume_d.argtypes = [P, u32, P, P]
+        L.orc_h27_volume_d.restype = C.c_double
+        L.orc_h27_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -509,4 +522,88 @@ def solve_t10(X, w, ep, params, O, dtype=np.float32):
     f = lib().orc_solve_t10_f if dtype == np.float32 else lib().orc_solve_t10_d
     if f(_p(X), _p(O), _p(w), _p(ep), C.byref(params)):
         raise ValueError("energy model not covered on quadratic tets")
+    return X
+
+
+H27_EP = 703  # values per H27 rest-state record (ElementParamsQuadraticHex flattened)
+
+
+def h27_tables():
+    """(g8[8][27][3], g27[27][27][3], n27[27][27], map27[27][8][3], w27[27])."""
+    g8, g27 = np.zeros((8, 27, 3), np.float32), np.zeros((27, 27, 3), np.float32)
+    n27, map27, w27 = np.zeros((27, 27), np.float32), np.zeros((27, 8, 3), np.float32), np.zeros(27, np.float32)
+    lib().orc_h27_tables(_p(g8), _p(g27), _p(n27), _p(map27), _p(w27))
+    return g8, g27, n27, map27, w27
+
+
+def h27_mesh(hexes, nv):
+    """Connectivity3d's edges and quads of a hex mesh and GeoQuadratic3d's H27
+    indices: (edges[ne, 2], quads[nq, 4], h27[nh, 27])."""
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    nh = hexes.shape[0]
+    edges = np.zeros((max(12 * nh, 1), 2), np.uint32)
+    quads = np.zeros((max(6 * nh, 1), 4), np.uint32)
+    h27 = np.zeros((nh, 27), np.uint32)
+    ne, nq = C.c_uint32(), C.c_uint32()
+    if lib().orc_h27_mesh(_p(hexes), nh, nv, _p(edges), C.byref(ne), _p(quads), C.byref(nq), _p(h27)):
+        raise MemoryError("mesh enumeration failed")
+    return edges[:ne.value].copy(), quads[:nq.value].copy(), h27
+
+
+class QuadraticHex:
+    """A hex mesh as GeoQuadratic3d builds it: H27 elements."""
+
+    def __init__(self, nodes, idx, density, dtype=np.float32):
+        nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+        self.hexes, self.nv = parse_hexes(idx)
+        self.edges, self.quads, self.h27 = h27_mesh(self.hexes, self.nv)
+        nh = self.hexes.shape[0]
+        n = self.nv + self.edges.shape[0] + self.quads.shape[0] + nh
+        self.X0 = np.zeros((n, 3), np.float64)
+        self.ep = np.zeros((nh, H27_EP), dtype)
+        self.w = np.zeros(n, dtype)
+        self.flags = np.zeros(n, np.uint8)
+        f = lib().orc_h27_init_rest_f if dtype == np.float32 else lib().orc_h27_init_rest_d
+        f(_p(nodes), self.nv, _p(self.hexes), nh, _p(self.edges), self.edges.shape[0], _p(self.quads),
+          self.quads.shape[0], _p(self.h27), density, _p(self.X0), _p(self.ep), _p(self.w), _p(self.flags))
+        self.dtype = dtype
+
+    def schedule(self, morton=1):
+        X = self.X0.astype(np.float32)
+        n, nh = X.shape[0], self.h27.shape[0]
+        rank = np.zeros(n, np.uint32)
+        order = np.zeros(nh, np.uint32)
+        cb = np.zeros(nh + 1, np.uint32)
+        ncol = C.c_uint32()
+        if lib().orc_h27_schedule(_p(X), n, _p(self.h27), nh, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
+            raise ValueError("H27 schedule needs more than 4096 colours")
+        return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def substeps(self, X, V, w, order, nsub, params, lock_mask=None):
+        X = np.array(X, np.float64).reshape(-1).copy()
+        V = np.array(V, np.float64).reshape(-1).copy()
+        w = np.array(w, self.dtype).copy()
+        order = np.ascontiguousarray(order, np.uint32)
+        lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+        contact = np.zeros(w.size, np.uint8)
+        f = lib().orc_h27_substeps_f if self.dtype == np.float32 else lib().orc_h27_substeps_d
+        if f(w.size, _p(X), _p(V), _p(w), _p(lm), self.h27.shape[0], _p(self.h27), _p(self.ep), _p(order), nsub,
+             C.byref(params), _p(contact)):
+            raise ValueError("energy model not covered on quadratic hexes")
+        return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+    def volume(self, X):
+        X = np.ascontiguousarray(X, np.float64).reshape(-1)
+        f = lib().orc_h27_volume_f if self.dtype == np.float32 else lib().orc_h27_volume_d
+        return f(_p(X), self.h27.shape[0], _p(self.h27), _p(self.ep))
+
+
+def solve_h27(X, w, ep, params, O, dtype=np.float32):
+    X = np.array(X, np.float64).reshape(27, 3).copy()
+    O = np.ascontiguousarray(O, np.float64).reshape(27, 3)
+    w = np.ascontiguousarray(w, dtype)
+    ep = np.ascontiguousarray(ep, dtype)
+    f = lib().orc_solve_h27_f if dtype == np.float32 else lib().orc_solve_h27_d
+    if f(_p(X), _p(O), _p(w), _p(ep), C.byref(params)):
+        raise ValueError("energy model not covered on quadratic hexes")
     return X

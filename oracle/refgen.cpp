@@ -76,6 +76,18 @@
  *   qordered / qdamped (as hordered / hdamped) < torder.u32
  *   qsolve seed count energy simultaneous compliance poisson dt
  *       SolveElement (XPBDFEM/Fem.cpp:893) on `count` seeded random T10s.
+ *
+ * Quadratic hexes: the same commands prefixed with `Q` build GeoQuadratic3d
+ * on a GenerateHexBlock mesh (H27s, XPBDFEM/Geo.cpp:902-933):
+ *   Qinit W H D sx sy sz pattern wonkiness density
+ *       all vertex positions (corners, edge midpoints, face centres, hex
+ *       centres), the H27 indices, the per-H27 rest state (703 values:
+ *       qcLo.Ji[8], qcLo.w[8], qcHi.Ji[27], qcHi.w[27], ic.QQ[26],
+ *       ic.QR[325], volume, surfaceArea), w, flags, hOrder and
+ *       CalculateVolume.
+ *   Qordered / Qdamped (as hordered / hdamped) < horder.u32
+ *   Qsolve seed count energy simultaneous compliance poisson dt
+ *       SolveElement (XPBDFEM/Fem.cpp:897) on `count` seeded random H27s.
  */
 #include <cstdio>
 #include <cstdlib>
@@ -221,6 +233,20 @@ static void t10_record(const ElementParamsQuadraticTet& e, float* o) {
 	o[55] = e.surfaceArea;
 }
 
+// ElementParamsQuadraticHex (XPBDFEM/Fem.h:101-111) flattened, 703 values.
+static void h27_record(const ElementParamsQuadraticHex& e, float* o) {
+	for (int p = 0; p < 8; p++)
+		for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[9 * p + c * 3 + r] = e.qcLo.Ji[p][c][r];
+	for (int p = 0; p < 8; p++) o[72 + p] = e.qcLo.w[p];
+	for (int p = 0; p < 27; p++)
+		for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[80 + 9 * p + c * 3 + r] = e.qcHi.Ji[p][c][r];
+	for (int p = 0; p < 27; p++) o[323 + p] = e.qcHi.w[p];
+	for (int k = 0; k < 26; k++) o[350 + k] = e.ic.QQ[k];
+	for (int k = 0; k < 325; k++) o[376 + k] = e.ic.QR[k];
+	o[701] = e.volume;
+	o[702] = e.surfaceArea;
+}
+
 template <typename G>
 static void dump_state(G* g, const char* xname, const char* vname) {
 	uint32_t nv = g->vertCount;
@@ -233,12 +259,12 @@ static void dump_state(G* g, const char* xname, const char* vname) {
 
 int main(int argc, char** argv) {
 	if (argc < 2) { fprintf(stderr, "usage: refgen <cmd> ...\n"); return 2; }
-	const bool hex = argv[1][0] == 'h', quad = argv[1][0] == 'q';
-	const char* cmd = argv[1] + (hex || quad ? 1 : 0);
+	const bool hex = argv[1][0] == 'h', quad = argv[1][0] == 'q', h27 = argv[1][0] == 'Q';
+	const char* cmd = argv[1] + (hex || quad || h27 ? 1 : 0);
 	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
 
-	if (quad && (!strcmp(cmd, "init") || !strcmp(cmd, "ordered") || !strcmp(cmd, "damped"))) {
+	if ((quad || h27) && (!strcmp(cmd, "init") || !strcmp(cmd, "ordered") || !strcmp(cmd, "damped"))) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
 		uint32_t W = U(2), H = U(3), D = U(4);
 		vec3 scale(F(5), F(6), F(7));
@@ -246,11 +272,35 @@ int main(int argc, char** argv) {
 		float wonk = F(9), density = F(10);
 		int a = 11;
 		const float* nodes; uint32_t nodeCount; const uint32_t* idx; uint32_t idxCount;
-		GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		if (h27)
+			GenerateHexBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
+		else
+			GenerateTetBlock(alloc, W, H, D, scale, pattern, wonk, &nodes, &nodeCount, &idx, &idxCount);
 		GeoQuadratic3d* g = alloc->New<GeoQuadratic3d>();
 		g->Init(alloc, density, nodes, nodeCount, idx, idxCount, false);
 		emit("nodes", 'f', nodes, nodeCount);
 		emit("idx", 'I', idx, idxCount);
+		if (h27 && !strcmp(cmd, "init")) {
+			uint32_t nh = g->con.hexCount, nv = g->vertCount;
+			std::vector<float> ep(nh * 703);
+			std::vector<uint32_t> hi(nh * 27);
+			for (uint32_t i = 0; i < nh; i++) {
+				h27_record(g->h[i].ep, &ep[i * 703]);
+				for (int k = 0; k < 27; k++) hi[i * 27 + k] = g->h[i].i[k];
+			}
+			std::vector<double> x0(nv * 3);
+			for (uint32_t i = 0; i < nv; i++) for (int k = 0; k < 3; k++) x0[i * 3 + k] = g->X[i][k];
+			std::vector<uint8_t> flags(g->flags, g->flags + nv);
+			emit("x0", 'd', x0.data(), x0.size());
+			emit("h27_idx", 'I', hi.data(), hi.size());
+			emit("h27ep", 'f', ep.data(), ep.size());
+			emit("w", 'f', g->w, nv);
+			emit("vflags", 'B', flags.data(), nv);
+			emit("horder", 'I', g->hOrder, nh);
+			float vol = g->CalculateVolume();
+			emit("volume", 'f', &vol, 1);
+			return 0;
+		}
 		if (!strcmp(cmd, "init")) {
 			uint32_t nt = g->con.tetCount, nv = g->vertCount;
 			std::vector<float> ep(nt * 56);
@@ -276,7 +326,8 @@ int main(int argc, char** argv) {
 		float compliance = F(a++), poisson = F(a++), gx = F(a++), gy = F(a++), dt = F(a++);
 		uint32_t nsub = U(a++), lockLeft = U(a++);
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
-		s.flags = (s.flags & ~(Settings_ElementTypeMask << Settings_ElementTypeBit)) | (Element_T10 << Settings_ElementTypeBit);
+		s.flags = (s.flags & ~(Settings_ElementTypeMask << Settings_ElementTypeBit)) |
+		          ((h27 ? Element_H27 : Element_T10) << Settings_ElementTypeBit);
 		if (!strcmp(cmd, "damped")) {
 			s.damping = F(a++);
 			s.pbdDamping = F(a++);
@@ -298,8 +349,9 @@ int main(int argc, char** argv) {
 			if (a < argc) s.volumePasses = U(a++);
 		}
 		uint32_t n = 0;
-		if (fread(&n, 4, 1, stdin) != 1 || n != g->con.tetCount) { fprintf(stderr, "bad order\n"); return 3; }
-		if (fread(g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+		const uint32_t nel = h27 ? g->con.hexCount : g->con.tetCount;
+		if (fread(&n, 4, 1, stdin) != 1 || n != nel) { fprintf(stderr, "bad order\n"); return 3; }
+		if (fread(h27 ? g->hOrder : g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
 		Manipulator manip;
 		manip.pickedGeo = nullptr;
 		for (uint32_t k = 0; k < nsub; k++) {
@@ -445,6 +497,60 @@ int main(int argc, char** argv) {
 		dump_state(g, "xn", "vn");
 		float vol = g->CalculateVolume();
 		emit("volume", 'f', &vol, 1);
+		return 0;
+	}
+
+	if (h27 && !strcmp(cmd, "solve")) {
+		g_rng = strtoull(argv[2], 0, 10);
+		uint32_t count = U(3), energy = U(4), simul = U(5);
+		float compliance = F(6), poisson = F(7), dt = F(8);
+		Settings s = make_settings(energy, simul, compliance, poisson, 0.0f, 0.0f, 0);
+		std::vector<double> xin(count * 81), xout(count * 81), rest(count * 81);
+		std::vector<float> win(count * 27), epo(count * 703);
+		for (uint32_t t = 0; t < count; t++) {
+			dvec3 C[8], X0[27], X[27], O[27];
+			float m[27] = {0}, w[27];
+			// Rest corners as `hsolve`'s random hex; node (i, j, k) of the
+			// 3x3x3 grid at the trilinear point of the corners
+			double ext[3];
+			for (int k = 0; k < 3; k++) ext[k] = 0.02 + 0.2 * urand();
+			for (int n = 0; n < 8; n++)
+				for (int k = 0; k < 3; k++) C[n][k] = (double)(float)(ext[k] * (((n >> k) & 1) + 0.1 * (urand() - 0.5)));
+			for (int n = 0; n < 27; n++) {
+				const double u[3] = {0.5 * (n % 3), 0.5 * ((n / 3) % 3), 0.5 * (n / 9)};
+				X0[n] = dvec3(0.0);
+				for (int c = 0; c < 8; c++) {
+					const double f = (c & 1 ? u[0] : 1.0 - u[0]) * (c & 2 ? u[1] : 1.0 - u[1]) * (c & 4 ? u[2] : 1.0 - u[2]);
+					X0[n] += f * C[c];
+				}
+			}
+			uint32_t is[27];
+			for (int n = 0; n < 27; n++) is[n] = n;
+			ElementParamsQuadraticHex ep;
+			InitFiniteElement(X0, is, 1000.0f, m, &ep);
+			uint32_t kind = t % 8;
+			double amp = kind < 4 ? 0.05 : kind < 6 ? 0.4 : 1.5;
+			double sc = (ext[0] + ext[1] + ext[2]) / 3.0;
+			for (int n = 0; n < 27; n++) {
+				for (int k = 0; k < 3; k++) X[n][k] = X0[n][k] + amp * sc * (urand() - 0.5);
+				O[n] = X0[n];
+				w[n] = (float)(0.5 + 2.0 * urand());
+			}
+			if (kind == 6) { dvec3 tmp = X[0]; X[0] = X[26]; X[26] = tmp; }  // inverted
+			if (kind == 7) { w[0] = 0.0f; w[26] = 0.0f; }
+			for (int n = 0; n < 27; n++) {
+				win[t * 27 + n] = w[n];
+				for (int k = 0; k < 3; k++) { xin[t * 81 + n * 3 + k] = X[n][k]; rest[t * 81 + n * 3 + k] = X0[n][k]; }
+			}
+			SolveElement(dt, X, O, w, is, ep, s);
+			for (int n = 0; n < 27; n++) for (int k = 0; k < 3; k++) xout[t * 81 + n * 3 + k] = X[n][k];
+			h27_record(ep, &epo[t * 703]);
+		}
+		emit("rest", 'd', rest.data(), rest.size());
+		emit("h27ep", 'f', epo.data(), epo.size());
+		emit("xin", 'd', xin.data(), xin.size());
+		emit("w", 'f', win.data(), win.size());
+		emit("xout", 'd', xout.data(), xout.size());
 		return 0;
 	}
 

@@ -176,6 +176,79 @@ void orc_t10_tables(float* g4, float* g10, float* w10) {
 	}
 }
 
+/* The 27-node hex's tables (XPBDFEM/Fem.cpp:16-18, 41-44, 70-73). Nodes and
+ * points are numbered i + 3j + 9k (i + 2j + 4k on the 2x2x2 rule) on the
+ * 1-D nodes -1, 0, 1; the 1-D shape functions are x (x - 1) / 2, 1 - x^2 and
+ * x (x + 1) / 2. The reference's generator evaluated them in double at the
+ * 1-D Gauss points and weights as printed to six decimals (0.774597 and 0
+ * on the 3-point rule with weights 0.555556 and 0.888889; 0.577350 on the
+ * 2-point rule) and printed each entry to six decimals: that method gives
+ * every printed entry, where the exact Gauss values miss some. */
+static const double h27_x3[3] = {-0.774597, 0.0, 0.774597};
+static const double h27_x2[2] = {-0.577350, 0.577350};
+static const double h27_w3[3] = {0.555556, 0.888889, 0.555556};
+
+static float h27_round6(double v) { return (float)(nearbyint(v * 1e6) / 1e6); }
+
+static double h27_q(int i, double x) { return i == 0 ? x * (x - 1) / 2 : i == 1 ? (1 - x) * (1 + x) : x * (x + 1) / 2; }
+static double h27_dq(int i, double x) { return i == 0 ? x - 0.5 : i == 1 ? -2 * x : x + 0.5; }
+
+/* the coordinates of point p of the np-point rule (np = 8 or 27) */
+static void h27_point(int np, int p, double x[3]) {
+	if (np == 27) {
+		x[0] = h27_x3[p % 3], x[1] = h27_x3[(p / 3) % 3], x[2] = h27_x3[p / 9];
+	} else {
+		x[0] = h27_x2[p & 1], x[1] = h27_x2[(p >> 1) & 1], x[2] = h27_x2[p >> 2];
+	}
+}
+
+/* ShapeFunctionGradients<Hex, 27, np>[p][n][k] */
+static float h27_g(int np, int p, int n, int k) {
+	double x[3];
+	h27_point(np, p, x);
+	const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+	double v = 1.0;
+	for (int a = 0; a < 3; a++) v *= a == k ? h27_dq(ix[a], x[a]) : h27_q(ix[a], x[a]);
+	return h27_round6(v);
+}
+
+/* ShapeFunctions<Hex, 27, 27>[p][n] */
+static float h27_n(int p, int n) {
+	double x[3];
+	h27_point(27, p, x);
+	return h27_round6(h27_q(n % 3, x[0]) * h27_q((n / 3) % 3, x[1]) * h27_q(n / 9, x[2]));
+}
+
+/* ShapeFunctionGradients<Hex, 8, 27>[p][n][k]: the corner map at the 3x3x3 points */
+static float h27_map_g(int p, int n, int k) {
+	double x[3];
+	h27_point(27, p, x);
+	double v = 1.0;
+	for (int a = 0; a < 3; a++) {
+		const int b = (n >> a) & 1;
+		v *= a == k ? (b ? 0.5 : -0.5) : (b ? (1 + x[a]) / 2 : (1 - x[a]) / 2);
+	}
+	return h27_round6(v);
+}
+
+/* QuadratureWeights<Hex, 27>[p] */
+static float h27_w(int p) { return h27_round6(h27_w3[p % 3] * h27_w3[(p / 3) % 3] * h27_w3[p / 9]); }
+
+void orc_h27_tables(float* g8, float* g27, float* n27, float* map27, float* w27) {
+	for (int p = 0; p < 27; p++) {
+		w27[p] = h27_w(p);
+		for (int n = 0; n < 27; n++) {
+			n27[27 * p + n] = h27_n(p, n);
+			for (int k = 0; k < 3; k++) {
+				g27[81 * p + 3 * n + k] = h27_g(27, p, n, k);
+				if (p < 8) g8[81 * p + 3 * n + k] = h27_g(8, p, n, k);
+			}
+		}
+		for (int n = 0; n < 8; n++)
+			for (int k = 0; k < 3; k++) map27[24 * p + 3 * n + k] = h27_map_g(p, n, k);
+	}
+}
+
 /* ---- float instantiation (reference semantics) ---------------------------- */
 #define R float
 #define SFX _f
@@ -188,6 +261,7 @@ void orc_t10_tables(float* g4, float* g10, float* w10) {
 #include "xfem_oracle_real.inc"
 #include "xfem_oracle_hex.inc"
 #include "xfem_oracle_t10.inc"
+#include "xfem_oracle_h27.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -209,6 +283,7 @@ void orc_t10_tables(float* g4, float* g10, float* w10) {
 #include "xfem_oracle_real.inc"
 #include "xfem_oracle_hex.inc"
 #include "xfem_oracle_t10.inc"
+#include "xfem_oracle_h27.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -733,6 +808,162 @@ done:
 	free(lst);
 	free(base);
 	return rc;
+}
+
+int orc_h27_mesh(const uint32_t* hexes, uint32_t nh, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* quads,
+                 uint32_t* nquads, uint32_t* h27) {
+	static const int he[12][2] = {{0, 1}, {0, 2}, {0, 4}, {1, 3}, {1, 5}, {2, 3}, {2, 6}, {3, 7}, {4, 5}, {4, 6}, {5, 7}, {6, 7}};
+	static const int hq[6][4] = {{0, 1, 3, 2}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 2, 6, 4}, {1, 3, 7, 5}};
+	const size_t ni = 12 * (size_t)nh, nqi = 6 * (size_t)nh;
+	uint32_t* eoff = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* ecnt = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* eup = (uint32_t*)malloc(4 * (ni ? ni : 1));
+	uint32_t* elst = (uint32_t*)malloc(4 * (ni ? ni : 1));
+	uint32_t* ebase = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qoff = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qcnt = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qv = (uint32_t*)malloc(16 * (nqi ? nqi : 1));
+	uint32_t* qlst = (uint32_t*)malloc(4 * (nqi ? nqi : 1));
+	uint32_t* qbase = (uint32_t*)calloc((size_t)nv + 1, 4);
+	int rc = -1;
+	if (!eoff || !ecnt || !eup || !elst || !ebase || !qoff || !qcnt || !qv || !qlst || !qbase) goto done;
+	/* edge instances under their lower vertex, in stream order
+	 * (XPBDFEM/Connectivity.cpp:384-394, 448-459) */
+	for (uint32_t h = 0; h < nh; h++)
+		for (int k = 0; k < 12; k++) {
+			const uint32_t a = hexes[8 * (size_t)h + he[k][0]], b = hexes[8 * (size_t)h + he[k][1]];
+			eoff[(a < b ? a : b) + 1]++;
+		}
+	for (uint32_t v = 0; v < nv; v++) eoff[v + 1] += eoff[v];
+	for (uint32_t h = 0; h < nh; h++)
+		for (int k = 0; k < 12; k++) {
+			const uint32_t a = hexes[8 * (size_t)h + he[k][0]], b = hexes[8 * (size_t)h + he[k][1]];
+			const uint32_t lo = a < b ? a : b, id = 12 * h + (uint32_t)k;
+			eup[id] = a < b ? b : a;
+			elst[eoff[lo] + ecnt[lo]++] = id;
+		}
+	/* quad instances rotated to their smallest vertex, filed under it
+	 * (:410-422, 460-465) */
+	for (uint32_t h = 0; h < nh; h++)
+		for (int f = 0; f < 6; f++) {
+			uint32_t vs[4], best = 0;
+			for (int j = 0; j < 4; j++) vs[j] = hexes[8 * (size_t)h + hq[f][j]];
+			for (int j = 1; j < 4; j++)
+				if (vs[j] < vs[best]) best = (uint32_t)j;
+			qoff[vs[best] + 1]++;
+		}
+	for (uint32_t v = 0; v < nv; v++) qoff[v + 1] += qoff[v];
+	for (uint32_t h = 0; h < nh; h++)
+		for (int f = 0; f < 6; f++) {
+			uint32_t vs[4], best = 0;
+			for (int j = 0; j < 4; j++) vs[j] = hexes[8 * (size_t)h + hq[f][j]];
+			for (int j = 1; j < 4; j++)
+				if (vs[j] < vs[best]) best = (uint32_t)j;
+			const uint32_t id = 6 * h + (uint32_t)f;
+			for (int j = 0; j < 4; j++) qv[4 * (size_t)id + j] = vs[(best + (uint32_t)j) % 4];
+			qlst[qoff[vs[best]] + qcnt[vs[best]]++] = id;
+		}
+	/* duplicates replaced by the list's last entry (:486-530); a quad is a
+	 * duplicate in either winding */
+	for (uint32_t v = 0; v < nv; v++) {
+		uint32_t* L = elst + eoff[v];
+		for (uint32_t j = 0; j < ecnt[v]; j++)
+			for (uint32_t k = j + 1; k < ecnt[v]; k++)
+				if (eup[L[j]] == eup[L[k]]) {
+					L[k] = L[ecnt[v] - 1];
+					--ecnt[v];
+					--k;
+				}
+		uint32_t* Q = qlst + qoff[v];
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (uint32_t k = j + 1; k < qcnt[v]; k++) {
+				const uint32_t* a = qv + 4 * (size_t)Q[j];
+				const uint32_t* b = qv + 4 * (size_t)Q[k];
+				if ((a[1] == b[1] && a[2] == b[2] && a[3] == b[3]) || (a[1] == b[3] && a[2] == b[2] && a[3] == b[1])) {
+					Q[k] = Q[qcnt[v] - 1];
+					--qcnt[v];
+					--k;
+				}
+			}
+	}
+	{
+		uint32_t ne = 0, nq = 0;
+		for (uint32_t v = 0; v < nv; v++) {
+			ebase[v] = ne;
+			for (uint32_t j = 0; j < ecnt[v]; j++) {
+				edges[2 * (size_t)ne] = v;
+				edges[2 * (size_t)ne + 1] = eup[elst[eoff[v] + j]];
+				ne++;
+			}
+			qbase[v] = nq;
+			for (uint32_t j = 0; j < qcnt[v]; j++) {
+				for (int k = 0; k < 4; k++) quads[4 * (size_t)nq + k] = qv[4 * (size_t)qlst[qoff[v] + j] + k];
+				nq++;
+			}
+		}
+		*nedges = ne;
+		*nquads = nq;
+		/* GeoQuadratic3d's H27 indices (XPBDFEM/Geo.cpp:904-931): node
+		 * i + 3j + 9k of the 3x3x3 grid; EdgeFromVerts / QuadFromVerts
+		 * (XPBDFEM/Connectivity.cpp:587-611) */
+		if (h27)
+			for (uint32_t h = 0; h < nh; h++) {
+				const uint32_t* c = hexes + 8 * (size_t)h;
+				uint32_t* o = h27 + 27 * (size_t)h;
+				for (int n = 0; n < 27; n++) {
+					const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+					int mid = 0, lo = 0, hi = 0;
+					for (int a = 0; a < 3; a++) {
+						mid += ix[a] == 1;
+						lo |= (ix[a] == 2) << a; /* corner bits of the fixed axes */
+						hi |= (ix[a] == 1) << a; /* the free axes */
+					}
+					if (mid == 0) {
+						o[n] = c[lo];
+					} else if (mid == 1) {
+						const int f = hi == 1 ? 1 : hi == 2 ? 2 : 4;
+						const uint32_t a = c[lo], b = c[lo | f];
+						const uint32_t l = a < b ? a : b, u = a < b ? b : a;
+						uint32_t e = 0;
+						while (edges[2 * (size_t)(ebase[l] + e) + 1] != u) e++;
+						o[n] = nv + ebase[l] + e;
+					} else if (mid == 2) {
+						const int f1 = hi & 1 ? 1 : 2, f2 = hi & 4 ? 4 : 2;
+						const uint32_t vs[4] = {c[lo], c[lo | f1], c[lo | f1 | f2], c[lo | f2]};
+						uint32_t best = 0;
+						for (int j = 1; j < 4; j++)
+							if (vs[j] < vs[best]) best = (uint32_t)j;
+						const uint32_t v0 = vs[best], v1 = vs[(best + 1) % 4], v2 = vs[(best + 2) % 4], v3 = vs[(best + 3) % 4];
+						uint32_t q = 0;
+						for (;; q++) {
+							const uint32_t* Q = quads + 4 * (size_t)(qbase[v0] + q);
+							if ((Q[1] == v1 && Q[2] == v2 && Q[3] == v3) || (Q[1] == v3 && Q[2] == v2 && Q[3] == v1)) break;
+						}
+						o[n] = nv + ne + qbase[v0] + q;
+					} else {
+						o[n] = nv + ne + nq + h;
+					}
+				}
+			}
+	}
+	rc = 0;
+done:
+	free(eoff);
+	free(ecnt);
+	free(eup);
+	free(elst);
+	free(ebase);
+	free(qoff);
+	free(qcnt);
+	free(qv);
+	free(qlst);
+	free(qbase);
+	return rc;
+}
+
+int orc_h27_schedule(const float* nodes, uint32_t nv, const uint32_t* h27, uint32_t nh, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours) {
+	return elem_schedule(nodes, nv, h27, nh, 27, morton, vert_rank, order, colour_begin, ncolours);
 }
 
 int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t mode, uint32_t morton,

@@ -229,6 +229,40 @@ double orc_t10_volume_d(const double* X, uint32_t nt, const uint32_t* t10, const
 int orc_t10_schedule(const float* nodes, uint32_t nv, const uint32_t* t10, uint32_t nt, uint32_t morton,
                      uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours);
 
+/* ---- quadratic hexahedra (H27) ---- */
+/* ElementParamsQuadraticHex (XPBDFEM/Fem.h:101-111) flattened: qcLo.Ji[p]
+ * [9p ..], qcLo.w[p] [72 + p], qcHi.Ji[p] [80 + 9p ..], qcHi.w[p] [323 + p],
+ * ic.QQ[26] [350..375], ic.QR[325] [376..700], volume [701], surfaceArea
+ * [702]. */
+#define ORC_EPH27 703
+/* The H27 tables: g8[8][27][3], g27[27][27][3], n27[27][27], the corner
+ * map's gradients at the 27 points map27[27][8][3], w27[27]. */
+void orc_h27_tables(float* g8, float* g27, float* n27, float* map27, float* w27);
+/* Connectivity3d's edges (2 each, capacity 24 nh) and quads (4 each, the
+ * smallest vertex first, capacity 24 nh) of a hex mesh, and GeoQuadratic3d's
+ * H27 indices (27 per hex, nullable): corners, then nv + edge, nv + ne +
+ * quad, nv + ne + nq + hex. */
+int orc_h27_mesh(const uint32_t* hexes, uint32_t nh, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* quads,
+                 uint32_t* nquads, uint32_t* h27);
+void orc_h27_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, const uint32_t* edges,
+                         uint32_t ne, const uint32_t* quads, uint32_t nq, const uint32_t* h27, float density, double* X,
+                         float* ep, float* w, uint8_t* vflags);
+void orc_h27_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, const uint32_t* edges,
+                         uint32_t ne, const uint32_t* quads, uint32_t nq, const uint32_t* h27, double density,
+                         double* X, double* ep, double* w, uint8_t* vflags);
+int orc_solve_h27_f(double* X, const double* O, const float* w, const float* ep, const orc_params* p);
+int orc_solve_h27_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p);
+int orc_h27_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nh,
+                       const uint32_t* h27, const float* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+int orc_h27_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nh,
+                       const uint32_t* h27, const double* ep, const uint32_t* order, uint32_t nsub,
+                       const orc_params* p, uint8_t* contact);
+float orc_h27_volume_f(const double* X, uint32_t nh, const uint32_t* h27, const float* ep);
+double orc_h27_volume_d(const double* X, uint32_t nh, const uint32_t* h27, const double* ep);
+int orc_h27_schedule(const float* nodes, uint32_t nv, const uint32_t* h27, uint32_t nh, uint32_t morton,
+                     uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours);
+
 /* CalculateVolume (XPBDFEM/Geo.cpp:827-832, XPBDFEM/Fem.cpp:1066). */
 float orc_volume_f(const double* X, uint32_t nt, const uint32_t* tets);
 double orc_volume_d(const double* X, uint32_t nt, const uint32_t* tets);

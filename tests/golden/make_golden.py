@@ -239,6 +239,34 @@ CASES = [
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
     ("hvolume_wonky_pixar_1_post_pbd", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
+    # quadratic hexahedra (GeoQuadratic3d on a GenerateHexBlock mesh, element
+    # type H27): the `Q` commands; the substep cases run in the GPU's H27
+    # colour order
+    ("h27init_2x2x1", ["Qinit", 2, 2, 1, 0.1, 0.1, 0.1, 0, 0.0, 1000.0]),
+    ("h27init_3x2x2_mirror_wonky", ["Qinit", 3, 2, 2, 0.1, 0.1, 0.1, 1, 0.3, 1000.0]),
+    ("h27solve_nh_sim_nu045", ["Qsolve", 71, 16, 4, 1, 0.01, 0.45, DT]),
+    ("h27solve_nh_sim_incompressible", ["Qsolve", 72, 16, 4, 1, C1_COMPLIANCE, 0.5, DT]),
+    ("h27solve_nh_serial_nu045", ["Qsolve", 73, 16, 4, 0, 0.01, 0.45, DT]),
+    ("h27solve_yeohfast_sim_nu049", ["Qsolve", 74, 16, 7, 1, 0.5, 0.49, DT]),
+    ("h27solve_mixed_sim_nu045", ["Qsolve", 75, 16, 3, 1, 0.01, 0.45, DT]),
+    ("h27solve_yeohskinsel_serial_nu045", ["Qsolve", 76, 16, 6, 0, 0.5, 0.45, DT]),
+    ("h27solve_pixar_nu045", ["Qsolve", 77, 16, 0, 1, 0.01, 0.45, DT]),
+    ("h27solve_pixarsel_nu049", ["Qsolve", 78, 16, 2, 1, 0.01, 0.49, DT]),
+    ("h27ordered_c1_nh_nu045", ["Qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 20, 1]),
+    ("h27ordered_c1_nh_incompressible", ["Qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1, C1_COMPLIANCE,
+                                         0.5, 0.0, -9.81, DT, 20, 1]),
+    ("h27ordered_wonky_yeohfast_serial_nu049", ["Qordered", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 7, 0, 3.2e-4,
+                                                0.49, -2.0, -9.81, DT, 10, 1]),
+    ("h27ordered_c1_mixed_nu045", ["Qordered", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 3, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                   0.0, -9.81, DT, 20, 1]),
+    ("h27damped_c1_nh_nu045_amortized_pbd", ["Qdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 4, 1,
+                                             4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.03, 0.002, 3,
+                                             0.1]),
+    ("h27damped_c1_pixar_nu045_limit", ["Qdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 0, 1, 4.0 * 1.45 / 1e5,
+                                        0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("h27volume_wonky_nh_serial_1_post", ["Qdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
+                                          -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
 ]
 
 
@@ -279,6 +307,15 @@ def main():
             nodes, idx = oracle.gen_hex_block(W, H, D, (sx, sy, sz), pattern, wonk)
             hexes, _ = oracle.parse_hexes(idx)
             sch = oracle.hex_schedule(nodes, hexes, morton=1)
+            order = sch["hex_order"].astype(np.uint32)
+            stdin = struct.pack("<I", order.size) + order.tobytes()
+            extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
+        if args[0] in ("Qordered", "Qdamped"):
+            import oracle  # noqa: E402
+            W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]
+            nodes, idx = oracle.gen_hex_block(W, H, D, (sx, sy, sz), pattern, wonk)
+            q = oracle.QuadraticHex(nodes, idx, dens)
+            sch = q.schedule(morton=1)
             order = sch["hex_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}

@@ -414,10 +414,10 @@ def test_t10_element_solve_bit_exact(orc, name):
 
 
 def q_params(orc, a, g, tick):
-    """orc_params of a `qordered` / `qdamped` fixture."""
+    """orc_params of a `qordered` / `qdamped` (T10) or `Qordered` / `Qdamped` (H27) fixture."""
     energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[10:19]
     kw = dict(rayleigh_type=2)
-    if a[0] == "qdamped":
+    if a[0] in ("qdamped", "Qdamped"):
         damping, pbd, drag, rtype, spacing = a[19:24]
         d = g["derived"]
         kw = dict(damping=damping, rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(d[0]),
@@ -452,4 +452,85 @@ def test_t10_schedule_is_a_valid_colouring(orc):
     assert sorted(order.tolist()) == list(range(q.t10.shape[0]))
     for c in range(s["colours"]):
         verts = q.t10[order[cb[c]:cb[c + 1]]].reshape(-1)
+        assert np.unique(verts).size == verts.size
+
+
+# ---- quadratic hexahedra (GeoQuadratic3d on hexes; oracle/xfem_oracle_h27.inc) ----
+H27INIT = ["h27init_2x2x1", "h27init_3x2x2_mirror_wonky"]
+H27SOLVE = ["h27solve_nh_sim_nu045", "h27solve_nh_sim_incompressible", "h27solve_nh_serial_nu045",
+            "h27solve_yeohfast_sim_nu049", "h27solve_mixed_sim_nu045", "h27solve_yeohskinsel_serial_nu045",
+            "h27solve_pixar_nu045", "h27solve_pixarsel_nu049"]
+H27SUBSTEP = ["h27ordered_c1_nh_nu045", "h27ordered_c1_nh_incompressible", "h27ordered_wonky_yeohfast_serial_nu049",
+              "h27ordered_c1_mixed_nu045", "h27damped_c1_nh_nu045_amortized_pbd", "h27damped_c1_pixar_nu045_limit",
+              "h27volume_wonky_nh_serial_1_post"]
+
+
+def test_h27_tables_structure(orc):
+    """The 27-node tables from the printed 1-D Gauss points and weights: the
+    gradients sum to ~0 at every point, the shape functions to ~1, the
+    weights to 8 (the cube [-1, 1]^3), and the corner map's gradients are
+    those of the trilinear map."""
+    g8, g27, n27, map27, w27 = orc.h27_tables()
+    assert np.allclose(g8.sum(1), 0.0, atol=5e-6) and np.allclose(g27.sum(1), 0.0, atol=5e-6)
+    assert np.allclose(n27.sum(1), 1.0, atol=5e-6)
+    assert abs(float(w27.sum()) - 8.0) < 1e-4
+    assert np.allclose(map27.sum(1), 0.0, atol=5e-6)
+
+
+@pytest.mark.parametrize("name", H27INIT)
+def test_h27_rest_state_bit_exact(orc, name):
+    """GeoQuadratic3d::Init on hexes: Connectivity3d's edge and quad
+    numbering (the H27 indices), edge, face and hex-centre positions, flags
+    of all vertices, the 703-value records, masses and CalculateVolume."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.QuadraticHex(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(q.h27.reshape(-1), g["h27_idx"])
+    assert np.array_equal(q.X0.reshape(-1).view(np.uint64), g["x0"].view(np.uint64))
+    assert np.array_equal(q.ep.reshape(-1).view(np.uint32), g["h27ep"].view(np.uint32))
+    assert np.array_equal(q.w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(q.flags, g["vflags"])
+    assert np.array_equal(orc.minstd_order(q.h27.shape[0]), g["horder"])
+    assert np.float32(q.volume(q.X0)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+@pytest.mark.parametrize("name", H27SOLVE)
+def test_h27_element_solve_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    p = orc.make_params(dt=a[7], compliance=a[5], poisson=a[6], energy=a[3], simultaneous=bool(a[4]))
+    n = a[2]
+    xin, xout = g["xin"].reshape(n, 27, 3), g["xout"].reshape(n, 27, 3)
+    ep, w, rest = g["h27ep"].reshape(n, orc.H27_EP), g["w"].reshape(n, 27), g["rest"].reshape(n, 27, 3)
+    for t in range(n):
+        x = orc.solve_h27(xin[t], w[t], ep[t], p, O=rest[t])
+        assert np.array_equal(x.view(np.uint64), xout[t].view(np.uint64)), t
+
+
+@pytest.mark.parametrize("name", H27SUBSTEP)
+def test_h27_substeps_bit_exact(orc, name):
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.QuadraticHex(g["nodes"], g["idx"], a[9])
+    sch = q.schedule()
+    assert np.array_equal(sch["hex_order"], g["order"])
+    assert np.array_equal(sch["colour_hex_begin"], g["colour_hex_begin"])
+    lm = (q.flags & 1).astype(np.uint8)
+    X1, V1, w1, _ = q.substeps(q.X0, np.zeros_like(q.X0), q.w, g["order"], 1, q_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = q.substeps(X1, V1, w1, g["order"], a[17] - 1, q_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+def test_h27_schedule_is_a_valid_colouring(orc):
+    nodes, idx = orc.gen_hex_block(4, 3, 2, (0.1, 0.1, 0.1), 1, 0.3)
+    q = orc.QuadraticHex(nodes, idx, 1000.0)
+    s = q.schedule()
+    cb, order = s["colour_hex_begin"], s["hex_order"]
+    assert sorted(order.tolist()) == list(range(q.h27.shape[0]))
+    for c in range(s["colours"]):
+        verts = q.h27[order[cb[c]:cb[c + 1]]].reshape(-1)
         assert np.unique(verts).size == verts.size
