@@ -70,7 +70,7 @@ extern "C" {
 #define XFEM_ELEMENT_T4 5u              /*   Element_T4: linear tets (as 0) */
 #define XFEM_ELEMENT_T10 6u             /*   Element_T10: a tet mesh runs as quadratic tets */
 #define XFEM_ELEMENT_H8 7u              /*   Element_H8: linear hexes (as 0) */
-#define XFEM_ELEMENT_H27 8u             /*   Element_H27: quadratic; on a tet mesh as T10, on hexes not built */
+#define XFEM_ELEMENT_H27 8u             /*   Element_H27: quadratic (tets: T10s, hexes: H27s; so does T10) */
 #define XFEM_ENERGY_BIT 6u
 #define XFEM_ENERGY_MASK 31u
 /* Energy ids (XPBDFEM/Settings.h:41-53) as SolveElement dispatches them on a
@@ -183,9 +183,9 @@ int xfem_settings_default(xfem_settings* s);
  * lumped masses and inverse masses — then builds the colour schedule and
  * uploads everything. A mesh of hexes (tag 8) gets the hex rest state
  * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
- * element type T10 (flags bits 0-3) on a tet mesh makes it a T10 body
- * (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941); a mesh mixing tets and
- * hexes, quadratic hexes, or hexes or T10s with the continuous-pressure
+ * element type T10 or H27 (flags bits 0-3) makes a tet mesh a T10 body and a
+ * hex mesh an H27 body (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941); a
+ * mesh mixing tets and hexes, or an element body with the continuous-pressure
  * models (energy 8-10), returns XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
@@ -378,6 +378,39 @@ int xfem_compute_t10_rest_state(const float* node_data, uint32_t node_data_count
                                 float* out_w, uint8_t* out_flags);
 int xfem_compute_t10_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                               uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* t10_order,
+                              uint32_t* colour_begin, uint32_t* ncolours);
+
+/* ---- quadratic hexahedra (H27 mode) ----------------------------------------- */
+/* A hex mesh whose settings carry element type H27 (or T10) in flags bits
+ * 0-3 runs as GeoQuadratic3d on hexes (XPBDFEM/Geo.cpp:836-1053): a node on
+ * every edge and face and at every hex centre, 27-node elements
+ * (ElementParamsQuadraticHex, SolveElement with PointsLo = 8 and PointsHi =
+ * 27). The body's vertices are the mesh's own, then the edge, face and centre
+ * nodes. */
+/* H27s, edge nodes and face nodes of one body; XFEM_EUNSUPPORTED for another body. */
+int xfem_body_h27_count(const xfem_body* b, uint32_t body, uint32_t* nh27, uint32_t* nedges, uint32_t* nquads);
+/* Rest state per H27 (caller hex order) as 703 floats, ElementParamsQuadraticHex
+ * (XPBDFEM/Fem.h:101-111) flattened: qcLo.Ji[p] column-major [9p ..],
+ * qcLo.w[p] [72 + p], qcHi.Ji[p] [80 + 9p ..], qcHi.w[p] [323 + p], ic.QQ[26]
+ * [350..375], ic.QR[325] [376..700], volume [701], surfaceArea [702]; the
+ * rest inverse masses of all vertices; the 27 indices of each H27 (node
+ * i + 3j + 9k of its 3x3x3 grid, XPBDFEM/Geo.cpp:904-931). Outputs may be NULL. */
+int xfem_get_h27_rest_state(const xfem_body* b, uint32_t body, float* out_ep703, float* out_w, uint32_t* out_h27);
+int xfem_get_h27_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_rank, uint32_t* h27_order,
+                          uint32_t* colour_begin, uint32_t* ncolours);
+/* Connectivity3d's edges (2 each, at most 12 per hex) and quads (4 each,
+ * smallest vertex first, at most 6 per hex) of a hex index stream, and the
+ * H27 indices (27 per hex). Outputs may be NULL (count first). */
+int xfem_compute_h27_mesh(const uint32_t* idx_data, uint32_t idx_data_count, uint32_t* out_edges,
+                          uint32_t* out_quads, uint32_t* out_h27, uint32_t* out_nedges, uint32_t* out_nquads);
+/* GeoQuadratic3d::Init's rest state on a hex mesh without a GPU: out_x the
+ * double rest positions of all vertices, the 703-float records, inverse
+ * masses and flags; and its schedule. */
+int xfem_compute_h27_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, double* out_x, float* out_ep703,
+                                float* out_w, uint8_t* out_flags);
+int xfem_compute_h27_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* h27_order,
                               uint32_t* colour_begin, uint32_t* ncolours);
 
 /* ---- helpers --------------------------------------------------------------- */

@@ -78,3 +78,52 @@ class T10OracleRun:
         p = oracle_params(self.s, dt)
         self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
         return self
+
+
+def envelope(make_run, checkpoints, dt, seeds=8):
+    """FP64 states at each checkpoint (substep counts) and how far FP32 runs
+    of the method land from them: the largest distance over the FP32 oracle
+    started from the rest positions perturbed by up to one float ulp
+    (seeded). With an incompressible material or volume passes the FP32
+    rounding of J grows chaotically, on T10s within the first substep, and
+    single runs spread over an order of magnitude. make_run(dtype) gives a
+    fresh oracle run (T10OracleRun, H27OracleRun)."""
+    ref = []
+    o = make_run(np.float64)
+    done = 0
+    for n in checkpoints:
+        o.step(n - done, dt)
+        o.s.tick_id = n
+        done = n
+        ref.append((o.X.copy(), o.V.copy()))
+    env = [[0.0, 0.0] for _ in checkpoints]
+    for seed in range(seeds):
+        r = make_run(np.float32)
+        r.X = r.X * (1.0 + np.random.default_rng(seed).uniform(-1.0, 1.0, r.X.shape) * 2.0 ** -24)
+        done = 0
+        for k, n in enumerate(checkpoints):
+            r.step(n - done, dt)
+            r.s.tick_id = n
+            done = n
+            env[k][0] = max(env[k][0], rel(r.X, ref[k][0]))
+            env[k][1] = max(env[k][1], rel(r.V, ref[k][1]))
+    return ref, env
+
+
+class H27OracleRun:
+    """The oracle's state for one hex mesh read as H27s (GeoQuadratic3d),
+    stepped in the body's H27 order."""
+
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+        self.q = oracle.QuadraticHex(nodes, idx, density, dtype)
+        self.lock = (self.q.flags & 1).astype(np.uint8)
+        self.X = self.q.X0.copy()
+        self.V = np.zeros_like(self.X)
+        self.w = self.q.w.copy()
+        self.s = settings
+        self.order = order
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt)
+        self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
+        return self

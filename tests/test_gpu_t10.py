@@ -26,7 +26,7 @@ import pytest
 import oracle
 import xfem
 from conftest import golden, golden_args
-from helpers import T10OracleRun, rel
+from helpers import T10OracleRun, envelope, rel
 
 pytestmark = pytest.mark.gpu
 
@@ -58,36 +58,6 @@ def t10_settings(name):
                               volume_and_time_corrected_pbd_damping=kw["vc"],
                               amortized_volume_and_time_corrected_pbd_damping=kw["avc"], volume_passes=kw["vp"])
     return g, s, dens, dt, nsub
-
-
-def envelope(make_run, checkpoints, dt, seeds=8):
-    """FP64 states at each checkpoint (substep counts) and how far FP32 runs
-    of the method land from them: the largest distance over the FP32 oracle
-    started from the rest positions perturbed by up to one float ulp
-    (seeded). With an incompressible material or volume passes the FP32
-    rounding of J grows chaotically, on T10s within the first substep, and
-    single runs spread over an order of magnitude. make_run(dtype) gives a
-    fresh T10OracleRun."""
-    ref = []
-    o = make_run(np.float64)
-    done = 0
-    for n in checkpoints:
-        o.step(n - done, dt)
-        o.s.tick_id = n
-        done = n
-        ref.append((o.X.copy(), o.V.copy()))
-    env = [[0.0, 0.0] for _ in checkpoints]
-    for seed in range(seeds):
-        r = make_run(np.float32)
-        r.X = r.X * (1.0 + np.random.default_rng(seed).uniform(-1.0, 1.0, r.X.shape) * 2.0 ** -24)
-        done = 0
-        for k, n in enumerate(checkpoints):
-            r.step(n - done, dt)
-            r.s.tick_id = n
-            done = n
-            env[k][0] = max(env[k][0], rel(r.X, ref[k][0]))
-            env[k][1] = max(env[k][1], rel(r.V, ref[k][1]))
-    return ref, env
 
 
 @pytest.mark.parametrize("name", QFIX)
@@ -237,10 +207,8 @@ def test_t10_errors():
         with pytest.raises(xfem.XfemError) as ex:
             xfem.Body(nodes, idx, 1000.0, xfem.default_settings(flags=xfem.ELEMENT_T10 | (e << xfem.ENERGY_BIT)))
         assert ex.value.code == xfem.EUNSUPPORTED
-    # quadratic hexes are not built
-    with pytest.raises(xfem.XfemError) as ex:
-        xfem.Body(hn, hi, 1000.0, xfem.default_settings(flags=xfem.default_settings().flags | xfem.ELEMENT_H27))
-    assert ex.value.code == xfem.EUNSUPPORTED
+    # element type T10 on a hex mesh makes quadratic hexes, as in the reference
+    assert xfem.Body(hn, hi, 1000.0, xfem.default_settings(flags=t10)).h27_count()[0] == 12
     # linear and quadratic tets cannot share a handle
     with pytest.raises(xfem.XfemError) as ex:
         xfem.Body(meshes=[(nodes, idx, 1000.0), (nodes, idx, 1000.0)],

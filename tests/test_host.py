@@ -299,3 +299,50 @@ def test_t10_schedule_is_the_fixture_order(name):
     assert np.array_equal(s["t10_order"], g["order"])
     assert np.array_equal(s["colour_t10_begin"], g["colour_tet_begin"])
 
+
+
+# ---- quadratic hexes (GeoQuadratic3d on a hex mesh) ----
+@pytest.mark.parametrize("name", ["h27init_2x2x1", "h27init_3x2x2_mirror_wonky"])
+def test_h27_rest_state_bit_exact_vs_reference(name):
+    """GeoQuadratic3d::Init on hexes (XPBDFEM/Geo.cpp:836-933): the H27
+    indices (Connectivity3d's edge and quad numbering), the double positions
+    of the edge, face and centre nodes, the 703-value records, the inverse
+    masses and the flags of every vertex."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    _, _, h27 = xfem.compute_h27_mesh(g["idx"])
+    assert np.array_equal(h27.reshape(-1), g["h27_idx"])
+    x, ep, w, fl = xfem.compute_h27_rest_state(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(x.reshape(-1).view(np.uint64), g["x0"].view(np.uint64))
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["h27ep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+def test_h27_host_matches_oracle_on_jittered_meshes(orc, seed):
+    rng = np.random.default_rng(seed)
+    nodes, idx = xfem.generate_hex_block(4, 3, 3, (0.03, 0.05, 0.04), seed % 2, 0.3)
+    nodes = (nodes + rng.normal(0, 0.002, nodes.shape)).astype(np.float32)
+    q = orc.QuadraticHex(nodes, idx, 700.0)
+    edges, quads, h27 = xfem.compute_h27_mesh(idx)
+    assert np.array_equal(edges, q.edges) and np.array_equal(quads, q.quads) and np.array_equal(h27, q.h27)
+    x, ep, w, fl = xfem.compute_h27_rest_state(nodes, idx, 700.0)
+    assert np.array_equal(x.view(np.uint64), q.X0.view(np.uint64))
+    assert np.array_equal(ep.view(np.uint32), q.ep.view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), q.w.view(np.uint32))
+    assert np.array_equal(fl, q.flags)
+    for morton in (True, False):
+        s = xfem.compute_h27_schedule(nodes, idx, morton=morton)
+        o = q.schedule(morton=1 if morton else 0)
+        assert np.array_equal(s["vert_rank"], o["vert_rank"])
+        assert np.array_equal(s["h27_order"], o["hex_order"])
+        assert np.array_equal(s["colour_h27_begin"], o["colour_hex_begin"])
+
+
+@pytest.mark.parametrize("name", ["h27ordered_c1_nh_nu045", "h27volume_wonky_nh_serial_1_post"])
+def test_h27_schedule_is_the_fixture_order(name):
+    g = golden(name)
+    s = xfem.compute_h27_schedule(g["nodes"], g["idx"])
+    assert np.array_equal(s["h27_order"], g["order"])
+    assert np.array_equal(s["colour_h27_begin"], g["colour_hex_begin"])

@@ -36,9 +36,9 @@ int fail(int code, const std::string& msg) {
 	} while (0)
 
 // Element kinds of a body: linear tets (the chunked tet path, the one-ring
-// mode), linear hexahedra (H8) and quadratic tets (T10), the last two in the
-// element kernel.
-constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2;
+// mode), linear hexahedra (H8), quadratic tets (T10) and quadratic hexahedra
+// (H27), the last three in the element kernel.
+constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2, kElH27 = 3;
 
 struct BodyHost {
 	uint32_t nv = 0, nt = 0, vbase = 0, tbase = 0;
@@ -54,12 +54,13 @@ struct BodyHost {
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
 	// element bodies (linear hexahedra or quadratic tets; no linear tets)
-	uint32_t el = 0;                  // kElTets, kElHexes, kElT10
+	uint32_t el = 0;                  // kElTets, kElHexes, kElT10, kElH27
 	uint32_t nh = 0;                  // elements
-	uint32_t ncorner = 0;             // T10: the mesh's own vertices; the nv - ncorner edge nodes follow
-	std::vector<uint32_t> elems;      // 8 per hex or 10 per T10, caller order
-	std::vector<uint32_t> edges;      // T10: the two corners of each edge node
-	std::vector<float> eep;           // rest::kHexRec per hex or rest::kT10Rec per T10
+	uint32_t ncorner = 0;             // T10, H27: the mesh's own vertices; the added nodes follow
+	std::vector<uint32_t> elems;      // 8 per hex, 10 per T10 or 27 per H27, caller order
+	std::vector<uint32_t> edges;      // T10, H27: the two corners of each edge node
+	std::vector<uint32_t> quads;      // H27: the four corners of each face node
+	std::vector<float> eep;           // rest::kHexRec per hex, rest::kT10Rec per T10, rest::kH27Rec per H27
 	ElemSchedule esched;
 };
 
@@ -130,12 +131,12 @@ struct xfem_body {
 	DevBuf<float4> ring_ent;
 	DevBuf<uint2> pbd_cl;
 	DevBuf<uint4> pbd_ent;
-	// element mode (kElHexes or kElT10; kElTets: the tet path)
+	// element mode (kElHexes, kElT10 or kElH27; kElTets: the tet path)
 	uint32_t el_mode = kElTets;
 	DevBuf<uint4> el_vid;
 	DevBuf<float4> el_rec;
 	DevBuf<uint32_t> el_cb, el_flat;
-	DevBuf<float> el_g4;
+	DevBuf<float> el_tab;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -384,6 +385,33 @@ void prepare_t10(const xfem_mesh& m, BodyHost& b, std::vector<double>* X = nullp
 	if (X) *X = std::move(x);
 }
 
+// GeoQuadratic3d::Init on a hex mesh (XPBDFEM/Geo.cpp:836-933): nodes on the
+// edges, the faces and the hex centres, and the H27 rest state; the body's
+// vertices become the corners followed by those nodes. X as for prepare_t10.
+void prepare_h27(const xfem_mesh& m, BodyHost& b, std::vector<double>* X = nullptr) {
+	std::vector<uint32_t> h27;
+	hex_edges_quads(b.elems.data(), b.nh, b.nv, b.edges, b.quads, h27);
+	const uint32_t ne = (uint32_t)(b.edges.size() / 2), nq = (uint32_t)(b.quads.size() / 4);
+	const uint32_t n = b.nv + ne + nq + b.nh;
+	std::vector<double> x(3 * (size_t)n);
+	std::vector<float> eep((size_t)rest::kH27Rec * b.nh);
+	b.w0.resize(n);
+	b.vflags.resize(n);
+	h27_init_rest(b.nodes.data(), b.nv, b.elems.data(), b.nh, b.edges.data(), ne, b.quads.data(), nq, h27.data(),
+	              m.density, x.data(), eep.data(), b.w0.data(), b.vflags.data());
+	b.eep = std::move(eep);
+	b.nodes.resize(3 * (size_t)n);
+	for (size_t i = 0; i < 3 * (size_t)n; i++) b.nodes[i] = (float)x[i];
+	b.el = kElH27;
+	b.ncorner = b.nv;
+	b.nv = n;
+	b.elems = std::move(h27);
+	if (X) *X = std::move(x);
+}
+
+// Elements of an element body, and vertices per element.
+uint32_t nodes_per_element(uint32_t el) { return el == kElH27 ? 27u : el == kElT10 ? 10u : 8u; }
+
 // Whether the settings ask for quadratic elements (GeoQuadratic3d: element
 // type T10 or H27 in flags bits 0-3, XPBDFEM/Demo.cpp:145-150).
 bool quadratic_type(uint32_t flags) {
@@ -409,19 +437,20 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	const bool ring = model_of(energy) == kModelRing;
 	const bool quad = quadratic_type(b.settings.flags);
-	if (quad && b.el == kElHexes) return fail(XFEM_EUNSUPPORTED, "quadratic hexahedra (H27) are not built");
 	if (b.el == kElHexes || quad) {
-		// hexes and T10s: set-up on the host (rest state, Morton vertex
+		// hexes, T10s and H27s: set-up on the host (rest state, Morton vertex
 		// ranks, the element colouring)
 		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
 			return fail(XFEM_EUNSUPPORTED,
-			            "hex and T10 meshes run every energy model but the continuous-pressure ones (8-10)");
-		if (quad)
+			            "hex, T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
+		if (quad && b.el == kElHexes)
+			prepare_h27(m, b);
+		else if (quad)
 			prepare_t10(m, b);
 		else
 			host_rest(m, b);
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
-		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, quad ? 10u : 8u, morton, b.esched))
+		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, nodes_per_element(b.el), morton, b.esched))
 			return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
 		return XFEM_OK;
 	}
@@ -643,9 +672,9 @@ int build_rings(xfem_body* h) {
 // volume, surface area, QQ, QR), each element's index in its body's order,
 // and for T10s the shape-function gradients at the 4-point rule.
 int build_elements(xfem_body* h) {
-	const bool t10 = h->el_mode == kElT10;
-	const uint32_t per = t10 ? 10u : 8u, nvid4 = t10 ? 3u : 2u, nrec4 = t10 ? 14u : 30u;
-	const size_t rsz = t10 ? rest::kT10Rec : rest::kHexRec;
+	const bool t10 = h->el_mode == kElT10, h27 = h->el_mode == kElH27;
+	const uint32_t per = nodes_per_element(h->el_mode), nvid4 = (per + 3) / 4, nrec4 = h27 ? 176u : t10 ? 14u : 30u;
+	const size_t rsz = h27 ? rest::kH27Rec : t10 ? rest::kT10Rec : rest::kHexRec;
 	uint32_t ncol = 0, nel = 0;
 	for (const BodyHost& b : h->bodies) {
 		ncol = std::max(ncol, b.esched.ncolours);
@@ -662,12 +691,18 @@ int build_elements(xfem_body* h) {
 			if (c >= es.ncolours) continue;
 			for (uint32_t k = es.colour_begin[c]; k < es.colour_begin[c + 1]; k++, o++) {
 				const uint32_t el = es.order[k];
-				uint32_t d[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+				uint32_t d[28] = {0};
 				for (uint32_t n = 0; n < per; n++) d[n] = b.vbase + b.sched.vert_rank[b.elems[per * (size_t)el + n]];
 				for (uint32_t j = 0; j < nvid4; j++)
 					vid[nvid4 * (size_t)o + j] = make_uint4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
 				flat[o] = k;
 				const float* e = &b.eep[rsz * el];
+				if (h27) {  // element-major, the 703 values and a pad
+					float* dst = reinterpret_cast<float*>(&rec[(size_t)o * nrec4]);
+					for (size_t j = 0; j < rsz; j++) dst[j] = e[j];
+					dst[rsz] = 0.0f;
+					continue;
+				}
 				float r[120];
 				if (t10) {
 					for (int j = 0; j < 9; j++) r[j] = e[rest::kT10Qi + j];
@@ -691,16 +726,25 @@ int build_elements(xfem_body* h) {
 		}
 	}
 	cb[ncol] = o;
-	std::vector<float> g4(t10 ? 120 : 1, 0.0f);
+	std::vector<float> g4(t10 ? 120 : h27 ? 8 * 81 + 27 * 81 : 1, 0.0f);
 	if (t10)
 		for (int p = 0; p < 4; p++)
 			for (int n = 0; n < 10; n++)
 				for (int k = 0; k < 3; k++) g4[(p * 10 + n) * 3 + k] = rest::t10_tables().g4[p][n][k];
+	if (h27) {
+		const rest::H27Tables& tb = rest::h27_tables();
+		for (int p = 0; p < 8; p++)
+			for (int n = 0; n < 27; n++)
+				for (int k = 0; k < 3; k++) g4[(p * 27 + n) * 3 + k] = tb.g8[p][n][k];
+		for (int p = 0; p < 27; p++)
+			for (int n = 0; n < 27; n++)
+				for (int k = 0; k < 3; k++) g4[8 * 81 + (p * 27 + n) * 3 + k] = tb.g27[p][n][k];
+	}
 	XCUDA(h->el_vid.alloc(vid.size()));
 	XCUDA(h->el_rec.alloc(rec.size()));
 	XCUDA(h->el_cb.alloc(cb.size()));
 	XCUDA(h->el_flat.alloc(flat.size()));
-	XCUDA(h->el_g4.alloc(g4.size()));
+	XCUDA(h->el_tab.alloc(g4.size()));
 	auto up = [&](void* dst, const void* src, size_t bytes) {
 		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
 	};
@@ -708,7 +752,7 @@ int build_elements(xfem_body* h) {
 	XCUDA(up(h->el_rec.p, rec.data(), rec.size() * sizeof(float4)));
 	XCUDA(up(h->el_cb.p, cb.data(), cb.size() * 4));
 	XCUDA(up(h->el_flat.p, flat.data(), flat.size() * 4));
-	XCUDA(up(h->el_g4.p, g4.data(), g4.size() * 4));
+	XCUDA(up(h->el_tab.p, g4.data(), g4.size() * 4));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	h->ctx.el_colours = ncol;
 	h->ctx.nel = nel;
@@ -1085,7 +1129,7 @@ int build_device(xfem_body* h) {
 	c.el_vid = h->el_vid.p;
 	c.el_rec = h->el_rec.p;
 	c.colour_el_begin = h->el_cb.p;
-	c.el_g4 = h->el_g4.p;
+	c.el_tab = h->el_tab.p;
 	c.el_flat = h->el_flat.p;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
@@ -1278,8 +1322,9 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 		return XFEM_OK;
 	}
 	if (h->el_mode) {
-		const int e = h->el_mode == kElT10 ? launch_t10(h->ctx, 256, nsub, dt, h->stream)
-		                                   : launch_hexes(h->ctx, 256, nsub, dt, h->stream);
+		const int e = h->el_mode == kElH27 ? launch_h27(h->ctx, 256, nsub, dt, h->stream)
+		              : h->el_mode == kElT10 ? launch_t10(h->ctx, 256, nsub, dt, h->stream)
+		                                     : launch_hexes(h->ctx, 256, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
@@ -1412,8 +1457,9 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	if (h->el_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
-		return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes run every energy model but the continuous-pressure ones (8-10)");
-	if (quadratic_type(s->flags) != (b->el == kElT10))
+		return fail(XFEM_EUNSUPPORTED,
+		            "hex, T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
+	if (quadratic_type(s->flags) != (b->el == kElT10 || b->el == kElH27))
 		return fail(XFEM_EUNSUPPORTED, "switching between linear and quadratic elements (flags bits 0-3) needs a new handle");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
@@ -1479,7 +1525,7 @@ int xfem_set_tet_mu(xfem_body* h, uint32_t body, const float* mu) {
 	if (!b) return XFEM_EINVAL;
 	if (h->ring_mode && mu)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) take the body's material only");
-	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes take the body's material only");
+	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex, T10 and H27 meshes take the body's material only");
 	if (mu) {
 		for (uint32_t t = 0; t < b->nt; t++)
 			if (!(mu[t] > 0.0f) || !isfinite(mu[t])) return fail(XFEM_EINVAL, "tet mu must be finite and > 0");
@@ -1510,8 +1556,9 @@ int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, f
 	XCUDA(cudaSetDevice(h->device));
 	if (h->el_mode) {
 		// the element launches allocate nothing
-		const int e = h->el_mode == kElT10 ? launch_t10(h->ctx, 256, (uint32_t)n, dt, h->stream)
-		                                   : launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
+		const int e = h->el_mode == kElH27 ? launch_h27(h->ctx, 256, (uint32_t)n, dt, h->stream)
+		              : h->el_mode == kElT10 ? launch_t10(h->ctx, 256, (uint32_t)n, dt, h->stream)
+		                                     : launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
 		return check_device_error(h);
 	}
@@ -1553,7 +1600,7 @@ int xfem_get_lambdas(xfem_body* h, uint32_t body, float* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
-	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex and T10 meshes keep no multipliers");
+	if (h->el_mode) return fail(XFEM_EUNSUPPORTED, "hex, T10 and H27 meshes keep no multipliers");
 	if (!h->tlam.p) return fail(XFEM_EINVAL, "create the handle with keep_lambdas = 1");
 	XCUDA(cudaSetDevice(h->device));
 	std::vector<float2> all(h->tlam.n);
@@ -1572,6 +1619,39 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
 	XCUDA(cudaSetDevice(h->device));
+	if (b->el == kElH27) {
+		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per H27: rest
+		// volume times the weighted det F over the 3x3x3 points, in double
+		std::vector<float> x(3 * (size_t)b->nv);
+		const int rc = get_xyz(h, body, 0, x.data());
+		if (rc) return rc;
+		const rest::H27Tables& tb = rest::h27_tables();
+		double v = 0.0;
+		for (uint32_t q = 0; q < b->nh; q++) {
+			const uint32_t* is = &b->elems[27 * (size_t)q];
+			const float* e = &b->eep[(size_t)rest::kH27Rec * q];
+			double P[26][3];
+			for (int i = 0; i < 26; i++)
+				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[26] + k];
+			double scale = 0.0;
+			for (int p = 0; p < 27; p++) {
+				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+				for (int n = 0; n < 26; n++)
+					for (int c = 0; c < 3; c++)
+						for (int r = 0; r < 3; r++) Dm[c][r] += (double)tb.g27[p][n][r] * P[n][c];
+				const float* ji = e + rest::kH27JH + 9 * p;
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
+				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+				scale += (double)e[rest::kH27WH + p] * det;
+			}
+			v += (double)e[rest::kH27Vol] * scale;
+		}
+		*out = v;
+		return XFEM_OK;
+	}
 	if (b->el == kElT10) {
 		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per T10: rest
 		// volume times the mean det F over the 4 points, in double
@@ -1647,7 +1727,7 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 int xfem_get_rest_state(const xfem_body* h, uint32_t body, float* out_ep17, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex or T10 body: use xfem_get_hex_rest_state or xfem_get_t10_rest_state");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "an element body: use xfem_get_hex_rest_state, _t10_ or _h27_");
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
@@ -1657,7 +1737,7 @@ int xfem_get_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, ui
                       uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el) return fail(XFEM_EUNSUPPORTED, "a hex or T10 body: use xfem_get_hex_schedule or xfem_get_t10_schedule");
+	if (b.el) return fail(XFEM_EUNSUPPORTED, "an element body: use xfem_get_hex_schedule, _t10_ or _h27_");
 	const Schedule& s = b.sched;
 	if (vert_rank) memcpy(vert_rank, s.vert_rank.data(), s.vert_rank.size() * 4);
 	if (ncolours) *ncolours = s.ncolours;
@@ -1869,6 +1949,84 @@ int xfem_compute_t10_rest_state(const float* node_data, uint32_t node_data_count
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
 	return XFEM_OK;
+}
+
+int xfem_body_h27_count(const xfem_body* h, uint32_t body, uint32_t* nh27, uint32_t* nedges, uint32_t* nquads) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	if (nh27) *nh27 = b.nh;
+	if (nedges) *nedges = (uint32_t)(b.edges.size() / 2);
+	if (nquads) *nquads = (uint32_t)(b.quads.size() / 4);
+	return XFEM_OK;
+}
+
+int xfem_get_h27_rest_state(const xfem_body* h, uint32_t body, float* out_ep703, float* out_w, uint32_t* out_h27) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	if (out_ep703) memcpy(out_ep703, b.eep.data(), b.eep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_h27) memcpy(out_h27, b.elems.data(), b.elems.size() * 4);
+	return XFEM_OK;
+}
+
+int xfem_get_h27_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank, uint32_t* h27_order,
+                          uint32_t* colour_begin, uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	return elem_schedule_out(b, vert_rank, h27_order, colour_begin, ncolours);
+}
+
+// A hex mesh read as H27s (prepare_mesh then prepare_h27).
+static int h27_mesh(const xfem_mesh& m, BodyHost& b, std::vector<double>* X) {
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (b.el != kElHexes) return fail(XFEM_EINVAL, "not a hex mesh (tag 8)");
+	prepare_h27(m, b, X);
+	return XFEM_OK;
+}
+
+int xfem_compute_h27_mesh(const uint32_t* idx_data, uint32_t idx_data_count, uint32_t* out_edges, uint32_t* out_quads,
+                          uint32_t* out_h27, uint32_t* out_nedges, uint32_t* out_nquads) {
+	if (!idx_data) return fail(XFEM_EINVAL, "null index stream");
+	std::vector<uint32_t> hexes, edges, quads, h27;
+	uint32_t nv = 0;
+	if (parse_hexes(idx_data, idx_data_count, hexes, nv)) return fail(XFEM_EINVAL, "not a hex index stream (tag 8)");
+	hex_edges_quads(hexes.data(), (uint32_t)(hexes.size() / 8), nv, edges, quads, h27);
+	if (out_edges) memcpy(out_edges, edges.data(), edges.size() * 4);
+	if (out_quads) memcpy(out_quads, quads.data(), quads.size() * 4);
+	if (out_h27) memcpy(out_h27, h27.data(), h27.size() * 4);
+	if (out_nedges) *out_nedges = (uint32_t)(edges.size() / 2);
+	if (out_nquads) *out_nquads = (uint32_t)(quads.size() / 4);
+	return XFEM_OK;
+}
+
+int xfem_compute_h27_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, float density, double* out_x, float* out_ep703,
+                                float* out_w, uint8_t* out_flags) {
+	BodyHost b;
+	std::vector<double> X;
+	const int rc = h27_mesh({node_data, node_data_count, idx_data, idx_data_count, density}, b, &X);
+	if (rc) return rc;
+	if (out_x) memcpy(out_x, X.data(), X.size() * sizeof(double));
+	if (out_ep703) memcpy(out_ep703, b.eep.data(), b.eep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
+	return XFEM_OK;
+}
+
+int xfem_compute_h27_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                              uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* h27_order,
+                              uint32_t* colour_begin, uint32_t* ncolours) {
+	BodyHost b;
+	const int rc = h27_mesh({node_data, node_data_count, idx_data, idx_data_count, 1.0f}, b, nullptr);
+	if (rc) return rc;
+	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
+	if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 27, no_morton ? 0u : 1u, b.esched))
+		return fail(XFEM_ELIMIT, "the H27 colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+	return elem_schedule_out(b, vert_rank, h27_order, colour_begin, ncolours);
 }
 
 int xfem_compute_t10_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,

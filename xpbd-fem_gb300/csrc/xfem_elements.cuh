@@ -79,13 +79,11 @@ __device__ __forceinline__ void moven(const float w[N], float l, const Vec3 g[N]
 }
 
 // One constraint (XPBDFEM/Xpbd.h:87-121) with the in-solve Rayleigh damping
-// (types 0 Paper, 1 Limit) when `damp` > 0.
-template <int N>
-__device__ __forceinline__ float lambda1n(float U, const Vec3 g[N], const float w[N], const float4 D[N], float alpha,
-                                         float comp, float damp, bool limit, float inv_dt) {
-	const float wgg = wdotn<N>(w, g, g);
+// (types 0 Paper, 1 Limit) when `damp` > 0, from wgg = sum w g.g and gV =
+// sum g.(X - O) (read only with damping).
+__device__ __forceinline__ float lambda1_of(float U, float wgg, float gV, float alpha, float comp, float damp, bool limit,
+                                           float inv_dt) {
 	if (!(damp > 0.0f)) return (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
-	const float gV = gdotn<N>(g, D);
 	const float gamma = damp * inv_dt;
 	if (!limit) return (-2.0f * U - gamma * gV) / fmaf(wgg, 1.0f + gamma, 2.0f * U * alpha);
 	const float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
@@ -94,18 +92,23 @@ __device__ __forceinline__ float lambda1n(float U, const Vec3 g[N], const float 
 	return l + b / A;
 }
 
-// The coupled pair (XPBDFEM/Xpbd.h:123-215): Cramer's rule, the damping forms
-// of :133-205.
 template <int N>
-__device__ __forceinline__ void lambda2n(float U0, float U1, const Vec3 g0[N], const Vec3 g1[N], const float w[N],
-                                        const float4 D[N], float alpha0, float alpha1, float comp0, float comp1,
-                                        float damp, bool limit, float inv_dt, float& l0, float& l1) {
-	const float wgg0 = wdotn<N>(w, g0, g0), wgg1 = wdotn<N>(w, g1, g0), wgg2 = wdotn<N>(w, g1, g1);
+__device__ __forceinline__ float lambda1n(float U, const Vec3 g[N], const float w[N], const float4 D[N], float alpha,
+                                         float comp, float damp, bool limit, float inv_dt) {
+	const float wgg = wdotn<N>(w, g, g);
+	return lambda1_of(U, wgg, damp > 0.0f ? gdotn<N>(g, D) : 0.0f, alpha, comp, damp, limit, inv_dt);
+}
+
+// The coupled pair (XPBDFEM/Xpbd.h:123-215): Cramer's rule, the damping forms
+// of :133-205, from the weighted gradient products and (with damping) the
+// gradients' products with X - O.
+__device__ __forceinline__ void lambda2_of(float U0, float U1, float wgg0, float wgg1, float wgg2, float gV0, float gV1,
+                                           float alpha0, float alpha1, float comp0, float comp1, float damp, bool limit,
+                                           float inv_dt, float& l0, float& l1) {
 	if (!(damp > 0.0f)) {
 		cramer(fmaf(2.0f * U0, alpha0, wgg0), wgg1, fmaf(2.0f * U1, alpha1, wgg2), -2.0f * U0, -2.0f * U1, l0, l1);
 		return;
 	}
-	const float gV0 = gdotn<N>(g0, D), gV1 = gdotn<N>(g1, D);
 	const float gamma = damp * inv_dt;
 	float A0, A2, b0 = -2.0f * U0, b1 = -2.0f * U1;
 	if (!limit) {
@@ -129,6 +132,16 @@ __device__ __forceinline__ void lambda2n(float U0, float U1, const Vec3 g0[N], c
 		l0 += d0;
 		l1 += d1;
 	}
+}
+
+template <int N>
+__device__ __forceinline__ void lambda2n(float U0, float U1, const Vec3 g0[N], const Vec3 g1[N], const float w[N],
+                                        const float4 D[N], float alpha0, float alpha1, float comp0, float comp1,
+                                        float damp, bool limit, float inv_dt, float& l0, float& l1) {
+	const float wgg0 = wdotn<N>(w, g0, g0), wgg1 = wdotn<N>(w, g1, g0), wgg2 = wdotn<N>(w, g1, g1);
+	const bool dm = damp > 0.0f;
+	lambda2_of(U0, U1, wgg0, wgg1, wgg2, dm ? gdotn<N>(g0, D) : 0.0f, dm ? gdotn<N>(g1, D) : 0.0f, alpha0, alpha1,
+	           comp0, comp1, damp, limit, inv_dt, l0, l1);
 }
 
 __device__ __forceinline__ bool full_quadrature(uint32_t e) { return e == 3u || e == 5u || e == 6u; }
@@ -204,11 +217,15 @@ __device__ __forceinline__ const BodyParams& body_of_el(const DevCtx& C, uint32_
 }
 
 // The persistent element kernel (cooperative launch, co-resident grid). E:
-// the element type (kVid4 uint4 of vertex ids per element; pass<KIND>, pbd).
+// the element type (kVid4 uint4 of vertex ids per element; pass<KIND>, pbd;
+// kWarp: one warp per element, every lane of the warp calling with the same
+// element, else one thread per element).
 template <class E>
 __global__ void __launch_bounds__(256) k_elements(DevCtx C, uint32_t nsub, float dt) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	// the element loops run over units: threads, or warps (warp-uniform i)
+	const uint32_t unit = E::kWarp ? gtid >> 5 : gtid, nunits = E::kWarp ? nthreads >> 5 : nthreads;
 	const uint32_t tick0 = __ldcg(C.tick);
 	const bool dmode = C.damp_kinds != 0u;
 	uint32_t target = 0;
@@ -222,13 +239,13 @@ __global__ void __launch_bounds__(256) k_elements(DevCtx C, uint32_t nsub, float
 		if (!grid_sync(C, target)) return;
 		for (uint32_t c = 0; c < C.el_colours; c++) {
 			const uint32_t b = __ldg(C.colour_el_begin + c), e = __ldg(C.colour_el_begin + c + 1);
-			for (uint32_t i = b + gtid; i < e; i += nthreads) E::template pass<kSolve>(C, i, inv_dt, inv_dt2, 0.0f);
+			for (uint32_t i = b + unit; i < e; i += nunits) E::template pass<kSolve>(C, i, inv_dt, inv_dt2, 0.0f);
 			if (!grid_sync(C, target)) return;
 		}
 		for (uint32_t it = 0; it < C.nvol; it++)
 			for (uint32_t c = 0; c < C.el_colours; c++) {
 				const uint32_t b = __ldg(C.colour_el_begin + c), e = __ldg(C.colour_el_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads)
+				for (uint32_t i = b + unit; i < e; i += nunits)
 					if (it < __ldg(&body_of_el<E>(C, i).volume_passes)) E::template pass<kVolume>(C, i, inv_dt, inv_dt2, 0.0f);
 				if (!grid_sync(C, target)) return;
 			}
@@ -244,7 +261,7 @@ __global__ void __launch_bounds__(256) k_elements(DevCtx C, uint32_t nsub, float
 		if (C.damp_kinds & 1u)
 			for (uint32_t c = 0; c < C.el_colours; c++) {
 				const uint32_t b = __ldg(C.colour_el_begin + c), e = __ldg(C.colour_el_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads) {
+				for (uint32_t i = b + unit; i < e; i += nunits) {
 					const BodyParams& bp = body_of_el<E>(C, i);
 					const uint32_t type = __ldg(&bp.rayleigh_type);
 					const float rd = __ldg(&bp.damping) * (type == 3u ? 8.0f : 1.0f);
@@ -255,7 +272,7 @@ __global__ void __launch_bounds__(256) k_elements(DevCtx C, uint32_t nsub, float
 		if (C.damp_kinds & 2u)
 			for (uint32_t c = 0; c < C.el_colours; c++) {
 				const uint32_t b = __ldg(C.colour_el_begin + c), e = __ldg(C.colour_el_begin + c + 1);
-				for (uint32_t i = b + gtid; i < e; i += nthreads) {
+				for (uint32_t i = b + unit; i < e; i += nunits) {
 					const BodyParams& bp = body_of_el<E>(C, i);
 					if (__ldg(&bp.pbd_on) && in_slice(C, bp, i, tick))
 						E::pbd(C, i, __ldg(&bp.rayleigh_type) == 3u ? __ldg(&bp.pbd_coeff_amortized) : __ldg(&bp.pbd_coeff));

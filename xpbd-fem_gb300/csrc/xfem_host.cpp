@@ -512,4 +512,155 @@ void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const ui
 	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
 }
 
+void hex_edges_quads(const uint32_t* hexes, uint32_t nhexes, uint32_t nverts, std::vector<uint32_t>& edges,
+                     std::vector<uint32_t>& quads, std::vector<uint32_t>& h27) {
+	static const int he[12][2] = {{0, 1}, {0, 2}, {0, 4}, {1, 3}, {1, 5}, {2, 3}, {2, 6}, {3, 7}, {4, 5}, {4, 6}, {5, 7}, {6, 7}};
+	static const int hq[6][4] = {{0, 1, 3, 2}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 2, 6, 4}, {1, 3, 7, 5}};
+	// edge and quad instances, each under the vertex it is filed under
+	std::vector<uint32_t> eoff(nverts + 1, 0), qoff(nverts + 1, 0);
+	std::vector<uint32_t> eup(12 * (size_t)nhexes), einst(12 * (size_t)nhexes), qv(24 * (size_t)nhexes),
+	    qinst(6 * (size_t)nhexes);
+	auto face = [&](uint32_t h, int f, uint32_t out[4]) {  // rotated to start at its smallest vertex
+		uint32_t vs[4], best = 0;
+		for (int j = 0; j < 4; j++) vs[j] = hexes[8 * (size_t)h + hq[f][j]];
+		for (uint32_t j = 1; j < 4; j++)
+			if (vs[j] < vs[best]) best = j;
+		for (uint32_t j = 0; j < 4; j++) out[j] = vs[(best + j) % 4];
+	};
+	for (uint32_t h = 0; h < nhexes; h++) {
+		for (int k = 0; k < 12; k++)
+			eoff[std::min(hexes[8 * (size_t)h + he[k][0]], hexes[8 * (size_t)h + he[k][1]]) + 1]++;
+		for (int f = 0; f < 6; f++) {
+			uint32_t v[4];
+			face(h, f, v);
+			qoff[v[0] + 1]++;
+		}
+	}
+	for (uint32_t v = 0; v < nverts; v++) {
+		eoff[v + 1] += eoff[v];
+		qoff[v + 1] += qoff[v];
+	}
+	std::vector<uint32_t> ecnt(nverts, 0), qcnt(nverts, 0);
+	for (uint32_t h = 0; h < nhexes; h++) {
+		for (int k = 0; k < 12; k++) {
+			const uint32_t a = hexes[8 * (size_t)h + he[k][0]], b = hexes[8 * (size_t)h + he[k][1]];
+			const uint32_t lo = std::min(a, b), id = 12 * h + (uint32_t)k;
+			eup[id] = std::max(a, b);
+			einst[eoff[lo] + ecnt[lo]++] = id;
+		}
+		for (int f = 0; f < 6; f++) {
+			const uint32_t id = 6 * h + (uint32_t)f;
+			face(h, f, &qv[4 * (size_t)id]);
+			qinst[qoff[qv[4 * (size_t)id]] + qcnt[qv[4 * (size_t)id]]++] = id;
+		}
+	}
+	// a later duplicate takes the list's last entry in its place; a quad is a
+	// duplicate in either winding
+	for (uint32_t v = 0; v < nverts; v++) {
+		uint32_t* L = einst.data() + eoff[v];
+		for (uint32_t j = 0; j < ecnt[v]; j++)
+			for (uint32_t k = j + 1; k < ecnt[v]; k++)
+				if (eup[L[j]] == eup[L[k]]) L[k--] = L[--ecnt[v]];
+		uint32_t* Q = qinst.data() + qoff[v];
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (uint32_t k = j + 1; k < qcnt[v]; k++) {
+				const uint32_t* a = &qv[4 * (size_t)Q[j]];
+				const uint32_t* b = &qv[4 * (size_t)Q[k]];
+				if ((a[1] == b[1] && a[2] == b[2] && a[3] == b[3]) || (a[1] == b[3] && a[2] == b[2] && a[3] == b[1]))
+					Q[k--] = Q[--qcnt[v]];
+			}
+	}
+	std::vector<uint32_t> efirst(nverts), qfirst(nverts);
+	edges.clear();
+	quads.clear();
+	for (uint32_t v = 0; v < nverts; v++) {
+		efirst[v] = (uint32_t)(edges.size() / 2);
+		for (uint32_t j = 0; j < ecnt[v]; j++) {
+			edges.push_back(v);
+			edges.push_back(eup[einst[eoff[v] + j]]);
+		}
+		qfirst[v] = (uint32_t)(quads.size() / 4);
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (int k = 0; k < 4; k++) quads.push_back(qv[4 * (size_t)qinst[qoff[v] + j] + k]);
+	}
+	const uint32_t ne = (uint32_t)(edges.size() / 2), nq = (uint32_t)(quads.size() / 4);
+	h27.resize(27 * (size_t)nhexes);
+	for (uint32_t h = 0; h < nhexes; h++) {
+		const uint32_t* c = hexes + 8 * (size_t)h;
+		for (int n = 0; n < 27; n++) {
+			const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+			int mid = 0, lo = 0, free = 0;
+			for (int a = 0; a < 3; a++) {
+				mid += ix[a] == 1;
+				lo |= (ix[a] == 2) << a;
+				free |= (ix[a] == 1) << a;
+			}
+			uint32_t id;
+			if (mid == 0) {
+				id = c[lo];
+			} else if (mid == 1) {
+				const uint32_t a = c[lo], b = c[lo | free];
+				const uint32_t l = std::min(a, b), u = std::max(a, b);
+				uint32_t e = 0;
+				while (edges[2 * (size_t)(efirst[l] + e) + 1] != u) e++;
+				id = nverts + efirst[l] + e;
+			} else if (mid == 2) {
+				const int f1 = free & 1 ? 1 : 2, f2 = free & 4 ? 4 : 2;
+				const uint32_t vs[4] = {c[lo], c[lo | f1], c[lo | f1 | f2], c[lo | f2]};
+				uint32_t best = 0;
+				for (uint32_t j = 1; j < 4; j++)
+					if (vs[j] < vs[best]) best = j;
+				const uint32_t v0 = vs[best], v1 = vs[(best + 1) % 4], v2 = vs[(best + 2) % 4], v3 = vs[(best + 3) % 4];
+				uint32_t q = 0;
+				for (;; q++) {
+					const uint32_t* Q = &quads[4 * (size_t)(qfirst[v0] + q)];
+					if ((Q[1] == v1 && Q[2] == v2 && Q[3] == v3) || (Q[1] == v3 && Q[2] == v2 && Q[3] == v1)) break;
+				}
+				id = nverts + ne + qfirst[v0] + q;
+			} else {
+				id = nverts + ne + nq + h;
+			}
+			h27[27 * (size_t)h + n] = id;
+		}
+	}
+}
+
+void h27_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, const uint32_t* edges,
+                   uint32_t nedges, const uint32_t* quads, uint32_t nquads, const uint32_t* h27, float density,
+                   double* X, float* ep, float* w, uint8_t* vflags) {
+	const uint32_t n = nverts + nedges + nquads + nhexes;
+	for (size_t i = 0; i < 3 * (size_t)nverts; i++) X[i] = (double)nodes[i];
+	for (uint32_t e = 0; e < nedges; e++)
+		for (int k = 0; k < 3; k++)
+			X[3 * (size_t)(nverts + e) + k] = 0.5 * (X[3 * (size_t)edges[2 * e] + k] + X[3 * (size_t)edges[2 * e + 1] + k]);
+	for (uint32_t q = 0; q < nquads; q++) {
+		const uint32_t* v = quads + 4 * (size_t)q;
+		for (int k = 0; k < 3; k++)
+			X[3 * (size_t)(nverts + nedges + q) + k] =
+			    0.25 * (X[3 * (size_t)v[0] + k] + X[3 * (size_t)v[1] + k] + X[3 * (size_t)v[2] + k] + X[3 * (size_t)v[3] + k]);
+	}
+	for (uint32_t h = 0; h < nhexes; h++)
+		for (int k = 0; k < 3; k++) {
+			double s = X[3 * (size_t)hexes[8 * (size_t)h] + k];
+			for (int c = 1; c < 8; c++) s = s + X[3 * (size_t)hexes[8 * (size_t)h + c] + k];
+			X[3 * (size_t)(nverts + nedges + nquads + h) + k] = 0.125 * s;
+		}
+	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};
+	for (uint32_t i = 0; i < n; i++) {
+		w[i] = 0.0f;
+		for (int k = 0; k < 3; k++) {
+			mn[k] = fminf(mn[k], (float)X[3 * (size_t)i + k]);
+			mx[k] = fmaxf(mx[k], (float)X[3 * (size_t)i + k]);
+		}
+	}
+	for (uint32_t i = 0; i < n; i++) vflags[i] = rest::vertex_flags((float)X[3 * (size_t)i], mn[0], mx[0]);
+	for (uint32_t h = 0; h < nhexes; h++) {
+		const uint32_t* is = h27 + 27 * (size_t)h;
+		float m[27];
+		rest::h27(X, is, density, ep + (size_t)rest::kH27Rec * h, m);
+		for (int c = 0; c < 27; c++) w[is[c]] += m[c];
+	}
+	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
+}
+
 }  // namespace xfem

@@ -126,6 +126,25 @@ void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const ui
                    uint32_t nedges, const uint32_t* t10, float density, double* X, float* qep, float* w,
                    uint8_t* vflags);
 
+// Quadratic hexahedra (H27, GeoQuadratic3d on a hex mesh). Connectivity3d's
+// edges (as tet_edges, each hex filing its 12 edges in the order of
+// XPBDFEM/Connectivity.cpp:443-454) and quads (each hex face rotated to start
+// at its smallest vertex and filed under it, XPBDFEM/Connectivity.cpp:
+// 410-422, 456-461; a later duplicate in either winding swap-removed,
+// :515-530; numbered vertex by vertex), and GeoQuadratic3d's 27 indices per
+// hex (XPBDFEM/Geo.cpp:904-931): node i + 3j + 9k of the hex's 3x3x3 grid is
+// a corner, nverts + an edge, nverts + nedges + a quad, or nverts + nedges +
+// nquads + the hex.
+void hex_edges_quads(const uint32_t* hexes, uint32_t nhexes, uint32_t nverts, std::vector<uint32_t>& edges,
+                     std::vector<uint32_t>& quads, std::vector<uint32_t>& h27);
+// GeoQuadratic3d::Init's rest state on a hex mesh (XPBDFEM/Geo.cpp:836-933):
+// X (3 doubles per vertex: corners, edge midpoints, face centres, hex
+// centres), flags over all of them, 703 floats per H27 (rest::kH27* offsets)
+// and the inverse lumped masses, bit for bit.
+void h27_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, const uint32_t* edges,
+                   uint32_t nedges, const uint32_t* quads, uint32_t nquads, const uint32_t* h27, float density,
+                   double* X, float* ep, float* w, uint8_t* vflags);
+
 // ---- GPU set-up path (xfem_setup.cu) ------------------------------------------
 // The parallel phases of the set-up on the device, bit for bit the host's:
 // rest state (init_rest), incidence, Morton vertex ranks (vertex_ranks) and
@@ -285,13 +304,16 @@ struct DevCtx {
 	const uint32_t* tet_verts;
 	uint32_t pbd_colours;
 	// Element modes (xfem_hexes.cu: linear hexahedra; xfem_t10.cu: quadratic
-	// tets): elements in device order, colour-major (bodies in order inside a
-	// colour). el_vid: the element's device vertex ids (hex: 8 in two uint4;
-	// T10: 10 in three uint4); el_rec: the records as a structure of arrays
-	// (float4 k of element i at el_rec[k * nel + i]; hex 30 float4, T10 14);
-	// el_flat: each element's index in its body's element order (the
-	// amortized damping slices); el_g4 (T10): the shape-function gradients at
-	// the 4-point rule, [point][node][axis].
+	// tets; xfem_h27.cu: quadratic hexahedra): elements in device order,
+	// colour-major (bodies in order inside a colour). el_vid: the element's
+	// device vertex ids (hex: 8 in two uint4; T10: 10 in three uint4; H27: 27
+	// in seven); el_rec: the records, as a structure of arrays for the
+	// one-thread-per-element modes (float4 k of element i at
+	// el_rec[k * nel + i]; hex 30 float4, T10 14) and element-major for H27
+	// (704 floats per element, read by its warp); el_flat: each element's
+	// index in its body's element order (the amortized damping slices);
+	// el_tab: the mode's shape-function gradient tables, [point][node][axis]
+	// (T10: the 4-point rule; H27: the 2x2x2 rule, then the 3x3x3 rule).
 	uint32_t el_colours;
 	const uint4* el_vid;
 	const float4* el_rec;
@@ -299,7 +321,7 @@ struct DevCtx {
 	const uint32_t* el_flat;
 	uint32_t nel;
 	uint32_t pad6;
-	const float* el_g4;
+	const float* el_tab;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
@@ -379,6 +401,9 @@ int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* st
 int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-tet mode (xfem_t10.cu): nsub substeps of a T10 mesh, likewise.
 int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp
+// per element (block must be 256).
+int launch_h27(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Per-tet material (n tets from the given per-tet tables): c0 of each record
 // and 1/mu; mu null = mu_uniform for all.
 int launch_set_c0(float4* cblk, const uint32_t* rec, const float* vol, const float* mu, float mu_uniform, uint32_t n,

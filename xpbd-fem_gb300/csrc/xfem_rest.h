@@ -370,6 +370,156 @@ inline void t10(const double* X, const uint32_t* is, float density, float* o, fl
 	for (int n = 0; n < 10; n++) m[n] = ((n < 4 ? 13.0f : 70.0f) / 472.0f) * density * vol;
 }
 
+// ---- quadratic hexahedra (H27), host only ----
+// Nodes and quadrature points are numbered i + 3j + 9k on each element's
+// 3x3x3 grid (i + 2j + 4k on the 2x2x2 rule), with the 1-D nodes -1, 0, 1 and
+// the 1-D shape functions x (x - 1) / 2, 1 - x^2, x (x + 1) / 2. The
+// reference's tables (XPBDFEM/Fem.cpp:16-18, 41-44, 70-73) are those
+// functions evaluated in double at the 1-D Gauss points and weights as
+// printed to six decimals (0.774597, 0 and 0.577350; weights 0.555556 and
+// 0.888889), each entry then printed to six decimals; that method gives
+// every entry, so the tables are built with it.
+struct H27Tables {
+	float g8[8][27][3], g27[27][27][3], n27[27][27], map27[27][8][3], w27[27];
+};
+inline const H27Tables& h27_tables() {
+	static const H27Tables t = [] {
+		const double x3[3] = {-0.774597, 0.0, 0.774597}, x2[2] = {-0.577350, 0.577350};
+		const double w3[3] = {0.555556, 0.888889, 0.555556};
+		auto q = [](int i, double x) { return i == 0 ? x * (x - 1) / 2 : i == 1 ? (1 - x) * (1 + x) : x * (x + 1) / 2; };
+		auto dq = [](int i, double x) { return i == 0 ? x - 0.5 : i == 1 ? -2 * x : x + 0.5; };
+		auto r6 = [](double v) { return (float)(nearbyint(v * 1e6) / 1e6); };
+		H27Tables r;
+		for (int p = 0; p < 27; p++) {
+			const double x[3] = {x3[p % 3], x3[(p / 3) % 3], x3[p / 9]};
+			r.w27[p] = r6(w3[p % 3] * w3[(p / 3) % 3] * w3[p / 9]);
+			for (int n = 0; n < 27; n++) {
+				const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+				r.n27[p][n] = r6(q(ix[0], x[0]) * q(ix[1], x[1]) * q(ix[2], x[2]));
+				for (int k = 0; k < 3; k++) {
+					double v = 1.0;
+					for (int a = 0; a < 3; a++) v *= a == k ? dq(ix[a], x[a]) : q(ix[a], x[a]);
+					r.g27[p][n][k] = r6(v);
+					if (p < 8) {
+						const double y[3] = {x2[p & 1], x2[(p >> 1) & 1], x2[p >> 2]};
+						double u = 1.0;
+						for (int a = 0; a < 3; a++) u *= a == k ? dq(ix[a], y[a]) : q(ix[a], y[a]);
+						r.g8[p][n][k] = r6(u);
+					}
+				}
+			}
+			for (int n = 0; n < 8; n++)
+				for (int k = 0; k < 3; k++) {
+					double v = 1.0;
+					for (int a = 0; a < 3; a++) {
+						const int b = (n >> a) & 1;
+						v *= a == k ? (b ? 0.5 : -0.5) : (b ? (1 + x[a]) / 2 : (1 - x[a]) / 2);
+					}
+					r.map27[p][n][k] = r6(v);
+				}
+		}
+		return r;
+	}();
+	return t;
+}
+
+// Offsets in the 703-value H27 record (ElementParamsQuadraticHex,
+// XPBDFEM/Fem.h:101-111, flattened): qcLo.Ji[p] column-major, qcLo.w[p],
+// qcHi.Ji[p], qcHi.w[p], ic.QQ[26], ic.QR[325], volume, surfaceArea.
+constexpr int kH27JL = 0, kH27WL = 72, kH27JH = 80, kH27WH = 323, kH27QQ = 350, kH27QR = 376, kH27Vol = 701,
+              kH27Area = 702, kH27Rec = 703;
+
+// The corner map's jacobian at point p of the 2x2x2 (np 8) or 3x3x3 rule.
+inline M3 h27_map_jacobian(const float P[8][3], int np, int p) {
+	const H27Tables& tb = h27_tables();
+	M3 J;
+	for (int c = 0; c < 3; c++)
+		for (int r = 0; r < 3; r++) J.c[c][r] = 0.0f;
+	for (int n = 0; n < 8; n++)
+		for (int c = 0; c < 3; c++)
+			for (int r = 0; r < 3; r++) J.c[c][r] = J.c[c][r] + (np == 8 ? hex_g8(p, n, r) : tb.map27[p][n][r]) * P[n][c];
+	return J;
+}
+
+// One H27: InitQuadHexFiniteElement (XPBDFEM/Fem.cpp:225-265) with the map
+// over the corners is[0, 2, 6, 8, 18, 20, 24, 26] (:274): the mapped
+// quadrature on the 2x2x2 and 3x3x3 rules, the prefactored I1 on the 3x3x3
+// rule, the volume on the 2x2x2 rule, the surface area, and the masses from
+// the normalised mass-matrix diagonal. X: the vertex positions in double.
+inline void h27(const double* X, const uint32_t* is, float density, float* o, float m[27]) {
+	static const int corner[8] = {0, 2, 6, 8, 18, 20, 24, 26};
+	const H27Tables& tb = h27_tables();
+	float P[8][3];
+	for (int n = 0; n < 8; n++)
+		for (int k = 0; k < 3; k++)
+			P[n][k] = (float)(X[3 * (size_t)is[corner[n]] + k] - X[3 * (size_t)is[corner[7]] + k]);
+	for (int hi = 0; hi < 2; hi++) {
+		const int np = hi ? 27 : 8;
+		float vsum = 0.0f;
+		for (int p = 0; p < np; p++) {
+			const M3 J = h27_map_jacobian(P, np, p);
+			const float detJ = det3(J);
+			const M3 Ji = inverse3(J);
+			float* j = o + (hi ? kH27JH : kH27JL) + 9 * p;
+			for (int c = 0; c < 3; c++)
+				for (int r = 0; r < 3; r++) j[c * 3 + r] = Ji.c[c][r];
+			float& w = o[(hi ? kH27WH : kH27WL) + p];
+			w = detJ * (hi ? tb.w27[p] : 1.0f);
+			vsum += w;
+		}
+		for (int p = 0; p < np; p++) o[(hi ? kH27WH : kH27WL) + p] /= vsum;
+	}
+	float* QQ = o + kH27QQ;
+	float* QR = o + kH27QR;
+	for (int i = 0; i < 26; i++) QQ[i] = 0.0f;
+	for (int i = 0; i < 325; i++) QR[i] = 0.0f;
+	float vsum = 0.0f;
+	for (int p = 0; p < 27; p++) {
+		const M3 J = h27_map_jacobian(P, 27, p);
+		const M3 Ji = inverse3(J);
+		const float w = det3(J) * 1.0f * tb.w27[p];
+		float q[26][3];
+		for (int i = 0; i < 26; i++)
+			for (int r = 0; r < 3; r++) {
+				const float row[3] = {Ji.c[0][r], Ji.c[1][r], Ji.c[2][r]};
+				q[i][r] = dot3(row, tb.g27[p][i]);
+			}
+		vsum += w;
+		for (int i = 0; i < 26; i++) QQ[i] += w * dot3(q[i], q[i]);
+		int head = 0;
+		for (int i = 0; i < 26; i++)
+			for (int j = i + 1; j < 26; j++) QR[head++] += w * 2.0f * dot3(q[i], q[j]);
+	}
+	for (int i = 0; i < 26; i++) QQ[i] /= vsum;
+	for (int i = 0; i < 325; i++) QR[i] /= vsum;
+	float vol = 0.0f;
+	for (int p = 0; p < 8; p++) vol += det3(h27_map_jacobian(P, 8, p)) * 1.0f;
+	o[kH27Vol] = vol;
+	const int faces[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 4, 5}, {2, 3, 6, 7}, {0, 2, 4, 6}, {1, 3, 5, 7}};
+	float area = 0.0f;
+	for (int f = 0; f < 6; f++) {
+		float a[3], b[3];
+		for (int k = 0; k < 3; k++) {
+			a[k] = P[faces[f][0]][k] - P[faces[f][3]][k];
+			b[k] = P[faces[f][1]][k] - P[faces[f][2]][k];
+		}
+		const float c[3] = {a[1] * b[2] - b[1] * a[2], a[2] * b[0] - b[2] * a[0], a[0] * b[1] - b[0] * a[1]};
+		area += 0.5f * sqrtf(dot3(c, c));
+	}
+	o[kH27Area] = area;
+	float mmd[27], msum = 0.0f;
+	for (int n = 0; n < 27; n++) mmd[n] = 0.0f;
+	for (int p = 0; p < 27; p++) {
+		const float w = o[kH27WH + p];
+		for (int n = 0; n < 27; n++) {
+			const float Nn = tb.n27[p][n];
+			mmd[n] += w * Nn * Nn;
+			msum += w * Nn * Nn;
+		}
+	}
+	for (int n = 0; n < 27; n++) m[n] = (mmd[n] / msum) * density * vol;
+}
+
 // The Left / Right flags of a vertex (XPBDFEM/Geo.cpp:713-727) from the AABB
 // of the node data along x: bit 0 Left, bit 1 Right, bit 4 Pickable.
 XFEM_HD uint8_t vertex_flags(float x, float mn, float mx) {

@@ -11,7 +11,7 @@
 // at el_rec[k * nel + i]): Qi column-major, volume, surface area, the
 // prefactored QQ[9] and QR[36]. The map from the corners is linear, so one
 // Qi serves all four points; their shape-function gradients come from a
-// 120-float table (el_g4) that every thread reads at the same addresses.
+// 120-float table (el_tab) that every thread reads at the same addresses.
 #include "xfem_elements.cuh"
 
 namespace xfem {
@@ -28,7 +28,7 @@ struct QRec {
 	}
 };
 
-__device__ __forceinline__ float g4(const DevCtx& C, int p, int n, int k) { return __ldg(C.el_g4 + (p * 10 + n) * 3 + k); }
+__device__ __forceinline__ float g4(const DevCtx& C, int p, int n, int k) { return __ldg(C.el_tab + (p * 10 + n) * 3 + k); }
 
 // F = Qi MatMul(dN[0..8], P) at point p (XPBDFEM/Fem.cpp:311-316)
 __device__ __forceinline__ void q_def_grad(const DevCtx& C, const float Qi[3][3], int p, const Vec3 P[9], float F[3][3]) {
@@ -328,6 +328,7 @@ __device__ __noinline__ void q_pbd(const DevCtx& C, uint32_t i, float coeff) {
 }
 
 struct T10Elem {
+	static constexpr bool kWarp = false;
 	static constexpr uint32_t kVid4 = 3;
 	template <int KIND>
 	__device__ static void pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {

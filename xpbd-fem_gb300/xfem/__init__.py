@@ -92,10 +92,12 @@ EXPORTS = [
     "xfem_get_ring_schedule", "xfem_compute_ring_schedule", "xfem_body_hex_count", "xfem_get_hex_rest_state",
     "xfem_get_hex_schedule", "xfem_compute_hex_rest_state", "xfem_compute_hex_schedule", "xfem_generate_hex_block",
     "xfem_body_t10_count", "xfem_get_t10_rest_state", "xfem_get_t10_schedule", "xfem_compute_t10_edges",
-    "xfem_compute_t10_rest_state", "xfem_compute_t10_schedule",
+    "xfem_compute_t10_rest_state", "xfem_compute_t10_schedule", "xfem_body_h27_count", "xfem_get_h27_rest_state",
+    "xfem_get_h27_schedule", "xfem_compute_h27_mesh", "xfem_compute_h27_rest_state", "xfem_compute_h27_schedule",
 ]
 HEX_EP = 120  # floats per hex rest-state record (ElementParamsLinearHex flattened)
 T10_EP = 56  # floats per T10 rest-state record (ElementParamsQuadraticTet flattened)
+H27_EP = 703  # floats per H27 rest-state record (ElementParamsQuadraticHex flattened)
 
 _lib = None
 
@@ -154,6 +156,12 @@ def lib():
         L.xfem_compute_t10_edges.argtypes = [P, u32, P, P, P]
         L.xfem_compute_t10_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P, P]
         L.xfem_compute_t10_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.xfem_body_h27_count.argtypes = [P, u32, P, P, P]
+        L.xfem_get_h27_rest_state.argtypes = [P, u32, P, P, P]
+        L.xfem_get_h27_schedule.argtypes = [P, u32, P, P, P, P]
+        L.xfem_compute_h27_mesh.argtypes = [P, u32, P, P, P, P, P]
+        L.xfem_compute_h27_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P, P]
+        L.xfem_compute_h27_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
         _lib = L
     return _lib
 
@@ -282,6 +290,52 @@ def compute_t10_schedule(node_data, idx_data, morton=True):
     _check(lib().xfem_compute_t10_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
                                            _p(cb), C.byref(ncol)))
     return dict(vert_rank=rank, t10_order=order, colour_t10_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+def compute_h27_mesh(idx_data):
+    """Connectivity3d's edges and quads of a hex mesh and GeoQuadratic3d's H27
+    indices (no GPU): (edges[ne, 2], quads[nq, 4], h27[nh, 27])."""
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nh = ix.size // 9
+    edges = np.zeros((max(12 * nh, 1), 2), np.uint32)
+    quads = np.zeros((max(6 * nh, 1), 4), np.uint32)
+    h27 = np.zeros((nh, 27), np.uint32)
+    ne, nq = C.c_uint32(), C.c_uint32()
+    _check(lib().xfem_compute_h27_mesh(_p(ix), ix.size, _p(edges), _p(quads), _p(h27), C.byref(ne), C.byref(nq)))
+    return edges[:ne.value].copy(), quads[:nq.value].copy(), h27
+
+
+def compute_h27_rest_state(node_data, idx_data, density):
+    """Host-only rest state of a hex mesh read as H27s (no GPU):
+    (x[nv, 3] double, ep[nh, 703], w[nv], flags[nv]) over all vertices."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    edges, quads, h27 = compute_h27_mesh(ix)
+    nh = h27.shape[0]
+    nv = nd.size // 3 + edges.shape[0] + quads.shape[0] + nh
+    x = np.zeros((nv, 3), np.float64)
+    ep = np.zeros((nh, H27_EP), np.float32)
+    w = np.zeros(nv, np.float32)
+    fl = np.zeros(nv, np.uint8)
+    _check(lib().xfem_compute_h27_rest_state(_p(nd), nd.size, _p(ix), ix.size, density, _p(x), _p(ep), _p(w),
+                                             _p(fl)))
+    return x, ep, w, fl
+
+
+def compute_h27_schedule(node_data, idx_data, morton=True):
+    """Host-only H27 schedule (no GPU), in the form of Body.h27_schedule()."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    edges, quads, h27 = compute_h27_mesh(ix)
+    nh = h27.shape[0]
+    nv = nd.size // 3 + edges.shape[0] + quads.shape[0] + nh
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nh, np.uint32)
+    cb = np.zeros(nh + 1, np.uint32)
+    ncol = C.c_uint32()
+    _check(lib().xfem_compute_h27_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
+                                           _p(cb), C.byref(ncol)))
+    return dict(vert_rank=rank, h27_order=order, colour_h27_begin=cb[:ncol.value + 1], colours=ncol.value)
 
 
 def compute_rest_state(node_data, idx_data, density):
@@ -483,6 +537,33 @@ class Body:
         ncol = C.c_uint32()
         _check(lib().xfem_get_hex_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def h27_count(self, body=0):
+        """(H27s, edge nodes, face nodes) of an H27 body."""
+        n, ne, nq = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().xfem_body_h27_count(self._h, body, C.byref(n), C.byref(ne), C.byref(nq)))
+        return n.value, ne.value, nq.value
+
+    def h27_rest_state(self, body=0):
+        """Rest state of an H27 body: (ep[nh, 703], w[nv], h27[nh, 27])."""
+        nv = self.counts[body][0]
+        nh = self.h27_count(body)[0]
+        ep = np.zeros((nh, H27_EP), np.float32)
+        w = np.zeros(nv, np.float32)
+        h27 = np.zeros((nh, 27), np.uint32)
+        _check(lib().xfem_get_h27_rest_state(self._h, body, _p(ep), _p(w), _p(h27)))
+        return ep, w, h27
+
+    def h27_schedule(self, body=0):
+        """Vertex ranks, H27 order (colour-major) and colour offsets of an H27 body."""
+        nv = self.counts[body][0]
+        nh = self.h27_count(body)[0]
+        rank = np.zeros(nv, np.uint32)
+        order = np.zeros(nh, np.uint32)
+        cb = np.zeros(nh + 1, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_h27_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
+        return dict(vert_rank=rank, h27_order=order, colour_h27_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     def t10_count(self, body=0):
         """(T10s, edge nodes) of a T10 body."""
