@@ -26,7 +26,9 @@ shape the configuration names.
   YeohSkinFast, Mixed, CubeNeo) with the oracle port's single-thread hex substep as
   its CPU baseline, "t10": quadratic-tet mode on the same mesh's 1,572,864 tets
   read as T10s (MixedSel, YeohSkinFast) with the oracle port's single-thread
-  T10 substep as its CPU baseline,
+  T10 substep as its CPU baseline, "h27": quadratic-hex mode on a 96x48x24 block of
+  the grid read as 110,592 H27s (MixedSel, YeohSkinFast, Mixed) with the oracle
+  port's single-thread H27 substep as its CPU baseline,
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -302,6 +304,7 @@ def run_xfem(args, world, rank, local):
     setup = None if args.no_setup else run_setup(stream)
     hexes = None if args.no_hexes else run_hexes(stream)
     t10 = None if args.no_t10 else run_t10(stream)
+    h27 = None if args.no_h27 else run_h27(stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -326,6 +329,7 @@ def run_xfem(args, world, rank, local):
         "setup": setup,
         "hexes": hexes,
         "t10": t10,
+        "h27": h27,
         "clocks": clk.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -650,6 +654,49 @@ def run_t10(stream, frames=5, cpu_budget_s=6.0):
                              "sample": "%d substeps of the same mesh (MixedSel)" % n}}
 
 
+def run_h27(stream, frames=5, cpu_budget_s=6.0):
+    """Quadratic-hex mode: a 96x48x24 block of the throughput grid (same
+    spacing and jitter) read as 110,592 H27s (GeoQuadratic3d: nodes on the
+    edges, faces and centres, 27-node elements on the 2x2x2 and 3x3x3 rules;
+    one warp per element) with MixedSel, YeohSkinFast and Mixed, device-timed
+    frames of 20 substeps with L2 flushed between frames; and the oracle port
+    of the reference's H27 substep on one host thread on the same mesh (a
+    bounded sample of substeps) as the CPU baseline."""
+    import torch
+
+    import oracle
+    import xfem
+    from xfem import workloads as W
+    w = dict(W.throughput_hex(W=96, H=48, D=24), lock=None)
+    nh = w["idx"].size // 9
+    S = w["substeps"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    solve = (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT | xfem.ELEMENT_H27
+    cases = (("mixed_sel", dict(w["settings"], flags=w["settings"]["flags"] | xfem.ELEMENT_H27)),
+             ("yeoh_skin_fast", dict(w["settings"], flags=(xfem.ENERGY_YEOH_SKIN_FAST << xfem.ENERGY_BIT) | solve,
+                                     compliance=3.2e-4)),
+             ("mixed", dict(w["settings"], flags=(xfem.ENERGY_MIXED << xfem.ENERGY_BIT) | solve)))
+    out = {}
+    for key, s_ in cases:
+        r = time_frames(stream, w, s_, flush, frames)
+        r["value"] = nh * S / (r["ms_per_frame"] / 1e3)
+        r.pop("sync_mode")
+        r.pop("block")
+        out[key] = r
+    q = oracle.QuadraticHex(w["nodes"], w["idx"], w["density"])
+    order = q.schedule()["hex_order"]
+    p = oracle.params_from_settings(w["settings"], w["dt"] / S, lock=False)
+    X, wi = q.X0.copy(), q.w.copy()
+    n, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < cpu_budget_s or n == 0:
+        X, V, wi, _ = q.substeps(X, np.zeros_like(X), wi, order, 1, p)
+        n += 1
+    cpu = nh * n / (time.perf_counter() - t0)
+    return {"workload": w["name"] + " as H27s", "unit": "H27-substeps/s", "vertices": int(q.X0.shape[0]), **out,
+            "cpu_baseline": {"value": cpu, "unit": "H27-substeps/s", "cores": 1, "kind": "port",
+                             "sample": "%d substeps of the same mesh (MixedSel)" % n}}
+
+
 def C_void_p(v):
     import ctypes
     return ctypes.c_void_p(v)
@@ -679,6 +726,7 @@ def main():
     ap.add_argument("--no-setup", action="store_true")
     ap.add_argument("--no-hexes", action="store_true")
     ap.add_argument("--no-t10", action="store_true")
+    ap.add_argument("--no-h27", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")

@@ -7,6 +7,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <thread>
 #include <vector>
 
 #include "xfem_internal.h"
@@ -654,12 +655,25 @@ void h27_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, u
 		}
 	}
 	for (uint32_t i = 0; i < n; i++) vflags[i] = rest::vertex_flags((float)X[3 * (size_t)i], mn[0], mx[0]);
-	for (uint32_t h = 0; h < nhexes; h++) {
-		const uint32_t* is = h27 + 27 * (size_t)h;
-		float m[27];
-		rest::h27(X, is, density, ep + (size_t)rest::kH27Rec * h, m);
-		for (int c = 0; c < 27; c++) w[is[c]] += m[c];
+	// the records on all host threads (each H27's own), then the masses
+	// accumulated in element order
+	std::vector<float> m(27 * (size_t)nhexes);
+	(void)rest::h27_tables();  // built once, before the threads read it
+	const uint32_t nth = std::max(1u, std::min(std::thread::hardware_concurrency(), 64u));
+	auto work = [&](uint32_t t) {
+		for (uint32_t h = t; h < nhexes; h += nth)
+			rest::h27(X, h27 + 27 * (size_t)h, density, ep + (size_t)rest::kH27Rec * h, &m[27 * (size_t)h]);
+	};
+	if (nhexes < 256 || nth == 1) {
+		work(0);
+		for (uint32_t t = 1; t < nth; t++) work(t);
+	} else {
+		std::vector<std::thread> pool;
+		for (uint32_t t = 0; t < nth; t++) pool.emplace_back(work, t);
+		for (std::thread& th : pool) th.join();
 	}
+	for (uint32_t h = 0; h < nhexes; h++)
+		for (int c = 0; c < 27; c++) w[h27[27 * (size_t)h + c]] += m[27 * (size_t)h + c];
 	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
 }
 
