@@ -302,9 +302,9 @@ def run_xfem(args, world, rank, local):
     damped = None if args.no_damped else run_damped(stream)
     models = None if args.no_models else run_models(stream)
     setup = None if args.no_setup else run_setup(stream)
-    hexes = None if args.no_hexes else run_hexes(stream)
-    t10 = None if args.no_t10 else run_t10(stream)
-    h27 = None if args.no_h27 else run_h27(stream)
+    hexes = None if args.no_hexes else run_hexes(stream, cpu=not args.no_cpu)
+    t10 = None if args.no_t10 else run_t10(stream, cpu=not args.no_cpu)
+    h27 = None if args.no_h27 else run_h27(stream, cpu=not args.no_cpu)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -563,7 +563,7 @@ def run_models(stream, frames=5):
             "cost": {k: out[k]["ms_per_frame"] / out["mixed_sel"]["ms_per_frame"] for k, _ in cases[1:]}}
 
 
-def run_hexes(stream, frames=5, cpu_budget_s=6.0):
+def run_hexes(stream, frames=5, cpu_budget_s=6.0, cpu=True):
     """Hex mode: the throughput grid as 262,144 linear hexahedra (the same
     jittered nodes; each hex is the 6 tets of the tet mesh's cube) with
     MixedSel, YeohSkinFast, Mixed (2x2x2 quadrature) and CubeNeo (its short
@@ -593,6 +593,8 @@ def run_hexes(stream, frames=5, cpu_budget_s=6.0):
         r.pop("sync_mode")
         r.pop("block")
         out[key] = r
+    if not cpu:
+        return {"workload": w["name"], "unit": "hex-substeps/s", **out}
     # CPU: the oracle's float restatement, one thread, the reference's
     # algorithm in the GPU's hex order
     hexes, _ = oracle.parse_hexes(w["idx"])
@@ -611,7 +613,7 @@ def run_hexes(stream, frames=5, cpu_budget_s=6.0):
             "vs_tet_mesh_of_the_same_grid": "each hex covers the 6 tets of one cube of the throughput mesh"}
 
 
-def run_t10(stream, frames=5, cpu_budget_s=6.0):
+def run_t10(stream, frames=5, cpu_budget_s=6.0, cpu=True):
     """Quadratic-tet mode: the throughput mesh's 1,572,864 tets read as T10s
     (GeoQuadratic3d: a node on each of the 1.9 M edges, 10-node elements on
     the 4-point rule) with MixedSel and YeohSkinFast, device-timed frames of
@@ -638,6 +640,8 @@ def run_t10(stream, frames=5, cpu_budget_s=6.0):
         r.pop("sync_mode")
         r.pop("block")
         out[key] = r
+    if not cpu:
+        return {"workload": w["name"] + " as T10s", "unit": "T10-substeps/s", **out}
     # CPU: the oracle's float restatement, one thread, the reference's
     # algorithm in the GPU's T10 order
     q = oracle.Quadratic(w["nodes"], w["idx"], w["density"])
@@ -654,7 +658,7 @@ def run_t10(stream, frames=5, cpu_budget_s=6.0):
                              "sample": "%d substeps of the same mesh (MixedSel)" % n}}
 
 
-def run_h27(stream, frames=5, cpu_budget_s=6.0):
+def run_h27(stream, frames=5, cpu_budget_s=6.0, cpu=True):
     """Quadratic-hex mode: a 96x48x24 block of the throughput grid (same
     spacing and jitter) read as 110,592 H27s (GeoQuadratic3d: nodes on the
     edges, faces and centres, 27-node elements on the 2x2x2 and 3x3x3 rules;
@@ -683,6 +687,8 @@ def run_h27(stream, frames=5, cpu_budget_s=6.0):
         r.pop("sync_mode")
         r.pop("block")
         out[key] = r
+    if not cpu:
+        return {"workload": w["name"] + " as H27s", "unit": "H27-substeps/s", **out}
     q = oracle.QuadraticHex(w["nodes"], w["idx"], w["density"])
     order = q.schedule()["hex_order"]
     p = oracle.params_from_settings(w["settings"], w["dt"] / S, lock=False)
