@@ -219,9 +219,10 @@ __device__ __forceinline__ const BodyParams& body_of_el(const DevCtx& C, uint32_
 // The persistent element kernel (cooperative launch, co-resident grid). E:
 // the element type (kVid4 uint4 of vertex ids per element; pass<KIND>, pbd;
 // kWarp: one warp per element, every lane of the warp calling with the same
-// element, else one thread per element).
+// element, else one thread per element; kMinBlocks: the blocks per SM the
+// register budget is sized for).
 template <class E>
-__global__ void __launch_bounds__(256) k_elements(DevCtx C, uint32_t nsub, float dt) {
+__global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint32_t nsub, float dt) {
 	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
 	// the element loops run over units: threads, or warps (warp-uniform i)

@@ -567,6 +567,7 @@ __device__ __noinline__ void hex_pbd(const DevCtx& C, uint32_t i, float coeff) {
 
 struct HexElem {
 	static constexpr bool kWarp = false;
+	static constexpr int kMinBlocks = 1;
 	static constexpr uint32_t kVid4 = 2;
 	template <int KIND>
 	__device__ static void pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {

@@ -329,6 +329,7 @@ __device__ __noinline__ void q_pbd(const DevCtx& C, uint32_t i, float coeff) {
 
 struct T10Elem {
 	static constexpr bool kWarp = false;
+	static constexpr int kMinBlocks = 1;
 	static constexpr uint32_t kVid4 = 3;
 	template <int KIND>
 	__device__ static void pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {
