@@ -404,7 +404,7 @@ __device__ __noinline__ void h27_pbd(const DevCtx& C, uint32_t i, float coeff) {
 
 struct H27Elem {
 	static constexpr bool kWarp = true;
-	static constexpr int kMinBlocks = 1;
+	static constexpr int kMinBlocks = 3;  // at most 85 registers: three 256-thread blocks per SM
 	static constexpr uint32_t kVid4 = 7;
 	template <int KIND>
 	__device__ static void pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {

@@ -24,6 +24,8 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "xfem_device.cuh"
 #include "xfem_internal.h"
@@ -807,8 +809,24 @@ __global__ void k_volume(const float4* __restrict__ vert, const uint32_t* __rest
 
 size_t solve_smem_bytes(int block, uint32_t warp_smem) { return (size_t)(block / 32) * warp_smem; }
 
+// The dynamic shared-memory limit is a property of the kernel, shared by
+// every handle in the process: it only ever grows to the largest size any
+// handle launches with (a larger limit does not restrict smaller launches),
+// so one handle's configuration cannot lower another's below what it needs.
 static void set_smem_attr(const void* f, size_t bytes) {
+	static std::mutex mu;
+	static std::vector<std::pair<const void*, size_t>> done;
+	std::lock_guard<std::mutex> lk(mu);
+	for (auto& d : done)
+		if (d.first == f) {
+			if (bytes > d.second) {
+				cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+				d.second = bytes;
+			}
+			return;
+		}
 	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+	done.emplace_back(f, bytes);
 }
 
 static const void* persistent_fn(bool lambdas, bool ext) {
@@ -1000,6 +1018,7 @@ int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bo
 	cudaStream_t st = (cudaStream_t)stream;
 	const void* f = persistent_fn(lambdas, ctx.ext != 0u);
 	const size_t smem = solve_smem_bytes(block, warp_smem);
+	set_smem_attr(f, smem);  // no allocation: the kernel's shared-memory limit
 	int sms = 0, per_sm = 0;
 	cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, smem);
