@@ -28,7 +28,8 @@ shape the configuration names.
   read as T10s (MixedSel, YeohSkinFast) with the oracle port's single-thread
   T10 substep as its CPU baseline, "h27": quadratic-hex mode on a 96x48x24 block of
   the grid read as 110,592 H27s (MixedSel, YeohSkinFast, Mixed) with the oracle
-  port's single-thread H27 substep as its CPU baseline,
+  port's single-thread H27 substep as its CPU baseline (each element line with
+  its MixedSel element bandwidth against the measured HBM peak),
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
   checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
@@ -305,6 +306,9 @@ def run_xfem(args, world, rank, local):
     hexes = None if args.no_hexes else run_hexes(stream, cpu=not args.no_cpu)
     t10 = None if args.no_t10 else run_t10(stream, cpu=not args.no_cpu)
     h27 = None if args.no_h27 else run_h27(stream, cpu=not args.no_cpu)
+    for kind, rec in (("hexes", hexes), ("t10", t10), ("h27", h27)):
+        if rec is not None:
+            rec["roofline"] = element_roofline(kind, rec)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
@@ -701,6 +705,24 @@ def run_h27(stream, frames=5, cpu_budget_s=6.0, cpu=True):
     return {"workload": w["name"] + " as H27s", "unit": "H27-substeps/s", "vertices": int(q.X0.shape[0]), **out,
             "cpu_baseline": {"value": cpu, "unit": "H27-substeps/s", "cores": 1, "kind": "port",
                              "sample": "%d substeps of the same mesh (MixedSel)" % n}}
+
+
+# Element bytes a MixedSel element-substep moves (vertex state read and
+# written, 32 B each way per vertex; the record fields the solve reads; the
+# vertex ids): hex 8 x 64 + 192, T10 10 x 64 + 224 + 48, H27 27 x 64 + 1,728
+# (the 2x2x2 rule's Ji and weights, QQ, QR, volume) + 108. Vertices are shared
+# between elements, so DRAM sees less than this when they stay in L2.
+ELEMENT_BYTES = {"hexes": 8 * 64 + 192, "t10": 10 * 64 + 224 + 48, "h27": 27 * 64 + 1728 + 108}
+
+
+def element_roofline(kind, line):
+    """The element kernel's element bandwidth on the MixedSel case against
+    the measured HBM copy bandwidth."""
+    hbm, peak_kind = peaks()
+    achieved = ELEMENT_BYTES[kind] * line["mixed_sel"]["value"] / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "peak_kind": peak_kind, "bytes_per_element_substep": ELEMENT_BYTES[kind],
+            "note": "element bytes, not DRAM traffic: shared vertices hit in L2"}
 
 
 def C_void_p(v):
