@@ -13,8 +13,9 @@
 // owns quadrature point p when the deformation gradients are formed. The
 // node offsets P and each point's G Ji (the energy gradient mapped back to
 // the reference frame) pass between the two through 2.2 KB of shared memory
-// per warp. Sums over lanes are xor butterflies, so every lane holds the same
-// bits and every lane takes the same branch.
+// per warp, next to the warp's copy of the element's record. Sums over lanes
+// are xor butterflies, so every lane holds the same bits and every lane takes
+// the same branch.
 //
 // Records: 704 floats per H27 (the 703 of the reference's flattening, one
 // pad), element-major, read by every lane of the element's warp. The
@@ -36,22 +37,25 @@ __device__ __forceinline__ float wsum(float v) {
 	return v;
 }
 
-// per-warp scratch: node offsets from node 26, and each point's G Ji for the
-// first and the second constraint
+// per-warp scratch: the element's record (copied in once per element, so
+// the lanes' scattered reads of it wait on shared memory, not on L2), node
+// offsets from node 26, and each point's G Ji for the first and the second
+// constraint
 struct Scratch {
+	float4 rec[kRec / 4];
 	float P[26][3];
 	float M0[27][9], M1[27][9];
 };
 
 struct Elem {
-	const float* R;  // the record
+	const float* R;  // the record (this warp's shared copy)
 	uint32_t lane;
 	float4 O, D;  // this lane's node (lanes >= 27: zero)
 	float w;
 	uint32_t dv;
 };
 
-__device__ __forceinline__ float rec(const Elem& E, int j) { return __ldg(E.R + j); }
+__device__ __forceinline__ float rec(const Elem& E, int j) { return E.R[j]; }
 
 // P_n = (O_n - O_26) + (D_n - D_26) (solve), or O_n - O_26 (vmode)
 __device__ __forceinline__ void share_rel(Scratch& s, const Elem& E, bool vmode) {
@@ -243,9 +247,15 @@ __device__ __forceinline__ Scratch& scratch() {
 	return s[threadIdx.x >> 5];
 }
 
-__device__ __forceinline__ void load(const DevCtx& C, uint32_t i, Elem& E) {
+__device__ __forceinline__ void load(const DevCtx& C, uint32_t i, Scratch& s, Elem& E) {
 	E.lane = threadIdx.x & 31u;
-	E.R = reinterpret_cast<const float*>(C.el_rec) + (size_t)i * kRec;
+	// the record, 176 float4, coalesced across the warp, once every lane is
+	// done with the previous element's copy
+	__syncwarp();
+	const float4* src = C.el_rec + (size_t)i * (kRec / 4);
+	for (uint32_t k = E.lane; k < kRec / 4; k += 32) s.rec[k] = __ldg(src + k);
+	__syncwarp();
+	E.R = reinterpret_cast<const float*>(s.rec);
 	E.O = E.D = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	E.w = 0.0f;
 	E.dv = 0;
@@ -261,7 +271,7 @@ template <int KIND>
 __device__ __noinline__ void h27_pass(const DevCtx& C, uint32_t i, float inv_dt, float inv_dt2, float rd) {
 	Scratch& s = scratch();
 	Elem E;
-	load(C, i, E);
+	load(C, i, s, E);
 	const BodyParams& bp = C.bodies[__float_as_uint(__shfl_sync(kAll, E.D.w, 0)) >> 8];
 	const uint32_t e = __ldg(&bp.energy);
 	if (KIND != kVolume && (e == 11u || e == 12u)) return;  // SolveElementCube acts on 8-node hexes only
@@ -373,8 +383,9 @@ __device__ __noinline__ void h27_pass(const DevCtx& C, uint32_t i, float inv_dt,
 // PbdDamp over the 27 nodes (XPBDFEM/Xpbd.h:306-346) on the canonical state
 // (O = X, D = V), the coefficient coeff / surfaceArea capped at 1.
 __device__ __noinline__ void h27_pbd(const DevCtx& C, uint32_t i, float coeff) {
+	Scratch& s = scratch();
 	Elem E;
-	load(C, i, E);
+	load(C, i, s, E);
 	const bool node = E.lane < 27;
 	const float damping = fminf(1.0f, coeff / rec(E, kArea));
 	const float Wavg = (1.0e-8f + wsum(E.w)) * (1.0f / 27.0f), Wmin = 0.0001f * Wavg;
