@@ -63,7 +63,7 @@ UNIT = "tet-substeps/s"
 # w 4 B) x V/T.
 REC_BYTES, VERT_BYTES = 80.0, 76.0
 # DRAM bytes (read + write) per tet-substep of the persistent kernel, from the
-# ncu capture summarised in profiles/k_persistent_throughput_128x64x32.md
+# ncu capture of the same command (one k_persistent launch, --set full).
 # (2.143 GB per launch of 20 substeps x 1,572,864 tets).
 NCU_DRAM_BYTES_PER_TET_SUBSTEP = 68.12
 
