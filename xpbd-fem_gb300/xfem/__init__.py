@@ -5,8 +5,12 @@ construct it from the tagged index stream and node array exactly as
 GeoLinear3d::Init is called (XPBDFEM/Geo.cpp:697), then call `substep(dt)`
 (Geo3d::Substep, XPBDFEM/Geo.cpp:305) or `step_frames(...)` (the substep loop
 of Sim::Update, XPBDFEM/Demo.cpp:67-90). `Settings` mirrors struct Settings
-(XPBDFEM/Settings.h:79-102). All compute runs in libxfem.so on the GPU; there
-is no CPU fallback: without the library or a CUDA device every call raises.
+(XPBDFEM/Settings.h:79-102). A hex stream (tag 8) is GeoLinear3d's hex
+path; element type T10 or H27 in the settings' flags bits 0-3 makes a body
+GeoQuadratic3d (XPBDFEM/Geo.cpp:836): a tet stream becomes T10s, a hex stream
+H27s, and the body's vertices gain the added nodes. All compute runs in
+libxfem.so on the GPU; there is no CPU fallback: without the library or a
+CUDA device every call raises.
 """
 import ctypes as C
 import os
