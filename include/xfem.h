@@ -64,6 +64,7 @@ extern "C" {
 #define XFEM_ECUDA (-4)           /* CUDA runtime error (no device, launch or copy failure) */
 #define XFEM_EDEVICE_TIMEOUT (-5) /* a device-side bounded wait (grid barrier) ran out */
 #define XFEM_ELIMIT (-6)          /* a schedule limit was exceeded (colours, cluster size) */
+#define XFEM_ENONFINITE (-7)      /* a position or velocity became NaN or infinite (device sentinel) */
 
 /* ---- flags: the reference's Settings::flags layout (XPBDFEM/Settings.h:9-29) - */
 #define XFEM_ELEMENT_TYPE_MASK 15u      /* Settings_ElementTypeMask, bits 0-3 (XPBDFEM/Settings.h:9-10, 31-39): */
@@ -147,6 +148,9 @@ typedef struct xfem_options {
 	void* stream;          /* cudaStream_t to run on; NULL = a stream owned by the handle */
 	uint32_t host_setup;   /* 1 = rest state and schedule on the host (default: their parallel
 	                          phases on the GPU; the result is the same bit for bit) */
+	uint32_t wait_timeout_ms; /* limit of every bounded device wait (grid barrier, chunk copy,
+	                             neighbour chunk); 0 = 2000 ms. A wait that runs out makes the
+	                             call report XFEM_EDEVICE_TIMEOUT and leaves the context usable */
 } xfem_options;
 
 /* One mesh for xfem_batch_create, in GeoLinear3d::Init's argument form. */
@@ -223,23 +227,48 @@ int xfem_substep(xfem_body* b, float dt);
 int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
 /* No counterpart in the reference. The same stepping as xfem_step_frames
  * for callers that cannot allocate device memory when they step: a process
- * whose device memory is fully reserved by another allocator, a real-time
- * loop that must not take cudaMalloc's device-wide synchronisation, or code
- * running while a stream is captured (cudaMalloc is not permitted there).
- * It always runs the persistent kernel at the handle's block size, never the
- * autotuner or the CUDA-graph builder (which may allocate), and calls no
- * cudaMalloc, cudaFree or other allocating routine. The kernel's scratch (the
- * grid-barrier counter and the device error word) lives in one fixed 256-byte
- * device array that every GPU loading the library keeps until exit; all calls
- * share it, so calls whose kernels overlap on one GPU race and must not be
- * issued. The first call on a device looks the array's device address up; make
- * that first call before any stream capture. Limit: frames * substeps *
- * colours * persistent blocks must stay below 2^31 per call (else
- * XFEM_ELIMIT). Synchronises the handle's stream and reports device errors. */
+ * whose device memory is fully reserved by another allocator (a framework's
+ * caching pool), or a real-time loop that must not take cudaMalloc's
+ * device-wide synchronisation. It always runs the persistent kernel at the
+ * handle's block size, never the autotuner or the CUDA-graph builder (which
+ * may allocate), and calls no cudaMalloc, cudaFree or other allocating
+ * routine. The kernel's scratch (the grid-barrier counter and the device
+ * error word) lives in one fixed 256-byte device array that every GPU loading
+ * the library keeps until exit; all calls share it, so calls whose kernels
+ * overlap on one GPU race and must not be issued. The first call on a device
+ * looks the array's device address up; make that first call before any
+ * stream capture. Limit: one call's grid-barrier arrivals, substeps x passes
+ * per substep (colours, times 1 + volume sweeps + damping kinds when those
+ * run) x persistent blocks, must stay below 2^31 (else XFEM_ELIMIT; split
+ * the call). Hex, T10 and H27 handles step with their own scratch, allocated
+ * at create time. Synchronises the handle's stream and reports device errors. */
 int xfem_step_frames_noalloc(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
 /* Waits for queued work; returns XFEM_EDEVICE_TIMEOUT if a bounded device
- * wait ran out since the last check. */
+ * wait ran out since the last check, XFEM_ENONFINITE if a finished position
+ * or velocity was NaN or infinite. */
 int xfem_synchronize(xfem_body* b);
+
+/* ---- failure-detection test hooks --------------------------------------------- */
+/* No counterpart in the reference, whose only checks are asserts
+ * (XPBDFEM/Allocator.cpp:5-10, XPBDFEM/Connectivity.cpp:261-263). They make
+ * the failures the library detects happen on purpose, without faulting the
+ * GPU, so that the detection can be tested.
+ *   XFEM_HOOK_MISSING_ARRIVAL (handle): the next stepping call's bounded
+ *     device waits (grid barriers; neighbour-chunk waits in dataflow mode)
+ *     expect `value` arrivals more than the blocks make, so they run out
+ *     after the handle's wait_timeout_ms; the call (or the next synchronising
+ *     one) reports XFEM_EDEVICE_TIMEOUT. One call only; the CUDA-graph launch
+ *     form has no grid barrier and ignores it.
+ *   XFEM_HOOK_BARRIER_BASE (handle): value 1 starts the grid-barrier arrival
+ *     counter at 2^32 - 1 in every persistent launch, so the first barrier
+ *     wraps it (the results must not change); 0 starts it at 0.
+ *   XFEM_HOOK_FAIL_ALLOC (process-wide, b may be NULL): the value-th device
+ *     buffer allocation from now on fails as if the device were full
+ *     (XFEM_ENOMEM); 0 turns it off. */
+#define XFEM_HOOK_MISSING_ARRIVAL 1u
+#define XFEM_HOOK_BARRIER_BASE 2u
+#define XFEM_HOOK_FAIL_ALLOC 3u
+int xfem_test_hook(xfem_body* b, uint32_t hook, uint32_t value);
 
 /* ---- reverse-mode adjoint ---------------------------------------------------- */
 /* No counterpart in the reference, which only steps forward: the derivative

@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) k_reverse(DevCtx C, AdjCtx A, uint32_t ns
 	const uint32_t wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
 	const uint32_t gwarp = wib * gridDim.x + blockIdx.x, nwarps = wpb * gridDim.x;
 	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
-	uint32_t target = 0;
+	uint32_t target = C.bar_base;
 	for (uint32_t v = gtid; v < C.nverts; v += nthreads) finalize_reverse(C, A, v, nsub, inv_dt, last != 0);
 	bool ok = grid_sync(C, target);
 	if (ok) isolated_reverse(C, A, gtid, nthreads, nsub, dt);
@@ -515,7 +515,7 @@ int launch_reverse(const DevCtx& ctx, const AdjCtx& adj, int block, uint32_t, ui
 	// block i % grid, so a colour pass with fewer chunks than warps still
 	// spreads one chunk per SM (a pass lasts as long as its slowest chunk)
 	const uint32_t blocks = (uint32_t)(per_sm * sms);
-	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+	e = reset_barrier(ctx, st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
 	AdjCtx a = adj;

@@ -32,8 +32,22 @@ int fail(int code, const std::string& msg) {
 #define XCUDA(call)                                                                                    \
 	do {                                                                                               \
 		cudaError_t e_ = (call);                                                                       \
-		if (e_ != cudaSuccess) return fail(XFEM_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+		if (e_ != cudaSuccess)                                                                         \
+			return fail(e_ == cudaErrorMemoryAllocation ? XFEM_ENOMEM : XFEM_ECUDA,                    \
+			            std::string(#call) + ": " + cudaGetErrorString(e_));                           \
 	} while (0)
+
+// Test hook XFEM_HOOK_FAIL_ALLOC: the n-th device allocation from the
+// handles' buffers fails as if the device were full (0 = off).
+std::atomic<uint32_t> g_fail_alloc_in{0};
+
+cudaError_t injected_alloc_failure() {
+	uint32_t n = g_fail_alloc_in.load();
+	while (n != 0) {
+		if (g_fail_alloc_in.compare_exchange_weak(n, n - 1)) return n == 1 ? cudaErrorMemoryAllocation : cudaSuccess;
+	}
+	return cudaSuccess;
+}
 
 // Element kinds of a body: linear tets (the chunked tet path, the one-ring
 // mode), linear hexahedra (H8), quadratic tets (T10) and quadratic hexahedra
@@ -77,6 +91,10 @@ struct DevBuf {
 			p = nullptr;
 		}
 		n = count;
+		if (injected_alloc_failure() != cudaSuccess) {
+			n = 0;
+			return cudaErrorMemoryAllocation;
+		}
 		return cudaMalloc((void**)&p, sizeof(T) * (count ? count : 1));
 	}
 	// keeps the buffer when it is already large enough
@@ -140,6 +158,7 @@ struct xfem_body {
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
+	uint32_t hook_wait_miss = 0;  // XFEM_HOOK_MISSING_ARRIVAL for the next stepping call
 	bool tuned = false;
 	// cached CUDA graph (graph mode)
 	cudaGraphExec_t graph = nullptr;
@@ -304,14 +323,25 @@ float tet_c0(const BodyHost& b, uint32_t t) {
 	return 1.0f / mu / b.ep[17 * (size_t)t + 15];
 }
 
+// Status and message of a device error word (kErr*).
+int device_error(int e) {
+	switch (e) {
+	case kErrBarrierTimeout: return fail(XFEM_EDEVICE_TIMEOUT, "device grid barrier timed out");
+	case kErrCopyTimeout: return fail(XFEM_EDEVICE_TIMEOUT, "device wait for a chunk copy timed out");
+	case kErrDepTimeout: return fail(XFEM_EDEVICE_TIMEOUT, "device wait for a neighbouring chunk timed out");
+	case kErrNonFinite: return fail(XFEM_ENONFINITE, "a position or velocity became NaN or infinite");
+	default: return fail(XFEM_ECUDA, "device error " + std::to_string(e));
+	}
+}
+
 int check_device_error(xfem_body* h) {
 	int e = 0;
 	XCUDA(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
 	XCUDA(cudaStreamSynchronize(h->stream));
 	if (e != 0) {
 		XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
-		if (e == kErrBarrierTimeout) return fail(XFEM_EDEVICE_TIMEOUT, "device grid barrier timed out");
-		return fail(XFEM_ECUDA, "device error " + std::to_string(e));
+		XCUDA(cudaStreamSynchronize(h->stream));
+		return device_error(e);
 	}
 	return XFEM_OK;
 }
@@ -342,6 +372,42 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	b.nt = (uint32_t)(b.tets.size() / 4);
 	b.nh = (uint32_t)(b.elems.size() / 8);
 	b.nodes.assign(m.node_data, m.node_data + m.node_data_count);
+	return XFEM_OK;
+}
+
+// The argument checks of prepare_mesh and validate_settings for every body,
+// made before any device is touched: a bad tag, a truncated stream, a vertex
+// count that does not match the node array or invalid settings fail the same
+// way with or without a GPU.
+int precheck_inputs(uint32_t nb, const xfem_mesh* meshes, const xfem_settings* settings) {
+	for (uint32_t k = 0; k < nb; k++) {
+		const xfem_mesh& m = meshes[k];
+		const std::string who = nb > 1 ? "body " + std::to_string(k) + ": " : std::string();
+		if (!m.node_data || !m.idx_data) return fail(XFEM_EINVAL, who + "null mesh array");
+		if (m.node_data_count % 3) return fail(XFEM_EINVAL, who + "node_data_count must be a multiple of 3");
+		uint32_t ntag[2] = {0, 0};
+		uint64_t nv = 0;
+		for (uint32_t i = 0; i < m.idx_data_count;) {
+			const uint32_t tag = m.idx_data[i];
+			if (tag != 4u && tag != 8u)
+				return fail(XFEM_EINVAL, who + "unknown element tag " + std::to_string(tag) + " at " + std::to_string(i));
+			if ((uint64_t)i + tag >= m.idx_data_count) return fail(XFEM_EINVAL, who + "truncated index stream");
+			for (uint32_t j = 1; j <= tag; j++) nv = std::max<uint64_t>(nv, (uint64_t)m.idx_data[i + j] + 1u);
+			ntag[tag == 8u]++;
+			i += tag + 1;
+		}
+		if (ntag[0] && ntag[1])
+			return fail(XFEM_EUNSUPPORTED, who + "meshes mixing tets (tag 4) and hexes (tag 8) are not supported");
+		if (nv != m.node_data_count / 3)
+			return fail(XFEM_EINVAL, who + "vertex count " + std::to_string(nv) +
+			                             " implied by the index stream != node_data_count/3 = " +
+			                             std::to_string(m.node_data_count / 3));
+		if (!(m.density > 0.0f)) return fail(XFEM_EINVAL, who + "density must be > 0");
+		if (settings) {
+			const int rc = validate_settings(settings[k]);
+			if (rc) return fail(rc, who + g_err);
+		}
+	}
 	return XFEM_OK;
 }
 
@@ -1113,6 +1179,7 @@ int build_device(xfem_body* h) {
 	c.ncolours = ncol;
 	c.bar_count = h->bar.p;
 	c.err = h->err.p;
+	c.timeout_ns = h->opt.wait_timeout_ms ? (uint64_t)h->opt.wait_timeout_ms * 1000000ull : kDefaultTimeoutNs;
 	h->cfg.lambdas = h->opt.keep_lambdas != 0;
 	h->cfg.ext = c.ext != 0u;
 	c.ring_hdr = h->ring_hdr.p;
@@ -1266,6 +1333,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
 	const uint32_t mode = h->opt.cluster_mode == 1 ? 0u : 1u;
 	const uint32_t morton = h->opt.no_morton ? 0u : 1u;
+	if (const int prc = precheck_inputs(nbodies, meshes, settings)) return prc;
 	int ndev = 0;
 	if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(XFEM_ECUDA, "no CUDA device");
 	h->device = h->opt.device > 0 ? h->opt.device : 0;
@@ -1311,22 +1379,39 @@ BodyHost* body_of(xfem_body* h, uint32_t body) {
 	return &h->bodies[body];
 }
 
+// The element and one-ring launches (no autotuner, no CUDA graph).
+int launch_mode(xfem_body* h, const DevCtx& ctx, uint32_t nsub, float dt) {
+	if (h->ring_mode) {
+		const int e = launch_rings(ctx, 256, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
+		return XFEM_OK;
+	}
+	const int e = h->el_mode == kElH27 ? launch_h27(ctx, 256, nsub, dt, h->stream)
+	              : h->el_mode == kElT10 ? launch_t10(ctx, 256, nsub, dt, h->stream)
+	                                     : launch_hexes(ctx, 256, nsub, dt, h->stream);
+	if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
+	return XFEM_OK;
+}
+
+// Takes the pending XFEM_HOOK_MISSING_ARRIVAL into the context for one
+// launch; the destructor clears it again.
+struct WaitMissScope {
+	xfem_body* h;
+	explicit WaitMissScope(xfem_body* hh) : h(hh) {
+		h->ctx.wait_miss = h->hook_wait_miss;
+		h->hook_wait_miss = 0;
+	}
+	~WaitMissScope() { h->ctx.wait_miss = 0; }
+};
+
 int step(xfem_body* h, uint32_t nsub, float dt) {
 	if (!h) return fail(XFEM_EINVAL, "null handle");
 	if (!(dt > 0.0f) || !isfinite(dt)) return fail(XFEM_EINVAL, "dt must be > 0");
 	if (nsub == 0) return XFEM_OK;
 	XCUDA(cudaSetDevice(h->device));
-	if (h->ring_mode) {
-		const int e = launch_rings(h->ctx, 256, nsub, dt, h->stream);
-		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
-		return XFEM_OK;
-	}
-	if (h->el_mode) {
-		const int e = h->el_mode == kElH27 ? launch_h27(h->ctx, 256, nsub, dt, h->stream)
-		              : h->el_mode == kElT10 ? launch_t10(h->ctx, 256, nsub, dt, h->stream)
-		                                     : launch_hexes(h->ctx, 256, nsub, dt, h->stream);
-		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
-		return XFEM_OK;
+	if (h->ring_mode || h->el_mode) {
+		WaitMissScope miss(h);
+		return launch_mode(h, h->ctx, nsub, dt);
 	}
 	int rc = autotune(h, nsub, dt);
 	if (rc) return rc;
@@ -1338,6 +1423,7 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 		rc = set_config(h, 1, h->cfg.block);
 		if (rc) return rc;
 	}
+	WaitMissScope miss(h);
 	return run(h, nsub, dt);
 }
 
@@ -1554,23 +1640,41 @@ int xfem_step_frames_noalloc(xfem_body* h, uint32_t frames, uint32_t substeps, f
 	if (h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) have no allocation-free launch");
 	XCUDA(cudaSetDevice(h->device));
+	WaitMissScope miss(h);
 	if (h->el_mode) {
-		// the element launches allocate nothing
-		const int e = h->el_mode == kElH27 ? launch_h27(h->ctx, 256, (uint32_t)n, dt, h->stream)
-		              : h->el_mode == kElT10 ? launch_t10(h->ctx, 256, (uint32_t)n, dt, h->stream)
-		                                     : launch_hexes(h->ctx, 256, (uint32_t)n, dt, h->stream);
-		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
-		return check_device_error(h);
+		// the element launches use the handle's own scratch and allocate nothing
+		const int rc = launch_mode(h, h->ctx, (uint32_t)n, dt);
+		return rc ? rc : check_device_error(h);
 	}
 	int dev_err = 0;
 	const int e = launch_substeps_noalloc(h->ctx, h->cfg.block, h->cfg.warp_smem, h->cfg.lambdas, (uint32_t)n, dt,
 	                                      h->stream, h->device, &dev_err);
-	if (e == (int)cudaErrorInvalidValue)
-		return fail(XFEM_ELIMIT, "frames * substeps * colours * persistent blocks must stay below 2^31 per call");
+	if (e == kNoAllocTooLong)
+		return fail(XFEM_ELIMIT, "one call's grid-barrier arrivals (substeps x passes per substep x persistent "
+		                         "blocks) must stay below 2^31; split the call");
 	if (e) return fail(XFEM_ECUDA, std::string("allocation-free launch: ") + cudaGetErrorString((cudaError_t)e));
-	if (dev_err == kErrBarrierTimeout) return fail(XFEM_EDEVICE_TIMEOUT, "device grid barrier timed out");
-	if (dev_err) return fail(XFEM_ECUDA, "device error " + std::to_string(dev_err));
+	if (dev_err) return device_error(dev_err);
 	return XFEM_OK;
+}
+
+int xfem_test_hook(xfem_body* b, uint32_t hook, uint32_t value) {
+	if (hook == XFEM_HOOK_FAIL_ALLOC) {
+		g_fail_alloc_in.store(value);
+		return XFEM_OK;
+	}
+	if (!b) return fail(XFEM_EINVAL, "null handle");
+	switch (hook) {
+	case XFEM_HOOK_MISSING_ARRIVAL: b->hook_wait_miss = value; return XFEM_OK;
+	case XFEM_HOOK_BARRIER_BASE:
+		if (value > 1u) return fail(XFEM_EINVAL, "XFEM_HOOK_BARRIER_BASE takes 0 or 1");
+		b->ctx.bar_base = value ? 0xffffffffu : 0u;
+		if (b->graph) {  // no grid barrier there, but keep the captured context current
+			cudaGraphExecDestroy(b->graph);
+			b->graph = nullptr;
+		}
+		return XFEM_OK;
+	default: return fail(XFEM_EINVAL, "unknown test hook " + std::to_string(hook));
+	}
 }
 
 int xfem_synchronize(xfem_body* b) {

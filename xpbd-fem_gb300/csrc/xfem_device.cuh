@@ -14,7 +14,11 @@ namespace xfem {
 
 namespace {
 
-constexpr uint64_t kBarrierTimeoutNs = 2000000000ull;  // 2 s: far above any legal wait
+// Sets the grid-barrier arrival counter to ctx.bar_base (0 or 0xffffffff)
+// before a persistent launch.
+inline cudaError_t reset_barrier(const DevCtx& ctx, cudaStream_t st) {
+	return cudaMemsetAsync(ctx.bar_count, ctx.bar_base ? 0xff : 0, sizeof(uint32_t), st);
+}
 
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
 	uint32_t v;
@@ -29,19 +33,25 @@ __device__ __forceinline__ uint64_t global_ns() {
 }
 
 // Grid-wide barrier for the co-resident persistent grid. Monotonic arrival
-// counter (zeroed before each launch); every wait is bounded: on timeout the
-// block records kErrBarrierTimeout and all blocks leave at their next barrier.
+// counter, set to C.bar_base before each launch; every block's target starts
+// there too. The counter may wrap past 2^32 within a launch: arrival and
+// target are compared through their signed 32-bit difference, which stays
+// within +-gridDim.x (no block can be more than one barrier ahead of another).
+// Every wait is bounded by C.timeout_ns: on timeout the block records
+// kErrBarrierTimeout and all blocks leave at their next barrier.
+// C.wait_miss (a test hook, normally 0) adds arrivals that no block makes,
+// so the wait runs out on purpose.
 __device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
 	__shared__ int s_ok;
 	__syncthreads();
-	target += gridDim.x;
+	target += gridDim.x + C.wait_miss;
 	if (threadIdx.x == 0) {
 		int ok = 1;
 		__threadfence();
 		atomicAdd(C.bar_count, 1u);
 		uint32_t spins = 0;
 		uint64_t t0 = 0;
-		while (ld_acquire_gpu(C.bar_count) < target) {
+		while ((int32_t)(ld_acquire_gpu(C.bar_count) - target) < 0) {
 			if (++spins == 256) {
 				spins = 0;
 				if (*(volatile int*)C.err) {
@@ -51,7 +61,7 @@ __device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
 				const uint64_t t = global_ns();
 				if (t0 == 0) {
 					t0 = t;
-				} else if (t - t0 > kBarrierTimeoutNs) {
+				} else if (t - t0 > C.timeout_ns) {
 					atomicCAS(C.err, 0, kErrBarrierTimeout);
 					ok = 0;
 					break;
@@ -143,15 +153,21 @@ __device__ __forceinline__ void advance_vertex(const BodyParams* bodies, float4&
 	D = make_float4(V.x * dt, V.y * dt, V.z * dt, __uint_as_float(bits));
 }
 
-// Finalize the last substep of a launch: (O, D) -> canonical (X, V).
-__device__ __forceinline__ void finalize_vertex(const BodyParams* bodies, float4& O, float4& D, float inv_dt) {
+// Finalize the last substep of a launch: (O, D) -> canonical (X, V). A
+// position or velocity that is no longer finite (a diverged solve, or a NaN
+// the caller set) is recorded in the error word as kErrNonFinite, which the
+// next synchronising call reports.
+__device__ __forceinline__ void finalize_vertex(const DevCtx& C, float4& O, float4& D, float inv_dt) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = bodies[bits >> 8];
+	const BodyParams& bp = C.bodies[bits >> 8];
 	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt);
 	O.x += D.x;
 	O.y += D.y;
 	O.z += D.z;
 	D = make_float4(V.x, V.y, V.z, __uint_as_float(bits));
+	// inf - inf and NaN - NaN are NaN: one compare for all six values
+	const float z = (O.x - O.x) + (O.y - O.y) + (O.z - O.z) + (V.x - V.x) + (V.y - V.y) + (V.z - V.z);
+	if (z != 0.0f) atomicCAS(C.err, 0, kErrNonFinite);
 }
 
 // Rest state of one tet: Qi column-major q[c][r], QQ, QR and c0 = (1/mu)/vol.
@@ -553,11 +569,11 @@ __device__ bool mbar_wait(const DevCtx& C, uint64_t* m, uint32_t parity) {
 			const uint64_t t = global_ns();
 			if (t0 == 0) {
 				t0 = t;
-			} else if (t - t0 > kBarrierTimeoutNs) {
+			} else if (t - t0 > C.timeout_ns) {
 				atomicCAS(C.err, 0, kErrCopyTimeout);
 				for (uint32_t k = 0;; k++) {
 					if (mbar_test(m, parity)) break;
-					if ((k & 1023u) == 1023u && global_ns() - t > kBarrierTimeoutNs) break;
+					if ((k & 1023u) == 1023u && global_ns() - t > C.timeout_ns) break;
 				}
 				return false;
 			}

@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 	const uint32_t unit = E::kWarp ? gtid >> 5 : gtid, nunits = E::kWarp ? nthreads >> 5 : nthreads;
 	const uint32_t tick0 = __ldcg(C.tick);
 	const bool dmode = C.damp_kinds != 0u;
-	uint32_t target = 0;
+	uint32_t target = C.bar_base;
 	for (uint32_t s = 0; s < nsub; s++) {
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C.bodies, O, D, inv_dt);
+			finalize_vertex(C, O, D, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 		if (!grid_sync(C, target)) return;
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C.bodies, O, D, inv_dt);
+			finalize_vertex(C, O, D, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 	}
@@ -303,7 +303,7 @@ int launch_elements(const DevCtx& ctx, int block, uint32_t nsub, float dt, void*
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, 0);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
-	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+	e = reset_barrier(ctx, st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
 	void* args[] = {&c, &nsub, &dt};

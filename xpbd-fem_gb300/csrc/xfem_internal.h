@@ -253,6 +253,11 @@ struct DevCtx {
 	uint32_t vs_off;            // byte offset of the vertex slots in a warp's area
 	uint32_t* bar_count;        // grid barrier arrival counter
 	int* err;                   // device error word (0 = ok)
+	uint64_t timeout_ns;        // limit of every bounded device wait (barrier, copy, dependency)
+	uint32_t bar_base;          // the arrival counter's value at launch: 0, or 0xffffffff
+	                            // (a test of the counter's wrap: the first barrier wraps it)
+	uint32_t wait_miss;         // test hook, normally 0: arrivals (dependency steps) each
+	                            // bounded wait expects beyond those that come, so it runs out
 	// Adjoint tape, written only by the recording forward kernel (null otherwise).
 	// Substep indices are relative to the launch; `sub_base` is the launch's
 	// first substep in the whole run (checkpointed segments).
@@ -344,6 +349,10 @@ constexpr uint32_t kFlagContact = 2u;
 constexpr int kErrBarrierTimeout = 1;
 constexpr int kErrCopyTimeout = 2;
 constexpr int kErrDepTimeout = 3;
+constexpr int kErrNonFinite = 4;  // a finished position or velocity is NaN or infinite
+
+// Default limit of a bounded device wait: far above any legal wait.
+constexpr uint64_t kDefaultTimeoutNs = 2000000000ull;
 
 // ---- kernel launchers (xfem_kernels.cu) ---------------------------------------
 struct LaunchCfg {
@@ -370,8 +379,10 @@ size_t solve_smem_bytes(int block, uint32_t warp_smem);
 
 // Allocation-free stepping: the persistent kernel with its scratch words in a
 // fixed device array (xfem_kernels.cu). Synchronises `stream` and returns the
-// device error word in *device_error. cudaErrorInvalidValue when the call's
-// barrier arrivals (nsub x colours x blocks) would reach 2^31.
+// device error word in *device_error. kNoAllocTooLong when the call's
+// grid-barrier arrivals (substeps x passes per substep x blocks) would reach
+// 2^31; otherwise a cudaError_t value.
+constexpr int kNoAllocTooLong = -1;
 int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bool lambdas, uint32_t nsub, float dt,
                             void* stream, int device, int* device_error);
 

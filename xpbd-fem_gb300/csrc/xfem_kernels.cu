@@ -215,7 +215,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 		// or finished the vertex, and no other cluster of the pass touches it
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
-			if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O[s], D[s], inv_dt);
+			if (EXT && (last & (1u << s))) finalize_vertex(C, O[s], D[s], inv_dt);
 			st_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
 		}
 	}
@@ -288,7 +288,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
 				float4 O = sO[s * kLanes], D = sD[s * kLanes];
-				if (EXT && (last & (1u << s))) finalize_vertex(C.bodies, O, D, inv_dt);
+				if (EXT && (last & (1u << s))) finalize_vertex(C, O, D, inv_dt);
 				st_vertex(C.vert + 2 * (size_t)vid[s], O, D);
 			}
 		}
@@ -359,7 +359,7 @@ __device__ __noinline__ void vol_chunk(const DevCtx& C, Stage& st, uint32_t chun
 		for (uint32_t s = 0; s < NV; s++) {
 			if (s < nv) {
 				if (last & (1u << s)) {
-					finalize_vertex(C.bodies, O[s], D[s], inv_dt);
+					finalize_vertex(C, O[s], D[s], inv_dt);
 					__stcg(C.vert + 2 * (size_t)vid[s], O[s]);
 				}
 				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
@@ -484,7 +484,7 @@ __device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, ui
 			advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
 			if (TAPE) tape_vertex(C, v, O, Dbefore, s, s == 0);
 		}
-		if (finalize_end) finalize_vertex(C.bodies, O, D, inv_dt);
+		if (finalize_end) finalize_vertex(C, O, D, inv_dt);
 		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 }
@@ -496,7 +496,7 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 		float4 O, D;
 		ld_vertex(C.vert + 2 * (size_t)v, O, D);
 		if (TAPE) __stcs(C.tape_fin + v, D);
-		finalize_vertex(C.bodies, O, D, inv_dt);
+		finalize_vertex(C, O, D, inv_dt);
 		if (TAPE) {
 			const int q = __ldg(C.tip_of + v);
 			if (q >= 0) C.traj[(size_t)(C.sub_base + nsub - 1) * C.ntips + q] = O;
@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	const uint32_t tick0 = __ldcg(C.tick);  // read before the first barrier; block 0 advances it at the end
 	Stage st = stage_init(C, lane);
 	run_isolated<TAPE>(C, gtid, nthreads, nsub, dt, inv_dt, dmode);
-	uint32_t target = 0;
+	uint32_t target = C.bar_base;
 	bool ok = true;
 	for (uint32_t s = 0; s < nsub && ok; s++) {
 		for (uint32_t q = 0; q < P && ok; q++) {
@@ -615,7 +615,7 @@ __device__ bool wait_deps(const DevCtx& C, uint32_t ch, uint32_t s, uint32_t lan
 	bool ok = true;
 	for (uint32_t i = b + lane; i < e && ok; i += kLanes) {
 		const uint32_t d = __ldg(C.deps + i);
-		const uint32_t need = s + (d >> 31);
+		const uint32_t need = s + (d >> 31) + C.wait_miss;
 		if (need == 0) continue;
 		const uint32_t* f = C.done + (d & 0x7fffffffu);
 		uint32_t spins = 0;
@@ -630,7 +630,7 @@ __device__ bool wait_deps(const DevCtx& C, uint32_t ch, uint32_t s, uint32_t lan
 				const uint64_t t = global_ns();
 				if (t0 == 0) {
 					t0 = t;
-				} else if (t - t0 > kBarrierTimeoutNs) {
+				} else if (t - t0 > C.timeout_ns) {
 					atomicCAS(C.err, 0, kErrDepTimeout);
 					ok = false;
 					break;
@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 		mbar_wait(C, st.mbar, st.parity);  // leave no copy in flight
 		st.inflight = -1;
 	}
-	uint32_t target = 0;
+	uint32_t target = C.bar_base;
 	if (!grid_sync(C, target) || !ok) return;
 	run_finalize(C, gtid, nthreads, inv_dt);
 	if (gtid == 0) *C.tick = tick0 + nsub;
@@ -809,24 +809,35 @@ __global__ void k_volume(const float4* __restrict__ vert, const uint32_t* __rest
 
 size_t solve_smem_bytes(int block, uint32_t warp_smem) { return (size_t)(block / 32) * warp_smem; }
 
-// The dynamic shared-memory limit is a property of the kernel, shared by
-// every handle in the process: it only ever grows to the largest size any
+// The dynamic shared-memory limit is a property of the kernel on one device
+// (cudaFuncSetAttribute acts in the current device's context), shared by
+// every handle on that device: it only ever grows to the largest size any
 // handle launches with (a larger limit does not restrict smaller launches),
 // so one handle's configuration cannot lower another's below what it needs.
-static void set_smem_attr(const void* f, size_t bytes) {
+// Kept per (device, kernel); a failed raise is returned and not recorded.
+static cudaError_t set_smem_attr(const void* f, size_t bytes) {
+	struct Entry {
+		int dev;
+		const void* f;
+		size_t bytes;
+	};
 	static std::mutex mu;
-	static std::vector<std::pair<const void*, size_t>> done;
+	static std::vector<Entry> done;
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
 	std::lock_guard<std::mutex> lk(mu);
 	for (auto& d : done)
-		if (d.first == f) {
-			if (bytes > d.second) {
-				cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-				d.second = bytes;
+		if (d.dev == dev && d.f == f) {
+			if (bytes > d.bytes) {
+				e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+				if (e == cudaSuccess) d.bytes = bytes;
 			}
-			return;
+			return e;
 		}
-	cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-	done.emplace_back(f, bytes);
+	e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+	if (e == cudaSuccess) done.push_back({dev, f, bytes});
+	return e;
 }
 
 static const void* persistent_fn(bool lambdas, bool ext) {
@@ -841,12 +852,14 @@ static const void* colour_fn(bool lambdas, bool ext) {
 
 int configure_kernels(const LaunchCfg& cfg) {
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
+	cudaError_t e = cudaSuccess;
 	for (bool ext : {false, true}) {
-		set_smem_attr(persistent_fn(cfg.lambdas, ext), smem);
-		set_smem_attr(colour_fn(cfg.lambdas, ext), smem);
+		if (e == cudaSuccess) e = set_smem_attr(persistent_fn(cfg.lambdas, ext), smem);
+		if (e == cudaSuccess) e = set_smem_attr(colour_fn(cfg.lambdas, ext), smem);
 	}
-	set_smem_attr(cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>, smem);
-	return (int)cudaGetLastError();
+	if (e == cudaSuccess)
+		e = set_smem_attr(cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>, smem);
+	return (int)e;
 }
 
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
@@ -869,7 +882,7 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 	cudaError_t e = cudaSuccess;
 	if (nsub == 0) return 0;
 	if (cfg.sync_mode == 1 || cfg.sync_mode == 3) {
-		e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+		e = reset_barrier(ctx, st);
 		if (e == cudaSuccess && cfg.sync_mode == 3) e = cudaMemsetAsync(ctx.done, 0, sizeof(uint32_t) * ctx.nchunks, st);
 		if (e != cudaSuccess) return (int)e;
 		DevCtx c = ctx;
@@ -923,14 +936,14 @@ int launch_substeps_tape(const DevCtx& ctx, int block, uint32_t warp_smem, uint3
 	cudaStream_t st = (cudaStream_t)stream;
 	const void* f = (const void*)k_persistent<false, true>;
 	const size_t smem = solve_smem_bytes(block, warp_smem);
-	cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	cudaError_t e = set_smem_attr(f, smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	if (e == cudaSuccess) e = cudaGetDevice(&dev);
 	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, smem);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
-	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+	e = reset_barrier(ctx, st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
 	void* args[] = {&c, &nsub, &dt};
@@ -979,9 +992,8 @@ int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, dou
 // ---- allocation-free stepping ---------------------------------------------------
 // Some callers cannot allocate device memory at the moment they step: a
 // process whose device memory is fully reserved by another allocator (a
-// framework's caching pool), a real-time loop that must not take cudaMalloc's
-// implicit device-wide synchronisation, or code running while a stream is
-// being captured, where cudaMalloc is not permitted. For them the persistent
+// framework's caching pool), or a real-time loop that must not take
+// cudaMalloc's implicit device-wide synchronisation. For them the persistent
 // substep kernel is launched with its scratch words (the grid-barrier arrival
 // counter and the device error word) taken from this fixed array instead of
 // buffers of the handle, and without the autotuner or CUDA-graph builder,
@@ -989,7 +1001,7 @@ int launch_volume(const float4* vert, const uint32_t* tets_dev, uint32_t nt, dou
 //
 // The array lives in every device that loads the library until the process
 // exits. All calls share it and it keeps the last call's contents, so each
-// call zeroes the words it uses first; calls whose kernels overlap on one GPU
+// call sets the words it uses first; calls whose kernels overlap on one GPU
 // would race on it and must not be issued.
 namespace {
 constexpr uint32_t kNoAllocScratchWords = 64;  // 256 bytes; words 0 and 1 are used
@@ -1018,16 +1030,20 @@ int launch_substeps_noalloc(const DevCtx& ctx, int block, uint32_t warp_smem, bo
 	cudaStream_t st = (cudaStream_t)stream;
 	const void* f = persistent_fn(lambdas, ctx.ext != 0u);
 	const size_t smem = solve_smem_bytes(block, warp_smem);
-	set_smem_attr(f, smem);  // no allocation: the kernel's shared-memory limit
+	cudaError_t e = set_smem_attr(f, smem);  // no allocation: the kernel's shared-memory limit on this device
 	int sms = 0, per_sm = 0;
-	cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, smem);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
 	const uint32_t blocks = (uint32_t)(per_sm * sms);
-	// the 32-bit arrival counter must not wrap within one call
-	if ((uint64_t)nsub * ctx.ncolours * blocks >= (1ull << 31)) return (int)cudaErrorInvalidValue;
-	e = cudaMemsetAsync(p, 0, 2 * sizeof(uint32_t), st);
+	// One call's grid-barrier arrivals stay below 2^31: every block arrives
+	// once per pass, and a substep runs (1 + volume sweeps + damping kinds) x
+	// colours passes in the extended kernel, one per colour otherwise.
+	const uint64_t kinds = ctx.ext ? 1ull + ctx.nvol + (uint64_t)__builtin_popcount(ctx.damp_kinds) : 1ull;
+	if ((uint64_t)nsub * kinds * ctx.ncolours * blocks >= (1ull << 31)) return kNoAllocTooLong;
+	e = cudaMemsetAsync(p, ctx.bar_base ? 0xff : 0, sizeof(uint32_t), st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(p + 1, 0, sizeof(uint32_t), st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
 	c.bar_count = p;

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(256) k_rings(DevCtx C, uint32_t nsub, float dt
 	RingScratch& S = reinterpret_cast<RingScratch*>(smem)[wib];
 	const uint32_t tick0 = __ldcg(C.tick);
 	const bool dmode = DAMP && C.damp_kinds != 0u;
-	uint32_t target = 0;
+	uint32_t target = C.bar_base;
 	for (uint32_t s = 0; s < nsub; s++) {
 		// finish the previous substep (unless the damping passes left the
 		// canonical state) and predict this one, every vertex
@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(256) k_rings(DevCtx C, uint32_t nsub, float dt
 			for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 				float4 O, D;
 				ld_vertex(C.vert + 2 * (size_t)v, O, D);
-				finalize_vertex(C.bodies, O, D, inv_dt);
+				finalize_vertex(C, O, D, inv_dt);
 				st_vertex(C.vert + 2 * (size_t)v, O, D);
 			}
 			if (!grid_sync(C, target)) return;
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256) k_rings(DevCtx C, uint32_t nsub, float dt
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C.bodies, O, D, inv_dt);
+			finalize_vertex(C, O, D, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 	}
@@ -356,7 +356,7 @@ int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* st
 	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, block, smem);
 	if (e != cudaSuccess) return (int)e;
 	if (per_sm <= 0) return (int)cudaErrorInvalidConfiguration;
-	e = cudaMemsetAsync(ctx.bar_count, 0, sizeof(uint32_t), st);
+	e = reset_barrier(ctx, st);
 	if (e != cudaSuccess) return (int)e;
 	DevCtx c = ctx;
 	void* args[] = {&c, &nsub, &dt};

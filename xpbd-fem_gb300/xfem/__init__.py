@@ -20,7 +20,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libxfem.so")
 
-OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT = 0, -1, -2, -3, -4, -5, -6
+OK, EINVAL, EUNSUPPORTED, ENOMEM, ECUDA, EDEVICE_TIMEOUT, ELIMIT, ENONFINITE = 0, -1, -2, -3, -4, -5, -6, -7
+# failure-detection test hooks (xfem_test_hook)
+HOOK_MISSING_ARRIVAL, HOOK_BARRIER_BASE, HOOK_FAIL_ALLOC = 1, 2, 3
 ELEMENT_TYPE_MASK = 15  # flags bits 0-3 (Settings_ElementTypeMask)
 ELEMENT_T4, ELEMENT_T10, ELEMENT_H8, ELEMENT_H27 = 5, 6, 7, 8
 ENERGY_BIT = 6
@@ -68,7 +70,7 @@ class Options(C.Structure):
     _fields_ = [
         ("cluster_mode", C.c_uint32), ("no_morton", C.c_uint32), ("sync_mode", C.c_uint32),
         ("block_size", C.c_uint32), ("keep_lambdas", C.c_uint32), ("device", C.c_int32),
-        ("stream", C.c_void_p), ("host_setup", C.c_uint32),
+        ("stream", C.c_void_p), ("host_setup", C.c_uint32), ("wait_timeout_ms", C.c_uint32),
     ]
 
 
@@ -98,6 +100,7 @@ EXPORTS = [
     "xfem_body_t10_count", "xfem_get_t10_rest_state", "xfem_get_t10_schedule", "xfem_compute_t10_edges",
     "xfem_compute_t10_rest_state", "xfem_compute_t10_schedule", "xfem_body_h27_count", "xfem_get_h27_rest_state",
     "xfem_get_h27_schedule", "xfem_compute_h27_mesh", "xfem_compute_h27_rest_state", "xfem_compute_h27_schedule",
+    "xfem_test_hook",
 ]
 HEX_EP = 120  # floats per hex rest-state record (ElementParamsLinearHex flattened)
 T10_EP = 56  # floats per T10 rest-state record (ElementParamsQuadraticTet flattened)
@@ -136,6 +139,7 @@ def lib():
         L.xfem_step_frames.argtypes = [P, u32, u32, f32]
         L.xfem_synchronize.argtypes = [P]
         L.xfem_step_frames_noalloc.argtypes = [P, u32, u32, f32]
+        L.xfem_test_hook.argtypes = [P, u32, u32]
         for n in ("xfem_get_positions", "xfem_set_positions", "xfem_get_velocities", "xfem_set_velocities",
                   "xfem_get_inverse_masses", "xfem_get_contacts", "xfem_get_lambdas", "xfem_calculate_volume"):
             getattr(L, n).argtypes = [P, u32, P]
@@ -383,12 +387,19 @@ def compute_ring_schedule(node_data, idx_data, morton=True):
 
 
 def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None,
-             host_setup=False):
+             host_setup=False, wait_timeout_ms=0):
     o = Options()
     o.cluster_mode, o.no_morton, o.sync_mode = cluster_mode, 0 if morton else 1, sync_mode
     o.block_size, o.keep_lambdas, o.device, o.stream = block_size, 1 if keep_lambdas else 0, device, stream
     o.host_setup = 1 if host_setup else 0
+    o.wait_timeout_ms = wait_timeout_ms
     return o
+
+
+def test_hook(body, hook, value):
+    """xfem_test_hook: make a detected failure happen on purpose (HOOK_*);
+    body is a Body, or None for the process-wide HOOK_FAIL_ALLOC."""
+    _check(lib().xfem_test_hook(body._h if body is not None else None, hook, value))
 
 
 class Body:
