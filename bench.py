@@ -32,10 +32,14 @@ shape the configuration names.
   its MixedSel element bandwidth against the measured HBM peak),
   "adjoint": cost of the reverse-mode gradient (recording forward + backward)
   against the plain forward, on the 32x8x8 beam (200 substeps, 20 tips,
-  checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame).
+  checkpoints every 20 substeps) and on the 1.5M-tet mesh (one frame),
+  "drop": the drop configuration (64x16x16 cubes of Yeoh C10/C20/C30 =
+  3e4/1e3/1e2 Pa dropped from 0.5 m onto a frictional ground), all 300 frames
+  of 30 substeps, with its CPU baseline; and "summary", the side legs'
+  headline figures in one compact object at the end of the line.
 --impl reference: the reference's CPU algorithm (the oracle port, run in the
-  GPU's colour order with all host threads) on the same mesh; each step is a
-  bounded sample of substeps.
+  GPU's colour order with all host threads) on the same mesh; each step is
+  one frame (20 substeps), as in the GPU arm.
 
 Multi-GPU (torchrun): replicas only — every rank steps its own copy of the
 mesh, no collective on the data path; value sums the ranks.
@@ -197,7 +201,7 @@ def run_reference(args, world, rank):
     X = w["nodes"].reshape(-1, 3).astype(np.float64)
     V = np.zeros_like(X)
     threads = os.cpu_count() or 1
-    per_step = 1
+    per_step = w["substeps"]  # one step = one frame, as in the GPU arm
     nt = tets.shape[0]
 
     def step(X, V, wi):
@@ -217,10 +221,10 @@ def run_reference(args, world, rank):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
             "impl": "reference",
             "config": {"workload": w["name"], "tets": nt, "vertices": int(X.shape[0]),
-                       "substeps_per_step": per_step, "order": "colour order (same schedule as the GPU)",
+                       "substeps_per_step": per_step, "dt": w["dt"], "order": "colour order (same schedule as the GPU)",
                        "l2": "n/a (CPU)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{per_step} substep(s) of the full mesh per step, {threads} threads"},
+                             "sample": f"one frame ({per_step} substeps) of the full mesh per step, {threads} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -306,6 +310,7 @@ def run_xfem(args, world, rank, local):
     hexes = None if args.no_hexes else run_hexes(stream, cpu=not args.no_cpu)
     t10 = None if args.no_t10 else run_t10(stream, cpu=not args.no_cpu)
     h27 = None if args.no_h27 else run_h27(stream, cpu=not args.no_cpu)
+    drop = None if args.no_drop else run_drop(stream, cpu=not args.no_cpu)
     for kind, rec in (("hexes", hexes), ("t10", t10), ("h27", h27)):
         if rec is not None:
             rec["roofline"] = element_roofline(kind, rec)
@@ -334,9 +339,96 @@ def run_xfem(args, world, rank, local):
         "hexes": hexes,
         "t10": t10,
         "h27": h27,
+        "drop": drop,
         "clocks": clk.summary(),
     }
+    line["summary"] = summary(line)
     print(json.dumps(line), flush=True)
+
+
+def summary(line):
+    """The side legs' headline figures in one compact object, printed last
+    on the line so that a reader keeping only the end of the output has them."""
+    def g(*keys):
+        v = line
+        for k in keys:
+            if not isinstance(v, dict) or v.get(k) is None:
+                return None
+            v = v[k]
+        return round(v, 4) if isinstance(v, float) else v
+    return {"value": g("value"), "frac": g("roofline", "frac"), "e2e": g("e2e", "value"),
+            "batched_speedup": g("batched", "speedup"), "batched_value": g("batched", "value"),
+            "adjoint_beam_cost": g("adjoint", "beam", "record_plus_backward_over_forward"),
+            "adjoint_large_cost": g("adjoint", "large", "record_plus_backward_over_forward"),
+            "damped_cost": g("damped", "cost"), "hexes_frac": g("hexes", "roofline", "frac"),
+            "t10_frac": g("t10", "roofline", "frac"), "h27_frac": g("h27", "roofline", "frac"),
+            "drop_value": g("drop", "value"), "drop_ms_per_frame": g("drop", "ms_per_frame"),
+            "drop_frac": g("drop", "roofline", "frac"), "setup_s": g("setup", "throughput")}
+
+
+def run_drop(stream, cpu=True, cpu_budget_s=6.0):
+    """The drop configuration: 64x16x16 cubes (98,304 tets) of Yeoh with C10 =
+    3e4, C20 = 1e3, C30 = 1e2 Pa, incompressible, dropped from 0.5 m with a
+    seeded random rotation onto a frictional ground (mu = 0.4), 30 substeps
+    per frame of 1/60 s: all 300 frames device-timed one event pair per frame
+    (the L2 flushed between frames, outside the pairs), the body landing and
+    bouncing on the way; its element bandwidth against the measured HBM peak;
+    and the oracle port of the reference, one thread in the reference's
+    shuffled order, on a bounded sample of substeps of the same mesh."""
+    import torch
+
+    import oracle
+    import xfem
+    from xfem import workloads as W
+    w = W.drop_yeoh()
+    nt, nv = w["idx"].size // 5, w["nodes"].size // 3
+    S, frames = w["substeps"], w["frames"]
+    sdt = w["dt"] / S
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=stream.device)
+    body = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], stream=C_void_p(stream.cuda_stream))
+    x0, v0 = body.positions(), body.velocities()
+    for _ in range(3):
+        body.step_frames(1, S, sdt)
+    body.set_positions(x0)
+    body.set_velocities(v0)
+    body.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    for k in range(frames):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            ev[k][0].record(stream)
+        body.step_frames(1, S, sdt)
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+    body.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    x = body.positions()
+    info = body.info()
+    body.close()
+    per_frame = sum(ms) / frames
+    hbm, peak_kind = peaks()
+    bpu = REC_BYTES + VERT_BYTES * nv / nt
+    achieved = bpu * nt * S / (per_frame / 1e3) / 1e9
+    out = {"workload": w["name"], "frames": frames, "substeps_per_frame": S, "ms_per_frame": per_frame,
+           "value": nt * S / (per_frame / 1e3), "unit": UNIT,
+           "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+           "block": info["block_size"], "final_min_z": float(x[:, 2].min()),
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                        "peak_kind": peak_kind, "bytes_per_tet_substep": bpu}}
+    if cpu:
+        tets, _ = oracle.parse_tets(w["idx"])
+        ep, wi, _ = oracle.init_rest(w["nodes"], tets, w["density"])
+        order = oracle.minstd_order(tets.shape[0])
+        p = oracle.params_from_settings(w["settings"], sdt)
+        X = w["nodes"].reshape(-1, 3).astype(np.float64)
+        V = np.zeros_like(X)
+        n, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < cpu_budget_s or n == 0:
+            X, V, wi, _ = oracle.substeps(X, V, wi, tets, ep, order, 1, p)
+            n += 1
+        out["cpu_baseline"] = {"value": nt * n / (time.perf_counter() - t0), "unit": UNIT, "cores": 1, "kind": "port",
+                               "sample": f"{n} substeps of the same mesh, reference shuffled order, 1 thread"}
+    return out
 
 
 def run_batched(stream, frames=5, plain_frames=2):
@@ -755,6 +847,7 @@ def main():
     ap.add_argument("--no-hexes", action="store_true")
     ap.add_argument("--no-t10", action="store_true")
     ap.add_argument("--no-h27", action="store_true")
+    ap.add_argument("--no-drop", action="store_true")
     ap.add_argument("--adjoint-only", choices=["beam", "large", "both"], default=None,
                     help="time only the adjoint (no main metric line)")
     ap.add_argument("--adjoint-substeps", type=int, default=None, help="substeps of the large adjoint case")

@@ -141,22 +141,24 @@ def cantilever_small():
                 settings=s, lock=lock_mask_axis(nodes, 0), dt=1.0 / 60.0, substeps=20, frames=100)
 
 
-def drop_yeoh(seed=2):
+def drop_yeoh(seed=2, W=64, H=16, D=16, height=0.5, nu=0.5):
     """64x16x16 cubes of 0.02 m (98,304 tets), Yeoh C10 = 3e4, C20 = 1e3,
     C30 = 1e2 Pa, incompressible, dropped from 0.5 m with a random rotation
-    onto z = 0 with Coulomb friction 0.4; dt = 1/60, 30 substeps, 300 frames."""
+    onto z = 0 with Coulomb friction 0.4; dt = 1/60, 30 substeps, 300 frames.
+    W, H, D, height and nu give scaled copies (same cube edge, coefficients,
+    rotation draw and ground) for tests whose oracle must finish in seconds."""
     rng = Rng(seed)
-    nodes, idx = box(64, 16, 16, 0.02)
+    nodes, idx = box(W, H, D, 0.02)
     n = nodes.reshape(-1, 3).astype(np.float64)
     n = (n - n.mean(0)) @ random_rotation(rng).T
-    n[:, 2] += 0.5 - n[:, 2].min()
+    n[:, 2] += height - n[:, 2].min()
     nodes = n.astype(np.float32).reshape(-1)
     C10, C20, C30 = 3e4, 1e3, 1e2
-    s = default_settings(gravity=(0.0, 0.0, -9.81), compliance=1.0 / C10, poissons_ratio=0.5,
+    s = default_settings(gravity=(0.0, 0.0, -9.81), compliance=1.0 / C10, poissons_ratio=nu,
                          flags=YEOH_FLAGS & ~LOCK_LEFT, yeoh=(1.0, C20 / C10, C30 / C10), ground=1,
                          ground_normal=(0.0, 0.0, 1.0), ground_offset=0.0, friction=0.4)
-    return dict(name="drop 64x16x16 (98,304 tets) Yeoh", nodes=nodes, idx=idx, density=1000.0, settings=s,
-                lock=None, dt=1.0 / 60.0, substeps=30, frames=300)
+    return dict(name=f"drop {W}x{H}x{D} ({6 * W * H * D} tets) Yeoh", nodes=nodes, idx=idx, density=1000.0,
+                settings=s, lock=None, dt=1.0 / 60.0, substeps=30, frames=300)
 
 
 def throughput(seed=3, W=128, H=64, D=32):
@@ -188,11 +190,12 @@ def throughput_hex(seed=3, W=128, H=64, D=32):
                 density=1000.0, settings=s, lock=lock_mask_axis(nodes, 2), dt=1.0 / 60.0, substeps=20, frames=50)
 
 
-def batched(seed=4, nbodies=512, lo=2, hi=24):
+def batched(seed=4, nbodies=512, lo=2, hi=24, height=0.5, nu=0.5):
     """nbodies boxes of a x b x c cubes, a, b, c ~ U{lo..hi}, coin-flip
     Neo-Hookean / Yeoh, E ~ LogUniform(1e4, 1e6) Pa, each dropped from 0.5 m
     with a random rotation onto its own ground (z = 0, friction 0.4),
-    20 substeps per frame of 1/60 s."""
+    20 substeps per frame of 1/60 s. height and nu give variants for tests
+    (bodies that reach the ground within a frame; a compressible material)."""
     rng = Rng(seed)
     dims = rng.integers(lo, hi, 3 * nbodies).reshape(nbodies, 3)
     coins = rng.uniform(nbodies)
@@ -204,16 +207,16 @@ def batched(seed=4, nbodies=512, lo=2, hi=24):
         nodes, idx = box(a_, b_, c_, edge)
         n = nodes.reshape(-1, 3).astype(np.float64)
         n = (n - n.mean(0)) @ random_rotation(rng).T
-        n[:, 2] += 0.5 - n[:, 2].min()
+        n[:, 2] += height - n[:, 2].min()
         nodes = n.astype(np.float32).reshape(-1)
         E = float(np.exp(logE[b]))
         if coins[b] < 0.5:
-            s = default_settings(gravity=(0, 0, -9.81), compliance=nh_compliance(E), poissons_ratio=0.5,
+            s = default_settings(gravity=(0, 0, -9.81), compliance=nh_compliance(E, nu), poissons_ratio=nu,
                                  flags=NH_FLAGS & ~LOCK_LEFT, ground=1, ground_normal=(0, 0, 1), friction=0.4)
         else:
             # Yeoh: C10 = E / 6 (the Neo-Hookean limit) and the reference's own
             # coefficient ratios (XPBDFEM/Fem.cpp:526) for C20 / C10, C30 / C10
-            s = default_settings(gravity=(0, 0, -9.81), compliance=nh_compliance(E), poissons_ratio=0.5,
+            s = default_settings(gravity=(0, 0, -9.81), compliance=nh_compliance(E, nu), poissons_ratio=nu,
                                  flags=YEOH_FLAGS & ~LOCK_LEFT, ground=1, ground_normal=(0, 0, 1), friction=0.4,
                                  yeoh=(1.0, 14.95 / 0.1095, 4.595 / 0.1095))
         meshes.append((nodes, idx, 1000.0))
