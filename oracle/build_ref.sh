@@ -7,10 +7,12 @@
 # prelude (oracle/prelude.h) that supplies the <cmath> float overloads MSVC and
 # the wasm libc shim put in the global namespace. -ffp-contract=off keeps the
 # float arithmetic unfused so results are the same on x86-64 and AArch64.
-# Skipped (exit 0 with a note) where the reference tree is absent.
+# The reference tree is XFEM_REFERENCE_DIR, by default a directory named
+# "reference" beside this repository's root. Skipped (exit 0 with a note)
+# where the reference tree is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${XFEM_REFERENCE_DIR:-/root/reference}/XPBDFEM"
+REF="${XFEM_REFERENCE_DIR:-$HERE/../../reference}/XPBDFEM"
 OUT="$HERE/_ref"
 if [ ! -f "$REF/Fem.cpp" ]; then
   echo "build_ref: reference sources not found at $REF; skipping"

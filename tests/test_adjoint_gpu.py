@@ -277,38 +277,58 @@ def test_beam_vjp(beam):
 
 
 def test_beam_fd(beam):
-    """GPU dL/dlog(mu) of the three most sensitive tets against FP64 central
-    differences of the FP64 loss (h = 1e-3 in log mu)."""
+    """GPU dL/dlog(mu) of the ten most sensitive tets and dL/dV0 of the three
+    largest initial-velocity entries against FP64 central differences of the
+    FP64 loss (h = 1e-3 in log mu, 1e-5 m/s in V0), each within 1e-3 of the
+    largest |FD| of its kind among the checked entries (1e-3 relative, on
+    the scale of the gradient)."""
     c = beam
     r = c.gpu()
     X0 = np.asarray(c.nodes, np.float64).reshape(-1, 3)
     mu64 = c.mu.astype(np.float64)
 
-    def loss(m):
-        return oracle.adjoint(X0, c.V0, c.w, c.tets, c.ep, m, c.order, c.nsub, c.p, c.tips, c.targets, c.lock,
-                              grad=False)
+    def loss(m, V0=None):
+        return oracle.adjoint(X0, c.V0 if V0 is None else V0, c.w, c.tets, c.ep, m, c.order, c.nsub, c.p, c.tips,
+                              c.targets, c.lock, grad=False)
 
     h = 1e-3
-    for t in np.argsort(-np.abs(c.dmu * mu64))[:3]:
+    pairs = []
+    for t in np.argsort(-np.abs(c.dmu * mu64))[:10]:
         mp, mm = mu64.copy(), mu64.copy()
         mp[t] *= np.exp(h)
         mm[t] *= np.exp(-h)
-        fd = (loss(mp) - loss(mm)) / (2 * h)
-        ad = float(r.dmu[t]) * mu64[t]
-        assert abs(ad - fd) <= ADJ_TOL * abs(fd), (t, fd, ad)
+        pairs.append((t, (loss(mp) - loss(mm)) / (2 * h), float(r.dmu[t]) * mu64[t]))
+    scale = max(abs(fd) for _, fd, _ in pairs)
+    for t, fd, ad in pairs:
+        assert abs(ad - fd) <= ADJ_TOL * scale, ("dlogmu", t, fd, ad, scale)
+    hv = 1e-5
+    dv = np.asarray(r.dv).reshape(-1)
+    vpairs = []
+    for k in np.argsort(-np.abs(np.asarray(c.dv).reshape(-1)))[:3]:
+        vp, vm = c.V0.copy().reshape(-1), c.V0.copy().reshape(-1)
+        vp[k] += hv
+        vm[k] -= hv
+        fd = (loss(mu64, vp.reshape(-1, 3)) - loss(mu64, vm.reshape(-1, 3))) / (2 * hv)
+        vpairs.append((k, fd, float(dv[k])))
+    vscale = max(abs(fd) for _, fd, _ in vpairs)
+    for k, fd, ad in vpairs:
+        assert abs(ad - fd) <= ADJ_TOL * vscale, ("dV0", k, fd, ad, vscale)
 
 
 def test_beam_end_to_end(beam):
     """The gradient of the tip loss with G from the GPU's own float32
     trajectory. The loss compares two nearby trajectories (tip residuals of
-    ~3e-5 m against positions of ~1 m), so the float forward's rounding
-    enters G directly; the bound is on the gradient as a whole."""
+    ~3e-5 m against positions of ~1 m), so the float forward's rounding of
+    the positions (about 6e-8 m per substep at 1 m) enters G directly, at
+    ~1e-3 of it: measured 1.75e-3 of max |g| on a GB300, against the 1e-3
+    that the same reverse pass meets with the FP64 cotangent
+    (test_beam_vjp). Bound: 2.5e-3 of max |g| and cosine >= 0.999."""
     c = beam
     r0 = c.gpu()
     G = (2.0 * (r0.traj.astype(np.float64) - c.targets)).astype(np.float32)
     r = c.gpu(G=G)
     e = rel(r.dmu, c.dmu)
     print(f"end-to-end dL/dmu error vs FP64: {e:.3e}")
-    assert e <= 2e-2, e
+    assert e <= 2.5e-3, e
     cos = float(np.dot(r.dmu, c.dmu) / (np.linalg.norm(r.dmu) * np.linalg.norm(c.dmu)))
     assert cos >= 0.999, cos
