@@ -97,6 +97,8 @@ extern "C" {
 #define XFEM_RAYLEIGH_POST 2u          /*   element damping after the velocity update (Rayleigh_Post) */
 #define XFEM_RAYLEIGH_POST_AMORTIZED 3u /*  the same on one eighth of the order per substep, x 8 */
 #define XFEM_LOCK_LEFT (1u << 26)      /* Settings_LockLeft: apply the lock mask */
+#define XFEM_LOCK_RIGHT (1u << 27)     /* Settings_LockRight: hold the Right vertices (x above 98% of
+                                          the body's extent) at origin + locked_right_transform X0 */
 
 /* Solver settings. The first block mirrors the reference's Settings field by
  * field (XPBDFEM/Settings.h:79-91) with gravity widened to 3-D; fields this
@@ -134,6 +136,15 @@ typedef struct xfem_settings {
 	 * eighth of the order damped by Rayleigh_PostAmortized. The handle counts it
 	 * up by one per substep; xfem_set_settings sets it. */
 	uint32_t tick_id;
+	/* Settings::lockedRightTransform3d (XPBDFEM/Settings.h:100), column-major
+	 * like the reference's mat3, and Geo3d::origin (XPBDFEM/Geo.h:69): with
+	 * XFEM_LOCK_RIGHT every substep ends with the Right vertices at origin +
+	 * transform X0 (X0 the rest position) and a zero inverse mass
+	 * (XPBDFEM/Geo.cpp:323-331). The reference's demo animates the transform
+	 * per substep (XPBDFEM/Demo.cpp:69-80); here it holds for a stepping call,
+	 * so animate it with xfem_set_settings between xfem_substep calls. */
+	float locked_right_transform[9];
+	float origin[3];
 } xfem_settings;
 
 /* Create-time options (all zero = defaults). */

@@ -43,14 +43,18 @@ class Params(C.Structure):
         ("ground", C.c_uint32), ("ground_n", C.c_float * 3), ("ground_d", C.c_float),
         ("friction", C.c_float), ("damping", C.c_float), ("rayleigh_type", C.c_uint32),
         ("pbd_damping", C.c_float), ("pbd_coeff", C.c_float), ("pbd_coeff_amortized", C.c_float),
-        ("tick", C.c_uint32), ("volume_passes", C.c_uint32),
+        ("tick", C.c_uint32), ("volume_passes", C.c_uint32), ("lock_right", C.c_uint32),
+        ("right_target", C.c_void_p),
     ]
 
 
 def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=True,
                 gravity=(0.0, 0.0, 0.0), drag=0.0, yeoh=REF_YEOH, lock=False,
                 ground=False, ground_n=(0.0, 0.0, 1.0), ground_d=0.0, friction=0.0, damping=0.0, rayleigh_type=2,
-                pbd_damping=0.0, pbd_coeff=0.0, pbd_coeff_amortized=0.0, tick=0, volume_passes=0):
+                pbd_damping=0.0, pbd_coeff=0.0, pbd_coeff_amortized=0.0, tick=0, volume_passes=0,
+                right_target=None):
+    """right_target: the Right lock's targets (right_targets()); given, the
+    Right vertices (lock mask bit 1) are held there (Settings_LockRight)."""
     p = Params()
     p.gravity[:] = [float(g) for g in gravity]
     p.dt = dt
@@ -72,13 +76,29 @@ def make_params(dt, compliance, poisson, energy=ENERGY_MIXED_SEL, simultaneous=T
     p.pbd_coeff_amortized = pbd_coeff_amortized
     p.tick = tick
     p.volume_passes = volume_passes
+    if right_target is not None:
+        p._right_target = np.ascontiguousarray(right_target, np.float64).reshape(-1)  # kept alive with p
+        p.lock_right = 1
+        p.right_target = p._right_target.ctypes.data
     return p
 
 
-def params_from_settings(s, dt, lock=True, tick=None):
+def right_targets(nodes, transform, origin):
+    """origin + transform * vec3(X0) per vertex (XPBDFEM/Geo.cpp:327), float
+    arithmetic as the reference; transform column-major (9 floats)."""
+    nd = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    m = np.ascontiguousarray(transform, np.float32)
+    o = np.ascontiguousarray(origin, np.float32)
+    out = np.zeros(nd.size, np.float64)
+    lib().orc_right_targets(nd.size // 3, _p(nd), _p(m), _p(o), _p(out))
+    return out.reshape(-1, 3)
+
+
+def params_from_settings(s, dt, lock=True, tick=None, nodes=None):
     """orc_params from solver settings given as an xfem Settings struct or as
     a dict of its fields (reference semantics). tick: the tickId of the first
-    substep (default: the settings' tick_id)."""
+    substep (default: the settings' tick_id). nodes: the rest positions, for
+    the Right lock's targets when the settings lock the Right side."""
     def g(k, default=None):
         if isinstance(s, dict):
             return s.get(k, default) if default is not None else s[k]
@@ -94,7 +114,9 @@ def params_from_settings(s, dt, lock=True, tick=None):
                        pbd_coeff=g("volume_and_time_corrected_pbd_damping", 0.0),
                        pbd_coeff_amortized=g("amortized_volume_and_time_corrected_pbd_damping", 0.0),
                        tick=int(g("tick_id", 0)) if tick is None else int(tick),
-                       volume_passes=int(g("volume_passes", 0)))
+                       volume_passes=int(g("volume_passes", 0)),
+                       right_target=(right_targets(nodes, list(g("locked_right_transform")), list(g("origin")))
+                                     if nodes is not None and lock and flags & (1 << 27) else None))
 
 
 _lib = None
@@ -114,6 +136,8 @@ def lib():
         P = C.c_void_p
         u32 = C.c_uint32
         L.orc_gen_tet_block.argtypes = [u32, u32, u32, C.c_float, C.c_float, C.c_float, u32, C.c_float, P, P]
+        L.orc_right_targets.argtypes = [u32, P, P, P, P]
+        L.orc_right_targets.restype = None
         L.orc_parse_tets.argtypes = [P, u32, P, P, P]
         L.orc_minstd_order.argtypes = [u32, P]
         L.orc_init_rest_f.argtypes = [P, u32, P, u32, C.c_float, P, P, P]

@@ -45,6 +45,11 @@
  *       Settings::volumePasses: GeoLinear3d::Constrain then runs that many
  *       SolveElementVolume sweeps over the order after the solve
  *       (XPBDFEM/Geo.cpp:780-783).
+ *   locked (arguments as `damped`, volumePasses given) m00 m01 m02 m10 m11 m12
+ *          m20 m21 m22 ox oy oz < order.u32
+ *       `damped` with Settings_LockRight: Settings::lockedRightTransform3d
+ *       (column-major) and Geo3d::origin set as given; Geo3d::Substep then
+ *       holds the Right vertices at origin + m X0 (XPBDFEM/Geo.cpp:323-331).
  *   rings  (arguments as `damped`) < torder.u32 vorder.u32
  *       `damped` with a continuous-pressure energy (8-10): stdin holds the
  *       tet order and then the vertex order (each u32 count, then the ids),
@@ -413,7 +418,7 @@ int main(int argc, char** argv) {
 	}
 
 	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered") ||
-	    !strcmp(cmd, "damped") || !strcmp(cmd, "rings")) {
+	    !strcmp(cmd, "damped") || !strcmp(cmd, "rings") || !strcmp(cmd, "locked")) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
 		uint32_t W = U(2), H = U(3), D = U(4);
 		vec3 scale(F(5), F(6), F(7));
@@ -448,7 +453,8 @@ int main(int argc, char** argv) {
 		uint32_t nsub = U(a++), lockLeft = U(a++);
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
 		const bool rings = !strcmp(cmd, "rings");
-		const bool damped = !strcmp(cmd, "damped") || rings;
+		const bool locked = !strcmp(cmd, "locked");
+		const bool damped = !strcmp(cmd, "damped") || rings || locked;
 		if (damped) {
 			s.damping = F(a++);
 			s.pbdDamping = F(a++);
@@ -470,6 +476,14 @@ int main(int argc, char** argv) {
 			                          s.timeCorrectedDrag};
 			emit("derived", 'f', derived, 3);
 			if (a < argc) s.volumePasses = U(a++);
+		}
+		if (locked) {
+			float m[9];
+			for (int k = 0; k < 9; k++) m[k] = F(a++);
+			s.lockedRightTransform3d = mat3(vec3(m[0], m[1], m[2]), vec3(m[3], m[4], m[5]), vec3(m[6], m[7], m[8]));
+			g->origin = vec3(F(a), F(a + 1), F(a + 2));
+			a += 3;
+			s.flags |= Settings_LockRight;
 		}
 		Manipulator manip;
 		manip.pickedGeo = nullptr;

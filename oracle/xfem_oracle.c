@@ -362,6 +362,18 @@ void orc_gen_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, f
 			}
 }
 
+/* The Right lock's targets (XPBDFEM/Geo.cpp:327): origin + m * vec3(X0),
+ * m column-major, each row dotted left to right in float. */
+void orc_right_targets(uint32_t nv, const float* nodes, const float m[9], const float origin[3], double* out) {
+	for (uint32_t i = 0; i < nv; i++) {
+		const float x = nodes[3 * (size_t)i], y = nodes[3 * (size_t)i + 1], z = nodes[3 * (size_t)i + 2];
+		for (int k = 0; k < 3; k++) {
+			const float r = m[k] * x + m[3 + k] * y + m[6 + k] * z;
+			out[3 * (size_t)i + k] = (double)(origin[k] + r);
+		}
+	}
+}
+
 /* GenerateHexBlock + GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244). */
 void orc_gen_tet_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz, uint32_t pattern,
                        float wonkiness, float* nodes, uint32_t* idx) {

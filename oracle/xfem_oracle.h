@@ -79,7 +79,18 @@ typedef struct orc_params {
 	float pbd_coeff_amortized; /* Settings::amortizedVolumeAndTimeCorrectedPbdDamping */
 	uint32_t tick;             /* Settings::tickId of the first substep; +1 per substep */
 	uint32_t volume_passes;    /* Settings::volumePasses: SolveElementVolume sweeps after the solve */
+	/* Settings_LockRight (XPBDFEM/Geo.cpp:323-331): vertices whose lock mask
+	 * has bit 1 (the Right flag) end every substep at right_target (3 doubles
+	 * per vertex, origin + lockedRightTransform3d X0, see orc_right_targets)
+	 * with a zero inverse mass. Left vertices are those with bit 0. */
+	uint32_t lock_right;
+	const double* right_target;
 } orc_params;
+
+/* origin + m * vec3(X0) for every vertex in float, the reference's mat3 *
+ * vec3 (rows dotted with the vector, XPBDFEM/vectormath.h:508-513) and vec3
+ * addition (XPBDFEM/Geo.cpp:327); m column-major. out: 3 doubles per vertex. */
+void orc_right_targets(uint32_t nv, const float* nodes, const float m[9], const float origin[3], double* out);
 
 /* ---- mesh ---------------------------------------------------------------- */
 /* GenerateTetBlock (XPBDFEM/MeshGen.cpp:156-244): nodes[3*(W+1)(H+1)(D+1)],

@@ -240,7 +240,7 @@ int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double*
 		}
 		const double* O = Os + n3 * s;
 		for (uint32_t i = 0; i < nv; i++) {
-			if (p->lock_active && lock_mask && lock_mask[i]) {
+			if (p->lock_active && lock_mask && (lock_mask[i] & 1u)) {
 				memcpy(X + 3 * (size_t)i, O + 3 * (size_t)i, sizeof(double) * 3);
 				w[i] = 0.0;
 			}
@@ -275,7 +275,7 @@ int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double*
 		}
 		/* locks and ground forward again (Y is the post-sweep position) */
 		for (uint32_t i = 0; i < nv; i++) {
-			const int locked = p->lock_active && lock_mask && lock_mask[i];
+			const int locked = p->lock_active && lock_mask && (lock_mask[i] & 1u);
 			gf[i].contact = 0;
 			if (locked) memcpy(Y + 3 * (size_t)i, O + 3 * (size_t)i, sizeof(double) * 3);
 			const double wi = locked ? 0.0 : wsub[i];
@@ -295,7 +295,7 @@ int orc_adjoint_d(uint32_t nv, const double* X0, const double* V0, const double*
 		/* ground, locks */
 		for (uint32_t i = 0; i < nv; i++) {
 			ground_reverse(&gf[i], Xb + 3 * (size_t)i, Ob + 3 * (size_t)i);
-			if (p->lock_active && lock_mask && lock_mask[i]) {
+			if (p->lock_active && lock_mask && (lock_mask[i] & 1u)) {
 				acc(Ob + 3 * (size_t)i, ld(Xb + 3 * (size_t)i));
 				st(Xb + 3 * (size_t)i, v(0, 0, 0));
 			}

@@ -146,6 +146,21 @@ CASES = [
                                             0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
     ("rings_wonky_cpixar_post_star", ["rings", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
                                       -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
+    # the Right lock (Settings_LockRight, XPBDFEM/Geo.cpp:323-331): the
+    # `damped` arguments with volumePasses, then lockedRightTransform3d
+    # (column-major; the demo's rotation(0.3) * scale(1.2, 1) form,
+    # XPBDFEM/Demo.cpp:71-79) and Geo3d::origin
+    ("locked_c1_nh_nu045_star", ["locked", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 4, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                 0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 0,
+                                 1.1464038, 0.35462425, 0.0, -0.29552021, 0.9553365, 0.0, 0.0, 0.0, 1.0,
+                                 0.02, -0.01, 0.005]),
+    ("locked_c1_yeoh_nu049_amortized_pbd_tet", ["locked", 8, 2, 2, 0.1, 0.1, 0.1, 0.0, 1000.0, 7, 1, 3.2e-4, 0.49,
+                                                0.0, -9.81, DT, 40, 1, 0.02, 0.05, 0.0, 3, 0.1, 0,
+                                                1.1464038, 0.35462425, 0.0, -0.29552021, 0.9553365, 0.0, 0.0, 0.0,
+                                                1.0, 0.0, 0.0, 0.0]),
+    ("locked_wonky_nh_serial_nu045_right_only_star", ["locked", 4, 3, 2, 0.05, 0.05, 0.05, 0.3, 1000.0, 4, 0, 1e-3,
+                                                      0.45, -2.0, -9.81, DT, 10, 0, 0.0, 0.0, 0.0, 2, 0.05, 0,
+                                                      1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.01, 0.02, -0.03]),
     # linear hexahedra (GeoLinear3d's hex loops on a GenerateHexBlock mesh):
     # the `h` commands take the element pattern after the scale; the substep
     # cases run in the GPU's hex colour order
@@ -328,7 +343,7 @@ def main():
             order = sch["tet_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
-        if args[0] in ("ordered", "damped", "rings"):
+        if args[0] in ("ordered", "damped", "rings", "locked"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]
             nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), 0, wonk)
@@ -349,7 +364,7 @@ def main():
         arrays.update(extra)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
         manifest[name] = {"args": args}
-        if args[0] in ("ordered", "damped", "rings"):
+        if args[0] in ("ordered", "damped", "rings", "locked"):
             manifest[name]["schedule_mode"] = manifest_mode
         print(f"{name}: " + ", ".join(f"{k}{list(v.shape)}" for k, v in arrays.items()))
     manifest = {n: manifest[n] for n, _ in CASES if n in manifest}

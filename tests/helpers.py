@@ -5,9 +5,10 @@ import oracle
 import xfem
 
 
-def oracle_params(s, dt, lock=True):
-    """orc_params from an xfem Settings struct or settings dict."""
-    return oracle.params_from_settings(s, dt, lock)
+def oracle_params(s, dt, lock=True, nodes=None):
+    """orc_params from an xfem Settings struct or settings dict (nodes: the
+    rest positions, for the Right lock's targets)."""
+    return oracle.params_from_settings(s, dt, lock, nodes=nodes)
 
 
 def rel(a, b):
@@ -23,7 +24,10 @@ class OracleRun:
     def __init__(self, nodes, idx, density, settings, order, lock_mask=None, tet_mu=None, dtype=np.float32):
         self.tets, nv = oracle.parse_tets(idx)
         self.ep, self.w, fl = oracle.init_rest(nodes, self.tets, density, dtype)
-        self.lock = (fl & 1).astype(np.uint8) if lock_mask is None else np.asarray(lock_mask, np.uint8)
+        # bit 0: the Left lock (or the caller's mask), bit 1: the Right flag
+        self.lock = ((fl & 1) if lock_mask is None else np.asarray(lock_mask, np.uint8) & 1) | (fl & 2)
+        self.lock = self.lock.astype(np.uint8)
+        self.nodes = np.asarray(nodes, np.float32).reshape(-1)
         self.X = np.asarray(nodes, np.float64).reshape(-1, 3).copy()
         self.V = np.zeros_like(self.X)
         self.s = settings
@@ -34,7 +38,7 @@ class OracleRun:
         self.lam = None
 
     def step(self, n, dt):
-        p = oracle_params(self.s, dt)
+        p = oracle_params(self.s, dt, nodes=self.nodes)
         self.X, self.V, self.w, self.contact, self.lam = oracle.substeps(
             self.X, self.V, self.w, self.tets, self.ep, self.order, n, p, lock_mask=self.lock,
             tet_mu=self.tet_mu, dtype=self.dtype, want_lambdas=True)
@@ -47,7 +51,8 @@ class HexOracleRun:
     def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
         self.hexes, nv = oracle.parse_hexes(idx)
         self.ep, self.w, fl = oracle.hex_init_rest(nodes, self.hexes, density, dtype)
-        self.lock = (fl & 1).astype(np.uint8)
+        self.lock = (fl & 3).astype(np.uint8)
+        self.nodes = np.asarray(nodes, np.float32).reshape(-1)
         self.X = np.asarray(nodes, np.float64).reshape(-1, 3).copy()
         self.V = np.zeros_like(self.X)
         self.s = settings
@@ -55,7 +60,7 @@ class HexOracleRun:
         self.dtype = dtype
 
     def step(self, n, dt):
-        p = oracle_params(self.s, dt)
+        p = oracle_params(self.s, dt, nodes=self.nodes)
         self.X, self.V, self.w, _ = oracle.hex_substeps(self.X, self.V, self.w, self.hexes, self.ep, self.order, n, p,
                                                         lock_mask=self.lock, dtype=self.dtype)
         return self
@@ -67,7 +72,8 @@ class T10OracleRun:
 
     def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
         self.q = oracle.Quadratic(nodes, idx, density, dtype)
-        self.lock = (self.q.flags & 1).astype(np.uint8)
+        self.lock = (self.q.flags & 3).astype(np.uint8)
+        self.nodes = self.q.X0.astype(np.float32).reshape(-1)
         self.X = self.q.X0.copy()
         self.V = np.zeros_like(self.X)
         self.w = self.q.w.copy()
@@ -75,7 +81,7 @@ class T10OracleRun:
         self.order = order
 
     def step(self, n, dt):
-        p = oracle_params(self.s, dt)
+        p = oracle_params(self.s, dt, nodes=self.nodes)
         self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
         return self
 
@@ -116,7 +122,8 @@ class H27OracleRun:
 
     def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
         self.q = oracle.QuadraticHex(nodes, idx, density, dtype)
-        self.lock = (self.q.flags & 1).astype(np.uint8)
+        self.lock = (self.q.flags & 3).astype(np.uint8)
+        self.nodes = self.q.X0.astype(np.float32).reshape(-1)
         self.X = self.q.X0.copy()
         self.V = np.zeros_like(self.X)
         self.w = self.q.w.copy()
@@ -124,6 +131,6 @@ class H27OracleRun:
         self.order = order
 
     def step(self, n, dt):
-        p = oracle_params(self.s, dt)
+        p = oracle_params(self.s, dt, nodes=self.nodes)
         self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
         return self

@@ -152,6 +152,53 @@ def test_damped_substeps_bit_exact(orc, name):
     assert not np.array_equal(Xu.reshape(-1), g["xn"])
 
 
+LOCKED = ["locked_c1_nh_nu045_star", "locked_c1_yeoh_nu049_amortized_pbd_tet",
+          "locked_wonky_nh_serial_nu045_right_only_star"]
+
+
+def locked_params(orc, a, derived, tick, nodes):
+    """orc_params of a `locked` fixture: the `damped` ones plus the Right
+    lock's targets from lockedRightTransform3d and Geo3d::origin."""
+    p = damped_params(orc, a[:24], derived, tick)
+    targets = orc.right_targets(nodes, a[24:33], a[33:36])
+    return orc.make_params(dt=p.dt, compliance=p.compliance, poisson=p.poisson, energy=p.energy,
+                           simultaneous=bool(p.simultaneous), gravity=tuple(p.gravity), lock=bool(p.lock_active),
+                           drag=p.time_corrected_drag, damping=p.damping, rayleigh_type=p.rayleigh_type,
+                           pbd_damping=p.pbd_damping, pbd_coeff=p.pbd_coeff, pbd_coeff_amortized=p.pbd_coeff_amortized,
+                           tick=tick, volume_passes=p.volume_passes, right_target=targets)
+
+
+@pytest.mark.parametrize("name", LOCKED)
+def test_locked_right_substeps_bit_exact(orc, name):
+    """Settings_LockRight (XPBDFEM/Geo.cpp:323-331): the Right vertices (x
+    above 98% of the extent) end every substep at origin +
+    lockedRightTransform3d X0 with a zero inverse mass, after the Left lock;
+    the oracle in the fixture's order equals the reference bit for bit."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[8], a[16]
+    tets, nv = orc.parse_tets(g["idx"])
+    ep, w, fl = orc.init_rest(g["nodes"], tets, dens)
+    assert (fl & 2).any()
+    order = g["order"]
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lock_mask = (fl & 3).astype(np.uint8)
+    X1, V1, w1, _ = orc.substeps(X0, V0, w, tets, ep, order, 1, locked_params(orc, a, g["derived"], 0, g["nodes"]),
+                                 lock_mask=lock_mask)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, wn, _ = orc.substeps(X1, V1, w1, tets, ep, order, nsub - 1,
+                                 locked_params(orc, a, g["derived"], 1, g["nodes"]), lock_mask=lock_mask)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.all(wn[(fl & 2) != 0] == 0)
+    # the lock moved them: without it the run differs
+    Xu, _, _, _ = orc.substeps(X0, V0, w, tets, ep, order, nsub, damped_params(orc, a[:24], g["derived"], 0),
+                               lock_mask=lock_mask)
+    assert not np.array_equal(Xu.reshape(-1), g["xn"])
+
+
 RINGS = ["rings_c1_cpixar_nu045_star", "rings_c1_cmixed_nu045_star", "rings_c1_cmixed_incompressible_star",
          "rings_c1_cskin_nu049_star", "rings_wonky_cmixed_paper_star", "rings_c1_cskin_limit_star",
          "rings_c1_cmixed_amortized_pbd_star", "rings_wonky_cpixar_post_star"]

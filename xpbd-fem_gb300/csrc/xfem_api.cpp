@@ -138,6 +138,7 @@ struct xfem_body {
 	DevBuf<uint32_t> tet_rec_dev, tet_slot_dev;
 	DevBuf<uint32_t> tflat, tick;   // per tet row: index in the body's order; the tick word
 	DevBuf<float> tarea;            // per tet row: surface area
+	DevBuf<float4> right_target;    // per device vertex: the Right lock's target (LockRight bodies)
 	DevBuf<uint32_t> lastmask;      // per chunk lane: slots whose last solve it makes
 	DevBuf<uint8_t> pass_on;        // [damping kind][tick % 8][colour]
 	DevBuf<float> tet_vol_dev, tet_inv_mu, io;
@@ -205,7 +206,10 @@ int validate_settings(const xfem_settings& s) {
 	if (model == kModelPixar && !(s.poissons_ratio < 0.5f))
 		return fail(XFEM_EINVAL, "the Pixar models need poissons_ratio < 0.5 (lambda = 2 / (1 - 2 nu))");
 	if (!(s.damping >= 0.0f) || !(s.pbd_damping >= 0.0f)) return fail(XFEM_EINVAL, "damping and pbd_damping must be >= 0");
-	if (s.flags & (1u << 27)) return fail(XFEM_EUNSUPPORTED, "Settings_LockRight is not supported");
+	for (int k = 0; k < 9; k++)
+		if (!isfinite(s.locked_right_transform[k])) return fail(XFEM_EINVAL, "locked_right_transform must be finite");
+	for (int k = 0; k < 3; k++)
+		if (!isfinite(s.origin[k])) return fail(XFEM_EINVAL, "origin must be finite");
 	if (!(s.compliance > 0.0f)) return fail(XFEM_EINVAL, "compliance must be > 0");
 	if (!(s.poissons_ratio > 0.0f && s.poissons_ratio <= 0.5f))
 		return fail(XFEM_EINVAL, "poissons_ratio must be in (0, 0.5]");
@@ -242,6 +246,7 @@ BodyParams make_params(const xfem_settings& s) {
 	for (int k = 0; k < 3; k++) p.gravity[k] = s.gravity[k];
 	p.drag_mul = 1.0f - s.time_corrected_drag;
 	p.lock_active = (s.flags & XFEM_LOCK_LEFT) ? 1u : 0u;
+	p.lock_right = (s.flags & XFEM_LOCK_RIGHT) ? 1u : 0u;
 	p.ground = s.ground ? 1u : 0u;
 	p.friction = s.friction;
 	for (int k = 0; k < 3; k++) p.ground_n[k] = s.ground_normal[k];
@@ -321,6 +326,38 @@ std::vector<uint8_t> pass_table(const std::vector<BodyHost>& bodies, uint32_t nc
 float tet_c0(const BodyHost& b, uint32_t t) {
 	const float mu = b.tet_mu.empty() ? 1.0f / b.settings.compliance : b.tet_mu[t];
 	return 1.0f / mu / b.ep[17 * (size_t)t + 15];
+}
+
+// The Right lock's target of every Right vertex of the bodies that lock them,
+// origin + lockedRightTransform3d * vec3(X0) in float with the reference's
+// mat3 * vec3 (rows dotted with X0, XPBDFEM/vectormath.h:508-513, and dot's
+// left-to-right sum) and the vec3 addition (XPBDFEM/Geo.cpp:327), in device
+// vertex order; the buffer exists only while some body locks its Right side.
+int update_right_targets(xfem_body* h) {
+	bool any = false;
+	for (const BodyHost& b : h->bodies) any = any || (b.settings.flags & XFEM_LOCK_RIGHT);
+	if (!any) {
+		h->ctx.right_target = nullptr;
+		return XFEM_OK;
+	}
+	std::vector<float4> t(h->nverts, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+	for (const BodyHost& b : h->bodies) {
+		if (!(b.settings.flags & XFEM_LOCK_RIGHT)) continue;
+		const float* T = b.settings.locked_right_transform;
+		const float* o = b.settings.origin;
+		for (uint32_t v = 0; v < b.nv; v++) {
+			if (!(b.vflags[v] & 2u)) continue;
+			const float x = b.nodes[3 * (size_t)v], y = b.nodes[3 * (size_t)v + 1], z = b.nodes[3 * (size_t)v + 2];
+			float r[3];
+			for (int k = 0; k < 3; k++) r[k] = T[k] * x + T[3 + k] * y + T[6 + k] * z;
+			t[b.vbase + b.sched.vert_rank[v]] = make_float4(o[0] + r[0], o[1] + r[1], o[2] + r[2], 0.0f);
+		}
+	}
+	XCUDA(h->right_target.reserve(t.size()));
+	XCUDA(cudaMemcpyAsync(h->right_target.p, t.data(), t.size() * sizeof(float4), cudaMemcpyHostToDevice, h->stream));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	h->ctx.right_target = h->right_target.p;
+	return XFEM_OK;
 }
 
 // Status and message of a device error word (kErr*).
@@ -1036,7 +1073,7 @@ int build_device(xfem_body* h) {
 		for (uint32_t v = 0; v < b.nv; v++) {
 			const uint32_t dv = b.vbase + b.sched.vert_rank[v];
 			dev_of[b.vbase + v] = dv;
-			const uint32_t bits = (b.vflags[v] & 1u ? kFlagLocked : 0u) | (bi << 8);
+			const uint32_t bits = (b.vflags[v] & 1u ? kFlagLocked : 0u) | (b.vflags[v] & 2u ? kFlagRight : 0u) | (bi << 8);
 			vert[2 * (size_t)dv] = make_float4(b.nodes[3 * (size_t)v], b.nodes[3 * (size_t)v + 1], b.nodes[3 * (size_t)v + 2], b.w0[v]);
 			vert[2 * (size_t)dv + 1] = make_float4(0.0f, 0.0f, 0.0f, __builtin_bit_cast(float, bits));
 		}
@@ -1201,7 +1238,7 @@ int build_device(xfem_body* h) {
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
-	return XFEM_OK;
+	return update_right_targets(h);
 }
 
 int set_config(xfem_body* h, int sync_mode, int block) {
@@ -1498,6 +1535,9 @@ int xfem_settings_default(xfem_settings* s) {
 	s->ground_normal[2] = 1.0f;
 	s->ground_offset = 0.0f;
 	s->friction = 0.0f;
+	// Settings::lockedRightTransform3d = mat3(1) and Geo3d::origin = 0 until
+	// the demo sets them (XPBDFEM/Demo.cpp:79, XPBDFEM/Geo.h:69)
+	s->locked_right_transform[0] = s->locked_right_transform[4] = s->locked_right_transform[8] = 1.0f;
 	return XFEM_OK;
 }
 
@@ -1581,6 +1621,12 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 		}
 	}
 	if (h->ring_mode) h->ctx.ext = ring_damp_of(h->bodies) ? 1u : 0u;
+	const float4* rt_before = h->ctx.right_target;
+	if (const int rr = update_right_targets(h)) return rr;
+	if (h->graph && h->ctx.right_target != rt_before) {  // the captured launches hold the old pointer
+		cudaGraphExecDestroy(h->graph);
+		h->graph = nullptr;
+	}
 	if (material && b->tet_mu.empty() && !h->el_mode) return update_material(h, *b);
 	return XFEM_OK;
 }
@@ -2244,6 +2290,8 @@ int xfem_adjoint_forward(xfem_body* h, uint32_t nsub, float dt, uint32_t checkpo
 			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate volume passes (volume_passes must be 0)");
 		if (b.settings.damping > 0.0f || b.settings.pbd_damping > 0.0f)
 			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate damping (damping, pbd_damping must be 0)");
+		if (b.settings.flags & XFEM_LOCK_RIGHT)
+			return fail(XFEM_EUNSUPPORTED, "the adjoint does not differentiate the Right lock (XFEM_LOCK_RIGHT)");
 	}
 	XCUDA(cudaSetDevice(h->device));
 	AdjointRun& a = h->adj;

@@ -120,12 +120,21 @@ __device__ __forceinline__ bool ground_contact(const BodyParams& bp, const float
 	return true;
 }
 
-// End of a substep for one vertex: locks (XPBDFEM/Geo.cpp:318-322), ground,
-// then the velocity V = D / dt (XPBDFEM/Geo.cpp:342-344) is returned.
-__device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, float4& D, uint32_t& bits, float inv_dt) {
+// End of a substep for one vertex: locks (XPBDFEM/Geo.cpp:318-331), ground,
+// then the velocity V = D / dt (XPBDFEM/Geo.cpp:342-344) is returned. A Left
+// vertex stays where the substep started (X = O); a Right vertex goes to its
+// target origin + lockedRightTransform3d X0 (X = O = target, so V = 0), read
+// from right_target[v] (device vertex v); both keep a zero inverse mass.
+__device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, float4& D, uint32_t& bits, float inv_dt,
+                                              const float4* right_target, uint32_t v) {
 	if (bp.lock_active && (bits & kFlagLocked)) {
 		D.x = D.y = D.z = 0.0f;
 		O.w = 0.0f;
+	}
+	if (bp.lock_right && (bits & kFlagRight)) {
+		const float4 t = __ldg(right_target + v);
+		O = make_float4(t.x, t.y, t.z, 0.0f);
+		D.x = D.y = D.z = 0.0f;
 	}
 	bits &= ~kFlagContact;
 	if (bp.ground && O.w > 0.0f && ground_contact(bp, O, D)) bits |= kFlagContact;
@@ -133,16 +142,17 @@ __device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, f
 }
 
 // Finalize the previous substep (unless `first`: (O, D) then hold the
-// canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312).
-__device__ __forceinline__ void advance_vertex(const BodyParams* bodies, float4& O, float4& D, bool first, float dt,
+// canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312) for
+// device vertex v.
+__device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, bool first, float dt,
                                                float inv_dt) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = bodies[bits >> 8];
+	const BodyParams& bp = C.bodies[bits >> 8];
 	Vec3 V;
 	if (first) {
 		V = v3(D);
 	} else {
-		V = finish_vertex(bp, O, D, bits, inv_dt);
+		V = finish_vertex(bp, O, D, bits, inv_dt, C.right_target, v);
 		O.x += D.x;
 		O.y += D.y;
 		O.z += D.z;
@@ -153,14 +163,14 @@ __device__ __forceinline__ void advance_vertex(const BodyParams* bodies, float4&
 	D = make_float4(V.x * dt, V.y * dt, V.z * dt, __uint_as_float(bits));
 }
 
-// Finalize the last substep of a launch: (O, D) -> canonical (X, V). A
-// position or velocity that is no longer finite (a diverged solve, or a NaN
-// the caller set) is recorded in the error word as kErrNonFinite, which the
-// next synchronising call reports.
-__device__ __forceinline__ void finalize_vertex(const DevCtx& C, float4& O, float4& D, float inv_dt) {
+// Finalize the last substep of a launch: (O, D) -> canonical (X, V) for
+// device vertex v. A position or velocity that is no longer finite (a
+// diverged solve, or a NaN the caller set) is recorded in the error word as
+// kErrNonFinite, which the next synchronising call reports.
+__device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, float inv_dt) {
 	uint32_t bits = __float_as_uint(D.w);
 	const BodyParams& bp = C.bodies[bits >> 8];
-	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt);
+	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt, C.right_target, v);
 	O.x += D.x;
 	O.y += D.y;
 	O.z += D.z;

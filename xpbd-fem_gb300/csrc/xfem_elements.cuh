@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			advance_vertex(C.bodies, O, D, s == 0 || dmode, dt, inv_dt);
+			advance_vertex(C, v, O, D, s == 0 || dmode, dt, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 		if (!grid_sync(C, target)) return;
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C, O, D, inv_dt);
+			finalize_vertex(C, v, O, D, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 		if (!grid_sync(C, target)) return;
@@ -285,7 +285,7 @@ __global__ void __launch_bounds__(256, E::kMinBlocks) k_elements(DevCtx C, uint3
 		for (uint32_t v = gtid; v < C.nverts; v += nthreads) {
 			float4 O, D;
 			ld_vertex(C.vert + 2 * (size_t)v, O, D);
-			finalize_vertex(C, O, D, inv_dt);
+			finalize_vertex(C, v, O, D, inv_dt);
 			st_vertex(C.vert + 2 * (size_t)v, O, D);
 		}
 	}

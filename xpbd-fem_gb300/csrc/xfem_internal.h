@@ -192,7 +192,8 @@ struct BodyParams {
 	float lambda;             // (2 mu nu) / (1 - 2 nu) (continuous-pressure models)
 	uint32_t nverts;          // vertices of the body (amortized ring damping slices)
 	uint32_t cube_fast;       // SolveElementCube's short path on hexes: CubeNeo, nu >= 0.5, no damping
-	uint32_t pad4[2];
+	uint32_t lock_right;      // Settings_LockRight: hold the Right vertices at DevCtx::right_target
+	uint32_t pad4;
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
@@ -253,6 +254,8 @@ struct DevCtx {
 	uint32_t vs_off;            // byte offset of the vertex slots in a warp's area
 	uint32_t* bar_count;        // grid barrier arrival counter
 	int* err;                   // device error word (0 = ok)
+	const float4* right_target; // per device vertex: origin + lockedRightTransform3d X0 of the
+	                            // Right vertices of bodies that lock them (null when none does)
 	uint64_t timeout_ns;        // limit of every bounded device wait (barrier, copy, dependency)
 	uint32_t bar_base;          // the arrival counter's value at launch: 0, or 0xffffffff
 	                            // (a test of the counter's wrap: the first barrier wraps it)
@@ -344,6 +347,7 @@ struct AdjCtx {
 // Vertex flag bits kept in the .w word of the second float4.
 constexpr uint32_t kFlagLocked = 1u;
 constexpr uint32_t kFlagContact = 2u;
+constexpr uint32_t kFlagRight = 4u;  // the reference's Right flag (x above 98% of the extent)
 
 // Device error codes written to DevCtx::err.
 constexpr int kErrBarrierTimeout = 1;

@@ -190,7 +190,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 		for (int s = 0; s < 8; s++)
 			if (mask & (1u << s)) {
 				const float4 Dbefore = D[s];
-				advance_vertex(C.bodies, O[s], D[s], first, dt, inv_dt);
+				advance_vertex(C, vid[s], O[s], D[s], first, dt, inv_dt);
 				if (TAPE) tape_vertex(C, vid[s], O[s], Dbefore, s_launch, first);
 			}
 #pragma unroll
@@ -215,7 +215,7 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 		// or finished the vertex, and no other cluster of the pass touches it
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
-			if (EXT && (last & (1u << s))) finalize_vertex(C, O[s], D[s], inv_dt);
+			if (EXT && (last & (1u << s))) finalize_vertex(C, vid[s], O[s], D[s], inv_dt);
 			st_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
 		}
 	}
@@ -258,7 +258,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 				ld_vertex(C.vert + 2 * (size_t)vid[s], O, D);
 				if (mask & (1u << s)) {
 					const float4 Dbefore = D;
-					advance_vertex(C.bodies, O, D, first, dt, inv_dt);
+					advance_vertex(C, vid[s], O, D, first, dt, inv_dt);
 					if (TAPE) tape_vertex(C, vid[s], O, Dbefore, s_launch, first);
 				}
 				sO[s * kLanes] = O;
@@ -288,7 +288,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 		for (uint32_t s = 0; s < kMaxClusterVerts; s++) {
 			if (s < nv) {
 				float4 O = sO[s * kLanes], D = sD[s * kLanes];
-				if (EXT && (last & (1u << s))) finalize_vertex(C, O, D, inv_dt);
+				if (EXT && (last & (1u << s))) finalize_vertex(C, vid[s], O, D, inv_dt);
 				st_vertex(C.vert + 2 * (size_t)vid[s], O, D);
 			}
 		}
@@ -359,7 +359,7 @@ __device__ __noinline__ void vol_chunk(const DevCtx& C, Stage& st, uint32_t chun
 		for (uint32_t s = 0; s < NV; s++) {
 			if (s < nv) {
 				if (last & (1u << s)) {
-					finalize_vertex(C, O[s], D[s], inv_dt);
+					finalize_vertex(C, vid[s], O[s], D[s], inv_dt);
 					__stcg(C.vert + 2 * (size_t)vid[s], O[s]);
 				}
 				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
@@ -481,10 +481,10 @@ __device__ __forceinline__ void run_isolated(const DevCtx& C, uint32_t begin, ui
 		ld_vertex(C.vert + 2 * (size_t)v, O, D);
 		for (uint32_t s = 0; s < nsub; s++) {
 			const float4 Dbefore = D;
-			advance_vertex(C.bodies, O, D, s == 0, dt, inv_dt);
+			advance_vertex(C, v, O, D, s == 0, dt, inv_dt);
 			if (TAPE) tape_vertex(C, v, O, Dbefore, s, s == 0);
 		}
-		if (finalize_end) finalize_vertex(C, O, D, inv_dt);
+		if (finalize_end) finalize_vertex(C, v, O, D, inv_dt);
 		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 }
@@ -496,7 +496,7 @@ __device__ __forceinline__ void run_finalize(const DevCtx& C, uint32_t begin, ui
 		float4 O, D;
 		ld_vertex(C.vert + 2 * (size_t)v, O, D);
 		if (TAPE) __stcs(C.tape_fin + v, D);
-		finalize_vertex(C, O, D, inv_dt);
+		finalize_vertex(C, v, O, D, inv_dt);
 		if (TAPE) {
 			const int q = __ldg(C.tip_of + v);
 			if (q >= 0) C.traj[(size_t)(C.sub_base + nsub - 1) * C.ntips + q] = O;

@@ -43,6 +43,7 @@ ENERGY_CUBE_SKIN = 12
 MAX_VOLUME_PASSES = 64
 XPBD_SOLVE_BIT = 11
 LOCK_LEFT = 1 << 26
+LOCK_RIGHT = 1 << 27
 REF_YEOH = (0.1095, 14.95, 4.595)  # XPBDFEM/Fem.cpp:526
 
 
@@ -63,6 +64,7 @@ class Settings(C.Structure):
         ("ground_normal", C.c_float * 3), ("ground_offset", C.c_float), ("friction", C.c_float),
         ("volume_and_time_corrected_pbd_damping", C.c_float),
         ("amortized_volume_and_time_corrected_pbd_damping", C.c_float), ("tick_id", C.c_uint32),
+        ("locked_right_transform", C.c_float * 9), ("origin", C.c_float * 3),
     ]
 
 
@@ -187,7 +189,7 @@ def default_settings(**kw):
     s = Settings()
     _check(lib().xfem_settings_default(C.byref(s)))
     for k, v in kw.items():
-        if k in ("gravity", "yeoh", "ground_normal"):
+        if k in ("gravity", "yeoh", "ground_normal", "locked_right_transform", "origin"):
             getattr(s, k)[:] = [float(x) for x in v]
         else:
             setattr(s, k, v)
