@@ -154,8 +154,11 @@ def lib():
         L.orc_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P, P, P, P]
         L.orc_adjoint_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, u32, P, P, P, P, P, P]
         L.orc_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
+        L.orc_hex_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
+        L.orc_hex_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
         L.orc_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, P, P]
         L.orc_ring_schedule.argtypes = [P, u32, P, u32, u32, P, P, P]
+        L.orc_ring_schedule_elems.argtypes = [P, u32, P, u32, u32, u32, P, P, P]
         L.orc_gen_hex_block.argtypes = [u32, u32, u32, C.c_float, C.c_float, C.c_float, u32, C.c_float, P, P]
         L.orc_parse_hexes.argtypes = [P, u32, P, P, P]
         L.orc_hex_tables.argtypes = [P, P, P]
@@ -308,14 +311,15 @@ def substeps_rings(X, V, w, tets, ep, torder, vorder, nsub, params, lock_mask=No
 
 def ring_schedule(nodes, tets, morton=1):
     """Vertex ring order of the continuous-pressure models (colour-major) and
-    the colour offsets."""
+    the colour offsets; tets (n, 4) or, on a hex mesh, hexes (n, 8)."""
     nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
     tets = np.ascontiguousarray(tets, np.uint32)
     nv = nodes.size // 3
     vorder = np.zeros(nv, np.uint32)
     cb = np.zeros(nv + 1, np.uint32)
     ncol = C.c_uint32()
-    if lib().orc_ring_schedule(_p(nodes), nv, _p(tets), tets.shape[0], morton, _p(vorder), _p(cb), C.byref(ncol)):
+    if lib().orc_ring_schedule_elems(_p(nodes), nv, _p(tets), tets.shape[1], tets.shape[0], morton, _p(vorder),
+                                     _p(cb), C.byref(ncol)):
         raise ValueError("ring schedule limits exceeded")
     return dict(vert_order=vorder, colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
 
@@ -441,6 +445,27 @@ def hex_substeps(X, V, w, hexes, ep, order, nsub, params, lock_mask=None, dtype=
     if f(nv, _p(X), _p(V), _p(w), _p(lm), hexes.shape[0], _p(hexes), _p(ep), _p(order), nsub, C.byref(params),
          _p(contact)):
         raise ValueError("energy model not covered on hexes")
+    return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+
+def hex_substeps_rings(X, V, w, hexes, ep, horder, vorder, nsub, params, lock_mask=None, dtype=np.float32):
+    """nsub substeps of a continuous-pressure model (energy 8-10) on a hex
+    mesh: every vertex's one-ring solved in `vorder`, PBD damping over the
+    hexes in `horder`. Returns X, V, w, contact mask."""
+    X = np.array(X, np.float64).reshape(-1).copy()
+    V = np.array(V, np.float64).reshape(-1).copy()
+    w = np.array(w, dtype).copy()
+    nv = w.size
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    horder = np.ascontiguousarray(horder, np.uint32)
+    vorder = np.ascontiguousarray(vorder, np.uint32)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    contact = np.zeros(nv, np.uint8)
+    f = lib().orc_hex_substeps_rings_f if dtype == np.float32 else lib().orc_hex_substeps_rings_d
+    if f(nv, _p(X), _p(V), _p(w), _p(lm), hexes.shape[0], _p(hexes), _p(ep), _p(horder), _p(vorder), nsub,
+         C.byref(params), _p(contact)):
+        raise ValueError("not a continuous-pressure energy model")
     return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
 
 

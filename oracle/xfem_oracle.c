@@ -15,16 +15,17 @@
 /* ---- one-rings (integer; shared by both instantiations) ------------------ */
 /* The one-ring of every vertex as OneRingConstructor builds it
  * (XPBDFEM/Connectivity.h:114-160), filled as GeoLinear3d::Init fills it
- * (XPBDFEM/Geo.cpp:747-757): the vertex's tets in increasing id (the order
- * Connectivity3d::Init lists them, XPBDFEM/Connectivity.cpp:437-439); the
- * ring's nodes, the vertex first, then each tet's vertices in order of first
- * appearance; and for each tet corner its node index. */
+ * (XPBDFEM/Geo.cpp:747-757): the vertex's elements (tets, or on a hex mesh
+ * hexes) in increasing id (the order Connectivity3d::Init lists them,
+ * XPBDFEM/Connectivity.cpp:437-439); the ring's nodes, the vertex first,
+ * then each element's vertices in order of first appearance; and for each
+ * element corner its node index. */
 typedef struct {
 	uint32_t* tet_off;  /* nv + 1, into tet_list */
-	uint32_t* tet_list;
+	uint32_t* tet_list; /* element ids */
 	uint32_t* node_off; /* nv + 1, into nodes */
 	uint32_t* nodes;
-	uint16_t* corner;   /* 4 per tet_list entry */
+	uint16_t* corner;   /* npe per tet_list entry */
 } orc_rings;
 
 static void rings_free(orc_rings* r) {
@@ -35,21 +36,23 @@ static void rings_free(orc_rings* r) {
 	free(r->corner);
 }
 
-static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings* r) {
+/* elems: npe vertex ids per element (4 for tets, 8 for hexes), ne elements. */
+static int rings_build(const uint32_t* elems, uint32_t npe, uint32_t ne, uint32_t nv, orc_rings* r) {
 	memset(r, 0, sizeof(*r));
+	const size_t ninc = (size_t)npe * ne;
 	r->tet_off = (uint32_t*)calloc((size_t)nv + 1, 4);
 	r->node_off = (uint32_t*)calloc((size_t)nv + 1, 4);
-	r->tet_list = (uint32_t*)malloc(4 * (size_t)(nt ? 4 * nt : 1));
-	r->corner = (uint16_t*)malloc(2 * (size_t)(nt ? 16 * nt : 1));
-	r->nodes = (uint32_t*)malloc(4 * (size_t)(nt ? 16 * nt + nv : nv + 1));
+	r->tet_list = (uint32_t*)malloc(4 * (ninc ? ninc : 1));
+	r->corner = (uint16_t*)malloc(2 * (ninc ? npe * ninc : 1));
+	r->nodes = (uint32_t*)malloc(4 * (npe * ninc + nv + 1));
 	if (!r->tet_off || !r->node_off || !r->tet_list || !r->corner || !r->nodes) return -1;
-	for (size_t i = 0; i < 4 * (size_t)nt; i++) r->tet_off[tets[i] + 1]++;
+	for (size_t i = 0; i < ninc; i++) r->tet_off[elems[i] + 1]++;
 	for (uint32_t v = 0; v < nv; v++) r->tet_off[v + 1] += r->tet_off[v];
 	uint32_t* fill = (uint32_t*)malloc(4 * ((size_t)nv + 1));
 	if (!fill) return -1;
 	memcpy(fill, r->tet_off, 4 * (size_t)nv);
-	for (uint32_t t = 0; t < nt; t++)
-		for (int n = 0; n < 4; n++) r->tet_list[fill[tets[4 * (size_t)t + n]]++] = t;
+	for (uint32_t t = 0; t < ne; t++)
+		for (uint32_t n = 0; n < npe; n++) r->tet_list[fill[elems[(size_t)npe * t + n]]++] = t;
 	free(fill);
 	uint32_t head = 0;
 	for (uint32_t v = 0; v < nv; v++) {
@@ -58,8 +61,8 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 		uint32_t cnt = 1;
 		nodes[0] = v;
 		for (uint32_t j = r->tet_off[v]; j < r->tet_off[v + 1]; j++) {
-			const uint32_t* tv = tets + 4 * (size_t)r->tet_list[j];
-			for (int n = 0; n < 4; n++) {
+			const uint32_t* tv = elems + (size_t)npe * r->tet_list[j];
+			for (uint32_t n = 0; n < npe; n++) {
 				uint32_t k = cnt;
 				for (uint32_t q = 0; q < cnt; q++)
 					if (nodes[q] == tv[n]) {
@@ -67,7 +70,7 @@ static int rings_build(const uint32_t* tets, uint32_t nt, uint32_t nv, orc_rings
 						break;
 					}
 				if (k == cnt) nodes[cnt++] = tv[n];
-				r->corner[4 * (size_t)j + n] = (uint16_t)k;
+				r->corner[(size_t)npe * j + n] = (uint16_t)k;
 			}
 		}
 		head += cnt;
@@ -601,22 +604,27 @@ static int orc_vertex_ranks(const float* nodes, uint32_t nv, uint32_t morton, ui
 
 int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t morton,
                       uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours) {
+	return orc_ring_schedule_elems(nodes, nv, tets, 4, nt, morton, vorder, colour_begin, ncolours);
+}
+
+int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
+                            uint32_t morton, uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours) {
 	orc_rings rg;
-	if (rings_build(tets, nt, nv, &rg)) {
+	if (rings_build(elems, npe, ne, nv, &rg)) {
 		rings_free(&rg);
 		return -1;
 	}
 	/* the vertices whose ring holds each node */
-	const uint32_t ne = rg.node_off[nv];
+	const uint32_t nent = rg.node_off[nv];
 	uint32_t* ho = (uint32_t*)calloc((size_t)nv + 1, 4);
-	uint32_t* hl = (uint32_t*)malloc(4 * (size_t)(ne ? ne : 1));
+	uint32_t* hl = (uint32_t*)malloc(4 * (size_t)(nent ? nent : 1));
 	uint32_t* colour = (uint32_t*)malloc(4 * (size_t)(nv ? nv : 1));
 	uint32_t* mark = (uint32_t*)malloc(4 * (size_t)ORC_MAXCOL);
 	uint32_t* rank = (uint32_t*)malloc(4 * (size_t)(nv ? nv : 1));
 	orc_kv* kv = (orc_kv*)malloc(sizeof(orc_kv) * (nv ? nv : 1));
 	int rc = -1;
 	if (!ho || !hl || !colour || !mark || !rank || !kv) goto done;
-	for (uint32_t i = 0; i < ne; i++) ho[rg.nodes[i] + 1]++;
+	for (uint32_t i = 0; i < nent; i++) ho[rg.nodes[i] + 1]++;
 	for (uint32_t v = 0; v < nv; v++) ho[v + 1] += ho[v];
 	{
 		uint32_t* f = (uint32_t*)malloc(4 * ((size_t)nv + 1));

@@ -197,6 +197,16 @@ int orc_hex_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_
 int orc_hex_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nh,
                        const uint32_t* hexes, const double* ep, const uint32_t* order, uint32_t nsub,
                        const orc_params* p, uint8_t* contact);
+/* Substeps of a hex mesh with a continuous-pressure model (energy 8-10):
+ * every vertex's one-ring solved in `vorder` (SolveRing's hex branch,
+ * XPBDFEM/Geo.cpp:147-225), the rings' post-step Rayleigh damping in
+ * `vorder` and the PBD damping over the hexes in `horder`. Returns 0 or -1. */
+int orc_hex_substeps_rings_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nh,
+                             const uint32_t* hexes, const float* ep, const uint32_t* horder, const uint32_t* vorder,
+                             uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_hex_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nh,
+                             const uint32_t* hexes, const double* ep, const uint32_t* horder, const uint32_t* vorder,
+                             uint32_t nsub, const orc_params* p, uint8_t* contact);
 /* CalculateVolume of a hex mesh (XPBDFEM/Geo.cpp:830, XPBDFEM/Fem.cpp:1046-1071). */
 float orc_hex_volume_f(const double* X, uint32_t nh, const uint32_t* hexes, const float* ep);
 double orc_hex_volume_d(const double* X, uint32_t nh, const uint32_t* hexes, const double* ep);
@@ -313,6 +323,9 @@ int orc_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t
  * allocates nv + 1). Returns 0, or -1 if a limit is exceeded. */
 int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, uint32_t morton,
                       uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours);
+/* The same over elements of npe vertices each (4: tets, 8: hexes). */
+int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
+                            uint32_t morton, uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours);
 
 /* Hex schedule: hexes coloured greedily in id order so that the hexes of one
  * colour share no vertex (each takes the smallest colour not held by an

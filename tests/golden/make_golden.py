@@ -225,6 +225,26 @@ CASES = [
     ("hdamped_c1_cube_neo_incompressible_amortized_pbd", ["hdamped", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 11, 1,
                                                           C1_COMPLIANCE, 0.5, 0.0, -9.81, DT, 40, 1, 0.01, 0.03,
                                                           0.002, 3, 0.1, 1]),
+    # continuous-pressure models on a hex mesh (SolveRing's hex branch,
+    # XPBDFEM/Geo.cpp:147-225; XPBDFEM/Fem.cpp:983-1036): the `damped`
+    # arguments with the pattern after the scale; stdin holds the GPU's hex
+    # colour order (PBD damping) and its ring vertex order
+    ("hrings_c1_cpixar_nu045", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("hrings_c1_cmixed_nu045", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("hrings_c1_cmixed_incompressible", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
+                                         0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("hrings_c1_cskin_nu049", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
+                               0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("hrings_wonky_cmixed_paper", ["hrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
+                                   -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05]),
+    ("hrings_c1_cskin_limit", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
+                               0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("hrings_c1_cmixed_amortized_pbd", ["hrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
+                                        0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("hrings_wonky_cpixar_post", ["hrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
+                                  -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
     # quadratic tets (GeoQuadratic3d on a GenerateTetBlock mesh; element
     # type T10 in the settings' flags): the `q` commands take the pattern
     # after the scale; the substep cases run in the GPU's T10 colour order
@@ -325,6 +345,18 @@ def main():
             order = sch["hex_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
+        if args[0] == "hrings":
+            import oracle  # noqa: E402
+            W, H, D, sx, sy, sz, pattern, wonk = args[1:9]
+            nodes, idx = oracle.gen_hex_block(W, H, D, (sx, sy, sz), pattern, wonk)
+            hexes, _ = oracle.parse_hexes(idx)
+            sch = oracle.hex_schedule(nodes, hexes, morton=1)
+            order = sch["hex_order"].astype(np.uint32)
+            rs = oracle.ring_schedule(nodes, hexes, morton=1)
+            vorder = rs["vert_order"].astype(np.uint32)
+            stdin = struct.pack("<I", order.size) + order.tobytes() + struct.pack("<I", vorder.size) + vorder.tobytes()
+            extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"], "vorder": vorder,
+                     "colour_vert_begin": rs["colour_vert_begin"]}
         if args[0] in ("Qordered", "Qdamped"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]

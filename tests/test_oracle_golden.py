@@ -345,7 +345,7 @@ def hex_params(orc, a, g, tick):
     """orc_params of an `hordered` / `hdamped` fixture (refgen's argument order)."""
     energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[10:19]
     kw = dict(rayleigh_type=2)
-    if a[0] == "hdamped":
+    if a[0] in ("hdamped", "hrings"):
         damping, pbd, drag, rtype, spacing = a[19:24]
         d = g["derived"]
         kw = dict(damping=damping, rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(d[0]),
@@ -376,6 +376,39 @@ def test_hex_substeps_bit_exact(orc, name):
     assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
     assert np.float32(orc.hex_volume(Xn, hexes, ep)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+HRINGS = ["hrings_c1_cpixar_nu045", "hrings_c1_cmixed_nu045", "hrings_c1_cmixed_incompressible",
+          "hrings_c1_cskin_nu049", "hrings_wonky_cmixed_paper", "hrings_c1_cskin_limit",
+          "hrings_c1_cmixed_amortized_pbd", "hrings_wonky_cpixar_post"]
+
+
+@pytest.mark.parametrize("name", HRINGS)
+def test_hex_ring_substeps_bit_exact(orc, name):
+    """The continuous-pressure models on a hex mesh: every vertex's one-ring
+    (its hexes) solved in the fixture's vertex order through the full-energy
+    branch (XPBDFEM/Geo.cpp:147-225, 774-811; XPBDFEM/Fem.cpp:983-1036), the
+    PBD damping over the hexes in the fixture's hex order; and the ring
+    schedule restatement reproduces the vertex order."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[9], a[17]
+    hexes, nv = orc.parse_hexes(g["idx"])
+    rs = orc.ring_schedule(g["nodes"], hexes, morton=1)
+    assert np.array_equal(rs["vert_order"], g["vorder"])
+    assert np.array_equal(rs["colour_vert_begin"], g["colour_vert_begin"])
+    ep, w, fl = orc.hex_init_rest(g["nodes"], hexes, dens)
+    X0 = g["nodes"].astype(np.float64)
+    V0 = np.zeros_like(X0)
+    lm = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.hex_substeps_rings(X0, V0, w, hexes, ep, g["order"], g["vorder"], 1, hex_params(orc, a, g, 0),
+                                           lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.hex_substeps_rings(X1, V1, w1, hexes, ep, g["order"], g["vorder"], nsub - 1,
+                                          hex_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
 
 
 def test_hex_schedule_is_a_valid_colouring(orc):
