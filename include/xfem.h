@@ -32,16 +32,19 @@
  *
  * Meshes of linear hexahedra (tag 8) run in hex mode: GeoLinear3d's hex loops
  * (XPBDFEM/Geo.cpp:736-740, 777-811) with SolveElement on
- * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), every energy model but the
- * continuous-pressure ones (8-10). A mesh holds tets or hexes, not both, and
- * so does a handle.
+ * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), every energy model. With
+ * the continuous-pressure ones (8-10) a hex mesh solves one constraint (pair)
+ * per vertex one-ring over the hexes around it (SolveRing's full-energy
+ * branch, XPBDFEM/Geo.cpp:147-225, XPBDFEM/Fem.cpp:980-1036). A mesh holds
+ * tets or hexes, not both, and so does a handle.
  *
  * A tet mesh whose settings ask for quadratic elements (element type
  * XFEM_ELEMENT_T10 in flags bits 0-3) runs as GeoQuadratic3d
  * (XPBDFEM/Geo.cpp:836-1053, picked by Sim::AddBlock, XPBDFEM/Demo.cpp:145-150):
  * one node added on every edge (Connectivity3d's edge numbering), T10
  * elements (ElementParamsQuadraticTet, SolveElement with Nodes = 10 on the
- * 4-point rule) and the same energy models as hexes. The body's vertices are
+ * 4-point rule) and the energy models of hexes but the continuous-pressure
+ * ones. The body's vertices are
  * then the mesh's own followed by the edge nodes, and every per-vertex call
  * (positions, velocities, lock mask) covers all of them. A handle holds
  * linear tets, hexes or T10s.
@@ -200,7 +203,7 @@ int xfem_settings_default(xfem_settings* s);
  * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
  * element type T10 or H27 (flags bits 0-3) makes a tet mesh a T10 body and a
  * hex mesh an H27 body (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941); a
- * mesh mixing tets and hexes, or an element body with the continuous-pressure
+ * mesh mixing tets and hexes, or a T10 or H27 body with the continuous-pressure
  * models (energy 8-10), returns XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
@@ -351,7 +354,7 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
                           uint32_t* tet_order, uint32_t* colour_begin, uint32_t* ncolours, uint32_t* nclusters);
 /* The ring schedule of the continuous-pressure models (energy 8-10), whose
  * GeoLinear3d::Constrain solves one constraint pair per vertex over the tets
- * around it (XPBDFEM/Geo.cpp:147-193, 784-787; the vertex order vOrder,
+ * (or hexes) around it (XPBDFEM/Geo.cpp:147-225, 784-787; the vertex order vOrder,
  * XPBDFEM/Geo.cpp:759-771, is replaced by it): vertices coloured so that the
  * one-rings of a colour share no vertex, in caller ids, colour-major;
  * colour_begin needs room for vertices + 1 entries. Any output may be NULL.

@@ -46,9 +46,10 @@ class OracleRun:
 
 
 class HexOracleRun:
-    """The oracle's state for one hex body, stepped in the body's hex order."""
+    """The oracle's state for one hex body, stepped in the body's hex order
+    (and with vorder, a continuous-pressure model's ring order)."""
 
-    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32, vorder=None):
         self.hexes, nv = oracle.parse_hexes(idx)
         self.ep, self.w, fl = oracle.hex_init_rest(nodes, self.hexes, density, dtype)
         self.lock = (fl & 3).astype(np.uint8)
@@ -57,10 +58,16 @@ class HexOracleRun:
         self.V = np.zeros_like(self.X)
         self.s = settings
         self.order = order
+        self.vorder = vorder
         self.dtype = dtype
 
     def step(self, n, dt):
         p = oracle_params(self.s, dt, nodes=self.nodes)
+        if self.vorder is not None:
+            self.X, self.V, self.w, _ = oracle.hex_substeps_rings(self.X, self.V, self.w, self.hexes, self.ep, self.order,
+                                                                  self.vorder, n, p, lock_mask=self.lock,
+                                                                  dtype=self.dtype)
+            return self
         self.X, self.V, self.w, _ = oracle.hex_substeps(self.X, self.V, self.w, self.hexes, self.ep, self.order, n, p,
                                                         lock_mask=self.lock, dtype=self.dtype)
         return self

@@ -179,6 +179,27 @@ def test_ring_schedule_bit_exact_vs_oracle(orc, morton, mesh):
     assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])
 
 
+@pytest.mark.parametrize("morton", [True, False])
+def test_hex_ring_schedule_bit_exact_vs_oracle(orc, morton):
+    """The continuous-pressure models on a hex mesh: one-rings over the hexes
+    around each vertex, the same colouring rule; equal to the oracle's
+    restatement and, with Morton order, to the vertex order the reference's
+    own `hrings` fixtures ran in."""
+    nodes, idx = xfem.generate_hex_block(7, 5, 4, (0.1, 0.1, 0.1), 1, 0.3)
+    s = xfem.compute_ring_schedule(nodes, idx, morton=morton)
+    hexes, _ = orc.parse_hexes(idx)
+    o = orc.ring_schedule(nodes, hexes, morton=int(morton))
+    assert s["colours"] == o["colours"]
+    assert np.array_equal(s["vert_order"], o["vert_order"])
+    assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])
+    if morton:
+        for name in ("hrings_c1_cpixar_nu045", "hrings_wonky_cmixed_paper"):
+            g = golden(name)
+            f = xfem.compute_ring_schedule(g["nodes"], g["idx"])
+            assert np.array_equal(f["vert_order"], g["vorder"]), name
+            assert np.array_equal(f["colour_vert_begin"], g["colour_vert_begin"]), name
+
+
 # ---- linear hexahedra: the host side of hex mode ----
 def test_generate_hex_block_bit_exact():
     g = golden("hmeshgen_3x2x2_mirror_wonky")

@@ -76,6 +76,7 @@ struct BodyHost {
 	std::vector<uint32_t> quads;      // H27: the four corners of each face node
 	std::vector<float> eep;           // rest::kHexRec per hex, rest::kT10Rec per T10, rest::kH27Rec per H27
 	ElemSchedule esched;
+	std::vector<uint32_t> el_dev;     // hexes, T10s, H27s: each element's device index (build_elements)
 };
 
 template <typename T>
@@ -247,6 +248,7 @@ BodyParams make_params(const xfem_settings& s) {
 	p.drag_mul = 1.0f - s.time_corrected_drag;
 	p.lock_active = (s.flags & XFEM_LOCK_LEFT) ? 1u : 0u;
 	p.lock_right = (s.flags & XFEM_LOCK_RIGHT) ? 1u : 0u;
+	p.a_ring = p.energy == 8u ? 1.0f + (1.0f - 2.0f * nu) : 1.0f / (2.0f * nu);
 	p.ground = s.ground ? 1u : 0u;
 	p.friction = s.friction;
 	for (int k = 0; k < 3; k++) p.ground_n[k] = s.ground_normal[k];
@@ -543,9 +545,9 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	if (b.el == kElHexes || quad) {
 		// hexes, T10s and H27s: set-up on the host (rest state, Morton vertex
 		// ranks, the element colouring)
-		if (energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
+		if (ring && quad)
 			return fail(XFEM_EUNSUPPORTED,
-			            "hex, T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
+			            "T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
 		if (quad && b.el == kElHexes)
 			prepare_h27(m, b);
 		else if (quad)
@@ -555,6 +557,15 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
 		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, nodes_per_element(b.el), morton, b.esched))
 			return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+		if (ring) {
+			// the continuous-pressure models on hexes: one-rings over the hexes
+			std::vector<uint32_t> off, lst;
+			incidence(b.elems.data(), b.nv, b.nh, off, lst, 8);
+			const int rc2 =
+			    build_ring_schedule(b.elems.data(), b.nv, off.data(), lst.data(), b.sched.vert_rank.data(), b.rings, 8);
+			if (rc2 == -2) return fail(XFEM_ELIMIT, "a vertex one-ring has more than 16 hexes or 32 vertices");
+			if (rc2) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
+		}
 		return XFEM_OK;
 	}
 	std::vector<uint32_t> off, lst;
@@ -686,25 +697,38 @@ int build_rings(xfem_body* h) {
 			for (uint32_t i = rs.colour_begin[c]; i < rs.colour_begin[c + 1]; i++) {
 				const uint32_t v = rs.order[i];
 				const uint32_t nn = rs.node_off[v + 1] - rs.node_off[v], nt = rs.tet_off[v + 1] - rs.tet_off[v];
+				const uint32_t npe = rs.npe, sh = npe == 8 ? 3u : 2u;
 				hdr.push_back(make_uint4((uint32_t)node.size(), (uint32_t)(ent.size() / 2), nn | (nt << 8) | (bi << 16), i));
 				for (uint32_t n = rs.node_off[v]; n < rs.node_off[v + 1]; n++)
 					node.push_back(b.vbase + b.sched.vert_rank[rs.nodes[n]]);
 				for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++) {
+					if (npe == 8) {
+						// a hex: its device element index and its 8 corners' node indices
+						uint32_t lo = 0, hi = 0;
+						for (int k = 0; k < 4; k++) lo |= (uint32_t)rs.corner[8 * (size_t)j + k] << (8 * k);
+						for (int k = 0; k < 4; k++) hi |= (uint32_t)rs.corner[8 * (size_t)j + 4 + k] << (8 * k);
+						const float4 f = make_float4(__builtin_bit_cast(float, b.el_dev[rs.tets[j]]),
+						                             __builtin_bit_cast(float, lo), __builtin_bit_cast(float, hi), 0.0f);
+						ent.push_back(f);
+						ent.push_back(f);
+						continue;
+					}
 					const float* e = &b.ep[17 * (size_t)rs.tets[j]];
 					uint32_t cn = 0;
 					for (int k = 0; k < 4; k++) cn |= (uint32_t)rs.corner[4 * (size_t)j + k] << (8 * k);
 					ent.push_back(make_float4(e[9], e[10], e[11], e[12]));
 					ent.push_back(make_float4(e[13], e[14], e[15], __builtin_bit_cast(float, cn)));
 				}
-				// each node's corners (local tet << 2 | corner), in tet order
+				// each node's corners (local element << 2 (tets) or << 3 (hexes) | corner), in element order
 				clist.push_back((uint32_t)cwords.size());
 				const size_t ob = cwords.size();
 				cwords.resize(ob + nn + 1);
 				for (uint32_t n = 0; n < nn; n++) {
 					cwords[ob + n] = (uint16_t)(cwords.size() - ob - (nn + 1));
 					for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++)
-						for (int k = 0; k < 4; k++)
-							if (rs.corner[4 * (size_t)j + k] == n) cwords.push_back((uint16_t)(((j - rs.tet_off[v]) << 2) | k));
+						for (uint32_t k = 0; k < npe; k++)
+							if (rs.corner[npe * (size_t)j + k] == n)
+								cwords.push_back((uint16_t)(((j - rs.tet_off[v]) << sh) | k));
 				}
 				cwords[ob + nn] = (uint16_t)(cwords.size() - ob - (nn + 1));
 			}
@@ -787,13 +811,15 @@ int build_elements(xfem_body* h) {
 	std::vector<uint32_t> cb(ncol + 1, 0), flat(nel);
 	std::vector<float4> rec(nrec4 * (size_t)nel);
 	uint32_t o = 0;
+	for (BodyHost& b : h->bodies) b.el_dev.assign(b.nh, 0);
 	for (uint32_t c = 0; c < ncol; c++) {
 		cb[c] = o;
-		for (const BodyHost& b : h->bodies) {
+		for (BodyHost& b : h->bodies) {
 			const ElemSchedule& es = b.esched;
 			if (c >= es.ncolours) continue;
 			for (uint32_t k = es.colour_begin[c]; k < es.colour_begin[c + 1]; k++, o++) {
 				const uint32_t el = es.order[k];
+				b.el_dev[el] = o;
 				uint32_t d[28] = {0};
 				for (uint32_t n = 0; n < per; n++) d[n] = b.vbase + b.sched.vert_rank[b.elems[per * (size_t)el + n]];
 				for (uint32_t j = 0; j < nvid4; j++)
@@ -1172,12 +1198,12 @@ int build_device(xfem_body* h) {
 		h->device_bytes += (uint64_t)trows * kLanes * 8 + 4;
 		h->device_bytes += (uint64_t)ntets * 16 + h->io.n * 4;
 	}
-	if (h->ring_mode) {
-		int rr = build_rings(h);
+	if (h->el_mode) {  // before the rings: a hex ring addresses its hexes by device index
+		int rr = build_elements(h);
 		if (rr) return rr;
 	}
-	if (h->el_mode) {
-		int rr = build_elements(h);
+	if (h->ring_mode) {
+		int rr = build_rings(h);
 		if (rr) return rr;
 	}
 	DevCtx& c = h->ctx;
@@ -1419,7 +1445,8 @@ BodyHost* body_of(xfem_body* h, uint32_t body) {
 // The element and one-ring launches (no autotuner, no CUDA graph).
 int launch_mode(xfem_body* h, const DevCtx& ctx, uint32_t nsub, float dt) {
 	if (h->ring_mode) {
-		const int e = launch_rings(ctx, 256, nsub, dt, h->stream);
+		const int e = h->el_mode == kElHexes ? launch_hex_rings(ctx, 256, nsub, dt, h->stream)
+		                                     : launch_rings(ctx, 256, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
@@ -1582,9 +1609,9 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	int rc = validate_settings(*s);
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (h->el_mode && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
-		return fail(XFEM_EUNSUPPORTED,
-		            "hex, T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
+	if ((b->el == kElT10 || b->el == kElH27) && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR &&
+	    energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
+		return fail(XFEM_EUNSUPPORTED, "T10 and H27 meshes run every energy model but the continuous-pressure ones (8-10)");
 	if (quadratic_type(s->flags) != (b->el == kElT10 || b->el == kElH27))
 		return fail(XFEM_EUNSUPPORTED, "switching between linear and quadratic elements (flags bits 0-3) needs a new handle");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)
@@ -1965,11 +1992,16 @@ int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count,
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
 	int rc = prepare_mesh(m, b);
 	if (rc) return rc;
+	// a tet stream (tag 4) or a hex stream (tag 8): rings over its elements
+	const bool hex = b.el == kElHexes;
+	const uint32_t* el = hex ? b.elems.data() : b.tets.data();
 	std::vector<uint32_t> off, lst;
-	incidence(b.tets.data(), b.nv, b.nt, off, lst);
+	incidence(el, b.nv, hex ? b.nh : b.nt, off, lst, hex ? 8u : 4u);
 	vertex_ranks(b.nodes.data(), b.nv, no_morton ? 0u : 1u, b.sched);
-	rc = build_ring_schedule(b.tets.data(), b.nv, off.data(), lst.data(), b.sched.vert_rank.data(), b.rings);
-	if (rc == -2) return fail(XFEM_ELIMIT, "a vertex one-ring has more than 64 tets or 32 vertices");
+	rc = build_ring_schedule(el, b.nv, off.data(), lst.data(), b.sched.vert_rank.data(), b.rings, hex ? 8u : 4u);
+	if (rc == -2)
+		return fail(XFEM_ELIMIT, hex ? "a vertex one-ring has more than 16 hexes or 32 vertices"
+		                             : "a vertex one-ring has more than 64 tets or 32 vertices");
 	if (rc) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
 	return ring_schedule_out(b.rings, vert_order, colour_begin, ncolours);
 }

@@ -167,14 +167,14 @@ bool tet_has(const uint32_t* tv, uint32_t v) { return tv[0] == v || tv[1] == v |
 //  5. inside a colour, clusters by (Morton code of their centroid, id), or
 //     (smallest vertex id, id) without Morton order.
 void incidence(const uint32_t* tets, uint32_t nverts, uint32_t ntets, std::vector<uint32_t>& off,
-               std::vector<uint32_t>& lst) {
+               std::vector<uint32_t>& lst, uint32_t npe) {
 	off.assign(nverts + 1, 0);
-	lst.resize(4 * (size_t)ntets);
-	for (size_t i = 0; i < 4 * (size_t)ntets; i++) off[tets[i] + 1]++;
+	lst.resize(npe * (size_t)ntets);
+	for (size_t i = 0; i < npe * (size_t)ntets; i++) off[tets[i] + 1]++;
 	for (uint32_t v = 0; v < nverts; v++) off[v + 1] += off[v];
 	std::vector<uint32_t> fill(off.begin(), off.end() - 1);
 	for (uint32_t t = 0; t < ntets; t++)
-		for (int n = 0; n < 4; n++) lst[fill[tets[4 * (size_t)t + n]]++] = t;
+		for (uint32_t n = 0; n < npe; n++) lst[fill[tets[npe * (size_t)t + n]]++] = t;
 }
 
 int cluster_and_colour(const uint32_t* tets, uint32_t ntets, const uint32_t* off, const uint32_t* lst, uint32_t mode,
@@ -308,24 +308,26 @@ void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 }
 
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
-                        const uint32_t* vert_rank, RingSchedule& rs) {
+                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe) {
 	const uint32_t kNone = 0xffffffffu;
+	const uint32_t max_elems = npe == 8 ? kMaxRingHexes : kMaxRingTets;
+	rs.npe = npe;
 	rs.tet_off.assign(off, off + nverts + 1);
 	rs.tets.assign(lst, lst + off[nverts]);
 	rs.node_off.assign(nverts + 1, 0);
 	rs.nodes.clear();
-	rs.corner.assign(off[nverts] * 4u, 0);
+	rs.corner.assign(off[nverts] * npe, 0);
 	for (uint32_t v = 0; v < nverts; v++) {
 		rs.node_off[v] = (uint32_t)rs.nodes.size();
-		if (off[v + 1] - off[v] > kMaxRingTets) return -2;
+		if (off[v + 1] - off[v] > max_elems) return -2;
 		uint32_t nodes[4 * kMaxRingTets + 1], cnt = 1;
 		nodes[0] = v;
 		for (uint32_t j = off[v]; j < off[v + 1]; j++) {
-			const uint32_t* tv = tets + 4 * (size_t)lst[j];
-			for (int n = 0; n < 4; n++) {
+			const uint32_t* tv = tets + npe * (size_t)lst[j];
+			for (uint32_t n = 0; n < npe; n++) {
 				const uint32_t k = (uint32_t)(std::find(nodes, nodes + cnt, tv[n]) - nodes);
 				if (k == cnt) nodes[cnt++] = tv[n];
-				rs.corner[4 * (size_t)j + n] = (uint8_t)k;
+				rs.corner[npe * (size_t)j + n] = (uint8_t)k;
 			}
 		}
 		if (cnt > kMaxRingNodes) return -2;

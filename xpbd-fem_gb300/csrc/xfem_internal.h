@@ -52,7 +52,7 @@ int build_schedule(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
                    uint32_t morton, Schedule& s);
 // vertex -> tets in increasing tet id (CSR: off[nverts + 1], lst[4 ntets])
 void incidence(const uint32_t* tets, uint32_t nverts, uint32_t ntets, std::vector<uint32_t>& off,
-               std::vector<uint32_t>& lst);
+               std::vector<uint32_t>& lst, uint32_t npe = 4);
 // the greedy clusters and colours in tet / cluster id order (sequential by
 // definition); fills nclusters, cl_begin, cl_tets, cl_colour, ncolours
 int cluster_and_colour(const uint32_t* tets, uint32_t ntets, const uint32_t* off, const uint32_t* lst, uint32_t mode,
@@ -72,15 +72,16 @@ struct RingSchedule {
 	uint32_t ncolours = 0;
 	std::vector<uint32_t> tet_off, tets;    // the incidence: nverts + 1 offsets; tet ids
 	std::vector<uint32_t> node_off, nodes;  // nverts + 1 offsets; caller vertex ids
-	std::vector<uint8_t> corner;            // 4 per incidence entry: node index of each tet corner
+	uint32_t npe = 4;                       // vertices per element: 4 (tets) or 8 (hexes)
+	std::vector<uint8_t> corner;            // npe per incidence entry: node index of each element corner
 	std::vector<uint32_t> order;            // vertices in ring order, colour-major
 	std::vector<uint32_t> colour_begin;     // ncolours + 1, into order
 };
 // off / lst: the incidence (vertex -> tets in increasing id); vert_rank: the
 // vertex ranks. Returns 0, -1 when the colour limit is exceeded, -2 when a
-// ring has more than kMaxRingTets tets or kMaxRingNodes vertices.
+// ring has more than kMaxRingTets tets (kMaxRingHexes hexes) or kMaxRingNodes vertices.
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
-                        const uint32_t* vert_rank, RingSchedule& rs);
+                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe = 4);
 
 // Linear hexahedra (H8). The tagged index stream with tag 8 (8 vertex ids
 // per hex); -1 on another tag or a truncated record.
@@ -193,7 +194,8 @@ struct BodyParams {
 	uint32_t nverts;          // vertices of the body (amortized ring damping slices)
 	uint32_t cube_fast;       // SolveElementCube's short path on hexes: CubeNeo, nu >= 0.5, no damping
 	uint32_t lock_right;      // Settings_LockRight: hold the Right vertices at DevCtx::right_target
-	uint32_t pad4;
+	float a_ring;             // the continuous-pressure models' (J - a)^2 on hexes: a = 1 + (1 - 2 nu)
+	                          // (ContinuousPixar) or 1 / (2 nu) (XPBDFEM/Fem.cpp:1016)
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
@@ -212,6 +214,7 @@ constexpr uint32_t kModelRing = 5;      // ContinuousPixar (8), ContinuousMixed 
                                         // one constraint (pair) per vertex one-ring, not per tet
 constexpr uint32_t kMaxRingNodes = 32;  // vertices of a one-ring (one warp lane each)
 constexpr uint32_t kMaxRingTets = 64;   // tets of a one-ring (two per warp lane)
+constexpr uint32_t kMaxRingHexes = 16;  // hexes of a one-ring on a hex mesh (one per warp lane)
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
@@ -414,6 +417,10 @@ int launch_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* st
 // Hex mode (xfem_hexes.cu): nsub substeps of a hex mesh, a cooperative
 // persistent launch (canonical (X, V) in and out).
 int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// The continuous-pressure models on a hex mesh (xfem_hexes.cu): nsub
+// substeps of one-ring solves over the hexes, a cooperative persistent
+// launch (canonical (X, V) in and out).
+int launch_hex_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-tet mode (xfem_t10.cu): nsub substeps of a T10 mesh, likewise.
 int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp

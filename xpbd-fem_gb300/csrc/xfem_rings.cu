@@ -20,6 +20,7 @@
 
 #include "xfem_device.cuh"
 #include "xfem_internal.h"
+#include "xfem_ring_update.cuh"
 
 namespace xfem {
 
@@ -31,12 +32,6 @@ struct RingScratch {
 	float g0[kMaxRingTets][4][3];               // per tet corner: I1 gradient contribution
 	float g1[kMaxRingTets][4][3];               // per tet corner: J gradient contribution
 };
-
-__device__ __forceinline__ float warp_sum(float x) {
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-	return x;
-}
 
 // SolveRing of ring r by the calling warp (every lane takes part). VMODE:
 // the post-step Rayleigh damping form (SolveRing with V, XPBDFEM/Geo.cpp:
@@ -129,8 +124,6 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 		w = S.O[lane].w;
 		Dn = S.D[lane];
 	}
-	const float damp = DAMP && __ldg(&bp.rayleigh_type) < 2u ? __ldg(&bp.damping) : 0.0f;
-	const bool limit = __ldg(&bp.rayleigh_type) == 1u;
 	if (__ldg(&bp.energy) == 8u) {
 		// ContinuousPixar: mu = 2, one constraint U = I1 + (lambda/2)(J - a)^2
 		// with compliance per the ring volume
@@ -138,41 +131,8 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 		const float U = fmaxf(0.0000001f, fmaf(hw * (J - a), J - a, I1));
 		const float s1 = 2.0f * hw * (J - a);
 		const Vec3 g = {fmaf(s1, g1.x, g0.x), fmaf(s1, g1.y, g0.y), fmaf(s1, g1.z, g0.z)};
-		const float comp = __ldg(&bp.compliance) / volume;
-		const float alpha = comp * inv_dt2;
-		const float wgg = 1.0e-22f + warp_sum(w * dot(g, g));
-		if constexpr (VMODE) {
-			const float gV = warp_sum(lane < nn ? dot(g, v3(Dn)) : 0.0f);
-			const float l = -gV / fmaf(2.0f * U, comp * inv_dt / rd, wgg);
-			if (lane < nn) {
-				const float sc = w * l;
-				Dn.x = fmaf(sc, g.x, Dn.x);
-				Dn.y = fmaf(sc, g.y, Dn.y);
-				Dn.z = fmaf(sc, g.z, Dn.z);
-				st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
-			}
-			return;
-		}
-		float l = (-2.0f * U) / fmaf(2.0f * U, alpha, wgg);
-		if constexpr (DAMP) {
-			const float gV = warp_sum(lane < nn ? dot(g, v3(Dn)) : 0.0f);
-			const float gamma = damp * inv_dt;
-			if (!(damp > 0.0f)) {
-			} else if (!limit) {
-				l = (-2.0f * U - gamma * gV) / fmaf(wgg, 1.0f + gamma, 2.0f * U * alpha);
-			} else {
-				const float A = fmaf(2.0f * U, comp * inv_dt / damp, wgg);
-				const float b = (-gV - wgg * l) * (A / fmaxf(A, 4.0f * wgg));
-				l += b / A;
-			}
-		}
-		if (lane < nn) {
-			const float sc = w * l;
-			Dn.x = fmaf(sc, g.x, Dn.x);
-			Dn.y = fmaf(sc, g.y, Dn.y);
-			Dn.z = fmaf(sc, g.z, Dn.z);
-			st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
-		}
+		ring_update1<DAMP, VMODE>(C, bp, lane, nn, dv, S.O[lane], Dn, w, g, U, __ldg(&bp.compliance) / volume, inv_dt,
+		                          inv_dt2, rd);
 		return;
 	}
 	// ContinuousMixed / ContinuousSkin: the deviatoric and hydrostatic pair
@@ -188,62 +148,8 @@ __device__ __noinline__ void ring_solve(const DevCtx& C, RingScratch& S, uint32_
 	const float U1 = (J - a) * (J - a);
 	const float gs1 = 2.0f * (J - a);
 	g1 = {g1.x * gs1, g1.y * gs1, g1.z * gs1};
-	const float comp0 = 1.0f / (mu * volume), comp1 = 1.0f / (lambda * volume);
-	const float alpha0 = comp0 * inv_dt2, alpha1 = comp1 * inv_dt2;
-	const float wgg0 = 1.0e-22f + warp_sum(w * dot(g0, g0));
-	const float wgg1 = 1.0e-22f + warp_sum(w * dot(g1, g0));
-	const float wgg2 = 1.0e-22f + warp_sum(w * dot(g1, g1));
-	float l0, l1;
-	if constexpr (VMODE) {
-		const float b0 = -warp_sum(lane < nn ? dot(g0, v3(Dn)) : 0.0f);
-		const float b1 = -warp_sum(lane < nn ? dot(g1, v3(Dn)) : 0.0f);
-		cramer(fmaf(2.0f * U0, comp0 * inv_dt / rd, wgg0), wgg1, fmaf(2.0f * U1, comp1 * inv_dt / rd, wgg2), b0, b1, l0,
-		       l1);
-		if (lane < nn) {
-			Dn.x = fmaf(w, fmaf(l1, g1.x, l0 * g0.x), Dn.x);
-			Dn.y = fmaf(w, fmaf(l1, g1.y, l0 * g0.y), Dn.y);
-			Dn.z = fmaf(w, fmaf(l1, g1.z, l0 * g0.z), Dn.z);
-			st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
-		}
-		return;
-	}
-	cramer(fmaf(2.0f * U0, alpha0, wgg0), wgg1, fmaf(2.0f * U1, alpha1, wgg2), -2.0f * U0, -2.0f * U1, l0, l1);
-	if constexpr (DAMP) {
-		// warp-uniform: one body per ring
-		if (damp > 0.0f) {
-			const float gV0 = warp_sum(lane < nn ? dot(g0, v3(Dn)) : 0.0f);
-			const float gV1 = warp_sum(lane < nn ? dot(g1, v3(Dn)) : 0.0f);
-			const float gamma = damp * inv_dt;
-			float A0, A2, b0 = -2.0f * U0, b1 = -2.0f * U1;
-			if (!limit) {
-				const float s = 1.0f / (1.0f + gamma);
-				A0 = wgg0 + (2.0f * U0 * alpha0) * s;
-				A2 = wgg2 + (2.0f * U1 * alpha1) * s;
-				b0 = (b0 - gamma * gV0) * s;
-				b1 = (b1 - gamma * gV1) * s;
-			} else {
-				A0 = fmaf(2.0f * U0, alpha0, wgg0);
-				A2 = fmaf(2.0f * U1, alpha1, wgg2);
-			}
-			cramer(A0, wgg1, A2, b0, b1, l0, l1);
-			if (limit) {
-				const float B0 = fmaf(2.0f * U0, comp0 * inv_dt / damp, wgg0), B2 = fmaf(2.0f * U1, comp1 * inv_dt / damp, wgg2);
-				float e0 = fmaf(b0, -1.0f - alpha0 * l0, -gV0), e1 = fmaf(b1, -1.0f - alpha1 * l1, -gV1);
-				e0 *= B0 / fmaxf(B0, 8.0f * wgg0);
-				e1 *= B2 / fmaxf(B2, 8.0f * wgg2);
-				float d0, d1;
-				cramer(B0, wgg1, B2, e0, e1, d0, d1);
-				l0 += d0;
-				l1 += d1;
-			}
-		}
-	}
-	if (lane < nn) {
-		Dn.x = fmaf(w, fmaf(l1, g1.x, l0 * g0.x), Dn.x);
-		Dn.y = fmaf(w, fmaf(l1, g1.y, l0 * g0.y), Dn.y);
-		Dn.z = fmaf(w, fmaf(l1, g1.z, l0 * g0.z), Dn.z);
-		st_vertex(C.vert + 2 * (size_t)dv, S.O[lane], Dn);
-	}
+	ring_update2<DAMP, VMODE>(C, bp, lane, nn, dv, S.O[lane], Dn, w, g0, g1, U0, U1, 1.0f / (mu * volume),
+	                          1.0f / (lambda * volume), inv_dt, inv_dt2, rd);
 }
 
 // PBD damping of one tet cluster (its tets in sequence; clusters of one
