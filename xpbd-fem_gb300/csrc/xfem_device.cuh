@@ -598,13 +598,19 @@ struct Stage {
 	uint64_t* mbar;
 	uint32_t parity;
 	int inflight;     // chunk whose copy is in flight or resident, -1 = none
+	uint4 meta;       // that chunk's descriptor (DevCtx::chunks)
 };
 
-__device__ __forceinline__ void stage_issue(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
-	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+// Starts the copy of `chunk`, whose descriptor m the caller has loaded.
+__device__ __forceinline__ void stage_issue_m(const DevCtx& C, Stage& st, uint32_t chunk, const uint4& m, uint32_t lane) {
 	__syncwarp();
 	if (lane == 0) bulk_copy_g2s(st.buf, C.cblk + m.x, m.y, st.mbar);
 	st.inflight = (int)chunk;
+	st.meta = m;
+}
+
+__device__ __forceinline__ void stage_issue(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	stage_issue_m(C, st, chunk, __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk), lane);
 }
 
 // Starts the copy of `chunk` when the buffer is idle (dataflow mode issues it
@@ -650,7 +656,7 @@ __device__ __forceinline__ Stage stage_init(const DevCtx& C, uint32_t lane) {
 	__shared__ uint64_t mbars[32];
 	const uint32_t w = threadIdx.x >> 5;
 	uint8_t* base = smem + (size_t)w * C.warp_smem;
-	Stage st = {base, reinterpret_cast<float4*>(base + C.vs_off), &mbars[w], 0u, -1};
+	Stage st = {base, reinterpret_cast<float4*>(base + C.vs_off), &mbars[w], 0u, -1, make_uint4(0u, 0u, 0u, 0u)};
 	if (lane == 0) mbar_init(st.mbar);
 	__syncwarp();
 	return st;

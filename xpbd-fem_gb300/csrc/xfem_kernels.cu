@@ -167,9 +167,9 @@ __device__ __forceinline__ DampTet damp_of(const DevCtx& C, const BodyParams& bp
 // the lowest-colour cluster touching it, just before that cluster's solve.
 
 template <bool LAMBDAS, bool TAPE, bool EXT>
-__device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first, float dt,
-                                               float inv_dt, float inv_dt2, uint32_t trow, uint32_t s_launch,
-                                               uint32_t chunk, bool finish_last) {
+__device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int next, const uint4& mnext, uint32_t lane,
+                                               bool first, float dt, float inv_dt, float inv_dt2, uint32_t trow,
+                                               uint32_t s_launch, uint32_t chunk, bool finish_last) {
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
 	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
 	const uint32_t* vids = hdrs + kLanes;
@@ -206,17 +206,21 @@ __device__ __forceinline__ void run_chunk_cube(const DevCtx& C, Stage& st, int n
 			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
 		}
 	}
-	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
+	if (next >= 0) stage_issue_m(C, st, (uint32_t)next, mnext, lane);  // buffer consumed: prefetch
 	if (live) {
 		// with damping sweeps, the vertex's last solve of the substep finishes
 		// it (to the canonical X, V that the sweeps work on)
 		const uint32_t last = fin ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
-		// the whole 32-byte state: O is unchanged unless this cluster advanced
-		// or finished the vertex, and no other cluster of the pass touches it
+		// O changes only where this cluster advanced or finished the vertex
+		// (then the whole 32-byte state is stored); no other cluster of the
+		// pass touches these vertices
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
 			if (EXT && (last & (1u << s))) finalize_vertex(C, vid[s], O[s], D[s], inv_dt);
-			st_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
+			if ((mask | last) & (1u << s))
+				st_vertex(C.vert + 2 * (size_t)vid[s], O[s], D[s]);
+			else  // only D moved: a 16-byte store
+				__stcg(C.vert + 2 * (size_t)vid[s] + 1, D[s]);
 		}
 	}
 }
@@ -228,10 +232,13 @@ template <bool LAMBDAS, bool TAPE = false, bool EXT = false>
 __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t chunk, int next, uint32_t lane, bool first,
                                           float dt, float inv_dt, float inv_dt2, uint32_t s_launch = 0,
                                           bool finish_last = false) {
-	const uint4 m = __ldg(reinterpret_cast<const uint4*>(C.chunks) + chunk);
+	// the staged chunk's descriptor came with its copy; the next one's is
+	// loaded now, off the critical path of the prefetch
+	const uint4 m = st.meta;
+	const uint4 mnext = next >= 0 ? __ldg(reinterpret_cast<const uint4*>(C.chunks) + next) : make_uint4(0u, 0u, 0u, 0u);
 	const uint32_t ntmax = m.z & 0xffu, nvmax = (m.z >> 8) & 0xffu, trow = m.w;
 	if (m.z & kShapeCube) {
-		run_chunk_cube<LAMBDAS, TAPE, EXT>(C, st, next, lane, first, dt, inv_dt, inv_dt2, trow, s_launch, chunk,
+		run_chunk_cube<LAMBDAS, TAPE, EXT>(C, st, next, mnext, lane, first, dt, inv_dt, inv_dt2, trow, s_launch, chunk,
 		                                    finish_last);
 		return;
 	}
@@ -281,7 +288,7 @@ __device__ __forceinline__ void run_chunk(const DevCtx& C, Stage& st, uint32_t c
 			if (LAMBDAS) C.tlam[(size_t)(trow + t) * kLanes + lane] = lam;
 		}
 	}
-	if (next >= 0) stage_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
+	if (next >= 0) stage_issue_m(C, st, (uint32_t)next, mnext, lane);  // buffer consumed: prefetch
 	if (nv) {
 		const uint32_t last = fin ? __ldg(C.lastmask + (size_t)chunk * kLanes + lane) : 0u;
 #pragma unroll
@@ -529,8 +536,10 @@ __device__ __forceinline__ bool pass_runs(const DevCtx& C, uint32_t q, uint32_t 
 // else its first chunk of the following passes that run (wrapping into the
 // next substep); -1 when the launch has no more work for it.
 __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t nsub, uint32_t q, uint32_t P,
-                                          uint32_t ch, uint32_t gwarp, uint32_t nwarps, uint32_t tick0 = 0) {
-	if (ch + nwarps < __ldg(C.colour_chunk_begin + q % C.ncolours + 1)) return (int)(ch + nwarps);
+                                          uint32_t ch, uint32_t gwarp, uint32_t nwarps, uint32_t tick0 = 0,
+                                          const uint32_t* ccb = nullptr) {
+	if (!ccb) ccb = C.colour_chunk_begin;
+	if (ch + nwarps < ccb[q % C.ncolours + 1]) return (int)(ch + nwarps);
 	for (uint32_t k = 1; k <= P; k++) {
 		uint32_t q2 = q + k, s2 = s;
 		if (q2 >= P) {
@@ -540,8 +549,8 @@ __device__ __forceinline__ int next_chunk(const DevCtx& C, uint32_t s, uint32_t 
 		if (s2 >= nsub) return -1;
 		if (P > C.ncolours && !pass_runs(C, q2, tick0 + s2)) continue;
 		const uint32_t c2 = q2 % C.ncolours;
-		const uint32_t first = __ldg(C.colour_chunk_begin + c2) + gwarp;
-		if (first < __ldg(C.colour_chunk_begin + c2 + 1)) return (int)first;
+		const uint32_t first = ccb[c2] + gwarp;
+		if (first < ccb[c2 + 1]) return (int)first;
 	}
 	return -1;
 }
@@ -566,6 +575,14 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 	const uint32_t P = (EXT ? pass_kinds(C) : 1u) * C.ncolours;
 	const uint32_t tick0 = __ldcg(C.tick);  // read before the first barrier; block 0 advances it at the end
 	Stage st = stage_init(C, lane);
+	// the colour table in shared memory (up to 64 colours): read after every
+	// barrier, a global load there would sit on each pass's critical path
+	__shared__ uint32_t s_ccb[65];
+	const bool ccb_sh = C.ncolours <= 64u;
+	if (ccb_sh)
+		for (uint32_t i = threadIdx.x; i <= C.ncolours; i += blockDim.x) s_ccb[i] = __ldg(C.colour_chunk_begin + i);
+	__syncthreads();
+	const uint32_t* ccb = ccb_sh ? s_ccb : C.colour_chunk_begin;
 	run_isolated<TAPE>(C, gtid, nthreads, nsub, dt, inv_dt, dmode);
 	uint32_t target = C.bar_base;
 	bool ok = true;
@@ -575,13 +592,13 @@ __global__ void __launch_bounds__(256) k_persistent(DevCtx C, uint32_t nsub, flo
 			// a damping pass with nothing to damp at this tick is skipped by
 			// every block alike (same table, same tick): no work, no barrier
 			if (EXT && kind > 0 && !pass_runs(C, q, tick0 + s)) continue;
-			const uint32_t cb = __ldg(C.colour_chunk_begin + c), ce = __ldg(C.colour_chunk_begin + c + 1);
+			const uint32_t cb = ccb[c], ce = ccb[c + 1];
 			for (uint32_t ch = cb + gwarp; ch < ce; ch += nwarps) {
 				if (!stage_acquire(C, st, ch, lane)) {
 					ok = false;
 					break;
 				}
-				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps, tick0);
+				const int next = next_chunk(C, s, nsub, q, P, ch, gwarp, nwarps, tick0, ccb);
 				if (!EXT || kind == 0)
 					run_chunk<LAMBDAS, TAPE, EXT>(C, st, ch, next, lane, dmode || s == 0, dt, inv_dt, inv_dt2, s,
 					                               dmode);
