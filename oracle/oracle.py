@@ -173,6 +173,16 @@ def lib():
         L.orc_hex_volume_d.argtypes = [P, u32, P, P]
         L.orc_hex_volume_d.restype = C.c_double
         L.orc_hex_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.orc_parse_mixed.argtypes = [P, u32, P, P, P, P, P]
+        L.orc_elem_schedule.argtypes = [P, u32, P, u32, u32, u32, P, P, P, P]
+        L.orc_mixed_init_rest_f.argtypes = [P, u32, P, u32, P, u32, C.c_float, P, P, P, P]
+        L.orc_mixed_init_rest_d.argtypes = [P, u32, P, u32, P, u32, C.c_double, P, P, P, P]
+        L.orc_mixed_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_mixed_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_mixed_volume_f.argtypes = [P, u32, P, u32, P, P]
+        L.orc_mixed_volume_f.restype = C.c_float
+        L.orc_mixed_volume_d.argtypes = [P, u32, P, u32, P, P]
+        L.orc_mixed_volume_d.restype = C.c_double
         L.orc_t10_tables.argtypes = [P, P, P]
         L.orc_tet_edges.argtypes = [P, u32, u32, P, P, P]
         L.orc_t10_init_rest_f.argtypes = [P, u32, P, u32, P, u32, P, C.c_float, P, P, P, P]
@@ -490,6 +500,104 @@ def hex_schedule(nodes, hexes, morton=1):
     if lib().orc_hex_schedule(_p(nodes), nv, _p(hexes), nh, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
         raise ValueError("hex schedule needs more than 4096 colours")
     return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+# ---- meshes mixing tets and hexes (oracle/xfem_oracle_mixed.inc) ----
+def parse_mixed(idx):
+    """(tets[nt, 4], hexes[nh, 8], vertex count) of a tagged stream of tets
+    and hexes, each kind in stream order."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    nt, nh, nv = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    if lib().orc_parse_mixed(_p(idx), idx.size, None, C.byref(nt), None, C.byref(nh), C.byref(nv)):
+        raise ValueError("index stream holds an element that is neither a tet nor a hex")
+    tets = np.zeros((nt.value, 4), np.uint32)
+    hexes = np.zeros((nh.value, 8), np.uint32)
+    lib().orc_parse_mixed(_p(idx), idx.size, _p(tets), C.byref(nt), _p(hexes), C.byref(nh), C.byref(nv))
+    return tets, hexes, nv.value
+
+
+def tet_element_schedule(nodes, tets, morton=1):
+    """The tets of a mixed mesh coloured and ordered as hexes are: tet order
+    (colour-major), colour offsets, vertex ranks."""
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    nv, nt = nodes.size // 3, tets.shape[0]
+    rank = np.zeros(nv, np.uint32)
+    order = np.zeros(nt, np.uint32)
+    cb = np.zeros(nt + 1, np.uint32)
+    ncol = C.c_uint32()
+    if lib().orc_elem_schedule(_p(nodes), nv, _p(tets), nt, 4, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
+        raise ValueError("tet schedule needs more than 4096 colours")
+    return dict(vert_rank=rank, tet_order=order, colour_tet_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+def mixed_init_rest(nodes, tets, hexes, density, dtype=np.float32):
+    """GeoLinear3d::Init on a mixed mesh: (tet records, hex records, w, flags)."""
+    nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    nv, nt, nh = nodes.size // 3, tets.shape[0], hexes.shape[0]
+    ep = np.zeros((nt, 17), dtype)
+    hep = np.zeros((nh, HEX_EP), dtype)
+    w = np.zeros(nv, dtype)
+    fl = np.zeros(nv, np.uint8)
+    f = lib().orc_mixed_init_rest_f if dtype == np.float32 else lib().orc_mixed_init_rest_d
+    f(_p(nodes), nv, _p(tets), nt, _p(hexes), nh, density, _p(ep), _p(hep), _p(w), _p(fl))
+    return ep, hep, w, fl
+
+
+def mixed_substeps(X, V, w, tets, ep, torder, hexes, hep, horder, nsub, params, lock_mask=None, dtype=np.float32):
+    """nsub substeps of a mixed mesh (tets in torder, then hexes in horder).
+    Returns X, V, w, contact mask."""
+    X = np.array(X, np.float64).reshape(-1).copy()
+    V = np.array(V, np.float64).reshape(-1).copy()
+    w = np.array(w, dtype).copy()
+    nv = w.size
+    tets = np.ascontiguousarray(tets, np.uint32)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    ep = np.ascontiguousarray(ep, dtype)
+    hep = np.ascontiguousarray(hep, dtype)
+    torder = np.ascontiguousarray(torder, np.uint32)
+    horder = np.ascontiguousarray(horder, np.uint32)
+    lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+    contact = np.zeros(nv, np.uint8)
+    f = lib().orc_mixed_substeps_f if dtype == np.float32 else lib().orc_mixed_substeps_d
+    if f(nv, _p(X), _p(V), _p(w), _p(lm), tets.shape[0], _p(tets), _p(ep), _p(torder), hexes.shape[0], _p(hexes),
+         _p(hep), _p(horder), nsub, C.byref(params), _p(contact)):
+        raise ValueError("energy model not covered on mixed meshes")
+    return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+
+def mixed_volume(X, tets, hexes, hep, dtype=np.float32):
+    X = np.ascontiguousarray(X, np.float64).reshape(-1)
+    tets = np.ascontiguousarray(tets, np.uint32)
+    hexes = np.ascontiguousarray(hexes, np.uint32)
+    hep = np.ascontiguousarray(hep, dtype)
+    f = lib().orc_mixed_volume_f if dtype == np.float32 else lib().orc_mixed_volume_d
+    return f(_p(X), tets.shape[0], _p(tets), hexes.shape[0], _p(hexes), _p(hep))
+
+
+def mixed_block(W, H, D, scale, pattern, wonkiness, split):
+    """A GenerateHexBlock mesh (XPBDFEM/MeshGen.cpp:156-221) in which the
+    cells that `split(x, y, z)` selects are replaced by GenerateTetBlock's six
+    tets of the same corners (XPBDFEM/MeshGen.cpp:223-244), in cell order:
+    a mixed stream of tag-4 and tag-8 records on the same nodes."""
+    nodes, idx = gen_hex_block(W, H, D, scale, pattern, wonkiness)
+    cells = idx.reshape(-1, 9)[:, 1:]
+    six = ((0, 1, 5, 7), (0, 7, 3, 1), (0, 2, 3, 7), (0, 7, 6, 2), (0, 4, 6, 7), (0, 7, 5, 4))
+    out = []
+    k = 0
+    for z in range(D):
+        for y in range(H):
+            for x in range(W):
+                c = cells[k]
+                k += 1
+                if split(x, y, z):
+                    for t in six:
+                        out += [4] + [int(c[n]) for n in t]
+                else:
+                    out += [8] + [int(n) for n in c]
+    return nodes, np.array(out, np.uint32)
 
 
 # ---- quadratic tetrahedra (oracle/xfem_oracle_t10.inc) ----

@@ -57,6 +57,17 @@
  *       the one-rings in that vertex order (XPBDFEM/Geo.cpp:784-787) and
  *       GeoLinear3d::Damp damps them in it (XPBDFEM/Geo.cpp:800-806).
  *
+ *   mixed density energy simultaneous compliance poisson gx gy dt nsub lockleft
+ *         damping pbdDamping drag rayleighType spacing volumePasses
+ *         < mesh order.u32
+ *       GeoLinear3d::Init on the tagged stream read from stdin (u32 node
+ *       count, the floats, u32 index count, the words), which may mix tets
+ *       and hexes; dumps the tet records (as `init`), the hex records (as
+ *       `hinit`), w and the flags; then reads the tet order and the hex
+ *       order (each u32 count, then the ids) into tOrder and hOrder and runs
+ *       Geo3d::Substep as `damped` does: every tet, then every hex
+ *       (XPBDFEM/Geo.cpp:777-811).
+ *
  * Linear hexahedra: the same commands prefixed with `h` run on a
  * GenerateHexBlock mesh (XPBDFEM/MeshGen.cpp:156-221) and always take the
  * element pattern after the scale:
@@ -170,6 +181,27 @@ static Settings make_settings(uint32_t energy, uint32_t simultaneous, float comp
 	s.lockedRightTransform3d = mat3(1.0f);
 	s.tickId = 0;
 	return s;
+}
+
+// Settings::damping, pbdDamping, drag and the Rayleigh type, with the derived
+// fields filled as Sim::Update does (XPBDFEM/Demo.cpp:53-63, `spacing` for
+// kSpacing); emits the derived values.
+static void set_damping(Settings& s, float dt, float damping, float pbd, float drag, uint32_t rtype, float spacing) {
+	s.damping = damping;
+	s.pbdDamping = pbd;
+	s.drag = drag;
+	s.flags = (s.flags & ~(Settings_RayleighTypeMask << Settings_RayleighTypeBit)) | (rtype << Settings_RayleighTypeBit);
+	const float sdt = dt;
+	float tcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * sdt);
+	s.areaAndTimeCorrectedPbdDamping = tcpd * spacing * spacing;
+	s.volumeAndTimeCorrectedPbdDamping = tcpd * 6.0f * spacing * spacing;
+	float atcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * (float)AmortizationPeriod * sdt);
+	s.amortizedAreaAndTimeCorrectedPbdDamping = atcpd * spacing * spacing;
+	s.amortizedVolumeAndTimeCorrectedPbdDamping = atcpd * 6.0f * spacing * spacing;
+	s.timeCorrectedDrag = 1.0f - pow(1.0f - s.drag, 1000.0f * sdt);
+	const float derived[3] = {s.volumeAndTimeCorrectedPbdDamping, s.amortizedVolumeAndTimeCorrectedPbdDamping,
+	                          s.timeCorrectedDrag};
+	emit("derived", 'f', derived, 3);
 }
 
 static void dump_geo(GeoLinear3d* g) {
@@ -417,6 +449,60 @@ int main(int argc, char** argv) {
 		return 0;
 	}
 
+	if (!strcmp(cmd, "mixed")) {
+		// the mesh, then the tet order and the hex order, from stdin
+		Allocator* alloc = make_alloc((size_t)1 << 31);
+		auto rd = [&](void* p, size_t bytes) { return fread(p, 1, bytes, stdin) == bytes; };
+		uint32_t nodeCount = 0, idxCount = 0;
+		if (!rd(&nodeCount, 4)) { fprintf(stderr, "bad mesh\n"); return 3; }
+		std::vector<float> nodes(nodeCount);
+		if (!rd(nodes.data(), 4 * (size_t)nodeCount) || !rd(&idxCount, 4)) { fprintf(stderr, "bad mesh\n"); return 3; }
+		std::vector<uint32_t> idx(idxCount);
+		if (!rd(idx.data(), 4 * (size_t)idxCount)) { fprintf(stderr, "bad mesh\n"); return 3; }
+		const float density = F(2);
+		const uint32_t energy = U(3), simul = U(4);
+		const float compliance = F(5), poisson = F(6), gx = F(7), gy = F(8), dt = F(9);
+		const uint32_t nsub = U(10), lockLeft = U(11);
+		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
+		set_damping(s, dt, F(12), F(13), F(14), U(15), F(16));
+		s.volumePasses = U(17);
+		GeoLinear3d* g = alloc->New<GeoLinear3d>();
+		g->Init(alloc, density, nodes.data(), nodeCount, idx.data(), idxCount, false);
+		emit("nodes", 'f', nodes.data(), nodeCount);
+		emit("idx", 'I', idx.data(), idxCount);
+		const uint32_t nt = g->con.tetCount, nh = g->con.hexCount, nv = g->vertCount;
+		std::vector<float> ep(nt * 17), hep(nh * 120);
+		for (uint32_t i = 0; i < nt; i++) {
+			const ElementParamsLinearTet& e = g->t[i].ep;
+			float* o = &ep[i * 17];
+			for (int c = 0; c < 3; c++) for (int r = 0; r < 3; r++) o[c * 3 + r] = e.Qi[c][r];
+			for (int k = 0; k < 3; k++) o[9 + k] = e.ic.QQ[k];
+			for (int k = 0; k < 3; k++) o[12 + k] = e.ic.QR[k];
+			o[15] = e.volume;
+			o[16] = e.surfaceArea;
+		}
+		for (uint32_t i = 0; i < nh; i++) hex_record(g->h[i].ep, &hep[i * 120]);
+		std::vector<uint8_t> flags(g->flags, g->flags + nv);
+		emit("ep", 'f', ep.data(), ep.size());
+		emit("hep", 'f', hep.data(), hep.size());
+		emit("w", 'f', g->w, nv);
+		emit("vflags", 'B', flags.data(), nv);
+		uint32_t n = 0;
+		if (!rd(&n, 4) || n != nt || !rd(g->tOrder, 4 * (size_t)n)) { fprintf(stderr, "bad tet order\n"); return 3; }
+		if (!rd(&n, 4) || n != nh || !rd(g->hOrder, 4 * (size_t)n)) { fprintf(stderr, "bad hex order\n"); return 3; }
+		Manipulator manip;
+		manip.pickedGeo = nullptr;
+		for (uint32_t k = 0; k < nsub; k++) {
+			s.tickId = k;
+			g->Substep(s, manip, dt);
+			if (k == 0) dump_state(g, "x1", "v1");
+		}
+		dump_state(g, "xn", "vn");
+		float vol = g->CalculateVolume();
+		emit("volume", 'f', &vol, 1);
+		return 0;
+	}
+
 	if (!strcmp(cmd, "meshgen") || !strcmp(cmd, "init") || !strcmp(cmd, "substep") || !strcmp(cmd, "ordered") ||
 	    !strcmp(cmd, "damped") || !strcmp(cmd, "rings") || !strcmp(cmd, "locked")) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
@@ -456,25 +542,8 @@ int main(int argc, char** argv) {
 		const bool locked = !strcmp(cmd, "locked");
 		const bool damped = !strcmp(cmd, "damped") || rings || locked;
 		if (damped) {
-			s.damping = F(a++);
-			s.pbdDamping = F(a++);
-			s.drag = F(a++);
-			const uint32_t rtype = U(a++);
-			const float spacing = F(a++);
-			s.flags = (s.flags & ~(Settings_RayleighTypeMask << Settings_RayleighTypeBit)) |
-			          (rtype << Settings_RayleighTypeBit);
-			// XPBDFEM/Demo.cpp:53-63 with spacing for kSpacing
-			const float sdt = dt;
-			float tcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * sdt);
-			s.areaAndTimeCorrectedPbdDamping = tcpd * spacing * spacing;
-			s.volumeAndTimeCorrectedPbdDamping = tcpd * 6.0f * spacing * spacing;
-			float atcpd = 1.0f - pow(1.0f - s.pbdDamping, 1000.0f * (float)AmortizationPeriod * sdt);
-			s.amortizedAreaAndTimeCorrectedPbdDamping = atcpd * spacing * spacing;
-			s.amortizedVolumeAndTimeCorrectedPbdDamping = atcpd * 6.0f * spacing * spacing;
-			s.timeCorrectedDrag = 1.0f - pow(1.0f - s.drag, 1000.0f * sdt);
-			const float derived[3] = {s.volumeAndTimeCorrectedPbdDamping, s.amortizedVolumeAndTimeCorrectedPbdDamping,
-			                          s.timeCorrectedDrag};
-			emit("derived", 'f', derived, 3);
+			set_damping(s, dt, F(a), F(a + 1), F(a + 2), U(a + 3), F(a + 4));
+			a += 5;
 			if (a < argc) s.volumePasses = U(a++);
 		}
 		if (locked) {

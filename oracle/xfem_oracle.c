@@ -265,6 +265,7 @@ void orc_h27_tables(float* g8, float* g27, float* n27, float* map27, float* w27)
 #include "xfem_oracle_hex.inc"
 #include "xfem_oracle_t10.inc"
 #include "xfem_oracle_h27.inc"
+#include "xfem_oracle_mixed.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -287,6 +288,7 @@ void orc_h27_tables(float* g8, float* g27, float* n27, float* map27, float* w27)
 #include "xfem_oracle_hex.inc"
 #include "xfem_oracle_t10.inc"
 #include "xfem_oracle_h27.inc"
+#include "xfem_oracle_mixed.inc"
 #undef R
 #undef SFX
 #undef SQRT
@@ -414,6 +416,33 @@ int orc_parse_hexes(const uint32_t* idx, uint32_t idx_count, uint32_t* hexes, ui
 	}
 	*hex_count = nh;
 	*vert_count = nh ? mx + 1 : 0;
+	return 0;
+}
+
+/* A tagged stream of tets (tag 4) and hexes (tag 8) in any mix
+ * (Connectivity3d::Init, XPBDFEM/Connectivity.cpp:251-265): each kind in
+ * stream order; another tag or a truncated record is an error. With
+ * tets == NULL or hexes == NULL only counts. */
+int orc_parse_mixed(const uint32_t* idx, uint32_t idx_count, uint32_t* tets, uint32_t* tet_count, uint32_t* hexes,
+                    uint32_t* hex_count, uint32_t* vert_count) {
+	uint32_t nt = 0, nh = 0, mx = 0, any = 0;
+	for (uint32_t i = 0; i < idx_count; i++) {
+		const uint32_t tag = idx[i];
+		if ((tag != 4u && tag != 8u) || (uint64_t)i + tag >= (uint64_t)idx_count) return -1;
+		for (uint32_t n = 0; n < tag; n++) {
+			uint32_t v = idx[i + 1 + n];
+			if (v > mx) mx = v;
+			if (tag == 4u && tets) tets[4 * (size_t)nt + n] = v;
+			if (tag == 8u && hexes) hexes[8 * (size_t)nh + n] = v;
+		}
+		if (tag == 4u) nt++;
+		else nh++;
+		any = 1;
+		i += tag;
+	}
+	*tet_count = nt;
+	*hex_count = nh;
+	*vert_count = any ? mx + 1 : 0;
 	return 0;
 }
 
@@ -750,6 +779,11 @@ done:
 int orc_hex_schedule(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, uint32_t morton,
                      uint32_t* vert_rank, uint32_t* hex_order, uint32_t* colour_begin, uint32_t* ncolours) {
 	return elem_schedule(nodes, nv, hexes, nh, 8, morton, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int orc_elem_schedule(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t ne, uint32_t per, uint32_t morton,
+                      uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours) {
+	return elem_schedule(nodes, nv, elems, ne, per, morton, vert_rank, order, colour_begin, ncolours);
 }
 
 int orc_t10_schedule(const float* nodes, uint32_t nv, const uint32_t* t10, uint32_t nt, uint32_t morton,

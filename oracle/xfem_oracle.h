@@ -211,6 +211,35 @@ int orc_hex_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const
 float orc_hex_volume_f(const double* X, uint32_t nh, const uint32_t* hexes, const float* ep);
 double orc_hex_volume_d(const double* X, uint32_t nh, const uint32_t* hexes, const double* ep);
 
+/* ---- meshes mixing tets and hexes (oracle/xfem_oracle_mixed.inc) ---------- */
+int orc_parse_mixed(const uint32_t* idx, uint32_t idx_count, uint32_t* tets, uint32_t* tet_count, uint32_t* hexes,
+                    uint32_t* hex_count, uint32_t* vert_count);
+/* Elements of `per` vertices coloured and ordered as the hexes are
+ * (orc_hex_schedule): a mixed mesh's tets take it with per = 4. */
+int orc_elem_schedule(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t ne, uint32_t per, uint32_t morton,
+                      uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours);
+/* GeoLinear3d::Init on a mixed stream: tet records (ORC_EP), hex records
+ * (ORC_EPH), masses summed over the tets then the hexes, then inverted. */
+void orc_mixed_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, const uint32_t* hexes,
+                           uint32_t nh, float density, float* ep, float* hep, float* w, uint8_t* vflags);
+void orc_mixed_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* tets, uint32_t nt, const uint32_t* hexes,
+                           uint32_t nh, double density, double* ep, double* hep, double* w, uint8_t* vflags);
+/* Substeps of a mixed mesh: the tets in torder, then the hexes in horder, per
+ * solve and per volume pass; Rayleigh damping over the tets then the hexes,
+ * then PBD damping over both (XPBDFEM/Geo.cpp:777-811). Returns 0 or -1 (a
+ * continuous-pressure model). */
+int orc_mixed_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                         const uint32_t* tets, const float* ep, const uint32_t* torder, uint32_t nh, const uint32_t* hexes,
+                         const float* hep, const uint32_t* horder, uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_mixed_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
+                         const uint32_t* tets, const double* ep, const uint32_t* torder, uint32_t nh,
+                         const uint32_t* hexes, const double* hep, const uint32_t* horder, uint32_t nsub,
+                         const orc_params* p, uint8_t* contact);
+float orc_mixed_volume_f(const double* X, uint32_t nt, const uint32_t* tets, uint32_t nh, const uint32_t* hexes,
+                         const float* hep);
+double orc_mixed_volume_d(const double* X, uint32_t nt, const uint32_t* tets, uint32_t nh, const uint32_t* hexes,
+                          const double* hep);
+
 /* ---- quadratic tetrahedra (oracle/xfem_oracle_t10.inc) -------------------- */
 /* T10 record, 56 values (ElementParamsQuadraticTet, XPBDFEM/Fem.h:61-68,
  * flattened): Qi column-major [0..8], ic.QQ[9] [9..17], ic.QR[36] [18..53],

@@ -302,7 +302,42 @@ CASES = [
                                         0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1]),
     ("h27volume_wonky_nh_serial_1_post", ["Qdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
                                           -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
+    # meshes mixing tets and hexes (GeoLinear3d on one tagged stream): a
+    # GenerateHexBlock mesh whose `split` cells ("checker": x + y + z even,
+    # "left": x < W / 2) are GenerateTetBlock's six tets; args W H D sx sy sz
+    # pattern wonkiness split, then refgen's `mixed` arguments (density
+    # energy simultaneous compliance poisson gx gy dt nsub lockleft damping
+    # pbdDamping drag rayleighType spacing volumePasses); stdin holds the
+    # mesh, the GPU's tet colour order and its hex colour order
+    ("mixed_c1_nh_nu045_checker", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "checker", 1000.0, 4, 1,
+                                   4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 0]),
+    ("mixed_c1_nh_incompressible_left", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 4, 1,
+                                         C1_COMPLIANCE, 0.5, 0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1, 0]),
+    ("mixed_wonky_yeohfast_serial_nu049_checker", ["mixed", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, "checker", 1000.0, 7, 0,
+                                                   3.2e-4, 0.49, -2.0, -9.81, DT, 10, 1, 0.0, 0.0, 0.0, 2, 0.05, 0]),
+    ("mixed_c1_pixar_nu045_amortized_pbd_checker", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "checker", 1000.0, 0, 1,
+                                                    4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002,
+                                                    3, 0.1, 0]),
+    ("mixed_c1_mixed_nu045_limit_left", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 3, 1,
+                                         4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1, 0]),
+    ("mixed_wonky_nh_paper_volume_checker", ["mixed", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, "checker", 1000.0, 4, 1,
+                                             1e-3, 0.45, -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05, 1]),
+    ("mixed_c1_cube_neo_nu045_post_checker", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "checker", 1000.0, 11, 1,
+                                              4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 2, 0.1,
+                                              0]),
+    ("mixed_c1_yeohskin_nu045_post_pbd_left", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 5, 1, 0.5,
+                                               0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.05, 0.0, 2, 0.1, 0]),
 ]
+
+MIXED_SPLITS = {"checker": lambda x, y, z, W: (x + y + z) % 2 == 0, "left": lambda x, y, z, W: 2 * x < W}
+
+
+def mixed_mesh(args):
+    """The mesh of a `mixed` case: (nodes, idx)."""
+    import oracle  # noqa: E402
+    W, H, D, sx, sy, sz, pattern, wonk, split = args[1:10]
+    f = MIXED_SPLITS[split]
+    return oracle.mixed_block(W, H, D, (sx, sy, sz), pattern, wonk, lambda x, y, z: f(x, y, z, W))
 
 
 def parse(blob):
@@ -375,6 +410,19 @@ def main():
             order = sch["tet_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
+        if args[0] == "mixed":
+            import oracle  # noqa: E402
+            nodes, idx = mixed_mesh(args)
+            tets, hexes, _ = oracle.parse_mixed(idx)
+            ts = oracle.tet_element_schedule(nodes, tets, morton=1)
+            hs = oracle.hex_schedule(nodes, hexes, morton=1)
+            torder, horder = ts["tet_order"].astype(np.uint32), hs["hex_order"].astype(np.uint32)
+            argv = [REFGEN, "mixed"] + [str(a) for a in args[10:]]
+            stdin = (struct.pack("<I", nodes.size) + nodes.astype(np.float32).tobytes() + struct.pack("<I", idx.size) +
+                     idx.astype(np.uint32).tobytes() + struct.pack("<I", torder.size) + torder.tobytes() +
+                     struct.pack("<I", horder.size) + horder.tobytes())
+            extra = {"torder": torder, "colour_tet_begin": ts["colour_tet_begin"], "horder": horder,
+                     "colour_hex_begin": hs["colour_hex_begin"]}
         if args[0] in ("ordered", "damped", "rings", "locked"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]

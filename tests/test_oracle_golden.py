@@ -411,6 +411,55 @@ def test_hex_ring_substeps_bit_exact(orc, name):
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
 
 
+MIXED = ["mixed_c1_nh_nu045_checker", "mixed_c1_nh_incompressible_left", "mixed_wonky_yeohfast_serial_nu049_checker",
+         "mixed_c1_pixar_nu045_amortized_pbd_checker", "mixed_c1_mixed_nu045_limit_left",
+         "mixed_wonky_nh_paper_volume_checker", "mixed_c1_cube_neo_nu045_post_checker",
+         "mixed_c1_yeohskin_nu045_post_pbd_left"]
+
+
+def mixed_params(orc, a, g, tick):
+    """orc_params of a `mixed` fixture (its arguments after the mesh ones)."""
+    dens, energy, simul, comp, nu, gx, gy, dt, nsub, lock, damping, pbd, drag, rtype, spacing, vpasses = a[10:26]
+    d = g["derived"]
+    return orc.make_params(dt=dt, compliance=comp, poisson=nu, energy=energy, simultaneous=bool(simul),
+                           gravity=(gx, gy, 0.0), lock=bool(lock), tick=tick, damping=damping, rayleigh_type=rtype,
+                           pbd_damping=pbd, pbd_coeff=float(d[0]), pbd_coeff_amortized=float(d[1]), drag=float(d[2]),
+                           volume_passes=vpasses)
+
+
+@pytest.mark.parametrize("name", MIXED)
+def test_mixed_mesh_substeps_bit_exact(orc, name):
+    """A mesh mixing tets and hexes (GeoLinear3d on one tagged stream): rest
+    state with the masses of both kinds summed tets first, then substeps
+    that solve every tet, then every hex, and damp likewise
+    (XPBDFEM/Geo.cpp:697-745, 777-811), in the fixture's tet and hex colour
+    orders, which the element schedule restatement reproduces."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[10], a[18]
+    tets, hexes, nv = orc.parse_mixed(g["idx"])
+    assert tets.shape[0] and hexes.shape[0] and nv == g["nodes"].size // 3
+    ep, hep, w, fl = orc.mixed_init_rest(g["nodes"], tets, hexes, dens)
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["ep"].view(np.uint32))
+    assert np.array_equal(hep.reshape(-1).view(np.uint32), g["hep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+    ts = orc.tet_element_schedule(g["nodes"], tets, morton=1)
+    hs = orc.hex_schedule(g["nodes"], hexes, morton=1)
+    assert np.array_equal(ts["tet_order"], g["torder"]) and np.array_equal(hs["hex_order"], g["horder"])
+    X0 = g["nodes"].astype(np.float64)
+    lm = (fl & 1).astype(np.uint8)
+    X1, V1, w1, _ = orc.mixed_substeps(X0, np.zeros_like(X0), w, tets, ep, g["torder"], hexes, hep, g["horder"], 1,
+                                       mixed_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = orc.mixed_substeps(X1, V1, w1, tets, ep, g["torder"], hexes, hep, g["horder"], nsub - 1,
+                                      mixed_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(orc.mixed_volume(Xn, tets, hexes, hep)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
 def test_hex_schedule_is_a_valid_colouring(orc):
     """Hexes of one colour share no vertex; greedy first fit in id order
     (each hex takes the smallest colour free among earlier neighbours)."""
