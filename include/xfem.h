@@ -202,9 +202,13 @@ int xfem_settings_default(xfem_settings* s);
  * uploads everything. A mesh of hexes (tag 8) gets the hex rest state
  * (InitQuadHexFiniteElement, XPBDFEM/Fem.cpp:225-265) and the hex colouring;
  * element type T10 or H27 (flags bits 0-3) makes a tet mesh a T10 body and a
- * hex mesh an H27 body (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941); a
- * mesh mixing tets and hexes, or a T10 or H27 body with the continuous-pressure
- * models (energy 8-10), returns XFEM_EUNSUPPORTED. */
+ * hex mesh an H27 body (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941). A
+ * mesh mixing tets and hexes is one body holding both (GeoLinear3d on one
+ * tagged stream, XPBDFEM/Geo.cpp:697-811): each sweep solves every tet, then
+ * every hex, each kind in a colouring of its own. Such a mesh with the
+ * continuous-pressure models (energy 8-10) or with quadratic elements, and a
+ * T10 or H27 body with the continuous-pressure models, return
+ * XFEM_EUNSUPPORTED. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -392,6 +396,31 @@ int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, 
  * idx[9 W H D] (tag 8 and 8 vertex ids per hex). */
 int xfem_generate_hex_block(uint32_t W, uint32_t H, uint32_t D, float sx, float sy, float sz,
                             uint32_t pattern, float wonkiness, float* nodes, uint32_t* idx);
+
+/* ---- meshes mixing tets and hexes (mixed mode) --------------------------------
+ * A body whose tagged stream holds tets (tag 4) and hexes (tag 8), as
+ * GeoLinear3d::Init takes it (XPBDFEM/Geo.cpp:697-745): xfem_body_counts gives
+ * its tets, xfem_body_hex_count its hexes, xfem_get_rest_state the tets' 17
+ * floats each with the inverse masses of every vertex (the masses of all tets,
+ * then all hexes, summed per vertex), xfem_get_hex_rest_state and
+ * xfem_get_hex_schedule the hexes' records and colouring. The tets' own
+ * colouring (colour-major; the tets of one colour share no vertex; caller tet
+ * ids, colour offsets with ncolours + 1 entries, at most 4097), which replaces
+ * the stream order of GeoLinear3d::Constrain's tet loop
+ * (XPBDFEM/Geo.cpp:777-778): */
+int xfem_get_mixed_tet_schedule(const xfem_body* b, uint32_t body, uint32_t* tet_order, uint32_t* colour_begin,
+                                uint32_t* ncolours);
+/* The same, computed on the host without a handle or a GPU: the rest state
+ * (17 floats per tet, 120 per hex, inverse masses, vertex flags) and the
+ * schedule (vertex ranks, the tet and the hex colourings). Any output may be
+ * NULL; XFEM_EINVAL unless the stream holds both kinds. */
+int xfem_compute_mixed_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                  uint32_t idx_data_count, float density, float* out_ep17, float* out_ep120,
+                                  float* out_w, uint8_t* out_flags);
+int xfem_compute_mixed_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* tet_order,
+                                uint32_t* tet_colour_begin, uint32_t* tet_ncolours, uint32_t* hex_order,
+                                uint32_t* hex_colour_begin, uint32_t* hex_ncolours);
 
 /* ---- quadratic tets (T10 mode) ----------------------------------------------- */
 /* T10s and edge nodes of one body; XFEM_EUNSUPPORTED for another body. */

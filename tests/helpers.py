@@ -73,6 +73,31 @@ class HexOracleRun:
         return self
 
 
+class MixedOracleRun:
+    """The oracle's state for one mesh mixing tets and hexes, stepped in the
+    body's tet and hex colour orders."""
+
+    def __init__(self, nodes, idx, density, settings, torder, horder, dtype=np.float32):
+        self.tets, self.hexes, nv = oracle.parse_mixed(idx)
+        self.ep, self.hep, self.w, fl = oracle.mixed_init_rest(nodes, self.tets, self.hexes, density, dtype)
+        self.lock = (fl & 3).astype(np.uint8)
+        self.nodes = np.asarray(nodes, np.float32).reshape(-1)
+        self.X = np.asarray(nodes, np.float64).reshape(-1, 3).copy()
+        self.V = np.zeros_like(self.X)
+        self.s = settings
+        self.torder = torder
+        self.horder = horder
+        self.dtype = dtype
+        self.contact = None
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt, nodes=self.nodes)
+        self.X, self.V, self.w, self.contact = oracle.mixed_substeps(
+            self.X, self.V, self.w, self.tets, self.ep, self.torder, self.hexes, self.hep, self.horder, n, p,
+            lock_mask=self.lock, dtype=self.dtype)
+        return self
+
+
 class T10OracleRun:
     """The oracle's state for one tet mesh read as T10s (GeoQuadratic3d),
     stepped in the body's T10 order."""

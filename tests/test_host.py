@@ -261,15 +261,68 @@ def test_hex_mesh_errors():
     assert e.value.code == xfem.EUNSUPPORTED
     with pytest.raises(xfem.XfemError):
         xfem.compute_hex_rest_state(tn, ti, 1000.0)
-    # mixing tets and hexes in one stream
+    # a stream mixing tets and hexes is not a hex mesh (its own helpers below)
     mixed = np.concatenate([idx[:9], ti[:5]])
     with pytest.raises(xfem.XfemError) as e:
         xfem.compute_hex_rest_state(nodes, mixed, 1000.0)
-    assert e.value.code == xfem.EUNSUPPORTED
+    assert e.value.code == xfem.EINVAL
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.compute_mixed_rest_state(nodes, idx, 1000.0)
+    assert e.value.code == xfem.EINVAL
     # a truncated hex record
     with pytest.raises(xfem.XfemError) as e:
         xfem.compute_hex_rest_state(nodes, idx[:-1], 1000.0)
     assert e.value.code == xfem.EINVAL
+
+
+# ---- meshes mixing tets and hexes (GeoLinear3d on one tagged stream) ----
+MIXED_FIX = ["mixed_c1_nh_nu045_checker", "mixed_c1_nh_incompressible_left", "mixed_wonky_yeohfast_serial_nu049_checker",
+             "mixed_wonky_nh_paper_volume_checker"]
+
+
+@pytest.mark.parametrize("name", MIXED_FIX)
+def test_mixed_host_setup_bit_exact_vs_reference(name):
+    """The library's host set-up of a mixed mesh against the reference's
+    own GeoLinear3d::Init (XPBDFEM/Geo.cpp:697-745): tet and hex records,
+    inverse masses of both kinds summed tets first, vertex flags; and the
+    tet and hex colourings in the fixture's orders."""
+    g = golden(name)
+    dens = golden_args(name)["args"][10]
+    ep, hep, w, fl = xfem.compute_mixed_rest_state(g["nodes"], g["idx"], dens)
+    assert np.array_equal(ep.reshape(-1).view(np.uint32), g["ep"].view(np.uint32))
+    assert np.array_equal(hep.reshape(-1).view(np.uint32), g["hep"].view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(fl, g["vflags"])
+    s = xfem.compute_mixed_schedule(g["nodes"], g["idx"])
+    assert np.array_equal(s["tet_order"], g["torder"])
+    assert np.array_equal(s["colour_tet_begin"], g["colour_tet_begin"])
+    assert np.array_equal(s["hex_order"], g["horder"])
+    assert np.array_equal(s["colour_hex_begin"], g["colour_hex_begin"])
+
+
+@pytest.mark.parametrize("morton", [True, False])
+def test_mixed_host_matches_oracle_on_a_jittered_block(orc, morton):
+    import oracle
+    nodes, idx = oracle.mixed_block(5, 4, 3, (0.05, 0.06, 0.04), 1, 0.25, lambda x, y, z: (x * 7 + y * 3 + z) % 3 == 0)
+    nodes = (nodes + np.random.default_rng(3).normal(0, 0.002, nodes.shape)).astype(np.float32)
+    tets, hexes, _ = orc.parse_mixed(idx)
+    ep, hep, w, fl = xfem.compute_mixed_rest_state(nodes, idx, 950.0)
+    e2, h2, w2, f2 = orc.mixed_init_rest(nodes, tets, hexes, 950.0)
+    assert np.array_equal(ep.view(np.uint32), e2.view(np.uint32))
+    assert np.array_equal(hep.view(np.uint32), h2.view(np.uint32))
+    assert np.array_equal(w.view(np.uint32), w2.view(np.uint32))
+    assert np.array_equal(fl, f2)
+    s = xfem.compute_mixed_schedule(nodes, idx, morton=morton)
+    ts = orc.tet_element_schedule(nodes, tets, morton=1 if morton else 0)
+    hs = orc.hex_schedule(nodes, hexes, morton=1 if morton else 0)
+    assert np.array_equal(s["vert_rank"], hs["vert_rank"])
+    assert np.array_equal(s["tet_order"], ts["tet_order"])
+    assert np.array_equal(s["colour_tet_begin"], ts["colour_tet_begin"])
+    assert np.array_equal(s["hex_order"], hs["hex_order"])
+    for order, els, cb in ((s["tet_order"], tets, s["colour_tet_begin"]), (s["hex_order"], hexes, s["colour_hex_begin"])):
+        for c in range(cb.size - 1):
+            verts = els[order[cb[c]:cb[c + 1]]].reshape(-1)
+            assert np.unique(verts).size == verts.size
 
 
 # ---- quadratic tets (GeoQuadratic3d on a tet mesh) ----

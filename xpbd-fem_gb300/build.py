@@ -18,7 +18,8 @@ SRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "xfem")
 LIB = os.path.join(OUT_DIR, "libxfem.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["xfem_kernels.cu", "xfem_adjoint.cu", "xfem_setup.cu", "xfem_rings.cu", "xfem_hexes.cu", "xfem_t10.cu", "xfem_h27.cu",
+SOURCES = ["xfem_kernels.cu", "xfem_adjoint.cu", "xfem_setup.cu", "xfem_rings.cu", "xfem_hexes.cu", "xfem_mixed.cu", "xfem_t10.cu",
+           "xfem_h27.cu",
            "xfem_api.cpp",
            "xfem_host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -52,7 +52,7 @@ cudaError_t injected_alloc_failure() {
 // Element kinds of a body: linear tets (the chunked tet path, the one-ring
 // mode), linear hexahedra (H8), quadratic tets (T10) and quadratic hexahedra
 // (H27), the last three in the element kernel.
-constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2, kElH27 = 3;
+constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2, kElH27 = 3, kElMixed = 4;
 
 struct BodyHost {
 	uint32_t nv = 0, nt = 0, vbase = 0, tbase = 0;
@@ -68,7 +68,7 @@ struct BodyHost {
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
 	// element bodies (linear hexahedra or quadratic tets; no linear tets)
-	uint32_t el = 0;                  // kElTets, kElHexes, kElT10, kElH27
+	uint32_t el = 0;                  // kElTets, kElHexes, kElT10, kElH27, kElMixed (tets and hexes)
 	uint32_t nh = 0;                  // elements
 	uint32_t ncorner = 0;             // T10, H27: the mesh's own vertices; the added nodes follow
 	std::vector<uint32_t> elems;      // 8 per hex, 10 per T10 or 27 per H27, caller order
@@ -77,6 +77,7 @@ struct BodyHost {
 	std::vector<float> eep;           // rest::kHexRec per hex, rest::kT10Rec per T10, rest::kH27Rec per H27
 	ElemSchedule esched;
 	std::vector<uint32_t> el_dev;     // hexes, T10s, H27s: each element's device index (build_elements)
+	ElemSchedule tsched;              // kElMixed: the tets' own colouring (elements of 4 vertices)
 };
 
 template <typename T>
@@ -157,6 +158,10 @@ struct xfem_body {
 	DevBuf<float4> el_rec;
 	DevBuf<uint32_t> el_cb, el_flat;
 	DevBuf<float> el_tab;
+	// meshes mixing tets and hexes (kElMixed): the tets as elements of their own colouring
+	DevBuf<uint4> mt_vid;
+	DevBuf<float4> mt_rec;
+	DevBuf<uint32_t> mt_cb, mt_flat;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -259,6 +264,15 @@ BodyParams make_params(const xfem_settings& s) {
 	p.pbd_coeff = s.volume_and_time_corrected_pbd_damping;
 	p.pbd_coeff_amortized = s.amortized_volume_and_time_corrected_pbd_damping;
 	return p;
+}
+
+// The element counts a body's damping slices divide: its tets (tet bodies),
+// its elements (hex, T10 and H27 bodies), or its tets and its hexes (a mesh
+// mixing the two, XPBDFEM/Geo.cpp:792-811).
+void set_counts(BodyParams& p, const BodyHost& b) {
+	p.ntets = b.el == kElTets || b.el == kElMixed ? b.nt : b.nh;
+	p.nhexes = b.el == kElMixed ? b.nh : 0u;
+	p.nverts = b.nv;
 }
 
 // Whether any body needs the extended kernels: it damps (in the solve or
@@ -396,11 +410,11 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 		ntag[tag == 8u]++;
 		i += tag + 1;
 	}
-	if (ntag[0] && ntag[1]) return fail(XFEM_EUNSUPPORTED, "meshes mixing tets (tag 4) and hexes (tag 8) are not supported");
-	b.el = ntag[1] > 0 ? kElHexes : kElTets;
+	b.el = ntag[0] && ntag[1] ? kElMixed : ntag[1] > 0 ? kElHexes : kElTets;
 	uint32_t nv = 0;
-	if (b.el == kElHexes ? parse_hexes(m.idx_data, m.idx_data_count, b.elems, nv)
-	                     : parse_tets(m.idx_data, m.idx_data_count, b.tets, nv))
+	if (b.el == kElMixed ? parse_mixed(m.idx_data, m.idx_data_count, b.tets, b.elems, nv)
+	    : b.el == kElHexes ? parse_hexes(m.idx_data, m.idx_data_count, b.elems, nv)
+	                       : parse_tets(m.idx_data, m.idx_data_count, b.tets, nv))
 		return fail(XFEM_EINVAL, "truncated index stream");
 	// GeoLinear3d::Init asserts vertCount == nodeDataCount / 3 (XPBDFEM/Geo.cpp:700)
 	if (nv != m.node_data_count / 3)
@@ -414,6 +428,13 @@ int prepare_mesh(const xfem_mesh& m, BodyHost& b) {
 	return XFEM_OK;
 }
 
+// Whether the settings ask for quadratic elements (GeoQuadratic3d: element
+// type T10 or H27 in flags bits 0-3, XPBDFEM/Demo.cpp:145-150).
+bool quadratic_type(uint32_t flags) {
+	const uint32_t t = flags & XFEM_ELEMENT_TYPE_MASK;
+	return t == XFEM_ELEMENT_T10 || t == XFEM_ELEMENT_H27;
+}
+
 // The argument checks of prepare_mesh and validate_settings for every body,
 // made before any device is touched: a bad tag, a truncated stream, a vertex
 // count that does not match the node array or invalid settings fail the same
@@ -424,8 +445,8 @@ int precheck_inputs(uint32_t nb, const xfem_mesh* meshes, const xfem_settings* s
 		const std::string who = nb > 1 ? "body " + std::to_string(k) + ": " : std::string();
 		if (!m.node_data || !m.idx_data) return fail(XFEM_EINVAL, who + "null mesh array");
 		if (m.node_data_count % 3) return fail(XFEM_EINVAL, who + "node_data_count must be a multiple of 3");
-		uint32_t ntag[2] = {0, 0};
 		uint64_t nv = 0;
+		uint32_t ntag[2] = {0, 0};
 		for (uint32_t i = 0; i < m.idx_data_count;) {
 			const uint32_t tag = m.idx_data[i];
 			if (tag != 4u && tag != 8u)
@@ -435,8 +456,14 @@ int precheck_inputs(uint32_t nb, const xfem_mesh* meshes, const xfem_settings* s
 			ntag[tag == 8u]++;
 			i += tag + 1;
 		}
-		if (ntag[0] && ntag[1])
-			return fail(XFEM_EUNSUPPORTED, who + "meshes mixing tets (tag 4) and hexes (tag 8) are not supported");
+		if (ntag[0] && ntag[1] && settings) {
+			const uint32_t energy = (settings[k].flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
+			if (model_of(energy) == kModelRing)
+				return fail(XFEM_EUNSUPPORTED, who + "the continuous-pressure models (energy 8-10) run on meshes of one "
+				                                     "element kind");
+			if (quadratic_type(settings[k].flags))
+				return fail(XFEM_EUNSUPPORTED, who + "quadratic elements (flags bits 0-3) on a mesh mixing tets and hexes");
+		}
 		if (nv != m.node_data_count / 3)
 			return fail(XFEM_EINVAL, who + "vertex count " + std::to_string(nv) +
 			                             " implied by the index stream != node_data_count/3 = " +
@@ -458,6 +485,12 @@ void host_rest(const xfem_mesh& m, BodyHost& b) {
 	if (b.el == kElHexes) {
 		b.eep.resize((size_t)rest::kHexRec * b.nh);
 		hex_init_rest(b.nodes.data(), b.nv, b.elems.data(), b.nh, m.density, b.eep.data(), b.w0.data(), b.vflags.data());
+		return;
+	}
+	if (b.el == kElMixed) {
+		b.eep.resize((size_t)rest::kHexRec * b.nh);
+		mixed_init_rest(b.nodes.data(), b.nv, b.tets.data(), b.nt, b.elems.data(), b.nh, m.density, b.ep.data(),
+		                b.eep.data(), b.w0.data(), b.vflags.data());
 		return;
 	}
 	init_rest(b.nodes.data(), b.nv, b.tets.data(), b.nt, m.density, b.ep.data(), b.w0.data(), b.vflags.data());
@@ -515,14 +548,7 @@ void prepare_h27(const xfem_mesh& m, BodyHost& b, std::vector<double>* X = nullp
 }
 
 // Elements of an element body, and vertices per element.
-uint32_t nodes_per_element(uint32_t el) { return el == kElH27 ? 27u : el == kElT10 ? 10u : 8u; }
-
-// Whether the settings ask for quadratic elements (GeoQuadratic3d: element
-// type T10 or H27 in flags bits 0-3, XPBDFEM/Demo.cpp:145-150).
-bool quadratic_type(uint32_t flags) {
-	const uint32_t t = flags & XFEM_ELEMENT_TYPE_MASK;
-	return t == XFEM_ELEMENT_T10 || t == XFEM_ELEMENT_H27;
-}
+uint32_t nodes_per_element(uint32_t el) { return el == kElH27 ? 27u : el == kElT10 ? 10u : 8u; }  // kElMixed: its hexes
 
 // Rest state and schedule of one body: on the host (gpu false), or with the
 // parallel phases on the GPU (rest state, incidence, vertex ranks, cluster
@@ -542,6 +568,20 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	const uint32_t energy = (b.settings.flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
 	const bool ring = model_of(energy) == kModelRing;
 	const bool quad = quadratic_type(b.settings.flags);
+	if (b.el == kElMixed) {
+		// tets and hexes in one mesh: set-up on the host, each kind with a
+		// colouring of its own
+		if (ring)
+			return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) run on meshes of one element kind: "
+			                               "on a mixed mesh the reference indexes a ring's hexes two different ways");
+		if (quad) return fail(XFEM_EUNSUPPORTED, "quadratic elements (flags bits 0-3) on a mesh mixing tets and hexes");
+		host_rest(m, b);
+		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
+		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 8, morton, b.esched) ||
+		    elem_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, 4, morton, b.tsched))
+			return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+		return XFEM_OK;
+	}
 	if (b.el == kElHexes || quad) {
 		// hexes, T10s and H27s: set-up on the host (rest state, Morton vertex
 		// ranks, the element colouring)
@@ -889,6 +929,58 @@ int build_elements(xfem_body* h) {
 	return XFEM_OK;
 }
 
+// The tets of every mixed body in device order (colour-major over the tets'
+// own colouring, bodies in order inside a colour): four device vertex ids,
+// the record as five float4 planes (plane k of tet i at rec[k * n + i]: the
+// 17 floats of ElementParamsLinearTet, XPBDFEM/Fem.h:52-60, then three pads)
+// and each tet's index in its body's tet order (the amortized damping slices).
+int build_mixed_tets(xfem_body* h) {
+	uint32_t ncol = 0, n = 0;
+	for (const BodyHost& b : h->bodies) {
+		ncol = std::max(ncol, b.tsched.ncolours);
+		n += b.nt;
+	}
+	std::vector<uint4> vid(n);
+	std::vector<uint32_t> cb(ncol + 1, 0), flat(n);
+	std::vector<float4> rec(5 * (size_t)n);
+	uint32_t o = 0;
+	for (uint32_t c = 0; c < ncol; c++) {
+		cb[c] = o;
+		for (const BodyHost& b : h->bodies) {
+			const ElemSchedule& es = b.tsched;
+			if (c >= es.ncolours) continue;
+			for (uint32_t k = es.colour_begin[c]; k < es.colour_begin[c + 1]; k++, o++) {
+				const uint32_t t = es.order[k];
+				const uint32_t* is = &b.tets[4 * (size_t)t];
+				vid[o] = make_uint4(b.vbase + b.sched.vert_rank[is[0]], b.vbase + b.sched.vert_rank[is[1]],
+				                    b.vbase + b.sched.vert_rank[is[2]], b.vbase + b.sched.vert_rank[is[3]]);
+				flat[o] = k;
+				const float* e = &b.ep[17 * (size_t)t];
+				for (uint32_t k4 = 0; k4 < 4; k4++)
+					rec[(size_t)k4 * n + o] = make_float4(e[4 * k4], e[4 * k4 + 1], e[4 * k4 + 2], e[4 * k4 + 3]);
+				rec[4 * (size_t)n + o] = make_float4(e[16], 0.0f, 0.0f, 0.0f);
+			}
+		}
+	}
+	cb[ncol] = o;
+	XCUDA(h->mt_vid.alloc(vid.size()));
+	XCUDA(h->mt_rec.alloc(rec.size()));
+	XCUDA(h->mt_cb.alloc(cb.size()));
+	XCUDA(h->mt_flat.alloc(flat.size()));
+	auto up = [&](void* dst, const void* src, size_t bytes) {
+		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+	};
+	XCUDA(up(h->mt_vid.p, vid.data(), vid.size() * sizeof(uint4)));
+	XCUDA(up(h->mt_rec.p, rec.data(), rec.size() * sizeof(float4)));
+	XCUDA(up(h->mt_cb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(h->mt_flat.p, flat.data(), flat.size() * 4));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	h->ctx.mt_colours = ncol;
+	h->ctx.nmt = n;
+	h->device_bytes += vid.size() * 16 + rec.size() * 16 + cb.size() * 4 + flat.size() * 4;
+	return XFEM_OK;
+}
+
 // Packs every body's schedule into the merged device layout and uploads it.
 int build_device(xfem_body* h) {
 	SetupClock clk;
@@ -1106,8 +1198,7 @@ int build_device(xfem_body* h) {
 		for (size_t i = 0; i < 4 * (size_t)b.nt; i++) tets_dev[tbase + i] = b.vbase + b.sched.vert_rank[b.tets[i]];
 		tbase += 4 * (size_t)b.nt;
 		params[bi] = make_params(b.settings);
-		params[bi].ntets = b.el ? b.nh : b.nt;
-		params[bi].nverts = b.nv;
+		set_counts(params[bi], b);
 	}
 	clk.lap("vertex state");
 	// upload
@@ -1200,6 +1291,7 @@ int build_device(xfem_body* h) {
 	}
 	if (h->el_mode) {  // before the rings: a hex ring addresses its hexes by device index
 		int rr = build_elements(h);
+		if (!rr && h->el_mode == kElMixed) rr = build_mixed_tets(h);
 		if (rr) return rr;
 	}
 	if (h->ring_mode) {
@@ -1261,6 +1353,10 @@ int build_device(xfem_body* h) {
 	c.colour_el_begin = h->el_cb.p;
 	c.el_tab = h->el_tab.p;
 	c.el_flat = h->el_flat.p;
+	c.mt_vid = h->mt_vid.p;
+	c.mt_rec = h->mt_rec.p;
+	c.colour_mt_begin = h->mt_cb.p;
+	c.mt_flat = h->mt_flat.p;
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
@@ -1450,9 +1546,10 @@ int launch_mode(xfem_body* h, const DevCtx& ctx, uint32_t nsub, float dt) {
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
-	const int e = h->el_mode == kElH27 ? launch_h27(ctx, 256, nsub, dt, h->stream)
-	              : h->el_mode == kElT10 ? launch_t10(ctx, 256, nsub, dt, h->stream)
-	                                     : launch_hexes(ctx, 256, nsub, dt, h->stream);
+	const int e = h->el_mode == kElH27     ? launch_h27(ctx, 256, nsub, dt, h->stream)
+	              : h->el_mode == kElT10   ? launch_t10(ctx, 256, nsub, dt, h->stream)
+	              : h->el_mode == kElMixed ? launch_mixed(ctx, 256, nsub, dt, h->stream)
+	                                       : launch_hexes(ctx, 256, nsub, dt, h->stream);
 	if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
 	return XFEM_OK;
 }
@@ -1621,8 +1718,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	b->settings = *s;
 	XCUDA(cudaSetDevice(h->device));
 	BodyParams p = make_params(*s);
-	p.ntets = b->el ? b->nh : b->nt;
-	p.nverts = b->nv;
+	set_counts(p, *b);
 	XCUDA(cudaMemcpyAsync(h->params.p + body, &p, sizeof(p), cudaMemcpyHostToDevice, h->stream));
 	// Settings::tickId: the handle's substep counter continues from here
 	XCUDA(cudaMemcpyAsync(h->tick.p, &s->tick_id, 4, cudaMemcpyHostToDevice, h->stream));
@@ -1791,6 +1887,38 @@ int xfem_get_lambdas(xfem_body* h, uint32_t body, float* out) {
 	return XFEM_OK;
 }
 
+// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) summed over a body's
+// linear hexes at positions x (caller order): rest volume times the weighted
+// det F over the 2x2x2 points, in double.
+static double hex_volume(const BodyHost& b, const float* x) {
+	double v = 0.0;
+	for (uint32_t hx = 0; hx < b.nh; hx++) {
+		const uint32_t* is = &b.elems[8 * (size_t)hx];
+		const float* e = &b.eep[(size_t)rest::kHexRec * hx];
+		double P[7][3];
+		for (int i = 0; i < 7; i++)
+			for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[7] + k];
+		double scale = 0.0;
+		for (int p = 0; p < 8; p++) {
+			double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+			for (int n = 0; n < 7; n++)
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::hex_g8(p, n, r) * P[n][c];
+			const float* ji = e + rest::kHexJH + 9 * p;
+			for (int c = 0; c < 3; c++)
+				for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
+			const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+			                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+			                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+			scale += (double)e[rest::kHexWH + p] * det;
+		}
+		v += (double)e[rest::kHexVol] * scale;
+	}
+	return v;
+}
+
+static int tet_volume(xfem_body* h, uint32_t body, double* out);
+
 int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
@@ -1861,38 +1989,29 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 		*out = v;
 		return XFEM_OK;
 	}
-	if (b->el == kElHexes) {
-		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per hex: rest
-		// volume times the weighted det F over the 2x2x2 points, in double
+	if (b->el == kElHexes || b->el == kElMixed) {
 		std::vector<float> x(3 * (size_t)b->nv);
 		const int rc = get_xyz(h, body, 0, x.data());
 		if (rc) return rc;
-		double v = 0.0;
-		for (uint32_t hx = 0; hx < b->nh; hx++) {
-			const uint32_t* is = &b->elems[8 * (size_t)hx];
-			const float* e = &b->eep[(size_t)rest::kHexRec * hx];
-			double P[7][3];
-			for (int i = 0; i < 7; i++)
-				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[7] + k];
-			double scale = 0.0;
-			for (int p = 0; p < 8; p++) {
-				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
-				for (int n = 0; n < 7; n++)
-					for (int c = 0; c < 3; c++)
-						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::hex_g8(p, n, r) * P[n][c];
-				const float* ji = e + rest::kHexJH + 9 * p;
-				for (int c = 0; c < 3; c++)
-					for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
-				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
-				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
-				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
-				scale += (double)e[rest::kHexWH + p] * det;
-			}
-			v += (double)e[rest::kHexVol] * scale;
+		const double vh = hex_volume(*b, x.data());
+		if (b->el == kElHexes) {
+			*out = vh;
+			return XFEM_OK;
 		}
-		*out = v;
+		// a mixed mesh: the tets' volumes (below) plus the hexes'
+		// (XPBDFEM/Geo.cpp:827-832 sums every element of the stream)
+		double vt = 0.0;
+		const int rt = tet_volume(h, body, &vt);
+		if (rt) return rt;
+		*out = vt + vh;
 		return XFEM_OK;
 	}
+	return tet_volume(h, body, out);
+}
+
+// The tets' part of xfem_calculate_volume, summed on the device in double.
+static int tet_volume(xfem_body* h, uint32_t body, double* out) {
+	const BodyHost* b = &h->bodies[body];
 	size_t tb = 0;
 	for (uint32_t i = 0; i < body; i++) tb += 4 * (size_t)h->bodies[i].nt;
 	const int e = launch_volume(h->vert.p, h->tets_dev.p + tb, b->nt, h->vol.p, h->stream);
@@ -1904,7 +2023,8 @@ int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 int xfem_get_rest_state(const xfem_body* h, uint32_t body, float* out_ep17, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el) return fail(XFEM_EUNSUPPORTED, "an element body: use xfem_get_hex_rest_state, _t10_ or _h27_");
+	if (b.el && b.el != kElMixed)
+		return fail(XFEM_EUNSUPPORTED, "an element body: use xfem_get_hex_rest_state, _t10_ or _h27_");
 	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
@@ -2015,7 +2135,7 @@ int xfem_body_hex_count(const xfem_body* h, uint32_t body, uint32_t* nhexes) {
 int xfem_get_hex_rest_state(const xfem_body* h, uint32_t body, float* out_ep120, float* out_w) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElHexes) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	if (b.el != kElHexes && b.el != kElMixed) return fail(XFEM_EUNSUPPORTED, "not a hex body");
 	if (out_ep120) memcpy(out_ep120, b.eep.data(), b.eep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	return XFEM_OK;
@@ -2034,8 +2154,55 @@ int xfem_get_hex_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank
                           uint32_t* colour_begin, uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElHexes) return fail(XFEM_EUNSUPPORTED, "not a hex body");
+	if (b.el != kElHexes && b.el != kElMixed) return fail(XFEM_EUNSUPPORTED, "not a hex body");
 	return elem_schedule_out(b, vert_rank, hex_order, colour_begin, ncolours);
+}
+
+int xfem_get_mixed_tet_schedule(const xfem_body* h, uint32_t body, uint32_t* tet_order, uint32_t* colour_begin,
+                                uint32_t* ncolours) {
+	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
+	const BodyHost& b = h->bodies[body];
+	if (b.el != kElMixed) return fail(XFEM_EUNSUPPORTED, "not a mesh mixing tets and hexes");
+	if (tet_order) memcpy(tet_order, b.tsched.order.data(), b.tsched.order.size() * 4);
+	if (colour_begin) memcpy(colour_begin, b.tsched.colour_begin.data(), b.tsched.colour_begin.size() * 4);
+	if (ncolours) *ncolours = b.tsched.ncolours;
+	return XFEM_OK;
+}
+
+int xfem_compute_mixed_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                  uint32_t idx_data_count, float density, float* out_ep17, float* out_ep120, float* out_w,
+                                  uint8_t* out_flags) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (b.el != kElMixed) return fail(XFEM_EINVAL, "not a mesh mixing tets and hexes");
+	host_rest(m, b);
+	if (out_ep17) memcpy(out_ep17, b.ep.data(), b.ep.size() * sizeof(float));
+	if (out_ep120) memcpy(out_ep120, b.eep.data(), b.eep.size() * sizeof(float));
+	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
+	if (out_flags) memcpy(out_flags, b.vflags.data(), b.vflags.size());
+	return XFEM_OK;
+}
+
+int xfem_compute_mixed_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
+                                uint32_t idx_data_count, uint32_t no_morton, uint32_t* vert_rank, uint32_t* tet_order,
+                                uint32_t* tet_colour_begin, uint32_t* tet_ncolours, uint32_t* hex_order,
+                                uint32_t* hex_colour_begin, uint32_t* hex_ncolours) {
+	BodyHost b;
+	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, 1.0f};
+	const int rc = prepare_mesh(m, b);
+	if (rc) return rc;
+	if (b.el != kElMixed) return fail(XFEM_EINVAL, "not a mesh mixing tets and hexes");
+	const uint32_t morton = no_morton ? 0u : 1u;
+	vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
+	if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 8, morton, b.esched) ||
+	    elem_schedule(b.nodes.data(), b.nv, b.tets.data(), b.nt, 4, morton, b.tsched))
+		return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+	if (tet_order) memcpy(tet_order, b.tsched.order.data(), b.tsched.order.size() * 4);
+	if (tet_colour_begin) memcpy(tet_colour_begin, b.tsched.colour_begin.data(), b.tsched.colour_begin.size() * 4);
+	if (tet_ncolours) *tet_ncolours = b.tsched.ncolours;
+	return elem_schedule_out(b, vert_rank, hex_order, hex_colour_begin, hex_ncolours);
 }
 
 int xfem_compute_hex_rest_state(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,

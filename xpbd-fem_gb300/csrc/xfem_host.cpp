@@ -124,6 +124,54 @@ int parse_hexes(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& 
 	return 0;
 }
 
+int parse_mixed(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& tets, std::vector<uint32_t>& hexes,
+                uint32_t& nverts) {
+	tets.clear();
+	hexes.clear();
+	uint32_t mx = 0;
+	bool any = false;
+	for (uint64_t i = 0; i < idx_count;) {
+		const uint32_t tag = idx[i];
+		if ((tag != 4u && tag != 8u) || i + tag >= idx_count) return -1;
+		std::vector<uint32_t>& out = tag == 4u ? tets : hexes;
+		for (uint32_t n = 0; n < tag; n++) {
+			const uint32_t v = idx[i + 1 + n];
+			mx = v > mx ? v : mx;
+			out.push_back(v);
+		}
+		any = true;
+		i += tag + 1;
+	}
+	nverts = any ? mx + 1 : 0;
+	return 0;
+}
+
+void mixed_init_rest(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, const uint32_t* hexes,
+                     uint32_t nhexes, float density, float* ep, float* hep, float* w, uint8_t* vflags) {
+	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};
+	for (uint32_t i = 0; i < nverts; i++) {
+		w[i] = 0.0f;
+		for (int k = 0; k < 3; k++) {
+			mn[k] = fminf(mn[k], nodes[3 * (size_t)i + k]);
+			mx[k] = fmaxf(mx[k], nodes[3 * (size_t)i + k]);
+		}
+	}
+	for (uint32_t i = 0; i < nverts; i++) vflags[i] = rest::vertex_flags(nodes[3 * (size_t)i], mn[0], mx[0]);
+	// the tets' lumped masses first, then the hexes' (XPBDFEM/Geo.cpp:733-742)
+	for (uint32_t t = 0; t < ntets; t++) {
+		const uint32_t* is = tets + 4 * (size_t)t;
+		const float dm = rest::tet(nodes, is, density, ep + 17 * (size_t)t);
+		for (int n = 0; n < 4; n++) w[is[n]] += dm;
+	}
+	for (uint32_t h = 0; h < nhexes; h++) {
+		const uint32_t* is = hexes + 8 * (size_t)h;
+		float m[8];
+		rest::hex(nodes, is, density, hep + (size_t)rest::kHexRec * h, m);
+		for (int n = 0; n < 8; n++) w[is[n]] += m[n];
+	}
+	for (uint32_t i = 0; i < nverts; i++) w[i] = 1.0f / w[i];
+}
+
 void hex_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, float density,
                    float* hep, float* w, uint8_t* vflags) {
 	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};

@@ -83,6 +83,16 @@ struct RingSchedule {
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
                         const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe = 4);
 
+// A tagged stream that may mix tets (tag 4) and hexes (tag 8), each kind in
+// stream order; -1 on another tag or a truncated record.
+int parse_mixed(const uint32_t* idx, uint32_t count, std::vector<uint32_t>& tets, std::vector<uint32_t>& hexes,
+                uint32_t& nverts);
+// GeoLinear3d::Init on a mixed mesh (XPBDFEM/Geo.cpp:697-745): tet records
+// (17 floats), hex records (rest::kHexRec), the masses of all tets then all
+// hexes summed per vertex and inverted, the Left / Right flags.
+void mixed_init_rest(const float* nodes, uint32_t nverts, const uint32_t* tets, uint32_t ntets, const uint32_t* hexes,
+                     uint32_t nhexes, float density, float* ep, float* hep, float* w, uint8_t* vflags);
+
 // Linear hexahedra (H8). The tagged index stream with tag 8 (8 vertex ids
 // per hex); -1 on another tag or a truncated record.
 int parse_hexes(const uint32_t* idx, uint32_t idx_count, std::vector<uint32_t>& hexes, uint32_t& nverts);
@@ -196,6 +206,8 @@ struct BodyParams {
 	uint32_t lock_right;      // Settings_LockRight: hold the Right vertices at DevCtx::right_target
 	float a_ring;             // the continuous-pressure models' (J - a)^2 on hexes: a = 1 + (1 - 2 nu)
 	                          // (ContinuousPixar) or 1 / (2 nu) (XPBDFEM/Fem.cpp:1016)
+	uint32_t nhexes;          // hexes of a body mixing tets and hexes (its hex damping slices)
+	uint32_t pad5[3];
 };
 
 // Energy models on linear tets, as the solve treats them (BodyParams::model).
@@ -331,8 +343,19 @@ struct DevCtx {
 	const uint32_t* colour_el_begin;  // el_colours + 1
 	const uint32_t* el_flat;
 	uint32_t nel;
-	uint32_t pad6;
+	uint32_t mt_colours;
 	const float* el_tab;
+	// Meshes mixing tets and hexes (xfem_hexes.cu, k_mixed): the hexes as
+	// above, the tets as elements of their own colouring: mt_vid the four
+	// device vertex ids, mt_rec five float4 per tet as a structure of arrays
+	// (float4 k of tet i at mt_rec[k * nmt + i]: Qi column-major, QQ, QR,
+	// rest volume, surface area), mt_flat each tet's index in its body's tet
+	// order.
+	const uint4* mt_vid;
+	const float4* mt_rec;
+	const uint32_t* colour_mt_begin;  // mt_colours + 1
+	const uint32_t* mt_flat;
+	uint32_t nmt;
 };
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
@@ -421,6 +444,9 @@ int launch_hexes(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* st
 // substeps of one-ring solves over the hexes, a cooperative persistent
 // launch (canonical (X, V) in and out).
 int launch_hex_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// Meshes mixing tets and hexes (xfem_hexes.cu): nsub substeps, every tet
+// colour then every hex colour per sweep, a cooperative persistent launch.
+int launch_mixed(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-tet mode (xfem_t10.cu): nsub substeps of a T10 mesh, likewise.
 int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp

@@ -61,77 +61,6 @@ __device__ __forceinline__ void tape_tet(const DevCtx& C, uint32_t s, uint32_t r
 // ---- damping after the velocity update (GeoLinear3d::Damp) ------------------
 // State during the damping sweeps: vert[2v] = (X, w), vert[2v+1] = (V, bits).
 
-// DampElement (XPBDFEM/Fem.cpp:908-931): energies and gradients of the tet at
-// its current positions, then RayleighDamp (XPBDFEM/Xpbd.h:217-263) on its
-// velocities: one constraint for the Pixar models, the pair for the others,
-// nothing for the cube models. damp: the Rayleigh ratio (x 8 when amortized).
-__device__ __forceinline__ void rayleigh_tet(const Mat& bp, const TetRec& r, const float4 X[4], float4 V[4],
-                                             float inv_dt, float damp) {
-	if (bp.model == kModelNone) return;  // SolveElementCube damps quads and hexes only
-	const float q[3][3] = {{r.a.x, r.a.y, r.a.z}, {r.a.w, r.b.x, r.b.y}, {r.b.z, r.b.w, r.c.x}};
-	const float QQ[3] = {r.c.y, r.c.z, r.c.w};
-	const float QR[3] = {r.d.x, r.d.y, r.d.z};
-	const float w[4] = {X[0].w, X[1].w, X[2].w, X[3].w};
-	Vec3 P[3];
-#pragma unroll
-	for (int i = 0; i < 3; i++) P[i] = {X[i].x - X[3].x, X[i].y - X[3].y, X[i].z - X[3].z};
-	Vec3 g0[4], g1[4];
-	const float ib0 = r.d.w * inv_dt / damp, ib1 = ib0 * bp.ratio;  // comp / (dt damping)
-	if (bp.model == kModelPixar) {
-		// SolveElementPixar with DampingMode::On (XPBDFEM/Fem.cpp:429-430): one constraint
-		const float U = pixar_energy(bp, q, QQ, QR, P, g0, g1);
-		float gV = 0.0f;
-#pragma unroll
-		for (int n = 0; n < 4; n++) gV = fmaf(g0[n].x, V[n].x, fmaf(g0[n].y, V[n].y, fmaf(g0[n].z, V[n].z, gV)));
-		const float l = -gV / fmaf(2.0f * U, ib0, wdot(w, g0, g0));
-#pragma unroll
-		for (int n = 0; n < 4; n++) {
-			const float s = w[n] * l;
-			V[n].x = fmaf(s, g0[n].x, V[n].x);
-			V[n].y = fmaf(s, g0[n].y, V[n].y);
-			V[n].z = fmaf(s, g0[n].z, V[n].z);
-		}
-		return;
-	}
-	const float U0 = deviatoric<true>(bp, QQ, QR, P, g0);
-	const float U1 = hydrostatic(q, P, bp.a, g1);
-	if (bp.simultaneous) {
-		float b0 = 0.0f, b1 = 0.0f;
-#pragma unroll
-		for (int n = 0; n < 4; n++) {
-			b0 -= fmaf(g0[n].x, V[n].x, fmaf(g0[n].y, V[n].y, g0[n].z * V[n].z));
-			b1 -= fmaf(g1[n].x, V[n].x, fmaf(g1[n].y, V[n].y, g1[n].z * V[n].z));
-		}
-		float l0, l1;
-		cramer(fmaf(2.0f * U0, ib0, wdot(w, g0, g0)), wdot(w, g0, g1), fmaf(2.0f * U1, ib1, wdot(w, g1, g1)), b0, b1, l0,
-		       l1);
-#pragma unroll
-		for (int n = 0; n < 4; n++) {
-			V[n].x = fmaf(w[n], fmaf(l1, g1[n].x, l0 * g0[n].x), V[n].x);
-			V[n].y = fmaf(w[n], fmaf(l1, g1[n].y, l0 * g0[n].y), V[n].y);
-			V[n].z = fmaf(w[n], fmaf(l1, g1[n].z, l0 * g0[n].z), V[n].z);
-		}
-	} else {
-		const Vec3* gs[2] = {g0, g1};
-		const float Us[2] = {U0, U1}, ibs[2] = {ib0, ib1};
-#pragma unroll
-		for (int k = 0; k < 2; k++) {
-			const Vec3* g = gs[k];
-			float gV = 0.0f;
-#pragma unroll
-			for (int n = 0; n < 4; n++) gV = fmaf(g[n].x, V[n].x, fmaf(g[n].y, V[n].y, fmaf(g[n].z, V[n].z, gV)));
-			const float l = -gV / fmaf(2.0f * Us[k], ibs[k], wdot(w, g, g));
-#pragma unroll
-			for (int n = 0; n < 4; n++) {
-				const float s = w[n] * l;
-				V[n].x = fmaf(s, g[n].x, V[n].x);
-				V[n].y = fmaf(s, g[n].y, V[n].y);
-				V[n].z = fmaf(s, g[n].z, V[n].z);
-			}
-		}
-	}
-}
-
 // Whether tet row `row` (lane `lane`) of body bp is damped at this tick, and
 // with which Rayleigh ratio and PBD fraction (XPBDFEM/Geo.cpp:346-352,
 // 792-798): the amortized type damps one eighth of the body's order per

@@ -102,7 +102,7 @@ EXPORTS = [
     "xfem_body_t10_count", "xfem_get_t10_rest_state", "xfem_get_t10_schedule", "xfem_compute_t10_edges",
     "xfem_compute_t10_rest_state", "xfem_compute_t10_schedule", "xfem_body_h27_count", "xfem_get_h27_rest_state",
     "xfem_get_h27_schedule", "xfem_compute_h27_mesh", "xfem_compute_h27_rest_state", "xfem_compute_h27_schedule",
-    "xfem_test_hook",
+    "xfem_test_hook", "xfem_get_mixed_tet_schedule", "xfem_compute_mixed_rest_state", "xfem_compute_mixed_schedule",
 ]
 HEX_EP = 120  # floats per hex rest-state record (ElementParamsLinearHex flattened)
 T10_EP = 56  # floats per T10 rest-state record (ElementParamsQuadraticTet flattened)
@@ -172,6 +172,9 @@ def lib():
         L.xfem_compute_h27_mesh.argtypes = [P, u32, P, P, P, P, P]
         L.xfem_compute_h27_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P, P]
         L.xfem_compute_h27_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P]
+        L.xfem_get_mixed_tet_schedule.argtypes = [P, u32, P, P, P]
+        L.xfem_compute_mixed_rest_state.argtypes = [P, u32, P, u32, f32, P, P, P, P]
+        L.xfem_compute_mixed_schedule.argtypes = [P, u32, P, u32, u32, P, P, P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -256,6 +259,49 @@ def compute_hex_schedule(node_data, idx_data, morton=True):
     _check(lib().xfem_compute_hex_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(order),
                                            _p(cb), C.byref(ncol)))
     return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+
+def _mixed_counts(idx_data):
+    """(tets, hexes) of a tagged stream of tets (tag 4) and hexes (tag 8)."""
+    nt = nh = i = 0
+    while i < idx_data.size:
+        tag = int(idx_data[i])
+        nt += tag == 4
+        nh += tag == 8
+        i += tag + 1
+    return nt, nh
+
+
+def compute_mixed_rest_state(node_data, idx_data, density):
+    """Host-only rest state of a mesh mixing tets and hexes (no GPU):
+    (ep[nt, 17], hep[nh, 120], w[nv], flags[nv])."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nt, nh = _mixed_counts(ix)
+    nv = nd.size // 3
+    ep = np.zeros((nt, 17), np.float32)
+    hep = np.zeros((nh, HEX_EP), np.float32)
+    w = np.zeros(nv, np.float32)
+    fl = np.zeros(nv, np.uint8)
+    _check(lib().xfem_compute_mixed_rest_state(_p(nd), nd.size, _p(ix), ix.size, density, _p(ep), _p(hep), _p(w),
+                                               _p(fl)))
+    return ep, hep, w, fl
+
+
+def compute_mixed_schedule(node_data, idx_data, morton=True):
+    """Host-only schedule of a mesh mixing tets and hexes (no GPU): vertex
+    ranks, the tets' and the hexes' colourings."""
+    nd = np.ascontiguousarray(node_data, np.float32).reshape(-1)
+    ix = np.ascontiguousarray(idx_data, np.uint32).reshape(-1)
+    nt, nh = _mixed_counts(ix)
+    rank = np.zeros(nd.size // 3, np.uint32)
+    to, ho = np.zeros(nt, np.uint32), np.zeros(nh, np.uint32)
+    tcb, hcb = np.zeros(nt + 1, np.uint32), np.zeros(nh + 1, np.uint32)
+    tn, hn = C.c_uint32(), C.c_uint32()
+    _check(lib().xfem_compute_mixed_schedule(_p(nd), nd.size, _p(ix), ix.size, 0 if morton else 1, _p(rank), _p(to),
+                                             _p(tcb), C.byref(tn), _p(ho), _p(hcb), C.byref(hn)))
+    return dict(vert_rank=rank, tet_order=to, colour_tet_begin=tcb[:tn.value + 1], tet_colours=tn.value,
+                hex_order=ho, colour_hex_begin=hcb[:hn.value + 1], hex_colours=hn.value)
 
 
 def compute_t10_edges(idx_data):
@@ -554,6 +600,16 @@ class Body:
         ncol = C.c_uint32()
         _check(lib().xfem_get_hex_schedule(self._h, body, _p(rank), _p(order), _p(cb), C.byref(ncol)))
         return dict(vert_rank=rank, hex_order=order, colour_hex_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def mixed_tet_schedule(self, body=0):
+        """The tets' own colouring of a mesh mixing tets and hexes: tet order
+        (colour-major, caller ids) and colour offsets."""
+        nt = self.counts[body][1]
+        order = np.zeros(nt, np.uint32)
+        cb = np.zeros(nt + 1, np.uint32)
+        ncol = C.c_uint32()
+        _check(lib().xfem_get_mixed_tet_schedule(self._h, body, _p(order), _p(cb), C.byref(ncol)))
+        return dict(tet_order=order, colour_tet_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     def h27_count(self, body=0):
         """(H27s, edge nodes, face nodes) of an H27 body."""
