@@ -66,10 +66,13 @@ UNIT = "tet-substeps/s"
 # QR, volume) + 76 B per vertex per substep (X, V, O read/write 24 B each,
 # w 4 B) x V/T.
 REC_BYTES, VERT_BYTES = 80.0, 76.0
-# DRAM bytes (read + write) per tet-substep of the persistent kernel, from the
-# ncu capture of the same command (one k_persistent launch, --set full).
-# (2.143 GB per launch of 20 substeps x 1,572,864 tets).
-NCU_DRAM_BYTES_PER_TET_SUBSTEP = 68.12
+# DRAM bytes (read + write) per tet-substep of each launch form's kernel, from
+# the ncu capture of the same command (one launch, --set full): k_persistent
+# 2.143 GB per launch of 20 substeps x 1,572,864 tets.
+NCU_DRAM_BYTES_PER_TET_SUBSTEP = {"k_persistent": 68.12}
+# Launch forms (xfem_options.sync_mode) and the kernel each one times.
+SYNC_NAMES = {1: "persistent", 2: "cuda-graph", 3: "dataflow", 4: "bricks"}
+SYNC_KERNELS = {1: "k_persistent", 3: "k_dataflow", 4: "k_bricks"}
 
 
 def peaks():
@@ -242,7 +245,8 @@ def run_xfem(args, world, rank, local):
     S = w["substeps"]
     stream = torch.cuda.Stream(device=dev)
     body = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], device=local,
-                     stream=C_void_p(stream.cuda_stream), sync_mode=args.sync_mode, block_size=args.block)
+                     stream=C_void_p(stream.cuda_stream), sync_mode=args.sync_mode, block_size=args.block,
+                     bricks=args.bricks)
     body.set_lock_mask(w["lock"])
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
     for _ in range(args.warmup):
@@ -298,9 +302,11 @@ def run_xfem(args, world, rank, local):
     hbm, peak_kind = peaks()
     bpu = REC_BYTES + VERT_BYTES * nv / nt
     per_launch_ms = statistics.mean(ms)
-    launches_per_frame = 1 if info["sync_mode"] in (1, 3) else S * info["colours"] + 1
+    launches_per_frame = 1 if info["sync_mode"] != 2 else S * info["colours"] + 1
     achieved = bpu * nt * S / (per_launch_ms / 1e3) / 1e9
-    traffic = None if NCU_DRAM_BYTES_PER_TET_SUBSTEP is None else NCU_DRAM_BYTES_PER_TET_SUBSTEP * nt * S
+    kernel = SYNC_KERNELS.get(info["sync_mode"], "k_colour (whole frame)")
+    dram = NCU_DRAM_BYTES_PER_TET_SUBSTEP.get(kernel)
+    traffic = None if dram is None else dram * nt * S
     cpu = cpu_baseline_native(w) if not args.no_cpu else None
     batched = None if args.no_batched else run_batched(stream)
     adjoint = None if args.no_adjoint else run_adjoint(stream)
@@ -321,11 +327,11 @@ def run_xfem(args, world, rank, local):
         "config": {"workload": w["name"], "tets": nt, "vertices": nv, "substeps_per_step": S,
                    "dt": w["dt"], "parallelism": f"replicas{world}", "l2": "flushed between steps (256 MB write)",
                    "colours": info["colours"], "clusters": info["clusters"], "sync_mode":
-                   {1: "persistent", 2: "cuda-graph", 3: "dataflow"}[info["sync_mode"]], "block": info["block_size"],
+                   SYNC_NAMES[info["sync_mode"]], "block": info["block_size"],
                    "blocks": info["blocks"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": peak_kind, "bytes_per_tet_substep": bpu,
-                     "kernel": {1: "k_persistent", 3: "k_dataflow"}.get(info["sync_mode"], "k_colour (whole frame)"),
+                     "kernel": kernel,
                      "launch_ms": per_launch_ms},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 2 * 12 * nv, "d2h_bytes_per_step": 12 * nv,
@@ -411,7 +417,7 @@ def run_drop(stream, cpu=True, cpu_budget_s=6.0):
     achieved = bpu * nt * S / (per_frame / 1e3) / 1e9
     out = {"workload": w["name"], "frames": frames, "substeps_per_frame": S, "ms_per_frame": per_frame,
            "value": nt * S / (per_frame / 1e3), "unit": UNIT,
-           "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+           "sync_mode": SYNC_NAMES.get(info["sync_mode"]),
            "block": info["block_size"], "final_min_z": float(x[:, 2].min()),
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                         "peak_kind": peak_kind, "bytes_per_tet_substep": bpu}}
@@ -477,7 +483,7 @@ def run_batched(stream, frames=5, plain_frames=2):
     return {"workload": w["name"], "bodies": len(w["meshes"]), "tets": nt, "substeps_per_frame": 20,
             "value": nt * 20 / tb, "unit": UNIT, "ms_per_frame": 1e3 * tb,
             "plain_one_body_per_launch": nt * 20 / tp, "plain_ms_per_frame": 1e3 * tp, "speedup": tp / tb,
-            "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+            "sync_mode": SYNC_NAMES.get(info["sync_mode"]),
             "launches_per_frame": 1 if info["sync_mode"] != 2 else 20 * info["colours"] + 1}
 
 
@@ -608,7 +614,7 @@ def time_frames(stream, w, settings, flush, frames):
     body.close()
     nt = w["idx"].size // 5
     return {"ms_per_frame": statistics.median(ms), "value": nt * S / (statistics.median(ms) / 1e3),
-            "sync_mode": {1: "persistent", 2: "cuda-graph", 3: "dataflow"}.get(info["sync_mode"]),
+            "sync_mode": SYNC_NAMES.get(info["sync_mode"]),
             "block": info["block_size"]}
 
 
@@ -838,6 +844,7 @@ def main():
     ap.add_argument("--impl", default="xfem", choices=["xfem", "reference"])
     ap.add_argument("--sync-mode", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--bricks", type=int, default=0, help="bricks of the brick launch form (0: one per SM)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

@@ -155,7 +155,11 @@ typedef struct xfem_options {
 	uint32_t cluster_mode; /* 0 = default (edge-star clusters), 1 = one tet per cluster, 2 = edge-star */
 	uint32_t no_morton;    /* 1 = keep the caller's vertex order on the device */
 	uint32_t sync_mode;    /* 0 = auto (autotuned), 1 = persistent kernel + grid barrier, 2 = CUDA graph,
-	                          3 = persistent kernel, chunks wait only on neighbouring chunks (dataflow) */
+	                          3 = persistent kernel, chunks wait only on neighbouring chunks (dataflow),
+	                          4 = persistent kernel over bricks: each block owns a compact brick of cube
+	                          clusters whose own vertices stay in shared memory, and waits only on the
+	                          bricks it shares vertices with (the plain solve on meshes of whole cubes;
+	                          no damping, Pixar or cube models, volume passes or keep_lambdas) */
 	uint32_t block_size;   /* 0 = auto; else 64..1024, multiple of 32 */
 	uint32_t keep_lambdas; /* 1 = record each tet's two multipliers of the last substep */
 	int32_t device;        /* CUDA device ordinal; -1 or 0 = current / 0 */
@@ -165,6 +169,7 @@ typedef struct xfem_options {
 	uint32_t wait_timeout_ms; /* limit of every bounded device wait (grid barrier, chunk copy,
 	                             neighbour chunk); 0 = 2000 ms. A wait that runs out makes the
 	                             call report XFEM_EDEVICE_TIMEOUT and leaves the context usable */
+	uint32_t bricks;       /* sync_mode 4: number of bricks (blocks); 0 = one per SM */
 } xfem_options;
 
 /* One mesh for xfem_batch_create, in GeoLinear3d::Init's argument form. */
@@ -180,10 +185,11 @@ typedef struct xfem_info {
 	uint32_t bodies, vertices, tets, clusters, colours;
 	uint32_t isolated;        /* vertices in no tet */
 	uint32_t chunks, tet_rows, block_size, blocks;
-	uint32_t sync_mode;       /* 1 persistent + grid barrier, 2 CUDA graph, 3 persistent dataflow */
+	uint32_t sync_mode;       /* 1 persistent + grid barrier, 2 CUDA graph, 3 persistent dataflow,
+	                             4 persistent bricks */
 	uint32_t cluster_mode;    /* 1 one tet per cluster, 2 edge stars */
 	uint32_t max_chunk_deps;  /* largest neighbour-chunk list (dataflow mode) */
-	uint32_t reserved;
+	uint32_t bricks;          /* bricks of the brick layout (0: none built) */
 	uint64_t device_bytes;
 } xfem_info;
 

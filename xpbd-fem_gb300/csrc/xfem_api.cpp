@@ -158,6 +158,9 @@ struct xfem_body {
 	DevBuf<float4> el_rec;
 	DevBuf<uint32_t> el_cb, el_flat;
 	DevBuf<float> el_tab;
+	// brick launch form (sync_mode 4; built when every chunk is a cube chunk)
+	DevBuf<float4> bcblk;
+	DevBuf<uint32_t> bcb, bwait, bcnb_begin, bcnb, bpriv_begin, bpriv_vid, bfin_begin, bfin_vid, bnb_begin, bnb, bflag;
 	// meshes mixing tets and hexes (kElMixed): the tets as elements of their own colouring
 	DevBuf<uint4> mt_vid;
 	DevBuf<float4> mt_rec;
@@ -981,6 +984,215 @@ int build_mixed_tets(xfem_body* h) {
 	return XFEM_OK;
 }
 
+// The brick layout of the launch form sync_mode 4 (k_bricks), built from the
+// packed cube chunks. Clusters are sorted by their lowest device vertex (a
+// Morton rank, so nearby clusters sort together) and cut into `nbricks`
+// runs of equal length: the bricks. A brick's clusters of one colour form its
+// chunks of that colour, in the colour's own order. A vertex whose clusters
+// all lie in one brick gets a slot in that brick's shared memory (up to
+// `slot_cap` per brick; the rest stay in vert). Bricks are neighbours when
+// they share a vertex. The results do not depend on the split: the colours
+// and the clusters are those of the other launch forms.
+int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vector<float4>& cblk,
+                 const std::vector<ChunkMeta>& meta, const std::vector<uint32_t>& lane_dv,
+                 const std::vector<uint8_t>& lane_nv) {
+	const uint32_t ncol = h->ncolours, nch = (uint32_t)meta.size();
+	int sms = 0, optin = 0;
+	XCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+	XCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+	const int64_t cap = ((int64_t)optin - 8 * (int64_t)kBrickChunkBytes - 4096) / kBrickVertexBytes;
+	if (cap <= 0 || ncol > 64) return XFEM_OK;
+	// populated lanes, keyed by their lowest device vertex
+	std::vector<uint64_t> lanes;
+	std::vector<uint32_t> chunk_colour(nch);
+	for (uint32_t c = 0; c < ncol; c++)
+		for (uint32_t k = ccb[c]; k < ccb[c + 1]; k++) chunk_colour[k] = c;
+	for (size_t i = 0; i < (size_t)nch * kLanes; i++) {
+		if (!lane_nv[i]) continue;
+		uint32_t key = 0xffffffffu;
+		for (uint32_t sl = 0; sl < lane_nv[i]; sl++) key = std::min(key, lane_dv[i * kMaxClusterVerts + sl]);
+		lanes.push_back((uint64_t)key << 32 | (uint64_t)i);
+	}
+	if (lanes.empty()) return XFEM_OK;
+	std::sort(lanes.begin(), lanes.end());
+	const uint64_t L = lanes.size();
+	// one brick per SM (or xfem_options.bricks), about one chunk per brick and colour at least
+	const uint64_t want = h->opt.bricks ? (uint64_t)h->opt.bricks : (uint64_t)sms;
+	const uint32_t nb = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, L / ((uint64_t)kLanes * ncol)));
+	std::vector<uint32_t> brick_of((size_t)nch * kLanes, 0xffffffffu);
+	for (uint64_t j = 0; j < L; j++) brick_of[(uint32_t)lanes[j]] = (uint32_t)(j * nb / L);
+	// (vertex, brick) incidences
+	std::vector<uint64_t> vb;
+	vb.reserve(L * kMaxClusterVerts);
+	for (uint64_t j = 0; j < L; j++) {
+		const uint32_t i = (uint32_t)lanes[j];
+		for (uint32_t sl = 0; sl < lane_nv[i]; sl++) vb.push_back((uint64_t)lane_dv[(size_t)i * kMaxClusterVerts + sl] << 32 | brick_of[i]);
+	}
+	std::sort(vb.begin(), vb.end());
+	vb.erase(std::unique(vb.begin(), vb.end()), vb.end());
+	std::vector<uint32_t> slot(h->nverts, 0xffffffffu), npriv(nb, 0);
+	std::vector<std::vector<uint32_t>> priv(nb), fin(nb);
+	std::vector<std::vector<uint32_t>> nbl(nb);
+	for (size_t a = 0; a < vb.size();) {
+		size_t e = a + 1;
+		while (e < vb.size() && (vb[e] >> 32) == (vb[a] >> 32)) e++;
+		const uint32_t v = (uint32_t)(vb[a] >> 32), b0 = (uint32_t)vb[a];
+		if (e - a == 1 && npriv[b0] < (uint64_t)cap) {
+			slot[v] = npriv[b0]++;
+			priv[b0].push_back(v);
+		} else {
+			fin[b0].push_back(v);  // the lowest brick touching it finalizes it
+			for (size_t x = a; x < e; x++)
+				for (size_t y = a; y < e; y++)
+					if (x != y) nbl[(uint32_t)vb[x]].push_back((uint32_t)vb[y]);
+		}
+		a = e;
+	}
+	std::vector<uint32_t> pbeg(nb + 1, 0), pvid, fbeg(nb + 1, 0), fvid, nbeg(nb + 1, 0), nbv;
+	uint32_t pmax = 0;
+	for (uint32_t b = 0; b < nb; b++) {
+		pbeg[b] = (uint32_t)pvid.size();
+		pvid.insert(pvid.end(), priv[b].begin(), priv[b].end());
+		pmax = std::max(pmax, (uint32_t)priv[b].size());
+		fbeg[b] = (uint32_t)fvid.size();
+		fvid.insert(fvid.end(), fin[b].begin(), fin[b].end());
+		std::sort(nbl[b].begin(), nbl[b].end());
+		nbl[b].erase(std::unique(nbl[b].begin(), nbl[b].end()), nbl[b].end());
+		nbeg[b] = (uint32_t)nbv.size();
+		nbv.insert(nbv.end(), nbl[b].begin(), nbl[b].end());
+	}
+	pbeg[nb] = (uint32_t)pvid.size();
+	fbeg[nb] = (uint32_t)fvid.size();
+	nbeg[nb] = (uint32_t)nbv.size();
+	// brick chunks: brick-major, colour-major inside a brick. Inside a brick
+	// and colour the clusters touching a vertex of another brick (boundary)
+	// come first, in the colour's own order, then the others (interior); the
+	// chunks up to the one holding the last boundary cluster wait for the
+	// neighbouring bricks, the rest run at once.
+	std::vector<std::vector<uint32_t>> bc((size_t)nb * ncol), bi((size_t)nb * ncol);
+	for (uint32_t k = 0; k < nch; k++)
+		for (uint32_t lane = 0; lane < kLanes; lane++) {
+			const uint32_t i = k * kLanes + lane;
+			if (brick_of[i] == 0xffffffffu) continue;
+			bool bnd = false;
+			for (uint32_t sl = 0; sl < lane_nv[i]; sl++) bnd = bnd || slot[lane_dv[(size_t)i * kMaxClusterVerts + sl]] == 0xffffffffu;
+			(bnd ? bc : bi)[(size_t)brick_of[i] * ncol + chunk_colour[k]].push_back(i);
+		}
+	// per brick and colour, the bricks its boundary clusters wait for: for
+	// each vertex of such a cluster, the brick of the cluster that touched it
+	// last before (the highest lower colour touching it, else the highest
+	// colour, in the previous substep), when that is another brick
+	std::vector<uint64_t> touch;  // vertex << 32 | colour << 16 | brick
+	touch.reserve(L * kMaxClusterVerts);
+	for (uint32_t k = 0; k < nch; k++)
+		for (uint32_t lane = 0; lane < kLanes; lane++) {
+			const uint32_t i = k * kLanes + lane;
+			if (brick_of[i] == 0xffffffffu) continue;
+			for (uint32_t sl = 0; sl < lane_nv[i]; sl++)
+				touch.push_back((uint64_t)lane_dv[(size_t)i * kMaxClusterVerts + sl] << 32 |
+				                (uint64_t)chunk_colour[k] << 16 | brick_of[i]);
+		}
+	std::sort(touch.begin(), touch.end());
+	std::vector<std::vector<uint32_t>> nbc_l((size_t)nb * ncol);
+	for (size_t a = 0; a < touch.size();) {
+		size_t e = a + 1;
+		while (e < touch.size() && (touch[e] >> 32) == (touch[a] >> 32)) e++;
+		for (size_t x = a; x < e; x++) {
+			const size_t prev = x > a ? x - 1 : e - 1;  // colours ascend: the previous touch, wrapping
+			const uint32_t bx = (uint32_t)(touch[x] & 0xffffu), bp = (uint32_t)(touch[prev] & 0xffffu);
+			if (bp != bx) nbc_l[(size_t)bx * ncol + ((touch[x] >> 16) & 0xffffu)].push_back(bp);
+		}
+		a = e;
+	}
+	std::vector<uint32_t> cnb_begin((size_t)nb * ncol + 1, 0), cnb;
+	for (size_t q = 0; q < nbc_l.size(); q++) {
+		std::sort(nbc_l[q].begin(), nbc_l[q].end());
+		nbc_l[q].erase(std::unique(nbc_l[q].begin(), nbc_l[q].end()), nbc_l[q].end());
+		cnb_begin[q] = (uint32_t)cnb.size();
+		cnb.insert(cnb.end(), nbc_l[q].begin(), nbc_l[q].end());
+	}
+	cnb_begin[nbc_l.size()] = (uint32_t)cnb.size();
+	std::vector<uint32_t> bcb((size_t)nb * ncol + 1, 0), bwait((size_t)nb * ncol, 0);
+	uint32_t nbc = 0;
+	size_t nbnd = 0;
+	for (size_t q = 0; q < bc.size(); q++) {
+		bcb[q] = nbc;
+		bwait[q] = nbc + (uint32_t)((bc[q].size() + kLanes - 1) / kLanes);
+		nbnd += bc[q].size();
+		bc[q].insert(bc[q].end(), bi[q].begin(), bi[q].end());
+		nbc += (uint32_t)((bc[q].size() + kLanes - 1) / kLanes);
+	}
+	bcb[bc.size()] = nbc;
+	const uint32_t per16 = kBrickChunkBytes / 16u;
+	std::vector<float4> blk((size_t)nbc * per16, make_float4(0, 0, 0, 0));
+	parallel_for((uint32_t)bc.size(), [&](uint32_t q) {
+		for (size_t j = 0; j < bc[q].size(); j++) {
+			const uint32_t i = bc[q][j], k = i / kLanes, a = i % kLanes;
+			const uint32_t dch = bcb[q] + (uint32_t)(j / kLanes), dl = (uint32_t)(j % kLanes);
+			const float4* src = &cblk[meta[k].off16];
+			float4* dst = &blk[(size_t)dch * per16];
+			for (uint32_t r = 0; r < 24; r++) dst[r * kLanes + dl] = src[r * kLanes + a];
+			const uint32_t* sw = reinterpret_cast<const uint32_t*>(src + 24 * kLanes);
+			uint32_t* dw = reinterpret_cast<uint32_t*>(dst + 24 * kLanes);
+			dw[dl] = sw[a];  // header
+			for (uint32_t sl = 0; sl < 8; sl++) {
+				const uint32_t v = sw[kLanes + sl * kLanes + a];
+				dw[kLanes + sl * kLanes + dl] = slot[v] != 0xffffffffu ? (kPrivate | slot[v]) : v;
+			}
+		}
+	});
+	XCUDA(h->bcblk.alloc(blk.size()));
+	XCUDA(h->bcb.alloc(bcb.size()));
+	XCUDA(h->bwait.alloc(bwait.size()));
+	XCUDA(h->bcnb_begin.alloc(cnb_begin.size()));
+	XCUDA(h->bcnb.alloc(std::max<size_t>(1, cnb.size())));
+	XCUDA(h->bpriv_begin.alloc(pbeg.size()));
+	XCUDA(h->bpriv_vid.alloc(std::max<size_t>(1, pvid.size())));
+	XCUDA(h->bfin_begin.alloc(fbeg.size()));
+	XCUDA(h->bfin_vid.alloc(std::max<size_t>(1, fvid.size())));
+	XCUDA(h->bnb_begin.alloc(nbeg.size()));
+	XCUDA(h->bnb.alloc(std::max<size_t>(1, nbv.size())));
+	XCUDA(h->bflag.alloc((size_t)nb * kBrickFlagStride));
+	auto up = [&](void* dst, const void* src, size_t bytes) {
+		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
+	};
+	XCUDA(up(h->bcblk.p, blk.data(), blk.size() * sizeof(float4)));
+	XCUDA(up(h->bcb.p, bcb.data(), bcb.size() * 4));
+	XCUDA(up(h->bwait.p, bwait.data(), bwait.size() * 4));
+	XCUDA(up(h->bcnb_begin.p, cnb_begin.data(), cnb_begin.size() * 4));
+	XCUDA(up(h->bcnb.p, cnb.data(), cnb.size() * 4));
+	XCUDA(up(h->bpriv_begin.p, pbeg.data(), pbeg.size() * 4));
+	XCUDA(up(h->bpriv_vid.p, pvid.data(), pvid.size() * 4));
+	XCUDA(up(h->bfin_begin.p, fbeg.data(), fbeg.size() * 4));
+	XCUDA(up(h->bfin_vid.p, fvid.data(), fvid.size() * 4));
+	XCUDA(up(h->bnb_begin.p, nbeg.data(), nbeg.size() * 4));
+	XCUDA(up(h->bnb.p, nbv.data(), nbv.size() * 4));
+	XCUDA(cudaStreamSynchronize(h->stream));
+	DevCtx& c = h->ctx;
+	c.bcblk = h->bcblk.p;
+	c.bchunk_begin = h->bcb.p;
+	c.bchunk_wait_end = h->bwait.p;
+	c.bcnb_begin = h->bcnb_begin.p;
+	c.bcnb = h->bcnb.p;
+	c.bpriv_begin = h->bpriv_begin.p;
+	c.bpriv_vid = h->bpriv_vid.p;
+	c.bfin_begin = h->bfin_begin.p;
+	c.bfin_vid = h->bfin_vid.p;
+	c.bnb_begin = h->bnb_begin.p;
+	c.bnb = h->bnb.p;
+	c.bflag = h->bflag.p;
+	c.nbricks = nb;
+	c.bpriv_max = pmax;
+	h->device_bytes += blk.size() * 16 + (bcb.size() + bwait.size() + cnb_begin.size() + cnb.size() + pbeg.size() + pvid.size() + fbeg.size() + fvid.size() +
+	                                      nbeg.size() + nbv.size() + (size_t)nb * kBrickFlagStride) * 4;
+	if (getenv("XFEM_SETUP_TIMING"))
+		fprintf(stderr, "xfem bricks: %u bricks, %u chunks, %zu private and %zu shared vertices, at most %u private "
+		                "per brick, %zu neighbour links (%zu waits per substep over the colours), %zu of %zu clusters "
+		                "on a brick boundary\n",
+		        nb, nbc, pvid.size(), fvid.size(), pmax, nbv.size(), cnb.size(), nbnd, (size_t)L);
+	return XFEM_OK;
+}
+
 // Packs every body's schedule into the merged device layout and uploads it.
 int build_device(xfem_body* h) {
 	SetupClock clk;
@@ -1330,6 +1542,7 @@ int build_device(xfem_body* h) {
 	c.nchunks = nch;
 	c.bodies = h->params.p;
 	c.nverts = nverts;
+	c.nbodies = nb;
 	c.nisolated = h->nisolated;
 	c.ncolours = ncol;
 	c.bar_count = h->bar.p;
@@ -1360,12 +1573,42 @@ int build_device(xfem_body* h) {
 	h->cfg.warp_smem = c.warp_smem;
 	h->cfg.total_chunks = nch;
 	h->cfg.colour_chunk_begin_host = ccb;
+	if (all_cube && !h->ring_mode && !h->el_mode && nch && (h->opt.sync_mode == 0 || h->opt.sync_mode == 4)) {
+		const int rb = build_bricks(h, ccb, cblk, meta, lane_dv, lane_nv);
+		if (rb) return rb;
+		clk.lap("bricks");
+	}
 	return update_right_targets(h);
 }
 
 int set_config(xfem_body* h, int sync_mode, int block) {
 	int optin = 0;
 	XCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
+	if (sync_mode == 4) {
+		// the brick form: the plain solve on an all-cube handle, every brick resident
+		if (!h->ctx.nbricks)
+			return fail(XFEM_EUNSUPPORTED, "sync_mode 4 (bricks) needs a mesh whose clusters are all whole cubes "
+			                               "(the generator's blocks) and one-ring and element modes off");
+		if (h->ctx.ext || h->cfg.lambdas)
+			return fail(XFEM_EUNSUPPORTED, "sync_mode 4 (bricks) runs no damping, Pixar or cube models, volume passes "
+			                               "or multiplier output");
+		if (block != 128 && block != 192 && block != 224 && block != 256)
+			return fail(XFEM_EINVAL, "sync_mode 4 (bricks) takes blocks of 128, 192, 224 or 256 threads");
+		if (brick_smem_bytes(block, h->ctx.bpriv_max) > (size_t)optin)
+			return fail(XFEM_EINVAL, "the bricks need more shared memory than the device allows");
+		bool fits = false;
+		if (const int e = brick_grid_fits(block, h->ctx.bpriv_max, h->ctx.nbricks, &fits))
+			return fail(XFEM_ECUDA, std::string("brick kernel configuration: ") + cudaGetErrorString((cudaError_t)e));
+		if (!fits) return fail(XFEM_EUNSUPPORTED, "the bricks do not fit on the device at once");
+		h->cfg.sync_mode = 4;
+		h->cfg.block = block;
+		h->cfg.blocks = (int)h->ctx.nbricks;
+		if (h->graph) {
+			cudaGraphExecDestroy(h->graph);
+			h->graph = nullptr;
+		}
+		return XFEM_OK;
+	}
 	if (solve_smem_bytes(block, h->cfg.warp_smem) > (size_t)optin)
 		return fail(XFEM_EINVAL, "block size " + std::to_string(block) + " needs " +
 		                             std::to_string(solve_smem_bytes(block, h->cfg.warp_smem)) +
@@ -1388,7 +1631,7 @@ int set_config(xfem_body* h, int sync_mode, int block) {
 }
 
 int run(xfem_body* h, uint32_t nsub, float dt) {
-	if (h->cfg.sync_mode == 1 || h->cfg.sync_mode == 3) {
+	if (h->cfg.sync_mode == 1 || h->cfg.sync_mode == 3 || h->cfg.sync_mode == 4) {
 		const int e = launch_substeps(h->ctx, h->cfg, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("persistent launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
@@ -1424,11 +1667,14 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	// 192 and 224 as well: a colour pass of the throughput mesh has 1,024
 	// chunks (6.7 per SM), and fewer warps per block means less shared memory
 	const int blocks[] = {64, 128, 192, 224, 256};
-	for (int sm : {1, 2, 3}) {
+	for (int sm : {1, 2, 3, 4}) {
 		if (fixed_sync && sm != fixed_sync) continue;
 		if (sm == 3 && h->ctx.ext) continue;  // the dataflow kernel runs only the plain solve
+		// the brick kernel too, on all-cube handles, without multiplier output
+		if (sm == 4 && (h->ctx.ext || !h->ctx.nbricks || h->cfg.lambdas)) continue;
 		for (int bs : blocks) {
 			if (fixed_block && bs != fixed_block) continue;
+			if (sm == 4 && bs == 64) continue;
 			cand.push_back({sm, bs});
 		}
 	}
@@ -1488,7 +1734,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (options) h->opt = *options;
 	if (h->opt.block_size && (h->opt.block_size < 64 || h->opt.block_size > 1024 || h->opt.block_size % 32))
 		return fail(XFEM_EINVAL, "block_size must be a multiple of 32 in [64, 1024]");
-	if (h->opt.sync_mode > 3) return fail(XFEM_EINVAL, "sync_mode must be 0, 1, 2 or 3");
+	if (h->opt.sync_mode > 4) return fail(XFEM_EINVAL, "sync_mode must be 0, 1, 2, 3 or 4");
 	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
 	const uint32_t mode = h->opt.cluster_mode == 1 ? 0u : 1u;
 	const uint32_t morton = h->opt.no_morton ? 0u : 1u;
@@ -1523,7 +1769,8 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	clk.lap("device layout");
 	if (rc) return rc;
 	// default configuration until the first step tunes it
-	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1, h->opt.block_size ? (int)h->opt.block_size : 128);
+	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1,
+	                h->opt.block_size ? (int)h->opt.block_size : h->opt.sync_mode == 4 ? 256 : 128);
 	if (rc) return rc;
 	if (h->opt.sync_mode && h->opt.block_size) h->tuned = true;
 	*out = h.release();
@@ -1576,11 +1823,13 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 	}
 	int rc = autotune(h, nsub, dt);
 	if (rc) return rc;
-	if (h->ctx.ext && h->cfg.sync_mode == 3) {
+	if (h->ctx.ext && (h->cfg.sync_mode == 3 || h->cfg.sync_mode == 4)) {
 		// damping, a Pixar or cube model or volume passes switched on after
-		// the dataflow kernel was chosen
+		// the dataflow or the brick kernel was chosen
 		if (h->opt.sync_mode == 3)
 			return fail(XFEM_EUNSUPPORTED, "sync_mode 3 (dataflow) runs no damping, Pixar or cube models or volume passes");
+		if (h->opt.sync_mode == 4)
+			return fail(XFEM_EUNSUPPORTED, "sync_mode 4 (bricks) runs no damping, Pixar or cube models or volume passes");
 		rc = set_config(h, 1, h->cfg.block);
 		if (rc) return rc;
 	}
@@ -1695,7 +1944,7 @@ int xfem_get_info(const xfem_body* b, xfem_info* out) {
 	for (auto& x : b->bodies) ncl += x.sched.nclusters;
 	*out = {(uint32_t)b->bodies.size(), b->nverts, b->ntets, ncl, b->ncolours, b->nisolated,
 	        b->nchunks, b->nrows, (uint32_t)b->cfg.block, (uint32_t)b->cfg.blocks, (uint32_t)b->cfg.sync_mode,
-	        b->opt.cluster_mode == 1 ? 1u : 2u, b->max_deps, 0u, b->device_bytes};
+	        b->opt.cluster_mode == 1 ? 1u : 2u, b->max_deps, b->ctx.nbricks, b->device_bytes};
 	return XFEM_OK;
 }
 

@@ -143,11 +143,11 @@ __device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, f
 
 // Finalize the previous substep (unless `first`: (O, D) then hold the
 // canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312) for
-// device vertex v.
+// device vertex v. bodies: C.bodies, or a copy of them in shared memory.
 __device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, bool first, float dt,
-                                               float inv_dt) {
+                                               float inv_dt, const BodyParams* bodies = nullptr) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = C.bodies[bits >> 8];
+	const BodyParams& bp = (bodies ? bodies : C.bodies)[bits >> 8];
 	Vec3 V;
 	if (first) {
 		V = v3(D);
@@ -167,9 +167,10 @@ __device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, floa
 // device vertex v. A position or velocity that is no longer finite (a
 // diverged solve, or a NaN the caller set) is recorded in the error word as
 // kErrNonFinite, which the next synchronising call reports.
-__device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, float inv_dt) {
+__device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, float inv_dt,
+                                                const BodyParams* bodies = nullptr) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = C.bodies[bits >> 8];
+	const BodyParams& bp = (bodies ? bodies : C.bodies)[bits >> 8];
 	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt, C.right_target, v);
 	O.x += D.x;
 	O.y += D.y;
@@ -196,6 +197,14 @@ struct Mat {
 	float compliance;  // volume passes
 	uint32_t nvol;     // volume passes of the body
 };
+
+// The same from a copy of the bodies in shared memory (plain loads).
+__device__ __forceinline__ Mat load_mat_shared(const BodyParams* bodies, uint32_t body) {
+	const BodyParams& b = bodies[body];
+	const uint32_t type = b.rayleigh_type;
+	return {b.a,  b.ratio, b.yeoh[0], b.yeoh[1], b.yeoh[2], b.model, b.simultaneous, type < 2u ? b.damping : 0.0f,
+	        type == 1u ? 1u : 0u, b.hw, b.compliance, b.volume_passes};
+}
 
 __device__ __forceinline__ Mat load_mat(const BodyParams* bodies, uint32_t body) {
 	const BodyParams* b = bodies + body;

@@ -356,7 +356,49 @@ struct DevCtx {
 	const uint32_t* colour_mt_begin;  // mt_colours + 1
 	const uint32_t* mt_flat;
 	uint32_t nmt;
+	// Brick launch form (sync_mode 4, k_bricks): the clusters split into
+	// nbricks spatially compact bricks, one per block. Brick chunks: 32
+	// clusters of one brick and one colour, each block kBrickChunkBytes (the
+	// cube chunk's records and header, then the vertex words), brick b's
+	// chunks of colour c at [bchunk_begin[b * ncolours + c],
+	// bchunk_begin[b * ncolours + c + 1]). A vertex that only one brick's
+	// clusters touch lives in that block's shared memory for the whole launch
+	// (bpriv_vid: the device vertex of each slot, per brick from
+	// bpriv_begin[b]); the others stay in vert. Instead of a grid barrier a
+	// block waits after each pass for the bricks it shares vertices with
+	// (bnb, from bnb_begin[b]) through their pass counters (bflag). bfin_vid:
+	// the shared vertices each brick finalizes at the end of a launch.
+	const float4* bcblk;
+	const uint32_t* bchunk_begin;
+	const uint32_t* bchunk_wait_end;  // per brick and colour: its chunks before this one hold
+	                                  // boundary clusters and wait for the neighbours
+	const uint32_t* bcnb_begin;       // per brick and colour: the bricks those chunks wait for,
+	const uint32_t* bcnb;             // those that touched their shared vertices last before
+	const uint32_t* bpriv_begin;
+	const uint32_t* bpriv_vid;
+	const uint32_t* bfin_begin;
+	const uint32_t* bfin_vid;
+	const uint32_t* bnb_begin;
+	const uint32_t* bnb;
+	uint32_t* bflag;
+	uint32_t nbricks, bpriv_max;
+	uint32_t nbodies;
 };
+
+// Brick chunk block: records (6 x 4 x 32 float4), header (32 u32), vertex
+// words (8 x 32 u32): the device vertex id, or kPrivate | the vertex's slot
+// in the brick's shared memory.
+constexpr uint32_t kBrickChunkBytes = 2048u * 6u + 128u * (1u + 8u);
+constexpr uint32_t kPrivate = 0x80000000u;
+// Bodies whose parameters the brick kernel keeps in shared memory (handles
+// with more bodies read them from global memory).
+constexpr uint32_t kBrickBodies = 8u;
+// Shared-memory bytes per private vertex: its state (32) and device id (4).
+constexpr uint32_t kBrickVertexBytes = 36u;
+// Words between two bricks' pass counters: each in a 128-byte line of its
+// own, so that the polls of one brick's neighbours do not queue behind every
+// other brick's on a few shared lines.
+constexpr uint32_t kBrickFlagStride = 32u;
 // A substep's passes, colour-major within each kind: the solve sweep (kind
 // 0), volume sweeps 1..nvol, then one sweep per damping kind.
 
@@ -388,7 +430,8 @@ constexpr uint64_t kDefaultTimeoutNs = 2000000000ull;
 struct LaunchCfg {
 	int block = 256;
 	int blocks = 0;        // persistent grid size
-	int sync_mode = 1;     // 1 persistent + grid barrier, 2 per-colour launches (CUDA graph), 3 persistent dataflow
+	int sync_mode = 1;     // 1 persistent + grid barrier, 2 per-colour launches (CUDA graph), 3 persistent dataflow,
+	                       // 4 persistent bricks (k_bricks: brick-resident vertices, neighbour waits)
 	bool lambdas = false;
 	bool ext = false;      // launch the extended instantiations (DevCtx::ext)
 	uint32_t warp_smem = 0;
@@ -404,6 +447,12 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 int configure_kernels(const LaunchCfg& cfg);
 // Largest co-resident grid for the persistent kernel at this block size.
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out);
+// Dynamic shared memory bytes per block of the brick kernel, and whether
+// `nbricks` blocks of `block` threads fit on the device at once (the
+// cooperative launch needs the whole grid resident). Returns a cudaError_t
+// value; *fits is set on success.
+size_t brick_smem_bytes(int block, uint32_t bpriv_max);
+int brick_grid_fits(int block, uint32_t bpriv_max, uint32_t nbricks, bool* fits);
 // Dynamic shared memory bytes per block of the solve kernels.
 size_t solve_smem_bytes(int block, uint32_t warp_smem);
 

@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <mutex>
 #include <utility>
 #include <vector>
@@ -634,6 +635,267 @@ __global__ void __launch_bounds__(256) k_dataflow(DevCtx C, uint32_t nsub, float
 	if (gtid == 0) *C.tick = tick0 + nsub;
 }
 
+// ---- brick launch form (sync_mode 4) ------------------------------------------
+//
+// The clusters are split into spatially compact bricks, one per block. A
+// vertex that only one brick's clusters touch stays in that block's shared
+// memory for the whole launch; the others stay in vert (L2). A pass is the
+// brick's chunks of one colour; instead of a grid barrier the block then
+// publishes its pass count and waits for the bricks it shares vertices with.
+// Any vertex a pass reads was last written by a brick that shares it, which
+// has finished the previous pass; no brick can be more than one pass ahead of
+// a brick it shares vertices with. The colour order, the clusters and the
+// arithmetic are those of k_persistent, so the results are bit-identical.
+
+// The calling warp's brick chunk buffer and mbarrier.
+__device__ __forceinline__ Stage brick_stage_init(uint32_t lane) {
+	extern __shared__ __align__(128) uint8_t smem[];
+	__shared__ uint64_t bmbars[32];
+	const uint32_t w = threadIdx.x >> 5;
+	Stage st = {smem + (size_t)w * kBrickChunkBytes, nullptr, &bmbars[w], 0u, -1, make_uint4(0u, 0u, 0u, 0u)};
+	if (lane == 0) mbar_init(st.mbar);
+	__syncwarp();
+	return st;
+}
+
+__device__ __forceinline__ void brick_issue(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	__syncwarp();
+	if (lane == 0)
+		bulk_copy_g2s(st.buf, C.bcblk + (size_t)chunk * (kBrickChunkBytes / 16u), kBrickChunkBytes, st.mbar);
+	st.inflight = (int)chunk;
+}
+
+// Makes brick chunk `chunk` resident in the warp's buffer; false on timeout.
+__device__ __forceinline__ bool brick_acquire(const DevCtx& C, Stage& st, uint32_t chunk, uint32_t lane) {
+	if (st.inflight != (int)chunk) {
+		if (st.inflight >= 0) {
+			if (!mbar_wait(C, st.mbar, st.parity)) return false;
+			st.parity ^= 1u;
+		}
+		brick_issue(C, st, chunk, lane);
+	}
+	const bool ok = mbar_wait(C, st.mbar, st.parity);
+	st.parity ^= 1u;
+	st.inflight = -1;
+	return ok;
+}
+
+// The warp's next brick chunk after `ch` (colour c of substep s; bcb: the
+// brick's colour chunk offsets), -1 when the launch has no more for it.
+__device__ __forceinline__ int next_brick_chunk(const uint32_t* bcb, uint32_t ncol, uint32_t s, uint32_t nsub,
+                                                uint32_t c, uint32_t ch, uint32_t wib, uint32_t wpb) {
+	if (ch + wpb < bcb[c + 1]) return (int)(ch + wpb);
+	for (uint32_t k = 1; k <= ncol; k++) {
+		uint32_t c2 = c + k, s2 = s;
+		if (c2 >= ncol) {
+			c2 -= ncol;
+			s2++;
+		}
+		if (s2 >= nsub) return -1;
+		const uint32_t f = bcb[c2] + wib;
+		if (f < bcb[c2 + 1]) return (int)f;
+	}
+	return -1;
+}
+
+// One resident brick chunk (every lane a whole cube, as run_chunk_cube).
+// Vertex word w of a lane: a device vertex in vert, or kPrivate | p for the
+// brick's shared-memory slot p (state sv[2p], sv[2p + 1], device id spid[p]).
+// bodies: the body parameters (a shared-memory copy when the handle has few).
+__device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first,
+                                                float dt, float inv_dt, float inv_dt2, float4* sv,
+                                                const uint32_t* spid, const BodyParams* bodies, bool bshared) {
+	const float4* rec = reinterpret_cast<const float4*>(st.buf);
+	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
+	const uint32_t* vws = hdrs + kLanes;
+	const uint32_t hdr = hdrs[lane];
+	const bool live = (hdr & 15u) != 0;
+	const uint32_t mask = (hdr >> 8) & 0xffu;
+	uint32_t vw[8];
+	float4 O[8], D[8];
+	if (live) {
+		const Mat mat = bshared ? load_mat_shared(bodies, hdr >> 16) : load_mat(bodies, hdr >> 16);
+#pragma unroll
+		for (int s = 0; s < 8; s++) vw[s] = vws[s * kLanes + lane];
+#pragma unroll
+		for (int s = 0; s < 8; s++) {
+			if (vw[s] & kPrivate) {
+				const uint32_t p = vw[s] & ~kPrivate;
+				O[s] = sv[2 * p];
+				D[s] = sv[2 * p + 1];
+			} else {
+				ld_vertex(C.vert + 2 * (size_t)vw[s], O[s], D[s]);
+			}
+		}
+#pragma unroll
+		for (int s = 0; s < 8; s++)
+			if (mask & (1u << s)) {
+				const uint32_t v = (vw[s] & kPrivate) ? spid[vw[s] & ~kPrivate] : vw[s];
+				advance_vertex(C, v, O[s], D[s], first, dt, inv_dt, bodies);
+			}
+#pragma unroll
+		for (int t = 0; t < 6; t++) {
+			const float4* r = rec + t * 4 * kLanes + lane;
+			const TetRec tr = {r[0], r[kLanes], r[2 * kLanes], r[3 * kLanes]};
+			const float4 Ot[4] = {O[cube_slot(t, 0)], O[cube_slot(t, 1)], O[cube_slot(t, 2)], O[cube_slot(t, 3)]};
+			float4 Dt[4] = {D[cube_slot(t, 0)], D[cube_slot(t, 1)], D[cube_slot(t, 2)], D[cube_slot(t, 3)]};
+			solve_tet<false>(mat, tr, inv_dt, inv_dt2, Ot, Dt);
+#pragma unroll
+			for (int k = 0; k < 4; k++) D[cube_slot(t, k)] = Dt[k];
+		}
+	}
+	if (next >= 0) brick_issue(C, st, (uint32_t)next, lane);  // buffer consumed: prefetch
+	if (live) {
+#pragma unroll
+		for (int s = 0; s < 8; s++) {
+			if (vw[s] & kPrivate) {
+				const uint32_t p = vw[s] & ~kPrivate;
+				if (mask & (1u << s)) sv[2 * p] = O[s];
+				sv[2 * p + 1] = D[s];
+			} else if (mask & (1u << s)) {
+				st_vertex(C.vert + 2 * (size_t)vw[s], O[s], D[s]);
+			} else {
+				__stcg(C.vert + 2 * (size_t)vw[s] + 1, D[s]);
+			}
+		}
+	}
+}
+
+// Bounded wait, by the calling threads (`first` of them striding by
+// `stride`), until every brick of list[nb0, nb1) has published at least
+// `target` passes. Returns false when a wait ran out or another
+// block reported an error.
+__device__ bool brick_wait(const DevCtx& C, const uint32_t* list, uint32_t nb0, uint32_t nb1, uint32_t target,
+                           uint32_t first, uint32_t stride) {
+	target += C.wait_miss;
+	bool bad = false;
+	for (uint32_t i = nb0 + first; i < nb1 && !bad; i += stride) {
+		const uint32_t* f = C.bflag + (size_t)__ldg(list + i) * kBrickFlagStride;
+		uint32_t spins = 0;
+		uint64_t t0 = 0;
+		while ((int32_t)(ld_acquire_gpu(f) - target) < 0) {
+			if (++spins == 256) {
+				spins = 0;
+				if (*(volatile int*)C.err) {
+					bad = true;
+					break;
+				}
+				const uint64_t t = global_ns();
+				if (t0 == 0) {
+					t0 = t;
+				} else if (t - t0 > C.timeout_ns) {
+					atomicCAS(C.err, 0, kErrBarrierTimeout);
+					bad = true;
+					break;
+				}
+			}
+		}
+	}
+	return !bad;
+}
+
+// Persistent brick kernel: one block per brick (grid = nbricks, cooperative
+// launch so that every brick is resident), the plain solve only (no damping,
+// volume passes or multiplier output). The state between substeps stays
+// (O, D), and each brick finalizes its own vertices at the end.
+__global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float dt) {
+	extern __shared__ __align__(128) uint8_t smem[];
+	__shared__ uint32_t s_bcb[65], s_bwait[64];
+	__shared__ BodyParams s_bodies[kBrickBodies];
+	const float inv_dt = 1.0f / dt, inv_dt2 = 1.0f / (dt * dt);
+	const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+	const uint32_t b = blockIdx.x, ncol = C.ncolours;
+	const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
+	const uint32_t tick0 = __ldcg(C.tick);  // read before any brick publishes; block 0 advances it at the end
+	Stage st = brick_stage_init(lane);
+	float4* sv = reinterpret_cast<float4*>(smem + (size_t)wpb * kBrickChunkBytes);
+	uint32_t* spid = reinterpret_cast<uint32_t*>(sv + 2 * (size_t)C.bpriv_max);
+	for (uint32_t i = threadIdx.x; i <= ncol; i += blockDim.x) {
+		s_bcb[i] = __ldg(C.bchunk_begin + (size_t)b * ncol + i);
+		if (i < ncol) s_bwait[i] = __ldg(C.bchunk_wait_end + (size_t)b * ncol + i);
+	}
+	// few bodies: their parameters in shared memory (the advance reads them per vertex)
+	const bool bshared = C.nbodies <= kBrickBodies;
+	if (bshared) {
+		const uint32_t words = C.nbodies * (uint32_t)(sizeof(BodyParams) / 4);
+		for (uint32_t i = threadIdx.x; i < words; i += blockDim.x)
+			reinterpret_cast<uint32_t*>(s_bodies)[i] = __ldg(reinterpret_cast<const uint32_t*>(C.bodies) + i);
+	}
+	const BodyParams* bodies = bshared ? s_bodies : C.bodies;
+	// the brick's own vertices into shared memory, for the whole launch
+	const uint32_t pb = __ldg(C.bpriv_begin + b), pe = __ldg(C.bpriv_begin + b + 1);
+	for (uint32_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+		const uint32_t v = __ldg(C.bpriv_vid + i);
+		float4 O, D;
+		ld_vertex(C.vert + 2 * (size_t)v, O, D);
+		sv[2 * (i - pb)] = O;
+		sv[2 * (i - pb) + 1] = D;
+		spid[i - pb] = v;
+	}
+	__syncthreads();
+	// vertices in no tet, finalized here too (no closing pass over all vertices)
+	run_isolated(C, gtid, nthreads, nsub, dt, inv_dt, true);
+	const uint32_t nb0 = __ldg(C.bnb_begin + b), nb1 = __ldg(C.bnb_begin + b + 1);
+	// A pass: the warps whose chunk holds only interior clusters (every vertex
+	// private) start at once; a warp with a boundary cluster first waits
+	// until the neighbouring bricks have finished the previous pass (their
+	// writes to the shared vertices are visible). The block's barrier then
+	// ends the pass, and it publishes the pass count.
+	uint32_t epoch = 0;
+	bool ok = true;
+	for (uint32_t s = 0; s < nsub && ok; s++) {
+		for (uint32_t c = 0; c < ncol && ok; c++) {
+			const uint32_t wend = s_bwait[c];
+			bool bad = false, waited = false;
+			for (uint32_t ch = s_bcb[c] + wib; ch < s_bcb[c + 1] && !bad; ch += wpb) {
+				if (ch < wend && !waited) {
+					const uint32_t q = b * ncol + c;
+					bad = __any_sync(0xffffffffu, !brick_wait(C, C.bcnb, __ldg(C.bcnb_begin + q),
+					                                             __ldg(C.bcnb_begin + q + 1), epoch, lane, 32u));
+					__syncwarp();  // orders every lane's loads after the lanes' acquires
+					waited = true;
+					if (bad) break;
+				}
+				if (!brick_acquire(C, st, ch, lane)) {
+					bad = true;
+					break;
+				}
+				const int next = next_brick_chunk(s_bcb, ncol, s, nsub, c, ch, wib, wpb);
+				run_chunk_brick(C, st, next, lane, s == 0, dt, inv_dt, inv_dt2, sv, spid, bodies, bshared);
+			}
+			if (__syncthreads_or(bad ? 1 : 0)) {
+				ok = false;
+				break;
+			}
+			++epoch;
+			// the release store orders every write of the pass that the
+			// barrier made visible to this thread before the count
+			if (threadIdx.x == 0) st_release_gpu(C.bflag + (size_t)b * kBrickFlagStride, epoch);
+		}
+	}
+	// every brick sharing a vertex with this one has finished the last pass
+	if (ok) ok = !__syncthreads_or(brick_wait(C, C.bnb, nb0, nb1, epoch, threadIdx.x, blockDim.x) ? 0 : 1);
+	if (!ok) {
+		if (st.inflight >= 0) mbar_wait(C, st.mbar, st.parity);  // leave no copy in flight
+		return;
+	}
+	for (uint32_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+		const uint32_t v = __ldg(C.bpriv_vid + i);
+		float4 O = sv[2 * (i - pb)], D = sv[2 * (i - pb) + 1];
+		finalize_vertex(C, v, O, D, inv_dt, bodies);
+		st_vertex(C.vert + 2 * (size_t)v, O, D);
+	}
+	const uint32_t fb = __ldg(C.bfin_begin + b), fe = __ldg(C.bfin_begin + b + 1);
+	for (uint32_t i = fb + threadIdx.x; i < fe; i += blockDim.x) {
+		const uint32_t v = __ldg(C.bfin_vid + i);
+		float4 O, D;
+		ld_vertex(C.vert + 2 * (size_t)v, O, D);
+		finalize_vertex(C, v, O, D, inv_dt, bodies);
+		st_vertex(C.vert + 2 * (size_t)v, O, D);
+	}
+	if (gtid == 0) *C.tick = tick0 + nsub;
+}
+
 // One colour pass as its own launch (CUDA-graph mode): one chunk per warp.
 // kind 0 is the solve pass (first: the state is canonical), 1..nvol the
 // volume passes, the rest the damping passes (damp_kind); sub: the substep's
@@ -808,6 +1070,22 @@ int configure_kernels(const LaunchCfg& cfg) {
 	return (int)e;
 }
 
+size_t brick_smem_bytes(int block, uint32_t bpriv_max) {
+	return (size_t)(block / 32) * kBrickChunkBytes + (size_t)bpriv_max * kBrickVertexBytes;
+}
+
+int brick_grid_fits(int block, uint32_t bpriv_max, uint32_t nbricks, bool* fits) {
+	const size_t smem = brick_smem_bytes(block, bpriv_max);
+	cudaError_t e = set_smem_attr((const void*)k_bricks, smem);
+	int dev = 0, sms = 0, per_sm = 0;
+	if (e == cudaSuccess) e = cudaGetDevice(&dev);
+	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_bricks, block, smem);
+	if (e != cudaSuccess) return (int)e;
+	*fits = (uint64_t)per_sm * (uint64_t)sms >= nbricks && nbricks > 0;
+	return 0;
+}
+
 int persistent_grid(const LaunchCfg& cfg, int* blocks_out) {
 	const void* f = cfg.sync_mode == 3
 	                    ? (cfg.lambdas ? (const void*)k_dataflow<true> : (const void*)k_dataflow<false>)
@@ -827,6 +1105,23 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 	const size_t smem = solve_smem_bytes(cfg.block, cfg.warp_smem);
 	cudaError_t e = cudaSuccess;
 	if (nsub == 0) return 0;
+	if (cfg.sync_mode == 4) {
+		// pass counters start at 0; one launch counts at most 2^30 passes
+		const size_t smem_b = brick_smem_bytes(cfg.block, ctx.bpriv_max);
+		const uint32_t per = std::max(1u, (1u << 30) / std::max(1u, ctx.ncolours));
+		for (uint32_t done = 0; done < nsub;) {
+			uint32_t n = std::min(per, nsub - done);
+			e = cudaMemsetAsync(ctx.bflag, 0, sizeof(uint32_t) * kBrickFlagStride * ctx.nbricks, st);
+			if (e != cudaSuccess) return (int)e;
+			DevCtx c = ctx;
+			float dtv = dt;
+			void* args[] = {&c, &n, &dtv};
+			e = cudaLaunchCooperativeKernel((const void*)k_bricks, dim3(ctx.nbricks), dim3(cfg.block), args, smem_b, st);
+			if (e != cudaSuccess) return (int)e;
+			done += n;
+		}
+		return 0;
+	}
 	if (cfg.sync_mode == 1 || cfg.sync_mode == 3) {
 		e = reset_barrier(ctx, st);
 		if (e == cudaSuccess && cfg.sync_mode == 3) e = cudaMemsetAsync(ctx.done, 0, sizeof(uint32_t) * ctx.nchunks, st);

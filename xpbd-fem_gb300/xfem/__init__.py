@@ -73,6 +73,7 @@ class Options(C.Structure):
         ("cluster_mode", C.c_uint32), ("no_morton", C.c_uint32), ("sync_mode", C.c_uint32),
         ("block_size", C.c_uint32), ("keep_lambdas", C.c_uint32), ("device", C.c_int32),
         ("stream", C.c_void_p), ("host_setup", C.c_uint32), ("wait_timeout_ms", C.c_uint32),
+        ("bricks", C.c_uint32),
     ]
 
 
@@ -84,7 +85,7 @@ class Mesh(C.Structure):
 class Info(C.Structure):
     _fields_ = [(n, C.c_uint32) for n in ("bodies", "vertices", "tets", "clusters", "colours", "isolated",
                                           "chunks", "tet_rows", "block_size", "blocks", "sync_mode",
-                                          "cluster_mode", "max_chunk_deps", "reserved")] + [("device_bytes", C.c_uint64)]
+                                          "cluster_mode", "max_chunk_deps", "bricks")] + [("device_bytes", C.c_uint64)]
 
 
 # every symbol include/xfem.h declares
@@ -435,12 +436,13 @@ def compute_ring_schedule(node_data, idx_data, morton=True):
 
 
 def _options(cluster_mode=0, morton=True, sync_mode=0, block_size=0, keep_lambdas=False, device=0, stream=None,
-             host_setup=False, wait_timeout_ms=0):
+             host_setup=False, wait_timeout_ms=0, bricks=0):
     o = Options()
     o.cluster_mode, o.no_morton, o.sync_mode = cluster_mode, 0 if morton else 1, sync_mode
     o.block_size, o.keep_lambdas, o.device, o.stream = block_size, 1 if keep_lambdas else 0, device, stream
     o.host_setup = 1 if host_setup else 0
     o.wait_timeout_ms = wait_timeout_ms
+    o.bricks = bricks
     return o
 
 
