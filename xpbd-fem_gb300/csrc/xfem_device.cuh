@@ -144,10 +144,9 @@ __device__ __forceinline__ Vec3 finish_vertex(const BodyParams& bp, float4& O, f
 // Finalize the previous substep (unless `first`: (O, D) then hold the
 // canonical (X, V)) and predict the next (XPBDFEM/Geo.cpp:307-312) for
 // device vertex v. bodies: C.bodies, or a copy of them in shared memory.
-__device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, bool first, float dt,
-                                               float inv_dt, const BodyParams* bodies = nullptr) {
+__device__ __forceinline__ void advance_vertex_bp(const DevCtx& C, const BodyParams& bp, uint32_t v, float4& O,
+                                                  float4& D, bool first, float dt, float inv_dt) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = (bodies ? bodies : C.bodies)[bits >> 8];
 	Vec3 V;
 	if (first) {
 		V = v3(D);
@@ -163,14 +162,18 @@ __device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, floa
 	D = make_float4(V.x * dt, V.y * dt, V.z * dt, __uint_as_float(bits));
 }
 
+__device__ __forceinline__ void advance_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, bool first, float dt,
+                                               float inv_dt, const BodyParams* bodies = nullptr) {
+	advance_vertex_bp(C, (bodies ? bodies : C.bodies)[__float_as_uint(D.w) >> 8], v, O, D, first, dt, inv_dt);
+}
+
 // Finalize the last substep of a launch: (O, D) -> canonical (X, V) for
 // device vertex v. A position or velocity that is no longer finite (a
 // diverged solve, or a NaN the caller set) is recorded in the error word as
 // kErrNonFinite, which the next synchronising call reports.
-__device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, float inv_dt,
-                                                const BodyParams* bodies = nullptr) {
+__device__ __forceinline__ void finalize_vertex_bp(const DevCtx& C, const BodyParams& bp, uint32_t v, float4& O,
+                                                   float4& D, float inv_dt) {
 	uint32_t bits = __float_as_uint(D.w);
-	const BodyParams& bp = (bodies ? bodies : C.bodies)[bits >> 8];
 	const Vec3 V = finish_vertex(bp, O, D, bits, inv_dt, C.right_target, v);
 	O.x += D.x;
 	O.y += D.y;
@@ -179,6 +182,11 @@ __device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, flo
 	// inf - inf and NaN - NaN are NaN: one compare for all six values
 	const float z = (O.x - O.x) + (O.y - O.y) + (O.z - O.z) + (V.x - V.x) + (V.y - V.y) + (V.z - V.z);
 	if (z != 0.0f) atomicCAS(C.err, 0, kErrNonFinite);
+}
+
+__device__ __forceinline__ void finalize_vertex(const DevCtx& C, uint32_t v, float4& O, float4& D, float inv_dt,
+                                                const BodyParams* bodies = nullptr) {
+	finalize_vertex_bp(C, (bodies ? bodies : C.bodies)[__float_as_uint(D.w) >> 8], v, O, D, inv_dt);
 }
 
 // Rest state of one tet: Qi column-major q[c][r], QQ, QR and c0 = (1/mu)/vol.

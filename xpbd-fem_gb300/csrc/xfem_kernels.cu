@@ -700,11 +700,17 @@ __device__ __forceinline__ int next_brick_chunk(const uint32_t* bcb, uint32_t nc
 
 // One resident brick chunk (every lane a whole cube, as run_chunk_cube).
 // Vertex word w of a lane: a device vertex in vert, or kPrivate | p for the
-// brick's shared-memory slot p (state sv[2p], sv[2p + 1], device id spid[p]).
+// brick's shared-memory slot p (O at sv[p], D at sv[bpriv_max + p], device id
+// spid[p]; O and D in two arrays so that the 16-byte accesses of a warp, whose
+// lanes hold nearby slots, fall in different bank groups).
 // bodies: the body parameters (a shared-memory copy when the handle has few).
+// ONE: a single body, whose parameters bp1 and material mat1 the kernel holds
+// in registers.
+template <bool ONE>
 __device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int next, uint32_t lane, bool first,
                                                 float dt, float inv_dt, float inv_dt2, float4* sv,
-                                                const uint32_t* spid, const BodyParams* bodies, bool bshared) {
+                                                const uint32_t* spid, const BodyParams* bodies, bool bshared,
+                                                const BodyParams& bp1, const Mat& mat1) {
 	const float4* rec = reinterpret_cast<const float4*>(st.buf);
 	const uint32_t* hdrs = reinterpret_cast<const uint32_t*>(st.buf + 2048u * 6u);
 	const uint32_t* vws = hdrs + kLanes;
@@ -714,15 +720,15 @@ __device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int 
 	uint32_t vw[8];
 	float4 O[8], D[8];
 	if (live) {
-		const Mat mat = bshared ? load_mat_shared(bodies, hdr >> 16) : load_mat(bodies, hdr >> 16);
+		const Mat mat = ONE ? mat1 : bshared ? load_mat_shared(bodies, hdr >> 16) : load_mat(bodies, hdr >> 16);
 #pragma unroll
 		for (int s = 0; s < 8; s++) vw[s] = vws[s * kLanes + lane];
 #pragma unroll
 		for (int s = 0; s < 8; s++) {
 			if (vw[s] & kPrivate) {
 				const uint32_t p = vw[s] & ~kPrivate;
-				O[s] = sv[2 * p];
-				D[s] = sv[2 * p + 1];
+				O[s] = sv[p];
+				D[s] = sv[C.bpriv_max + p];
 			} else {
 				ld_vertex(C.vert + 2 * (size_t)vw[s], O[s], D[s]);
 			}
@@ -731,7 +737,10 @@ __device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int 
 		for (int s = 0; s < 8; s++)
 			if (mask & (1u << s)) {
 				const uint32_t v = (vw[s] & kPrivate) ? spid[vw[s] & ~kPrivate] : vw[s];
-				advance_vertex(C, v, O[s], D[s], first, dt, inv_dt, bodies);
+				if (ONE)
+					advance_vertex_bp(C, bp1, v, O[s], D[s], first, dt, inv_dt);
+				else
+					advance_vertex(C, v, O[s], D[s], first, dt, inv_dt, bodies);
 			}
 #pragma unroll
 		for (int t = 0; t < 6; t++) {
@@ -750,8 +759,8 @@ __device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int 
 		for (int s = 0; s < 8; s++) {
 			if (vw[s] & kPrivate) {
 				const uint32_t p = vw[s] & ~kPrivate;
-				if (mask & (1u << s)) sv[2 * p] = O[s];
-				sv[2 * p + 1] = D[s];
+				if (mask & (1u << s)) sv[p] = O[s];
+				sv[C.bpriv_max + p] = D[s];
 			} else if (mask & (1u << s)) {
 				st_vertex(C.vert + 2 * (size_t)vw[s], O[s], D[s]);
 			} else {
@@ -798,6 +807,7 @@ __device__ bool brick_wait(const DevCtx& C, const uint32_t* list, uint32_t nb0, 
 // launch so that every brick is resident), the plain solve only (no damping,
 // volume passes or multiplier output). The state between substeps stays
 // (O, D), and each brick finalizes its own vertices at the end.
+template <bool ONE>
 __global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float dt) {
 	extern __shared__ __align__(128) uint8_t smem[];
 	__shared__ uint32_t s_bcb[65], s_bwait[64];
@@ -822,14 +832,21 @@ __global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float d
 			reinterpret_cast<uint32_t*>(s_bodies)[i] = __ldg(reinterpret_cast<const uint32_t*>(C.bodies) + i);
 	}
 	const BodyParams* bodies = bshared ? s_bodies : C.bodies;
+	// a single body: its parameters and material in registers
+	BodyParams bp1;
+	Mat mat1;
+	if (ONE) {
+		bp1 = C.bodies[0];
+		mat1 = load_mat(C.bodies, 0);
+	}
 	// the brick's own vertices into shared memory, for the whole launch
 	const uint32_t pb = __ldg(C.bpriv_begin + b), pe = __ldg(C.bpriv_begin + b + 1);
 	for (uint32_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
 		const uint32_t v = __ldg(C.bpriv_vid + i);
 		float4 O, D;
 		ld_vertex(C.vert + 2 * (size_t)v, O, D);
-		sv[2 * (i - pb)] = O;
-		sv[2 * (i - pb) + 1] = D;
+		sv[i - pb] = O;
+		sv[C.bpriv_max + (i - pb)] = D;
 		spid[i - pb] = v;
 	}
 	__syncthreads();
@@ -861,7 +878,8 @@ __global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float d
 					break;
 				}
 				const int next = next_brick_chunk(s_bcb, ncol, s, nsub, c, ch, wib, wpb);
-				run_chunk_brick(C, st, next, lane, s == 0, dt, inv_dt, inv_dt2, sv, spid, bodies, bshared);
+				run_chunk_brick<ONE>(C, st, next, lane, s == 0, dt, inv_dt, inv_dt2, sv, spid, bodies, bshared, bp1,
+				                     mat1);
 			}
 			if (__syncthreads_or(bad ? 1 : 0)) {
 				ok = false;
@@ -881,8 +899,11 @@ __global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float d
 	}
 	for (uint32_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
 		const uint32_t v = __ldg(C.bpriv_vid + i);
-		float4 O = sv[2 * (i - pb)], D = sv[2 * (i - pb) + 1];
-		finalize_vertex(C, v, O, D, inv_dt, bodies);
+		float4 O = sv[i - pb], D = sv[C.bpriv_max + (i - pb)];
+		if (ONE)
+			finalize_vertex_bp(C, bp1, v, O, D, inv_dt);
+		else
+			finalize_vertex(C, v, O, D, inv_dt, bodies);
 		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 	const uint32_t fb = __ldg(C.bfin_begin + b), fe = __ldg(C.bfin_begin + b + 1);
@@ -890,7 +911,10 @@ __global__ void __launch_bounds__(256) k_bricks(DevCtx C, uint32_t nsub, float d
 		const uint32_t v = __ldg(C.bfin_vid + i);
 		float4 O, D;
 		ld_vertex(C.vert + 2 * (size_t)v, O, D);
-		finalize_vertex(C, v, O, D, inv_dt, bodies);
+		if (ONE)
+			finalize_vertex_bp(C, bp1, v, O, D, inv_dt);
+		else
+			finalize_vertex(C, v, O, D, inv_dt, bodies);
 		st_vertex(C.vert + 2 * (size_t)v, O, D);
 	}
 	if (gtid == 0) *C.tick = tick0 + nsub;
@@ -1076,13 +1100,18 @@ size_t brick_smem_bytes(int block, uint32_t bpriv_max) {
 
 int brick_grid_fits(int block, uint32_t bpriv_max, uint32_t nbricks, bool* fits) {
 	const size_t smem = brick_smem_bytes(block, bpriv_max);
-	cudaError_t e = set_smem_attr((const void*)k_bricks, smem);
+	cudaError_t e = set_smem_attr((const void*)k_bricks<true>, smem);
+	if (e == cudaSuccess) e = set_smem_attr((const void*)k_bricks<false>, smem);
 	int dev = 0, sms = 0, per_sm = 0;
 	if (e == cudaSuccess) e = cudaGetDevice(&dev);
 	if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-	if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_bricks, block, smem);
+	int per_sm1 = 0;
+	if (e == cudaSuccess)
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_bricks<false>, block, smem);
+	if (e == cudaSuccess)
+		e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm1, (const void*)k_bricks<true>, block, smem);
 	if (e != cudaSuccess) return (int)e;
-	*fits = (uint64_t)per_sm * (uint64_t)sms >= nbricks && nbricks > 0;
+	*fits = (uint64_t)std::min(per_sm, per_sm1) * (uint64_t)sms >= nbricks && nbricks > 0;
 	return 0;
 }
 
@@ -1116,7 +1145,8 @@ int launch_substeps(const DevCtx& ctx, const LaunchCfg& cfg, uint32_t nsub, floa
 			DevCtx c = ctx;
 			float dtv = dt;
 			void* args[] = {&c, &n, &dtv};
-			e = cudaLaunchCooperativeKernel((const void*)k_bricks, dim3(ctx.nbricks), dim3(cfg.block), args, smem_b, st);
+			const void* f = ctx.nbodies == 1 ? (const void*)k_bricks<true> : (const void*)k_bricks<false>;
+			e = cudaLaunchCooperativeKernel(f, dim3(ctx.nbricks), dim3(cfg.block), args, smem_b, st);
 			if (e != cudaSuccess) return (int)e;
 			done += n;
 		}
