@@ -1022,31 +1022,49 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 	std::vector<uint32_t> brick_of((size_t)nch * kLanes, 0xffffffffu);
 	for (uint64_t j = 0; j < L; j++) brick_of[(uint32_t)lanes[j]] = (uint32_t)(j * nb / L);
 	// (vertex, brick) incidences
-	std::vector<uint64_t> vb;
-	vb.reserve(L * kMaxClusterVerts);
-	for (uint64_t j = 0; j < L; j++) {
-		const uint32_t i = (uint32_t)lanes[j];
-		for (uint32_t sl = 0; sl < lane_nv[i]; sl++) vb.push_back((uint64_t)lane_dv[(size_t)i * kMaxClusterVerts + sl] << 32 | brick_of[i]);
+	// every cluster touching each vertex, as colour << 16 | brick; chunks are
+	// colour-major, so each vertex's touches come in ascending colour order
+	const uint32_t nvv = h->nverts;
+	std::vector<uint32_t> toff((size_t)nvv + 1, 0);
+	for (uint32_t k = 0; k < nch; k++)
+		for (uint32_t lane = 0; lane < kLanes; lane++) {
+			const uint32_t i = k * kLanes + lane;
+			if (brick_of[i] != 0xffffffffu)
+				for (uint32_t sl = 0; sl < lane_nv[i]; sl++) toff[lane_dv[(size_t)i * kMaxClusterVerts + sl] + 1]++;
+		}
+	for (uint32_t v = 0; v < nvv; v++) toff[v + 1] += toff[v];
+	std::vector<uint32_t> touch(toff[nvv]);
+	{
+		std::vector<uint32_t> fill(toff.begin(), toff.end() - 1);
+		for (uint32_t k = 0; k < nch; k++)
+			for (uint32_t lane = 0; lane < kLanes; lane++) {
+				const uint32_t i = k * kLanes + lane;
+				if (brick_of[i] != 0xffffffffu)
+					for (uint32_t sl = 0; sl < lane_nv[i]; sl++)
+						touch[fill[lane_dv[(size_t)i * kMaxClusterVerts + sl]]++] = chunk_colour[k] << 16 | brick_of[i];
+			}
 	}
-	std::sort(vb.begin(), vb.end());
-	vb.erase(std::unique(vb.begin(), vb.end()), vb.end());
-	std::vector<uint32_t> slot(h->nverts, 0xffffffffu), npriv(nb, 0);
+	std::vector<uint32_t> slot(nvv, 0xffffffffu), npriv(nb, 0);
 	std::vector<std::vector<uint32_t>> priv(nb), fin(nb);
 	std::vector<std::vector<uint32_t>> nbl(nb);
-	for (size_t a = 0; a < vb.size();) {
-		size_t e = a + 1;
-		while (e < vb.size() && (vb[e] >> 32) == (vb[a] >> 32)) e++;
-		const uint32_t v = (uint32_t)(vb[a] >> 32), b0 = (uint32_t)vb[a];
-		if (e - a == 1 && npriv[b0] < (uint64_t)cap) {
-			slot[v] = npriv[b0]++;
-			priv[b0].push_back(v);
-		} else {
-			fin[b0].push_back(v);  // the lowest brick touching it finalizes it
-			for (size_t x = a; x < e; x++)
-				for (size_t y = a; y < e; y++)
-					if (x != y) nbl[(uint32_t)vb[x]].push_back((uint32_t)vb[y]);
+	for (uint32_t v = 0; v < nvv; v++) {
+		const uint32_t t0 = toff[v], t1 = toff[v + 1];
+		if (t0 == t1) continue;  // in no cluster
+		uint32_t bmin = 0xffffu;
+		bool one = true;
+		for (uint32_t t = t0; t < t1; t++) {
+			bmin = std::min(bmin, touch[t] & 0xffffu);
+			one = one && (touch[t] & 0xffffu) == (touch[t0] & 0xffffu);
 		}
-		a = e;
+		if (one && npriv[bmin] < (uint64_t)cap) {
+			slot[v] = npriv[bmin]++;
+			priv[bmin].push_back(v);
+		} else {
+			fin[bmin].push_back(v);  // the lowest brick touching it finalizes it
+			for (uint32_t x = t0; x < t1; x++)
+				for (uint32_t y = t0; y < t1; y++)
+					if ((touch[x] & 0xffffu) != (touch[y] & 0xffffu)) nbl[touch[x] & 0xffffu].push_back(touch[y] & 0xffffu);
+		}
 	}
 	std::vector<uint32_t> pbeg(nb + 1, 0), pvid, fbeg(nb + 1, 0), fvid, nbeg(nb + 1, 0), nbv;
 	uint32_t pmax = 0;
@@ -1082,28 +1100,13 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 	// each vertex of such a cluster, the brick of the cluster that touched it
 	// last before (the highest lower colour touching it, else the highest
 	// colour, in the previous substep), when that is another brick
-	std::vector<uint64_t> touch;  // vertex << 32 | colour << 16 | brick
-	touch.reserve(L * kMaxClusterVerts);
-	for (uint32_t k = 0; k < nch; k++)
-		for (uint32_t lane = 0; lane < kLanes; lane++) {
-			const uint32_t i = k * kLanes + lane;
-			if (brick_of[i] == 0xffffffffu) continue;
-			for (uint32_t sl = 0; sl < lane_nv[i]; sl++)
-				touch.push_back((uint64_t)lane_dv[(size_t)i * kMaxClusterVerts + sl] << 32 |
-				                (uint64_t)chunk_colour[k] << 16 | brick_of[i]);
-		}
-	std::sort(touch.begin(), touch.end());
 	std::vector<std::vector<uint32_t>> nbc_l((size_t)nb * ncol);
-	for (size_t a = 0; a < touch.size();) {
-		size_t e = a + 1;
-		while (e < touch.size() && (touch[e] >> 32) == (touch[a] >> 32)) e++;
-		for (size_t x = a; x < e; x++) {
-			const size_t prev = x > a ? x - 1 : e - 1;  // colours ascend: the previous touch, wrapping
-			const uint32_t bx = (uint32_t)(touch[x] & 0xffffu), bp = (uint32_t)(touch[prev] & 0xffffu);
-			if (bp != bx) nbc_l[(size_t)bx * ncol + ((touch[x] >> 16) & 0xffffu)].push_back(bp);
+	for (uint32_t v = 0; v < nvv; v++)
+		for (uint32_t x = toff[v]; x < toff[v + 1]; x++) {
+			const uint32_t prev = x > toff[v] ? x - 1 : toff[v + 1] - 1;  // the previous touch, wrapping
+			const uint32_t bx = touch[x] & 0xffffu, bp = touch[prev] & 0xffffu;
+			if (bp != bx) nbc_l[(size_t)bx * ncol + (touch[x] >> 16)].push_back(bp);
 		}
-		a = e;
-	}
 	std::vector<uint32_t> cnb_begin((size_t)nb * ncol + 1, 0), cnb;
 	for (size_t q = 0; q < nbc_l.size(); q++) {
 		std::sort(nbc_l[q].begin(), nbc_l[q].end());
