@@ -163,3 +163,28 @@ def test_bricks_refuse_what_they_do_not_run():
     b.set_settings(_settings(damping=0.01, flags=W.NH_FLAGS | (2 << 20)))
     b.step_frames(1, 4, DT)
     assert b.info()["sync_mode"] != 4 and np.isfinite(b.positions()).all()
+
+
+def test_bricks_follow_material_changes():
+    """Per-tet shear moduli set after creation, then a new body compliance,
+    then back to the uniform material: the brick chunks hold their own copy
+    of each tet's record and must follow every change."""
+    nodes, idx = xfem.generate_tet_block(24, 16, 8, (0.05, 0.05, 0.05), 0, 0.2)
+    nt = idx.size // 5
+    s = _settings()
+    a, b = _pair(nodes, idx, s)
+    mu = (1.0 / s.compliance * np.exp(0.3 * np.random.default_rng(4).normal(size=nt))).astype(np.float32)
+    for h in (a, b):
+        h.set_tet_mu(mu)
+    for n in (10, 10):
+        a.step_frames(1, n, DT)
+        b.step_frames(1, n, DT)
+        _same(a, b)
+    s2 = _settings(nu=0.45)
+    s2.compliance = s.compliance * 0.5
+    for h in (a, b):
+        h.set_tet_mu(None)
+        h.set_settings(s2)
+    a.step_frames(1, 10, DT)
+    b.step_frames(1, 10, DT)
+    _same(a, b)

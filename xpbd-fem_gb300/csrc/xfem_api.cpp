@@ -160,6 +160,7 @@ struct xfem_body {
 	DevBuf<float> el_tab;
 	// brick launch form (sync_mode 4; built when every chunk is a cube chunk)
 	DevBuf<float4> bcblk;
+	DevBuf<uint32_t> tet_brec_dev;  // per tet (all bodies): its c0 word in the brick chunks
 	DevBuf<uint32_t> bcb, bwait, bcnb_begin, bcnb, bpriv_begin, bpriv_vid, bfin_begin, bfin_vid, bnb_begin, bnb, bflag;
 	// meshes mixing tets and hexes (kElMixed): the tets as elements of their own colouring
 	DevBuf<uint4> mt_vid;
@@ -1128,12 +1129,18 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 	bcb[bc.size()] = nbc;
 	const uint32_t per16 = kBrickChunkBytes / 16u;
 	std::vector<float4> blk((size_t)nbc * per16, make_float4(0, 0, 0, 0));
+	// per tet row and lane of the persistent layout: where the tet's c0 word
+	// (plane 3 of its record) sits in the brick chunks, so that material
+	// changes reach both layouts
+	std::vector<uint32_t> brec_of_slot((size_t)h->nrows * kLanes, 0);
 	parallel_for((uint32_t)bc.size(), [&](uint32_t q) {
 		for (size_t j = 0; j < bc[q].size(); j++) {
 			const uint32_t i = bc[q][j], k = i / kLanes, a = i % kLanes;
 			const uint32_t dch = bcb[q] + (uint32_t)(j / kLanes), dl = (uint32_t)(j % kLanes);
 			const float4* src = &cblk[meta[k].off16];
 			float4* dst = &blk[(size_t)dch * per16];
+			for (uint32_t t = 0; t < 6; t++)
+				brec_of_slot[((size_t)meta[k].trow + t) * kLanes + a] = dch * per16 + (t * 4u + 3u) * kLanes + dl;
 			for (uint32_t r = 0; r < 24; r++) dst[r * kLanes + dl] = src[r * kLanes + a];
 			const uint32_t* sw = reinterpret_cast<const uint32_t*>(src + 24 * kLanes);
 			uint32_t* dw = reinterpret_cast<uint32_t*>(dst + 24 * kLanes);
@@ -1144,6 +1151,11 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 			}
 		}
 	});
+	std::vector<uint32_t> brec(h->ntets, 0);
+	for (const BodyHost& bh : h->bodies)
+		for (uint32_t t = 0; t < bh.nt; t++) brec[bh.tbase + t] = brec_of_slot[bh.tet_slot[t]];
+	if ((uint64_t)nbc * per16 > 0xffffffffull) return fail(XFEM_ELIMIT, "brick chunks exceed 64 GiB");
+	XCUDA(h->tet_brec_dev.alloc(brec.size()));
 	XCUDA(h->bcblk.alloc(blk.size()));
 	XCUDA(h->bcb.alloc(bcb.size()));
 	XCUDA(h->bwait.alloc(bwait.size()));
@@ -1160,6 +1172,7 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
 	};
 	XCUDA(up(h->bcblk.p, blk.data(), blk.size() * sizeof(float4)));
+	XCUDA(up(h->tet_brec_dev.p, brec.data(), brec.size() * 4));
 	XCUDA(up(h->bcb.p, bcb.data(), bcb.size() * 4));
 	XCUDA(up(h->bwait.p, bwait.data(), bwait.size() * 4));
 	XCUDA(up(h->bcnb_begin.p, cnb_begin.data(), cnb_begin.size() * 4));
@@ -1186,7 +1199,7 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 	c.bflag = h->bflag.p;
 	c.nbricks = nb;
 	c.bpriv_max = pmax;
-	h->device_bytes += blk.size() * 16 + (bcb.size() + bwait.size() + cnb_begin.size() + cnb.size() + pbeg.size() + pvid.size() + fbeg.size() + fvid.size() +
+	h->device_bytes += blk.size() * 16 + (brec.size() + bcb.size() + bwait.size() + cnb_begin.size() + cnb.size() + pbeg.size() + pvid.size() + fbeg.size() + fvid.size() +
 	                                      nbeg.size() + nbv.size() + (size_t)nb * kBrickFlagStride) * 4;
 	if (getenv("XFEM_SETUP_TIMING"))
 		fprintf(stderr, "xfem bricks: %u bricks, %u chunks, %zu private and %zu shared vertices, at most %u private "
@@ -1872,8 +1885,11 @@ int update_material(xfem_body* h, const BodyHost& b) {
 		XCUDA(cudaMemcpyAsync(h->io.p, b.tet_mu.data(), b.nt * sizeof(float), cudaMemcpyHostToDevice, h->stream));
 		mu_dev = h->io.p;
 	}
-	const int e = launch_set_c0(h->cblk.p, h->tet_rec_dev.p + b.tbase, h->tet_vol_dev.p + b.tbase, mu_dev,
-	                            1.0f / b.settings.compliance, b.nt, h->tet_inv_mu.p + b.tbase, h->stream);
+	int e = launch_set_c0(h->cblk.p, h->tet_rec_dev.p + b.tbase, h->tet_vol_dev.p + b.tbase, mu_dev,
+	                      1.0f / b.settings.compliance, b.nt, h->tet_inv_mu.p + b.tbase, h->stream);
+	if (!e && h->bcblk.p)  // the brick chunks hold their own copy of each record
+		e = launch_set_c0(h->bcblk.p, h->tet_brec_dev.p + b.tbase, h->tet_vol_dev.p + b.tbase, mu_dev,
+		                  1.0f / b.settings.compliance, b.nt, h->tet_inv_mu.p + b.tbase, h->stream);
 	if (e) return fail(XFEM_ECUDA, "material update launch failed");
 	XCUDA(cudaStreamSynchronize(h->stream));
 	return XFEM_OK;
