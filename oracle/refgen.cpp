@@ -90,6 +90,10 @@
  *       the per-T10 rest state (Qi, ic.QQ[9], ic.QR[36], volume,
  *       surfaceArea), w, flags, tOrder and CalculateVolume.
  *   qordered / qdamped (as hordered / hdamped) < torder.u32
+ *   qrings (as qdamped, with a continuous-pressure energy 8-10) < torder.u32 vorder.u32
+ *       the vertex order (the mesh's own vertices) replaces vOrder:
+ *       GeoQuadratic3d::Constrain solves their rings over the T10s in it
+ *       and Damp damps them in it (XPBDFEM/Geo.cpp:971-1008).
  *   qsolve seed count energy simultaneous compliance poisson dt
  *       SolveElement (XPBDFEM/Fem.cpp:893) on `count` seeded random T10s.
  *
@@ -102,6 +106,7 @@
  *       ic.QR[325], volume, surfaceArea), w, flags, hOrder and
  *       CalculateVolume.
  *   Qordered / Qdamped (as hordered / hdamped) < horder.u32
+ *   Qrings (as Qdamped, energy 8-10) < horder.u32 vorder.u32 (as qrings)
  *   Qsolve seed count energy simultaneous compliance poisson dt
  *       SolveElement (XPBDFEM/Fem.cpp:897) on `count` seeded random H27s.
  */
@@ -301,7 +306,8 @@ int main(int argc, char** argv) {
 	auto U = [&](int i) { return (uint32_t)strtoul(argv[i], 0, 10); };
 	auto F = [&](int i) { return (float)strtod(argv[i], 0); };
 
-	if ((quad || h27) && (!strcmp(cmd, "init") || !strcmp(cmd, "ordered") || !strcmp(cmd, "damped"))) {
+	if ((quad || h27) &&
+	    (!strcmp(cmd, "init") || !strcmp(cmd, "ordered") || !strcmp(cmd, "damped") || !strcmp(cmd, "rings"))) {
 		Allocator* alloc = make_alloc((size_t)1 << 31);
 		uint32_t W = U(2), H = U(3), D = U(4);
 		vec3 scale(F(5), F(6), F(7));
@@ -365,7 +371,7 @@ int main(int argc, char** argv) {
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
 		s.flags = (s.flags & ~(Settings_ElementTypeMask << Settings_ElementTypeBit)) |
 		          ((h27 ? Element_H27 : Element_T10) << Settings_ElementTypeBit);
-		if (!strcmp(cmd, "damped")) {
+		if (!strcmp(cmd, "damped") || !strcmp(cmd, "rings")) {
 			s.damping = F(a++);
 			s.pbdDamping = F(a++);
 			s.drag = F(a++);
@@ -389,6 +395,11 @@ int main(int argc, char** argv) {
 		const uint32_t nel = h27 ? g->con.hexCount : g->con.tetCount;
 		if (fread(&n, 4, 1, stdin) != 1 || n != nel) { fprintf(stderr, "bad order\n"); return 3; }
 		if (fread(h27 ? g->hOrder : g->tOrder, 4, n, stdin) != n) { fprintf(stderr, "short order\n"); return 3; }
+		if (!strcmp(cmd, "rings")) {
+			// the rings of the mesh's own vertices, in the order read
+			if (fread(&n, 4, 1, stdin) != 1 || n != g->con.vertCount) { fprintf(stderr, "bad vertex order\n"); return 3; }
+			if (fread(g->vOrder, 4, n, stdin) != n) { fprintf(stderr, "short vertex order\n"); return 3; }
+		}
 		Manipulator manip;
 		manip.pickedGeo = nullptr;
 		for (uint32_t k = 0; k < nsub; k++) {

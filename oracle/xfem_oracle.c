@@ -638,13 +638,23 @@ int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uin
 
 int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
                             uint32_t morton, uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours) {
+	return orc_ring_schedule_centres(nodes, nv, elems, npe, ne, nv, morton, vorder, colour_begin, ncolours);
+}
+
+/* The rings of the first `ncentre` vertices only (GeoQuadratic3d builds
+ * rings for the mesh's own vertices, not for the added nodes): colouring in
+ * id order over those rings, then (colour, Morton rank among all nv
+ * vertices); vorder holds ncentre ids. */
+int orc_ring_schedule_centres(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
+                              uint32_t ncentre, uint32_t morton, uint32_t* vorder, uint32_t* colour_begin,
+                              uint32_t* ncolours) {
 	orc_rings rg;
 	if (rings_build(elems, npe, ne, nv, &rg)) {
 		rings_free(&rg);
 		return -1;
 	}
 	/* the vertices whose ring holds each node */
-	const uint32_t nent = rg.node_off[nv];
+	const uint32_t nent = rg.node_off[ncentre];
 	uint32_t* ho = (uint32_t*)calloc((size_t)nv + 1, 4);
 	uint32_t* hl = (uint32_t*)malloc(4 * (size_t)(nent ? nent : 1));
 	uint32_t* colour = (uint32_t*)malloc(4 * (size_t)(nv ? nv : 1));
@@ -659,14 +669,14 @@ int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* ele
 		uint32_t* f = (uint32_t*)malloc(4 * ((size_t)nv + 1));
 		if (!f) goto done;
 		memcpy(f, ho, 4 * (size_t)nv);
-		for (uint32_t v = 0; v < nv; v++)
+		for (uint32_t v = 0; v < ncentre; v++)
 			for (uint32_t i = rg.node_off[v]; i < rg.node_off[v + 1]; i++) hl[f[rg.nodes[i]]++] = v;
 		free(f);
 	}
 	/* greedy colouring in id order: rings of one colour share no node */
 	uint32_t ncol = 0;
 	for (uint32_t c = 0; c < ORC_MAXCOL; c++) mark[c] = 0xffffffffu;
-	for (uint32_t u = 0; u < nv; u++) {
+	for (uint32_t u = 0; u < ncentre; u++) {
 		for (uint32_t i = rg.node_off[u]; i < rg.node_off[u + 1]; i++) {
 			const uint32_t x = rg.nodes[i];
 			for (uint32_t j = ho[x]; j < ho[x + 1]; j++)
@@ -682,13 +692,13 @@ int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* ele
 		float mn[3] = {INFINITY, INFINITY, INFINITY}, sc[3] = {0.0f, 0.0f, 0.0f};
 		if (orc_vertex_ranks(nodes, nv, morton, rank, mn, sc)) goto done;
 	}
-	for (uint32_t v = 0; v < nv; v++) {
+	for (uint32_t v = 0; v < ncentre; v++) {
 		kv[v].key = ((uint64_t)colour[v] << 32) | rank[v];
 		kv[v].id = v;
 	}
-	qsort(kv, nv, sizeof(orc_kv), kv_cmp);
+	qsort(kv, ncentre, sizeof(orc_kv), kv_cmp);
 	for (uint32_t c = 0; c <= ncol; c++) colour_begin[c] = 0;
-	for (uint32_t i = 0; i < nv; i++) {
+	for (uint32_t i = 0; i < ncentre; i++) {
 		vorder[i] = kv[i].id;
 		colour_begin[colour[kv[i].id] + 1]++;
 	}

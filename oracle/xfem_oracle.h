@@ -266,6 +266,16 @@ int orc_solve_t10_f(double* X, const double* O, const float* w, const float* ep,
 int orc_solve_t10_d(double* X, const double* O, const double* w, const double* ep, const orc_params* p);
 /* Substeps of a T10 mesh in `order` (GeoQuadratic3d::Constrain and Damp's
  * tet loops, XPBDFEM/Geo.cpp:973-1006). */
+/* Substeps of a T10 mesh with a continuous-pressure model (8-10): the rings
+ * of the first ncorner nodes (the mesh's own vertices) in vorder, the PBD
+ * damping over the T10s in torder (GeoQuadratic3d::Constrain and Damp,
+ * XPBDFEM/Geo.cpp:971-1008). */
+int orc_t10_substeps_rings_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                             const uint32_t* t10, const float* ep, const uint32_t* torder, const uint32_t* vorder,
+                             uint32_t ncorner, uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_t10_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
+                             const uint32_t* t10, const double* ep, const uint32_t* torder, const uint32_t* vorder,
+                             uint32_t ncorner, uint32_t nsub, const orc_params* p, uint8_t* contact);
 int orc_t10_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
                        const uint32_t* t10, const float* ep, const uint32_t* order, uint32_t nsub,
                        const orc_params* p, uint8_t* contact);
@@ -355,6 +365,11 @@ int orc_ring_schedule(const float* nodes, uint32_t nv, const uint32_t* tets, uin
 /* The same over elements of npe vertices each (4: tets, 8: hexes). */
 int orc_ring_schedule_elems(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
                             uint32_t morton, uint32_t* vorder, uint32_t* colour_begin, uint32_t* ncolours);
+/* The rings of the first ncentre vertices only, in the same form (vorder:
+ * ncentre ids). */
+int orc_ring_schedule_centres(const float* nodes, uint32_t nv, const uint32_t* elems, uint32_t npe, uint32_t ne,
+                              uint32_t ncentre, uint32_t morton, uint32_t* vorder, uint32_t* colour_begin,
+                              uint32_t* ncolours);
 
 /* Hex schedule: hexes coloured greedily in id order so that the hexes of one
  * colour share no vertex (each takes the smallest colour not held by an

@@ -272,6 +272,26 @@ CASES = [
                                       0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
     ("qvolume_wonky_nh_serial_1_post", ["qdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
+    # continuous-pressure models on quadratic tets (SolveRing over the T10s
+    # around each mesh vertex, XPBDFEM/Geo.cpp:147-225, 944-953, 971-1008):
+    # the `qdamped` arguments; stdin holds the GPU's T10 colour order (PBD
+    # damping) and its ring order over the mesh's own vertices
+    ("qrings_c1_cpixar_nu045", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("qrings_c1_cmixed_nu045", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("qrings_c1_cmixed_incompressible", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
+                                         0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("qrings_c1_cskin_nu049", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
+                               0.0, -9.81, DT, 40, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("qrings_wonky_cmixed_paper", ["qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
+                                   -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05]),
+    ("qrings_c1_cskin_limit", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
+                               0.0, -9.81, DT, 40, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("qrings_c1_cmixed_amortized_pbd", ["qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
+                                        0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("qrings_wonky_cpixar_post", ["qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
+                                  -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
     ("hvolume_wonky_pixar_1_post_pbd", ["hdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 0, 1, 1e-3, 0.45,
                                         -2.0, -9.81, DT, 10, 1, 0.01, 0.05, 0.0, 2, 0.05, 1]),
     # quadratic hexahedra (GeoQuadratic3d on a GenerateHexBlock mesh, element
@@ -401,7 +421,7 @@ def main():
             order = sch["hex_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
-        if args[0] in ("qordered", "qdamped"):
+        if args[0] in ("qordered", "qdamped", "qrings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]
             nodes, idx = oracle.gen_tet_block(W, H, D, (sx, sy, sz), pattern, wonk)
@@ -410,6 +430,11 @@ def main():
             order = sch["tet_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_tet_begin": sch["colour_tet_begin"]}
+            if args[0] == "qrings":
+                rs = q.ring_schedule(morton=1)
+                vorder = rs["vert_order"].astype(np.uint32)
+                stdin += struct.pack("<I", vorder.size) + vorder.tobytes()
+                extra.update(vorder=vorder, colour_vert_begin=rs["colour_vert_begin"])
         if args[0] == "mixed":
             import oracle  # noqa: E402
             nodes, idx = mixed_mesh(args)

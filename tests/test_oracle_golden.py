@@ -546,7 +546,7 @@ def q_params(orc, a, g, tick):
     """orc_params of a `qordered` / `qdamped` (T10) or `Qordered` / `Qdamped` (H27) fixture."""
     energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[10:19]
     kw = dict(rayleigh_type=2)
-    if a[0] in ("qdamped", "Qdamped"):
+    if a[0] in ("qdamped", "Qdamped", "qrings", "Qrings"):
         damping, pbd, drag, rtype, spacing = a[19:24]
         d = g["derived"]
         kw = dict(damping=damping, rayleigh_type=rtype, pbd_damping=pbd, pbd_coeff=float(d[0]),
@@ -568,6 +568,37 @@ def test_t10_substeps_bit_exact(orc, name):
     assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
     assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
     Xn, Vn, _, _ = q.substeps(X1, V1, w1, g["order"], a[17] - 1, q_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+QRINGS = ["qrings_c1_cpixar_nu045", "qrings_c1_cmixed_nu045", "qrings_c1_cmixed_incompressible",
+          "qrings_c1_cskin_nu049", "qrings_wonky_cmixed_paper", "qrings_c1_cskin_limit",
+          "qrings_c1_cmixed_amortized_pbd", "qrings_wonky_cpixar_post"]
+
+
+@pytest.mark.parametrize("name", QRINGS)
+def test_t10_rings_bit_exact(orc, name):
+    """The continuous-pressure models on quadratic tets: GeoQuadratic3d's
+    rings of the mesh's own vertices over the T10s around them (SolveRing,
+    XPBDFEM/Geo.cpp:147-225, 944-953, 971-1008) in the fixture's ring order,
+    which the centres-only ring schedule reproduces; PBD damping over the
+    T10s in the fixture's T10 order."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.Quadratic(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(q.schedule()["tet_order"], g["order"])
+    rs = q.ring_schedule()
+    assert np.array_equal(rs["vert_order"], g["vorder"])
+    assert np.array_equal(rs["colour_vert_begin"], g["colour_vert_begin"])
+    lm = (q.flags & 1).astype(np.uint8)
+    X1, V1, w1, _ = q.substeps_rings(q.X0, np.zeros_like(q.X0), q.w, g["order"], g["vorder"], 1,
+                                     q_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = q.substeps_rings(X1, V1, w1, g["order"], g["vorder"], a[17] - 1, q_params(orc, a, g, 1),
+                                    lock_mask=lm)
     assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
     assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
