@@ -102,7 +102,7 @@ class T10OracleRun:
     """The oracle's state for one tet mesh read as T10s (GeoQuadratic3d),
     stepped in the body's T10 order."""
 
-    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32, vorder=None):
         self.q = oracle.Quadratic(nodes, idx, density, dtype)
         self.lock = (self.q.flags & 3).astype(np.uint8)
         self.nodes = self.q.X0.astype(np.float32).reshape(-1)
@@ -111,9 +111,14 @@ class T10OracleRun:
         self.w = self.q.w.copy()
         self.s = settings
         self.order = order
+        self.vorder = vorder  # a continuous-pressure model's ring order
 
     def step(self, n, dt):
         p = oracle_params(self.s, dt, nodes=self.nodes)
+        if self.vorder is not None:
+            self.X, self.V, self.w, _ = self.q.substeps_rings(self.X, self.V, self.w, self.order, self.vorder, n, p,
+                                                              lock_mask=self.lock)
+            return self
         self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
         return self
 

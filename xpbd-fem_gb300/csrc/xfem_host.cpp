@@ -356,46 +356,50 @@ void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 }
 
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
-                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe) {
+                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe, uint32_t ncentre) {
 	const uint32_t kNone = 0xffffffffu;
-	const uint32_t max_elems = npe == 8 ? kMaxRingHexes : kMaxRingTets;
+	if (ncentre > nverts) ncentre = nverts;
+	const uint32_t max_elems = npe == 10 ? kMaxQRingElems : npe == 8 ? kMaxRingHexes : kMaxRingTets;
+	const uint32_t max_nodes = npe == 10 ? kMaxQRingNodes : kMaxRingNodes;
 	rs.npe = npe;
+	rs.nrings = ncentre;
 	rs.tet_off.assign(off, off + nverts + 1);
 	rs.tets.assign(lst, lst + off[nverts]);
-	rs.node_off.assign(nverts + 1, 0);
+	rs.node_off.assign(ncentre + 1, 0);
 	rs.nodes.clear();
 	rs.corner.assign(off[nverts] * npe, 0);
-	for (uint32_t v = 0; v < nverts; v++) {
+	std::vector<uint32_t> nodes(npe * (size_t)max_elems + 1);
+	for (uint32_t v = 0; v < ncentre; v++) {
 		rs.node_off[v] = (uint32_t)rs.nodes.size();
 		if (off[v + 1] - off[v] > max_elems) return -2;
-		uint32_t nodes[4 * kMaxRingTets + 1], cnt = 1;
+		uint32_t cnt = 1;
 		nodes[0] = v;
 		for (uint32_t j = off[v]; j < off[v + 1]; j++) {
 			const uint32_t* tv = tets + npe * (size_t)lst[j];
 			for (uint32_t n = 0; n < npe; n++) {
-				const uint32_t k = (uint32_t)(std::find(nodes, nodes + cnt, tv[n]) - nodes);
+				const uint32_t k = (uint32_t)(std::find(nodes.begin(), nodes.begin() + cnt, tv[n]) - nodes.begin());
 				if (k == cnt) nodes[cnt++] = tv[n];
 				rs.corner[npe * (size_t)j + n] = (uint8_t)k;
 			}
 		}
-		if (cnt > kMaxRingNodes) return -2;
-		rs.nodes.insert(rs.nodes.end(), nodes, nodes + cnt);
+		if (cnt > max_nodes) return -2;
+		rs.nodes.insert(rs.nodes.end(), nodes.begin(), nodes.begin() + cnt);
 	}
-	rs.node_off[nverts] = (uint32_t)rs.nodes.size();
+	rs.node_off[ncentre] = (uint32_t)rs.nodes.size();
 	// the rings holding each node
 	std::vector<uint32_t> hoff(nverts + 1, 0), hl(rs.nodes.size());
 	for (uint32_t x : rs.nodes) hoff[x + 1]++;
 	for (uint32_t v = 0; v < nverts; v++) hoff[v + 1] += hoff[v];
 	{
 		std::vector<uint32_t> fill(hoff.begin(), hoff.end() - 1);
-		for (uint32_t v = 0; v < nverts; v++)
+		for (uint32_t v = 0; v < ncentre; v++)
 			for (uint32_t i = rs.node_off[v]; i < rs.node_off[v + 1]; i++) hl[fill[rs.nodes[i]]++] = v;
 	}
 	// greedy colouring in vertex id order: the smallest colour not used by an
 	// earlier ring sharing a node
-	std::vector<uint32_t> colour(nverts, 0), mark(kMaxColours, kNone);
+	std::vector<uint32_t> colour(ncentre, 0), mark(kMaxColours, kNone);
 	uint32_t ncol = 0;
-	for (uint32_t u = 0; u < nverts; u++) {
+	for (uint32_t u = 0; u < ncentre; u++) {
 		for (uint32_t i = rs.node_off[u]; i < rs.node_off[u + 1]; i++) {
 			const uint32_t x = rs.nodes[i];
 			for (uint32_t j = hoff[x]; j < hoff[x + 1]; j++)
@@ -408,14 +412,14 @@ int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* o
 		ncol = std::max(ncol, c + 1);
 	}
 	rs.ncolours = ncol;
-	std::vector<uint64_t> key(nverts);
-	for (uint32_t v = 0; v < nverts; v++) key[v] = ((uint64_t)colour[v] << 32) | vert_rank[v];
-	std::vector<uint32_t> idx(nverts);
-	for (uint32_t v = 0; v < nverts; v++) idx[v] = v;
+	std::vector<uint64_t> key(ncentre);
+	for (uint32_t v = 0; v < ncentre; v++) key[v] = ((uint64_t)colour[v] << 32) | vert_rank[v];
+	std::vector<uint32_t> idx(ncentre);
+	for (uint32_t v = 0; v < ncentre; v++) idx[v] = v;
 	std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
 	rs.order = idx;
 	rs.colour_begin.assign(ncol + 1, 0);
-	for (uint32_t v = 0; v < nverts; v++) rs.colour_begin[colour[v] + 1]++;
+	for (uint32_t v = 0; v < ncentre; v++) rs.colour_begin[colour[v] + 1]++;
 	for (uint32_t c = 0; c < ncol; c++) rs.colour_begin[c + 1] += rs.colour_begin[c];
 	return 0;
 }

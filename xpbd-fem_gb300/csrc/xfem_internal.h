@@ -70,18 +70,22 @@ void cluster_order(const float* nodes, uint32_t nverts, const uint32_t* tets, ui
 // vertex rank.
 struct RingSchedule {
 	uint32_t ncolours = 0;
+	uint32_t nrings = 0;                    // ring centres: the first nrings vertices
 	std::vector<uint32_t> tet_off, tets;    // the incidence: nverts + 1 offsets; tet ids
-	std::vector<uint32_t> node_off, nodes;  // nverts + 1 offsets; caller vertex ids
-	uint32_t npe = 4;                       // vertices per element: 4 (tets) or 8 (hexes)
+	std::vector<uint32_t> node_off, nodes;  // nrings + 1 offsets; caller vertex ids
+	uint32_t npe = 4;                       // vertices per element: 4 (tets), 8 (hexes) or 10 (T10s)
 	std::vector<uint8_t> corner;            // npe per incidence entry: node index of each element corner
 	std::vector<uint32_t> order;            // vertices in ring order, colour-major
 	std::vector<uint32_t> colour_begin;     // ncolours + 1, into order
 };
 // off / lst: the incidence (vertex -> tets in increasing id); vert_rank: the
-// vertex ranks. Returns 0, -1 when the colour limit is exceeded, -2 when a
-// ring has more than kMaxRingTets tets (kMaxRingHexes hexes) or kMaxRingNodes vertices.
+// vertex ranks. Rings are built around the first ncentre vertices (all when
+// larger than nverts; a T10 mesh rings its own vertices, not the edge
+// nodes). Returns 0, -1 when the colour limit is exceeded, -2 when a ring
+// has more than kMaxRingTets tets (kMaxRingHexes hexes, kMaxQRingElems T10s)
+// or kMaxRingNodes vertices (kMaxQRingNodes on T10s).
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
-                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe = 4);
+                        const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe = 4, uint32_t ncentre = 0xffffffffu);
 
 // A tagged stream that may mix tets (tag 4) and hexes (tag 8), each kind in
 // stream order; -1 on another tag or a truncated record.
@@ -227,6 +231,9 @@ constexpr uint32_t kModelRing = 5;      // ContinuousPixar (8), ContinuousMixed 
 constexpr uint32_t kMaxRingNodes = 32;  // vertices of a one-ring (one warp lane each)
 constexpr uint32_t kMaxRingTets = 64;   // tets of a one-ring (two per warp lane)
 constexpr uint32_t kMaxRingHexes = 16;  // hexes of a one-ring on a hex mesh (one per warp lane)
+constexpr uint32_t kMaxQRingNodes = 128; // nodes of a one-ring over T10s (four per warp lane)
+constexpr uint32_t kMaxQRingElems = 64;  // T10s of a one-ring (two per warp lane; 48 around a vertex
+                                         // on which eight mirrored cubes' diagonals meet)
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
@@ -498,6 +505,10 @@ int launch_hex_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void
 int launch_mixed(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-tet mode (xfem_t10.cu): nsub substeps of a T10 mesh, likewise.
 int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// The continuous-pressure models on a T10 mesh (xfem_t10.cu): nsub substeps
+// of one-ring solves over the T10s around the mesh vertices, a cooperative
+// persistent launch (canonical (X, V) in and out).
+int launch_t10_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp
 // per element (block must be 256).
 int launch_h27(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
