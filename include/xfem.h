@@ -35,19 +35,21 @@
  * ElementParamsLinearHex (XPBDFEM/Fem.cpp:871-896), every energy model. With
  * the continuous-pressure ones (8-10) a hex mesh solves one constraint (pair)
  * per vertex one-ring over the hexes around it (SolveRing's full-energy
- * branch, XPBDFEM/Geo.cpp:147-225, XPBDFEM/Fem.cpp:980-1036). A mesh holds
- * tets or hexes, not both, and so does a handle.
+ * branch, XPBDFEM/Geo.cpp:147-225, XPBDFEM/Fem.cpp:980-1036). A mesh that
+ * holds both tets and hexes runs in mixed mode (see below).
  *
  * A tet mesh whose settings ask for quadratic elements (element type
  * XFEM_ELEMENT_T10 in flags bits 0-3) runs as GeoQuadratic3d
  * (XPBDFEM/Geo.cpp:836-1053, picked by Sim::AddBlock, XPBDFEM/Demo.cpp:145-150):
  * one node added on every edge (Connectivity3d's edge numbering), T10
  * elements (ElementParamsQuadraticTet, SolveElement with Nodes = 10 on the
- * 4-point rule) and the energy models of hexes but the continuous-pressure
- * ones. The body's vertices are
- * then the mesh's own followed by the edge nodes, and every per-vertex call
- * (positions, velocities, lock mask) covers all of them. A handle holds
- * linear tets, hexes or T10s.
+ * 4-point rule) and every energy model: with the continuous-pressure ones
+ * (8-10) one constraint pair per one-ring of a mesh vertex over the T10s
+ * around it (XPBDFEM/Geo.cpp:944-953, 973-982), up to 64 T10s and 128 nodes
+ * per ring. The body's vertices are then the mesh's own followed by the edge
+ * nodes, and every per-vertex call (positions, velocities, lock mask) covers
+ * all of them. A handle holds one element type (linear tets, hexes, mixed,
+ * T10s or H27s).
  */
 #ifndef XFEM_H
 #define XFEM_H
@@ -212,9 +214,9 @@ int xfem_settings_default(xfem_settings* s);
  * mesh mixing tets and hexes is one body holding both (GeoLinear3d on one
  * tagged stream, XPBDFEM/Geo.cpp:697-811): each sweep solves every tet, then
  * every hex, each kind in a colouring of its own. Such a mesh with the
- * continuous-pressure models (energy 8-10) or with quadratic elements, and a
- * T10 or H27 body with the continuous-pressure models, return
- * XFEM_EUNSUPPORTED. */
+ * continuous-pressure models (energy 8-10) or with quadratic elements, an
+ * H27 body with the continuous-pressure models, and a T10 body whose
+ * one-rings exceed 64 T10s or 128 nodes (XFEM_ELIMIT) are refused. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -370,7 +372,10 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
  * colour_begin needs room for vertices + 1 entries. Any output may be NULL.
  * xfem_get_ring_schedule reads a handle's (XFEM_EUNSUPPORTED for a body that
  * is not in one-ring mode); xfem_compute_ring_schedule computes the one
- * xfem_create_ex would build, without a GPU. */
+ * xfem_create_ex would build, without a GPU. A T10 body rings the mesh's own
+ * vertices; two of its rings that share an edge node share that edge's
+ * vertices, so its schedule is the one of the linear tet mesh (vert_order
+ * then lists mesh vertices only). */
 int xfem_get_ring_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_order, uint32_t* colour_begin,
                            uint32_t* ncolours);
 int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,

@@ -200,6 +200,28 @@ def test_hex_ring_schedule_bit_exact_vs_oracle(orc, morton):
             assert np.array_equal(f["colour_vert_begin"], g["colour_vert_begin"]), name
 
 
+@pytest.mark.parametrize("morton", [True, False])
+@pytest.mark.parametrize("pattern", [0, 1])
+def test_t10_ring_schedule_is_the_linear_one(orc, morton, pattern):
+    """A T10 body rings its mesh vertices over the T10s around them. Two such
+    rings that share an edge node share that edge's two vertices, so the
+    colouring (and the order) is the linear tet mesh's: the oracle's T10 ring
+    schedule equals compute_ring_schedule of the linear mesh, and the
+    reference's own `qrings` fixtures ran in that order."""
+    nodes, idx = xfem.generate_tet_block(6, 4, 5, (0.05, 0.05, 0.05), pattern, 0.2)
+    s = xfem.compute_ring_schedule(nodes, idx, morton=morton)
+    o = orc.Quadratic(nodes, idx, 1000.0).ring_schedule(morton=int(morton))
+    assert s["colours"] == o["colours"]
+    assert np.array_equal(s["vert_order"], o["vert_order"])
+    assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])
+    if morton and pattern == 0:
+        for name in ("qrings_c1_cpixar_nu045", "qrings_wonky_cmixed_paper"):
+            g = golden(name)
+            f = xfem.compute_ring_schedule(g["nodes"], g["idx"])
+            assert np.array_equal(f["vert_order"], g["vorder"]), name
+            assert np.array_equal(f["colour_vert_begin"], g["colour_vert_begin"]), name
+
+
 # ---- linear hexahedra: the host side of hex mode ----
 def test_generate_hex_block_bit_exact():
     g = golden("hmeshgen_3x2x2_mirror_wonky")
