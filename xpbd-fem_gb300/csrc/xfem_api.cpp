@@ -171,6 +171,7 @@ struct xfem_body {
 	DevCtx ctx{};
 	uint32_t hook_wait_miss = 0;  // XFEM_HOOK_MISSING_ARRIVAL for the next stepping call
 	bool tuned = false;
+	float tune_ms = 0.0f;  // the autotuner's best trial time (3 calls), when it timed any
 	// cached CUDA graph (graph mode)
 	cudaGraphExec_t graph = nullptr;
 	uint32_t graph_nsub = 0;
@@ -1700,7 +1701,9 @@ int run(xfem_body* h, uint32_t nsub, float dt) {
 
 // Times the candidate launch configurations on a saved copy of the state and
 // keeps the fastest. The state is restored afterwards.
-int autotune(xfem_body* h, uint32_t nsub, float dt) {
+// force_time: time the pick even when it is the only candidate (the cluster
+// layout trial compares two handles by their best time).
+int autotune(xfem_body* h, uint32_t nsub, float dt, bool force_time = false) {
 	if (h->tuned) return XFEM_OK;
 	h->tuned = true;
 	const int fixed_sync = (int)h->opt.sync_mode, fixed_block = (int)h->opt.block_size;
@@ -1728,7 +1731,7 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 		h->tuned = false;
 		return fail(XFEM_EINVAL, "no launch configuration for these options");
 	}
-	if (cand.size() == 1) return set_config(h, cand[0].first, cand[0].second);
+	if (cand.size() == 1 && !force_time) return set_config(h, cand[0].first, cand[0].second);
 	DevBuf<float4> save;
 	XCUDA(save.alloc(h->vert.n));
 	XCUDA(cudaMemcpyAsync(save.p, h->vert.p, h->vert.n * sizeof(float4), cudaMemcpyDeviceToDevice, h->stream));
@@ -1762,6 +1765,7 @@ int autotune(xfem_body* h, uint32_t nsub, float dt) {
 	XCUDA(cudaStreamSynchronize(h->stream));
 	int rc = check_device_error(h);
 	if (rc) return rc;
+	h->tune_ms = best;
 	return set_config(h, pick.first, pick.second);
 }
 
@@ -1776,7 +1780,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (h->opt.block_size && (h->opt.block_size < 64 || h->opt.block_size > 1024 || h->opt.block_size % 32))
 		return fail(XFEM_EINVAL, "block_size must be a multiple of 32 in [64, 1024]");
 	if (h->opt.sync_mode > 4) return fail(XFEM_EINVAL, "sync_mode must be 0, 1, 2, 3 or 4");
-	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1 or 2");
+	if (h->opt.cluster_mode > 2) return fail(XFEM_EINVAL, "cluster_mode must be 0, 1, 2 or 3");
 	const uint32_t mode = h->opt.cluster_mode == 1 ? 0u : 1u;
 	const uint32_t morton = h->opt.no_morton ? 0u : 1u;
 	if (const int prc = precheck_inputs(nbodies, meshes, settings)) return prc;
@@ -1964,15 +1968,57 @@ int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t
 	return xfem_create_ex(node_data, node_data_count, idx_data, idx_data_count, density, settings, nullptr, out);
 }
 
+// cluster_mode 3, the tets-per-lane axis of the launch configuration: edge-star
+// clusters (up to 6 tets per lane, 192 per warp) or one tet per lane (32 per
+// warp). The cluster layout fixes the colour order, so it cannot change under
+// a handle: both layouts are built, each is tuned over block size and launch
+// form and timed on a saved copy of its state (20 substeps of 1/1200 s, the
+// state restored afterwards), and the faster handle is kept. Meshes without
+// linear-tet clusters (rings, hexes, quadratic or mixed meshes) keep the
+// first.
+static int create_tuned_layout(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings,
+                               const xfem_options* options, xfem_body** out) {
+	if (!out) return fail(XFEM_EINVAL, "null output handle");
+	*out = nullptr;
+	xfem_options o = *options;
+	std::unique_ptr<xfem_body> best;
+	for (uint32_t m : {2u, 1u}) {
+		o.cluster_mode = m;
+		xfem_body* raw = nullptr;
+		int rc = create_common(nbodies, meshes, settings, &o, &raw);
+		if (rc) {
+			if (best) break;  // e.g. the brick form forced: one tet per lane has no cube chunks
+			return rc;
+		}
+		std::unique_ptr<xfem_body> h(raw);
+		if (h->ring_mode || h->el_mode) {
+			*out = h.release();
+			return XFEM_OK;
+		}
+		h->tuned = false;  // a fixed sync_mode and block_size are still timed
+		rc = autotune(h.get(), 20, 1.0f / 1200.0f, true);
+		if (rc) return rc;
+		if (!best || h->tune_ms < best->tune_ms) best = std::move(h);
+	}
+	*out = best.release();
+	return XFEM_OK;
+}
+
+static int create_any(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings,
+                      const xfem_options* options, xfem_body** out) {
+	if (options && options->cluster_mode == 3) return create_tuned_layout(nbodies, meshes, settings, options, out);
+	return create_common(nbodies, meshes, settings, options, out);
+}
+
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data, uint32_t idx_data_count,
                    float density, const xfem_settings* settings, const xfem_options* options, xfem_body** out) {
 	const xfem_mesh m = {node_data, node_data_count, idx_data, idx_data_count, density};
-	return create_common(1, &m, settings, options, out);
+	return create_any(1, &m, settings, options, out);
 }
 
 int xfem_batch_create(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings* settings,
                       const xfem_options* options, xfem_body** out) {
-	return create_common(nbodies, meshes, settings, options, out);
+	return create_any(nbodies, meshes, settings, options, out);
 }
 
 int xfem_destroy(xfem_body* b) {
