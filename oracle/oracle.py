@@ -192,6 +192,8 @@ def lib():
         L.orc_t10_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
         L.orc_t10_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
         L.orc_ring_schedule_centres.argtypes = [P, u32, P, u32, u32, u32, u32, P, P, P]
+        L.orc_h27_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
+        L.orc_h27_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
         L.orc_t10_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
         L.orc_t10_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
         L.orc_t10_volume_f.argtypes = [P, u32, P, P]
@@ -778,6 +780,34 @@ class QuadraticHex:
         if f(w.size, _p(X), _p(V), _p(w), _p(lm), self.h27.shape[0], _p(self.h27), _p(self.ep), _p(order), nsub,
              C.byref(params), _p(contact)):
             raise ValueError("energy model not covered on quadratic hexes")
+        return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+    def ring_schedule(self, morton=1):
+        """Ring order of the continuous-pressure models over the H27s: the
+        rings of the mesh's own vertices (not the added nodes), colour-major."""
+        X = self.X0.astype(np.float32).reshape(-1)
+        n = self.X0.shape[0]
+        vorder = np.zeros(self.nv, np.uint32)
+        cb = np.zeros(self.nv + 1, np.uint32)
+        ncol = C.c_uint32()
+        if lib().orc_ring_schedule_centres(_p(X), n, _p(self.h27), 27, self.h27.shape[0], self.nv, morton, _p(vorder),
+                                           _p(cb), C.byref(ncol)):
+            raise ValueError("ring schedule limits exceeded")
+        return dict(vert_order=vorder, colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
+
+    def substeps_rings(self, X, V, w, horder, vorder, nsub, params, lock_mask=None):
+        """Substeps with a continuous-pressure model (energy 8-10)."""
+        X = np.array(X, np.float64).reshape(-1).copy()
+        V = np.array(V, np.float64).reshape(-1).copy()
+        w = np.array(w, self.dtype).copy()
+        horder = np.ascontiguousarray(horder, np.uint32)
+        vorder = np.ascontiguousarray(vorder, np.uint32)
+        lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+        contact = np.zeros(w.size, np.uint8)
+        f = lib().orc_h27_substeps_rings_f if self.dtype == np.float32 else lib().orc_h27_substeps_rings_d
+        if f(w.size, _p(X), _p(V), _p(w), _p(lm), self.h27.shape[0], _p(self.h27), _p(self.ep), _p(horder),
+             _p(vorder), self.nv, nsub, C.byref(params), _p(contact)):
+            raise ValueError("not a continuous-pressure model")
         return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
 
     def volume(self, X):

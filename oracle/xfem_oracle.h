@@ -276,6 +276,14 @@ int orc_t10_substeps_rings_f(uint32_t nv, double* X, double* V, float* w, const 
 int orc_t10_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
                              const uint32_t* t10, const double* ep, const uint32_t* torder, const uint32_t* vorder,
                              uint32_t ncorner, uint32_t nsub, const orc_params* p, uint8_t* contact);
+/* The same on an H27 mesh: rings over the H27s around each of the first
+ * ncorner nodes, PBD damping over the H27s in horder. */
+int orc_h27_substeps_rings_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nh,
+                             const uint32_t* h27, const float* ep, const uint32_t* horder, const uint32_t* vorder,
+                             uint32_t ncorner, uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_h27_substeps_rings_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nh,
+                             const uint32_t* h27, const double* ep, const uint32_t* horder, const uint32_t* vorder,
+                             uint32_t ncorner, uint32_t nsub, const orc_params* p, uint8_t* contact);
 int orc_t10_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
                        const uint32_t* t10, const float* ep, const uint32_t* order, uint32_t nsub,
                        const orc_params* p, uint8_t* contact);

@@ -322,6 +322,26 @@ CASES = [
                                         0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1]),
     ("h27volume_wonky_nh_serial_1_post", ["Qdamped", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 4, 0, 1e-3, 0.45,
                                           -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05, 1]),
+    # continuous-pressure models on quadratic hexes (SolveRing over the H27s
+    # around each mesh vertex): the `Qdamped` arguments; stdin holds the GPU's
+    # H27 colour order (PBD damping) and its ring order over the mesh's own
+    # vertices
+    ("Qrings_c1_cpixar_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("Qrings_c1_cmixed_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
+                                0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("Qrings_c1_cmixed_incompressible", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
+                                         0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("Qrings_c1_cskin_nu049", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
+                               0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
+    ("Qrings_wonky_cmixed_paper", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
+                                   -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05]),
+    ("Qrings_c1_cskin_limit", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
+                               0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1]),
+    ("Qrings_c1_cmixed_amortized_pbd", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
+                                        0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.03, 0.002, 3, 0.1]),
+    ("Qrings_wonky_cpixar_post", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
+                                  -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
     # meshes mixing tets and hexes (GeoLinear3d on one tagged stream): a
     # GenerateHexBlock mesh whose `split` cells ("checker": x + y + z even,
     # "left": x < W / 2) are GenerateTetBlock's six tets; args W H D sx sy sz
@@ -412,7 +432,7 @@ def main():
             stdin = struct.pack("<I", order.size) + order.tobytes() + struct.pack("<I", vorder.size) + vorder.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"], "vorder": vorder,
                      "colour_vert_begin": rs["colour_vert_begin"]}
-        if args[0] in ("Qordered", "Qdamped"):
+        if args[0] in ("Qordered", "Qdamped", "Qrings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]
             nodes, idx = oracle.gen_hex_block(W, H, D, (sx, sy, sz), pattern, wonk)
@@ -421,6 +441,11 @@ def main():
             order = sch["hex_order"].astype(np.uint32)
             stdin = struct.pack("<I", order.size) + order.tobytes()
             extra = {"order": order, "colour_hex_begin": sch["colour_hex_begin"]}
+            if args[0] == "Qrings":
+                rs = q.ring_schedule(morton=1)
+                vorder = rs["vert_order"].astype(np.uint32)
+                stdin += struct.pack("<I", vorder.size) + vorder.tobytes()
+                extra.update(vorder=vorder, colour_vert_begin=rs["colour_vert_begin"])
         if args[0] in ("qordered", "qdamped", "qrings"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, pattern, wonk, dens = args[1:10]

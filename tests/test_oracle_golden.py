@@ -694,3 +694,35 @@ def test_h27_schedule_is_a_valid_colouring(orc):
     for c in range(s["colours"]):
         verts = q.h27[order[cb[c]:cb[c + 1]]].reshape(-1)
         assert np.unique(verts).size == verts.size
+
+
+H27RINGS = ["Qrings_c1_cpixar_nu045", "Qrings_c1_cmixed_nu045", "Qrings_c1_cmixed_incompressible",
+            "Qrings_c1_cskin_nu049", "Qrings_wonky_cmixed_paper", "Qrings_c1_cskin_limit",
+            "Qrings_c1_cmixed_amortized_pbd", "Qrings_wonky_cpixar_post"]
+
+
+@pytest.mark.parametrize("name", H27RINGS)
+def test_h27_rings_bit_exact(orc, name):
+    """The continuous-pressure models on quadratic hexes: GeoQuadratic3d's
+    rings of the mesh's own vertices over the H27s around them (SolveRing,
+    XPBDFEM/Geo.cpp:147-225, 944-953, 971-1008; the full-energy branch on
+    the 8- and 27-point rules, XPBDFEM/Fem.cpp:983-1036) in the fixture's
+    ring order, which the centres-only ring schedule reproduces; PBD damping
+    over the H27s in the fixture's H27 order."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    q = orc.QuadraticHex(g["nodes"], g["idx"], a[9])
+    assert np.array_equal(q.schedule()["hex_order"], g["order"])
+    rs = q.ring_schedule()
+    assert np.array_equal(rs["vert_order"], g["vorder"])
+    assert np.array_equal(rs["colour_vert_begin"], g["colour_vert_begin"])
+    lm = (q.flags & 1).astype(np.uint8)
+    X1, V1, w1, _ = q.substeps_rings(q.X0, np.zeros_like(q.X0), q.w, g["order"], g["vorder"], 1,
+                                     q_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = q.substeps_rings(X1, V1, w1, g["order"], g["vorder"], a[17] - 1, q_params(orc, a, g, 1),
+                                    lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
