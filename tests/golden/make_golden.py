@@ -326,21 +326,21 @@ CASES = [
     # around each mesh vertex): the `Qdamped` arguments; stdin holds the GPU's
     # H27 colour order (PBD damping) and its ring order over the mesh's own
     # vertices
-    ("Qrings_c1_cpixar_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
+    ("h27rings_c1_cpixar_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 8, 1, 4.0 * 1.45 / 1e5, 0.45,
                                 0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
-    ("Qrings_c1_cmixed_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
+    ("h27rings_c1_cmixed_nu045", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5, 0.45,
                                 0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
-    ("Qrings_c1_cmixed_incompressible", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
+    ("h27rings_c1_cmixed_incompressible", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, C1_COMPLIANCE, 0.5,
                                          0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
-    ("Qrings_c1_cskin_nu049", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
+    ("h27rings_c1_cskin_nu049", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.49,
                                0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1]),
-    ("Qrings_wonky_cmixed_paper", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
+    ("h27rings_wonky_cmixed_paper", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 9, 1, 1e-3, 0.45,
                                    -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05]),
-    ("Qrings_c1_cskin_limit", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
+    ("h27rings_c1_cskin_limit", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 10, 1, 3.2e-4, 0.45,
                                0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1]),
-    ("Qrings_c1_cmixed_amortized_pbd", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
+    ("h27rings_c1_cmixed_amortized_pbd", ["Qrings", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, 1000.0, 9, 1, 4.0 * 1.45 / 1e5,
                                         0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.03, 0.002, 3, 0.1]),
-    ("Qrings_wonky_cpixar_post", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
+    ("h27rings_wonky_cpixar_post", ["Qrings", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, 1000.0, 8, 1, 1e-3, 0.45,
                                   -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 2, 0.05]),
     # meshes mixing tets and hexes (GeoLinear3d on one tagged stream): a
     # GenerateHexBlock mesh whose `split` cells ("checker": x + y + z even,

@@ -696,9 +696,9 @@ def test_h27_schedule_is_a_valid_colouring(orc):
         assert np.unique(verts).size == verts.size
 
 
-H27RINGS = ["Qrings_c1_cpixar_nu045", "Qrings_c1_cmixed_nu045", "Qrings_c1_cmixed_incompressible",
-            "Qrings_c1_cskin_nu049", "Qrings_wonky_cmixed_paper", "Qrings_c1_cskin_limit",
-            "Qrings_c1_cmixed_amortized_pbd", "Qrings_wonky_cpixar_post"]
+H27RINGS = ["h27rings_c1_cpixar_nu045", "h27rings_c1_cmixed_nu045", "h27rings_c1_cmixed_incompressible",
+            "h27rings_c1_cskin_nu049", "h27rings_wonky_cmixed_paper", "h27rings_c1_cskin_limit",
+            "h27rings_c1_cmixed_amortized_pbd", "h27rings_wonky_cpixar_post"]
 
 
 @pytest.mark.parametrize("name", H27RINGS)
