@@ -155,9 +155,10 @@ def envelope(make_run, checkpoints, dt, seeds=8):
 
 class H27OracleRun:
     """The oracle's state for one hex mesh read as H27s (GeoQuadratic3d),
-    stepped in the body's H27 order."""
+    stepped in the body's H27 order (and with vorder, a continuous-pressure
+    model's ring order)."""
 
-    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32):
+    def __init__(self, nodes, idx, density, settings, order, dtype=np.float32, vorder=None):
         self.q = oracle.QuadraticHex(nodes, idx, density, dtype)
         self.lock = (self.q.flags & 3).astype(np.uint8)
         self.nodes = self.q.X0.astype(np.float32).reshape(-1)
@@ -166,8 +167,13 @@ class H27OracleRun:
         self.w = self.q.w.copy()
         self.s = settings
         self.order = order
+        self.vorder = vorder
 
     def step(self, n, dt):
         p = oracle_params(self.s, dt, nodes=self.nodes)
+        if self.vorder is not None:
+            self.X, self.V, self.w, _ = self.q.substeps_rings(self.X, self.V, self.w, self.order, self.vorder, n, p,
+                                                              lock_mask=self.lock)
+            return self
         self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.order, n, p, lock_mask=self.lock)
         return self

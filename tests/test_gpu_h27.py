@@ -204,10 +204,12 @@ def test_h27_batch_each_as_alone():
 def test_h27_errors():
     nodes, idx = xfem.generate_hex_block(3, 2, 2, (0.05, 0.05, 0.05))
     h27 = xfem.default_settings().flags | xfem.ELEMENT_H27
-    for e in (8, 9, 10):
-        with pytest.raises(xfem.XfemError) as ex:
-            xfem.Body(nodes, idx, 1000.0, xfem.default_settings(flags=xfem.ELEMENT_H27 | (e << xfem.ENERGY_BIT)))
-        assert ex.value.code == xfem.EUNSUPPORTED
+    # a ring body (energy 8-10) and an element body cannot share a handle
+    with pytest.raises(xfem.XfemError) as ex:
+        xfem.Body(meshes=[(nodes, idx, 1000.0), (nodes, idx, 1000.0)],
+                  settings=[xfem.default_settings(flags=xfem.ELEMENT_H27 | (9 << xfem.ENERGY_BIT)),
+                            xfem.default_settings(flags=h27)])
+    assert ex.value.code == xfem.EUNSUPPORTED
     # linear and quadratic hexes cannot share a handle
     with pytest.raises(xfem.XfemError) as ex:
         xfem.Body(meshes=[(nodes, idx, 1000.0), (nodes, idx, 1000.0)],

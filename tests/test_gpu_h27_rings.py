@@ -1,0 +1,167 @@
+"""GPU one-ring mode on quadratic hexes: the continuous-pressure models
+(energy 8-10) on an H27 mesh (xfem_h27.cu, k_h27_rings) through the C ABI.
+
+GeoQuadratic3d builds a one-ring for every vertex of the hex mesh (not for
+the added edge, face and centre nodes) over the H27s around it
+(XPBDFEM/Geo.cpp:944-953), and SolveRing solves one constraint (pair) per
+ring with the full-energy branch of CalculateElementEnergyAndGradients on
+each H27 (XPBDFEM/Geo.cpp:147-225, XPBDFEM/Fem.cpp:983-1036: the deviatoric
+term on the 27-point rule or prefactored, (J - a)^2 on the 8 points), then
+the rings' Rayleigh damping and the PBD damping over the H27s
+(XPBDFEM/Geo.cpp:987-1008).
+
+Against the reference's own substeps run in the GPU body's ring and H27
+orders (the `h27rings_*` fixtures) and against the pinned oracle on a larger
+jittered mirrored block. Tolerances as for the other rings: positions
+within 1e-5 of max |x_ref|, velocities within 1e-3; the incompressible case
+within 3x the FP32 reference's own distance from the FP64 run of the same
+method and order.
+"""
+import numpy as np
+import pytest
+
+import xfem
+from conftest import golden, golden_args
+from helpers import H27OracleRun, rel
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 1200.0
+H27RINGS = ["h27rings_c1_cpixar_nu045", "h27rings_c1_cmixed_nu045", "h27rings_c1_cmixed_incompressible",
+            "h27rings_c1_cskin_nu049", "h27rings_wonky_cmixed_paper", "h27rings_c1_cskin_limit",
+            "h27rings_c1_cmixed_amortized_pbd", "h27rings_wonky_cpixar_post"]
+
+
+def _copy(s):
+    return xfem.default_settings(**{k: getattr(s, k) for k, _ in s._fields_})
+
+
+def ring_settings(name):
+    """Settings of an `h27rings` fixture (refgen's `Qdamped` argument order),
+    element type H27."""
+    a = golden_args(name)["args"]
+    g = golden(name)
+    dens, energy, simul, comp, nu, gx, gy, dt, nsub, lock = a[9:19]
+    d = g["derived"]
+    flags = (xfem.ELEMENT_H27 | (energy << xfem.ENERGY_BIT) | (simul << xfem.XPBD_SOLVE_BIT) |
+             (xfem.LOCK_LEFT if lock else 0) | (a[22] << 20))
+    s = xfem.default_settings(gravity=(gx, gy, 0.0), compliance=comp, poissons_ratio=nu, flags=flags, damping=a[19],
+                              pbd_damping=a[20], time_corrected_drag=float(d[2]),
+                              volume_and_time_corrected_pbd_damping=float(d[0]),
+                              amortized_volume_and_time_corrected_pbd_damping=float(d[1]))
+    return g, s, dens, dt, nsub
+
+
+def _fp64(name, s, dens, dt, nsub):
+    """The oracle's FP64 instantiation in the fixture's orders: (X1, V1, Xn, Vn)."""
+    g = golden(name)
+    o = H27OracleRun(g["nodes"], g["idx"], dens, _copy(s), g["order"], dtype=np.float64, vorder=g["vorder"])
+    o.step(1, dt)
+    X1, V1 = o.X.copy(), o.V.copy()
+    o.s.tick_id = 1
+    o.step(nsub - 1, dt)
+    return X1, V1, o.X, o.V
+
+
+@pytest.mark.parametrize("name", H27RINGS)
+def test_h27_ring_reference_parity(name):
+    g, s, dens, dt, nsub = ring_settings(name)
+    b = xfem.Body(g["nodes"], g["idx"], dens, s)
+    rs = b.ring_schedule()
+    assert np.array_equal(rs["vert_order"], g["vorder"])
+    assert np.array_equal(rs["colour_vert_begin"], g["colour_vert_begin"])
+    assert np.array_equal(b.h27_schedule()["h27_order"], g["order"])
+    b.substep(dt)
+    x1, v1 = b.positions(), b.velocities()
+    b.step_frames(1, nsub - 1, dt)
+    xn, vn = b.positions(), b.velocities()
+    if s.poissons_ratio < 0.5:
+        assert rel(x1, g["x1"].reshape(-1, 3)) <= 1e-5
+        assert rel(v1, g["v1"].reshape(-1, 3)) <= 1e-3
+        assert rel(xn, g["xn"].reshape(-1, 3)) <= 1e-5
+        assert rel(vn, g["vn"].reshape(-1, 3)) <= 1e-3
+        return
+    X1, V1, Xn, Vn = _fp64(name, s, dens, dt, nsub)
+    for got, ref, f64 in ((x1, g["x1"], X1), (v1, g["v1"], V1), (xn, g["xn"], Xn), (vn, g["vn"], Vn)):
+        e_ref = rel(ref.reshape(-1, 3), f64)
+        assert rel(got, f64) <= 3 * e_ref + 1e-7, (e_ref, rel(got, f64))
+
+
+@pytest.mark.parametrize("energy,nu,comp,damping,rtype,pbd", [
+    (xfem.ENERGY_CONTINUOUS_PIXAR, 0.45, 1e-3, 0.0, 2, 0.0),
+    (xfem.ENERGY_CONTINUOUS_MIXED, 0.40, 1e-3, 0.01, 0, 0.0),
+    (xfem.ENERGY_CONTINUOUS_SKIN, 0.45, 0.5, 0.01, 1, 0.0),
+    (xfem.ENERGY_CONTINUOUS_MIXED, 0.45, 1e-3, 0.01, 3, 0.03),
+    (xfem.ENERGY_CONTINUOUS_PIXAR, 0.45, 1e-3, 0.02, 2, 0.05),
+])
+def test_h27_ring_oracle_parity(energy, nu, comp, damping, rtype, pbd):
+    """A larger jittered mirrored hex block as H27s over 20 substeps against
+    the oracle run in the body's ring and H27 orders."""
+    nodes, idx = xfem.generate_hex_block(5, 4, 3, (0.05, 0.05, 0.05), 1, 0.2)
+    rng = np.random.default_rng(7)
+    nodes = (nodes + rng.normal(0, 0.002, nodes.shape)).astype(np.float32)
+    flags = (xfem.ELEMENT_H27 | (energy << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT |
+             (rtype << 20))
+    vc, avc = xfem.pbd_damping_coefficients(pbd, DT, 0.05)
+    s = xfem.default_settings(gravity=(0.3, -9.81, -2.0), compliance=comp, poissons_ratio=nu, flags=flags,
+                              damping=damping, pbd_damping=pbd, volume_and_time_corrected_pbd_damping=vc,
+                              amortized_volume_and_time_corrected_pbd_damping=avc)
+    b = xfem.Body(nodes, idx, 800.0, s)
+    o = H27OracleRun(nodes, idx, 800.0, _copy(s), b.h27_schedule()["h27_order"],
+                     vorder=b.ring_schedule()["vert_order"])
+    for n in (1, 19):
+        b.step_frames(1, n, DT)
+        o.step(n, DT)
+        o.s.tick_id += n
+        assert rel(b.positions(), o.X) <= 1e-5, n
+        assert rel(b.velocities(), o.V) <= 1e-3, n
+
+
+def test_h27_ring_runs_repeat_bit_for_bit():
+    """Runs agree bit for bit, in one call or one call per substep, alone or
+    batched with another body."""
+    g, s, dens, dt, nsub = ring_settings("h27rings_c1_cskin_limit")
+    out = []
+    for split in (False, True, False):
+        b = xfem.Body(g["nodes"], g["idx"], dens, s)
+        if split:
+            for _ in range(nsub):
+                b.substep(dt)
+        else:
+            b.step_frames(1, nsub, dt)
+        out.append((b.positions(), b.velocities()))
+    for x, v in out[1:]:
+        assert np.array_equal(x, out[0][0])
+        assert np.array_equal(v, out[0][1])
+    g2, s2, dens2, _, _ = ring_settings("h27rings_wonky_cpixar_post")
+    batch = xfem.Body(meshes=[(g["nodes"], g["idx"], dens), (g2["nodes"], g2["idx"], dens2)], settings=[s, s2])
+    batch.step_frames(1, nsub, dt)
+    assert np.array_equal(batch.positions(0), out[0][0])
+    alone = xfem.Body(g2["nodes"], g2["idx"], dens2, s2)
+    alone.step_frames(1, nsub, dt)
+    assert np.array_equal(batch.positions(1), alone.positions())
+
+
+def test_h27_ring_limits_and_switches():
+    """A mesh whose vertex one-ring holds more H27s than the ring layout
+    takes is refused at create (XFEM_ELIMIT); switching an H27 handle between
+    the ring and element models is refused as for every element type."""
+    nodes, idx = xfem.generate_hex_block(3, 3, 3, (0.05, 0.05, 0.05))
+    hexes = idx.reshape(-1, 9)
+    centre = 2 * 16 + 1 * 4 + 1  # vertex (1, 1, 2) of the 4x4x4 grid: 4 hexes
+    # 17 copies of one hex that holds the vertex: 17 H27s in its ring
+    ring_hex = hexes[[k for k in range(hexes.shape[0]) if centre in hexes[k, 1:]][0]]
+    bad = np.concatenate([idx, np.tile(ring_hex, 17)]).astype(np.uint32)
+    s = xfem.default_settings(flags=xfem.ELEMENT_H27 | (xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) |
+                              (1 << xfem.XPBD_SOLVE_BIT), compliance=1e-3)
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.Body(nodes, bad, 1000.0, s)
+    assert e.value.code == xfem.ELIMIT
+    b = xfem.Body(nodes, idx, 1000.0, s)
+    b.step_frames(1, 4, DT)
+    s2 = _copy(s)
+    s2.flags = xfem.ELEMENT_H27 | (4 << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT)
+    with pytest.raises(xfem.XfemError) as e:
+        b.set_settings(s2)
+    assert e.value.code == xfem.EUNSUPPORTED
+    assert np.isfinite(b.positions()).all()

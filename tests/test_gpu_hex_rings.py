@@ -148,9 +148,9 @@ def test_hex_ring_errors():
     with pytest.raises(xfem.XfemError) as e:
         b.set_settings(xfem.default_settings())
     assert e.value.code == xfem.EUNSUPPORTED
-    # H27 and T10 bodies run no continuous-pressure model
-    for el, mesh in ((xfem.ELEMENT_H27, (nodes, idx)), (xfem.ELEMENT_T10, xfem.generate_tet_block(3, 2, 2, (0.05,) * 3))):
-        s = xfem.default_settings(flags=(xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) | el, poissons_ratio=0.45)
-        with pytest.raises(xfem.XfemError) as e:
-            xfem.Body(mesh[0], mesh[1], 1000.0, s)
-        assert e.value.code == xfem.EUNSUPPORTED
+    # linear and quadratic ring bodies cannot share a handle
+    q = xfem.default_settings(flags=(xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) | xfem.ELEMENT_H27,
+                              poissons_ratio=0.45)
+    with pytest.raises(xfem.XfemError) as e:
+        xfem.Body(meshes=[(nodes, idx, 1000.0), (nodes, idx, 1000.0)], settings=[ring, q])
+    assert e.value.code == xfem.EUNSUPPORTED

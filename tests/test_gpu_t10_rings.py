@@ -139,11 +139,3 @@ def test_t10_ring_runs_repeat_bit_for_bit():
     alone.step_frames(1, nsub, dt)
     assert np.array_equal(batch.positions(1), alone.positions())
 
-
-def test_h27_rings_still_refused():
-    """The continuous-pressure models on quadratic hexes are not built."""
-    nodes, idx = xfem.generate_hex_block(2, 2, 2, (0.05, 0.05, 0.05))
-    s = xfem.default_settings(flags=xfem.ELEMENT_H27 | (xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT))
-    with pytest.raises(xfem.XfemError) as e:
-        xfem.Body(nodes, idx, 1000.0, s)
-    assert e.value.code == xfem.EUNSUPPORTED

@@ -222,6 +222,26 @@ def test_t10_ring_schedule_is_the_linear_one(orc, morton, pattern):
             assert np.array_equal(f["colour_vert_begin"], g["colour_vert_begin"]), name
 
 
+@pytest.mark.parametrize("morton", [True, False])
+@pytest.mark.parametrize("pattern", [0, 1])
+def test_h27_ring_schedule_is_the_linear_one(orc, morton, pattern):
+    """The same for H27 bodies: a ring shares an added edge, face or centre
+    node with another only through an H27 holding both centres' corners, so
+    the order is the linear hex mesh's, as the `h27rings` fixtures ran."""
+    nodes, idx = xfem.generate_hex_block(6, 4, 5, (0.05, 0.05, 0.05), pattern, 0.2)
+    s = xfem.compute_ring_schedule(nodes, idx, morton=morton)
+    o = orc.QuadraticHex(nodes, idx, 1000.0).ring_schedule(morton=int(morton))
+    assert s["colours"] == o["colours"]
+    assert np.array_equal(s["vert_order"], o["vert_order"])
+    assert np.array_equal(s["colour_vert_begin"], o["colour_vert_begin"])
+    if morton and pattern == 0:
+        for name in ("h27rings_c1_cpixar_nu045", "h27rings_wonky_cmixed_paper"):
+            g = golden(name)
+            f = xfem.compute_ring_schedule(g["nodes"], g["idx"])
+            assert np.array_equal(f["vert_order"], g["vorder"]), name
+            assert np.array_equal(f["colour_vert_begin"], g["colour_vert_begin"]), name
+
+
 # ---- linear hexahedra: the host side of hex mode ----
 def test_generate_hex_block_bit_exact():
     g = golden("hmeshgen_3x2x2_mirror_wonky")

@@ -278,8 +278,8 @@ void set_counts(BodyParams& p, const BodyHost& b) {
 	p.ntets = b.el == kElTets || b.el == kElMixed ? b.nt : b.nh;
 	p.nhexes = b.el == kElMixed ? b.nh : 0u;
 	// the rings a body damps in amortized slices: one per vertex, or on a T10
-	// mesh one per mesh vertex (the edge nodes have none)
-	p.nverts = b.el == kElT10 ? b.ncorner : b.nv;
+	// or H27 mesh one per mesh vertex (the added nodes have none)
+	p.nverts = b.el == kElT10 || b.el == kElH27 ? b.ncorner : b.nv;
 }
 
 // Whether any body needs the extended kernels: it damps (in the solve or
@@ -592,8 +592,6 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 	if (b.el == kElHexes || quad) {
 		// hexes, T10s and H27s: set-up on the host (rest state, Morton vertex
 		// ranks, the element colouring)
-		if (ring && quad && b.el == kElHexes)
-			return fail(XFEM_EUNSUPPORTED, "H27 meshes run every energy model but the continuous-pressure ones (8-10)");
 		if (quad && b.el == kElHexes)
 			prepare_h27(m, b);
 		else if (quad)
@@ -603,16 +601,19 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
 		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, nodes_per_element(b.el), morton, b.esched))
 			return fail(XFEM_ELIMIT, "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
-		if (ring && b.el == kElT10) {
-			// the continuous-pressure models on T10s: one-rings over the T10s
-			// around the mesh's own vertices (GeoQuadratic3d::Init builds no
-			// rings for the edge nodes, XPBDFEM/Geo.cpp:944-953)
+		if (ring && (b.el == kElT10 || b.el == kElH27)) {
+			// the continuous-pressure models on T10s or H27s: one-rings over the
+			// elements around the mesh's own vertices (GeoQuadratic3d::Init
+			// builds no rings for the added nodes, XPBDFEM/Geo.cpp:944-953)
+			const uint32_t per = nodes_per_element(b.el);
 			std::vector<uint32_t> off, lst;
-			incidence(b.elems.data(), b.nv, b.nh, off, lst, 10);
+			incidence(b.elems.data(), b.nv, b.nh, off, lst, per);
 			const int rc2 = build_ring_schedule(b.elems.data(), b.nv, off.data(), lst.data(), b.sched.vert_rank.data(),
-			                                    b.rings, 10, b.ncorner);
+			                                    b.rings, per, b.ncorner);
 			if (rc2 == -2)
-				return fail(XFEM_ELIMIT, "a vertex one-ring has more than " + std::to_string(kMaxQRingElems) + " T10s or " +
+				return fail(XFEM_ELIMIT, "a vertex one-ring has more than " +
+				                             std::to_string(b.el == kElH27 ? kMaxH27RingElems : kMaxQRingElems) +
+				                             (b.el == kElH27 ? " H27s or " : " T10s or ") +
 				                             std::to_string(kMaxQRingNodes) + " nodes");
 			if (rc2) return fail(XFEM_ELIMIT, "ring colour limit exceeded");
 		} else if (ring) {
@@ -755,11 +756,22 @@ int build_rings(xfem_body* h) {
 			for (uint32_t i = rs.colour_begin[c]; i < rs.colour_begin[c + 1]; i++) {
 				const uint32_t v = rs.order[i];
 				const uint32_t nn = rs.node_off[v + 1] - rs.node_off[v], nt = rs.tet_off[v + 1] - rs.tet_off[v];
-				const uint32_t npe = rs.npe, sh = npe == 10 ? 4u : npe == 8 ? 3u : 2u;
+				const uint32_t npe = rs.npe, sh = npe == 27 ? 5u : npe == 10 ? 4u : npe == 8 ? 3u : 2u;
 				hdr.push_back(make_uint4((uint32_t)node.size(), (uint32_t)(ent.size() / 2), nn | (nt << 8) | (bi << 16), i));
 				for (uint32_t n = rs.node_off[v]; n < rs.node_off[v + 1]; n++)
 					node.push_back(b.vbase + b.sched.vert_rank[rs.nodes[n]]);
 				for (uint32_t j = rs.tet_off[v]; j < rs.tet_off[v + 1]; j++) {
+					if (npe == 27) {
+						// an H27: its device element index and its 27 nodes' ring node indices
+						uint32_t wd[7] = {0, 0, 0, 0, 0, 0, 0};
+						for (int k = 0; k < 27; k++) wd[k >> 2] |= (uint32_t)rs.corner[27 * (size_t)j + k] << (8 * (k & 3));
+						ent.push_back(make_float4(__builtin_bit_cast(float, b.el_dev[rs.tets[j]]),
+						                          __builtin_bit_cast(float, wd[0]), __builtin_bit_cast(float, wd[1]),
+						                          __builtin_bit_cast(float, wd[2])));
+						ent.push_back(make_float4(__builtin_bit_cast(float, wd[3]), __builtin_bit_cast(float, wd[4]),
+						                          __builtin_bit_cast(float, wd[5]), __builtin_bit_cast(float, wd[6])));
+						continue;
+					}
 					if (npe == 10) {
 						// a T10: its device element index and its 10 nodes' ring node indices
 						uint32_t wd[3] = {0, 0, 0};
@@ -788,7 +800,7 @@ int build_rings(xfem_body* h) {
 					ent.push_back(make_float4(e[9], e[10], e[11], e[12]));
 					ent.push_back(make_float4(e[13], e[14], e[15], __builtin_bit_cast(float, cn)));
 				}
-				// each node's corners (local element << 2 (tets), << 3 (hexes) or << 4 (T10s) | corner), in
+				// each node's corners (local element << 2 (tets), << 3 (hexes), << 4 (T10s) or << 5 (H27s) | corner), in
 				// element order
 				clist.push_back((uint32_t)cwords.size());
 				const size_t ob = cwords.size();
@@ -1835,6 +1847,7 @@ int launch_mode(xfem_body* h, const DevCtx& ctx, uint32_t nsub, float dt) {
 	if (h->ring_mode) {
 		const int e = h->el_mode == kElHexes ? launch_hex_rings(ctx, 256, nsub, dt, h->stream)
 		              : h->el_mode == kElT10 ? launch_t10_rings(ctx, 128, nsub, dt, h->stream)
+		              : h->el_mode == kElH27 ? launch_h27_rings(ctx, 128, nsub, dt, h->stream)
 		                                     : launch_rings(ctx, 256, nsub, dt, h->stream);
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
@@ -2046,8 +2059,6 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	int rc = validate_settings(*s);
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (b->el == kElH27 && energy >= XFEM_ENERGY_CONTINUOUS_PIXAR && energy <= XFEM_ENERGY_CONTINUOUS_SKIN)
-		return fail(XFEM_EUNSUPPORTED, "H27 meshes run every energy model but the continuous-pressure ones (8-10)");
 	if (quadratic_type(s->flags) != (b->el == kElT10 || b->el == kElH27))
 		return fail(XFEM_EUNSUPPORTED, "switching between linear and quadratic elements (flags bits 0-3) needs a new handle");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)

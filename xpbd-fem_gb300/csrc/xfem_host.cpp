@@ -359,8 +359,11 @@ int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* o
                         const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe, uint32_t ncentre) {
 	const uint32_t kNone = 0xffffffffu;
 	if (ncentre > nverts) ncentre = nverts;
-	const uint32_t max_elems = npe == 10 ? kMaxQRingElems : npe == 8 ? kMaxRingHexes : kMaxRingTets;
-	const uint32_t max_nodes = npe == 10 ? kMaxQRingNodes : kMaxRingNodes;
+	const uint32_t max_elems = npe == 27   ? kMaxH27RingElems
+	                           : npe == 10 ? kMaxQRingElems
+	                           : npe == 8  ? kMaxRingHexes
+	                                       : kMaxRingTets;
+	const uint32_t max_nodes = npe >= 10 ? kMaxQRingNodes : kMaxRingNodes;
 	rs.npe = npe;
 	rs.nrings = ncentre;
 	rs.tet_off.assign(off, off + nverts + 1);

@@ -82,8 +82,9 @@ struct RingSchedule {
 // vertex ranks. Rings are built around the first ncentre vertices (all when
 // larger than nverts; a T10 mesh rings its own vertices, not the edge
 // nodes). Returns 0, -1 when the colour limit is exceeded, -2 when a ring
-// has more than kMaxRingTets tets (kMaxRingHexes hexes, kMaxQRingElems T10s)
-// or kMaxRingNodes vertices (kMaxQRingNodes on T10s).
+// has more than kMaxRingTets tets (kMaxRingHexes hexes, kMaxQRingElems T10s,
+// kMaxH27RingElems H27s) or kMaxRingNodes vertices (kMaxQRingNodes on T10s
+// and H27s).
 int build_ring_schedule(const uint32_t* tets, uint32_t nverts, const uint32_t* off, const uint32_t* lst,
                         const uint32_t* vert_rank, RingSchedule& rs, uint32_t npe = 4, uint32_t ncentre = 0xffffffffu);
 
@@ -231,9 +232,10 @@ constexpr uint32_t kModelRing = 5;      // ContinuousPixar (8), ContinuousMixed 
 constexpr uint32_t kMaxRingNodes = 32;  // vertices of a one-ring (one warp lane each)
 constexpr uint32_t kMaxRingTets = 64;   // tets of a one-ring (two per warp lane)
 constexpr uint32_t kMaxRingHexes = 16;  // hexes of a one-ring on a hex mesh (one per warp lane)
-constexpr uint32_t kMaxQRingNodes = 128; // nodes of a one-ring over T10s (four per warp lane)
+constexpr uint32_t kMaxQRingNodes = 128; // nodes of a one-ring over T10s or H27s (four per warp lane)
 constexpr uint32_t kMaxQRingElems = 64;  // T10s of a one-ring (two per warp lane; 48 around a vertex
                                          // on which eight mirrored cubes' diagonals meet)
+constexpr uint32_t kMaxH27RingElems = 16; // H27s of a one-ring (taken one after another; 8 on a grid)
 
 // A chunk: 32 clusters of one colour side by side (lane = cluster), stored as
 // one contiguous block that a single bulk copy brings into shared memory:
@@ -509,6 +511,7 @@ int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stre
 // of one-ring solves over the T10s around the mesh vertices, a cooperative
 // persistent launch (canonical (X, V) in and out).
 int launch_t10_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+int launch_h27_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp
 // per element (block must be 256).
 int launch_h27(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);

@@ -357,8 +357,6 @@ struct T10Elem {
 // nodes n, n + 32, n + 64 and n + 96, sums each one's contributions in T10
 // order and takes its update.
 
-constexpr uint32_t kQNodesPerLane = kMaxQRingNodes / 32u;
-
 struct QRingScratch {
 	float4 O[kMaxQRingNodes], D[kMaxQRingNodes];  // ring nodes: (O, w), (D, bits)
 	float g0[kMaxQRingElems][10][3];              // per T10 node: deviatoric gradient contribution
@@ -441,107 +439,6 @@ __device__ __forceinline__ float2 q_ring_elem(const DevCtx& C, QRingScratch& S, 
 		S.g1[j][n][2] = g[n].z;
 	}
 	return make_float2(U0, U1);
-}
-
-// The multiplier update of a T10 ring (SolveRing's last step, as
-// ring_update1 / ring_update2 with up to kQNodesPerLane nodes per lane):
-// EnergyXpbdConstrain, EnergyXpbdConstrainSimultaneous<2> with the in-solve
-// Rayleigh damping (XPBDFEM/Xpbd.h:87-215), or RayleighDamp on V (VMODE).
-template <bool DAMP, bool VMODE>
-__device__ __forceinline__ void q_ring_update(const DevCtx& C, QRingScratch& S, const BodyParams& bp, uint32_t lane,
-                                              uint32_t nn, const uint32_t dv[kQNodesPerLane],
-                                              const Vec3 g0[kQNodesPerLane], const Vec3 g1[kQNodesPerLane], bool pair,
-                                              float U0, float U1, float comp0, float comp1, float inv_dt,
-                                              float inv_dt2, float rd) {
-	const float damp = DAMP && __ldg(&bp.rayleigh_type) < 2u ? __ldg(&bp.damping) : 0.0f;
-	const bool limit = __ldg(&bp.rayleigh_type) == 1u;
-	float s00 = 0.0f, s01 = 0.0f, s11 = 0.0f, v0 = 0.0f, v1 = 0.0f;
-#pragma unroll
-	for (uint32_t k = 0; k < kQNodesPerLane; k++) {
-		const uint32_t n = lane + 32u * k;
-		if (n >= nn) continue;
-		const float w = S.O[n].w;
-		const Vec3 d = v3(S.D[n]);
-		s00 = fmaf(w, dot(g0[k], g0[k]), s00);
-		s01 = fmaf(w, dot(g1[k], g0[k]), s01);
-		s11 = fmaf(w, dot(g1[k], g1[k]), s11);
-		v0 += dot(g0[k], d);
-		v1 += dot(g1[k], d);
-	}
-	const float wgg0 = 1.0e-22f + warp_sum(s00);
-	float l0 = 0.0f, l1 = 0.0f;
-	if (!pair) {
-		// one constraint (ContinuousPixar): U0 with gradient g0
-		const float alpha = comp0 * inv_dt2;
-		if (VMODE) {
-			l0 = -warp_sum(v0) / fmaf(2.0f * U0, comp0 * inv_dt / rd, wgg0);
-		} else {
-			l0 = (-2.0f * U0) / fmaf(2.0f * U0, alpha, wgg0);
-			if (DAMP && damp > 0.0f) {
-				const float gV = warp_sum(v0), gamma = damp * inv_dt;
-				if (!limit) {
-					l0 = (-2.0f * U0 - gamma * gV) / fmaf(wgg0, 1.0f + gamma, 2.0f * U0 * alpha);
-				} else {
-					const float A = fmaf(2.0f * U0, comp0 * inv_dt / damp, wgg0);
-					const float b = (-gV - wgg0 * l0) * (A / fmaxf(A, 4.0f * wgg0));
-					l0 += b / A;
-				}
-			}
-		}
-	} else {
-		const float wgg1 = 1.0e-22f + warp_sum(s01), wgg2 = 1.0e-22f + warp_sum(s11);
-		const float alpha0 = comp0 * inv_dt2, alpha1 = comp1 * inv_dt2;
-		if (VMODE) {
-			cramer(fmaf(2.0f * U0, comp0 * inv_dt / rd, wgg0), wgg1, fmaf(2.0f * U1, comp1 * inv_dt / rd, wgg2),
-			       -warp_sum(v0), -warp_sum(v1), l0, l1);
-		} else {
-			cramer(fmaf(2.0f * U0, alpha0, wgg0), wgg1, fmaf(2.0f * U1, alpha1, wgg2), -2.0f * U0, -2.0f * U1, l0, l1);
-			if (DAMP && damp > 0.0f) {
-				const float gV0 = warp_sum(v0), gV1 = warp_sum(v1), gamma = damp * inv_dt;
-				float A0, A2, b0 = -2.0f * U0, b1 = -2.0f * U1;
-				if (!limit) {
-					const float sc = 1.0f / (1.0f + gamma);
-					A0 = wgg0 + (2.0f * U0 * alpha0) * sc;
-					A2 = wgg2 + (2.0f * U1 * alpha1) * sc;
-					b0 = (b0 - gamma * gV0) * sc;
-					b1 = (b1 - gamma * gV1) * sc;
-				} else {
-					A0 = fmaf(2.0f * U0, alpha0, wgg0);
-					A2 = fmaf(2.0f * U1, alpha1, wgg2);
-				}
-				cramer(A0, wgg1, A2, b0, b1, l0, l1);
-				if (limit) {
-					const float B0 = fmaf(2.0f * U0, comp0 * inv_dt / damp, wgg0);
-					const float B2 = fmaf(2.0f * U1, comp1 * inv_dt / damp, wgg2);
-					float e0 = fmaf(b0, -1.0f - alpha0 * l0, -gV0), e1 = fmaf(b1, -1.0f - alpha1 * l1, -gV1);
-					e0 *= B0 / fmaxf(B0, 8.0f * wgg0);
-					e1 *= B2 / fmaxf(B2, 8.0f * wgg2);
-					float d0, d1;
-					cramer(B0, wgg1, B2, e0, e1, d0, d1);
-					l0 += d0;
-					l1 += d1;
-				}
-			}
-		}
-	}
-#pragma unroll
-	for (uint32_t k = 0; k < kQNodesPerLane; k++) {
-		const uint32_t n = lane + 32u * k;
-		if (n >= nn) continue;
-		const float w = S.O[n].w;
-		float4 Dn = S.D[n];
-		if (pair) {
-			Dn.x = fmaf(w, fmaf(l1, g1[k].x, l0 * g0[k].x), Dn.x);
-			Dn.y = fmaf(w, fmaf(l1, g1[k].y, l0 * g0[k].y), Dn.y);
-			Dn.z = fmaf(w, fmaf(l1, g1[k].z, l0 * g0[k].z), Dn.z);
-		} else {
-			const float sc = w * l0;
-			Dn.x = fmaf(sc, g0[k].x, Dn.x);
-			Dn.y = fmaf(sc, g0[k].y, Dn.y);
-			Dn.z = fmaf(sc, g0[k].z, Dn.z);
-		}
-		st_vertex(C.vert + 2 * (size_t)dv[k], S.O[n], Dn);
-	}
 }
 
 // Ring entry j of the ring whose entries start at e0: the T10's device index,

@@ -675,7 +675,7 @@ class Body:
         cb = np.zeros(nv + 1, np.uint32)
         ncol = C.c_uint32()
         _check(lib().xfem_get_ring_schedule(self._h, body, _p(order), _p(cb), C.byref(ncol)))
-        # a T10 body rings its mesh vertices only, not the edge nodes
+        # a T10 or H27 body rings its mesh vertices only, not the added nodes
         return dict(vert_order=order[:cb[ncol.value]], colour_vert_begin=cb[:ncol.value + 1], colours=ncol.value)
 
     # -- reverse-mode adjoint (no reference counterpart; see include/xfem.h)
