@@ -218,9 +218,9 @@ int xfem_settings_default(xfem_settings* s);
  * mesh mixing tets and hexes is one body holding both (GeoLinear3d on one
  * tagged stream, XPBDFEM/Geo.cpp:697-811): each sweep solves every tet, then
  * every hex, each kind in a colouring of its own. Such a mesh with the
- * continuous-pressure models (energy 8-10) or with quadratic elements, an
- * H27 body with the continuous-pressure models, and a T10 body whose
- * one-rings exceed 64 T10s or 128 nodes (XFEM_ELIMIT) are refused. */
+ * continuous-pressure models (energy 8-10) or with quadratic elements is
+ * refused (XFEM_EUNSUPPORTED), and so is a T10 or H27 body whose one-rings
+ * exceed 64 T10s (16 H27s) or 128 nodes (XFEM_ELIMIT). */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -376,10 +376,10 @@ int xfem_compute_schedule(const float* node_data, uint32_t node_data_count, cons
  * colour_begin needs room for vertices + 1 entries. Any output may be NULL.
  * xfem_get_ring_schedule reads a handle's (XFEM_EUNSUPPORTED for a body that
  * is not in one-ring mode); xfem_compute_ring_schedule computes the one
- * xfem_create_ex would build, without a GPU. A T10 body rings the mesh's own
- * vertices; two of its rings that share an edge node share that edge's
- * vertices, so its schedule is the one of the linear tet mesh (vert_order
- * then lists mesh vertices only). */
+ * xfem_create_ex would build, without a GPU. A T10 or H27 body rings the
+ * mesh's own vertices; two of its rings that share an added node share the
+ * vertices of the edge, face or element it belongs to, so its schedule is the
+ * one of the linear mesh (vert_order then lists mesh vertices only). */
 int xfem_get_ring_schedule(const xfem_body* b, uint32_t body, uint32_t* vert_order, uint32_t* colour_begin,
                            uint32_t* ncolours);
 int xfem_compute_ring_schedule(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -472,8 +472,10 @@ int xfem_compute_t10_schedule(const float* node_data, uint32_t node_data_count, 
  * 0-3 runs as GeoQuadratic3d on hexes (XPBDFEM/Geo.cpp:836-1053): a node on
  * every edge and face and at every hex centre, 27-node elements
  * (ElementParamsQuadraticHex, SolveElement with PointsLo = 8 and PointsHi =
- * 27). The body's vertices are the mesh's own, then the edge, face and centre
- * nodes. */
+ * 27). With the continuous-pressure models (8-10) one constraint pair per
+ * one-ring of a mesh vertex over the H27s around it (XPBDFEM/Geo.cpp:944-953,
+ * 973-982), up to 16 H27s and 128 nodes per ring. The body's vertices are the
+ * mesh's own, then the edge, face and centre nodes. */
 /* H27s, edge nodes and face nodes of one body; XFEM_EUNSUPPORTED for another body. */
 int xfem_body_h27_count(const xfem_body* b, uint32_t body, uint32_t* nh27, uint32_t* nedges, uint32_t* nquads);
 /* Rest state per H27 (caller hex order) as 703 floats, ElementParamsQuadraticHex
