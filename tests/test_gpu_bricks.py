@@ -188,3 +188,21 @@ def test_bricks_follow_material_changes():
     a.step_frames(1, 10, DT)
     b.step_frames(1, 10, DT)
     _same(a, b)
+
+
+def test_two_bricks_per_sm_on_the_throughput_mesh():
+    """A mesh with three chunks or more per brick and colour at two bricks
+    per SM (the 1,572,864-tet throughput mesh) is split that way, runs blocks
+    of 192 threads, and stays bit-identical to the persistent kernel."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    w = W.throughput()
+    sdt = w["dt"] / w["substeps"]
+    a = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], sync_mode=1, block_size=256)
+    b = xfem.Body(w["nodes"], w["idx"], w["density"], w["settings"], sync_mode=4)
+    info = b.info()
+    assert info["bricks"] == 2 * sms and info["block_size"] == 192 and info["sync_mode"] == 4
+    for h in (a, b):
+        h.set_lock_mask(w["lock"])
+        h.step_frames(1, w["substeps"], sdt)
+    _same(a, b)

@@ -171,6 +171,7 @@ struct xfem_body {
 	DevCtx ctx{};
 	uint32_t hook_wait_miss = 0;  // XFEM_HOOK_MISSING_ARRIVAL for the next stepping call
 	bool tuned = false;
+	int brick_block = 256;  // the brick form's default block size (192 with two bricks per SM)
 	float tune_ms = 0.0f;  // the autotuner's best trial time (3 calls), when it timed any
 	// cached CUDA graph (graph mode)
 	cudaGraphExec_t graph = nullptr;
@@ -1036,10 +1037,11 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
                  const std::vector<ChunkMeta>& meta, const std::vector<uint32_t>& lane_dv,
                  const std::vector<uint8_t>& lane_nv) {
 	const uint32_t ncol = h->ncolours, nch = (uint32_t)meta.size();
-	int sms = 0, optin = 0;
+	int sms = 0, optin = 0, per_sm_smem = 0;
 	XCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
 	XCUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device));
-	const int64_t cap = ((int64_t)optin - 8 * (int64_t)kBrickChunkBytes - 4096) / kBrickVertexBytes;
+	XCUDA(cudaDeviceGetAttribute(&per_sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, h->device));
+	int64_t cap = ((int64_t)optin - 8 * (int64_t)kBrickChunkBytes - 4096) / kBrickVertexBytes;
 	if (cap <= 0 || ncol > 64) return XFEM_OK;
 	// populated lanes, keyed by their lowest device vertex
 	std::vector<uint64_t> lanes;
@@ -1055,8 +1057,20 @@ int build_bricks(xfem_body* h, const std::vector<uint32_t>& ccb, const std::vect
 	if (lanes.empty()) return XFEM_OK;
 	std::sort(lanes.begin(), lanes.end());
 	const uint64_t L = lanes.size();
-	// one brick per SM (or xfem_options.bricks), about one chunk per brick and colour at least
-	const uint64_t want = h->opt.bricks ? (uint64_t)h->opt.bricks : (uint64_t)sms;
+	// one brick per SM (or xfem_options.bricks), about one chunk per brick and colour at least.
+	// Two bricks per SM, each with blocks of 192 threads, when each still gets three chunks
+	// per colour or more: one brick's neighbour waits and barrier then overlap the other's
+	// solves (the throughput mesh, 3.4 chunks per brick and colour: 0.979 ms per frame
+	// against 0.990 with one brick of 256 threads). Their private vertices are capped so
+	// that two blocks of six chunk buffers fit one SM.
+	const bool pairs = !h->opt.bricks && L >= 3ull * 2 * (uint64_t)sms * kLanes * ncol;
+	if (pairs) {
+		const int64_t cap2 = ((int64_t)per_sm_smem / 2 - 1024 - 6 * (int64_t)kBrickChunkBytes - 4096) / kBrickVertexBytes;
+		cap = std::min(cap, cap2);
+		if (cap <= 0) return XFEM_OK;
+	}
+	h->brick_block = pairs ? 192 : 256;
+	const uint64_t want = h->opt.bricks ? (uint64_t)h->opt.bricks : (uint64_t)sms * (pairs ? 2u : 1u);
 	const uint32_t nb = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(want, L / ((uint64_t)kLanes * ncol)));
 	std::vector<uint32_t> brick_of((size_t)nch * kLanes, 0xffffffffu);
 	for (uint64_t j = 0; j < L; j++) brick_of[(uint32_t)lanes[j]] = (uint32_t)(j * nb / L);
@@ -1827,7 +1841,7 @@ int create_common(uint32_t nbodies, const xfem_mesh* meshes, const xfem_settings
 	if (rc) return rc;
 	// default configuration until the first step tunes it
 	rc = set_config(h.get(), h->opt.sync_mode ? (int)h->opt.sync_mode : 1,
-	                h->opt.block_size ? (int)h->opt.block_size : h->opt.sync_mode == 4 ? 256 : 128);
+	                h->opt.block_size ? (int)h->opt.block_size : h->opt.sync_mode == 4 ? h->brick_block : 128);
 	if (rc) return rc;
 	if (h->opt.sync_mode && h->opt.block_size) h->tuned = true;
 	*out = h.release();
