@@ -278,6 +278,7 @@ def run_xfem(args, world, rank, local):
     # end to end through the public API with pinned host buffers
     px = np.frombuffer((ctypes_buffer(xfem, 3 * nv)), np.float32)
     pv = np.frombuffer((ctypes_buffer(xfem, 3 * nv)), np.float32)
+    po = np.frombuffer((ctypes_buffer(xfem, 3 * nv)), np.float32)  # the read-back, pinned too
     px[:] = w["nodes"]
     pv[:] = 0.0
     e2e_steps = max(3, min(args.steps, 20))
@@ -293,7 +294,7 @@ def run_xfem(args, world, rank, local):
         body.set_positions(px)
         body.set_velocities(pv)
         body.step_frames(1, S, sdt)
-        out = body.positions()
+        out = body.positions(out=po)
         e2e_t += time.perf_counter() - t0
         px[:] = out.reshape(-1)
     e2e_t = reduce_max(e2e_t, world)

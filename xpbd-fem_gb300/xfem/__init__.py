@@ -526,17 +526,22 @@ class Body:
         _check(lib().xfem_synchronize(self._h))
 
     # -- state
-    def _get(self, fn, body, width, dtype=np.float32):
+    def _get(self, fn, body, width, dtype=np.float32, out=None):
         nv = self.counts[body][0]
-        out = np.zeros(nv * width, dtype)
+        if out is None:
+            out = np.zeros(nv * width, dtype)
+        elif out.dtype != dtype or out.size != nv * width or not out.flags["C_CONTIGUOUS"]:
+            raise ValueError("out must be a contiguous %s array of %d values" % (np.dtype(dtype).name, nv * width))
         _check(fn(self._h, body, _p(out)))
         return out.reshape(nv, width) if width > 1 else out
 
-    def positions(self, body=0):
-        return self._get(lib().xfem_get_positions, body, 3)
+    def positions(self, body=0, out=None):
+        """Positions in caller vertex order; `out` (optional): a caller array
+        of 3 * vertices floats to read into (for instance pinned memory)."""
+        return self._get(lib().xfem_get_positions, body, 3, out=out)
 
-    def velocities(self, body=0):
-        return self._get(lib().xfem_get_velocities, body, 3)
+    def velocities(self, body=0, out=None):
+        return self._get(lib().xfem_get_velocities, body, 3, out=out)
 
     def inverse_masses(self, body=0):
         return self._get(lib().xfem_get_inverse_masses, body, 1)
