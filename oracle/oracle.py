@@ -193,6 +193,15 @@ def lib():
         L.orc_t10_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
         L.orc_ring_schedule_centres.argtypes = [P, u32, P, u32, u32, u32, u32, P, P, P]
         L.orc_h27_substeps_rings_f.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
+        L.orc_quad_mesh.argtypes = [P, u32, u32, P, P, P, P, P, P]
+        L.orc_qmixed_init_rest_f.argtypes = [P, u32, P, u32, P, u32, P, u32, P, u32, P, P, C.c_float, P, P, P, P, P]
+        L.orc_qmixed_init_rest_d.argtypes = [P, u32, P, u32, P, u32, P, u32, P, u32, P, P, C.c_double, P, P, P, P, P]
+        L.orc_qmixed_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_qmixed_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P, P, u32, P, P]
+        L.orc_qmixed_volume_f.argtypes = [P, u32, P, P, u32, P, P]
+        L.orc_qmixed_volume_f.restype = C.c_float
+        L.orc_qmixed_volume_d.argtypes = [P, u32, P, P, u32, P, P]
+        L.orc_qmixed_volume_d.restype = C.c_double
         L.orc_h27_substeps_rings_d.argtypes = [u32, P, P, P, P, u32, P, P, P, P, u32, u32, P, P]
         L.orc_t10_substeps_f.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
         L.orc_t10_substeps_d.argtypes = [u32, P, P, P, P, u32, P, P, P, u32, P, P]
@@ -814,6 +823,83 @@ class QuadraticHex:
         X = np.ascontiguousarray(X, np.float64).reshape(-1)
         f = lib().orc_h27_volume_f if self.dtype == np.float32 else lib().orc_h27_volume_d
         return f(_p(X), self.h27.shape[0], _p(self.h27), _p(self.ep))
+
+
+def quad_mesh(idx, nv):
+    """Connectivity3d's edges and quads of a tagged stream that may mix tets
+    and hexes, and GeoQuadratic3d's indices: (edges[ne, 2], quads[nq, 4],
+    t10[nt, 10], h27[nh, 27])."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    tets, hexes, _ = parse_mixed(idx)
+    nt, nh = tets.shape[0], hexes.shape[0]
+    edges = np.zeros((max(6 * nt + 12 * nh, 1), 2), np.uint32)
+    quads = np.zeros((max(6 * nh, 1), 4), np.uint32)
+    t10 = np.zeros((nt, 10), np.uint32)
+    h27 = np.zeros((nh, 27), np.uint32)
+    ne, nq = C.c_uint32(), C.c_uint32()
+    if lib().orc_quad_mesh(_p(idx), idx.size, nv, _p(edges), C.byref(ne), _p(quads), C.byref(nq), _p(t10), _p(h27)):
+        raise ValueError("not a stream of tets and hexes")
+    return edges[:ne.value].copy(), quads[:nq.value].copy(), t10, h27
+
+
+class QuadraticMixed:
+    """A mesh mixing tets and hexes as GeoQuadratic3d builds it: T10s and
+    H27s in one body."""
+
+    def __init__(self, nodes, idx, density, dtype=np.float32):
+        nodes = np.ascontiguousarray(nodes, np.float32).reshape(-1)
+        self.tets, self.hexes, self.nv = parse_mixed(idx)
+        self.edges, self.quads, self.t10, self.h27 = quad_mesh(idx, self.nv)
+        nt, nh = self.tets.shape[0], self.hexes.shape[0]
+        ne, nq = self.edges.shape[0], self.quads.shape[0]
+        n = self.nv + ne + nq + nh
+        self.X0 = np.zeros((n, 3), np.float64)
+        self.ept = np.zeros((nt, T10_EP), dtype)
+        self.eph = np.zeros((nh, H27_EP), dtype)
+        self.w = np.zeros(n, dtype)
+        self.flags = np.zeros(n, np.uint8)
+        f = lib().orc_qmixed_init_rest_f if dtype == np.float32 else lib().orc_qmixed_init_rest_d
+        f(_p(nodes), self.nv, _p(self.edges), ne, _p(self.quads), nq, _p(self.hexes), nh, _p(self.tets), nt,
+          _p(self.t10), _p(self.h27), density, _p(self.X0), _p(self.ept), _p(self.eph), _p(self.w), _p(self.flags))
+        self.dtype = dtype
+
+    def schedules(self, morton=1):
+        """The T10 colouring and the H27 colouring over all vertices' ranks."""
+        X = self.X0.astype(np.float32)
+        n = X.shape[0]
+        out = {}
+        for name, el, per, fn in (("t10", self.t10, 10, lib().orc_t10_schedule),
+                                  ("h27", self.h27, 27, lib().orc_h27_schedule)):
+            ne = el.shape[0]
+            rank = np.zeros(n, np.uint32)
+            order = np.zeros(ne, np.uint32)
+            cb = np.zeros(ne + 1, np.uint32)
+            ncol = C.c_uint32()
+            if fn(_p(X), n, _p(el), ne, morton, _p(rank), _p(order), _p(cb), C.byref(ncol)):
+                raise ValueError("schedule needs more than 4096 colours")
+            out[name + "_order"] = order
+            out["colour_" + name + "_begin"] = cb[:ncol.value + 1]
+            out["vert_rank"] = rank
+        return out
+
+    def substeps(self, X, V, w, torder, horder, nsub, params, lock_mask=None):
+        X = np.array(X, np.float64).reshape(-1).copy()
+        V = np.array(V, np.float64).reshape(-1).copy()
+        w = np.array(w, self.dtype).copy()
+        torder = np.ascontiguousarray(torder, np.uint32)
+        horder = np.ascontiguousarray(horder, np.uint32)
+        lm = None if lock_mask is None else np.ascontiguousarray(lock_mask, np.uint8)
+        contact = np.zeros(w.size, np.uint8)
+        f = lib().orc_qmixed_substeps_f if self.dtype == np.float32 else lib().orc_qmixed_substeps_d
+        if f(w.size, _p(X), _p(V), _p(w), _p(lm), self.t10.shape[0], _p(self.t10), _p(self.ept), _p(torder),
+             self.h27.shape[0], _p(self.h27), _p(self.eph), _p(horder), nsub, C.byref(params), _p(contact)):
+            raise ValueError("energy model not covered on quadratic mixed meshes")
+        return X.reshape(-1, 3), V.reshape(-1, 3), w, contact
+
+    def volume(self, X):
+        X = np.ascontiguousarray(X, np.float64).reshape(-1)
+        f = lib().orc_qmixed_volume_f if self.dtype == np.float32 else lib().orc_qmixed_volume_d
+        return f(_p(X), self.t10.shape[0], _p(self.t10), _p(self.ept), self.h27.shape[0], _p(self.h27), _p(self.eph))
 
 
 def solve_h27(X, w, ep, params, O, dtype=np.float32):

@@ -67,6 +67,12 @@
  *       order (each u32 count, then the ids) into tOrder and hOrder and runs
  *       Geo3d::Substep as `damped` does: every tet, then every hex
  *       (XPBDFEM/Geo.cpp:777-811).
+ *   qmixed (the arguments and stdin of `mixed`)
+ *       GeoQuadratic3d::Init on the same stream (XPBDFEM/Geo.cpp:836-953):
+ *       every vertex position (corners, edge midpoints, quad centres, hex
+ *       centres), the T10 and H27 indices and records, w and the flags;
+ *       then the T10 order and the H27 order into tOrder and hOrder and
+ *       Geo3d::Substep: every T10, then every H27 (XPBDFEM/Geo.cpp:955-1008).
  *
  * Linear hexahedra: the same commands prefixed with `h` run on a
  * GenerateHexBlock mesh (XPBDFEM/MeshGen.cpp:156-221) and always take the
@@ -477,6 +483,50 @@ int main(int argc, char** argv) {
 		Settings s = make_settings(energy, simul, compliance, poisson, gx, gy, lockLeft);
 		set_damping(s, dt, F(12), F(13), F(14), U(15), F(16));
 		s.volumePasses = U(17);
+		if (quad) {
+			// GeoQuadratic3d on the same stream: T10s and H27s in one body
+			s.flags = (s.flags & ~(Settings_ElementTypeMask << Settings_ElementTypeBit)) | (Element_T10 << Settings_ElementTypeBit);
+			GeoQuadratic3d* q = alloc->New<GeoQuadratic3d>();
+			q->Init(alloc, density, nodes.data(), nodeCount, idx.data(), idxCount, false);
+			emit("nodes", 'f', nodes.data(), nodeCount);
+			emit("idx", 'I', idx.data(), idxCount);
+			const uint32_t nt = q->con.tetCount, nh = q->con.hexCount, nv = q->vertCount;
+			std::vector<double> x0(nv * 3);
+			for (uint32_t i = 0; i < nv; i++)
+				for (int k = 0; k < 3; k++) x0[i * 3 + k] = q->X0[i][k];
+			std::vector<uint32_t> ti(nt * 10), hi(nh * 27);
+			std::vector<float> qep(nt * 56), hep(nh * 703);
+			for (uint32_t i = 0; i < nt; i++) {
+				for (int c = 0; c < 10; c++) ti[i * 10 + c] = q->t[i].i[c];
+				t10_record(q->t[i].ep, &qep[i * 56]);
+			}
+			for (uint32_t i = 0; i < nh; i++) {
+				for (int c = 0; c < 27; c++) hi[i * 27 + c] = q->h[i].i[c];
+				h27_record(q->h[i].ep, &hep[i * 703]);
+			}
+			std::vector<uint8_t> flags(q->flags, q->flags + nv);
+			emit("x0", 'd', x0.data(), x0.size());
+			emit("t10_idx", 'I', ti.data(), ti.size());
+			emit("h27_idx", 'I', hi.data(), hi.size());
+			emit("qep", 'f', qep.data(), qep.size());
+			emit("h27ep", 'f', hep.data(), hep.size());
+			emit("w", 'f', q->w, nv);
+			emit("vflags", 'B', flags.data(), nv);
+			uint32_t n = 0;
+			if (!rd(&n, 4) || n != nt || !rd(q->tOrder, 4 * (size_t)n)) { fprintf(stderr, "bad tet order\n"); return 3; }
+			if (!rd(&n, 4) || n != nh || !rd(q->hOrder, 4 * (size_t)n)) { fprintf(stderr, "bad hex order\n"); return 3; }
+			Manipulator manip;
+			manip.pickedGeo = nullptr;
+			for (uint32_t k = 0; k < nsub; k++) {
+				s.tickId = k;
+				q->Substep(s, manip, dt);
+				if (k == 0) dump_state(q, "x1", "v1");
+			}
+			dump_state(q, "xn", "vn");
+			float vol = q->CalculateVolume();
+			emit("volume", 'f', &vol, 1);
+			return 0;
+		}
 		GeoLinear3d* g = alloc->New<GeoLinear3d>();
 		g->Init(alloc, density, nodes.data(), nodeCount, idx.data(), idxCount, false);
 		emit("nodes", 'f', nodes.data(), nodeCount);

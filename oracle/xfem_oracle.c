@@ -1025,6 +1025,183 @@ done:
 	return rc;
 }
 
+/* Connectivity3d's edges and quads of a tagged stream that may mix tets and
+ * hexes (XPBDFEM/Connectivity.cpp:371-530): every element files its edge
+ * instances (a tet's 6, a hex's 12) under their lower vertex, and a hex its 6
+ * quad instances under their smallest vertex, in stream order; duplicates
+ * take the list's last entry in their place; edges and quads are numbered
+ * vertex by vertex. Then GeoQuadratic3d's element indices (XPBDFEM/Geo.cpp:
+ * 893-931): per tet (tet order) its corners and nv + the edges (0,1) (0,2)
+ * (0,3) (1,2) (1,3) (2,3); per hex (hex order) the 27 nodes of its 3x3x3
+ * grid, the centre nv + ne + nq + its hex index. t10 / h27 may be NULL. */
+int orc_quad_mesh(const uint32_t* idx, uint32_t count, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* quads,
+                  uint32_t* nquads, uint32_t* t10, uint32_t* h27) {
+	static const int te[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+	static const int he[12][2] = {{0, 1}, {0, 2}, {0, 4}, {1, 3}, {1, 5}, {2, 3}, {2, 6}, {3, 7}, {4, 5}, {4, 6}, {5, 7}, {6, 7}};
+	static const int hq[6][4] = {{0, 1, 3, 2}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 2, 6, 4}, {1, 3, 7, 5}};
+	uint32_t nt = 0, nh = 0, nvs = 0;
+	if (orc_parse_mixed(idx, count, NULL, &nt, NULL, &nh, &nvs) || nvs > nv) return -1;
+	const size_t ni = 6 * (size_t)nt + 12 * (size_t)nh, nqi = 6 * (size_t)nh;
+	uint32_t* eoff = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* ecnt = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* eup = (uint32_t*)malloc(4 * (ni ? ni : 1));
+	uint32_t* elst = (uint32_t*)malloc(4 * (ni ? ni : 1));
+	uint32_t* ebase = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qoff = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qcnt = (uint32_t*)calloc((size_t)nv + 1, 4);
+	uint32_t* qv = (uint32_t*)malloc(16 * (nqi ? nqi : 1));
+	uint32_t* qlst = (uint32_t*)malloc(4 * (nqi ? nqi : 1));
+	uint32_t* qbase = (uint32_t*)calloc((size_t)nv + 1, 4);
+	int rc = -1;
+	if (!eoff || !ecnt || !eup || !elst || !ebase || !qoff || !qcnt || !qv || !qlst || !qbase) goto done;
+	/* two walks over the stream: count the instances per vertex, then file them */
+	for (int pass = 0; pass < 2; pass++) {
+		uint32_t eid = 0, qid = 0;
+		for (uint32_t i = 0; i < count; i += 1 + idx[i]) {
+			const uint32_t* c = idx + i + 1;
+			const int tet = idx[i] == 4u;
+			const int ne_el = tet ? 6 : 12;
+			for (int k = 0; k < ne_el; k++, eid++) {
+				const uint32_t a = c[tet ? te[k][0] : he[k][0]], b = c[tet ? te[k][1] : he[k][1]];
+				const uint32_t lo = a < b ? a : b;
+				if (pass == 0) {
+					eoff[lo + 1]++;
+				} else {
+					eup[eid] = a < b ? b : a;
+					elst[eoff[lo] + ecnt[lo]++] = eid;
+				}
+			}
+			if (tet) continue;
+			for (int f = 0; f < 6; f++, qid++) {
+				uint32_t vs[4], best = 0;
+				for (int j = 0; j < 4; j++) vs[j] = c[hq[f][j]];
+				for (int j = 1; j < 4; j++)
+					if (vs[j] < vs[best]) best = (uint32_t)j;
+				if (pass == 0) {
+					qoff[vs[best] + 1]++;
+				} else {
+					for (int j = 0; j < 4; j++) qv[4 * (size_t)qid + j] = vs[(best + (uint32_t)j) % 4];
+					qlst[qoff[vs[best]] + qcnt[vs[best]]++] = qid;
+				}
+			}
+		}
+		if (pass == 0)
+			for (uint32_t v = 0; v < nv; v++) {
+				eoff[v + 1] += eoff[v];
+				qoff[v + 1] += qoff[v];
+			}
+	}
+	for (uint32_t v = 0; v < nv; v++) {
+		uint32_t* L = elst + eoff[v];
+		for (uint32_t j = 0; j < ecnt[v]; j++)
+			for (uint32_t k = j + 1; k < ecnt[v]; k++)
+				if (eup[L[j]] == eup[L[k]]) {
+					L[k] = L[ecnt[v] - 1];
+					--ecnt[v];
+					--k;
+				}
+		uint32_t* Q = qlst + qoff[v];
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (uint32_t k = j + 1; k < qcnt[v]; k++) {
+				const uint32_t* a = qv + 4 * (size_t)Q[j];
+				const uint32_t* b = qv + 4 * (size_t)Q[k];
+				if ((a[1] == b[1] && a[2] == b[2] && a[3] == b[3]) || (a[1] == b[3] && a[2] == b[2] && a[3] == b[1])) {
+					Q[k] = Q[qcnt[v] - 1];
+					--qcnt[v];
+					--k;
+				}
+			}
+	}
+	{
+		uint32_t ne = 0, nq = 0;
+		for (uint32_t v = 0; v < nv; v++) {
+			ebase[v] = ne;
+			for (uint32_t j = 0; j < ecnt[v]; j++) {
+				edges[2 * (size_t)ne] = v;
+				edges[2 * (size_t)ne + 1] = eup[elst[eoff[v] + j]];
+				ne++;
+			}
+			qbase[v] = nq;
+			for (uint32_t j = 0; j < qcnt[v]; j++) {
+				for (int k = 0; k < 4; k++) quads[4 * (size_t)nq + k] = qv[4 * (size_t)qlst[qoff[v] + j] + k];
+				nq++;
+			}
+		}
+		*nedges = ne;
+		*nquads = nq;
+		uint32_t t = 0, h = 0;
+		for (uint32_t i = 0; i < count; i += 1 + idx[i]) {
+			const uint32_t* c = idx + i + 1;
+			if (idx[i] == 4u) {
+				if (t10) {
+					uint32_t* o = t10 + 10 * (size_t)t;
+					for (int k = 0; k < 4; k++) o[k] = c[k];
+					for (int k = 0; k < 6; k++) {
+						const uint32_t a = c[te[k][0]], b = c[te[k][1]];
+						const uint32_t l = a < b ? a : b, u = a < b ? b : a;
+						uint32_t e = 0;
+						while (edges[2 * (size_t)(ebase[l] + e) + 1] != u) e++;
+						o[4 + k] = nv + ebase[l] + e;
+					}
+				}
+				t++;
+				continue;
+			}
+			if (h27) {
+				uint32_t* o = h27 + 27 * (size_t)h;
+				for (int n = 0; n < 27; n++) {
+					const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+					int mid = 0, lo = 0, hi = 0;
+					for (int a = 0; a < 3; a++) {
+						mid += ix[a] == 1;
+						lo |= (ix[a] == 2) << a;
+						hi |= (ix[a] == 1) << a;
+					}
+					if (mid == 0) {
+						o[n] = c[lo];
+					} else if (mid == 1) {
+						const int f = hi == 1 ? 1 : hi == 2 ? 2 : 4;
+						const uint32_t a = c[lo], b = c[lo | f];
+						const uint32_t l = a < b ? a : b, u = a < b ? b : a;
+						uint32_t e = 0;
+						while (edges[2 * (size_t)(ebase[l] + e) + 1] != u) e++;
+						o[n] = nv + ebase[l] + e;
+					} else if (mid == 2) {
+						const int f1 = hi & 1 ? 1 : 2, f2 = hi & 4 ? 4 : 2;
+						const uint32_t vs[4] = {c[lo], c[lo | f1], c[lo | f1 | f2], c[lo | f2]};
+						uint32_t best = 0;
+						for (int j = 1; j < 4; j++)
+							if (vs[j] < vs[best]) best = (uint32_t)j;
+						const uint32_t v0 = vs[best], v1 = vs[(best + 1) % 4], v2 = vs[(best + 2) % 4], v3 = vs[(best + 3) % 4];
+						uint32_t q = 0;
+						for (;; q++) {
+							const uint32_t* Q = quads + 4 * (size_t)(qbase[v0] + q);
+							if ((Q[1] == v1 && Q[2] == v2 && Q[3] == v3) || (Q[1] == v3 && Q[2] == v2 && Q[3] == v1)) break;
+						}
+						o[n] = nv + ne + qbase[v0] + q;
+					} else {
+						o[n] = nv + ne + nq + h;
+					}
+				}
+			}
+			h++;
+		}
+	}
+	rc = 0;
+done:
+	free(eoff);
+	free(ecnt);
+	free(eup);
+	free(elst);
+	free(ebase);
+	free(qoff);
+	free(qcnt);
+	free(qv);
+	free(qlst);
+	free(qbase);
+	return rc;
+}
+
 int orc_h27_schedule(const float* nodes, uint32_t nv, const uint32_t* h27, uint32_t nh, uint32_t morton,
                      uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin, uint32_t* ncolours) {
 	return elem_schedule(nodes, nv, h27, nh, 27, morton, vert_rank, order, colour_begin, ncolours);

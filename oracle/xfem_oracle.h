@@ -310,6 +310,32 @@ void orc_h27_tables(float* g8, float* g27, float* n27, float* map27, float* w27)
  * smallest vertex first, capacity 24 nh) of a hex mesh, and GeoQuadratic3d's
  * H27 indices (27 per hex, nullable): corners, then nv + edge, nv + ne +
  * quad, nv + ne + nq + hex. */
+/* Connectivity3d's edges and quads of a tagged stream mixing tets and hexes,
+ * numbered as the reference numbers them, and GeoQuadratic3d's T10 (per tet)
+ * and H27 (per hex) indices; t10 / h27 may be NULL. */
+int orc_quad_mesh(const uint32_t* idx, uint32_t count, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* quads,
+                  uint32_t* nquads, uint32_t* t10, uint32_t* h27);
+/* GeoQuadratic3d on a mesh mixing tets and hexes: rest state (all vertices'
+ * positions X, T10 records ept, H27 records eph, inverse masses, flags),
+ * substeps (T10s in torder, then H27s in horder) and CalculateVolume. */
+void orc_qmixed_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* edges, uint32_t ne, const uint32_t* quads,
+                            uint32_t nq, const uint32_t* hexes, uint32_t nh, const uint32_t* tets, uint32_t nt,
+                            const uint32_t* t10, const uint32_t* h27, float density, double* X, float* ept, float* eph,
+                            float* w, uint8_t* vflags);
+void orc_qmixed_init_rest_d(const float* nodes, uint32_t nv, const uint32_t* edges, uint32_t ne, const uint32_t* quads,
+                            uint32_t nq, const uint32_t* hexes, uint32_t nh, const uint32_t* tets, uint32_t nt,
+                            const uint32_t* t10, const uint32_t* h27, double density, double* X, double* ept,
+                            double* eph, double* w, uint8_t* vflags);
+int orc_qmixed_substeps_f(uint32_t nv, double* X, double* V, float* w, const uint8_t* lock_mask, uint32_t nt,
+                          const uint32_t* t10, const float* ept, const uint32_t* torder, uint32_t nh, const uint32_t* h27,
+                          const float* eph, const uint32_t* horder, uint32_t nsub, const orc_params* p, uint8_t* contact);
+int orc_qmixed_substeps_d(uint32_t nv, double* X, double* V, double* w, const uint8_t* lock_mask, uint32_t nt,
+                          const uint32_t* t10, const double* ept, const uint32_t* torder, uint32_t nh, const uint32_t* h27,
+                          const double* eph, const uint32_t* horder, uint32_t nsub, const orc_params* p, uint8_t* contact);
+float orc_qmixed_volume_f(const double* X, uint32_t nt, const uint32_t* t10, const float* ept, uint32_t nh,
+                          const uint32_t* h27, const float* eph);
+double orc_qmixed_volume_d(const double* X, uint32_t nt, const uint32_t* t10, const double* ept, uint32_t nh,
+                           const uint32_t* h27, const double* eph);
 int orc_h27_mesh(const uint32_t* hexes, uint32_t nh, uint32_t nv, uint32_t* edges, uint32_t* nedges, uint32_t* quads,
                  uint32_t* nquads, uint32_t* h27);
 void orc_h27_init_rest_f(const float* nodes, uint32_t nv, const uint32_t* hexes, uint32_t nh, const uint32_t* edges,

@@ -367,6 +367,24 @@ CASES = [
                                               0]),
     ("mixed_c1_yeohskin_nu045_post_pbd_left", ["mixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 5, 1, 0.5,
                                                0.45, 0.0, -9.81, DT, 40, 1, 0.01, 0.05, 0.0, 2, 0.1, 0]),
+    # the same meshes as GeoQuadratic3d (T10s and H27s in one body): refgen's
+    # `qmixed`, stdin the mesh, the GPU's T10 colour order and its H27 colour
+    # order
+    ("qmixed_c1_nh_nu045_checker", ["qmixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "checker", 1000.0, 4, 1,
+                                    4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1, 0]),
+    ("qmixed_c1_nh_incompressible_left", ["qmixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 4, 1,
+                                          C1_COMPLIANCE, 0.5, 0.0, -9.81, DT, 20, 1, 0.0, 0.0, 0.0, 2, 0.1, 0]),
+    ("qmixed_wonky_yeohfast_serial_nu049_checker", ["qmixed", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, "checker", 1000.0, 7,
+                                                    0, 3.2e-4, 0.49, -2.0, -9.81, DT, 10, 1, 0.0, 0.0, 0.0, 2, 0.05, 0]),
+    ("qmixed_c1_pixar_nu045_amortized_pbd_checker", ["qmixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "checker", 1000.0, 0, 1,
+                                                     4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.03, 0.002,
+                                                     3, 0.1, 0]),
+    ("qmixed_c1_mixed_nu045_limit_left", ["qmixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 3, 1,
+                                          4.0 * 1.45 / 1e5, 0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.0, 0.0, 1, 0.1, 0]),
+    ("qmixed_wonky_nh_paper_volume_checker", ["qmixed", 4, 3, 2, 0.05, 0.05, 0.05, 1, 0.3, "checker", 1000.0, 4, 1,
+                                              1e-3, 0.45, -2.0, -9.81, DT, 10, 1, 0.01, 0.0, 0.0, 0, 0.05, 1]),
+    ("qmixed_c1_yeohskin_nu045_post_pbd_left", ["qmixed", 8, 2, 2, 0.1, 0.1, 0.1, 0, 0.0, "left", 1000.0, 5, 1, 0.5,
+                                                0.45, 0.0, -9.81, DT, 20, 1, 0.01, 0.05, 0.0, 2, 0.1, 0]),
 ]
 
 MIXED_SPLITS = {"checker": lambda x, y, z, W: (x + y + z) % 2 == 0, "left": lambda x, y, z, W: 2 * x < W}
@@ -473,6 +491,17 @@ def main():
                      struct.pack("<I", horder.size) + horder.tobytes())
             extra = {"torder": torder, "colour_tet_begin": ts["colour_tet_begin"], "horder": horder,
                      "colour_hex_begin": hs["colour_hex_begin"]}
+        if args[0] == "qmixed":
+            import oracle  # noqa: E402
+            nodes, idx = mixed_mesh(args)
+            sch = oracle.QuadraticMixed(nodes, idx, args[10]).schedules(morton=1)
+            torder, horder = sch["t10_order"].astype(np.uint32), sch["h27_order"].astype(np.uint32)
+            argv = [REFGEN, "qmixed"] + [str(a) for a in args[10:]]
+            stdin = (struct.pack("<I", nodes.size) + nodes.astype(np.float32).tobytes() + struct.pack("<I", idx.size) +
+                     idx.astype(np.uint32).tobytes() + struct.pack("<I", torder.size) + torder.tobytes() +
+                     struct.pack("<I", horder.size) + horder.tobytes())
+            extra = {"torder": torder, "colour_t10_begin": sch["colour_t10_begin"], "horder": horder,
+                     "colour_h27_begin": sch["colour_h27_begin"]}
         if args[0] in ("ordered", "damped", "rings", "locked"):
             import oracle  # noqa: E402
             W, H, D, sx, sy, sz, wonk = args[1:8]

@@ -726,3 +726,56 @@ def test_h27_rings_bit_exact(orc, name):
     assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
     assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
     assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+QMIXED = ["qmixed_c1_nh_nu045_checker", "qmixed_c1_nh_incompressible_left", "qmixed_wonky_yeohfast_serial_nu049_checker",
+          "qmixed_c1_pixar_nu045_amortized_pbd_checker", "qmixed_c1_mixed_nu045_limit_left",
+          "qmixed_wonky_nh_paper_volume_checker", "qmixed_c1_yeohskin_nu045_post_pbd_left"]
+
+
+@pytest.mark.parametrize("name", QMIXED)
+def test_quadratic_mixed_mesh_bit_exact(orc, name):
+    """GeoQuadratic3d on a mesh mixing tets and hexes (XPBDFEM/Geo.cpp:836-1008):
+    Connectivity3d's edge and quad numbering over the interleaved stream, every
+    vertex position, the T10 and H27 indices and records, the masses of all
+    T10s then all H27s in one sum; then substeps that solve every T10, then
+    every H27, and damp likewise, in the fixture's T10 and H27 colour orders,
+    which the element schedule restatement reproduces."""
+    g = golden(name)
+    a = golden_args(name)["args"]
+    dens, nsub = a[10], a[18]
+    q = orc.QuadraticMixed(g["nodes"], g["idx"], dens)
+    assert q.tets.shape[0] and q.hexes.shape[0]
+    assert np.array_equal(q.X0.reshape(-1).view(np.uint64), g["x0"].view(np.uint64))
+    assert np.array_equal(q.t10.reshape(-1), g["t10_idx"]) and np.array_equal(q.h27.reshape(-1), g["h27_idx"])
+    assert np.array_equal(q.ept.reshape(-1).view(np.uint32), g["qep"].view(np.uint32))
+    assert np.array_equal(q.eph.reshape(-1).view(np.uint32), g["h27ep"].view(np.uint32))
+    assert np.array_equal(q.w.view(np.uint32), g["w"].view(np.uint32))
+    assert np.array_equal(q.flags, g["vflags"])
+    s = q.schedules()
+    assert np.array_equal(s["t10_order"], g["torder"]) and np.array_equal(s["h27_order"], g["horder"])
+    lm = (q.flags & 1).astype(np.uint8)
+    X1, V1, w1, _ = q.substeps(q.X0, np.zeros_like(q.X0), q.w, g["torder"], g["horder"], 1,
+                               mixed_params(orc, a, g, 0), lock_mask=lm)
+    assert np.array_equal(X1.reshape(-1).view(np.uint64), g["x1"].view(np.uint64))
+    assert np.array_equal(V1.reshape(-1).view(np.uint64), g["v1"].view(np.uint64))
+    Xn, Vn, _, _ = q.substeps(X1, V1, w1, g["torder"], g["horder"], nsub - 1, mixed_params(orc, a, g, 1), lock_mask=lm)
+    assert np.array_equal(Xn.reshape(-1).view(np.uint64), g["xn"].view(np.uint64))
+    assert np.array_equal(Vn.reshape(-1).view(np.uint64), g["vn"].view(np.uint64))
+    assert np.float32(q.volume(Xn)).view(np.uint32) == g["volume"].view(np.uint32)[0]
+
+
+@pytest.mark.parametrize("pattern", [0, 1])
+def test_quad_mesh_numbering_on_pure_streams(orc, pattern):
+    """The stream-order numbering of a mixed stream reduces to the tet and
+    hex numberings on streams of one kind."""
+    nodes, idx = orc.gen_tet_block(4, 3, 2, (0.1, 0.1, 0.1), pattern, 0.3)
+    tets, nv = orc.parse_tets(idx)
+    e1, t1 = orc.tet_edges(tets, nv)
+    e2, q2, t2, _ = orc.quad_mesh(idx, nv)
+    assert np.array_equal(e1, e2) and np.array_equal(t1, t2) and q2.shape[0] == 0
+    nodes, idx = orc.gen_hex_block(4, 3, 2, (0.1, 0.1, 0.1), pattern, 0.3)
+    hexes, nv = orc.parse_hexes(idx)
+    e1, q1, h1 = orc.h27_mesh(hexes, nv)
+    e2, q2, _, h2 = orc.quad_mesh(idx, nv)
+    assert np.array_equal(e1, e2) and np.array_equal(q1, q2) and np.array_equal(h1, h2)
