@@ -98,6 +98,28 @@ class MixedOracleRun:
         return self
 
 
+class QMixedOracleRun:
+    """The oracle's state for one mesh mixing tets and hexes read as T10s and
+    H27s (GeoQuadratic3d), stepped in the body's T10 and H27 colour orders."""
+
+    def __init__(self, nodes, idx, density, settings, torder, horder, dtype=np.float32):
+        self.q = oracle.QuadraticMixed(nodes, idx, density, dtype)
+        self.lock = (self.q.flags & 3).astype(np.uint8)
+        self.nodes = self.q.X0.astype(np.float32).reshape(-1)
+        self.X = self.q.X0.copy()
+        self.V = np.zeros_like(self.X)
+        self.w = self.q.w.copy()
+        self.s = settings
+        self.torder = torder
+        self.horder = horder
+
+    def step(self, n, dt):
+        p = oracle_params(self.s, dt, nodes=self.nodes)
+        self.X, self.V, self.w, _ = self.q.substeps(self.X, self.V, self.w, self.torder, self.horder, n, p,
+                                                    lock_mask=self.lock)
+        return self
+
+
 class T10OracleRun:
     """The oracle's state for one tet mesh read as T10s (GeoQuadratic3d),
     stepped in the body's T10 order."""

@@ -241,9 +241,9 @@ def test_mixed_batch_each_as_alone():
 
 def test_mixed_errors():
     g, s, dens, dt, nsub = mixed_settings("mixed_c1_nh_nu045_checker")
-    # the continuous-pressure models and quadratic elements are refused on a
-    # mixed mesh (the reference indexes a ring's hexes two ways there)
-    for flags in (9 << xfem.ENERGY_BIT, (s.flags & ~xfem.ELEMENT_TYPE_MASK) | xfem.ELEMENT_T10):
+    # the continuous-pressure models are refused on a mixed mesh, linear or
+    # quadratic (the reference indexes a ring's hexes two ways there)
+    for flags in (9 << xfem.ENERGY_BIT, (9 << xfem.ENERGY_BIT) | xfem.ELEMENT_T10):
         with pytest.raises(xfem.XfemError) as ex:
             xfem.Body(g["nodes"], g["idx"], dens, xfem.default_settings(flags=flags))
         assert ex.value.code == xfem.EUNSUPPORTED

@@ -19,6 +19,7 @@ OUT_DIR = os.path.join(HERE, "xfem")
 LIB = os.path.join(OUT_DIR, "libxfem.so")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["xfem_kernels.cu", "xfem_adjoint.cu", "xfem_setup.cu", "xfem_rings.cu", "xfem_hexes.cu", "xfem_mixed.cu", "xfem_t10.cu",
+           "xfem_qmixed.cu",
            "xfem_h27.cu",
            "xfem_api.cpp",
            "xfem_host.cpp"]

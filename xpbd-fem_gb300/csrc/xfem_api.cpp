@@ -52,7 +52,7 @@ cudaError_t injected_alloc_failure() {
 // Element kinds of a body: linear tets (the chunked tet path, the one-ring
 // mode), linear hexahedra (H8), quadratic tets (T10) and quadratic hexahedra
 // (H27), the last three in the element kernel.
-constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2, kElH27 = 3, kElMixed = 4;
+constexpr uint32_t kElTets = 0, kElHexes = 1, kElT10 = 2, kElH27 = 3, kElMixed = 4, kElQMixed = 5;
 
 struct BodyHost {
 	uint32_t nv = 0, nt = 0, vbase = 0, tbase = 0;
@@ -68,7 +68,8 @@ struct BodyHost {
 	std::vector<uint32_t> tet_slot;   // caller tet -> global row * 32 + lane (multiplier output)
 	std::vector<uint64_t> tet_rec;    // caller tet -> float4 index of its plane-3 record in the chunk blocks
 	// element bodies (linear hexahedra or quadratic tets; no linear tets)
-	uint32_t el = 0;                  // kElTets, kElHexes, kElT10, kElH27, kElMixed (tets and hexes)
+	uint32_t el = 0;                  // kElTets, kElHexes, kElT10, kElH27, kElMixed (tets and hexes),
+	                                  // kElQMixed (T10s and H27s: the H27s in elems, the T10s in qt)
 	uint32_t nh = 0;                  // elements
 	uint32_t ncorner = 0;             // T10, H27: the mesh's own vertices; the added nodes follow
 	std::vector<uint32_t> elems;      // 8 per hex, 10 per T10 or 27 per H27, caller order
@@ -77,7 +78,11 @@ struct BodyHost {
 	std::vector<float> eep;           // rest::kHexRec per hex, rest::kT10Rec per T10, rest::kH27Rec per H27
 	ElemSchedule esched;
 	std::vector<uint32_t> el_dev;     // hexes, T10s, H27s: each element's device index (build_elements)
-	ElemSchedule tsched;              // kElMixed: the tets' own colouring (elements of 4 vertices)
+	ElemSchedule tsched;              // kElMixed: the tets' own colouring (elements of 4 vertices); kElQMixed: the T10s'
+	uint32_t nqt = 0;                 // kElQMixed: T10s (nt stays 0, as for T10 bodies)
+	std::vector<uint32_t> qt;         // kElQMixed: 10 per T10 (caller tet order)
+	std::vector<float> qtep;          // kElQMixed: rest::kT10Rec per T10
+	std::vector<uint32_t> qt_dev;     // kElQMixed: each T10's device index
 };
 
 template <typename T>
@@ -166,6 +171,12 @@ struct xfem_body {
 	DevBuf<uint4> mt_vid;
 	DevBuf<float4> mt_rec;
 	DevBuf<uint32_t> mt_cb, mt_flat;
+	// meshes mixing T10s and H27s (kElQMixed): the T10s' element arrays (the H27s use el_*)
+	DevBuf<uint4> q_vid;
+	DevBuf<float4> q_rec;
+	DevBuf<uint32_t> q_cb, q_flat;
+	DevBuf<float> q_tab;
+	uint32_t q_colours = 0, q_nel = 0;
 	uint32_t nisolated = 0, max_deps = 0;
 	LaunchCfg cfg;
 	DevCtx ctx{};
@@ -276,8 +287,8 @@ BodyParams make_params(const xfem_settings& s) {
 // its elements (hex, T10 and H27 bodies), or its tets and its hexes (a mesh
 // mixing the two, XPBDFEM/Geo.cpp:792-811).
 void set_counts(BodyParams& p, const BodyHost& b) {
-	p.ntets = b.el == kElTets || b.el == kElMixed ? b.nt : b.nh;
-	p.nhexes = b.el == kElMixed ? b.nh : 0u;
+	p.ntets = b.el == kElQMixed ? b.nqt : b.el == kElTets || b.el == kElMixed ? b.nt : b.nh;
+	p.nhexes = b.el == kElMixed || b.el == kElQMixed ? b.nh : 0u;
 	// the rings a body damps in amortized slices: one per vertex, or on a T10
 	// or H27 mesh one per mesh vertex (the added nodes have none)
 	p.nverts = b.el == kElT10 || b.el == kElH27 ? b.ncorner : b.nv;
@@ -469,8 +480,6 @@ int precheck_inputs(uint32_t nb, const xfem_mesh* meshes, const xfem_settings* s
 			if (model_of(energy) == kModelRing)
 				return fail(XFEM_EUNSUPPORTED, who + "the continuous-pressure models (energy 8-10) run on meshes of one "
 				                                     "element kind");
-			if (quadratic_type(settings[k].flags))
-				return fail(XFEM_EUNSUPPORTED, who + "quadratic elements (flags bits 0-3) on a mesh mixing tets and hexes");
 		}
 		if (nv != m.node_data_count / 3)
 			return fail(XFEM_EINVAL, who + "vertex count " + std::to_string(nv) +
@@ -555,8 +564,40 @@ void prepare_h27(const xfem_mesh& m, BodyHost& b, std::vector<double>* X = nullp
 	if (X) *X = std::move(x);
 }
 
+// GeoQuadratic3d::Init on a mesh mixing tets and hexes (XPBDFEM/Geo.cpp:
+// 836-953): Connectivity3d's edges and quads over the interleaved stream,
+// nodes on the edges, the faces and the hex centres, the T10 and H27 rest
+// state and one mass sum. The body's vertices become the corners followed by
+// those nodes; its H27s take the element arrays (elems, eep), its T10s qt
+// and qtep, and b.nqt / b.nh count them (b.nt becomes 0: no linear tets).
+void prepare_qmixed(const xfem_mesh& m, BodyHost& b) {
+	std::vector<uint32_t> t10, h27;
+	quad_mesh(m.idx_data, m.idx_data_count, b.nv, b.edges, b.quads, t10, h27);
+	const uint32_t ne = (uint32_t)(b.edges.size() / 2), nq = (uint32_t)(b.quads.size() / 4), n = b.nv + ne + nq + b.nh;
+	std::vector<double> x(3 * (size_t)n);
+	b.qtep.resize((size_t)rest::kT10Rec * b.nt);
+	b.eep.resize((size_t)rest::kH27Rec * b.nh);
+	b.w0.resize(n);
+	b.vflags.resize(n);
+	qmixed_init_rest(b.nodes.data(), b.nv, b.nt, b.elems.data(), b.nh, b.edges.data(), ne, b.quads.data(), nq,
+	                 t10.data(), h27.data(), m.density, x.data(), b.qtep.data(), b.eep.data(), b.w0.data(),
+	                 b.vflags.data());
+	b.nodes.resize(3 * (size_t)n);
+	for (size_t i = 0; i < 3 * (size_t)n; i++) b.nodes[i] = (float)x[i];
+	b.el = kElQMixed;
+	b.ncorner = b.nv;
+	b.nv = n;
+	b.elems = std::move(h27);
+	b.qt = std::move(t10);
+	b.nqt = b.nt;
+	b.tets.clear();
+	b.nt = 0;
+}
+
 // Elements of an element body, and vertices per element.
-uint32_t nodes_per_element(uint32_t el) { return el == kElH27 ? 27u : el == kElT10 ? 10u : 8u; }  // kElMixed: its hexes
+uint32_t nodes_per_element(uint32_t el) {  // kElMixed: its hexes; kElQMixed: its H27s
+	return el == kElH27 || el == kElQMixed ? 27u : el == kElT10 ? 10u : 8u;
+}
 
 // Rest state and schedule of one body: on the host (gpu false), or with the
 // parallel phases on the GPU (rest state, incidence, vertex ranks, cluster
@@ -582,7 +623,16 @@ int prepare_body(const xfem_mesh& m, const xfem_settings* s, uint32_t mode, uint
 		if (ring)
 			return fail(XFEM_EUNSUPPORTED, "the continuous-pressure models (energy 8-10) run on meshes of one element kind: "
 			                               "on a mixed mesh the reference indexes a ring's hexes two different ways");
-		if (quad) return fail(XFEM_EUNSUPPORTED, "quadratic elements (flags bits 0-3) on a mesh mixing tets and hexes");
+		if (quad) {
+			// T10s and H27s in one body, each kind with a colouring of its own
+			prepare_qmixed(m, b);
+			vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
+			if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 27, morton, b.esched) ||
+			    elem_schedule(b.nodes.data(), b.nv, b.qt.data(), b.nqt, 10, morton, b.tsched))
+				return fail(XFEM_ELIMIT,
+				            "the element colouring needs more than " + std::to_string(kMaxElemColours) + " colours");
+			return XFEM_OK;
+		}
 		host_rest(m, b);
 		vertex_ranks(b.nodes.data(), b.nv, morton, b.sched);
 		if (elem_schedule(b.nodes.data(), b.nv, b.elems.data(), b.nh, 8, morton, b.esched) ||
@@ -881,34 +931,39 @@ int build_rings(xfem_body* h) {
 // the 2x2x2 points' inverse jacobians and weights; T10 14 float4: Qi,
 // volume, surface area, QQ, QR), each element's index in its body's order,
 // and for T10s the shape-function gradients at the 4-point rule.
-int build_elements(xfem_body* h) {
-	const bool t10 = h->el_mode == kElT10, h27 = h->el_mode == kElH27;
-	const uint32_t per = nodes_per_element(h->el_mode), nvid4 = (per + 3) / 4, nrec4 = h27 ? 176u : t10 ? 14u : 30u;
+// kind: the element type of the set (kElHexes or kElMixed: hexes; kElT10;
+// kElH27); qt: the T10s of meshes mixing T10s and H27s (their qt, tsched and
+// qtep, into the q_* arrays) instead of the bodies' element arrays.
+static int build_element_set(xfem_body* h, uint32_t kind, bool qt) {
+	const bool t10 = kind == kElT10, h27 = kind == kElH27;
+	const uint32_t per = nodes_per_element(kind), nvid4 = (per + 3) / 4, nrec4 = h27 ? 176u : t10 ? 14u : 30u;
 	const size_t rsz = h27 ? rest::kH27Rec : t10 ? rest::kT10Rec : rest::kHexRec;
 	uint32_t ncol = 0, nel = 0;
 	for (const BodyHost& b : h->bodies) {
-		ncol = std::max(ncol, b.esched.ncolours);
-		nel += b.nh;
+		ncol = std::max(ncol, (qt ? b.tsched : b.esched).ncolours);
+		nel += qt ? b.nqt : b.nh;
 	}
 	std::vector<uint4> vid(nvid4 * (size_t)nel);
 	std::vector<uint32_t> cb(ncol + 1, 0), flat(nel);
 	std::vector<float4> rec(nrec4 * (size_t)nel);
 	uint32_t o = 0;
-	for (BodyHost& b : h->bodies) b.el_dev.assign(b.nh, 0);
+	for (BodyHost& b : h->bodies) (qt ? b.qt_dev : b.el_dev).assign(qt ? b.nqt : b.nh, 0);
 	for (uint32_t c = 0; c < ncol; c++) {
 		cb[c] = o;
 		for (BodyHost& b : h->bodies) {
-			const ElemSchedule& es = b.esched;
+			const ElemSchedule& es = qt ? b.tsched : b.esched;
+			const std::vector<uint32_t>& els = qt ? b.qt : b.elems;
+			std::vector<uint32_t>& dev = qt ? b.qt_dev : b.el_dev;
 			if (c >= es.ncolours) continue;
 			for (uint32_t k = es.colour_begin[c]; k < es.colour_begin[c + 1]; k++, o++) {
 				const uint32_t el = es.order[k];
-				b.el_dev[el] = o;
+				dev[el] = o;
 				uint32_t d[28] = {0};
-				for (uint32_t n = 0; n < per; n++) d[n] = b.vbase + b.sched.vert_rank[b.elems[per * (size_t)el + n]];
+				for (uint32_t n = 0; n < per; n++) d[n] = b.vbase + b.sched.vert_rank[els[per * (size_t)el + n]];
 				for (uint32_t j = 0; j < nvid4; j++)
 					vid[nvid4 * (size_t)o + j] = make_uint4(d[4 * j], d[4 * j + 1], d[4 * j + 2], d[4 * j + 3]);
 				flat[o] = k;
-				const float* e = &b.eep[rsz * el];
+				const float* e = &(qt ? b.qtep : b.eep)[rsz * el];
 				if (h27) {  // element-major, the 703 values and a pad
 					float* dst = reinterpret_cast<float*>(&rec[(size_t)o * nrec4]);
 					for (size_t j = 0; j < rsz; j++) dst[j] = e[j];
@@ -952,24 +1007,40 @@ int build_elements(xfem_body* h) {
 			for (int n = 0; n < 27; n++)
 				for (int k = 0; k < 3; k++) g4[8 * 81 + (p * 27 + n) * 3 + k] = tb.g27[p][n][k];
 	}
-	XCUDA(h->el_vid.alloc(vid.size()));
-	XCUDA(h->el_rec.alloc(rec.size()));
-	XCUDA(h->el_cb.alloc(cb.size()));
-	XCUDA(h->el_flat.alloc(flat.size()));
-	XCUDA(h->el_tab.alloc(g4.size()));
+	DevBuf<uint4>& vidb = qt ? h->q_vid : h->el_vid;
+	DevBuf<float4>& recb = qt ? h->q_rec : h->el_rec;
+	DevBuf<uint32_t>& cbb = qt ? h->q_cb : h->el_cb;
+	DevBuf<uint32_t>& flatb = qt ? h->q_flat : h->el_flat;
+	DevBuf<float>& tabb = qt ? h->q_tab : h->el_tab;
+	XCUDA(vidb.alloc(vid.size()));
+	XCUDA(recb.alloc(rec.size()));
+	XCUDA(cbb.alloc(cb.size()));
+	XCUDA(flatb.alloc(flat.size()));
+	XCUDA(tabb.alloc(g4.size()));
 	auto up = [&](void* dst, const void* src, size_t bytes) {
 		return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream) : cudaSuccess;
 	};
-	XCUDA(up(h->el_vid.p, vid.data(), vid.size() * sizeof(uint4)));
-	XCUDA(up(h->el_rec.p, rec.data(), rec.size() * sizeof(float4)));
-	XCUDA(up(h->el_cb.p, cb.data(), cb.size() * 4));
-	XCUDA(up(h->el_flat.p, flat.data(), flat.size() * 4));
-	XCUDA(up(h->el_tab.p, g4.data(), g4.size() * 4));
+	XCUDA(up(vidb.p, vid.data(), vid.size() * sizeof(uint4)));
+	XCUDA(up(recb.p, rec.data(), rec.size() * sizeof(float4)));
+	XCUDA(up(cbb.p, cb.data(), cb.size() * 4));
+	XCUDA(up(flatb.p, flat.data(), flat.size() * 4));
+	XCUDA(up(tabb.p, g4.data(), g4.size() * 4));
 	XCUDA(cudaStreamSynchronize(h->stream));
-	h->ctx.el_colours = ncol;
-	h->ctx.nel = nel;
+	if (qt) {
+		h->q_colours = ncol;
+		h->q_nel = nel;
+	} else {
+		h->ctx.el_colours = ncol;
+		h->ctx.nel = nel;
+	}
 	h->device_bytes += vid.size() * 16 + rec.size() * 16 + cb.size() * 4 + flat.size() * 4 + g4.size() * 4;
 	return XFEM_OK;
+}
+
+int build_elements(xfem_body* h) {
+	if (h->el_mode != kElQMixed) return build_element_set(h, h->el_mode, false);
+	const int rc = build_element_set(h, kElH27, false);  // the H27s in el_*
+	return rc ? rc : build_element_set(h, kElT10, true);  // the T10s in q_*
 }
 
 // The tets of every mixed body in device order (colour-major over the tets'
@@ -1866,6 +1937,20 @@ int launch_mode(xfem_body* h, const DevCtx& ctx, uint32_t nsub, float dt) {
 		if (e) return fail(XFEM_ECUDA, std::string("ring launch: ") + cudaGetErrorString((cudaError_t)e));
 		return XFEM_OK;
 	}
+	if (h->el_mode == kElQMixed) {
+		// the T10s' context: the same state with the T10 element arrays
+		DevCtx ct = ctx;
+		ct.el_vid = h->q_vid.p;
+		ct.el_rec = h->q_rec.p;
+		ct.colour_el_begin = h->q_cb.p;
+		ct.el_tab = h->q_tab.p;
+		ct.el_flat = h->q_flat.p;
+		ct.el_colours = h->q_colours;
+		ct.nel = h->q_nel;
+		const int e = launch_qmixed(ctx, ct, 256, nsub, dt, h->stream);
+		if (e) return fail(XFEM_ECUDA, std::string("element launch: ") + cudaGetErrorString((cudaError_t)e));
+		return XFEM_OK;
+	}
 	const int e = h->el_mode == kElH27     ? launch_h27(ctx, 256, nsub, dt, h->stream)
 	              : h->el_mode == kElT10   ? launch_t10(ctx, 256, nsub, dt, h->stream)
 	              : h->el_mode == kElMixed ? launch_mixed(ctx, 256, nsub, dt, h->stream)
@@ -2073,7 +2158,7 @@ int xfem_set_settings(xfem_body* h, uint32_t body, const xfem_settings* s) {
 	int rc = validate_settings(*s);
 	if (rc) return rc;
 	const uint32_t energy = (s->flags >> XFEM_ENERGY_BIT) & XFEM_ENERGY_MASK;
-	if (quadratic_type(s->flags) != (b->el == kElT10 || b->el == kElH27))
+	if (quadratic_type(s->flags) != (b->el == kElT10 || b->el == kElH27 || b->el == kElQMixed))
 		return fail(XFEM_EUNSUPPORTED, "switching between linear and quadratic elements (flags bits 0-3) needs a new handle");
 	if ((model_of(energy) == kModelRing) != h->ring_mode)
 		return fail(XFEM_EUNSUPPORTED, "switching between the continuous-pressure models (energy 8-10) and the "
@@ -2283,74 +2368,78 @@ static double hex_volume(const BodyHost& b, const float* x) {
 
 static int tet_volume(xfem_body* h, uint32_t body, double* out);
 
+// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) summed over n H27s:
+// rest volume times the weighted det F over the 3x3x3 points, in double.
+static double h27_volume(const float* x, const uint32_t* elems, const float* eep, uint32_t n) {
+	const rest::H27Tables& tb = rest::h27_tables();
+	double v = 0.0;
+	for (uint32_t q = 0; q < n; q++) {
+		const uint32_t* is = elems + 27 * (size_t)q;
+		const float* e = eep + (size_t)rest::kH27Rec * q;
+		double P[26][3];
+		for (int i = 0; i < 26; i++)
+			for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[26] + k];
+		double scale = 0.0;
+		for (int p = 0; p < 27; p++) {
+			double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+			for (int nn = 0; nn < 26; nn++)
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) Dm[c][r] += (double)tb.g27[p][nn][r] * P[nn][c];
+			const float* ji = e + rest::kH27JH + 9 * p;
+			for (int c = 0; c < 3; c++)
+				for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
+			const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+			                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+			                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+			scale += (double)e[rest::kH27WH + p] * det;
+		}
+		v += (double)e[rest::kH27Vol] * scale;
+	}
+	return v;
+}
+
+// The same over n T10s: rest volume times the mean det F over the 4 points.
+static double t10_volume(const float* x, const uint32_t* elems, const float* eep, uint32_t n) {
+	double v = 0.0;
+	for (uint32_t q = 0; q < n; q++) {
+		const uint32_t* is = elems + 10 * (size_t)q;
+		const float* e = eep + (size_t)rest::kT10Rec * q;
+		double P[9][3];
+		for (int i = 0; i < 9; i++)
+			for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[9] + k];
+		double scale = 0.0;
+		for (int p = 0; p < 4; p++) {
+			double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
+			for (int nn = 0; nn < 9; nn++)
+				for (int c = 0; c < 3; c++)
+					for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::t10_tables().g4[p][nn][r] * P[nn][c];
+			const float* qi = e + rest::kT10Qi;
+			for (int c = 0; c < 3; c++)
+				for (int r = 0; r < 3; r++) F[c][r] = qi[r] * Dm[c][0] + qi[3 + r] * Dm[c][1] + qi[6 + r] * Dm[c][2];
+			const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
+			                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
+			                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
+			scale += 0.25 * det;
+		}
+		v += (double)e[rest::kT10Vol] * scale;
+	}
+	return v;
+}
+
 int xfem_calculate_volume(xfem_body* h, uint32_t body, double* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
 	XCUDA(cudaSetDevice(h->device));
-	if (b->el == kElH27) {
-		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per H27: rest
-		// volume times the weighted det F over the 3x3x3 points, in double
+	if (b->el == kElH27 || b->el == kElT10 || b->el == kElQMixed) {
 		std::vector<float> x(3 * (size_t)b->nv);
 		const int rc = get_xyz(h, body, 0, x.data());
 		if (rc) return rc;
-		const rest::H27Tables& tb = rest::h27_tables();
-		double v = 0.0;
-		for (uint32_t q = 0; q < b->nh; q++) {
-			const uint32_t* is = &b->elems[27 * (size_t)q];
-			const float* e = &b->eep[(size_t)rest::kH27Rec * q];
-			double P[26][3];
-			for (int i = 0; i < 26; i++)
-				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[26] + k];
-			double scale = 0.0;
-			for (int p = 0; p < 27; p++) {
-				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
-				for (int n = 0; n < 26; n++)
-					for (int c = 0; c < 3; c++)
-						for (int r = 0; r < 3; r++) Dm[c][r] += (double)tb.g27[p][n][r] * P[n][c];
-				const float* ji = e + rest::kH27JH + 9 * p;
-				for (int c = 0; c < 3; c++)
-					for (int r = 0; r < 3; r++) F[c][r] = ji[r] * Dm[c][0] + ji[3 + r] * Dm[c][1] + ji[6 + r] * Dm[c][2];
-				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
-				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
-				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
-				scale += (double)e[rest::kH27WH + p] * det;
-			}
-			v += (double)e[rest::kH27Vol] * scale;
-		}
-		*out = v;
-		return XFEM_OK;
-	}
-	if (b->el == kElT10) {
-		// TCalculateElementVolume (XPBDFEM/Fem.cpp:1046-1064) per T10: rest
-		// volume times the mean det F over the 4 points, in double
-		std::vector<float> x(3 * (size_t)b->nv);
-		const int rc = get_xyz(h, body, 0, x.data());
-		if (rc) return rc;
-		double v = 0.0;
-		for (uint32_t q = 0; q < b->nh; q++) {
-			const uint32_t* is = &b->elems[10 * (size_t)q];
-			const float* e = &b->eep[(size_t)rest::kT10Rec * q];
-			double P[9][3];
-			for (int i = 0; i < 9; i++)
-				for (int k = 0; k < 3; k++) P[i][k] = (double)x[3 * (size_t)is[i] + k] - (double)x[3 * (size_t)is[9] + k];
-			double scale = 0.0;
-			for (int p = 0; p < 4; p++) {
-				double Dm[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, F[3][3];
-				for (int n = 0; n < 9; n++)
-					for (int c = 0; c < 3; c++)
-						for (int r = 0; r < 3; r++) Dm[c][r] += (double)rest::t10_tables().g4[p][n][r] * P[n][c];
-				const float* qi = e + rest::kT10Qi;
-				for (int c = 0; c < 3; c++)
-					for (int r = 0; r < 3; r++) F[c][r] = qi[r] * Dm[c][0] + qi[3 + r] * Dm[c][1] + qi[6 + r] * Dm[c][2];
-				const double det = F[0][0] * (F[1][1] * F[2][2] - F[2][1] * F[1][2]) -
-				                   F[1][0] * (F[0][1] * F[2][2] - F[2][1] * F[0][2]) +
-				                   F[2][0] * (F[0][1] * F[1][2] - F[1][1] * F[0][2]);
-				scale += 0.25 * det;
-			}
-			v += (double)e[rest::kT10Vol] * scale;
-		}
-		*out = v;
+		// a mixed quadratic mesh: its T10s, then its H27s (XPBDFEM/Geo.cpp:1048-1053)
+		*out = b->el == kElH27   ? h27_volume(x.data(), b->elems.data(), b->eep.data(), b->nh)
+		       : b->el == kElT10 ? t10_volume(x.data(), b->elems.data(), b->eep.data(), b->nh)
+		                         : t10_volume(x.data(), b->qt.data(), b->qtep.data(), b->nqt) +
+		                               h27_volume(x.data(), b->elems.data(), b->eep.data(), b->nh);
 		return XFEM_OK;
 	}
 	if (b->el == kElHexes || b->el == kElMixed) {
@@ -2506,11 +2595,12 @@ int xfem_get_hex_rest_state(const xfem_body* h, uint32_t body, float* out_ep120,
 }
 
 static int elem_schedule_out(const BodyHost& b, uint32_t* vert_rank, uint32_t* order, uint32_t* colour_begin,
-                             uint32_t* ncolours) {
+                             uint32_t* ncolours, bool tsched = false) {
+	const ElemSchedule& es = tsched ? b.tsched : b.esched;
 	if (vert_rank) memcpy(vert_rank, b.sched.vert_rank.data(), b.sched.vert_rank.size() * 4);
-	if (order) memcpy(order, b.esched.order.data(), b.esched.order.size() * 4);
-	if (colour_begin) memcpy(colour_begin, b.esched.colour_begin.data(), b.esched.colour_begin.size() * 4);
-	if (ncolours) *ncolours = b.esched.ncolours;
+	if (order) memcpy(order, es.order.data(), es.order.size() * 4);
+	if (colour_begin) memcpy(colour_begin, es.colour_begin.data(), es.colour_begin.size() * 4);
+	if (ncolours) *ncolours = es.ncolours;
 	return XFEM_OK;
 }
 
@@ -2601,8 +2691,8 @@ int xfem_compute_hex_schedule(const float* node_data, uint32_t node_data_count, 
 int xfem_body_t10_count(const xfem_body* h, uint32_t body, uint32_t* nt10, uint32_t* nedges) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
-	if (nt10) *nt10 = b.nh;
+	if (b.el != kElT10 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	if (nt10) *nt10 = b.el == kElQMixed ? b.nqt : b.nh;
 	if (nedges) *nedges = (uint32_t)(b.edges.size() / 2);
 	return XFEM_OK;
 }
@@ -2611,10 +2701,12 @@ int xfem_get_t10_rest_state(const xfem_body* h, uint32_t body, float* out_ep56, 
                             uint32_t* out_edges) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
-	if (out_ep56) memcpy(out_ep56, b.eep.data(), b.eep.size() * sizeof(float));
+	if (b.el != kElT10 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	const std::vector<float>& ep = b.el == kElQMixed ? b.qtep : b.eep;
+	const std::vector<uint32_t>& t10 = b.el == kElQMixed ? b.qt : b.elems;
+	if (out_ep56) memcpy(out_ep56, ep.data(), ep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
-	if (out_t10) memcpy(out_t10, b.elems.data(), b.elems.size() * 4);
+	if (out_t10) memcpy(out_t10, t10.data(), t10.size() * 4);
 	if (out_edges) memcpy(out_edges, b.edges.data(), b.edges.size() * 4);
 	return XFEM_OK;
 }
@@ -2623,8 +2715,8 @@ int xfem_get_t10_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank
                           uint32_t* colour_begin, uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElT10) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
-	return elem_schedule_out(b, vert_rank, t10_order, colour_begin, ncolours);
+	if (b.el != kElT10 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not a T10 body");
+	return elem_schedule_out(b, vert_rank, t10_order, colour_begin, ncolours, b.el == kElQMixed);
 }
 
 int xfem_compute_t10_edges(const uint32_t* idx_data, uint32_t idx_data_count, uint32_t* out_edges, uint32_t* out_t10,
@@ -2667,7 +2759,7 @@ int xfem_compute_t10_rest_state(const float* node_data, uint32_t node_data_count
 int xfem_body_h27_count(const xfem_body* h, uint32_t body, uint32_t* nh27, uint32_t* nedges, uint32_t* nquads) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	if (b.el != kElH27 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
 	if (nh27) *nh27 = b.nh;
 	if (nedges) *nedges = (uint32_t)(b.edges.size() / 2);
 	if (nquads) *nquads = (uint32_t)(b.quads.size() / 4);
@@ -2677,7 +2769,7 @@ int xfem_body_h27_count(const xfem_body* h, uint32_t body, uint32_t* nh27, uint3
 int xfem_get_h27_rest_state(const xfem_body* h, uint32_t body, float* out_ep703, float* out_w, uint32_t* out_h27) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	if (b.el != kElH27 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
 	if (out_ep703) memcpy(out_ep703, b.eep.data(), b.eep.size() * sizeof(float));
 	if (out_w) memcpy(out_w, b.w0.data(), b.w0.size() * sizeof(float));
 	if (out_h27) memcpy(out_h27, b.elems.data(), b.elems.size() * 4);
@@ -2688,7 +2780,7 @@ int xfem_get_h27_schedule(const xfem_body* h, uint32_t body, uint32_t* vert_rank
                           uint32_t* colour_begin, uint32_t* ncolours) {
 	if (!h || body >= h->bodies.size()) return fail(XFEM_EINVAL, "bad handle or body index");
 	const BodyHost& b = h->bodies[body];
-	if (b.el != kElH27) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
+	if (b.el != kElH27 && b.el != kElQMixed) return fail(XFEM_EUNSUPPORTED, "not an H27 body");
 	return elem_schedule_out(b, vert_rank, h27_order, colour_begin, ncolours);
 }
 

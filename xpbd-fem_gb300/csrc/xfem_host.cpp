@@ -570,6 +570,50 @@ void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const ui
 	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
 }
 
+// GeoQuadratic3d's 27 indices of hex h with corners c (XPBDFEM/Geo.cpp:
+// 904-931): node i + 3j + 9k of its 3x3x3 grid is a corner, nverts + an
+// edge (EdgeFromVerts), nverts + ne + a quad (QuadFromVerts, either winding)
+// or nverts + ne + nq + h; efirst / qfirst: each vertex's first edge / quad.
+static void h27_node_ids(const uint32_t* c, uint32_t h, uint32_t nverts, const std::vector<uint32_t>& edges,
+                         const std::vector<uint32_t>& efirst, const std::vector<uint32_t>& quads,
+                         const std::vector<uint32_t>& qfirst, uint32_t ne, uint32_t nq, uint32_t* out) {
+	for (int n = 0; n < 27; n++) {
+		const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
+		int mid = 0, lo = 0, free = 0;
+		for (int a = 0; a < 3; a++) {
+			mid += ix[a] == 1;
+			lo |= (ix[a] == 2) << a;
+			free |= (ix[a] == 1) << a;
+		}
+		uint32_t id;
+		if (mid == 0) {
+			id = c[lo];
+		} else if (mid == 1) {
+			const uint32_t a = c[lo], b = c[lo | free];
+			const uint32_t l = std::min(a, b), u = std::max(a, b);
+			uint32_t e = 0;
+			while (edges[2 * (size_t)(efirst[l] + e) + 1] != u) e++;
+			id = nverts + efirst[l] + e;
+		} else if (mid == 2) {
+			const int f1 = free & 1 ? 1 : 2, f2 = free & 4 ? 4 : 2;
+			const uint32_t vs[4] = {c[lo], c[lo | f1], c[lo | f1 | f2], c[lo | f2]};
+			uint32_t best = 0;
+			for (uint32_t j = 1; j < 4; j++)
+				if (vs[j] < vs[best]) best = j;
+			const uint32_t v0 = vs[best], v1 = vs[(best + 1) % 4], v2 = vs[(best + 2) % 4], v3 = vs[(best + 3) % 4];
+			uint32_t q = 0;
+			for (;; q++) {
+				const uint32_t* Q = &quads[4 * (size_t)(qfirst[v0] + q)];
+				if ((Q[1] == v1 && Q[2] == v2 && Q[3] == v3) || (Q[1] == v3 && Q[2] == v2 && Q[3] == v1)) break;
+			}
+			id = nverts + ne + qfirst[v0] + q;
+		} else {
+			id = nverts + ne + nq + h;
+		}
+		out[n] = id;
+	}
+}
+
 void hex_edges_quads(const uint32_t* hexes, uint32_t nhexes, uint32_t nverts, std::vector<uint32_t>& edges,
                      std::vector<uint32_t>& quads, std::vector<uint32_t>& h27) {
 	static const int he[12][2] = {{0, 1}, {0, 2}, {0, 4}, {1, 3}, {1, 5}, {2, 3}, {2, 6}, {3, 7}, {4, 5}, {4, 6}, {5, 7}, {6, 7}};
@@ -643,44 +687,154 @@ void hex_edges_quads(const uint32_t* hexes, uint32_t nhexes, uint32_t nverts, st
 	}
 	const uint32_t ne = (uint32_t)(edges.size() / 2), nq = (uint32_t)(quads.size() / 4);
 	h27.resize(27 * (size_t)nhexes);
-	for (uint32_t h = 0; h < nhexes; h++) {
-		const uint32_t* c = hexes + 8 * (size_t)h;
-		for (int n = 0; n < 27; n++) {
-			const int ix[3] = {n % 3, (n / 3) % 3, n / 9};
-			int mid = 0, lo = 0, free = 0;
-			for (int a = 0; a < 3; a++) {
-				mid += ix[a] == 1;
-				lo |= (ix[a] == 2) << a;
-				free |= (ix[a] == 1) << a;
+	for (uint32_t h = 0; h < nhexes; h++)
+		h27_node_ids(hexes + 8 * (size_t)h, h, nverts, edges, efirst, quads, qfirst, ne, nq, &h27[27 * (size_t)h]);
+}
+
+void quad_mesh(const uint32_t* idx, uint32_t count, uint32_t nverts, std::vector<uint32_t>& edges,
+               std::vector<uint32_t>& quads, std::vector<uint32_t>& t10, std::vector<uint32_t>& h27) {
+	static const int te[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+	static const int he[12][2] = {{0, 1}, {0, 2}, {0, 4}, {1, 3}, {1, 5}, {2, 3}, {2, 6}, {3, 7}, {4, 5}, {4, 6}, {5, 7}, {6, 7}};
+	static const int hq[6][4] = {{0, 1, 3, 2}, {4, 5, 7, 6}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 2, 6, 4}, {1, 3, 7, 5}};
+	// instances in stream order, each element filing its edges (and a hex
+	// its faces) as it comes; two walks: count per vertex, then file
+	std::vector<uint32_t> eoff(nverts + 1, 0), qoff(nverts + 1, 0), ecnt(nverts, 0), qcnt(nverts, 0);
+	std::vector<uint32_t> eup, einst, qv, qinst;
+	uint32_t ntets = 0, nhexes = 0;
+	for (int pass = 0; pass < 2; pass++) {
+		uint32_t eid = 0, qid = 0;
+		for (uint32_t i = 0; i < count; i += 1 + idx[i]) {
+			const uint32_t* c = idx + i + 1;
+			const bool tet = idx[i] == 4u;
+			if (pass == 0) (tet ? ntets : nhexes)++;
+			for (int k = 0; k < (tet ? 6 : 12); k++, eid++) {
+				const uint32_t a = c[tet ? te[k][0] : he[k][0]], b = c[tet ? te[k][1] : he[k][1]];
+				const uint32_t lo = std::min(a, b);
+				if (pass == 0) {
+					eoff[lo + 1]++;
+				} else {
+					eup[eid] = std::max(a, b);
+					einst[eoff[lo] + ecnt[lo]++] = eid;
+				}
 			}
-			uint32_t id;
-			if (mid == 0) {
-				id = c[lo];
-			} else if (mid == 1) {
-				const uint32_t a = c[lo], b = c[lo | free];
-				const uint32_t l = std::min(a, b), u = std::max(a, b);
-				uint32_t e = 0;
-				while (edges[2 * (size_t)(efirst[l] + e) + 1] != u) e++;
-				id = nverts + efirst[l] + e;
-			} else if (mid == 2) {
-				const int f1 = free & 1 ? 1 : 2, f2 = free & 4 ? 4 : 2;
-				const uint32_t vs[4] = {c[lo], c[lo | f1], c[lo | f1 | f2], c[lo | f2]};
-				uint32_t best = 0;
+			if (tet) continue;
+			for (int f = 0; f < 6; f++, qid++) {
+				uint32_t vs[4], best = 0;
+				for (int j = 0; j < 4; j++) vs[j] = c[hq[f][j]];
 				for (uint32_t j = 1; j < 4; j++)
 					if (vs[j] < vs[best]) best = j;
-				const uint32_t v0 = vs[best], v1 = vs[(best + 1) % 4], v2 = vs[(best + 2) % 4], v3 = vs[(best + 3) % 4];
-				uint32_t q = 0;
-				for (;; q++) {
-					const uint32_t* Q = &quads[4 * (size_t)(qfirst[v0] + q)];
-					if ((Q[1] == v1 && Q[2] == v2 && Q[3] == v3) || (Q[1] == v3 && Q[2] == v2 && Q[3] == v1)) break;
+				if (pass == 0) {
+					qoff[vs[best] + 1]++;
+				} else {
+					for (uint32_t j = 0; j < 4; j++) qv[4 * (size_t)qid + j] = vs[(best + j) % 4];
+					qinst[qoff[vs[best]] + qcnt[vs[best]]++] = qid;
 				}
-				id = nverts + ne + qfirst[v0] + q;
-			} else {
-				id = nverts + ne + nq + h;
 			}
-			h27[27 * (size_t)h + n] = id;
+		}
+		if (pass == 0) {
+			for (uint32_t v = 0; v < nverts; v++) {
+				eoff[v + 1] += eoff[v];
+				qoff[v + 1] += qoff[v];
+			}
+			eup.resize(eoff[nverts]);
+			einst.resize(eoff[nverts]);
+			qv.resize(4 * (size_t)qoff[nverts]);
+			qinst.resize(qoff[nverts]);
 		}
 	}
+	for (uint32_t v = 0; v < nverts; v++) {
+		uint32_t* L = einst.data() + eoff[v];
+		for (uint32_t j = 0; j < ecnt[v]; j++)
+			for (uint32_t k = j + 1; k < ecnt[v]; k++)
+				if (eup[L[j]] == eup[L[k]]) L[k--] = L[--ecnt[v]];
+		uint32_t* Q = qinst.data() + qoff[v];
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (uint32_t k = j + 1; k < qcnt[v]; k++) {
+				const uint32_t* a = &qv[4 * (size_t)Q[j]];
+				const uint32_t* b = &qv[4 * (size_t)Q[k]];
+				if ((a[1] == b[1] && a[2] == b[2] && a[3] == b[3]) || (a[1] == b[3] && a[2] == b[2] && a[3] == b[1]))
+					Q[k--] = Q[--qcnt[v]];
+			}
+	}
+	std::vector<uint32_t> efirst(nverts), qfirst(nverts);
+	edges.clear();
+	quads.clear();
+	for (uint32_t v = 0; v < nverts; v++) {
+		efirst[v] = (uint32_t)(edges.size() / 2);
+		for (uint32_t j = 0; j < ecnt[v]; j++) {
+			edges.push_back(v);
+			edges.push_back(eup[einst[eoff[v] + j]]);
+		}
+		qfirst[v] = (uint32_t)(quads.size() / 4);
+		for (uint32_t j = 0; j < qcnt[v]; j++)
+			for (int k = 0; k < 4; k++) quads.push_back(qv[4 * (size_t)qinst[qoff[v] + j] + k]);
+	}
+	const uint32_t ne = (uint32_t)(edges.size() / 2), nq = (uint32_t)(quads.size() / 4);
+	t10.resize(10 * (size_t)ntets);
+	h27.resize(27 * (size_t)nhexes);
+	uint32_t t = 0, h = 0;
+	for (uint32_t i = 0; i < count; i += 1 + idx[i]) {
+		const uint32_t* c = idx + i + 1;
+		if (idx[i] != 4u) {
+			h27_node_ids(c, h, nverts, edges, efirst, quads, qfirst, ne, nq, &h27[27 * (size_t)h]);
+			h++;
+			continue;
+		}
+		uint32_t* o = &t10[10 * (size_t)t++];
+		for (int k = 0; k < 4; k++) o[k] = c[k];
+		for (int k = 0; k < 6; k++) {
+			const uint32_t a = c[te[k][0]], b = c[te[k][1]];
+			const uint32_t l = std::min(a, b), u = std::max(a, b);
+			uint32_t e = 0;
+			while (edges[2 * (size_t)(efirst[l] + e) + 1] != u) e++;
+			o[4 + k] = nverts + efirst[l] + e;
+		}
+	}
+}
+
+void qmixed_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const uint32_t* hexes, uint32_t nhexes,
+                      const uint32_t* edges, uint32_t nedges, const uint32_t* quads, uint32_t nquads, const uint32_t* t10,
+                      const uint32_t* h27, float density, double* X, float* qep, float* hep, float* w, uint8_t* vflags) {
+	const uint32_t n = nverts + nedges + nquads + nhexes;
+	for (size_t i = 0; i < 3 * (size_t)nverts; i++) X[i] = (double)nodes[i];
+	for (uint32_t e = 0; e < nedges; e++)
+		for (int k = 0; k < 3; k++)
+			X[3 * (size_t)(nverts + e) + k] = 0.5 * (X[3 * (size_t)edges[2 * e] + k] + X[3 * (size_t)edges[2 * e + 1] + k]);
+	for (uint32_t q = 0; q < nquads; q++) {
+		const uint32_t* v = quads + 4 * (size_t)q;
+		for (int k = 0; k < 3; k++)
+			X[3 * (size_t)(nverts + nedges + q) + k] =
+			    0.25 * (X[3 * (size_t)v[0] + k] + X[3 * (size_t)v[1] + k] + X[3 * (size_t)v[2] + k] + X[3 * (size_t)v[3] + k]);
+	}
+	for (uint32_t h = 0; h < nhexes; h++)
+		for (int k = 0; k < 3; k++) {
+			double s = X[3 * (size_t)hexes[8 * (size_t)h] + k];
+			for (int c = 1; c < 8; c++) s = s + X[3 * (size_t)hexes[8 * (size_t)h + c] + k];
+			X[3 * (size_t)(nverts + nedges + nquads + h) + k] = 0.125 * s;
+		}
+	float mn[3] = {1.0e24f, 1.0e24f, 1.0e24f}, mx[3] = {-1.0e24f, -1.0e24f, -1.0e24f};
+	for (uint32_t i = 0; i < n; i++) {
+		w[i] = 0.0f;
+		for (int k = 0; k < 3; k++) {
+			mn[k] = fminf(mn[k], (float)X[3 * (size_t)i + k]);
+			mx[k] = fmaxf(mx[k], (float)X[3 * (size_t)i + k]);
+		}
+	}
+	for (uint32_t i = 0; i < n; i++) vflags[i] = rest::vertex_flags((float)X[3 * (size_t)i], mn[0], mx[0]);
+	// the masses of every T10, then of every H27, in element order
+	for (uint32_t t = 0; t < ntets; t++) {
+		const uint32_t* is = t10 + 10 * (size_t)t;
+		float m[10];
+		rest::t10(X, is, density, qep + (size_t)rest::kT10Rec * t, m);
+		for (int c = 0; c < 10; c++) w[is[c]] += m[c];
+	}
+	(void)rest::h27_tables();
+	for (uint32_t h = 0; h < nhexes; h++) {
+		float m[27];
+		rest::h27(X, h27 + 27 * (size_t)h, density, hep + (size_t)rest::kH27Rec * h, m);
+		for (int c = 0; c < 27; c++) w[h27[27 * (size_t)h + c]] += m[c];
+	}
+	for (uint32_t i = 0; i < n; i++) w[i] = 1.0f / w[i];
 }
 
 void h27_init_rest(const float* nodes, uint32_t nverts, const uint32_t* hexes, uint32_t nhexes, const uint32_t* edges,

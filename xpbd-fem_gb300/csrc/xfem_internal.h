@@ -153,6 +153,22 @@ void t10_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const ui
 // nquads + the hex.
 void hex_edges_quads(const uint32_t* hexes, uint32_t nhexes, uint32_t nverts, std::vector<uint32_t>& edges,
                      std::vector<uint32_t>& quads, std::vector<uint32_t>& h27);
+// Connectivity3d's edges and quads of a tagged stream that may mix tets and
+// hexes (XPBDFEM/Connectivity.cpp:371-530): each element files its edges (a
+// tet's 6, a hex's 12) and a hex its faces in stream order, under the same
+// rules as tet_edges and hex_edges_quads, to which it reduces on a stream of
+// one kind; t10 gets 10 indices per tet (tet order), h27 27 per hex (hex
+// order) as those functions give them.
+void quad_mesh(const uint32_t* idx, uint32_t count, uint32_t nverts, std::vector<uint32_t>& edges,
+               std::vector<uint32_t>& quads, std::vector<uint32_t>& t10, std::vector<uint32_t>& h27);
+// GeoQuadratic3d::Init's rest state on a mesh mixing tets and hexes
+// (XPBDFEM/Geo.cpp:836-941): X over every vertex (corners, edge midpoints,
+// quad centres, hex centres), flags, the T10 records (56 floats each) and
+// the H27 records (703 floats each), the masses of all T10s then all H27s in
+// one sum, inverted once; bit for bit.
+void qmixed_init_rest(const float* nodes, uint32_t nverts, uint32_t ntets, const uint32_t* hexes, uint32_t nhexes,
+                      const uint32_t* edges, uint32_t nedges, const uint32_t* quads, uint32_t nquads, const uint32_t* t10,
+                      const uint32_t* h27, float density, double* X, float* qep, float* hep, float* w, uint8_t* vflags);
 // GeoQuadratic3d::Init's rest state on a hex mesh (XPBDFEM/Geo.cpp:836-933):
 // X (3 doubles per vertex: corners, edge midpoints, face centres, hex
 // centres), flags over all of them, 703 floats per H27 (rest::kH27* offsets)
@@ -512,6 +528,9 @@ int launch_t10(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stre
 // persistent launch (canonical (X, V) in and out).
 int launch_t10_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
 int launch_h27_rings(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
+// A mesh mixing T10s and H27s: ch27 with the H27 element arrays, ct10 the
+// same context with the T10 element arrays (blocks of 256 threads).
+int launch_qmixed(const DevCtx& ch27, const DevCtx& ct10, int block, uint32_t nsub, float dt, void* stream);
 // Quadratic-hex mode (xfem_h27.cu): nsub substeps of an H27 mesh, one warp
 // per element (block must be 256).
 int launch_h27(const DevCtx& ctx, int block, uint32_t nsub, float dt, void* stream);
