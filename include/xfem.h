@@ -217,10 +217,12 @@ int xfem_settings_default(xfem_settings* s);
  * hex mesh an H27 body (GeoQuadratic3d::Init, XPBDFEM/Geo.cpp:836-941). A
  * mesh mixing tets and hexes is one body holding both (GeoLinear3d on one
  * tagged stream, XPBDFEM/Geo.cpp:697-811): each sweep solves every tet, then
- * every hex, each kind in a colouring of its own. Such a mesh with the
- * continuous-pressure models (energy 8-10) or with quadratic elements is
- * refused (XFEM_EUNSUPPORTED), and so is a T10 or H27 body whose one-rings
- * exceed 64 T10s (16 H27s) or 128 nodes (XFEM_ELIMIT). */
+ * every hex, each kind in a colouring of its own; with element type T10 or
+ * H27 it is GeoQuadratic3d on that stream: T10s and H27s in one body, every
+ * sweep solving every T10, then every H27. Such a mesh with the
+ * continuous-pressure models (energy 8-10) is refused (XFEM_EUNSUPPORTED),
+ * and so is a T10 or H27 body whose one-rings exceed 64 T10s (16 H27s) or
+ * 128 nodes (XFEM_ELIMIT). */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
@@ -438,7 +440,10 @@ int xfem_compute_mixed_schedule(const float* node_data, uint32_t node_data_count
                                 uint32_t* hex_colour_begin, uint32_t* hex_ncolours);
 
 /* ---- quadratic tets (T10 mode) ----------------------------------------------- */
-/* T10s and edge nodes of one body; XFEM_EUNSUPPORTED for another body. */
+/* T10s and edge nodes of one body; XFEM_EUNSUPPORTED for another body. The
+ * xfem_*_t10_* queries also answer for the T10s of a mesh mixing tets and
+ * hexes read as quadratic elements (their records, indices and colouring),
+ * and the xfem_*_h27_* queries for its H27s; edge counts are the mesh's. */
 int xfem_body_t10_count(const xfem_body* b, uint32_t body, uint32_t* nt10, uint32_t* nedges);
 /* Rest state per T10 (caller tet order) as 56 floats, ElementParamsQuadraticTet
  * (XPBDFEM/Fem.h:61-69) flattened: Qi column-major [0..8], ic.QQ[9] [9..17],
