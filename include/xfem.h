@@ -222,7 +222,9 @@ int xfem_settings_default(xfem_settings* s);
  * sweep solving every T10, then every H27. Such a mesh with the
  * continuous-pressure models (energy 8-10) is refused (XFEM_EUNSUPPORTED),
  * and so is a T10 or H27 body whose one-rings exceed 64 T10s (16 H27s) or
- * 128 nodes (XFEM_ELIMIT). */
+ * 128 nodes (XFEM_ELIMIT). A mesh without elements returns XFEM_EINVAL (the
+ * reference's empty Geo3d steps nothing), as do unknown tags, a truncated
+ * stream and a vertex count that the stream does not imply. */
 int xfem_create(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,
                 uint32_t idx_data_count, float density, const xfem_settings* settings, xfem_body** out);
 int xfem_create_ex(const float* node_data, uint32_t node_data_count, const uint32_t* idx_data,

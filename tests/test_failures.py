@@ -34,10 +34,19 @@ def _block():
 
 
 # ---- bad input: refused with or without a GPU -----------------------------------
-@pytest.mark.parametrize("case", ["tag", "truncated", "count", "density", "mixed"])
+@pytest.mark.parametrize("case", ["tag", "truncated", "count", "density", "mixed", "empty", "empty_body"])
 def test_bad_mesh_is_refused_before_the_device(case):
     nodes, idx, s = _block()
     code = xfem.EINVAL
+    if case == "empty":
+        nodes, idx = np.zeros(0, np.float32), np.zeros(0, np.uint32)
+    elif case == "empty_body":
+        # one body of a batch without elements: named
+        with pytest.raises(xfem.XfemError) as e:
+            xfem.Body(meshes=[(nodes, idx, 1000.0), (np.zeros(0, np.float32), np.zeros(0, np.uint32), 1000.0)],
+                      settings=[s, s])
+        assert e.value.code == code and "body 1" in str(e.value)
+        return
     if case == "tag":
         idx = idx.copy()
         idx[5] = 6  # the second record's tag

@@ -464,6 +464,9 @@ int precheck_inputs(uint32_t nb, const xfem_mesh* meshes, const xfem_settings* s
 		const std::string who = nb > 1 ? "body " + std::to_string(k) + ": " : std::string();
 		if (!m.node_data || !m.idx_data) return fail(XFEM_EINVAL, who + "null mesh array");
 		if (m.node_data_count % 3) return fail(XFEM_EINVAL, who + "node_data_count must be a multiple of 3");
+		// the reference's empty Geo steps nothing; a handle with nothing to
+		// step is refused instead of launching empty grids
+		if (m.idx_data_count == 0) return fail(XFEM_EINVAL, who + "the mesh has no elements");
 		uint64_t nv = 0;
 		uint32_t ntag[2] = {0, 0};
 		for (uint32_t i = 0; i < m.idx_data_count;) {
