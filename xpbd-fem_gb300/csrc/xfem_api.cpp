@@ -138,6 +138,7 @@ struct xfem_body {
 	DevBuf<BodyParams> params;
 	DevBuf<float2> tlam;
 	DevBuf<int> err;
+	int* err_host = nullptr;  // pinned: the error word's read-back at every synchronising call
 	DevBuf<float> stage;
 	DevBuf<double> vol;
 	// per tet, caller order (all bodies): record index of c0, volume, output
@@ -191,6 +192,7 @@ struct xfem_body {
 	uint64_t device_bytes = 0;
 
 	~xfem_body() {
+		if (err_host) cudaFreeHost(err_host);
 		if (graph) cudaGraphExecDestroy(graph);
 		if (own_stream && stream) cudaStreamDestroy(stream);
 	}
@@ -408,8 +410,14 @@ int device_error(int e) {
 
 int check_device_error(xfem_body* h) {
 	int e = 0;
-	XCUDA(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-	XCUDA(cudaStreamSynchronize(h->stream));
+	if (h->err_host) {  // pinned: an asynchronous copy, no staging
+		XCUDA(cudaMemcpyAsync(h->err_host, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+		XCUDA(cudaStreamSynchronize(h->stream));
+		e = *h->err_host;
+	} else {
+		XCUDA(cudaMemcpyAsync(&e, h->err.p, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+		XCUDA(cudaStreamSynchronize(h->stream));
+	}
 	if (e != 0) {
 		XCUDA(cudaMemsetAsync(h->err.p, 0, sizeof(int), h->stream));
 		XCUDA(cudaStreamSynchronize(h->stream));
@@ -1569,6 +1577,8 @@ int build_device(xfem_body* h) {
 	XCUDA(h->params.alloc(params.size()));
 	XCUDA(h->bar.alloc(1));
 	XCUDA(h->err.alloc(1));
+	if (!h->err_host) XCUDA(cudaHostAlloc((void**)&h->err_host, sizeof(int), cudaHostAllocDefault));
+	*h->err_host = 0;
 	uint32_t maxnv = 1;
 	for (auto& b : h->bodies) maxnv = std::max(maxnv, b.nv);
 	XCUDA(h->stage.alloc(3 * (size_t)maxnv));
