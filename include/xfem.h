@@ -334,6 +334,9 @@ int xfem_adjoint_backward(xfem_body* b, const float* grad_tip_traj, const float*
                           float* dmu, float* dx0, float* dv0);
 
 /* ---- state transfer (caller vertex order; synchronising) ------------------ */
+/* Positions and velocities: 3 floats per vertex. A page-locked buffer
+ * (xfem_alloc_host) is read or written by the device directly, with no
+ * staging copy; any other buffer goes through the handle's device stage. */
 int xfem_get_positions(xfem_body* b, uint32_t body, float* out_xyz);
 int xfem_set_positions(xfem_body* b, uint32_t body, const float* xyz);
 int xfem_get_velocities(xfem_body* b, uint32_t body, float* out_xyz);

@@ -2009,11 +2009,31 @@ int step(xfem_body* h, uint32_t nsub, float dt) {
 }
 
 // which: 0 positions, 1 velocities
+// A page-locked host buffer that the device addresses directly (memory from
+// xfem_alloc_host / cudaMallocHost): its device address, else null.
+static void* mapped_host(const void* p) {
+	cudaPointerAttributes a{};
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		(void)cudaGetLastError();
+		return nullptr;
+	}
+	return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int get_xyz(xfem_body* h, uint32_t body, int which, float* out) {
 	BodyHost* b = body_of(h, body);
 	if (!b) return XFEM_EINVAL;
 	if (!out) return fail(XFEM_EINVAL, "null output");
 	XCUDA(cudaSetDevice(h->device));
+	if (which <= 1) {
+		// positions or velocities into page-locked memory: the gather writes
+		// them there itself (no staging copy)
+		if (float* direct = static_cast<float*>(mapped_host(out))) {
+			const int e = launch_gather_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, direct, h->stream);
+			if (e) return fail(XFEM_ECUDA, "gather launch failed");
+			return check_device_error(h);
+		}
+	}
 	const int e = launch_gather_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, h->stage.p, h->stream);
 	if (e) return fail(XFEM_ECUDA, "gather launch failed");
 	const size_t n = which >= 2 ? b->nv : 3 * (size_t)b->nv;
@@ -2026,8 +2046,13 @@ int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
 	if (!b) return XFEM_EINVAL;
 	if (!in) return fail(XFEM_EINVAL, "null input");
 	XCUDA(cudaSetDevice(h->device));
-	XCUDA(cudaMemcpyAsync(h->stage.p, in, 3 * (size_t)b->nv * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-	const int e = launch_scatter_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, h->stage.p, h->stream);
+	// page-locked input: the scatter reads it itself (no staging copy)
+	const float* src = static_cast<const float*>(mapped_host(in));
+	if (!src) {
+		XCUDA(cudaMemcpyAsync(h->stage.p, in, 3 * (size_t)b->nv * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+		src = h->stage.p;
+	}
+	const int e = launch_scatter_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, src, h->stream);
 	if (e) return fail(XFEM_ECUDA, "scatter launch failed");
 	return check_device_error(h);
 }
