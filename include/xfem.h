@@ -270,12 +270,13 @@ int xfem_step_frames(xfem_body* b, uint32_t frames, uint32_t substeps, float dt)
  * error word) lives in one fixed 256-byte device array that every GPU loading
  * the library keeps until exit; all calls share it, so calls whose kernels
  * overlap on one GPU race and must not be issued. The first call on a device
- * looks the array's device address up; make that first call before any
- * stream capture. Limit: one call's grid-barrier arrivals, substeps x passes
- * per substep (colours, times 1 + volume sweeps + damping kinds when those
- * run) x persistent blocks, must stay below 2^31 (else XFEM_ELIMIT; split
- * the call). Hex, T10 and H27 handles step with their own scratch, allocated
- * at create time. Synchronises the handle's stream and reports device errors. */
+ * looks the array's device address up. Limit: one call's grid-barrier
+ * arrivals, substeps x passes per substep (colours, times 1 + volume sweeps +
+ * damping kinds when those run) x persistent blocks, must stay below 2^31
+ * (else XFEM_ELIMIT; split the call). Hex, T10, H27 and mixed-mesh handles
+ * step with their own scratch, allocated at create time. Synchronises the
+ * handle's stream and reports device errors, so it is not a call to record
+ * into a CUDA graph (no stream of the process may be capturing then). */
 int xfem_step_frames_noalloc(xfem_body* b, uint32_t frames, uint32_t substeps, float dt);
 /* Waits for queued work; returns XFEM_EDEVICE_TIMEOUT if a bounded device
  * wait ran out since the last check, XFEM_ENONFINITE if a finished position
