@@ -26,6 +26,15 @@ __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
 	return v;
 }
 
+// A relaxed load for polls; one fence.acquire.gpu after the last poll orders
+// what follows (an acquire load per poll cost 0.9% of the persistent frame
+// and 1.7% of the brick frame).
+__device__ __forceinline__ uint32_t ld_relaxed_gpu(const uint32_t* p) {
+	uint32_t v;
+	asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
 __device__ __forceinline__ uint64_t global_ns() {
 	uint64_t t;
 	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -51,7 +60,7 @@ __device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
 		atomicAdd(C.bar_count, 1u);
 		uint32_t spins = 0;
 		uint64_t t0 = 0;
-		while ((int32_t)(ld_acquire_gpu(C.bar_count) - target) < 0) {
+		while ((int32_t)(ld_relaxed_gpu(C.bar_count) - target) < 0) {
 			if (++spins == 256) {
 				spins = 0;
 				if (*(volatile int*)C.err) {
@@ -68,6 +77,7 @@ __device__ bool grid_sync(const DevCtx& C, uint32_t& target) {
 				}
 			}
 		}
+		asm volatile("fence.acquire.gpu;" ::: "memory");  // the acquire pattern: relaxed polls, one fence
 		s_ok = ok;
 	}
 	__syncthreads();

@@ -773,7 +773,10 @@ __device__ __forceinline__ void run_chunk_brick(const DevCtx& C, Stage& st, int 
 // Bounded wait, by the calling threads (`first` of them striding by
 // `stride`), until every brick of list[nb0, nb1) has published at least
 // `target` passes. Returns false when a wait ran out or another
-// block reported an error.
+// block reported an error. The polls are relaxed loads and one acquire
+// fence follows them (the acquire pattern of the PTX memory model): an
+// acquire load on every poll, or an acquire-release fence, made the
+// throughput frame 1.7% and 11% slower.
 __device__ bool brick_wait(const DevCtx& C, const uint32_t* list, uint32_t nb0, uint32_t nb1, uint32_t target,
                            uint32_t first, uint32_t stride) {
 	target += C.wait_miss;
@@ -782,7 +785,7 @@ __device__ bool brick_wait(const DevCtx& C, const uint32_t* list, uint32_t nb0, 
 		const uint32_t* f = C.bflag + (size_t)__ldg(list + i) * kBrickFlagStride;
 		uint32_t spins = 0;
 		uint64_t t0 = 0;
-		while ((int32_t)(ld_acquire_gpu(f) - target) < 0) {
+		while ((int32_t)(ld_relaxed_gpu(f) - target) < 0) {
 			if (++spins == 256) {
 				spins = 0;
 				if (*(volatile int*)C.err) {
@@ -800,6 +803,7 @@ __device__ bool brick_wait(const DevCtx& C, const uint32_t* list, uint32_t nb0, 
 			}
 		}
 	}
+	asm volatile("fence.acquire.gpu;" ::: "memory");
 	return !bad;
 }
 
