@@ -291,8 +291,7 @@ def run_xfem(args, world, rank, local):
             flush.zero_()
         body.synchronize()
         t0 = time.perf_counter()
-        body.set_positions(px)
-        body.set_velocities(pv)
+        body.set_state(px, pv)
         body.step_frames(1, S, sdt)
         out = body.positions(out=po)
         e2e_t += time.perf_counter() - t0

@@ -342,6 +342,8 @@ int xfem_get_positions(xfem_body* b, uint32_t body, float* out_xyz);
 int xfem_set_positions(xfem_body* b, uint32_t body, const float* xyz);
 int xfem_get_velocities(xfem_body* b, uint32_t body, float* out_xyz);
 int xfem_set_velocities(xfem_body* b, uint32_t body, const float* xyz);
+/* Both at once, as the two calls above with one synchronisation. */
+int xfem_set_state(xfem_body* b, uint32_t body, const float* xyz, const float* vel);
 int xfem_get_inverse_masses(xfem_body* b, uint32_t body, float* out_w);
 /* Ground-contact set of the last substep (1 = in contact). */
 int xfem_get_contacts(xfem_body* b, uint32_t body, uint8_t* out);

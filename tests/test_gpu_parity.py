@@ -258,3 +258,42 @@ def test_throughput_mesh_one_substep_vs_fp64():
     assert abs(b.volume() - v_orc) <= 1e-5 * v_orc
     fixed = w["lock"].astype(bool)
     assert np.array_equal(x[fixed], w["nodes"].reshape(-1, 3)[fixed])
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_state_transfer_forms_agree(pinned):
+    """xfem_set_state equals xfem_set_positions then xfem_set_velocities, and
+    page-locked buffers (read and written by the kernels themselves) equal
+    pageable ones, bit for bit, on a batch's second body."""
+    import ctypes
+    meshes = [xfem.generate_tet_block(4, 3, 2, (0.05, 0.05, 0.05)) + (1000.0,),
+              xfem.generate_tet_block(6, 3, 3, (0.04, 0.05, 0.06), 1, 0.2) + (900.0,)]
+    s = xfem.default_settings(gravity=(0.3, -9.81, -2.0), compliance=1e-3, poissons_ratio=0.45)
+    a = xfem.Body(meshes=meshes, settings=[s, s])
+    b = xfem.Body(meshes=meshes, settings=[s, s])
+    nv = meshes[1][0].size // 3
+    rng = np.random.default_rng(5)
+    x = (meshes[1][0].reshape(-1, 3) + rng.normal(0, 1e-3, (nv, 3))).astype(np.float32)
+    v = rng.normal(0, 0.1, (nv, 3)).astype(np.float32)
+    bufs = []
+    if pinned:
+        for arr in (x, v):
+            p = xfem.lib().xfem_alloc_host(arr.nbytes)
+            buf = np.frombuffer((ctypes.c_float * arr.size).from_address(p), np.float32)
+            buf[:] = arr.reshape(-1)
+            bufs.append((p, buf))
+        xin, vin = bufs[0][1], bufs[1][1]
+    else:
+        xin, vin = x, v
+    a.set_positions(xin, body=1)
+    a.set_velocities(vin, body=1)
+    b.set_state(xin, vin, body=1)
+    for h in (a, b):
+        h.step_frames(1, 5, DT)
+    out = np.zeros(3 * nv, np.float32) if not pinned else bufs[0][1]
+    xa = a.positions(1, out=out).copy()
+    assert np.array_equal(xa, b.positions(1))
+    assert np.array_equal(a.velocities(1), b.velocities(1))
+    assert np.array_equal(a.positions(0), b.positions(0))
+    for p, _ in bufs:
+        xfem.lib().xfem_free_host(p)

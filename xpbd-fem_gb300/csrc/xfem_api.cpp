@@ -2041,11 +2041,9 @@ int get_xyz(xfem_body* h, uint32_t body, int which, float* out) {
 	return check_device_error(h);
 }
 
-int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
-	BodyHost* b = body_of(h, body);
-	if (!b) return XFEM_EINVAL;
-	if (!in) return fail(XFEM_EINVAL, "null input");
-	XCUDA(cudaSetDevice(h->device));
+// Queues the upload of one body's positions (which 0) or velocities (1) on
+// the handle's stream, without waiting for it.
+static int scatter_xyz(xfem_body* h, const BodyHost* b, int which, const float* in) {
 	// page-locked input: the scatter reads it itself (no staging copy)
 	const float* src = static_cast<const float*>(mapped_host(in));
 	if (!src) {
@@ -2054,7 +2052,16 @@ int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
 	}
 	const int e = launch_scatter_xyz(h->vert.p, which, h->dev_of_vert.p + b->vbase, b->nv, src, h->stream);
 	if (e) return fail(XFEM_ECUDA, "scatter launch failed");
-	return check_device_error(h);
+	return XFEM_OK;
+}
+
+int set_xyz(xfem_body* h, uint32_t body, int which, const float* in) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!in) return fail(XFEM_EINVAL, "null input");
+	XCUDA(cudaSetDevice(h->device));
+	const int rc = scatter_xyz(h, b, which, in);
+	return rc ? rc : check_device_error(h);
 }
 
 // Rewrites c0 = (1/mu)/volume in one body's records on the device (and 1/mu
@@ -2343,6 +2350,15 @@ int xfem_get_positions(xfem_body* b, uint32_t body, float* out) { return get_xyz
 int xfem_set_positions(xfem_body* b, uint32_t body, const float* in) { return set_xyz(b, body, 0, in); }
 int xfem_get_velocities(xfem_body* b, uint32_t body, float* out) { return get_xyz(b, body, 1, out); }
 int xfem_set_velocities(xfem_body* b, uint32_t body, const float* in) { return set_xyz(b, body, 1, in); }
+int xfem_set_state(xfem_body* h, uint32_t body, const float* xyz, const float* vel) {
+	BodyHost* b = body_of(h, body);
+	if (!b) return XFEM_EINVAL;
+	if (!xyz || !vel) return fail(XFEM_EINVAL, "null input");
+	XCUDA(cudaSetDevice(h->device));
+	int rc = scatter_xyz(h, b, 0, xyz);
+	if (!rc) rc = scatter_xyz(h, b, 1, vel);
+	return rc ? rc : check_device_error(h);  // one synchronisation for both
+}
 int xfem_get_inverse_masses(xfem_body* b, uint32_t body, float* out) { return get_xyz(b, body, 2, out); }
 
 int xfem_get_contacts(xfem_body* h, uint32_t body, uint8_t* out) {

@@ -93,7 +93,7 @@ EXPORTS = [
     "xfem_settings_default", "xfem_create", "xfem_create_ex", "xfem_batch_create", "xfem_destroy",
     "xfem_get_info", "xfem_set_settings", "xfem_set_lock_mask", "xfem_set_tet_mu", "xfem_substep",
     "xfem_step_frames", "xfem_synchronize", "xfem_get_positions", "xfem_set_positions",
-    "xfem_get_velocities", "xfem_set_velocities", "xfem_get_inverse_masses", "xfem_get_contacts",
+    "xfem_get_velocities", "xfem_set_velocities", "xfem_set_state", "xfem_get_inverse_masses", "xfem_get_contacts",
     "xfem_get_lambdas", "xfem_calculate_volume", "xfem_get_rest_state", "xfem_get_schedule",
     "xfem_body_counts", "xfem_time_corrected_drag", "xfem_generate_tet_block", "xfem_alloc_host",
     "xfem_free_host", "xfem_last_error", "xfem_compute_rest_state", "xfem_compute_schedule",
@@ -146,6 +146,7 @@ def lib():
         for n in ("xfem_get_positions", "xfem_set_positions", "xfem_get_velocities", "xfem_set_velocities",
                   "xfem_get_inverse_masses", "xfem_get_contacts", "xfem_get_lambdas", "xfem_calculate_volume"):
             getattr(L, n).argtypes = [P, u32, P]
+        L.xfem_set_state.argtypes = [P, u32, P, P]
         L.xfem_get_rest_state.argtypes = [P, u32, P, P]
         L.xfem_get_schedule.argtypes = [P, u32, P, P, P, P]
         L.xfem_body_counts.argtypes = [P, u32, P, P]
@@ -556,6 +557,12 @@ class Body:
     def set_velocities(self, v, body=0):
         a = np.ascontiguousarray(v, np.float32).reshape(-1)
         _check(lib().xfem_set_velocities(self._h, body, _p(a)))
+
+    def set_state(self, x, v, body=0):
+        """Positions and velocities with one synchronisation."""
+        a = np.ascontiguousarray(x, np.float32).reshape(-1)
+        c = np.ascontiguousarray(v, np.float32).reshape(-1)
+        _check(lib().xfem_set_state(self._h, body, _p(a), _p(c)))
 
     def lambdas(self, body=0):
         nt = self.counts[body][1]
