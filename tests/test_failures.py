@@ -202,3 +202,48 @@ def test_barrier_counter_wrap_keeps_results(sync_mode):
         b.step_frames(1, 25, DT)
         assert np.array_equal(a.positions(), b.positions())
         assert np.array_equal(a.velocities(), b.velocities())
+
+
+def _mode_mesh(mode):
+    """A small body of each element and one-ring mode: (nodes, idx, settings)."""
+    ring = (xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT
+    if mode in ("t10", "t10_rings", "tet_rings"):
+        nodes, idx = xfem.generate_tet_block(4, 3, 2, (0.05, 0.05, 0.05))
+    elif mode == "qmixed":
+        import oracle
+        nodes, idx = oracle.mixed_block(4, 2, 2, (0.05, 0.05, 0.05), 0, 0.0, lambda x, y, z: (x + y + z) % 2 == 0)
+    else:
+        nodes, idx = xfem.generate_hex_block(4, 3, 2, (0.05, 0.05, 0.05))
+    el = {"t10": xfem.ELEMENT_T10, "t10_rings": xfem.ELEMENT_T10, "h27": xfem.ELEMENT_H27,
+          "h27_rings": xfem.ELEMENT_H27, "qmixed": xfem.ELEMENT_T10}.get(mode, 0)
+    flags = (ring if mode.endswith("rings") else W.NH_FLAGS) | el
+    s = xfem.default_settings(gravity=(0.0, 0.0, -9.81), compliance=1e-3 if mode.endswith("rings") else
+                              W.nh_compliance(1e5, 0.45), poissons_ratio=0.45, flags=flags)
+    return nodes, idx, s
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["tet_rings", "hex_rings", "t10", "t10_rings", "h27", "h27_rings", "qmixed"])
+def test_element_and_ring_waits_time_out_and_recover(mode):
+    """The same bounded-wait check for the element and one-ring kernels
+    (k_rings, k_hex_rings, k_elements on T10s and H27s, k_t10_rings,
+    k_h27_rings, k_qmixed)."""
+    nodes, idx, s = _mode_mesh(mode)
+    ref = xfem.Body(nodes, idx, 1000.0, s)
+    b = xfem.Body(nodes, idx, 1000.0, s, wait_timeout_ms=100)
+    x0 = b.positions()
+    v0 = np.zeros_like(x0)
+    for h in (ref, b):  # the locks take hold in the first substep
+        h.step_frames(1, 1, DT)
+        h.set_positions(x0)
+        h.set_velocities(v0)
+    ref.step_frames(1, 6, DT)
+    xfem.test_hook(b, xfem.HOOK_MISSING_ARRIVAL, 1)
+    b.step_frames(1, 6, DT)
+    with pytest.raises(xfem.XfemError) as e:
+        b.synchronize()
+    assert e.value.code == xfem.EDEVICE_TIMEOUT, str(e.value)
+    b.set_positions(x0)
+    b.set_velocities(v0)
+    b.step_frames(1, 6, DT)
+    assert np.array_equal(b.positions(), ref.positions())
