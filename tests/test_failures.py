@@ -209,7 +209,7 @@ def _mode_mesh(mode):
     ring = (xfem.ENERGY_CONTINUOUS_MIXED << xfem.ENERGY_BIT) | (1 << xfem.XPBD_SOLVE_BIT) | xfem.LOCK_LEFT
     if mode in ("t10", "t10_rings", "tet_rings"):
         nodes, idx = xfem.generate_tet_block(4, 3, 2, (0.05, 0.05, 0.05))
-    elif mode == "qmixed":
+    elif mode in ("qmixed", "mixed"):
         import oracle
         nodes, idx = oracle.mixed_block(4, 2, 2, (0.05, 0.05, 0.05), 0, 0.0, lambda x, y, z: (x + y + z) % 2 == 0)
     else:
@@ -223,11 +223,11 @@ def _mode_mesh(mode):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["tet_rings", "hex_rings", "t10", "t10_rings", "h27", "h27_rings", "qmixed"])
+@pytest.mark.parametrize("mode", ["tet_rings", "hex_rings", "t10", "t10_rings", "h27", "h27_rings", "mixed", "qmixed"])
 def test_element_and_ring_waits_time_out_and_recover(mode):
     """The same bounded-wait check for the element and one-ring kernels
     (k_rings, k_hex_rings, k_elements on T10s and H27s, k_t10_rings,
-    k_h27_rings, k_qmixed)."""
+    k_h27_rings, k_mixed, k_qmixed)."""
     nodes, idx, s = _mode_mesh(mode)
     ref = xfem.Body(nodes, idx, 1000.0, s)
     b = xfem.Body(nodes, idx, 1000.0, s, wait_timeout_ms=100)
